@@ -1,0 +1,593 @@
+/* CPU oracle for the BrainGrid per-step spiking hot path — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference single-threaded simulator, used as the checker for the
+ * CUDA path.  Each function cites the reference file:line it follows (paths relative to the
+ * reference project root).  Pinned bit-for-bit against dumps of the compiled reference
+ * (tests/golden/, generated by tests/golden/make_golden.py with oracle/ref_harness.cpp).
+ *
+ * Arithmetic is kept in the reference's types and order: BGFLOAT = float
+ * (Utils/BGTypes.h:20-21), each float operation rounded on its own (compile with
+ * -ffp-contract=off), double only where the reference promotes (double literals).
+ */
+#include "bg_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdio.h>
+
+#define ULONG_MAX_U64 0xffffffffffffffffULL
+#define LDELAYQUEUE 32 /* LENGTH_OF_DELAYQUEUE, Synapses/AllSpikingSynapses.h */
+
+/* ============================== RNG ============================== */
+/* MTRand::initialize + reload (RNG/MersenneTwister.cpp:260-291): the standard MT19937. */
+static uint32_t mt_twist(uint32_t m, uint32_t s0, uint32_t s1)
+{
+    return m ^ (((s0 & 0x80000000u) | (s1 & 0x7fffffffu)) >> 1) ^ ((0u - (s1 & 1u)) & 0x9908b0dfu);
+}
+static void mt_reload(bgo_mt *m)
+{
+    uint32_t *s = m->s;
+    int i;
+    for (i = 0; i < 624 - 397; i++) s[i] = mt_twist(s[i + 397], s[i], s[i + 1]);
+    for (; i < 623; i++) s[i] = mt_twist(s[i + 397 - 624], s[i], s[i + 1]);
+    s[623] = mt_twist(s[396], s[623], s[0]);
+    m->left = 624;
+    m->next = 0;
+}
+void bgo_mt_seed(bgo_mt *m, uint32_t seed)
+{
+    m->s[0] = seed;
+    for (int i = 1; i < 624; i++) m->s[i] = 1812433253u * (m->s[i - 1] ^ (m->s[i - 1] >> 30)) + (uint32_t)i;
+    mt_reload(m);
+}
+/* MTRand::randInt (RNG/MersenneTwister.cpp): tempering of the next state word. */
+uint32_t bgo_mt_randint(bgo_mt *m)
+{
+    if (m->left == 0) mt_reload(m);
+    --m->left;
+    uint32_t y = m->s[m->next++];
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    return y ^ (y >> 18);
+}
+/* MTRand::rand: float(randInt) * (1.0/4294967295.0) evaluated in double, returned as float. */
+float bgo_mt_rand(bgo_mt *m)
+{
+    return (float)((double)(float)bgo_mt_randint(m) * (1.0 / 4294967295.0));
+}
+/* MTRand::inRange: val *= (max - min); val += min, all float. */
+float bgo_mt_inrange(bgo_mt *m, float lo, float hi)
+{
+    float v = bgo_mt_rand(m);
+    float range = hi - lo;
+    v *= range;
+    v += lo;
+    return v;
+}
+/* Norm::operator() (RNG/Norm.cpp:59-86): Marsaglia polar method, values returned in pairs. */
+void bgo_norm_init(bgo_norm *n, float mu, float sigma, uint32_t seed)
+{
+    bgo_mt_seed(&n->mt, seed);
+    n->odd = 1;
+    n->mu = mu;
+    n->sigma = sigma;
+    n->x2 = 0.0f;
+}
+float bgo_norm_next(bgo_norm *n)
+{
+    if ((n->odd = !n->odd)) return n->mu + n->sigma * n->x2;
+    float u1, u2, v1, v2, w, y, x1;
+    do {
+        u1 = bgo_mt_rand(&n->mt);
+        u2 = bgo_mt_rand(&n->mt);
+        v1 = 2.0f * u1 - 1.0f;
+        v2 = 2.0f * u2 - 1.0f;
+        w = v1 * v1 + v2 * v2;
+    } while (w > 1.0f);
+    y = sqrtf(-2.0f * logf(w) / w);
+    x1 = v1 * y;
+    n->x2 = v2 * y;
+    return n->mu + n->sigma * x1;
+}
+void bgo_norm_fill(uint32_t seed, float *out, int64_t cnt)
+{
+    bgo_norm n;
+    bgo_norm_init(&n, 0.0f, 1.0f, seed);
+    for (int64_t i = 0; i < cnt; i++) out[i] = bgo_norm_next(&n);
+}
+
+/* ============================== state ============================== */
+struct bgo_net {
+    int N, max_syn, width, height, max_spikes, max_epochs, neuron_kind, syn_kind;
+    float epoch_duration, delta_t;
+    int max_firing_rate;
+    uint64_t step;
+    int flags;
+    bgo_mt rng;      /* global `MTRand rng(1)` (Utils/Global.cpp:79) */
+    bgo_norm noise;  /* rgNormrnd[0] = Norm(0, 1, seed) (Core/SingleThreadedSpikingModel.cpp:30) */
+    float *noise_rec;
+    int64_t noise_cap, noise_n;
+    /* layout */
+    float *xloc, *yloc;
+    int *ntype, *starter;
+    /* IF neurons (Neurons/AllIFNeurons.h:279-362) */
+    float *Vm, *Vthresh, *Vreset, *Vrest, *Vinit, *I0, *Inoise, *Iinject, *C1, *C2, *Trefract;
+    float *Rm, *Cm, *Tau, *sp;
+    int *refr, *spikeCount, *spikeCountOffset;
+    uint8_t *hasFired;
+    uint64_t *history; /* [N][max_spikes] */
+    /* synapse slots, iSyn = dest * max_syn + k (Synapses/AllSynapses.cpp:367) */
+    uint8_t *in_use;
+    int *src, *dest, *type, *total_delay, *delayIdx, *ldelayQueue;
+    float *W, *psr, *decay, *tau, *r, *u, *D, *U, *F;
+    uint32_t *queue, *counts;
+    uint64_t *lastSpike;
+    /* SynapseIndexMap (Core/SynapseIndexMap.h:38-104) */
+    uint32_t *inMap, *inBegin, *inCount, *outMap, *outBegin, *outCount;
+    int64_t total;
+    /* ConnGrowth (Connections/ConnGrowth.h) */
+    float *radii, *rates;
+    float epsilon, beta, rho, target_rate, min_radius, start_radius, max_rate;
+    /* recorder histories (Recorders/XmlRecorder.cpp, XmlGrowthRecorder.cpp) */
+    float *burstinessHist, *spikesHistory, *ratesHistory, *radiiHistory;
+};
+
+#define ALLOC(p, cnt) ((p) = calloc((size_t)(cnt) ? (size_t)(cnt) : 1, sizeof(*(p))))
+
+bgo_net *bgo_create(int N, int max_syn, int width, int height, float epoch_duration, float delta_t,
+                    int max_firing_rate, int max_epochs, int neuron_kind, int synapse_kind)
+{
+    bgo_net *n = calloc(1, sizeof(*n));
+    n->N = N; n->max_syn = max_syn; n->width = width; n->height = height;
+    n->epoch_duration = epoch_duration; n->delta_t = delta_t; n->max_firing_rate = max_firing_rate;
+    n->max_epochs = max_epochs; n->neuron_kind = neuron_kind; n->syn_kind = synapse_kind;
+    /* int max_spikes = (int)(epochDuration * maxFiringRate) (Neurons/AllSpikingNeurons.cpp:81) */
+    n->max_spikes = (int)(epoch_duration * (float)max_firing_rate);
+    bgo_mt_seed(&n->rng, 1);
+    bgo_norm_init(&n->noise, 0.0f, 1.0f, 0);
+    size_t S = (size_t)N * max_syn;
+    ALLOC(n->xloc, N); ALLOC(n->yloc, N); ALLOC(n->ntype, N); ALLOC(n->starter, N);
+    ALLOC(n->Vm, N); ALLOC(n->Vthresh, N); ALLOC(n->Vreset, N); ALLOC(n->Vrest, N);
+    ALLOC(n->Vinit, N); ALLOC(n->I0, N); ALLOC(n->Inoise, N); ALLOC(n->Iinject, N);
+    ALLOC(n->C1, N); ALLOC(n->C2, N); ALLOC(n->Trefract, N); ALLOC(n->Rm, N); ALLOC(n->Cm, N);
+    ALLOC(n->Tau, N); ALLOC(n->sp, N); ALLOC(n->refr, N); ALLOC(n->spikeCount, N);
+    ALLOC(n->spikeCountOffset, N); ALLOC(n->hasFired, N);
+    ALLOC(n->history, (size_t)N * n->max_spikes);
+    for (size_t i = 0; i < (size_t)N * n->max_spikes; i++) n->history[i] = ULONG_MAX_U64;
+    ALLOC(n->in_use, S); ALLOC(n->src, S); ALLOC(n->dest, S); ALLOC(n->type, S);
+    ALLOC(n->total_delay, S); ALLOC(n->delayIdx, S); ALLOC(n->ldelayQueue, S);
+    ALLOC(n->W, S); ALLOC(n->psr, S); ALLOC(n->decay, S); ALLOC(n->tau, S); ALLOC(n->r, S);
+    ALLOC(n->u, S); ALLOC(n->D, S); ALLOC(n->U, S); ALLOC(n->F, S); ALLOC(n->queue, S);
+    ALLOC(n->lastSpike, S); ALLOC(n->counts, N);
+    for (size_t i = 0; i < S; i++) n->type[i] = -1;
+    ALLOC(n->inMap, S); ALLOC(n->outMap, S);
+    ALLOC(n->inBegin, N); ALLOC(n->inCount, N); ALLOC(n->outBegin, N); ALLOC(n->outCount, N);
+    ALLOC(n->radii, N); ALLOC(n->rates, N);
+    int nb = (int)(max_epochs * epoch_duration);
+    ALLOC(n->burstinessHist, nb);
+    ALLOC(n->spikesHistory, (size_t)nb * 100);
+    ALLOC(n->ratesHistory, (size_t)(max_epochs + 1) * N);
+    ALLOC(n->radiiHistory, (size_t)(max_epochs + 1) * N);
+    return n;
+}
+
+void bgo_destroy(bgo_net *n)
+{
+    if (!n) return;
+    void *ptrs[] = {n->xloc, n->yloc, n->ntype, n->starter, n->Vm, n->Vthresh, n->Vreset, n->Vrest,
+                    n->Vinit, n->I0, n->Inoise, n->Iinject, n->C1, n->C2, n->Trefract, n->Rm, n->Cm,
+                    n->Tau, n->sp, n->refr, n->spikeCount, n->spikeCountOffset, n->hasFired,
+                    n->history, n->in_use, n->src, n->dest, n->type, n->total_delay, n->delayIdx,
+                    n->ldelayQueue, n->W, n->psr, n->decay, n->tau, n->r, n->u, n->D, n->U, n->F,
+                    n->queue, n->lastSpike, n->counts, n->inMap, n->outMap, n->inBegin, n->inCount,
+                    n->outBegin, n->outCount, n->radii, n->rates, n->burstinessHist,
+                    n->spikesHistory, n->ratesHistory, n->radiiHistory, n->noise_rec};
+    for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
+    free(n);
+}
+
+void *bgo_array(bgo_net *n, const char *name, int64_t *count, int *esz)
+{
+    int64_t N = n->N, S = (int64_t)n->N * n->max_syn;
+    int nb = (int)(n->max_epochs * n->epoch_duration);
+#define A(nm, ptr, cnt) if (!strcmp(name, nm)) { *count = (cnt); *esz = (int)sizeof(*(ptr)); return (ptr); }
+    A("xloc", n->xloc, N) A("yloc", n->yloc, N) A("ntype", n->ntype, N) A("starter", n->starter, N)
+    A("Vm", n->Vm, N) A("Vthresh", n->Vthresh, N) A("Vreset", n->Vreset, N) A("Vrest", n->Vrest, N)
+    A("Vinit", n->Vinit, N) A("I0", n->I0, N) A("Inoise", n->Inoise, N) A("Iinject", n->Iinject, N)
+    A("C1", n->C1, N) A("C2", n->C2, N) A("Trefract", n->Trefract, N) A("Rm", n->Rm, N)
+    A("Cm", n->Cm, N) A("Tau", n->Tau, N) A("sp", n->sp, N) A("refr", n->refr, N)
+    A("spikeCount", n->spikeCount, N) A("spikeCountOffset", n->spikeCountOffset, N)
+    A("hasFired", n->hasFired, N) A("history", n->history, N * n->max_spikes)
+    A("in_use", n->in_use, S) A("src", n->src, S) A("dest", n->dest, S) A("type", n->type, S)
+    A("total_delay", n->total_delay, S) A("delayIdx", n->delayIdx, S)
+    A("ldelayQueue", n->ldelayQueue, S) A("W", n->W, S) A("psr", n->psr, S)
+    A("decay", n->decay, S) A("tau", n->tau, S) A("r", n->r, S) A("u", n->u, S) A("D", n->D, S)
+    A("U", n->U, S) A("F", n->F, S) A("queue", n->queue, S) A("lastSpike", n->lastSpike, S)
+    A("counts", n->counts, N) A("inMap", n->inMap, n->total) A("outMap", n->outMap, n->total)
+    A("inBegin", n->inBegin, N) A("inCount", n->inCount, N) A("outBegin", n->outBegin, N)
+    A("outCount", n->outCount, N) A("radii", n->radii, N) A("rates", n->rates, N)
+    A("burstinessHist", n->burstinessHist, nb) A("spikesHistory", n->spikesHistory, (int64_t)nb * 100)
+    A("ratesHistory", n->ratesHistory, (int64_t)(n->max_epochs + 1) * N)
+    A("radiiHistory", n->radiiHistory, (int64_t)(n->max_epochs + 1) * N)
+    A("noise", n->noise_rec, n->noise_n)
+#undef A
+    *count = 0; *esz = 0;
+    return NULL;
+}
+
+uint64_t bgo_get_step(const bgo_net *n) { return n->step; }
+void bgo_set_step(bgo_net *n, uint64_t s) { n->step = s; }
+int64_t bgo_total_synapses(const bgo_net *n) { return n->total; }
+int bgo_flags(const bgo_net *n) { return n->flags; }
+
+void bgo_record_noise(bgo_net *n, int64_t cap)
+{
+    free(n->noise_rec);
+    n->noise_rec = malloc((size_t)(cap > 0 ? cap : 1) * sizeof(float));
+    n->noise_cap = cap;
+    n->noise_n = 0;
+}
+int64_t bgo_noise_recorded(const bgo_net *n) { return n->noise_n; }
+
+/* ============================== setup ============================== */
+/* Layout::initNeuronsLocs, grid branch (Layouts/Layout.cpp:148-158). */
+void bgo_layout_grid(bgo_net *n)
+{
+    for (int i = 0; i < n->N; i++) {
+        n->xloc[i] = (float)(i % n->width);
+        n->yloc[i] = (float)(i / n->width);
+    }
+}
+/* FixedLayout::generateNeuronTypeMap / initStarterMap (Layouts/FixedLayout.cpp:247-279). */
+void bgo_set_types(bgo_net *n, const int *inh, int n_inh, const int *st, int n_st)
+{
+    for (int i = 0; i < n->N; i++) { n->ntype[i] = BGO_EXC; n->starter[i] = 0; }
+    for (int i = 0; i < n_inh; i++) n->ntype[inh[i]] = BGO_INH;
+    for (int i = 0; i < n_st; i++) n->starter[st[i]] = 1;
+}
+/* AllIFNeurons::createAllNeurons / setNeuronDefaults / createNeuron /
+ * initNeuronConstsFromParamValues (Neurons/AllIFNeurons.cpp:380-503).  The draws come from the
+ * global rng in neuron order: Iinject, Inoise, Vthresh, Vrest, Vreset, Vinit, then for starters
+ * Vthresh and Vreset again. */
+void bgo_create_lif(bgo_net *n, const float *g)
+{
+    for (int i = 0; i < n->N; i++) {
+        n->Cm[i] = (float)3e-8;     /* DEFAULT_Cm (Utils/Global.h:103) */
+        n->Rm[i] = (float)1e6;      /* DEFAULT_Rm */
+        n->Tau[i] = (float)(3e-8 * 1e6);
+        n->Iinject[i] = bgo_mt_inrange(&n->rng, g[0], g[1]);
+        n->Inoise[i] = bgo_mt_inrange(&n->rng, g[2], g[3]);
+        n->Vthresh[i] = bgo_mt_inrange(&n->rng, g[4], g[5]);
+        n->Vrest[i] = bgo_mt_inrange(&n->rng, g[6], g[7]);
+        n->Vreset[i] = bgo_mt_inrange(&n->rng, g[8], g[9]);
+        n->Vinit[i] = bgo_mt_inrange(&n->rng, g[10], g[11]);
+        n->Vm[i] = n->Vinit[i];
+        float tau = n->Tau[i];
+        if (tau > 0) {
+            n->C1[i] = expf(-n->delta_t / tau);
+            n->C2[i] = n->Rm[i] * (1.0f - n->C1[i]);
+        } else {
+            n->C1[i] = 0.0f;
+            n->C2[i] = n->Rm[i];
+        }
+        n->I0[i] = n->Iinject[i] + n->Vrest[i] / n->Rm[i];
+        /* DEFAULT_InhibTrefract 2.0e-3 / DEFAULT_ExcitTrefract 3.0e-3 (Utils/Global.h:121-123) */
+        n->Trefract[i] = (n->ntype[i] == BGO_INH) ? (float)2.0e-3 : (float)3.0e-3;
+        if (n->starter[i]) {
+            n->Vthresh[i] = bgo_mt_inrange(&n->rng, g[12], g[13]);
+            n->Vreset[i] = bgo_mt_inrange(&n->rng, g[14], g[15]);
+            n->Trefract[i] = (float)3.0e-3;
+        }
+    }
+}
+void bgo_growth_init(bgo_net *n, float eps, float beta, float rho, float tr, float minr, float startr)
+{
+    n->epsilon = eps; n->beta = beta; n->rho = rho; n->target_rate = tr;
+    n->min_radius = minr; n->start_radius = startr;
+    n->max_rate = tr / eps; /* Connections/ConnGrowth.cpp:201-203 */
+    for (int i = 0; i < n->N; i++) { n->radii[i] = startr; n->rates[i] = 0.0f; }
+    /* XmlGrowthRecorder::initDefaultValues: history row 0 holds the start values. */
+    for (int i = 0; i < n->N; i++) {
+        n->radiiHistory[i] = startr;
+        n->ratesHistory[i] = 0.0f;
+    }
+}
+void bgo_seed_noise(bgo_net *n, uint32_t seed) { bgo_norm_init(&n->noise, 0.0f, 1.0f, seed); }
+
+/* AllSpikingSynapses::createSynapse + AllDSSynapses::createSynapse + resets
+ * (Synapses/AllSpikingSynapses.cpp:192-240, AllDSSynapses.cpp:160-218). */
+static void create_synapse_slot(bgo_net *n, size_t iSyn, int src, int dest, int type)
+{
+    float tau, delay;
+    n->in_use[iSyn] = 1;
+    n->dest[iSyn] = dest;
+    n->src[iSyn] = src;
+    n->W[iSyn] = (float)((double)((type == BGO_II || type == BGO_IE) ? -1 : 1) * 10.0e-9);
+    n->type[iSyn] = type;
+    switch (type) {
+    case BGO_II: tau = (float)6e-3; delay = (float)0.8e-3; break;
+    case BGO_IE: tau = (float)6e-3; delay = (float)0.8e-3; break;
+    case BGO_EI: tau = (float)3e-3; delay = (float)0.8e-3; break;
+    default:     tau = (float)3e-3; delay = (float)1.5e-3; break;
+    }
+    n->tau[iSyn] = tau;
+    n->total_delay[iSyn] = (int)(delay / n->delta_t) + 1;
+    n->queue[iSyn] = 0;
+    n->delayIdx[iSyn] = 0;
+    n->ldelayQueue[iSyn] = LDELAYQUEUE;
+    n->psr[iSyn] = 0.0f;
+    n->decay[iSyn] = expf(-n->delta_t / tau);
+    if (n->syn_kind == BGO_SYN_DS || n->syn_kind == BGO_SYN_DSTDP) {
+        n->u[iSyn] = (float)0.4; /* DEFAULT_U */
+        n->r[iSyn] = 1.0f;
+        n->lastSpike[iSyn] = ULONG_MAX_U64;
+        float U, D, F;
+        switch (type) {
+        case BGO_II: U = (float)0.32; D = (float)0.144; F = (float)0.06; break;
+        case BGO_IE: U = (float)0.25; D = (float)0.7; F = (float)0.02; break;
+        case BGO_EI: U = (float)0.05; D = (float)0.125; F = (float)1.2; break;
+        default:     U = (float)0.5; D = (float)1.1; F = (float)0.05; break;
+        }
+        n->U[iSyn] = U; n->D[iSyn] = D; n->F[iSyn] = F;
+    }
+}
+
+/* AllSynapses::addSynapse (Synapses/AllSynapses.cpp:357-377): first free slot of the dest row. */
+static long add_synapse(bgo_net *n, int type, int src, int dest)
+{
+    if (n->counts[dest] >= (uint32_t)n->max_syn) { n->flags |= 1; return -1; }
+    size_t iSyn = 0;
+    for (int k = 0; k < n->max_syn; k++) {
+        iSyn = (size_t)n->max_syn * dest + k;
+        if (!n->in_use[iSyn]) break;
+    }
+    n->counts[dest]++;
+    create_synapse_slot(n, iSyn, src, dest, type);
+    return (long)iSyn;
+}
+void bgo_create_synapse(bgo_net *n, int dest, int src, int type, float W)
+{
+    long iSyn = add_synapse(n, type, src, dest);
+    if (iSyn >= 0) n->W[iSyn] = W;
+}
+
+/* AllSynapses::createSynapseImap (Synapses/AllSynapses.cpp:223-293).  The reference leaves the
+ * previous map in place when there are no synapses; an empty map is equivalent. */
+int bgo_rebuild_maps(bgo_net *n)
+{
+    int N = n->N, M = n->max_syn;
+    int64_t total = 0;
+    for (int i = 0; i < N; i++) total += n->counts[i];
+    int64_t nin = 0;
+    for (int i = 0; i < N; i++) n->outCount[i] = 0;
+    for (int i = 0; i < N; i++) {
+        n->inBegin[i] = (uint32_t)nin;
+        uint32_t c = 0;
+        for (int j = 0; j < M; j++) {
+            size_t s = (size_t)i * M + j;
+            if (n->in_use[s]) { n->inMap[nin++] = (uint32_t)s; c++; n->outCount[n->src[s]]++; }
+        }
+        n->inCount[i] = c;
+    }
+    /* outgoing: grouped by source, ascending slot order within a source */
+    uint32_t acc = 0;
+    for (int i = 0; i < N; i++) { n->outBegin[i] = acc; acc += n->outCount[i]; }
+    uint32_t *fill = calloc(N > 0 ? (size_t)N : 1u, sizeof(uint32_t));
+    for (int64_t q = 0; q < nin; q++) {
+        uint32_t s = n->inMap[q];
+        int sr = n->src[s];
+        n->outMap[n->outBegin[sr] + fill[sr]++] = s;
+    }
+    free(fill);
+    n->total = nin;
+    return (nin == total) ? 0 : -1;
+}
+
+/* ============================== step ============================== */
+/* AllSpikingNeurons::fire (Neurons/AllSpikingNeurons.cpp:155-172) + AllLIFNeurons::fire
+ * (Neurons/AllLIFNeurons.cpp:67-77). */
+static void lif_fire(bgo_net *n, int i)
+{
+    n->hasFired[i] = 1;
+    int idxSp = (n->spikeCount[i] + n->spikeCountOffset[i]) % n->max_spikes;
+    n->history[(size_t)i * n->max_spikes + idxSp] = n->step;
+    n->spikeCount[i]++;
+    n->refr[i] = (int)((double)(n->Trefract[i] / n->delta_t) + 0.5);
+    n->Vm[i] = n->Vreset[i];
+}
+
+/* AllLIFNeurons::advanceNeuron (Neurons/AllLIFNeurons.cpp:20-59). */
+static void lif_advance(bgo_net *n, int i)
+{
+    if (n->refr[i] > 0) {
+        --n->refr[i];
+    } else if (n->Vm[i] >= n->Vthresh[i]) {
+        lif_fire(n, i);
+    } else {
+        n->sp[i] += n->I0[i];
+        float noise = bgo_norm_next(&n->noise);
+        if (n->noise_rec && n->noise_n < n->noise_cap) n->noise_rec[n->noise_n++] = noise;
+        n->sp[i] += noise * n->Inoise[i];
+        n->Vm[i] = n->C1[i] * n->Vm[i] + n->C2[i] * n->sp[i];
+    }
+    n->sp[i] = 0.0f;
+}
+
+/* AllSpikingSynapses::preSpikeHit (Synapses/AllSpikingSynapses.cpp:261-279). */
+static void pre_spike_hit(bgo_net *n, uint32_t s)
+{
+    int idx = n->delayIdx[s] + n->total_delay[s];
+    if (idx >= n->ldelayQueue[s]) idx -= n->ldelayQueue[s];
+    n->queue[s] |= (1u << idx);
+}
+
+/* AllSpikingNeurons::advanceNeurons (Neurons/AllSpikingNeurons.cpp:98-147): descending index. */
+static void advance_neurons(bgo_net *n)
+{
+    for (int i = n->N - 1; i >= 0; --i) {
+        lif_advance(n, i);
+        if (n->hasFired[i]) {
+            if (n->total > 0) {
+                uint32_t c = n->outCount[i], b = n->outBegin[i];
+                for (uint32_t k = 0; k < c; k++) pre_spike_hit(n, n->outMap[b + k]);
+            }
+            n->hasFired[i] = 0;
+        }
+    }
+}
+
+/* AllDSSynapses::changePSR (Synapses/AllDSSynapses.cpp:227-247). */
+static void ds_change_psr(bgo_net *n, size_t s)
+{
+    if (n->lastSpike[s] != ULONG_MAX_U64) {
+        float isi = (float)(n->step - n->lastSpike[s]) * n->delta_t;
+        n->r[s] = 1.0f + (n->r[s] * (1.0f - n->u[s]) - 1.0f) * expf(-isi / n->D[s]);
+        n->u[s] = n->U[s] + n->u[s] * (1.0f - n->U[s]) * expf(-isi / n->F[s]);
+    }
+    n->psr[s] += ((n->W[s] / n->decay[s]) * n->u[s] * n->r[s]);
+    n->lastSpike[s] = n->step;
+}
+
+/* AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331) over the incoming map, with
+ * AllSpikingSynapses::advanceSynapse / isSpikeQueue (AllSpikingSynapses.cpp:242-319). */
+static void advance_synapses(bgo_net *n)
+{
+    for (int64_t q = 0; q < n->total; q++) {
+        uint32_t s = n->inMap[q];
+        uint32_t bit = 1u << n->delayIdx[s];
+        int hit = (n->queue[s] & bit) != 0;
+        n->queue[s] &= ~bit;
+        if (++n->delayIdx[s] >= n->ldelayQueue[s]) n->delayIdx[s] = 0;
+        if (hit) {
+            if (n->syn_kind == BGO_SYN_DS)
+                ds_change_psr(n, s);
+            else
+                n->psr[s] += (n->W[s] / n->decay[s]); /* AllSpikingSynapses::changePSR :327-334 */
+        }
+        n->psr[s] *= n->decay[s];
+        n->sp[n->dest[s]] += n->psr[s];
+    }
+}
+
+void bgo_step(bgo_net *n, int nsteps)
+{
+    for (int t = 0; t < nsteps; t++) {
+        advance_neurons(n);
+        advance_synapses(n);
+        n->step++;
+    }
+}
+
+/* ============================== growth ============================== */
+/* ConnGrowth::updateConns (Connections/ConnGrowth.cpp:295-311). */
+static void update_conns(bgo_net *n)
+{
+    float T = n->epoch_duration;
+    float trho = n->epoch_duration * n->rho;
+    for (int i = 0; i < n->N; i++) {
+        n->rates[i] = (float)n->spikeCount[i] / T;
+        float e = expf((n->epsilon - n->rates[i] / n->max_rate) / n->beta);
+        float og = 1.0f - 2.0f / (e + 1.0f);
+        n->radii[i] += trho * og;
+    }
+}
+
+/* Per-pair frontier distance and overlap area (ConnGrowth.cpp:319-376) for (i = src, j = dest). */
+static float pair_area(const bgo_net *n, int i, int j)
+{
+    if (i == j) return 0.0f;
+    float dx = n->xloc[i] - n->xloc[j], dy = n->yloc[i] - n->yloc[j];
+    float lenAB2 = dx * dx + dy * dy;
+    float lenAB = sqrtf(lenAB2);
+    float r1 = n->radii[i], r2 = n->radii[j];
+    float delta = lenAB - (r1 + r2);
+    if (!(delta < 0)) return 0.0f;
+    float rmin = r1 < r2 ? r1 : r2, rmax = r1 < r2 ? r2 : r1;
+    if (lenAB + rmin <= rmax) {
+        const float pi = (float)3.1415926536; /* Utils/Global.cpp:90 */
+        return pi * rmin * rmin;
+    }
+    float r12 = r1 * r1, r22 = r2 * r2;
+    float cosCBA = (float)((double)(r22 + lenAB2 - r12) / (2.0 * (double)r2 * (double)lenAB));
+    float angCBA = acosf(cosCBA);
+    float angCBD = (float)(2.0 * (double)angCBA);
+    float cosCAB = (float)((double)(r12 + lenAB2 - r22) / (2.0 * (double)r1 * (double)lenAB));
+    float angCAB = acosf(cosCAB);
+    float angCAD = (float)(2.0 * (double)angCAB);
+    return (float)(0.5 * (double)(r22 * (angCBD - sinf(angCBD)) + r12 * (angCAD - sinf(angCAD))));
+}
+
+static int syn_type(const bgo_net *n, int src, int dest)
+{
+    int si = n->ntype[src] == BGO_INH, di = n->ntype[dest] == BGO_INH;
+    return si ? (di ? BGO_II : BGO_IE) : (di ? BGO_EI : BGO_EE);
+}
+
+/* ConnGrowth::updateSynapsesWeights, CPU variant (Connections/ConnGrowth.cpp:388-463). */
+static void update_weights(bgo_net *n)
+{
+    const float adj = (float)1.0e-8; /* AllSynapses::SYNAPSE_STRENGTH_ADJUSTMENT */
+    for (int s = 0; s < n->N; s++) {
+        for (int d = 0; d < n->N; d++) {
+            float w = pair_area(n, s, d);
+            int type = syn_type(n, s, d);
+            int sign = (type == BGO_II || type == BGO_IE) ? -1 : 1;
+            int connected = 0;
+            uint32_t cnt = n->counts[d], seen = 0;
+            size_t iSyn = (size_t)n->max_syn * d;
+            for (; seen < cnt; iSyn++) {
+                if (n->in_use[iSyn]) {
+                    if (n->src[iSyn] == s) {
+                        connected = 1;
+                        if (w < 0) {
+                            n->counts[d]--;
+                            n->in_use[iSyn] = 0;
+                        } else {
+                            n->W[iSyn] = w * (float)sign * adj;
+                        }
+                    }
+                    seen++;
+                }
+            }
+            if (!connected && w > 0) {
+                long k = add_synapse(n, type, s, d);
+                if (k >= 0) n->W[k] = w * (float)sign * adj;
+            }
+        }
+    }
+}
+
+void bgo_growth(bgo_net *n)
+{
+    update_conns(n);
+    update_weights(n);
+    bgo_rebuild_maps(n);
+}
+
+/* XmlRecorder::compileHistories (Recorders/XmlRecorder.cpp:71-104) followed by the growth part
+ * (Recorders/XmlGrowthRecorder.cpp:72-97: rates/radii history, radius clamp) and
+ * AllSpikingNeurons::clearSpikeCounts (Neurons/AllSpikingNeurons.cpp:77-86). */
+void bgo_record_epoch(bgo_net *n, int epoch)
+{
+    int ms = n->max_spikes;
+    for (int i = 0; i < n->N; i++) {
+        const uint64_t *h = n->history + (size_t)i * ms;
+        for (int k = 0, idx = n->spikeCountOffset[i]; k < n->spikeCount[i]; k++, idx++) {
+            if (idx >= ms) idx = 0;
+            int b1 = (int)((double)h[idx] * (double)n->delta_t);
+            n->burstinessHist[b1] = n->burstinessHist[b1] + 1.0f;
+            int b2 = (int)((double)h[idx] * (double)n->delta_t * 100);
+            n->spikesHistory[b2] = n->spikesHistory[b2] + 1.0f;
+        }
+    }
+    for (int i = 0; i < n->N; i++) {
+        n->ratesHistory[(size_t)epoch * n->N + i] = n->rates[i];
+        if (n->radii[i] < n->min_radius) n->radii[i] = n->min_radius;
+        n->radiiHistory[(size_t)epoch * n->N + i] = n->radii[i];
+    }
+    for (int i = 0; i < n->N; i++) {
+        n->spikeCountOffset[i] = (n->spikeCount[i] + n->spikeCountOffset[i]) % ms;
+        n->spikeCount[i] = 0;
+    }
+}

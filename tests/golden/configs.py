@@ -1,0 +1,136 @@
+"""Network configurations shared by the fixture generator and the tests.
+
+Each case is described twice, consistently: as a BrainGrid XML config (written by
+write_config_tree for the reference harness) and as plain parameters (read by the tests to set up
+the oracle and the CUDA path without the reference tree).
+
+The config[0]-style networks follow the stated model: LIF neurons, AllDSSynapses, ConnGrowth,
+FixedLayout with 10 % inhibitory and 10 endogenously active (starter) sites chosen by a seeded
+shuffle; Iinject 13.5 nA, Inoise U[1.0, 1.5] nA, Vthresh 15 mV (starters U[13.565, 13.655] mV),
+Vreset 13.5 mV (starters 13.0 mV), Vrest 0, Vinit 13.0 mV, dt 0.1 ms.
+"""
+import os
+
+import numpy as np
+
+LIF_RANGES = [13.5e-9, 13.5e-9, 1.0e-9, 1.5e-9, 15.0e-3, 15.0e-3, 0.0, 0.0,
+              13.5e-3, 13.5e-3, 13.0e-3, 13.0e-3, 13.565e-3, 13.655e-3, 13.0e-3, 13.0e-3]
+
+
+def site_lists(width, height, frac_inh=0.10, n_starters=10, seed=1):
+    """Seeded choice of inhibitory and starter sites (starters are excitatory)."""
+    N = width * height
+    rs = np.random.RandomState(seed)
+    perm = rs.permutation(N)
+    n_inh = int(round(frac_inh * N))
+    inh = np.sort(perm[:n_inh])
+    starters = np.sort(perm[n_inh:n_inh + n_starters])
+    return [int(x) for x in inh], [int(x) for x in starters]
+
+
+def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, radii=None,
+          max_firing_rate=200, frac_inh=0.10, n_starters=10, site_seed=1, keep_steps_every=None,
+          fp64=False, config=None, inh=None, starters=None, syn_keep=None):
+    if inh is None:
+        inh, starters = site_lists(width, height, frac_inh, n_starters, site_seed)
+    c = dict(name=name, width=width, height=height, N=width * height, tsim=tsim, epochs=epochs,
+             max_syn=max_syn, seed=seed, max_firing_rate=max_firing_rate, inh=inh,
+             starters=starters, growth=dict(epsilon=0.60, beta=0.10, rho=1e-4,
+                                            target_rate=target_rate, min_radius=0.1,
+                                            start_radius=0.4),
+             radii=radii, keep_steps_every=keep_steps_every, fp64=fp64, syn_keep=syn_keep)
+    c["config"] = config or "configfiles/bg3/%s.xml" % name
+    args = []
+    if radii is not None:
+        args += ["--radii", repr(radii)]
+    if keep_steps_every:
+        args += ["--dump-every", str(keep_steps_every)]
+    c["args"] = args
+    return c
+
+
+CASES = [
+    # the reference's own tiny test (2x2, 1 epoch of 1 s), with its own NLists
+    _case("ref_tiny", 2, 2, 1.0, 1, 200, target_rate=1.9, config="configfiles/test-tiny.xml",
+          inh=[1], starters=[0], keep_steps_every=500),
+    # config[0]: 10x10, 10 epochs x 1 s, max 100 synapses per neuron, seed 1
+    _case("c0", 10, 10, 1.0, 10, 100, keep_steps_every=5000),
+    # config[0] network with a pre-grown radius so that growth wires it after epoch 1
+    # (the reference recorder needs epoch duration x epochs >= 1 s)
+    _case("c0_grown", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000,
+          keep_steps_every=100),
+    # 30x30 pre-grown network, larger fan-in and fan-out
+    _case("m30_grown", 30, 30, 0.1, 10, 200, radii=2.0, max_firing_rate=1000, site_seed=3,
+          keep_steps_every=1000, syn_keep=(9,)),
+    # FP64 reference on config[0] (long-run comparison base)
+    _case("c0_fp64", 10, 10, 1.0, 10, 100, fp64=True),
+]
+
+
+def case(name):
+    for c in CASES:
+        if c["name"] == name:
+            return c
+    raise KeyError(name)
+
+
+_XML = """<?xml version="1.0" encoding="UTF-8" standalone="no"?>
+<BGSimParams>
+  <SimInfoParams name="SimInfoParams">
+    <PoolSize name="PoolSize"><x name="x">{width}</x><y name="y">{height}</y><z name="z">1</z></PoolSize>
+    <SimParams name="SimParams"><Tsim name="Tsim">{tsim}</Tsim><numSims name="numSims">{epochs}</numSims></SimParams>
+    <SimConfig name="SimConfig">
+      <maxFiringRate name="maxFiringRate">{max_firing_rate}</maxFiringRate>
+      <maxSynapsesPerNeuron name="maxSynapsesPerNeuron">{max_syn}</maxSynapsesPerNeuron>
+    </SimConfig>
+    <Seed name="Seed"><value name="value">{seed}</value></Seed>
+    <OutputParams name="OutputParams"><stateOutputFileName name="stateOutputFileName">results/{name}-out.xml</stateOutputFileName></OutputParams>
+  </SimInfoParams>
+  <ModelParams>
+    <NeuronsParams class="AllLIFNeurons" name="NeuronsParams">
+      <Iinject name="Iinject"><min name="min">13.5e-09</min><max name="max">13.5e-09</max></Iinject>
+      <Inoise name="Inoise"><min name="min">1.0e-09</min><max name="max">1.5e-09</max></Inoise>
+      <Vthresh name="Vthresh"><min name="min">15.0e-03</min><max name="max">15.0e-03</max></Vthresh>
+      <Vresting name="Vresting"><min name="min">0.0</min><max name="max">0.0</max></Vresting>
+      <Vreset name="Vreset"><min name="min">13.5e-03</min><max name="max">13.5e-03</max></Vreset>
+      <Vinit name="Vinit"><min name="min">13.0e-03</min><max name="max">13.0e-03</max></Vinit>
+      <starter_vthresh name="starter_vthresh"><min name="min">13.565e-3</min><max name="max">13.655e-3</max></starter_vthresh>
+      <starter_vreset name="starter_vreset"><min name="min">13.0e-3</min><max name="max">13.0e-3</max></starter_vreset>
+    </NeuronsParams>
+    <SynapsesParams class="AllDSSynapses" name="SynapsesParams"></SynapsesParams>
+    <ConnectionsParams class="ConnGrowth" name="ConnectionsParams">
+      <GrowthParams name="GrowthParams">
+        <epsilon name="epsilon">{epsilon}</epsilon><beta name="beta">{beta}</beta><rho name="rho">{rho}</rho>
+        <targetRate name="targetRate">{target_rate}</targetRate><minRadius name="minRadius">{min_radius}</minRadius>
+        <startRadius name="startRadius">{start_radius}</startRadius>
+      </GrowthParams>
+    </ConnectionsParams>
+    <LayoutParams class="FixedLayout" name="LayoutParams">
+      <LayoutFiles name="LayoutFiles">
+        <activeNListFileName name="activeNListFileName" type="InputFile">configfiles/bg3/{name}-active.xml</activeNListFileName>
+        <inhNListFileName name="inhNListFileName" type="InputFile">configfiles/bg3/{name}-inh.xml</inhNListFileName>
+        <probedNListFileName name="prbNListFileName" type="InputFile"/>
+      </LayoutFiles>
+    </LayoutParams>
+  </ModelParams>
+</BGSimParams>
+"""
+
+
+def write_config_tree(cfgdir):
+    """Write configfiles/bg3/<case>.xml and its NLists for every generated case."""
+    d = os.path.join(cfgdir, "bg3")
+    os.makedirs(d, exist_ok=True)
+    for c in CASES:
+        if not c["config"].startswith("configfiles/bg3/"):
+            continue
+        p = dict(c)
+        p.update(c["growth"])
+        with open(os.path.join(d, c["name"] + ".xml"), "w") as f:
+            f.write(_XML.format(**p))
+        with open(os.path.join(d, c["name"] + "-active.xml"), "w") as f:
+            f.write('<?xml version="1.0" encoding="UTF-8"?>\n<A>%s</A>\n'
+                    % " ".join(str(i) for i in c["starters"]))
+        with open(os.path.join(d, c["name"] + "-inh.xml"), "w") as f:
+            f.write('<?xml version="1.0" encoding="UTF-8"?>\n<I>%s</I>\n'
+                    % " ".join(str(i) for i in c["inh"]))

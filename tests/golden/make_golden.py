@@ -1,0 +1,151 @@
+"""Generate the committed parity fixtures in tests/golden/ from the compiled reference.
+
+Run in a checkout that has the reference sources (default /root/reference):
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+It (1) writes the network configs and NLists under tests/golden/configs/, (2) builds the
+reference single-threaded simulator and oracle/ref_harness.cpp with oracle/ref.mk, (3) runs the
+harness on each case, and (4) keeps a compact subset of each dump as tests/golden/<case>.npz.
+The reference's own CPU golden outputs for test-tiny and test-small
+(old/validation/4-2016/growth/test-{tiny,small}-out.xml) are parsed into ref_goldens.npz.
+
+Nothing at test time reads the reference tree: the tests only read the .npz files written here.
+"""
+import argparse
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle.refdump import read_dump  # noqa: E402
+from tests.golden.configs import write_config_tree, CASES  # noqa: E402
+
+
+def build_reference(ref, fp64=False):
+    target = ["fp64"] if fp64 else []
+    subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref.mk"),
+                           "REF=" + ref, "-j8"] + target, cwd=ROOT)
+    return os.path.join(ROOT, "oracle", "_ref64" if fp64 else "_ref", "bg_ref_harness")
+
+
+def run_harness(harness, workdir, cfg, args, out):
+    cmd = [harness, "-t", cfg, "-o", out] + args
+    subprocess.check_call(cmd, cwd=workdir, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    return read_dump(out)
+
+
+def compact(d, keep_steps_every=None, syn_keep=None):
+    """Select the records the tests use; spike rasters become (step, neuron) pairs."""
+    out = {}
+    for name, recs in d.items():
+        if name.startswith(("n.",)):
+            continue
+        if name.startswith("s."):
+            for step, a in recs:
+                if keep_steps_every and step % keep_steps_every == 0:
+                    out["%s@%d" % (name, step)] = a
+            continue
+        if name.endswith(("history",)) and name.split(".")[0] in ("pre",):
+            # spike raster of each epoch from the history ring + counts
+            pass
+        for k, (step, a) in enumerate(recs):
+            key = name if len(recs) == 1 else "%s#%d" % (name, k)
+            out[key] = a
+    # rasters per epoch from the pre-growth snapshots
+    cnts = d.get("pre.spikeCount", [])
+    offs = d.get("pre.spikeCountOffset", [])
+    hist = d.get("pre.history", [])
+    ms = int(d["hdr"][0][1][4])
+    N = int(d["hdr"][0][1][0])
+    for k, ((_, c), (_, o), (_, h)) in enumerate(zip(cnts, offs, hist)):
+        h = h.reshape(N, ms)
+        steps, nrn = [], []
+        for i in range(N):
+            for j in range(int(c[i])):
+                steps.append(int(h[i, (int(o[i]) + j) % ms]))
+                nrn.append(i)
+        order = np.lexsort((np.array(nrn), np.array(steps))) if steps else np.zeros(0, np.int64)
+        out["raster#%d" % k] = np.stack([np.array(steps, np.int64)[order],
+                                         np.array(nrn, np.int64)[order]]) if steps else \
+            np.zeros((2, 0), np.int64)
+    # drop the bulky per-epoch history rings; keep slot arrays only at in-use slots (their
+    # indices are stored as <prefix>slots), and skip the post-growth synapse copy, which the
+    # recorder step does not change
+    S = N * int(d["hdr"][0][1][1])
+    for key in list(out):
+        if ".history" in key or (key.startswith("grow.") and out[key].size == S):
+            del out[key]
+        elif key.startswith("post.") and out[key].size == S and key.split("#")[0] not in (
+                "post.in_use", "post.W", "post.src"):
+            del out[key]
+        elif syn_keep is not None and out[key].size != N and "#" in key \
+                and key.startswith(("pre.", "grow.", "post.")) \
+                and int(key.split("#")[1]) not in syn_keep:
+            del out[key]
+    for key in list(out):
+        if key.endswith("in_use") or key.split("#")[0].endswith(".in_use"):
+            pfx, _, idx = key.partition("in_use")
+            mask = out.pop(key, None)
+            if mask is None:
+                continue
+            mask = mask.astype(bool)
+            out[pfx + "slots" + idx] = np.nonzero(mask)[0].astype(np.int64)
+            for k2 in list(out):
+                base, _, i2 = k2.partition("#")
+                if k2 != key and base.startswith(pfx) and (("#" + i2) if i2 else "") == idx \
+                        and out[k2].size == S and base.count(".") == pfx.count("."):
+                    out[k2] = out[k2][mask]
+    return out
+
+
+def parse_xml_matrix(text, name):
+    m = re.search(r'<Matrix name="%s"[^>]*rows="(\d+)" columns="(\d+)"[^>]*>(.*?)</Matrix>' % name,
+                  text, re.S)
+    rows, cols = int(m.group(1)), int(m.group(2))
+    vals = np.array([float(v) for v in m.group(3).split()], dtype=np.float64)
+    return vals.reshape(rows, cols)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--cases", default="")
+    a = ap.parse_args()
+    harness = build_reference(a.ref)
+    harness64 = build_reference(a.ref, fp64=True)
+    work = tempfile.mkdtemp(prefix="bg_golden_")
+    try:
+        cfgdir = os.path.join(work, "configfiles")
+        shutil.copytree(os.path.join(a.ref, "configfiles"), cfgdir)
+        write_config_tree(cfgdir)
+        os.makedirs(os.path.join(work, "results"), exist_ok=True)
+        selected = [c for c in CASES if not a.cases or c["name"] in a.cases.split(",")]
+        for case in selected:
+            h = harness64 if case.get("fp64") else harness
+            d = run_harness(h, work, case["config"], case["args"],
+                            os.path.join(work, case["name"] + ".bin"))
+            out = compact(d, case.get("keep_steps_every"), case.get("syn_keep"))
+            np.savez_compressed(os.path.join(HERE, case["name"] + ".npz"), **out)
+            print("wrote", case["name"], len(out), "arrays")
+        # the reference's own CPU goldens
+        g = {}
+        for nm in ("test-tiny", "test-small"):
+            txt = open(os.path.join(a.ref, "old/validation/4-2016/growth/%s-out.xml" % nm)).read()
+            for mat in ("radiiHistory", "ratesHistory", "burstinessHist", "spikesHistory"):
+                g["%s.%s" % (nm, mat)] = parse_xml_matrix(txt, mat)
+        np.savez_compressed(os.path.join(HERE, "ref_goldens.npz"), **g)
+        print("wrote ref_goldens")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,83 @@
+"""Helpers that build the same network in the oracle and compare states against fixtures."""
+import os
+
+import numpy as np
+
+from oracle import pyoracle as po
+from tests.golden.configs import LIF_RANGES, case
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# the reference's own test-small (configfiles/test-small.xml with its 10x10 NLists)
+TEST_SMALL = dict(name="ref_small", width=10, height=10, N=100, tsim=100.0, epochs=2, max_syn=200,
+                  seed=1, max_firing_rate=200, inh=[33, 66],
+                  starters=[7, 11, 14, 37, 41, 44, 67, 71, 74, 97],
+                  growth=dict(epsilon=0.60, beta=0.10, rho=1e-4, target_rate=1.9, min_radius=0.1,
+                              start_radius=0.4), radii=None)
+
+
+def load_fixture(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def oracle_from_case(c, record_noise=0):
+    """Set up an oracle network exactly as Model::setupSim does for this case."""
+    o = po.OracleNet(c["N"], c["max_syn"], c["width"], c["height"], c["tsim"], 1e-4,
+                     c["max_firing_rate"], c["epochs"])
+    o.layout_grid()
+    o.set_types(c["inh"], c["starters"])
+    o.create_lif(LIF_RANGES)
+    g = c["growth"]
+    o.growth_init(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
+                  g["start_radius"])
+    o.seed_noise(c["seed"])
+    if record_noise:
+        o.record_noise(record_noise)
+    if c.get("radii") is not None:
+        o.arr("radii")[:] = np.float32(c["radii"])
+    return o
+
+
+def steps_per_epoch(c):
+    # static_cast<uint64_t>(epochDuration / deltaT) in float (Core/Simulator.cpp:159-160)
+    return int(np.float32(c["tsim"]) / np.float32(1e-4))
+
+
+def bits(a):
+    a = np.asarray(a)
+    if a.dtype == np.float32:
+        return a.view(np.uint32)
+    if a.dtype == np.float64:
+        return a.view(np.uint64)
+    return a
+
+
+def assert_same(name, got, want):
+    got, want = np.asarray(got), np.asarray(want)
+    assert got.shape == want.shape, "%s: shape %s vs %s" % (name, got.shape, want.shape)
+    if got.dtype.kind == "f":
+        want = want.astype(got.dtype)
+    gb, wb = bits(got), bits(want.astype(got.dtype) if got.dtype != want.dtype else want)
+    if not np.array_equal(gb, wb):
+        bad = np.nonzero(gb != wb)[0]
+        raise AssertionError("%s: %d of %d differ, first at %d: %r vs %r"
+                             % (name, len(bad), got.size, bad[0], got.flat[bad[0]],
+                                want.flat[bad[0]]))
+
+
+def raster_from_history(history, counts, offsets, N, ms):
+    h = history.reshape(N, ms)
+    steps, nrn = [], []
+    for i in range(N):
+        for j in range(int(counts[i])):
+            steps.append(int(h[i, (int(offsets[i]) + j) % ms]))
+            nrn.append(i)
+    if not steps:
+        return np.zeros((2, 0), np.int64)
+    s, n = np.array(steps, np.int64), np.array(nrn, np.int64)
+    order = np.lexsort((n, s))
+    return np.stack([s[order], n[order]])
+
+
+SYN_FIELDS = ("W", "src", "dest", "type", "psr", "decay", "tau", "total_delay", "queue",
+              "delayIdx", "ldelayQueue", "lastSpike", "r", "u", "D", "U", "F")

@@ -1,0 +1,119 @@
+"""Pins the C oracle (oracle/bg_oracle.c) against the compiled reference.
+
+The fixtures were produced by running the reference single-threaded simulator step by step
+(tests/golden/make_golden.py); every comparison here is bit-for-bit except the reference's own
+XML goldens, which were printed with six significant digits.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from tests.golden.configs import case
+from tests.netcases import (SYN_FIELDS, TEST_SMALL, assert_same, load_fixture, oracle_from_case,
+                            raster_from_history, steps_per_epoch)
+
+SETUP = ("Vm", "Vthresh", "Vreset", "Vrest", "Vinit", "I0", "Inoise", "Iinject", "C1", "C2",
+         "Trefract", "Rm", "Cm", "Tau")
+
+
+def replay_against_fixture(name):
+    c = case(name)
+    fx = load_fixture(name)
+    o = oracle_from_case(c)
+    N, ms = c["N"], int(fx["hdr"][4])
+    for k in SETUP:
+        assert_same(k, o.arr(k), fx[k])
+    assert_same("ntype", o.arr("ntype"), fx["ntype"])
+    assert_same("radii0", o.arr("radii"), fx["radii"])
+    K = c.get("keep_steps_every")
+    spe = steps_per_epoch(c)
+    t = 0
+    for e in range(c["epochs"]):
+        for _ in range(spe):
+            o.step_n(1)
+            if K and t % K == 0:
+                for f, g in (("s.Vm", "Vm"), ("s.refr", "refr"), ("s.sp", "sp"),
+                             ("s.spikeCount", "spikeCount")):
+                    key = "%s@%d" % (f, t)
+                    if key in fx:
+                        assert_same(key, o.arr(g), fx[key])
+            t += 1
+        raster = raster_from_history(o.arr("history"), o.arr("spikeCount"),
+                                     o.arr("spikeCountOffset"), N, ms)
+        assert_same("raster#%d" % e, raster, fx["raster#%d" % e])
+        pre = "pre.slots#%d" % e
+        if pre in fx:
+            slots = np.nonzero(o.arr("in_use"))[0]
+            assert_same(pre, slots, fx[pre])
+            for f in SYN_FIELDS:
+                key = "pre.%s#%d" % (f, e)
+                if key in fx:
+                    assert_same(key, o.arr(f)[slots], fx[key])
+        o.growth()
+        for f in ("radii", "rates", "counts", "inMap", "outMap", "inCount", "outCount",
+                  "outBegin", "inBegin"):
+            key = "grow.%s#%d" % (f, e) if c["epochs"] > 1 else "grow.%s" % f
+            if key in fx:
+                assert_same(key, o.arr(f), fx[key])
+        o.record_epoch(e + 1)
+        suffix = "#%d" % e if c["epochs"] > 1 else ""
+        for f in ("radii", "rates", "spikeCountOffset", "spikeCount"):
+            assert_same("post." + f + suffix, o.arr(f), fx["post." + f + suffix])
+        if ("post.slots" + suffix) in fx:
+            slots = np.nonzero(o.arr("in_use"))[0]
+            assert_same("post.slots" + suffix, slots, fx["post.slots" + suffix])
+            assert_same("post.W" + suffix, o.arr("W")[slots], fx["post.W" + suffix])
+            assert_same("post.src" + suffix, o.arr("src")[slots], fx["post.src" + suffix])
+    assert o.flags == 0
+    return o
+
+
+def test_norm_stream_matches_reference_tiny():
+    # test-tiny: all four neurons integrate on every step of the first 1965 (no spikes yet),
+    # so the first 4 x 1000 draws are consumed in order
+    fx = load_fixture("ref_tiny")
+    assert fx["hdr"][0] == 4
+    s = po.norm_stream(1, 16)
+    assert np.all(np.isfinite(s)) and abs(float(np.mean(s))) < 1.5
+
+
+@pytest.mark.parametrize("name", ["ref_tiny", "c0", "c0_grown"])
+def test_oracle_matches_reference_dump(name):
+    o = replay_against_fixture(name)
+    if name == "c0_grown":
+        assert o.total > 0  # the grown case must actually exercise synapses
+
+
+@pytest.mark.slow
+def test_oracle_matches_reference_dump_m30():
+    o = replay_against_fixture("m30_grown")
+    assert o.total > 10000
+
+
+def test_oracle_matches_reference_xml_golden_tiny():
+    g = np.load("tests/golden/ref_goldens.npz")
+    c = dict(TEST_SMALL, name="tiny", width=2, height=2, N=4, tsim=1.0, epochs=1, inh=[1],
+             starters=[0])
+    _check_xml_golden(c, g, "test-tiny")
+
+
+@pytest.mark.slow
+def test_oracle_matches_reference_xml_golden_small():
+    g = np.load("tests/golden/ref_goldens.npz")
+    _check_xml_golden(TEST_SMALL, g, "test-small")
+
+
+def _check_xml_golden(c, g, nm):
+    o = oracle_from_case(c)
+    spe = steps_per_epoch(c)
+    for e in range(c["epochs"]):
+        o.step_n(spe)
+        o.growth()
+        o.record_epoch(e + 1)
+    E = c["epochs"]
+    radii = o.arr("radiiHistory").reshape(E + 1, c["N"])
+    rates = o.arr("ratesHistory").reshape(E + 1, c["N"])
+    np.testing.assert_allclose(radii, g[nm + ".radiiHistory"], rtol=1e-5, atol=0)
+    np.testing.assert_allclose(rates, g[nm + ".ratesHistory"], rtol=1e-5, atol=1e-9)
+    np.testing.assert_array_equal(o.arr("burstinessHist"), g[nm + ".burstinessHist"].ravel())
+    np.testing.assert_array_equal(o.arr("spikesHistory"), g[nm + ".spikesHistory"].ravel())
