@@ -1,0 +1,277 @@
+// Per-epoch ConnGrowth pass and recorder, on the device.
+//
+//   k_growth_radii     rates = spikeCount / T; radii += T * rho * outgrowth      (O(N))
+//   k_growth_existing  W of every in-use synapse from the overlap area of its pair (O(S))
+//   k_growth_add       one CTA per destination scans all sources in ascending order, computes the
+//                      frontier distance / overlap area, and appends the new synapses in source
+//                      order after the row's in-use prefix                      (O(N^2), no N^2
+//                                                                                storage)
+//   k_out_count/scan/fill  outgoing CSR rebuild (createSynapseImap)
+//   k_record_epoch     recorder histograms, rates/radii history, radius clamp, spike-count roll
+#include "bg3_internal.cuh"
+
+namespace bg3 {
+
+// ConnGrowth::updateConns (Connections/ConnGrowth.cpp:295-311).
+__global__ void k_growth_radii(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n.N) return;
+    float T = n.epoch_duration;
+    float rate = (float)n.spikeCount[i] / T;
+    n.rates[i] = rate;
+    float e = exp_cr((n.g_epsilon - rate / n.g_max_rate) / n.g_beta);
+    float og = 1.0f - 2.0f / (e + 1.0f);
+    float trho = T * n.g_rho;
+    n.radii[i] = n.radii[i] + trho * og;
+}
+
+// Frontier distance and overlap area of the pair (i = source, j = dest)
+// (Connections/ConnGrowth.cpp:319-376; dist from Layouts/Layout.cpp:54-69).  Returns 0 for pairs
+// that do not overlap.  Double where the reference promotes (2.0 * r * len, 2.0 * angle, 0.5 *).
+__device__ __forceinline__ float pair_area(float xi, float yi, float ri, float xj, float yj,
+                                           float rj)
+{
+    float dx = xi - xj, dy = yi - yj;
+    float len2 = dx * dx + dy * dy;
+    float len = sqrtf(len2);
+    float delta = len - (ri + rj);
+    if (!(delta < 0.0f)) return 0.0f;
+    float rmin = fminf(ri, rj), rmax = fmaxf(ri, rj);
+    if (len + rmin <= rmax) {
+        const float pi = 3.1415926536f;  // Utils/Global.cpp:90
+        return pi * rmin * rmin;
+    }
+    float r12 = ri * ri, r22 = rj * rj;
+    float cosCBA = (float)((double)(r22 + len2 - r12) / (2.0 * (double)rj * (double)len));
+    float angCBA = acos_cr(cosCBA);
+    float angCBD = (float)(2.0 * (double)angCBA);
+    float cosCAB = (float)((double)(r12 + len2 - r22) / (2.0 * (double)ri * (double)len));
+    float angCAB = acos_cr(cosCAB);
+    float angCAD = (float)(2.0 * (double)angCAB);
+    return (float)(0.5 * (double)(r22 * (angCBD - sin_cr(angCBD)) + r12 * (angCAD - sin_cr(angCAD))));
+}
+
+// Layout::synType (Layouts/Layout.cpp:129-140): II 0, IE 1, EI 2, EE 3.
+__device__ __forceinline__ int syn_type(int8_t ts, int8_t td)
+{
+    return (ts == 1) ? ((td == 1) ? 0 : 1) : ((td == 1) ? 2 : 3);
+}
+__device__ __forceinline__ float syn_sign(int type) { return (type <= 1) ? -1.0f : 1.0f; }
+
+// Weight update of existing synapses (ConnGrowth.cpp:420-438):
+// W = area * synSign(type) * SYNAPSE_STRENGTH_ADJUSTMENT (1.0e-8).
+__global__ void k_growth_existing(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    size_t total = (size_t)n.N * n.max_syn;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
+         p += (size_t)gridDim.x * blockDim.x) {
+        int d = (int)(p % n.N), k = (int)(p / n.N);
+        if (k >= (int)n.count[d]) continue;
+        int s = n.src[p];
+        float a = pair_area(n.xloc[s], n.yloc[s], n.radii[s], n.xloc[d], n.yloc[d], n.radii[d]);
+        if (a < 0.0f) set_err(n, 1u << 4);  // the reference would erase (never: area >= 0)
+        n.W[p] = a * syn_sign(n.stype[p]) * 1.0e-8f;
+    }
+}
+
+// New synapses (ConnGrowth.cpp:441-454, AllSynapses::addSynapse :357-377, create* of
+// AllSpikingSynapses.cpp:192-240 / AllDSSynapses.cpp:180-218).  One CTA per destination.
+constexpr int ADD_THREADS = 256;
+__global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    extern __shared__ uint32_t existing[];  // N bits
+    __shared__ int warp_cnt[ADD_THREADS / 32];
+    __shared__ int s_count;
+    const int d = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int words = (n.N + 31) / 32;
+    for (int w = threadIdx.x; w < words; w += blockDim.x) existing[w] = 0u;
+    if (threadIdx.x == 0) s_count = (int)n.count[d];
+    __syncthreads();
+    const int c0 = s_count;
+    for (int k = threadIdx.x; k < c0; k += blockDim.x) {
+        int s = n.src[(size_t)k * n.N + d];
+        atomicOr(&existing[s >> 5], 1u << (s & 31));
+    }
+    __syncthreads();
+    const float xd = n.xloc[d], yd = n.yloc[d], rd = n.radii[d];
+    const int8_t td = n.ntype[d];
+    const unsigned long long t = *n.step;
+    for (int base = 0; base < n.N; base += ADD_THREADS) {
+        int s = base + threadIdx.x;
+        float a = 0.0f;
+        bool add = false;
+        if (s < n.N && s != d && !((existing[s >> 5] >> (s & 31)) & 1u)) {
+            a = pair_area(n.xloc[s], n.yloc[s], n.radii[s], xd, yd, rd);
+            add = a > 0.0f;
+        }
+        unsigned m = __ballot_sync(0xffffffffu, add);
+        if (lane == 0) warp_cnt[warp] = __popc(m);
+        __syncthreads();
+        int before = 0, tot = 0;
+#pragma unroll
+        for (int w = 0; w < ADD_THREADS / 32; w++) {
+            int c = warp_cnt[w];
+            if (w < warp) before += c;
+            tot += c;
+        }
+        int cur = s_count;
+        if (add) {
+            int k = cur + before + __popc(m & ((1u << lane) - 1));
+            if (k < n.max_syn) {
+                size_t p = (size_t)k * n.N + d;
+                int type = syn_type(n.ntype[s], td);
+                n.src[p] = s;
+                n.stype[p] = (int8_t)type;
+                n.W[p] = a * syn_sign(type) * 1.0e-8f;
+                n.psr[p] = 0.0f;
+                n.decay[p] = n.t_decay[type];
+                n.queue[p] = 0u;
+                n.phase0[p] = (uint8_t)(t & 31u);
+                n.sdelay[p] = (uint8_t)n.t_delay[type];
+                n.u[p] = n.t_u0;
+                n.r[p] = n.t_r0;
+                n.lastSpike[p] = BG3_ULONG_MAX;
+                n.U[p] = n.t_U[type];
+                n.D[p] = n.t_D[type];
+                n.F[p] = n.t_F[type];
+            } else {
+                set_err(n, 1u << 2);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_count = min(cur + tot, n.max_syn);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) n.count[d] = (uint32_t)s_count;
+}
+
+// ---- outgoing map (AllSynapses::createSynapseImap, Synapses/AllSynapses.cpp:223-293) ---------
+__global__ void k_out_zero(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n.N; i += gridDim.x * blockDim.x) {
+        n.outCount[i] = 0u;
+        n.outFill[i] = 0u;
+    }
+}
+__global__ void k_out_count(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    size_t total = (size_t)n.N * n.max_syn;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
+         p += (size_t)gridDim.x * blockDim.x) {
+        int d = (int)(p % n.N), k = (int)(p / n.N);
+        if (k < (int)n.count[d]) atomicAdd(&n.outCount[n.src[p]], 1u);
+    }
+}
+// exclusive scan of outCount into outBegin; one CTA of 1024 threads walks N in chunks
+__global__ void __launch_bounds__(1024) k_out_scan(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b = 0; b < n.N; b += 1024) {
+        int i = b + threadIdx.x;
+        uint32_t v = (i < n.N) ? n.outCount[i] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = wsum[lane], z = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            wsum[lane] = z - w;
+        }
+        __syncthreads();
+        uint32_t c = carry;
+        if (i < n.N) n.outBegin[i] = c + wsum[warp] + x - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c + wsum[31] + x;
+        __syncthreads();
+    }
+}
+__global__ void k_out_fill(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    size_t total = (size_t)n.N * n.max_syn;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
+         p += (size_t)gridDim.x * blockDim.x) {
+        int d = (int)(p % n.N), k = (int)(p / n.N);
+        if (k >= (int)n.count[d]) continue;
+        int s = n.src[p];
+        uint32_t slot = n.outBegin[s] + atomicAdd(&n.outFill[s], 1u);
+        uint32_t dly = (uint32_t)n.sdelay[p];
+        n.outMap[slot] = (uint32_t)p | (dly << BG3_DELAY_SHIFT);
+    }
+}
+
+// ---- recorder (Recorders/XmlRecorder.cpp:71-104, XmlGrowthRecorder.cpp:72-97,
+//      Neurons/AllSpikingNeurons.cpp:77-86) ----------------------------------------------------
+__global__ void k_record_epoch(const NetDev *nets, int epoch)
+{
+    const NetDev &n = nets[0];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n.N) return;
+    const int ms = n.max_spikes;
+    const unsigned long long *h = n.history + (size_t)i * ms;
+    int cnt = n.spikeCount[i], off = n.spikeCountOffset[i];
+    for (int k = 0, idx = off; k < cnt; k++, idx++) {
+        if (idx >= ms) idx = 0;
+        int b1 = (int)((double)h[idx] * (double)n.dt);
+        int b2 = (int)((double)h[idx] * (double)n.dt * 100.0);
+        if (b1 >= 0 && b1 < n.n_burst_bins) atomicAdd(&n.burstiness[b1], 1.0f);
+        if (b2 >= 0 && b2 < n.n_spike_bins) atomicAdd(&n.spikes_hist[b2], 1.0f);
+    }
+    if (epoch >= 0 && epoch <= n.max_epochs) {
+        n.rates_hist[(size_t)epoch * n.N + i] = n.rates[i];
+        float r = n.radii[i];
+        if (r < n.g_min_radius) r = n.g_min_radius;
+        n.radii[i] = r;
+        n.radii_hist[(size_t)epoch * n.N + i] = r;
+    }
+    n.spikeCountOffset[i] = (cnt + off) % ms;
+    n.spikeCount[i] = 0;
+}
+
+void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s)
+{
+    int nb = (h.N + 255) / 256;
+    k_growth_radii<<<nb, 256, 0, s>>>(d_net);
+    int sb = 152 * 8;
+    k_growth_existing<<<sb, 256, 0, s>>>(d_net);
+    size_t smem = (size_t)((h.N + 31) / 32) * sizeof(uint32_t);
+    k_growth_add<<<h.N, ADD_THREADS, smem, s>>>(d_net);
+    k_out_zero<<<nb, 256, 0, s>>>(d_net);
+    k_out_count<<<sb, 256, 0, s>>>(d_net);
+    k_out_scan<<<1, 1024, 0, s>>>(d_net);
+    k_out_fill<<<sb, 256, 0, s>>>(d_net);
+    k_record_epoch<<<nb, 256, 0, s>>>(d_net, epoch);
+}
+
+void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s)
+{
+    int nb = (h.N + 255) / 256;
+    int sb = 152 * 8;
+    k_out_zero<<<nb, 256, 0, s>>>(d_net);
+    k_out_count<<<sb, 256, 0, s>>>(d_net);
+    k_out_scan<<<1, 1024, 0, s>>>(d_net);
+    k_out_fill<<<sb, 256, 0, s>>>(d_net);
+}
+
+}  // namespace bg3

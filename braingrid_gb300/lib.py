@@ -1,0 +1,325 @@
+"""ctypes binding of libbg3 (include/bg3.h) and a thin host-side network handle.
+
+The product path is the CUDA library; this module only marshals numpy arrays across the C-ABI.
+There is no CPU fallback: importing works without a GPU, but creating a network raises if the
+library or a CUDA device is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+c_f32p = ctypes.POINTER(ctypes.c_float)
+c_i32p = ctypes.POINTER(ctypes.c_int32)
+c_u32p = ctypes.POINTER(ctypes.c_uint32)
+c_u64p = ctypes.POINTER(ctypes.c_uint64)
+c_u8p = ctypes.POINTER(ctypes.c_uint8)
+
+BG3_NEURON_LIF, BG3_NEURON_IZH = 0, 1
+BG3_SYN_SPIKING, BG3_SYN_DS, BG3_SYN_STDP, BG3_SYN_DYNSTDP = 0, 1, 2, 3
+BG3_NOISE_DEVICE, BG3_NOISE_INJECT = 0, 1
+ERR_BITS = {1: "history overflow", 2: "double spike in a queue slot", 4: "synapse row full",
+            8: "injected noise exhausted", 16: "negative growth weight"}
+
+
+class NetDesc(ctypes.Structure):
+    _fields_ = [("n_neurons", ctypes.c_int32), ("max_syn_per_neuron", ctypes.c_int32),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("epoch_duration", ctypes.c_float), ("delta_t", ctypes.c_float),
+                ("max_firing_rate", ctypes.c_int32), ("max_epochs", ctypes.c_int32),
+                ("neuron_kind", ctypes.c_int32), ("synapse_kind", ctypes.c_int32),
+                ("noise_mode", ctypes.c_int32), ("noise_seed", ctypes.c_uint32)]
+
+
+class LifArrays(ctypes.Structure):
+    _fields_ = [(k, c_f32p) for k in ("Vm", "Vthresh", "Vreset", "I0", "Inoise", "C1", "C2",
+                                      "Trefract", "summation")] + \
+               [(k, c_i32p) for k in ("nStepsInRefr", "spikeCount", "spikeCountOffset")] + \
+               [("history", c_u64p)]
+
+
+class SynArrays(ctypes.Structure):
+    _fields_ = [("in_use", c_u8p)] + \
+               [(k, c_i32p) for k in ("src", "type", "delayIdx", "total_delay")] + \
+               [(k, c_f32p) for k in ("W", "psr", "decay", "tau")] + \
+               [(k, c_u32p) for k in ("delayQueue", "counts")] + \
+               [(k, c_f32p) for k in ("U", "D", "F", "u", "r")] + \
+               [("lastSpike", c_u64p)]
+
+
+class TypeConstants(ctypes.Structure):
+    _fields_ = [("tau", ctypes.c_float * 4), ("decay", ctypes.c_float * 4),
+                ("total_delay", ctypes.c_int32 * 4), ("U", ctypes.c_float * 4),
+                ("D", ctypes.c_float * 4), ("F", ctypes.c_float * 4),
+                ("u0", ctypes.c_float), ("r0", ctypes.c_float)]
+
+
+class GrowthParams(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_float) for k in ("epsilon", "beta", "rho", "target_rate",
+                                              "min_radius", "start_radius", "max_rate")]
+
+
+class IndexMaps(ctypes.Structure):
+    _fields_ = [(k, c_u32p) for k in ("outgoingSynapseIndexMap", "outgoingSynapseBegin",
+                                      "outgoingSynapseCount", "incomingSynapseIndexMap",
+                                      "incomingSynapseBegin", "incomingSynapseCount")]
+
+
+_LIB = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libbg3.so (building it first if absent).  Raises if it cannot be loaded."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("libbg3.so is not built; run braingrid_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    sig = {
+        "bg3_create": ([ctypes.POINTER(NetDesc), ctypes.POINTER(vp)], ctypes.c_int),
+        "bg3_destroy": ([vp], ctypes.c_int),
+        "bg3_upload_lif": ([vp, ctypes.POINTER(LifArrays)], ctypes.c_int),
+        "bg3_upload_layout": ([vp, c_f32p, c_f32p, c_i32p], ctypes.c_int),
+        "bg3_upload_synapses": ([vp, ctypes.POINTER(SynArrays), ctypes.c_uint64], ctypes.c_int),
+        "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
+        "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
+        "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
+        "bg3_upload_weights": ([vp, c_f32p], ctypes.c_int),
+        "bg3_step": ([vp, ctypes.c_int64], ctypes.c_int),
+        "bg3_epoch_growth": ([vp, ctypes.c_int32], ctypes.c_int),
+        "bg3_sync": ([vp], ctypes.c_int),
+        "bg3_get_step": ([vp, c_u64p], ctypes.c_int),
+        "bg3_error_word": ([vp, c_u32p], ctypes.c_int),
+        "bg3_download_lif": ([vp, ctypes.POINTER(LifArrays)], ctypes.c_int),
+        "bg3_download_synapses": ([vp, ctypes.POINTER(SynArrays)], ctypes.c_int),
+        "bg3_total_synapses": ([vp], ctypes.c_int64),
+        "bg3_download_maps": ([vp, ctypes.POINTER(IndexMaps)], ctypes.c_int),
+        "bg3_download_growth": ([vp, c_f32p, c_f32p], ctypes.c_int),
+        "bg3_download_histories": ([vp, c_f32p, c_f32p, c_f32p, c_f32p], ctypes.c_int),
+        "bg3_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "bg3_enable_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "bg3_kernel_times": ([vp, c_f32p, c_f32p, c_f32p, ctypes.POINTER(ctypes.c_int64)],
+                             ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = L
+    return L
+
+
+class Bg3Error(RuntimeError):
+    pass
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = load().bg3_status_string(rc).decode()
+        raise Bg3Error("%s failed: %s (%d)" % (what, msg, rc))
+
+
+def ptr(a, ctype):
+    if a is None:
+        return ctypes.cast(None, ctypes.POINTER(ctype))
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+_CT = {np.float32: ctypes.c_float, np.int32: ctypes.c_int32, np.uint32: ctypes.c_uint32,
+       np.uint64: ctypes.c_uint64, np.uint8: ctypes.c_uint8}
+
+
+def _p(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(_CT[a.dtype.type]))
+
+
+LIF_FIELDS = [("Vm", np.float32), ("Vthresh", np.float32), ("Vreset", np.float32),
+              ("I0", np.float32), ("Inoise", np.float32), ("C1", np.float32), ("C2", np.float32),
+              ("Trefract", np.float32), ("summation", np.float32), ("nStepsInRefr", np.int32),
+              ("spikeCount", np.int32), ("spikeCountOffset", np.int32)]
+SYN_FIELDS = [("in_use", np.uint8), ("src", np.int32), ("type", np.int32),
+              ("delayIdx", np.int32), ("total_delay", np.int32), ("W", np.float32),
+              ("psr", np.float32), ("decay", np.float32), ("tau", np.float32),
+              ("delayQueue", np.uint32), ("U", np.float32), ("D", np.float32),
+              ("F", np.float32), ("u", np.float32), ("r", np.float32), ("lastSpike", np.uint64)]
+
+
+class Network:
+    """One network on the GPU, driven through the C-ABI."""
+
+    def __init__(self, n_neurons, max_syn, width, height, epoch_duration, delta_t=1e-4,
+                 max_firing_rate=200, max_epochs=1, synapse_kind=BG3_SYN_DS,
+                 noise_mode=BG3_NOISE_DEVICE, noise_seed=1, neuron_kind=BG3_NEURON_LIF):
+        self.L = load()
+        self.desc = NetDesc(n_neurons, max_syn, width, height, epoch_duration, delta_t,
+                            max_firing_rate, max_epochs, neuron_kind, synapse_kind, noise_mode,
+                            noise_seed)
+        self.N, self.max_syn = n_neurons, max_syn
+        self.max_spikes = int(np.float32(epoch_duration) * np.float32(max_firing_rate))
+        self.max_epochs = max_epochs
+        self.epoch_duration = epoch_duration
+        h = ctypes.c_void_p()
+        check(self.L.bg3_create(ctypes.byref(self.desc), ctypes.byref(h)), "bg3_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.bg3_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # uploads
+    def upload_lif(self, **arrs):
+        keep = {}
+        s = LifArrays()
+        for k, dt in LIF_FIELDS:
+            if k in arrs and arrs[k] is not None:
+                keep[k] = np.ascontiguousarray(arrs[k], dtype=dt)
+                setattr(s, k, _p(keep[k]))
+        if arrs.get("history") is not None:
+            keep["history"] = np.ascontiguousarray(arrs["history"], dtype=np.uint64)
+            s.history = _p(keep["history"])
+        check(self.L.bg3_upload_lif(self.h, ctypes.byref(s)), "bg3_upload_lif")
+
+    def upload_layout(self, xloc, yloc, ntype):
+        x = np.ascontiguousarray(xloc, np.float32)
+        y = np.ascontiguousarray(yloc, np.float32)
+        t = np.ascontiguousarray(ntype, np.int32)
+        check(self.L.bg3_upload_layout(self.h, _p(x), _p(y), _p(t)), "bg3_upload_layout")
+
+    def upload_synapses(self, step, counts=None, **arrs):
+        keep = {}
+        s = SynArrays()
+        for k, dt in SYN_FIELDS:
+            if k in arrs and arrs[k] is not None:
+                keep[k] = np.ascontiguousarray(arrs[k], dtype=dt)
+                setattr(s, k, _p(keep[k]))
+        if counts is not None:
+            keep["counts"] = np.ascontiguousarray(counts, np.uint32)
+            s.counts = _p(keep["counts"])
+        check(self.L.bg3_upload_synapses(self.h, ctypes.byref(s), int(step)),
+              "bg3_upload_synapses")
+
+    def upload_growth(self, epsilon, beta, rho, target_rate, min_radius, start_radius, radii,
+                      rates=None):
+        g = GrowthParams(epsilon, beta, rho, target_rate, min_radius, start_radius,
+                         np.float32(target_rate) / np.float32(epsilon))
+        r = np.ascontiguousarray(radii, np.float32)
+        q = np.ascontiguousarray(rates if rates is not None else np.zeros(self.N), np.float32)
+        check(self.L.bg3_upload_growth(self.h, ctypes.byref(g), _p(r), _p(q)), "bg3_upload_growth")
+
+    def upload_weights(self, W):
+        w = np.ascontiguousarray(W, np.float32)
+        assert w.size == self.N * self.max_syn
+        check(self.L.bg3_upload_weights(self.h, _p(w)), "bg3_upload_weights")
+
+    def push_noise(self, values):
+        v = np.ascontiguousarray(values, np.float32)
+        check(self.L.bg3_push_noise(self.h, _p(v), len(v)), "bg3_push_noise")
+
+    # hot path
+    def step(self, n=1):
+        check(self.L.bg3_step(self.h, int(n)), "bg3_step")
+
+    def growth(self, epoch):
+        check(self.L.bg3_epoch_growth(self.h, int(epoch)), "bg3_epoch_growth")
+
+    def sync(self):
+        check(self.L.bg3_sync(self.h), "bg3_sync")
+
+    # downloads
+    @property
+    def sim_step(self):
+        v = ctypes.c_uint64()
+        check(self.L.bg3_get_step(self.h, ctypes.byref(v)), "bg3_get_step")
+        return v.value
+
+    @property
+    def error_word(self):
+        v = ctypes.c_uint32()
+        check(self.L.bg3_error_word(self.h, ctypes.byref(v)), "bg3_error_word")
+        return v.value
+
+    def download_lif(self):
+        out = {k: np.zeros(self.N, dt) for k, dt in LIF_FIELDS}
+        out["history"] = np.zeros(self.N * self.max_spikes, np.uint64)
+        s = LifArrays()
+        for k, _ in LIF_FIELDS:
+            setattr(s, k, _p(out[k]))
+        s.history = _p(out["history"])
+        check(self.L.bg3_download_lif(self.h, ctypes.byref(s)), "bg3_download_lif")
+        return out
+
+    def download_synapses(self):
+        S = self.N * self.max_syn
+        out = {k: np.zeros(S, dt) for k, dt in SYN_FIELDS}
+        out["counts"] = np.zeros(self.N, np.uint32)
+        s = SynArrays()
+        for k, _ in SYN_FIELDS:
+            setattr(s, k, _p(out[k]))
+        s.counts = _p(out["counts"])
+        check(self.L.bg3_download_synapses(self.h, ctypes.byref(s)), "bg3_download_synapses")
+        return out
+
+    def total_synapses(self):
+        v = self.L.bg3_total_synapses(self.h)
+        if v < 0:
+            check(int(v), "bg3_total_synapses")
+        return int(v)
+
+    def download_maps(self):
+        T = self.total_synapses()
+        out = {k: np.zeros(max(T, 1) if k.endswith("IndexMap") else self.N, np.uint32)
+               for k, _ in IndexMaps._fields_}
+        m = IndexMaps(*[_p(out[k]) for k, _ in IndexMaps._fields_])
+        check(self.L.bg3_download_maps(self.h, ctypes.byref(m)), "bg3_download_maps")
+        for k in out:
+            if k.endswith("IndexMap"):
+                out[k] = out[k][:T]
+        return out
+
+    def download_growth(self):
+        r = np.zeros(self.N, np.float32)
+        q = np.zeros(self.N, np.float32)
+        check(self.L.bg3_download_growth(self.h, _p(r), _p(q)), "bg3_download_growth")
+        return r, q
+
+    def download_histories(self):
+        nb = int(np.float32(self.max_epochs) * np.float32(self.epoch_duration))
+        ns = int(np.float32(self.max_epochs) * np.float32(self.epoch_duration) * np.float32(100))
+        b = np.zeros(max(nb, 1), np.float32)
+        s = np.zeros(max(ns, 1), np.float32)
+        rh = np.zeros((self.max_epochs + 1) * self.N, np.float32)
+        ra = np.zeros((self.max_epochs + 1) * self.N, np.float32)
+        check(self.L.bg3_download_histories(self.h, _p(b), _p(s), _p(rh), _p(ra)),
+              "bg3_download_histories")
+        return b[:nb], s[:ns], rh, ra
+
+    def enable_timing(self, on=True):
+        check(self.L.bg3_enable_timing(self.h, 1 if on else 0), "bg3_enable_timing")
+
+    def kernel_times(self):
+        a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+        n = ctypes.c_int64()
+        check(self.L.bg3_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                      ctypes.byref(n)), "bg3_kernel_times")
+        return a.value, b.value, c.value, n.value

@@ -1,0 +1,189 @@
+/* bg3 — GB300-native BrainGrid spiking-network hot path: the C-ABI boundary (libbg3.so).
+ *
+ * Every entry point takes plain pointers and sizes.  Arrays passed in or out are HOST arrays in
+ * the reference's own layouts (neuron-indexed SoA; synapse slots iSyn = dest * maxSyn + k as in
+ * Synapses/AllSynapses.cpp:367), so a reference-side shim can hand its host objects over without
+ * reshaping them.  Device layouts are private to the library.
+ *
+ * The reference calls these through its model and class interfaces; each declaration names the
+ * reference interface it replaces (paths relative to the reference project root).
+ *
+ * Status convention: every function returns an int; 0 is success, negative values are the
+ * BG3_E* codes below (the reference instead exit()s through HANDLE_ERROR).  bg3_status_string()
+ * turns a code into text.  A sticky device error word (bg3_error_word) reports conditions the
+ * reference would assert on (a spike-history ring overflow, a double spike in one delay-queue
+ * slot, a synapse row that would exceed maxSynapsesPerNeuron).
+ *
+ * Threading: calls on one handle must not overlap; different handles are independent.  Each
+ * handle owns one CUDA stream; every call is ordered on it and returns without a device sync
+ * unless it copies data back to the host.
+ */
+#ifndef BG3_H
+#define BG3_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    BG3_OK = 0,
+    BG3_EINVAL = -1,      /* bad argument or state                                        */
+    BG3_ENOMEM = -2,      /* device allocation failed                                     */
+    BG3_ECUDA = -3,       /* a CUDA call failed                                           */
+    BG3_ENOISE = -4,      /* injected noise stream ran out                                */
+    BG3_EDEVICE = -5,     /* the device error word is set (see bg3_error_word)            */
+    BG3_EUNSUPPORTED = -6 /* model combination not built                                  */
+};
+
+/* device error word bits */
+enum {
+    BG3_ERR_HISTORY_OVERFLOW = 1u << 0, /* spikeCount reached maxSpikes (AllSpikingNeurons.cpp:114) */
+    BG3_ERR_QUEUE_DOUBLE = 1u << 1,     /* preSpikeHit on a set bit (AllSpikingSynapses.cpp:277)    */
+    BG3_ERR_ROW_FULL = 1u << 2,         /* growth wanted a synapse in a full row (AllSynapses.cpp:360) */
+    BG3_ERR_NOISE_EXHAUSTED = 1u << 3,  /* injected noise stream shorter than needed                */
+    BG3_ERR_NEGATIVE_AREA = 1u << 4,    /* growth saw a negative weight (the reference would erase) */
+    BG3_ERR_SPIKE_LIST = 1u << 5        /* more spikes in one step than neurons (internal check)    */
+};
+
+enum { BG3_NEURON_LIF = 0, BG3_NEURON_IZH = 1 };
+enum { BG3_SYN_SPIKING = 0, BG3_SYN_DS = 1, BG3_SYN_STDP = 2, BG3_SYN_DYNSTDP = 3 };
+/* Noise source.  DEVICE: a counter-based generator keyed by (seed, step, neuron), one draw per
+ * neuron per step like the reference GPU path (Core/GPUSpikingModel.cu:194).  INJECT: values
+ * pushed by the host with bg3_push_noise, consumed in the reference CPU order (one value per
+ * integrating neuron, descending neuron index; Neurons/AllSpikingNeurons.cpp:104 and
+ * Neurons/AllLIFNeurons.cpp:40). */
+enum { BG3_NOISE_DEVICE = 0, BG3_NOISE_INJECT = 1 };
+
+typedef struct bg3_net bg3_net;
+
+/* Network shape; fields mirror SimulationInfo (Core/SimulationInfo.h:92-116). */
+typedef struct {
+    int32_t n_neurons;            /* totalNeurons                                      */
+    int32_t max_syn_per_neuron;   /* maxSynapsesPerNeuron                              */
+    int32_t width, height;        /* PoolSize x, y                                     */
+    float epoch_duration;         /* Tsim (s)                                          */
+    float delta_t;                /* deltaT (s)                                        */
+    int32_t max_firing_rate;      /* maxFiringRate (Hz); ring = epoch * rate            */
+    int32_t max_epochs;           /* numSims; sizes the recorder histories             */
+    int32_t neuron_kind;          /* BG3_NEURON_*                                      */
+    int32_t synapse_kind;         /* BG3_SYN_*                                         */
+    int32_t noise_mode;           /* BG3_NOISE_*                                       */
+    uint32_t noise_seed;          /* seed of the device generator                      */
+} bg3_net_desc;
+
+/* LIF neuron arrays, each n_neurons long (Neurons/AllIFNeurons.h:279-362,
+ * Neurons/AllSpikingNeurons.h:181-204).  history: n_neurons x max_spikes uint64, row-major;
+ * it may be NULL on upload (all ULONG_MAX). */
+typedef struct {
+    float *Vm, *Vthresh, *Vreset, *I0, *Inoise, *C1, *C2, *Trefract, *summation;
+    int32_t *nStepsInRefr, *spikeCount, *spikeCountOffset;
+    uint64_t *history;
+} bg3_lif_arrays;
+
+/* Synapse slot arrays in the reference layout, n_neurons * max_syn_per_neuron long
+ * (Synapses/AllSynapses.h:188-232, AllSpikingSynapses.h:342-355, AllDSSynapses.h:269-336).
+ * in_use uses one byte per slot; counts is n_neurons long (synapse_counts).  On upload the
+ * in-use slots of every row must form a prefix (what AllSynapses::addSynapse produces when no
+ * synapse was ever erased).  DS fields may be NULL for BG3_SYN_SPIKING. */
+typedef struct {
+    uint8_t *in_use;
+    int32_t *src, *type, *delayIdx, *total_delay;
+    float *W, *psr, *decay, *tau;
+    uint32_t *delayQueue, *counts;
+    float *U, *D, *F, *u, *r;
+    uint64_t *lastSpike;
+} bg3_synapse_arrays;
+
+/* Synapse constants per synapse type II, IE, EI, EE (Utils/Global.h:100), as the reference's
+ * createSynapse computes them on the host (Synapses/AllSpikingSynapses.cpp:192-240,
+ * AllDSSynapses.cpp:180-218).  Used for synapses the device growth pass creates. */
+typedef struct {
+    float tau[4], decay[4];
+    int32_t total_delay[4];
+    float U[4], D[4], F[4];
+    float u0, r0;
+} bg3_type_constants;
+
+/* ConnGrowth parameters (Connections/ConnGrowth.h, m_growth) and the layout it needs. */
+typedef struct {
+    float epsilon, beta, rho, target_rate, min_radius, start_radius, max_rate;
+} bg3_growth_params;
+
+/* Outgoing / incoming maps in the reference order (Core/SynapseIndexMap.h:38-104); each
+ * *_map holds total entries (bg3_total_synapses), the others n_neurons. */
+typedef struct {
+    uint32_t *outgoingSynapseIndexMap, *outgoingSynapseBegin, *outgoingSynapseCount;
+    uint32_t *incomingSynapseIndexMap, *incomingSynapseBegin, *incomingSynapseCount;
+} bg3_index_maps;
+
+/* ---- lifetime -------------------------------------------------------------------------- */
+/* Replaces GPUSpikingModel::setupSim's device allocation (Core/GPUSpikingModel.cu:106-160,
+ * IAllNeurons::allocNeuronDeviceStruct Neurons/IAllNeurons.h:98, IAllSynapses::
+ * allocSynapseDeviceStruct Synapses/IAllSynapses.h:134). */
+int bg3_create(const bg3_net_desc *desc, bg3_net **out);
+/* Replaces GPUSpikingModel::cleanupSim / delete*DeviceStruct (Core/GPUSpikingModel.cu:82-99). */
+int bg3_destroy(bg3_net *net);
+
+/* ---- host -> device ------------------------------------------------------------------- */
+/* IAllNeurons::copyNeuronHostToDevice (Neurons/IAllNeurons.h:114). */
+int bg3_upload_lif(bg3_net *net, const bg3_lif_arrays *a);
+/* Layout arrays (Layouts/Layout.h: xloc, yloc, neuron_type_map as INH=1 / EXC=2). */
+int bg3_upload_layout(bg3_net *net, const float *xloc, const float *yloc, const int32_t *ntype);
+/* IAllSynapses::copySynapseHostToDevice (Synapses/IAllSynapses.h:160) plus the index-map copy of
+ * GPUSpikingModel::copySynapseIndexMapHostToDevice (Core/GPUSpikingModel.cu:326); the maps are
+ * rebuilt on the device.  current_step is g_simulationStep (Utils/Global.h:85). */
+int bg3_upload_synapses(bg3_net *net, const bg3_synapse_arrays *a, uint64_t current_step);
+int bg3_set_type_constants(bg3_net *net, const bg3_type_constants *c);
+/* ConnGrowth state (radii, rates) and parameters (Connections/ConnGrowth.h:219+). */
+int bg3_upload_growth(bg3_net *net, const bg3_growth_params *p, const float *radii,
+                      const float *rates);
+/* Sets W of every in-use slot from a reference-layout array (n_neurons * max_syn_per_neuron),
+ * the weight upload of the reference's GPU growth path (Connections/ConnGrowth_d.cu:37-45). */
+int bg3_upload_weights(bg3_net *net, const float *W);
+/* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
+int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
+
+/* ---- hot path ------------------------------------------------------------------------- */
+/* nsteps of GPUSpikingModel::advance (Core/GPUSpikingModel.cu:188-230): neuron integration,
+ * spike propagation into the delay queues, synapse sweep with summation; g_simulationStep
+ * advances by nsteps. */
+int bg3_step(bg3_net *net, int64_t nsteps);
+/* GPUSpikingModel::updateConnections (Core/GPUSpikingModel.cu:246-258: ConnGrowth::
+ * updateConns / updateFrontiers / updateOverlap, ConnGrowth_d.cu:18-61 weights and rewiring,
+ * createSynapseImap) followed by updateHistory (:266, XmlGrowthRecorder::compileHistories:
+ * histograms, rates/radii history, radius clamp, spike-count roll).  epoch is the 1-based
+ * epoch number (SimulationInfo::currentStep). */
+int bg3_epoch_growth(bg3_net *net, int32_t epoch);
+
+/* ---- device -> host ------------------------------------------------------------------- */
+int bg3_sync(bg3_net *net);
+int bg3_get_step(bg3_net *net, uint64_t *step);
+int bg3_error_word(bg3_net *net, uint32_t *err);
+/* IAllNeurons::copyNeuronDeviceToHost (Neurons/IAllNeurons.h:122); history included. */
+int bg3_download_lif(bg3_net *net, bg3_lif_arrays *a);
+/* IAllSynapses::copySynapseDeviceToHost (Synapses/IAllSynapses.h:177), reference layout, with
+ * delayIdx and delayQueue in the reference's per-synapse phase. */
+int bg3_download_synapses(bg3_net *net, bg3_synapse_arrays *a);
+int64_t bg3_total_synapses(bg3_net *net);
+int bg3_download_maps(bg3_net *net, bg3_index_maps *m);
+int bg3_download_growth(bg3_net *net, float *radii, float *rates);
+/* XmlRecorder / XmlGrowthRecorder histories (Recorders/XmlRecorder.cpp:71-104,
+ * XmlGrowthRecorder.cpp:72-97): burstiness (epochs*Tsim bins), spikes (100 per second),
+ * rates and radii ((max_epochs+1) x n_neurons). */
+int bg3_download_histories(bg3_net *net, float *burstiness, float *spikes, float *rates_hist,
+                           float *radii_hist);
+
+/* ---- diagnostics ---------------------------------------------------------------------- */
+const char *bg3_status_string(int status);
+/* Per-launch timing of the last bg3_step call's kernels: fills up to n entries of
+ * (kernel id, milliseconds) measured with CUDA events on the handle's stream when enabled. */
+int bg3_enable_timing(bg3_net *net, int on);
+int bg3_kernel_times(bg3_net *net, float *ms_neurons, float *ms_fanout, float *ms_sweep,
+                     int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -524,38 +524,41 @@ static int syn_type(const bgo_net *n, int src, int dest)
     return si ? (di ? BGO_II : BGO_IE) : (di ? BGO_EI : BGO_EE);
 }
 
-/* ConnGrowth::updateSynapsesWeights, CPU variant (Connections/ConnGrowth.cpp:388-463). */
+/* ConnGrowth::updateSynapsesWeights, CPU variant (Connections/ConnGrowth.cpp:388-463).
+ * The reference walks src (outer) x dest (inner) and, for each pair, scans the dest row for a
+ * synapse from src.  Every action on a pair touches only the dest row, so walking dest (outer) x
+ * src (inner, ascending) performs the same actions in the same per-row order; a src -> slot table
+ * of the row replaces the row scan (rows hold at most one synapse per source). */
 static void update_weights(bgo_net *n)
 {
     const float adj = (float)1.0e-8; /* AllSynapses::SYNAPSE_STRENGTH_ADJUSTMENT */
-    for (int s = 0; s < n->N; s++) {
-        for (int d = 0; d < n->N; d++) {
+    long *slot_of = malloc((size_t)(n->N > 0 ? n->N : 1) * sizeof(long));
+    for (int s = 0; s < n->N; s++) slot_of[s] = -1;
+    for (int d = 0; d < n->N; d++) {
+        uint32_t cnt = n->counts[d], seen = 0;
+        for (size_t iSyn = (size_t)n->max_syn * d; seen < cnt; iSyn++)
+            if (n->in_use[iSyn]) { slot_of[n->src[iSyn]] = (long)iSyn; seen++; }
+        for (int s = 0; s < n->N; s++) {
             float w = pair_area(n, s, d);
             int type = syn_type(n, s, d);
             int sign = (type == BGO_II || type == BGO_IE) ? -1 : 1;
-            int connected = 0;
-            uint32_t cnt = n->counts[d], seen = 0;
-            size_t iSyn = (size_t)n->max_syn * d;
-            for (; seen < cnt; iSyn++) {
-                if (n->in_use[iSyn]) {
-                    if (n->src[iSyn] == s) {
-                        connected = 1;
-                        if (w < 0) {
-                            n->counts[d]--;
-                            n->in_use[iSyn] = 0;
-                        } else {
-                            n->W[iSyn] = w * (float)sign * adj;
-                        }
-                    }
-                    seen++;
+            long iSyn = slot_of[s];
+            if (iSyn >= 0) {
+                if (w < 0) {
+                    n->counts[d]--;
+                    n->in_use[iSyn] = 0;
+                } else {
+                    n->W[iSyn] = w * (float)sign * adj;
                 }
-            }
-            if (!connected && w > 0) {
+            } else if (w > 0) {
                 long k = add_synapse(n, type, s, d);
                 if (k >= 0) n->W[k] = w * (float)sign * adj;
             }
         }
+        for (size_t iSyn = (size_t)n->max_syn * d; iSyn < (size_t)n->max_syn * (d + 1); iSyn++)
+            if (n->src[iSyn] >= 0 && n->src[iSyn] < n->N) slot_of[n->src[iSyn]] = -1;
     }
+    free(slot_of);
 }
 
 void bgo_growth(bgo_net *n)

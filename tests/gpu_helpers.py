@@ -1,0 +1,70 @@
+"""Copy an oracle network onto the GPU through the C-ABI and compare the two states."""
+import numpy as np
+
+from braingrid_gb300 import lib as bg
+from oracle import pyoracle as po
+from tests.netcases import assert_same
+
+LIF_MAP = [("Vm", "Vm"), ("Vthresh", "Vthresh"), ("Vreset", "Vreset"), ("I0", "I0"),
+           ("Inoise", "Inoise"), ("C1", "C1"), ("C2", "C2"), ("Trefract", "Trefract"),
+           ("summation", "sp"), ("nStepsInRefr", "refr"), ("spikeCount", "spikeCount"),
+           ("spikeCountOffset", "spikeCountOffset")]
+SYN_MAP = [("in_use", "in_use"), ("src", "src"), ("type", "type"), ("delayIdx", "delayIdx"),
+           ("total_delay", "total_delay"), ("W", "W"), ("psr", "psr"), ("decay", "decay"),
+           ("delayQueue", "queue"), ("U", "U"), ("D", "D"), ("F", "F"), ("u", "u"), ("r", "r"),
+           ("lastSpike", "lastSpike")]
+
+
+def gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_INJECT, n_noise=0, noise_seed=None):
+    net = bg.Network(c["N"], c["max_syn"], c["width"], c["height"], c["tsim"], 1e-4,
+                     c["max_firing_rate"], c["epochs"], bg.BG3_SYN_DS, noise_mode,
+                     noise_seed if noise_seed is not None else c["seed"])
+    net.upload_layout(o.arr("xloc"), o.arr("yloc"), o.arr("ntype"))
+    kw = {k: o.arr(v) for k, v in LIF_MAP}
+    kw["history"] = o.arr("history")
+    net.upload_lif(**kw)
+    skw = {k: o.arr(v) for k, v in SYN_MAP}
+    net.upload_synapses(o.step, counts=o.arr("counts"), **skw)
+    g = c["growth"]
+    net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
+                      g["start_radius"], o.arr("radii"), o.arr("rates"))
+    if noise_mode == bg.BG3_NOISE_INJECT and n_noise:
+        net.push_noise(po.norm_stream(c["seed"], n_noise))
+    return net
+
+
+def compare_neurons(net, o, where, fields=("Vm", "summation", "nStepsInRefr", "spikeCount",
+                                           "spikeCountOffset")):
+    g = net.download_lif()
+    m = dict(LIF_MAP)
+    for f in fields:
+        assert_same("%s %s" % (where, f), g[f], o.arr(m[f]))
+    return g
+
+
+def compare_history(net, o, where):
+    g = net.download_lif()
+    assert_same(where + " history", g["history"], o.arr("history"))
+
+
+def compare_synapses(net, o, where, tol_fields=()):
+    g = net.download_synapses()
+    used = o.arr("in_use").astype(bool)
+    assert_same(where + " in_use", g["in_use"], o.arr("in_use"))
+    assert_same(where + " counts", g["counts"], o.arr("counts"))
+    for k, v in SYN_MAP[1:]:
+        a, b = g[k][used], o.arr(v)[used]
+        if k in tol_fields:
+            np.testing.assert_allclose(a, b, rtol=1e-5, atol=0, err_msg=where + " " + k)
+        else:
+            assert_same("%s %s" % (where, k), a, b)
+    return g
+
+
+def compare_maps(net, o, where):
+    m = net.download_maps()
+    assert_same(where + " outMap", m["outgoingSynapseIndexMap"], o.arr("outMap"))
+    assert_same(where + " outBegin", m["outgoingSynapseBegin"], o.arr("outBegin"))
+    assert_same(where + " outCount", m["outgoingSynapseCount"], o.arr("outCount"))
+    assert_same(where + " inMap", m["incomingSynapseIndexMap"], o.arr("inMap"))
+    assert_same(where + " inCount", m["incomingSynapseCount"], o.arr("inCount"))
