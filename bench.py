@@ -1,0 +1,320 @@
+"""Benchmark of the spiking hot path on one GB300: synapse-updates/s (and neuron-steps/s).
+
+Workload (config[1] of the stated benchmark): the plain single-network step of a 100x100 = 10,000
+neuron LIF + AllDSSynapses + ConnGrowth network, max 1,000 synapses per neuron, dt 0.1 ms,
+excitatory fraction 0.90, targetRate 1.0 Hz, seed 7, synthetic parameters with the config's
+value distributions (braingrid_gb300.netgen).  Connectivity is pre-grown (at the stated 0.4 start
+radius no pair overlaps, so no synapse would ever form): radii ~ U[8.35, 8.45] and one device
+growth pass wire every overlapping pair (~7.6 M synapses, up to ~930 per neuron); weights =
+overlap area x 1e-8 x a fixed scale.  A "step" is one simulation time step (neurons, spike
+propagation, synapse sweep with summation) of the whole network.  L2 is flushed (256 MiB write)
+before every timed step; device time per step comes from CUDA events on the library's stream.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bg3|reference]
+
+--impl reference times the reference algorithm's CPU path (the C restatement in oracle/, the
+reference's own sources are not on the GPU host) on the same network, single-threaded as the
+reference is.  Under torchrun every rank runs an independent replica (the path does not shard);
+value is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from braingrid_gb300.workloads import C1  # noqa: E402
+
+WIDTH, HEIGHT, MAX_SYN = C1["width"], C1["height"], C1["max_syn"]
+RADIUS, WEIGHT_SCALE, SEED = C1["radius"], C1["weight_scale"], C1["seed"]
+FLUSH_BYTES = 256 << 20
+METRIC = "synapse-updates/s"
+SWEEP_BYTES_PER_SYN = 28     # DS quiet path: psr, decay, queue, delayIdx read; psr, queue, delayIdx written
+EVENT_BYTES = 48             # per delivered spike: W, U, D, F, u, r, lastSpike read; u, r, lastSpike written
+SP_BYTES = 4                 # summation point write per neuron
+DEVICE_BYTES_PER_SYN = 16    # what the plane layout actually moves: psr r/w, decay, queue
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile(prefix="bg3clk", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_network():
+    from braingrid_gb300 import workloads
+    return workloads.build(workloads.C1)
+
+
+def traffic_per_launch(S):
+    """DRAM bytes per sweep launch from the committed ncu capture, scaled by synapse count."""
+    p = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return float(d["dram_bytes_per_launch"]) * S / float(d["synapses"])
+
+
+def cpu_baseline_port(net, spec, budget_s=12.0):
+    """Time the oracle (reference algorithm, C, one core) on the same network state."""
+    from oracle import pyoracle as po
+    from braingrid_gb300 import lib as bg
+    N = spec["N"]
+    o = po.OracleNet(N, MAX_SYN, WIDTH, HEIGHT, 1.0, 1e-4, 200, 10)
+    g = net.download_lif()
+    s = net.download_synapses()
+    for k, v in (("Vm", "Vm"), ("Vthresh", "Vthresh"), ("Vreset", "Vreset"), ("I0", "I0"),
+                 ("Inoise", "Inoise"), ("C1", "C1"), ("C2", "C2"), ("Trefract", "Trefract"),
+                 ("sp", "summation"), ("refr", "nStepsInRefr"), ("spikeCount", "spikeCount"),
+                 ("spikeCountOffset", "spikeCountOffset")):
+        o.arr(k)[:] = g[v]
+    o.arr("history")[:] = g["history"]
+    for k, v in (("in_use", "in_use"), ("src", "src"), ("type", "type"), ("W", "W"),
+                 ("psr", "psr"), ("decay", "decay"), ("total_delay", "total_delay"),
+                 ("queue", "delayQueue"), ("delayIdx", "delayIdx"), ("U", "U"), ("D", "D"),
+                 ("F", "F"), ("u", "u"), ("r", "r"), ("lastSpike", "lastSpike")):
+        o.arr(k)[:] = s[v]
+    o.arr("ldelayQueue")[:] = 32
+    o.arr("counts")[:] = s["counts"]
+    o.arr("ntype")[:] = spec["ntype"]
+    o.step = net.sim_step
+    o.rebuild_maps()
+    S = o.total
+    t0 = time.perf_counter()
+    o.step_n(1)
+    one = time.perf_counter() - t0
+    n = max(1, min(400, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    o.step_n(n)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": S * n / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": "%d steps of the same %d-neuron / %d-synapse network (oracle C port, one "
+                      "thread; host has %d cores)" % (n, N, S, os.cpu_count() or 0),
+            "neuron_steps_per_s": N * n / dt}
+
+
+def run_bg3(args):
+    rank, world, local = dist_env()
+    import torch  # plumbing: device selection, pinned host buffers, barrier for N>1
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from braingrid_gb300 import lib as bg
+    spec, net = build_network()
+    N = spec["N"]
+    S = net.total_synapses()
+    # warm-up
+    net.bench_steps(args.warmup, FLUSH_BYTES)
+    c0 = net.download_lif(fields=("spikeCount",))["spikeCount"].astype(np.int64)
+    maps = net.download_maps()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local) if rank == 0 else None
+    ms = net.bench_steps(args.steps, FLUSH_BYTES)
+    torch.cuda.synchronize()
+    clocks = clk.stop() if clk else None
+    if world > 1:
+        dist.barrier()
+    c1 = net.download_lif(fields=("spikeCount",))["spikeCount"].astype(np.int64)
+    t_total = float(np.sum(ms)) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    deliveries = float(((c1 - c0) * maps["outgoingSynapseCount"].astype(np.int64)).sum()) / args.steps
+    rate_hz = float((c1 - c0).mean()) / (args.steps * 1e-4)
+    value = S * args.steps * world / t_total
+    # roofline of the dominant kernel (the sweep), per-kernel events
+    nk = min(args.steps, 300)
+    _, km = net.bench_steps(nk, FLUSH_BYTES, per_kernel=True)
+    sweep_ms = float(np.mean(km[:, 2]))
+    shares = np.sum(km, axis=0) / np.sum(km)
+    peak, peak_kind = peaks()
+    alg_bytes = SWEEP_BYTES_PER_SYN * S + EVENT_BYTES * deliveries + SP_BYTES * N
+    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    dev_achieved = (DEVICE_BYTES_PER_SYN * S + EVENT_BYTES * deliveries + SP_BYTES * N) / (sweep_ms * 1e-3) / 1e9
+    # end to end through the C-ABI with pinned host buffers: every iteration uploads the neuron
+    # state (H2D), advances E2E_STEPS steps and reads back the spike counts and history (D2H)
+    E2E_STEPS = 500
+    e2e_iters = max(2, min(10, args.steps // 100))
+    pin = {}
+    st = net.download_lif()
+    for k in ("Vm", "Vthresh", "Vreset", "I0", "Inoise", "C1", "C2", "Trefract", "summation",
+              "nStepsInRefr", "spikeCount", "spikeCountOffset"):
+        t = torch.empty(N, dtype=torch.float32 if st[k].dtype == np.float32 else torch.int32,
+                        pin_memory=True)
+        t.numpy()[:] = st[k]
+        pin[k] = t
+    out_counts = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+    h2d = sum(v.numel() * v.element_size() for v in pin.values())
+    d2h = N * 4
+    net.sync()
+    t0 = time.perf_counter()
+    for _ in range(e2e_iters):
+        net.upload_lif(**{k: v.numpy() for k, v in pin.items()})
+        net.step(E2E_STEPS)
+        net.download_lif(fields=("spikeCount",), out={"spikeCount": out_counts})
+    net.sync()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": S * E2E_STEPS * e2e_iters * world / e2e_s, "unit": METRIC,
+           "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS}
+    err = net.error_word
+    if rank == 0:
+        cpu = cpu_baseline_port(net, spec)
+        tr = traffic_per_launch(S)
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "config[1] plain single-network step: 100x100 LIF + DS + "
+                                   "ConnGrowth, max 1000 synapses/neuron, pre-grown radius "
+                                   "U[8.35,8.45], weight scale %g" % WEIGHT_SCALE,
+                       "neurons": N, "synapses": S, "dt_s": 1e-4, "noise": "device",
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "mean_rate_hz": rate_hz, "deliveries_per_step": deliveries,
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "neuron_steps_per_s": N * args.steps * world / t_total,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": tr, "kernel": "k_sweep",
+                         "peak_kind": peak_kind, "launch_ms": sweep_ms,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "device_layout_achieved": dev_achieved,
+                         "device_layout_frac": dev_achieved / peak,
+                         "kernel_shares": {"neurons": float(shares[0]), "fanout": float(shares[1]),
+                                           "sweep": float(shares[2])}},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks,
+            "error_word": err,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference algorithm's CPU path (oracle C port), single-threaded like the reference."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from braingrid_gb300 import netgen
+    from oracle import pyoracle as po
+    spec = netgen.lif_network(WIDTH, HEIGHT, frac_inh=0.10, seed=SEED)
+    N = spec["N"]
+    o = po.OracleNet(N, MAX_SYN, WIDTH, HEIGHT, 1.0, 1e-4, 200, 10)
+    for k in ("xloc", "yloc", "ntype", "Vm", "Vthresh", "Vreset", "I0", "Inoise", "C1", "C2",
+              "Trefract"):
+        o.arr(k)[:] = spec[k]
+    o.growth_init(0.60, 0.10, 1e-4, 1.0, 0.1, 0.4)
+    rs = np.random.RandomState(11)
+    o.arr("radii")[:] = rs.uniform(RADIUS - 0.05, RADIUS + 0.05, N).astype(np.float32)
+    o.seed_noise(SEED)
+    o.growth()
+    o.arr("W")[:] = o.arr("W") * np.float32(WEIGHT_SCALE)
+    S = o.total
+    o.step_n(max(1, min(args.warmup, 3)))
+    # each timed "step" is one full simulation step; the sample is capped at ~60 s of CPU time
+    t0 = time.perf_counter()
+    o.step_n(1)
+    one = time.perf_counter() - t0
+    k = max(1, min(args.steps, int(60.0 / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    o.step_n(k)
+    dt = time.perf_counter() - t0
+    value = S * k / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
+            "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": dt * 1e3 / k,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "config[1] plain single-network step: 100x100 LIF + DS + "
+                                   "ConnGrowth, max 1000 synapses/neuron, pre-grown radius "
+                                   "U[8.35,8.45], weight scale %g" % WEIGHT_SCALE,
+                       "neurons": N, "synapses": S},
+            "neuron_steps_per_s": N * k / dt,
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": "%d of %d requested steps (capped at ~60 s), one thread; "
+                                       "host has %d cores" % (k, args.steps, os.cpu_count() or 0)},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    o.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="bg3", choices=["bg3", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_bg3(args)
+
+
+if __name__ == "__main__":
+    main()

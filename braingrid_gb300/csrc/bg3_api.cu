@@ -29,6 +29,8 @@ struct bg3_net {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float ms_neurons = 0, ms_fanout = 0, ms_sweep = 0;
     long long launches = 0;
+    void *flush_buf = nullptr;
+    size_t flush_size = 0;
 };
 
 #define CK(x)                                                                            \
@@ -178,6 +180,7 @@ int bg3_destroy(bg3_net *n)
     for (void *p : n->allocs) cudaFree(p);
     if (n->d) cudaFree(n->d);
     if (n->noise_dev) cudaFree(n->noise_dev);
+    if (n->flush_buf) cudaFree(n->flush_buf);
     for (int i = 0; i < 4; i++)
         if (n->ev[i]) cudaEventDestroy(n->ev[i]);
     if (n->stream) cudaStreamDestroy(n->stream);
@@ -578,6 +581,48 @@ int bg3_download_histories(bg3_net *n, float *burst, float *spikes, float *rh, f
         (rc = d2h(n, rh, h.rates_hist, rows)) || (rc = d2h(n, radh, h.radii_hist, rows)))
         return rc;
     CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step_ms,
+                    float *kernel_ms)
+{
+    if (!n || nsteps < 0 || !step_ms) return BG3_EINVAL;
+    if (flush_bytes > 0 && (size_t)flush_bytes > n->flush_size) {
+        if (n->flush_buf) cudaFree(n->flush_buf);
+        n->flush_buf = nullptr;
+        n->flush_size = 0;
+        if (cudaMalloc(&n->flush_buf, (size_t)flush_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return BG3_ENOMEM;
+        }
+        n->flush_size = (size_t)flush_bytes;
+    }
+    const int per = kernel_ms ? 4 : 2;
+    std::vector<cudaEvent_t> ev((size_t)nsteps * per);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (int64_t s = 0; s < nsteps; s++) {
+        if (flush_bytes > 0)
+            CK(cudaMemsetAsync(n->flush_buf, (int)(s & 0xff), (size_t)flush_bytes, n->stream));
+        cudaEvent_t *e = &ev[(size_t)s * per];
+        if (kernel_ms) {
+            bg3::launch_step_parts(n->h, n->d, n->stream, e);
+        } else {
+            CK(cudaEventRecord(e[0], n->stream));
+            bg3::launch_step(n->h, n->d, n->stream);
+            CK(cudaEventRecord(e[1], n->stream));
+        }
+    }
+    n->launches += 3 * nsteps;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(n->stream));
+    for (int64_t s = 0; s < nsteps; s++) {
+        cudaEvent_t *e = &ev[(size_t)s * per];
+        CK(cudaEventElapsedTime(&step_ms[s], e[0], e[per - 1]));
+        if (kernel_ms)
+            for (int k = 0; k < 3; k++) CK(cudaEventElapsedTime(&kernel_ms[3 * s + k], e[k], e[k + 1]));
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
     return BG3_OK;
 }
 

@@ -109,6 +109,7 @@ def load(build_if_missing=True):
         "bg3_download_histories": ([vp, c_f32p, c_f32p, c_f32p, c_f32p], ctypes.c_int),
         "bg3_status_string": ([ctypes.c_int], ctypes.c_char_p),
         "bg3_enable_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "bg3_bench_steps": ([vp, ctypes.c_int64, ctypes.c_int64, c_f32p, c_f32p], ctypes.c_int),
         "bg3_kernel_times": ([vp, c_f32p, c_f32p, c_f32p, ctypes.POINTER(ctypes.c_int64)],
                              ctypes.c_int),
     }
@@ -259,13 +260,23 @@ class Network:
         check(self.L.bg3_error_word(self.h, ctypes.byref(v)), "bg3_error_word")
         return v.value
 
-    def download_lif(self):
-        out = {k: np.zeros(self.N, dt) for k, dt in LIF_FIELDS}
-        out["history"] = np.zeros(self.N * self.max_spikes, np.uint64)
+    def download_lif(self, fields=None, out=None):
+        """Neuron state; fields limits the copy to the named arrays (plus 'history'), out may
+        supply destination arrays (e.g. pinned host buffers)."""
+        want = [k for k, _ in LIF_FIELDS] + ["history"] if fields is None else list(fields)
+        res = dict(out or {})
+        for k, dt in LIF_FIELDS:
+            if k in want and k not in res:
+                res[k] = np.zeros(self.N, dt)
+        if "history" in want and "history" not in res:
+            res["history"] = np.zeros(self.N * self.max_spikes, np.uint64)
+        out = res
         s = LifArrays()
         for k, _ in LIF_FIELDS:
-            setattr(s, k, _p(out[k]))
-        s.history = _p(out["history"])
+            if k in out:
+                setattr(s, k, _p(out[k]))
+        if "history" in out:
+            s.history = _p(out["history"])
         check(self.L.bg3_download_lif(self.h, ctypes.byref(s)), "bg3_download_lif")
         return out
 
@@ -313,6 +324,15 @@ class Network:
         check(self.L.bg3_download_histories(self.h, _p(b), _p(s), _p(rh), _p(ra)),
               "bg3_download_histories")
         return b[:nb], s[:ns], rh, ra
+
+    def bench_steps(self, nsteps, flush_bytes=0, per_kernel=False):
+        """Device time (ms) of each of nsteps steps; with per_kernel also (nsteps, 3) kernel
+        times (neurons, fan-out, sweep)."""
+        ms = np.zeros(max(int(nsteps), 1), np.float32)
+        km = np.zeros(3 * max(int(nsteps), 1), np.float32) if per_kernel else None
+        check(self.L.bg3_bench_steps(self.h, int(nsteps), int(flush_bytes), _p(ms), _p(km)),
+              "bg3_bench_steps")
+        return (ms[:nsteps], km[:3 * nsteps].reshape(-1, 3)) if per_kernel else ms[:nsteps]
 
     def enable_timing(self, on=True):
         check(self.L.bg3_enable_timing(self.h, 1 if on else 0), "bg3_enable_timing")

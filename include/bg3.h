@@ -183,6 +183,14 @@ int bg3_enable_timing(bg3_net *net, int on);
 int bg3_kernel_times(bg3_net *net, float *ms_neurons, float *ms_fanout, float *ms_sweep,
                      int64_t *launches);
 
+/* Benchmark helper: runs nsteps steps on the handle's stream.  Before each step, when
+ * flush_bytes > 0, a scratch buffer of that size is overwritten so that the step starts with a
+ * cold L2.  The device time of each step (CUDA events on the handle's stream, flush excluded) is
+ * written to step_ms[nsteps]; when kernel_ms is not NULL, the three kernels of each step are
+ * timed separately into kernel_ms[3 * nsteps] (neurons, fan-out, sweep). */
+int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *step_ms,
+                    float *kernel_ms);
+
 #ifdef __cplusplus
 }
 #endif
