@@ -6,8 +6,9 @@ excitatory fraction 0.90, targetRate 1.0 Hz, seed 7, synthetic parameters with t
 value distributions (braingrid_gb300.netgen).  Connectivity is pre-grown (at the stated 0.4 start
 radius no pair overlaps, so no synapse would ever form): radii ~ U[8.35, 8.45] and one device
 growth pass wire every overlapping pair (~7.6 M synapses, up to ~930 per neuron); weights =
-overlap area x 1e-8 x a fixed scale.  A "step" is one simulation time step (neurons, spike
-propagation, synapse sweep with summation) of the whole network.  L2 is flushed (256 MiB write)
+overlap area x 1e-8 x a fixed scale.  A "step" is one simulation time step of the whole network:
+one neuron pass, one spike-delivery pass and one synapse sweep with summation (the neuron pass
+of step t + 1 runs in the epilogue of sweep t; the first step's runs standalone).  L2 is flushed (256 MiB write)
 before every timed step; device time per step comes from CUDA events on the library's stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bg3|reference]
@@ -36,10 +37,14 @@ WIDTH, HEIGHT, MAX_SYN = C1["width"], C1["height"], C1["max_syn"]
 RADIUS, WEIGHT_SCALE, SEED = C1["radius"], C1["weight_scale"], C1["seed"]
 FLUSH_BYTES = 256 << 20
 METRIC = "synapse-updates/s"
-SWEEP_BYTES_PER_SYN = 28     # DS quiet path: psr, decay, queue, delayIdx read; psr, queue, delayIdx written
-EVENT_BYTES = 48             # per delivered spike: W, U, D, F, u, r, lastSpike read; u, r, lastSpike written
-SP_BYTES = 4                 # summation point write per neuron
-DEVICE_BYTES_PER_SYN = 16    # what the plane layout actually moves: psr r/w, decay, queue
+# Algorithmic bytes of the dominant kernel (k_sweep, with the next step's neuron pass fused in):
+# every in-use synapse's psr is read and written and its decay class (1 byte) read; every neuron
+# reads Vm, Vthresh, I0, Inoise, C1, C2, Trefract, refr and writes Vm, refr, sp (44 B, rounded
+# to 48 with the spike-ring entry).  The reference layout's per-synapse figure (psr, decay, queue
+# word, delay index read; psr, queue, delay index written: 28 B) is reported beside it.
+SWEEP_BYTES_PER_SYN = 9
+SWEEP_BYTES_PER_NEURON = 48
+SURVEY_BYTES_PER_SYN = 28
 
 
 def peaks():
@@ -189,9 +194,9 @@ def run_bg3(args):
     sweep_ms = float(np.mean(km[:, 2]))
     shares = np.sum(km, axis=0) / np.sum(km)
     peak, peak_kind = peaks()
-    alg_bytes = SWEEP_BYTES_PER_SYN * S + EVENT_BYTES * deliveries + SP_BYTES * N
+    alg_bytes = SWEEP_BYTES_PER_SYN * S + SWEEP_BYTES_PER_NEURON * N
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
-    dev_achieved = (DEVICE_BYTES_PER_SYN * S + EVENT_BYTES * deliveries + SP_BYTES * N) / (sweep_ms * 1e-3) / 1e9
+    survey_achieved = (SURVEY_BYTES_PER_SYN * S + 4 * N) / (sweep_ms * 1e-3) / 1e9
     # end to end through the C-ABI with pinned host buffers: every iteration uploads the neuron
     # state (H2D), advances E2E_STEPS steps and reads back the spike counts and history (D2H)
     E2E_STEPS = 500
@@ -238,13 +243,14 @@ def run_bg3(args):
                          "frac": achieved / peak, "traffic": tr, "kernel": "k_sweep",
                          "peak_kind": peak_kind, "launch_ms": sweep_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "device_layout_achieved": dev_achieved,
-                         "device_layout_frac": dev_achieved / peak,
-                         "kernel_shares": {"neurons": float(shares[0]), "fanout": float(shares[1]),
+                         "bytes_per_synapse": SWEEP_BYTES_PER_SYN,
+                         "reference_layout_bytes_per_synapse": SURVEY_BYTES_PER_SYN,
+                         "reference_layout_equivalent_gbs": survey_achieved,
+                         "kernel_shares": {"neurons": float(shares[0]), "deliver": float(shares[1]),
                                            "sweep": float(shares[2])}},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 2 * args.steps + 1,
             "clocks": clocks,
             "error_word": err,
         }

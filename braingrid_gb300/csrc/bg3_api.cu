@@ -1,21 +1,27 @@
-// C-ABI of libbg3: handle lifetime, host <-> device conversion between the reference's slot
-// layout and the device plane layout, and the launch sequence of a step and of an epoch.
+// C-ABI of libbg3: handle lifetime, conversion between the reference's slot layout and the
+// device plane layout, and the launch sequences of a step and of an epoch.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "../../include/bg3.h"
 #include "bg3_internal.cuh"
 
 namespace bg3 {
-void launch_step(const NetDev &h, const NetDev *d_net, cudaStream_t s);
-void launch_step_parts(const NetDev &h, const NetDev *d_net, cudaStream_t s, cudaEvent_t ev[4]);
+void launch_neurons(const NetDev &h, const NetDev *d_net, cudaStream_t s);
+void launch_deliver(const NetDev &h, const NetDev *d_net, cudaStream_t s);
+void launch_sweep(const NetDev &h, const NetDev *d_net, const CUtensorMap &tp,
+                  const CUtensorMap &tc, bool fuse, cudaStream_t s);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
 
+static const int GRAPH_STEPS = 32;  // fused steps captured per CUDA graph replay
 
 struct bg3_net {
     bg3_net_desc desc;
@@ -23,14 +29,18 @@ struct bg3_net {
     NetDev *d = nullptr;      // device copy
     cudaStream_t stream = nullptr;
     std::vector<void *> allocs;
-    long long noise_cap = 0;  // capacity of the injected-noise buffer (values)
+    CUtensorMap tm_psr, tm_cls;
+    std::vector<float> dtab;  // decay factor per decay class
+    std::vector<int> ltab;    // delay per delay class
+    long long noise_cap = 0;
     float *noise_dev = nullptr;
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float ms_neurons = 0, ms_fanout = 0, ms_sweep = 0;
     long long launches = 0;
-    void *flush_buf = nullptr;
+    void *flush_buf = nullptr, *scrub_buf = nullptr;
     size_t flush_size = 0;
+    cudaGraphExec_t graph = nullptr;
 };
 
 #define CK(x)                                                                            \
@@ -66,15 +76,80 @@ static int push_desc(bg3_net *n)
 template <typename T>
 static int h2d(bg3_net *n, T *dst, const T *src, size_t count)
 {
-    if (!src) return BG3_OK;
+    if (!src || !count) return BG3_OK;
     CK(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, n->stream));
     return BG3_OK;
 }
 template <typename T>
 static int d2h(bg3_net *n, T *dst, const T *src, size_t count)
 {
-    if (!dst) return BG3_OK;
+    if (!dst || !count) return BG3_OK;
     CK(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost, n->stream));
+    return BG3_OK;
+}
+
+static void drop_graph(bg3_net *n)
+{
+    if (n->graph) cudaGraphExecDestroy(n->graph);
+    n->graph = nullptr;
+}
+
+// decay / delay class tables (host copy is the source of truth; pushed on change)
+static int push_tables(bg3_net *n)
+{
+    n->h.n_dcls = (int)n->dtab.size();
+    n->h.n_delays = (int)n->ltab.size();
+    int rc;
+    if ((rc = h2d(n, n->h.dtab, n->dtab.data(), n->dtab.size())) ||
+        (rc = h2d(n, n->h.ltab, n->ltab.data(), n->ltab.size())))
+        return rc;
+    drop_graph(n);
+    return push_desc(n);
+}
+static int decay_class(bg3_net *n, float v)
+{
+    uint32_t b;
+    memcpy(&b, &v, 4);
+    for (size_t i = 0; i < n->dtab.size(); i++) {
+        uint32_t c;
+        memcpy(&c, &n->dtab[i], 4);
+        if (c == b) return (int)i;
+    }
+    if (n->dtab.size() >= BG3_MAX_DCLS) return -1;
+    n->dtab.push_back(v);
+    return (int)n->dtab.size() - 1;
+}
+static int delay_class(bg3_net *n, int D)
+{
+    for (size_t i = 0; i < n->ltab.size(); i++)
+        if (n->ltab[i] == D) return (int)i;
+    if (n->ltab.size() >= BG3_MAX_DELAYS || D < 1 || D > 31) return -1;
+    n->ltab.push_back(D);
+    return (int)n->ltab.size() - 1;
+}
+
+static int make_tensor_maps(bg3_net *n)
+{
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+        return BG3_ECUDA;
+    auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    const NetDev &h = n->h;
+    cuuint64_t dims[2] = {(cuuint64_t)h.N, (cuuint64_t)std::max(h.max_syn, 1)};
+    cuuint32_t box[2] = {32, 64};
+    cuuint32_t es[2] = {1, 1};
+    cuuint64_t st_f[1] = {(cuuint64_t)h.Np * 4};
+    cuuint64_t st_b[1] = {(cuuint64_t)h.Np};
+    if (encode(&n->tm_psr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, h.psr, dims, st_f, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return BG3_ECUDA;
+    if (encode(&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, h.dcls, dims, st_b, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return BG3_ECUDA;
     return BG3_OK;
 }
 
@@ -101,9 +176,10 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     const bg3_net_desc &D = *desc;
     if (D.n_neurons <= 0 || D.max_syn_per_neuron < 0 || D.delta_t <= 0 || D.epoch_duration <= 0)
         return BG3_EINVAL;
-    if ((size_t)D.n_neurons * (size_t)D.max_syn_per_neuron > (size_t)BG3_POS_MASK) return BG3_EINVAL;
+    if ((size_t)D.n_neurons * (size_t)D.max_syn_per_neuron >= (1ull << 32)) return BG3_EINVAL;
     if (D.neuron_kind != BG3_NEURON_LIF) return BG3_EUNSUPPORTED;
     if (D.synapse_kind != BG3_SYN_DS && D.synapse_kind != BG3_SYN_SPIKING) return BG3_EUNSUPPORTED;
+    if (D.noise_mode != BG3_NOISE_DEVICE && D.noise_mode != BG3_NOISE_INJECT) return BG3_EINVAL;
     int max_spikes = (int)(D.epoch_duration * (float)D.max_firing_rate);
     if (max_spikes <= 0) return BG3_EINVAL;
 
@@ -116,8 +192,11 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     }
     NetDev &h = n->h;
     memset(&h, 0, sizeof(h));
-    const size_t N = (size_t)D.n_neurons, S = N * (size_t)D.max_syn_per_neuron;
+    const size_t N = (size_t)D.n_neurons;
+    const size_t Np = (N + 31) / 32 * 32;
+    const size_t S = Np * (size_t)D.max_syn_per_neuron;
     h.N = D.n_neurons;
+    h.Np = (int)Np;
     h.max_syn = D.max_syn_per_neuron;
     h.max_spikes = max_spikes;
     h.neuron_kind = D.neuron_kind;
@@ -126,27 +205,28 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     h.noise_seed = D.noise_seed;
     h.dt = D.delta_t;
     h.epoch_duration = D.epoch_duration;
-    h.ntiles = (int)((N + 31) / 32);
+    h.ntiles = (int)(Np / 32);
     h.max_epochs = D.max_epochs;
     h.n_burst_bins = (int)((float)D.max_epochs * D.epoch_duration);
     h.n_spike_bins = (int)((float)D.max_epochs * D.epoch_duration * 100.0f);
     int rc = 0;
 #define A(ptr, cnt) if ((rc = dalloc(n, &h.ptr, (cnt))) != 0) goto fail;
-#define AF(ptr, cnt, f) if ((rc = dalloc(n, &h.ptr, (cnt), (f))) != 0) goto fail;
-    A(step, 1) A(sweep_done, 1) A(err, 1) A(nspikes, 1) A(noise_cursor, 1)
+    A(step, 1) A(sweep_done, 1) A(err, 1) A(noise_cursor, 1)
     A(Vm, N) A(Vthresh, N) A(Vreset, N) A(I0, N) A(Inoise, N) A(C1, N) A(C2, N) A(Trefract, N)
-    A(sp, N) A(refr, N) A(spikeCount, N) A(spikeCountOffset, N) A(ntype, N) A(spikes, N)
-    AF(history, N * (size_t)max_spikes, 0xff)
-    A(psr, S) A(decay, S) A(W, S) A(U, S) A(D, S) A(F, S) A(u, S) A(r, S) A(queue, S)
-    A(lastSpike, S) A(src, S) A(stype, S) A(phase0, S) A(sdelay, S) A(count, N)
-    A(outBegin, N) A(outCount, N) A(outMap, S) A(outFill, N)
+    A(sp, N) A(refr, N) A(spikeCount, N) A(spikeCountOffset, N) A(ntype, N)
+    A(ring, N * BG3_RING) A(ring_n, BG3_RING)
+    A(psr, S) A(dcls, S) A(lcls, S) A(ev, S) A(src, S) A(stype, S) A(count, N)
+    A(dtab, BG3_MAX_DCLS) A(ltab, BG3_MAX_DELAYS)
+    A(outBegin, N * BG3_MAX_DELAYS) A(outCount, N * BG3_MAX_DELAYS) A(outFill, N * BG3_MAX_DELAYS)
+    A(outMap, S)
     A(radii, N) A(rates, N) A(xloc, N) A(yloc, N)
     A(burstiness, (size_t)std::max(h.n_burst_bins, 1)) A(spikes_hist, (size_t)std::max(h.n_spike_bins, 1))
     A(rates_hist, (size_t)(D.max_epochs + 1) * N) A(radii_hist, (size_t)(D.max_epochs + 1) * N)
 #undef A
-#undef AF
+    if ((rc = dalloc(n, &h.history, N * (size_t)max_spikes, 0xff)) != 0) goto fail;
     if (cudaMalloc((void **)&n->d, sizeof(NetDev)) != cudaSuccess) { rc = BG3_ENOMEM; goto fail; }
-    // default type constants: tau, delay, U/D/F from createSynapse with this deltaT
+    // type constants of createSynapse at this deltaT (Synapses/AllSpikingSynapses.cpp:192-240,
+    // AllDSSynapses.cpp:180-218); decay = exp(-deltaT / tau) on the host, as the reference does
     {
         const float tau[4] = {6e-3f, 6e-3f, 3e-3f, 3e-3f};
         const float dly[4] = {0.8e-3f, 0.8e-3f, 0.8e-3f, 1.5e-3f};
@@ -154,8 +234,10 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
                     F[4] = {0.06f, 0.02f, 1.2f, 0.05f};
         for (int t = 0; t < 4; t++) {
             h.t_tau[t] = tau[t];
-            h.t_decay[t] = expf(-D.delta_t / tau[t]);
-            h.t_delay[t] = (int)(dly[t] / D.delta_t) + 1;
+            n->dtab.push_back(expf(-D.delta_t / tau[t]));
+            h.t_dcls[t] = t;
+            h.t_lcls[t] = delay_class(n, (int)(dly[t] / D.delta_t) + 1);
+            if (h.t_lcls[t] < 0) { rc = BG3_EINVAL; goto fail; }
             h.t_U[t] = U[t];
             h.t_D[t] = Dd[t];
             h.t_F[t] = F[t];
@@ -163,7 +245,8 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
         h.t_u0 = 0.4f;
         h.t_r0 = 1.0f;
     }
-    if ((rc = push_desc(n)) != 0) goto fail;
+    if ((rc = make_tensor_maps(n)) != 0) goto fail;
+    if ((rc = push_tables(n)) != 0) goto fail;
     if (cudaStreamSynchronize(n->stream) != cudaSuccess) { rc = BG3_ECUDA; goto fail; }
     *out = n;
     return BG3_OK;
@@ -177,10 +260,12 @@ int bg3_destroy(bg3_net *n)
 {
     if (!n) return BG3_EINVAL;
     if (n->stream) cudaStreamSynchronize(n->stream);
+    drop_graph(n);
     for (void *p : n->allocs) cudaFree(p);
     if (n->d) cudaFree(n->d);
     if (n->noise_dev) cudaFree(n->noise_dev);
     if (n->flush_buf) cudaFree(n->flush_buf);
+    if (n->scrub_buf) cudaFree(n->scrub_buf);
     for (int i = 0; i < 4; i++)
         if (n->ev[i]) cudaEventDestroy(n->ev[i]);
     if (n->stream) cudaStreamDestroy(n->stream);
@@ -189,7 +274,6 @@ int bg3_destroy(bg3_net *n)
 }
 
 // ---- uploads --------------------------------------------------------------------------------
-
 int bg3_upload_lif(bg3_net *n, const bg3_lif_arrays *a)
 {
     if (!n || !a) return BG3_EINVAL;
@@ -230,40 +314,47 @@ int bg3_set_type_constants(bg3_net *n, const bg3_type_constants *c)
 {
     if (!n || !c) return BG3_EINVAL;
     for (int t = 0; t < 4; t++) {
-        if (c->total_delay[t] < 1 || c->total_delay[t] > 31) return BG3_EINVAL;
+        int dc = decay_class(n, c->decay[t]);
+        int lc = delay_class(n, c->total_delay[t]);
+        if (dc < 0 || lc < 0) return BG3_EINVAL;
         n->h.t_tau[t] = c->tau[t];
-        n->h.t_decay[t] = c->decay[t];
-        n->h.t_delay[t] = c->total_delay[t];
+        n->h.t_dcls[t] = dc;
+        n->h.t_lcls[t] = lc;
         n->h.t_U[t] = c->U[t];
         n->h.t_D[t] = c->D[t];
         n->h.t_F[t] = c->F[t];
     }
     n->h.t_u0 = c->u0;
     n->h.t_r0 = c->r0;
-    int rc = push_desc(n);
+    int rc = push_tables(n);
     if (rc) return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
 }
 
-static inline uint32_t rotl32(uint32_t x, unsigned r) { r &= 31u; return r ? (x << r) | (x >> (32 - r)) : x; }
-static inline uint32_t rotr32(uint32_t x, unsigned r) { r &= 31u; return r ? (x >> r) | (x << (32 - r)) : x; }
-
+// Converts the reference's per-synapse delay queues into the device's spike ring and birth
+// steps.  Queue bit b of a synapse with read index di is checked (delivered) o = (b - di) & 31
+// steps from now, so its source fired at tf = step + o - D.  A synapse that lacks the bit of a
+// spike its source emitted while its queue would have recorded it did not exist yet: its birth
+// step is step - di (the reference's delayIdx counts steps since creation, mod 32).
 int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
 {
     if (!n || !a || !a->in_use || !a->src || !a->type || !a->W || !a->psr || !a->decay ||
         !a->delayQueue || !a->delayIdx || !a->total_delay)
         return BG3_EINVAL;
-    const size_t N = n->h.N, M = n->h.max_syn, S = N * M;
+    if (step >= 0xffffff00ull) return BG3_EINVAL;
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * M;
     const bool ds = n->h.syn_kind == BG3_SYN_DS;
     if (ds && (!a->U || !a->D || !a->F || !a->u || !a->r || !a->lastSpike)) return BG3_EINVAL;
-    std::vector<float> psr(S, 0.f), decay(S, 0.f), W(S, 0.f), U(S, 0.f), Dd(S, 0.f), F(S, 0.f),
-        u(S, 0.f), r(S, 0.f);
-    std::vector<uint32_t> queue(S, 0u), count(N, 0u);
-    std::vector<unsigned long long> last(S, BG3_ULONG_MAX);
+    std::vector<float> psr(S, 0.f);
+    std::vector<uint8_t> dc(S, 0), lc(S, 0);
+    std::vector<EvSlot> ev(S);
     std::vector<int32_t> src(S, 0);
     std::vector<int8_t> st(S, 0);
-    std::vector<uint8_t> ph(S, 0), dl(S, 0);
+    std::vector<uint32_t> count(N, 0u);
+    memset(ev.data(), 0, S * sizeof(EvSlot));
+    // fired[s] bit j: neuron s fired at step - 1 - j (j < 32), from the queues
+    std::vector<uint32_t> fired(N, 0u);
     for (size_t d = 0; d < N; d++) {
         size_t c = 0;
         while (c < M && a->in_use[d * M + c]) c++;
@@ -272,39 +363,72 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
         if (a->counts && a->counts[d] != c) return BG3_EINVAL;
         count[d] = (uint32_t)c;
         for (size_t k = 0; k < c; k++) {
-            size_t i = d * M + k, p = k * N + d;
+            size_t i = d * M + k, p = k * Np + d;
+            int D = a->total_delay[i], di = a->delayIdx[i];
             if (a->src[i] < 0 || (size_t)a->src[i] >= N || a->type[i] < 0 || a->type[i] > 3 ||
-                a->total_delay[i] < 1 || a->total_delay[i] > 31 || a->delayIdx[i] < 0 ||
-                a->delayIdx[i] > 31)
+                D < 1 || D > 31 || di < 0 || di > 31)
                 return BG3_EINVAL;
-            unsigned phase = (unsigned)((step - (uint64_t)a->delayIdx[i]) & 31u);
+            int dcl = decay_class(n, a->decay[i]), lcl = delay_class(n, D);
+            if (dcl < 0 || lcl < 0) return BG3_EINVAL;
             psr[p] = a->psr[i];
-            decay[p] = a->decay[i];
-            W[p] = a->W[i];
-            queue[p] = rotl32(a->delayQueue[i], phase);
+            dc[p] = (uint8_t)dcl;
+            lc[p] = (uint8_t)lcl;
             src[p] = a->src[i];
             st[p] = (int8_t)a->type[i];
-            ph[p] = (uint8_t)phase;
-            dl[p] = (uint8_t)a->total_delay[i];
+            EvSlot &e = ev[p];
+            e.W = a->W[i];
+            e.born = (uint32_t)(step - (uint64_t)di - 32u);
             if (ds) {
-                U[p] = a->U[i]; Dd[p] = a->D[i]; F[p] = a->F[i]; u[p] = a->u[i]; r[p] = a->r[i];
-                last[p] = a->lastSpike[i];
+                e.U = a->U[i]; e.D = a->D[i]; e.F = a->F[i]; e.u = a->u[i]; e.r = a->r[i];
+                uint64_t ls = a->lastSpike[i];
+                if (ls != BG3_ULONG_MAX && ls >= BG3_NO_SPIKE32) return BG3_EINVAL;
+                e.last = (ls == BG3_ULONG_MAX) ? BG3_NO_SPIKE32 : (uint32_t)ls;
+            } else {
+                e.last = BG3_NO_SPIKE32;
+            }
+            uint32_t q = a->delayQueue[i];
+            for (int b = 0; b < 32; b++) {
+                if (!((q >> b) & 1u)) continue;
+                int o = (b - di) & 31;
+                if (o >= D || (uint64_t)(D - o) > step) return BG3_EINVAL;  // not a past spike
+                fired[a->src[i]] |= 1u << (D - o - 1);
             }
         }
     }
+    for (size_t d = 0; d < N; d++) {
+        for (size_t k = 0; k < count[d]; k++) {
+            size_t i = d * M + k, p = k * Np + d;
+            int D = a->total_delay[i], di = a->delayIdx[i];
+            uint32_t f = fired[a->src[i]], q = a->delayQueue[i];
+            for (int j = 0; j < D; j++) {
+                if (!((f >> j) & 1u)) continue;
+                int o = D - 1 - j;  // pending spike from step - 1 - j, due in o steps
+                if ((q >> ((di + o) & 31)) & 1u) continue;
+                // missing: the synapse was created after that spike (step - di > step - 1 - j)
+                if (di > j) return BG3_EINVAL;
+                ev[p].born = (uint32_t)(step - (uint64_t)di);
+            }
+        }
+    }
+    std::vector<int32_t> ring(N * BG3_RING, 0), ring_n(BG3_RING, 0);
+    for (size_t s = 0; s < N; s++)
+        for (int j = 0; j < 32; j++)
+            if ((fired[s] >> j) & 1u) {
+                int slot = (int)((step - 1 - (uint64_t)j) & (BG3_RING - 1));
+                ring[(size_t)slot * N + ring_n[slot]++] = (int32_t)s;
+            }
     NetDev &h = n->h;
     int rc;
-    if ((rc = h2d(n, h.psr, psr.data(), S)) || (rc = h2d(n, h.decay, decay.data(), S)) ||
-        (rc = h2d(n, h.W, W.data(), S)) || (rc = h2d(n, h.U, U.data(), S)) ||
-        (rc = h2d(n, h.D, Dd.data(), S)) || (rc = h2d(n, h.F, F.data(), S)) ||
-        (rc = h2d(n, h.u, u.data(), S)) || (rc = h2d(n, h.r, r.data(), S)) ||
-        (rc = h2d(n, h.queue, queue.data(), S)) || (rc = h2d(n, h.lastSpike, last.data(), S)) ||
+    if ((rc = push_tables(n))) return rc;
+    if ((rc = h2d(n, h.psr, psr.data(), S)) || (rc = h2d(n, h.dcls, dc.data(), S)) ||
+        (rc = h2d(n, h.lcls, lc.data(), S)) || (rc = h2d(n, h.ev, ev.data(), S)) ||
         (rc = h2d(n, h.src, src.data(), S)) || (rc = h2d(n, h.stype, st.data(), S)) ||
-        (rc = h2d(n, h.phase0, ph.data(), S)) || (rc = h2d(n, h.sdelay, dl.data(), S)) ||
-        (rc = h2d(n, h.count, count.data(), N)))
+        (rc = h2d(n, h.count, count.data(), N)) || (rc = h2d(n, h.ring, ring.data(), ring.size())) ||
+        (rc = h2d(n, h.ring_n, ring_n.data(), ring_n.size())))
         return rc;
     unsigned long long s64 = step;
     CK(cudaMemcpyAsync(h.step, &s64, sizeof(s64), cudaMemcpyHostToDevice, n->stream));
+    CK(cudaStreamSynchronize(n->stream));
     bg3::launch_rebuild_maps(h, n->d, n->stream);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(n->stream));
@@ -323,8 +447,7 @@ int bg3_upload_growth(bg3_net *n, const bg3_growth_params *p, const float *radii
     int rc;
     if ((rc = h2d(n, h.radii, radii, N)) || (rc = h2d(n, h.rates, rates, N))) return rc;
     // recorder row 0 holds the start values (XmlGrowthRecorder::initDefaultValues / initValues)
-    if (radii) CK(cudaMemcpyAsync(h.radii_hist, radii, N * sizeof(float), cudaMemcpyHostToDevice, n->stream));
-    if (rates) CK(cudaMemcpyAsync(h.rates_hist, rates, N * sizeof(float), cudaMemcpyHostToDevice, n->stream));
+    if ((rc = h2d(n, h.radii_hist, radii, N)) || (rc = h2d(n, h.rates_hist, rates, N))) return rc;
     if ((rc = push_desc(n))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
@@ -333,15 +456,15 @@ int bg3_upload_growth(bg3_net *n, const bg3_growth_params *p, const float *radii
 int bg3_upload_weights(bg3_net *n, const float *Wref)
 {
     if (!n || !Wref) return BG3_EINVAL;
-    const size_t N = n->h.N, M = n->h.max_syn, S = N * M;
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * M;
     std::vector<uint32_t> count(N);
-    std::vector<float> W(S);
+    std::vector<EvSlot> ev(S);
     int rc;
-    if ((rc = d2h(n, count.data(), n->h.count, N)) || (rc = d2h(n, W.data(), n->h.W, S))) return rc;
+    if ((rc = d2h(n, count.data(), n->h.count, N)) || (rc = d2h(n, ev.data(), n->h.ev, S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     for (size_t d = 0; d < N; d++)
-        for (size_t k = 0; k < count[d]; k++) W[k * N + d] = Wref[d * M + k];
-    if ((rc = h2d(n, n->h.W, W.data(), S))) return rc;
+        for (size_t k = 0; k < count[d]; k++) ev[k * Np + d].W = Wref[d * M + k];
+    if ((rc = h2d(n, n->h.ev, ev.data(), S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
 }
@@ -379,28 +502,57 @@ int bg3_push_noise(bg3_net *n, const float *v, int64_t cnt)
 }
 
 // ---- hot path -------------------------------------------------------------------------------
+// Device-noise mode: neurons(t0), then per step deliver + sweep whose epilogue integrates the
+// next step's neurons, the last sweep without that epilogue.  Runs of interior steps replay a
+// CUDA graph of GRAPH_STEPS (deliver, fused sweep) pairs.  Injected-noise mode: neurons,
+// deliver, sweep for every step.
+static int run_steps(bg3_net *n, int64_t nsteps)
+{
+    if (nsteps <= 0) return BG3_OK;
+    const NetDev &h = n->h;
+    if (h.noise_mode == BG3_NOISE_INJECT) {
+        for (int64_t s = 0; s < nsteps; s++) {
+            bg3::launch_neurons(h, n->d, n->stream);
+            bg3::launch_deliver(h, n->d, n->stream);
+            bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, false, n->stream);
+        }
+        n->launches += 3 * nsteps;
+        CK(cudaGetLastError());
+        return BG3_OK;
+    }
+    bg3::launch_neurons(h, n->d, n->stream);
+    int64_t interior = nsteps - 1;
+    if (interior >= GRAPH_STEPS && !n->graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < GRAPH_STEPS; i++) {
+            bg3::launch_deliver(h, n->d, n->stream);
+            bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, true, n->stream);
+        }
+        CK(cudaStreamEndCapture(n->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&n->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { n->graph = nullptr; return BG3_ECUDA; }
+    }
+    while (n->graph && interior >= GRAPH_STEPS) {
+        CK(cudaGraphLaunch(n->graph, n->stream));
+        interior -= GRAPH_STEPS;
+    }
+    for (int64_t i = 0; i < interior; i++) {
+        bg3::launch_deliver(h, n->d, n->stream);
+        bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, true, n->stream);
+    }
+    bg3::launch_deliver(h, n->d, n->stream);
+    bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, false, n->stream);
+    n->launches += 1 + 2 * nsteps;
+    CK(cudaGetLastError());
+    return BG3_OK;
+}
+
 int bg3_step(bg3_net *n, int64_t nsteps)
 {
     if (!n || nsteps < 0) return BG3_EINVAL;
-    if (n->timing) {
-        for (int i = 0; i < 4; i++)
-            if (!n->ev[i]) CK(cudaEventCreate(&n->ev[i]));
-        n->ms_neurons = n->ms_fanout = n->ms_sweep = 0;
-        for (int64_t s = 0; s < nsteps; s++) {
-            bg3::launch_step_parts(n->h, n->d, n->stream, n->ev);
-            CK(cudaEventSynchronize(n->ev[3]));
-            float a, b, c;
-            cudaEventElapsedTime(&a, n->ev[0], n->ev[1]);
-            cudaEventElapsedTime(&b, n->ev[1], n->ev[2]);
-            cudaEventElapsedTime(&c, n->ev[2], n->ev[3]);
-            n->ms_neurons += a; n->ms_fanout += b; n->ms_sweep += c;
-        }
-    } else {
-        for (int64_t s = 0; s < nsteps; s++) bg3::launch_step(n->h, n->d, n->stream);
-    }
-    n->launches += 3 * nsteps;
-    CK(cudaGetLastError());
-    return BG3_OK;
+    return run_steps(n, nsteps);
 }
 
 int bg3_epoch_growth(bg3_net *n, int32_t epoch)
@@ -457,51 +609,69 @@ int bg3_download_lif(bg3_net *n, bg3_lif_arrays *a)
     return BG3_OK;
 }
 
+// Rebuilds the reference's delayQueue / delayIdx from the spike ring and birth steps: a spike
+// emitted at tf >= birth is due at tf + D; at step t it sits at bit (delayIdx + tf + D - t) & 31
+// with delayIdx = (t - birth) & 31.
 int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
 {
     if (!n || !a) return BG3_EINVAL;
-    const size_t N = n->h.N, M = n->h.max_syn, S = N * M;
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * M;
     NetDev &h = n->h;
-    std::vector<float> psr(S), decay(S), W(S), U(S), Dd(S), F(S), u(S), r(S);
-    std::vector<uint32_t> queue(S), count(N);
-    std::vector<unsigned long long> last(S);
-    std::vector<int32_t> src(S);
+    std::vector<float> psr(S);
+    std::vector<uint8_t> dc(S), lc(S);
+    std::vector<EvSlot> ev(S);
+    std::vector<int32_t> src(S), ring(N * BG3_RING), ring_n(BG3_RING);
     std::vector<int8_t> st(S);
-    std::vector<uint8_t> ph(S), dl(S);
+    std::vector<uint32_t> count(N);
     unsigned long long step = 0;
     int rc;
-    if ((rc = d2h(n, psr.data(), h.psr, S)) || (rc = d2h(n, decay.data(), h.decay, S)) ||
-        (rc = d2h(n, W.data(), h.W, S)) || (rc = d2h(n, U.data(), h.U, S)) ||
-        (rc = d2h(n, Dd.data(), h.D, S)) || (rc = d2h(n, F.data(), h.F, S)) ||
-        (rc = d2h(n, u.data(), h.u, S)) || (rc = d2h(n, r.data(), h.r, S)) ||
-        (rc = d2h(n, queue.data(), h.queue, S)) || (rc = d2h(n, last.data(), h.lastSpike, S)) ||
+    if ((rc = d2h(n, psr.data(), h.psr, S)) || (rc = d2h(n, dc.data(), h.dcls, S)) ||
+        (rc = d2h(n, lc.data(), h.lcls, S)) || (rc = d2h(n, ev.data(), h.ev, S)) ||
         (rc = d2h(n, src.data(), h.src, S)) || (rc = d2h(n, st.data(), h.stype, S)) ||
-        (rc = d2h(n, ph.data(), h.phase0, S)) || (rc = d2h(n, dl.data(), h.sdelay, S)) ||
-        (rc = d2h(n, count.data(), h.count, N)) || (rc = d2h(n, &step, h.step, 1)))
+        (rc = d2h(n, count.data(), h.count, N)) || (rc = d2h(n, &step, h.step, 1)) ||
+        (rc = d2h(n, ring.data(), h.ring, ring.size())) ||
+        (rc = d2h(n, ring_n.data(), h.ring_n, ring_n.size())))
         return rc;
     CK(cudaStreamSynchronize(n->stream));
+    // fired[s] bit j: neuron s fired at step - 1 - j
+    std::vector<uint32_t> fired(N, 0u);
+    for (int j = 0; j < 32 && (uint64_t)j < step; j++) {
+        int slot = (int)((step - 1 - (uint64_t)j) & (BG3_RING - 1));
+        for (int q = 0; q < std::min<int>(ring_n[slot], (int)N); q++)
+            fired[ring[(size_t)slot * N + q]] |= 1u << j;
+    }
     for (size_t d = 0; d < N; d++) {
         if (a->counts) a->counts[d] = count[d];
         for (size_t k = 0; k < M; k++) {
-            size_t i = d * M + k, p = k * N + d;
+            size_t i = d * M + k, p = k * Np + d;
             bool used = k < count[d];
             if (a->in_use) a->in_use[i] = used ? 1 : 0;
             if (!used) continue;
+            const EvSlot &e = ev[p];
+            int D = n->ltab[lc[p]];
+            uint32_t di = (uint32_t)((uint32_t)step - e.born) & 31u;
+            uint32_t q = 0;
+            for (int j = 0; j < D; j++) {
+                if (!((fired[src[p]] >> j) & 1u)) continue;
+                uint32_t tf = (uint32_t)(step - 1 - (uint64_t)j);
+                if ((int32_t)(tf - e.born) < 0) continue;
+                q |= 1u << ((di + (uint32_t)(D - 1 - j)) & 31u);
+            }
             if (a->src) a->src[i] = src[p];
             if (a->type) a->type[i] = st[p];
-            if (a->W) a->W[i] = W[p];
+            if (a->W) a->W[i] = e.W;
             if (a->psr) a->psr[i] = psr[p];
-            if (a->decay) a->decay[i] = decay[p];
-            if (a->total_delay) a->total_delay[i] = dl[p];
-            if (a->delayIdx) a->delayIdx[i] = (int32_t)((step - ph[p]) & 31u);
-            if (a->delayQueue) a->delayQueue[i] = rotr32(queue[p], ph[p]);
+            if (a->decay) a->decay[i] = n->dtab[dc[p]];
+            if (a->total_delay) a->total_delay[i] = D;
+            if (a->delayIdx) a->delayIdx[i] = (int32_t)di;
+            if (a->delayQueue) a->delayQueue[i] = q;
             if (a->tau) a->tau[i] = h.t_tau[st[p] & 3];
-            if (a->U) a->U[i] = U[p];
-            if (a->D) a->D[i] = Dd[p];
-            if (a->F) a->F[i] = F[p];
-            if (a->u) a->u[i] = u[p];
-            if (a->r) a->r[i] = r[p];
-            if (a->lastSpike) a->lastSpike[i] = last[p];
+            if (a->U) a->U[i] = e.U;
+            if (a->D) a->D[i] = e.D;
+            if (a->F) a->F[i] = e.F;
+            if (a->u) a->u[i] = e.u;
+            if (a->r) a->r[i] = e.r;
+            if (a->lastSpike) a->lastSpike[i] = (e.last == BG3_NO_SPIKE32) ? BG3_ULONG_MAX : (uint64_t)e.last;
         }
     }
     return BG3_OK;
@@ -519,17 +689,18 @@ int64_t bg3_total_synapses(bg3_net *n)
     return t;
 }
 
-// The device keeps the outgoing map as plane positions grouped by source in arbitrary order
-// (spike propagation does not depend on it) and the incoming map implicitly as the in-use row
-// prefixes.  Both are returned in the reference's order: slot ids d * maxSyn + k, ascending
+// The device keeps the outgoing map grouped by (delay class, source) with plane slots in
+// arbitrary order (delivery does not depend on it) and the incoming map implicitly as the in-use
+// row prefixes.  Both are returned in the reference's order: slot ids d * maxSyn + k, ascending
 // within each source; incoming in dest-major slot order (Synapses/AllSynapses.cpp:223-293).
 int bg3_download_maps(bg3_net *n, bg3_index_maps *m)
 {
     if (!n || !m) return BG3_EINVAL;
-    const size_t N = n->h.N, M = n->h.max_syn;
-    std::vector<uint32_t> ob(N), oc(N), count(N);
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn;
+    const size_t C = n->ltab.size();
+    std::vector<uint32_t> ob(N * C), oc(N * C), count(N);
     int rc;
-    if ((rc = d2h(n, ob.data(), n->h.outBegin, N)) || (rc = d2h(n, oc.data(), n->h.outCount, N)) ||
+    if ((rc = d2h(n, ob.data(), n->h.outBegin, N * C)) || (rc = d2h(n, oc.data(), n->h.outCount, N * C)) ||
         (rc = d2h(n, count.data(), n->h.count, N)))
         return rc;
     CK(cudaStreamSynchronize(n->stream));
@@ -538,19 +709,22 @@ int bg3_download_maps(bg3_net *n, bg3_index_maps *m)
     std::vector<uint32_t> om(std::max<size_t>(total, 1));
     if (total && (rc = d2h(n, om.data(), n->h.outMap, total))) return rc;
     CK(cudaStreamSynchronize(n->stream));
-    for (size_t i = 0; i < N; i++) {
-        if (m->outgoingSynapseBegin) m->outgoingSynapseBegin[i] = ob[i];
-        if (m->outgoingSynapseCount) m->outgoingSynapseCount[i] = oc[i];
-        std::vector<uint32_t> ids(oc[i]);
-        for (uint32_t j = 0; j < oc[i]; j++) {
-            uint32_t p = om[ob[i] + j] & BG3_POS_MASK;
-            ids[j] = (uint32_t)((p % N) * M + p / N);
-        }
-        std::sort(ids.begin(), ids.end());
-        if (m->outgoingSynapseIndexMap)
-            for (uint32_t j = 0; j < oc[i]; j++) m->outgoingSynapseIndexMap[ob[i] + j] = ids[j];
-    }
     uint32_t acc = 0;
+    for (size_t i = 0; i < N; i++) {
+        std::vector<uint32_t> ids;
+        for (size_t c = 0; c < C; c++)
+            for (uint32_t j = 0; j < oc[c * N + i]; j++) {
+                uint32_t p = om[ob[c * N + i] + j];
+                ids.push_back((uint32_t)((p % Np) * M + p / Np));
+            }
+        std::sort(ids.begin(), ids.end());
+        if (m->outgoingSynapseBegin) m->outgoingSynapseBegin[i] = acc;
+        if (m->outgoingSynapseCount) m->outgoingSynapseCount[i] = (uint32_t)ids.size();
+        if (m->outgoingSynapseIndexMap)
+            for (size_t j = 0; j < ids.size(); j++) m->outgoingSynapseIndexMap[acc + j] = ids[j];
+        acc += (uint32_t)ids.size();
+    }
+    acc = 0;
     for (size_t d = 0; d < N; d++) {
         if (m->incomingSynapseBegin) m->incomingSynapseBegin[d] = acc;
         if (m->incomingSynapseCount) m->incomingSynapseCount[d] = count[d];
@@ -584,41 +758,63 @@ int bg3_download_histories(bg3_net *n, float *burst, float *spikes, float *rh, f
     return BG3_OK;
 }
 
+// ---- benchmarking ---------------------------------------------------------------------------
+__global__ void k_scrub(const float4 *p, size_t n4, float *sink)
+{
+    float acc = 0.0f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = p[i];
+        acc += v.x + v.y + v.z + v.w;
+    }
+    if (acc == 12345.678f) *sink = acc;  // keeps the loads; practically never true
+}
+
 int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step_ms,
                     float *kernel_ms)
 {
     if (!n || nsteps < 0 || !step_ms) return BG3_EINVAL;
     if (flush_bytes > 0 && (size_t)flush_bytes > n->flush_size) {
         if (n->flush_buf) cudaFree(n->flush_buf);
-        n->flush_buf = nullptr;
+        if (n->scrub_buf) cudaFree(n->scrub_buf);
+        n->flush_buf = n->scrub_buf = nullptr;
         n->flush_size = 0;
-        if (cudaMalloc(&n->flush_buf, (size_t)flush_bytes) != cudaSuccess) {
+        if (cudaMalloc(&n->flush_buf, (size_t)flush_bytes) != cudaSuccess ||
+            cudaMalloc(&n->scrub_buf, (size_t)flush_bytes + 16) != cudaSuccess) {
             cudaGetLastError();
             return BG3_ENOMEM;
         }
+        CK(cudaMemsetAsync(n->scrub_buf, 0, (size_t)flush_bytes + 16, n->stream));
         n->flush_size = (size_t)flush_bytes;
     }
-    const int per = kernel_ms ? 4 : 2;
-    std::vector<cudaEvent_t> ev((size_t)nsteps * per);
+    const NetDev &h = n->h;
+    const bool inject = h.noise_mode == BG3_NOISE_INJECT;
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 4);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     for (int64_t s = 0; s < nsteps; s++) {
-        if (flush_bytes > 0)
+        if (flush_bytes > 0) {
+            // evict L2: write a buffer larger than L2, then read another one so the step does
+            // not pay for writing back the flush's dirty lines
             CK(cudaMemsetAsync(n->flush_buf, (int)(s & 0xff), (size_t)flush_bytes, n->stream));
-        cudaEvent_t *e = &ev[(size_t)s * per];
-        if (kernel_ms) {
-            bg3::launch_step_parts(n->h, n->d, n->stream, e);
-        } else {
-            CK(cudaEventRecord(e[0], n->stream));
-            bg3::launch_step(n->h, n->d, n->stream);
-            CK(cudaEventRecord(e[1], n->stream));
+            k_scrub<<<2 * 152, 512, 0, n->stream>>>((const float4 *)n->scrub_buf,
+                                                   (size_t)flush_bytes / 16,
+                                                   (float *)((char *)n->scrub_buf + flush_bytes));
         }
+        cudaEvent_t *e = &ev[(size_t)s * 4];
+        const bool last = s == nsteps - 1;
+        CK(cudaEventRecord(e[0], n->stream));
+        if (inject || s == 0) bg3::launch_neurons(h, n->d, n->stream);
+        CK(cudaEventRecord(e[1], n->stream));
+        bg3::launch_deliver(h, n->d, n->stream);
+        CK(cudaEventRecord(e[2], n->stream));
+        bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, !inject && !last, n->stream);
+        CK(cudaEventRecord(e[3], n->stream));
     }
-    n->launches += 3 * nsteps;
+    n->launches += (inject ? 3 : 2) * nsteps + (inject ? 0 : 1);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(n->stream));
     for (int64_t s = 0; s < nsteps; s++) {
-        cudaEvent_t *e = &ev[(size_t)s * per];
-        CK(cudaEventElapsedTime(&step_ms[s], e[0], e[per - 1]));
+        cudaEvent_t *e = &ev[(size_t)s * 4];
+        CK(cudaEventElapsedTime(&step_ms[s], e[0], e[3]));
         if (kernel_ms)
             for (int k = 0; k < 3; k++) CK(cudaEventElapsedTime(&kernel_ms[3 * s + k], e[k], e[k + 1]));
     }

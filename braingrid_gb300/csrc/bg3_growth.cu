@@ -6,7 +6,7 @@
 //                      frontier distance / overlap area, and appends the new synapses in source
 //                      order after the row's in-use prefix                      (O(N^2), no N^2
 //                                                                                storage)
-//   k_out_count/scan/fill  outgoing CSR rebuild (createSynapseImap)
+//   k_out_count/scan/fill  outgoing CSR rebuild per delay class (createSynapseImap)
 //   k_record_epoch     recorder histograms, rates/radii history, radius clamp, spike-count roll
 #include "bg3_internal.cuh"
 
@@ -65,15 +65,15 @@ __device__ __forceinline__ float syn_sign(int type) { return (type <= 1) ? -1.0f
 __global__ void k_growth_existing(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    size_t total = (size_t)n.N * n.max_syn;
+    size_t total = (size_t)n.Np * n.max_syn;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
-        int d = (int)(p % n.N), k = (int)(p / n.N);
-        if (k >= (int)n.count[d]) continue;
+        int d = (int)(p % n.Np), k = (int)(p / n.Np);
+        if (d >= n.N || k >= (int)n.count[d]) continue;
         int s = n.src[p];
         float a = pair_area(n.xloc[s], n.yloc[s], n.radii[s], n.xloc[d], n.yloc[d], n.radii[d]);
-        if (a < 0.0f) set_err(n, 1u << 4);  // the reference would erase (never: area >= 0)
-        n.W[p] = a * syn_sign(n.stype[p]) * 1.0e-8f;
+        if (a < 0.0f) set_err(n, ERR_NEGATIVE_AREA);  // the reference would erase (area >= 0)
+        n.ev[p].W = a * syn_sign(n.stype[p]) * 1.0e-8f;
     }
 }
 
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
     __syncthreads();
     const int c0 = s_count;
     for (int k = threadIdx.x; k < c0; k += blockDim.x) {
-        int s = n.src[(size_t)k * n.N + d];
+        int s = n.src[(size_t)k * n.Np + d];
         atomicOr(&existing[s >> 5], 1u << (s & 31));
     }
     __syncthreads();
@@ -123,24 +123,25 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
         if (add) {
             int k = cur + before + __popc(m & ((1u << lane) - 1));
             if (k < n.max_syn) {
-                size_t p = (size_t)k * n.N + d;
+                size_t p = (size_t)k * n.Np + d;
                 int type = syn_type(n.ntype[s], td);
                 n.src[p] = s;
                 n.stype[p] = (int8_t)type;
-                n.W[p] = a * syn_sign(type) * 1.0e-8f;
                 n.psr[p] = 0.0f;
-                n.decay[p] = n.t_decay[type];
-                n.queue[p] = 0u;
-                n.phase0[p] = (uint8_t)(t & 31u);
-                n.sdelay[p] = (uint8_t)n.t_delay[type];
-                n.u[p] = n.t_u0;
-                n.r[p] = n.t_r0;
-                n.lastSpike[p] = BG3_ULONG_MAX;
-                n.U[p] = n.t_U[type];
-                n.D[p] = n.t_D[type];
-                n.F[p] = n.t_F[type];
+                n.dcls[p] = (uint8_t)n.t_dcls[type];
+                n.lcls[p] = (uint8_t)n.t_lcls[type];
+                EvSlot e;
+                e.W = a * syn_sign(type) * 1.0e-8f;
+                e.U = n.t_U[type];
+                e.D = n.t_D[type];
+                e.F = n.t_F[type];
+                e.u = n.t_u0;
+                e.r = n.t_r0;
+                e.last = BG3_NO_SPIKE32;
+                e.born = (uint32_t)t;
+                n.ev[p] = e;
             } else {
-                set_err(n, 1u << 2);
+                set_err(n, ERR_ROW_FULL);
             }
         }
         __syncthreads();
@@ -151,10 +152,12 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
 }
 
 // ---- outgoing map (AllSynapses::createSynapseImap, Synapses/AllSynapses.cpp:223-293) ---------
+// Grouped by delay class c then source i (index c * N + i); entries are plane slots.
 __global__ void k_out_zero(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n.N; i += gridDim.x * blockDim.x) {
+    int total = n.N * n.n_delays;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         n.outCount[i] = 0u;
         n.outFill[i] = 0u;
     }
@@ -162,25 +165,27 @@ __global__ void k_out_zero(const NetDev *nets)
 __global__ void k_out_count(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    size_t total = (size_t)n.N * n.max_syn;
+    size_t total = (size_t)n.Np * n.max_syn;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
-        int d = (int)(p % n.N), k = (int)(p / n.N);
-        if (k < (int)n.count[d]) atomicAdd(&n.outCount[n.src[p]], 1u);
+        int d = (int)(p % n.Np), k = (int)(p / n.Np);
+        if (d < n.N && k < (int)n.count[d])
+            atomicAdd(&n.outCount[(size_t)n.lcls[p] * n.N + n.src[p]], 1u);
     }
 }
-// exclusive scan of outCount into outBegin; one CTA of 1024 threads walks N in chunks
+// exclusive scan of outCount into outBegin; one CTA of 1024 threads walks the table in chunks
 __global__ void __launch_bounds__(1024) k_out_scan(const NetDev *nets)
 {
     const NetDev &n = nets[0];
     __shared__ uint32_t wsum[32];
     __shared__ uint32_t carry;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int total = n.N * n.n_delays;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int b = 0; b < n.N; b += 1024) {
+    for (int b = 0; b < total; b += 1024) {
         int i = b + threadIdx.x;
-        uint32_t v = (i < n.N) ? n.outCount[i] : 0u;
+        uint32_t v = (i < total) ? n.outCount[i] : 0u;
         uint32_t x = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(1024) k_out_scan(const NetDev *nets)
         }
         __syncthreads();
         uint32_t c = carry;
-        if (i < n.N) n.outBegin[i] = c + wsum[warp] + x - v;
+        if (i < total) n.outBegin[i] = c + wsum[warp] + x - v;
         __syncthreads();
         if (threadIdx.x == 1023) carry = c + wsum[31] + x;
         __syncthreads();
@@ -209,15 +214,14 @@ __global__ void __launch_bounds__(1024) k_out_scan(const NetDev *nets)
 __global__ void k_out_fill(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    size_t total = (size_t)n.N * n.max_syn;
+    size_t total = (size_t)n.Np * n.max_syn;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
-        int d = (int)(p % n.N), k = (int)(p / n.N);
-        if (k >= (int)n.count[d]) continue;
-        int s = n.src[p];
-        uint32_t slot = n.outBegin[s] + atomicAdd(&n.outFill[s], 1u);
-        uint32_t dly = (uint32_t)n.sdelay[p];
-        n.outMap[slot] = (uint32_t)p | (dly << BG3_DELAY_SHIFT);
+        int d = (int)(p % n.Np), k = (int)(p / n.Np);
+        if (d >= n.N || k >= (int)n.count[d]) continue;
+        size_t key = (size_t)n.lcls[p] * n.N + n.src[p];
+        uint32_t slot = n.outBegin[key] + atomicAdd(&n.outFill[key], 1u);
+        n.outMap[slot] = (uint32_t)p;
     }
 }
 

@@ -1,31 +1,46 @@
 // Internal device-side layout and helpers of libbg3.
 //
-// HBM layout of one network (all arrays owned by bg3_net, allocated once at bg3_create):
+// HBM layout of one network (arrays owned by bg3_net, allocated once at bg3_create):
 //
-//   neurons (n = N)       SoA float/int arrays, neuron index contiguous.
-//   synapse slot planes   slot (dest d, row k) lives at plane index p = k * N + d ("ELL" order):
-//                         a warp that walks 32 consecutive dests of one row k reads 128
-//                         contiguous bytes per field.  The reference slot id is d * maxSyn + k.
-//   delay queues          one uint32 ring per slot, stored in the GLOBAL step phase: a spike
-//                         due at step t sits at bit (t & 31).  The reference keeps a per-slot
-//                         read index (delayIdx) instead; with phase0 = (creation step) & 31 the
-//                         two are related by q_global = rotl(q_ref, phase0) and
-//                         delayIdx = (t - phase0) & 31, so the hot sweep needs neither the
-//                         index read nor its write.
-//   outgoing map          CSR by source neuron; entry = plane index | (total_delay << 27).
+//   neurons               SoA float/int arrays, neuron index contiguous.
+//   synapse slot planes   slot (dest d, row k) lives at p = k * Np + d, Np = N rounded up to 32
+//                         ("ELL" order): one row of a 32-dest tile is 128 contiguous bytes of psr,
+//                         so the sweep moves [64 rows x 32 dests] tiles with 2-D TMA copies.  The
+//                         reference slot id of (d, k) is d * maxSyn + k.
+//   hot per-slot state    psr (f32) and a one-byte decay class (index into a per-network table
+//                         of decay factors): 9 bytes per synapse per step.
+//   event per-slot state  EvSlot (32 B, one sector): W, U, D, F, u, r, last spike step, birth
+//                         step — read only when a spike is delivered.
+//   spike propagation     instead of a 32-bit delay queue per synapse, the ids of the neurons
+//                         that fired at each of the last 64 steps are kept in a ring; the
+//                         outgoing map is grouped by delay class, so at step t the synapses of
+//                         delay D that receive a spike are the outgoing synapses (class D) of the
+//                         neurons in ring slot (t - D) & 63.  A synapse receives the spike only
+//                         if it existed when the spike was emitted (birth step <= emit step),
+//                         which is what the reference's per-synapse queue encodes.  The
+//                         reference's delayQueue / delayIdx are rebuilt from the ring on download.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #define BG3_ULONG_MAX 0xffffffffffffffffull
-#define BG3_DELAY_SHIFT 27
-#define BG3_POS_MASK ((1u << BG3_DELAY_SHIFT) - 1u)
+#define BG3_NO_SPIKE32 0xffffffffu
+#define BG3_RING 64          // spike-list ring depth (steps); delays must be < 32
+#define BG3_MAX_DCLS 256     // decay classes
+#define BG3_MAX_DELAYS 8     // delay classes
+
+struct __align__(32) EvSlot {
+    float W, U, D, F, u, r;
+    uint32_t last;   // step of the last delivered spike, BG3_NO_SPIKE32 = none (ULONG_MAX)
+    uint32_t born;   // step at which the synapse was created (low 32 bits)
+};
 
 struct NetDev {
-    int32_t N, max_syn, max_spikes, neuron_kind, syn_kind, noise_mode;
+    int32_t N, Np, max_syn, max_spikes, neuron_kind, syn_kind, noise_mode;
     float dt, epoch_duration;
     uint32_t noise_seed;
-    int32_t ntiles;           // sweep tiles of 32 dests
+    int32_t ntiles;                // sweep tiles of 32 dests
+    int32_t n_dcls, n_delays;
     // step counter and the last-CTA barrier of the sweep
     unsigned long long *step;
     uint32_t *sweep_done;
@@ -35,20 +50,20 @@ struct NetDev {
     int32_t *refr, *spikeCount, *spikeCountOffset;
     unsigned long long *history;   // [N][max_spikes]
     int8_t *ntype;                 // 1 INH, 2 EXC
-    // spikes of the current step
-    int32_t *spikes, *nspikes;
-    // synapse planes
-    float *psr, *decay, *W, *U, *D, *F, *u, *r;
-    uint32_t *queue;
-    unsigned long long *lastSpike;
+    // spike ring: ids of the neurons that fired at step t are ring[(t & 63) * N + i]
+    int32_t *ring, *ring_n;
+    // synapse planes (index k * Np + d)
+    float *psr;
+    uint8_t *dcls;                 // decay class
+    uint8_t *lcls;                 // delay class
+    EvSlot *ev;
     int32_t *src;
     int8_t *stype;
-    uint8_t *phase0;
-    uint8_t *sdelay;               // total_delay of the slot (steps)
     uint32_t *count;               // in-use prefix length per dest
-    // outgoing CSR
-    uint32_t *outBegin, *outCount, *outMap;
-    uint32_t *outFill;
+    float *dtab;                   // decay factor per decay class [BG3_MAX_DCLS]
+    int32_t *ltab;                 // delay (steps) per delay class [BG3_MAX_DELAYS]
+    // outgoing CSR per (delay class, source): index c * N + i
+    uint32_t *outBegin, *outCount, *outMap, *outFill;
     // growth
     float *radii, *rates, *xloc, *yloc;
     float g_epsilon, g_beta, g_rho, g_target_rate, g_min_radius, g_start_radius, g_max_rate;
@@ -60,8 +75,19 @@ struct NetDev {
     unsigned long long *noise_cursor;
     long long noise_len;
     // per-type constants for synapses created on the device
-    float t_tau[4], t_decay[4], t_U[4], t_D[4], t_F[4], t_u0, t_r0;
-    int32_t t_delay[4];
+    float t_tau[4], t_U[4], t_D[4], t_F[4], t_u0, t_r0;
+    int32_t t_dcls[4], t_lcls[4];
+};
+
+// device error word bits (mirrored in include/bg3.h)
+enum : uint32_t {
+    ERR_HISTORY_OVERFLOW = 1u << 0,
+    ERR_ROW_FULL = 1u << 2,
+    ERR_NOISE_EXHAUSTED = 1u << 3,
+    ERR_NEGATIVE_AREA = 1u << 4,
+    ERR_SPIKE_LIST = 1u << 5,
+    ERR_TIMEOUT = 1u << 6,
+    ERR_STEP_RANGE = 1u << 7,
 };
 
 // ---- exact-rounding helpers -----------------------------------------------------------------
@@ -87,7 +113,7 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
         k0 += W0; k1 += W1;
     }
 }
-// One N(0,1) value by the Box-Muller transform of two 32-bit uniforms.
+// One N(0,1) value by the Box-Muller transform of two 24-bit uniforms.
 __device__ __forceinline__ float normal_device(uint32_t seed, unsigned long long step, int i)
 {
     uint32_t c[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 0u};
@@ -98,3 +124,60 @@ __device__ __forceinline__ float normal_device(uint32_t seed, unsigned long long
 }
 
 __device__ __forceinline__ void set_err(const NetDev &n, uint32_t bit) { atomicOr(n.err, bit); }
+
+// ---- LIF neuron update (shared by the standalone kernels and the sweep epilogue) -------------
+enum { BR_REFRACTORY = 0, BR_FIRE = 1, BR_INTEGRATE = 2 };
+
+// AllLIFNeurons::advanceNeuron branch selection (Neurons/AllLIFNeurons.cpp:31-35).
+__device__ __forceinline__ int lif_branch(const NetDev &n, int i)
+{
+    if (n.refr[i] > 0) return BR_REFRACTORY;
+    if (n.Vm[i] >= n.Vthresh[i]) return BR_FIRE;
+    return BR_INTEGRATE;
+}
+
+// AllLIFNeurons::advanceNeuron / fire and AllSpikingNeurons::fire
+// (Neurons/AllLIFNeurons.cpp:20-77, Neurons/AllSpikingNeurons.cpp:155-172) with the summation
+// point value passed in.  Each float operation rounds on its own (-fmad=false).  Returns true
+// when the neuron fired.  The caller stores sp = 0 afterwards.
+__device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float sp, float noise,
+                                          unsigned long long t)
+{
+    if (br == BR_REFRACTORY) {
+        n.refr[i] = n.refr[i] - 1;
+        return false;
+    }
+    if (br == BR_FIRE) {
+        int cnt = n.spikeCount[i];
+        int idx = (cnt + n.spikeCountOffset[i]) % n.max_spikes;
+        n.history[(size_t)i * n.max_spikes + idx] = t;
+        cnt += 1;
+        n.spikeCount[i] = cnt;
+        if (cnt >= n.max_spikes) set_err(n, ERR_HISTORY_OVERFLOW);
+        n.refr[i] = (int)((double)(n.Trefract[i] / n.dt) + 0.5);
+        n.Vm[i] = n.Vreset[i];
+        return true;
+    }
+    sp = sp + n.I0[i];
+    sp = sp + noise * n.Inoise[i];
+    n.Vm[i] = n.C1[i] * n.Vm[i] + n.C2[i] * sp;
+    return false;
+}
+
+// Append the firing lanes' neuron ids to ring slot (t & 63) (warp-aggregated atomic).
+__device__ __forceinline__ void ring_push(const NetDev &n, unsigned long long t, bool fired, int i)
+{
+    unsigned mask = __ballot_sync(0xffffffffu, fired);
+    if (!mask) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    int slot = (int)(t & (BG3_RING - 1));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&n.ring_n[slot], __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (fired) {
+        int pos = base + __popc(mask & ((1u << lane) - 1));
+        if (pos < n.N) n.ring[(size_t)slot * n.N + pos] = i;
+        else set_err(n, ERR_SPIKE_LIST);
+    }
+}

@@ -1,72 +1,86 @@
-// Per-step kernels of the spiking hot path: neuron integration, spike propagation, synapse sweep.
+// Per-step kernels of the spiking hot path.
 //
-// One simulation step t is three launches on the network's stream:
-//   k_neurons_*  (t)  LIF integration / refractory / fire; spikers compacted into a list
-//   k_fanout     (t)  one warp per spiking neuron sets bit (t + delay) & 31 of each outgoing
-//                     synapse's delay queue (each synapse has a single source, so no two warps
-//                     touch one queue word)
-//   k_sweep      (t)  per 32-dest tile: pop the step's queue bit, DS facilitation/depression on a
-//                     hit, psr *= decay, and the ordered sum psr -> summation point of each dest;
-//                     the last tile to finish advances the device step counter.
+// One simulation step t on the network's stream:
+//   k_deliver    (t)  spike arrival: for every delay class D, the neurons that fired at step
+//                     t - D (spike ring) deliver to their outgoing synapses of that class; a hit
+//                     runs AllDSSynapses::changePSR on the synapse (one 32-byte EvSlot).
+//   k_sweep      (t)  per 32-dest tile, TMA-pipelined: psr *= decay for every slot row and the
+//                     ordered sum into each dest's summation point; in device-noise mode the
+//                     epilogue also integrates the tile's neurons for step t + 1 (they need only
+//                     their own summation point), so a step costs two launches.
+//   k_neurons_*  (t)  standalone neuron integration: the first step of a bg3_step call and every
+//                     step in injected-noise mode (the noise order needs a scan over all neurons).
+#include <cuda.h>
 #include "bg3_internal.cuh"
 
 namespace bg3 {
 
-// ---- neurons ---------------------------------------------------------------------------------
-enum { BR_REFRACTORY = 0, BR_FIRE = 1, BR_INTEGRATE = 2 };
-
-// AllLIFNeurons::advanceNeuron branch selection (Neurons/AllLIFNeurons.cpp:31-35).
-__device__ __forceinline__ int lif_branch(const NetDev &n, int i)
+// ---- PTX helpers: mbarrier, TMA (cp.async.bulk.tensor) ---------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
-    if (n.refr[i] > 0) return BR_REFRACTORY;
-    if (n.Vm[i] >= n.Vthresh[i]) return BR_FIRE;
-    return BR_INTEGRATE;
+    return (uint32_t)__cvta_generic_to_shared(p);
 }
-
-// AllLIFNeurons::advanceNeuron / fire and AllSpikingNeurons::fire
-// (Neurons/AllLIFNeurons.cpp:20-77, Neurons/AllSpikingNeurons.cpp:155-172).  Returns true when
-// the neuron fired.  The library is built with -fmad=false: each operation rounds on its own.
-__device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float noise,
-                                          unsigned long long t)
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 {
-    bool fired = false;
-    if (br == BR_REFRACTORY) {
-        n.refr[i] = n.refr[i] - 1;
-    } else if (br == BR_FIRE) {
-        int cnt = n.spikeCount[i];
-        int idx = (cnt + n.spikeCountOffset[i]) % n.max_spikes;
-        n.history[(size_t)i * n.max_spikes + idx] = t;
-        cnt += 1;
-        n.spikeCount[i] = cnt;
-        if (cnt >= n.max_spikes) set_err(n, 1u << 0);
-        n.refr[i] = (int)((double)(n.Trefract[i] / n.dt) + 0.5);
-        n.Vm[i] = n.Vreset[i];
-        fired = true;
-    } else {
-        float sp = n.sp[i];
-        sp = sp + n.I0[i];
-        sp = sp + noise * n.Inoise[i];
-        n.Vm[i] = n.C1[i] * n.Vm[i] + n.C2[i] * sp;
-    }
-    n.sp[i] = 0.0f;
-    return fired;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-
-__device__ __forceinline__ void push_spike(const NetDev &n, bool fired)
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
 {
-    unsigned mask = __ballot_sync(0xffffffffu, fired);
-    if (!mask) return;
-    int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == __ffs(mask) - 1) base = atomicAdd(n.nspikes, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
-    if (fired) {
-        int pos = base + __popc(mask & ((1u << lane) - 1));
-        if (pos < n.N) n.spikes[pos] = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-        else set_err(n, 1u << 5);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up after ~1 s of wall time (the caller sets the error flag).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    unsigned long long t0 = global_ns();
+    for (;;) {
+        for (int i = 0; i < 256; i++)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > 1000000000ull) return false;
     }
 }
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int y, const void *src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(map),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
+// ---- standalone neuron kernels ---------------------------------------------------------------
 // Device-noise mode: one N(0,1) draw per neuron per step, keyed by (seed, step, neuron).
 __global__ void __launch_bounds__(256) k_neurons_device(const NetDev *nets)
 {
@@ -77,9 +91,10 @@ __global__ void __launch_bounds__(256) k_neurons_device(const NetDev *nets)
     if (i < n.N) {
         int br = lif_branch(n, i);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = lif_apply(n, i, br, noise, t);
+        fired = lif_apply(n, i, br, n.sp[i], noise, t);
+        n.sp[i] = 0.0f;
     }
-    push_spike(n, fired);
+    ring_push(n, t, fired, i);
 }
 
 // Injected-noise mode: the reference CPU draws one value per integrating neuron while walking
@@ -123,22 +138,12 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const NetDev *nets)
             if (integ) {
                 long long pos = (long long)cursor + rank;
                 if (pos < n.noise_len) noise = n.noise_buf[pos];
-                else set_err(n, 1u << 3);
+                else set_err(n, ERR_NOISE_EXHAUSTED);
             }
-            fired = lif_apply(n, i, br, noise, t);
+            fired = lif_apply(n, i, br, n.sp[i], noise, t);
+            n.sp[i] = 0.0f;
         }
-        // compaction: neuron id, not thread id
-        unsigned fm = __ballot_sync(0xffffffffu, fired);
-        if (fm) {
-            int b = 0;
-            if (lane == __ffs(fm) - 1) b = atomicAdd(n.nspikes, __popc(fm));
-            b = __shfl_sync(0xffffffffu, b, __ffs(fm) - 1);
-            if (fired) {
-                int pos = b + __popc(fm & ((1u << lane) - 1));
-                if (pos < n.N) n.spikes[pos] = i;
-                else set_err(n, 1u << 5);
-            }
-        }
+        ring_push(n, t, fired, i);
         __syncthreads();
         if (threadIdx.x == 1023) s_running = running + warp_tot[31] + __popc(m);
         __syncthreads();
@@ -146,156 +151,221 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const NetDev *nets)
     if (threadIdx.x == 0) *n.noise_cursor = cursor + (unsigned long long)s_running;
 }
 
-// ---- spike propagation -----------------------------------------------------------------------
-// AllSpikingSynapses::preSpikeHit over the outgoing map (Neurons/AllSpikingNeurons.cpp:117-128,
-// Synapses/AllSpikingSynapses.cpp:261-279).  Global-phase queues: bit (t + total_delay) & 31.
-__global__ void __launch_bounds__(256) k_fanout(const NetDev *nets)
+// ---- spike arrival ---------------------------------------------------------------------------
+// Arrival of a spike emitted at step tf on plane slot p at step t: the isSpikeQueue hit of
+// AllSpikingSynapses::advanceSynapse (Synapses/AllSpikingSynapses.cpp:297-319) followed by
+// changePSR — AllDSSynapses.cpp:227-247 for DS, AllSpikingSynapses.cpp:327-334 otherwise.
+template <int SYN>
+__device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_t tf, uint32_t t)
+{
+    EvSlot e = n.ev[p];
+    if ((int32_t)(tf - e.born) < 0) return;  // the synapse did not exist when the spike left
+    float dec = n.dtab[n.dcls[p]];
+    float ps = n.psr[p];
+    if (SYN == 1) {
+        float u = e.u, r = e.r;
+        if (e.last != BG3_NO_SPIKE32) {
+            float isi = (float)(t - e.last) * n.dt;
+            r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_cr(-isi / e.D);
+            u = e.U + u * (1.0f - e.U) * exp_cr(-isi / e.F);
+        }
+        ps = ps + ((e.W / dec) * u * r);
+        EvSlot *q = &n.ev[p];
+        q->u = u;
+        q->r = r;
+        q->last = t;
+    } else {
+        ps = ps + e.W / dec;
+    }
+    n.psr[p] = ps;
+}
+
+// One warp per (delay class, spiking neuron) pair; lanes walk that neuron's outgoing synapses
+// of the class.  Each synapse has one source, which fires at most once per step, so no two
+// lanes touch one slot.  Block 0 also clears ring slot t + 1 for the next neuron pass.
+template <int SYN>
+__global__ void __launch_bounds__(256) k_deliver(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    unsigned long long t = *n.step;
-    int ns = min(*n.nspikes, n.N);
-    int lane = threadIdx.x & 31;
-    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int s = gw; s < ns; s += nw) {
-        int i = n.spikes[s];
-        uint32_t b = n.outBegin[i], c = n.outCount[i];
-        for (uint32_t j = lane; j < c; j += 32) {
-            uint32_t e = n.outMap[b + j];
-            uint32_t pos = e & BG3_POS_MASK;
-            uint32_t bit = 1u << ((uint32_t)(t + (e >> BG3_DELAY_SHIFT)) & 31u);
-            uint32_t q = n.queue[pos];
-            if (q & bit) set_err(n, 1u << 1);
-            n.queue[pos] = q | bit;
+    const unsigned long long t = *n.step;
+    if (blockIdx.x == 0 && threadIdx.x == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = 0; c < n.n_delays; c++) {
+        const int D = n.ltab[c];
+        if (D <= 0 || (unsigned long long)D > t) continue;
+        const unsigned long long tf = t - (unsigned long long)D;
+        const int slot = (int)(tf & (BG3_RING - 1));
+        const int m = min(n.ring_n[slot], n.N);
+        const int32_t *ids = n.ring + (size_t)slot * n.N;
+        const uint32_t *beg = n.outBegin + (size_t)c * n.N, *cnt = n.outCount + (size_t)c * n.N;
+        for (int s = gw; s < m; s += nw) {
+            const int i = ids[s];
+            const uint32_t b = beg[i], k = cnt[i];
+            for (uint32_t j = lane; j < k; j += 32)
+                deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, (uint32_t)t);
         }
     }
 }
 
 // ---- synapse sweep ---------------------------------------------------------------------------
-// AllDSSynapses::changePSR (Synapses/AllDSSynapses.cpp:227-247).
-__device__ __forceinline__ float ds_hit(const NetDev &n, size_t p, float psr, float decay,
-                                        unsigned long long t)
-{
-    float u = n.u[p], r = n.r[p];
-    unsigned long long last = n.lastSpike[p];
-    if (last != BG3_ULONG_MAX) {
-        float isi = (float)(t - last) * n.dt;
-        float D = n.D[p], F = n.F[p], U = n.U[p];
-        r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_cr(-isi / D);
-        u = U + u * (1.0f - U) * exp_cr(-isi / F);
-        n.r[p] = r;
-        n.u[p] = u;
-    }
-    n.lastSpike[p] = t;
-    return psr + ((n.W[p] / decay) * u * r);
-}
+constexpr int SW_DESTS = 32;   // dests per tile (one per consumer lane)
+constexpr int SW_ROWS = 64;    // slot rows per TMA chunk
+constexpr int SW_STAGES = 4;   // chunks in flight per tile
+constexpr uint32_t SW_CHUNK_BYTES = SW_ROWS * SW_DESTS * (4 + 1);
 
-constexpr int SW_DESTS = 32;   // dests per tile (one per lane)
-constexpr int SW_WARPS = 8;    // warps per CTA
-constexpr int SW_ROWS = 64;    // rows per chunk; each warp takes SW_ROWS / SW_WARPS of them
-constexpr int SW_RPW = SW_ROWS / SW_WARPS;
-
-// AllSpikingSynapses::advanceSynapse / isSpikeQueue over every in-use synapse
-// (Synapses/AllSpikingSynapses.cpp:242-319) with the summation of AllSynapses::advanceSynapses
-// (Synapses/AllSynapses.cpp:325-331): sp[d] = ((0 + psr_0) + psr_1) + ... in slot order, the
-// order the reference accumulates in.  All warps update psr for a 64-row chunk (loads first, so
-// each thread keeps 8 x 3 loads in flight), the chunk is staged in shared memory, and warp 0
-// adds it in row order for its 32 dests.
-template <int SYN>
-__global__ void __launch_bounds__(SW_WARPS * 32) k_sweep(const NetDev *nets)
+// AllSpikingSynapses::advanceSynapse's "psr *= decay" for every in-use synapse, and the
+// summation of AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331):
+// sp[d] = ((0 + psr_0) + psr_1) + ... in slot order, the reference's accumulation order.
+// Warp 0 lane 0 streams [64 rows x 32 dests] chunks of psr and of the decay class into a 4-stage
+// shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales each chunk in place,
+// adds it in row order, and writes it back with a TMA store.  FUSE: the epilogue integrates the
+// tile's neurons for step t + 1 (device-noise mode).
+template <int SYN, bool FUSE>
+__global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
+                                              const __grid_constant__ CUtensorMap tm_psr,
+                                              const __grid_constant__ CUtensorMap tm_cls)
 {
     const NetDev &n = nets[0];
-    __shared__ float stage[SW_ROWS][SW_DESTS + 1];
+    __shared__ __align__(128) float s_psr[SW_STAGES][SW_ROWS * SW_DESTS];
+    __shared__ __align__(128) uint8_t s_cls[SW_STAGES][SW_ROWS * SW_DESTS];
+    __shared__ float s_dtab[BG3_MAX_DCLS];
+    __shared__ __align__(8) uint64_t full[SW_STAGES], empty[SW_STAGES];
+    __shared__ int s_issued;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int d = blockIdx.x * SW_DESTS + lane;
+    const int d0 = blockIdx.x * SW_DESTS;
+    const int d = d0 + lane;
     const bool valid = d < n.N;
     const unsigned long long t = *n.step;
-    const uint32_t bit = 1u << ((uint32_t)t & 31u);
+    for (int i = threadIdx.x; i < n.n_dcls; i += blockDim.x) s_dtab[i] = n.dtab[i];
     const int cnt = valid ? (int)n.count[d] : 0;
     const int kmax = __reduce_max_sync(0xffffffffu, cnt);
-    const size_t N = (size_t)n.N;
-    float acc = 0.0f;
-    for (int kb = 0; kb < kmax; kb += SW_ROWS) {
-        float ps[SW_RPW], dc[SW_RPW];
-        uint32_t q[SW_RPW];
-#pragma unroll
-        for (int j = 0; j < SW_RPW; j++) {
-            int k = kb + warp + j * SW_WARPS;
-            if (k < cnt) {
-                size_t p = (size_t)k * N + d;
-                ps[j] = n.psr[p];
-                dc[j] = n.decay[p];
-                q[j] = n.queue[p];
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < SW_RPW; j++) {
-            int k = kb + warp + j * SW_WARPS;
-            if (k < cnt) {
-                size_t p = (size_t)k * N + d;
-                float v = ps[j];
-                if (q[j] & bit) {
-                    n.queue[p] = q[j] & ~bit;
-                    if (SYN == 1) v = ds_hit(n, p, v, dc[j], t);
-                    else v = v + n.W[p] / dc[j];
-                }
-                v = v * dc[j];
-                n.psr[p] = v;
-                stage[warp + j * SW_WARPS][lane] = v;
-            }
-        }
-        __syncthreads();
-        if (warp == 0) {
-            int kend = min(SW_ROWS, cnt - kb);
-            for (int kk = 0; kk < kend; kk++) acc = acc + stage[kk][lane];
-        }
-        __syncthreads();
-    }
-    if (warp == 0 && valid) n.sp[d] = acc;
-    // the last tile to finish advances the step and clears the spike list
+    const int nch = (kmax + SW_ROWS - 1) / SW_ROWS;
     if (threadIdx.x == 0) {
+        for (int s = 0; s < SW_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        fence_mbar_init();
+        s_issued = 0;
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int c = 0; c < nch; c++) {
+                const int s = c % SW_STAGES;
+                if (c >= SW_STAGES && !mbar_wait(&empty[s], (uint32_t)((c / SW_STAGES - 1) & 1))) {
+                    set_err(n, ERR_TIMEOUT);
+                    break;
+                }
+                mbar_expect_tx(&full[s], SW_CHUNK_BYTES);
+                tma_load_2d(s_psr[s], &tm_psr, d0, c * SW_ROWS, &full[s]);
+                tma_load_2d(s_cls[s], &tm_cls, d0, c * SW_ROWS, &full[s]);
+                *(volatile int *)&s_issued = c + 1;
+            }
+        }
+        return;
+    }
+
+    float acc = 0.0f;
+    int done = 0;
+    for (int c = 0; c < nch; c++) {
+        const int s = c % SW_STAGES;
+        if (!mbar_wait(&full[s], (uint32_t)((c / SW_STAGES) & 1))) {
+            set_err(n, ERR_TIMEOUT);
+            break;
+        }
+        done = c + 1;
+        float *ps = s_psr[s];
+        const uint8_t *cl = s_cls[s];
+        const int rows = cnt - c * SW_ROWS;  // this lane's in-use rows in the chunk
+#pragma unroll 16
+        for (int kk = 0; kk < SW_ROWS; kk++) {
+            float v = ps[kk * SW_DESTS + lane] * s_dtab[cl[kk * SW_DESTS + lane]];
+            ps[kk * SW_DESTS + lane] = v;
+            if (kk < rows) acc = acc + v;
+        }
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            tma_store_2d(&tm_psr, d0, c * SW_ROWS, ps);
+            bulk_commit();
+            if (c >= 1) {
+                bulk_wait_read1();
+                mbar_arrive(&empty[(c - 1) % SW_STAGES]);
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) bulk_wait_all();
+    __syncwarp();
+    if (done < nch) {
+        // error path: wait (bounded) for the loads already issued before the smem goes away
+        if (lane == 0) {
+            int issued = *(volatile int *)&s_issued;
+            for (int c = done; c < issued; c++)
+                if (!mbar_wait(&full[c % SW_STAGES], (uint32_t)((c / SW_STAGES) & 1))) break;
+        }
+        __syncwarp();
+    }
+
+    if (FUSE) {
+        const unsigned long long t1 = t + 1;
+        bool fired = false;
+        if (valid) {
+            int br = lif_branch(n, d);
+            float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t1, d) : 0.0f;
+            fired = lif_apply(n, d, br, acc, noise, t1);
+            n.sp[d] = 0.0f;
+        }
+        ring_push(n, t1, fired, d);
+    } else if (valid) {
+        n.sp[d] = acc;
+    }
+    // the last tile to finish advances the step counter
+    if (lane == 0) {
         __threadfence();
         unsigned prev = atomicAdd(n.sweep_done, 1u);
         if (prev == gridDim.x - 1) {
             *n.step = t + 1;
-            *n.nspikes = 0;
             *n.sweep_done = 0;
+            if (t + 1 >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
             __threadfence();
         }
     }
 }
 
 // ---- launchers -------------------------------------------------------------------------------
-int fanout_blocks() { return 2 * 152; }
+int deliver_blocks() { return 2 * 152; }
 
-void launch_step(const NetDev &h, const NetDev *d_net, cudaStream_t s)
+void launch_neurons(const NetDev &h, const NetDev *d_net, cudaStream_t s)
 {
     if (h.noise_mode == 1)
         k_neurons_inject<<<1, 1024, 0, s>>>(d_net);
     else
         k_neurons_device<<<(h.N + 255) / 256, 256, 0, s>>>(d_net);
-    k_fanout<<<fanout_blocks(), 256, 0, s>>>(d_net);
-    if (h.syn_kind == 1)
-        k_sweep<1><<<h.ntiles, SW_WARPS * 32, 0, s>>>(d_net);
-    else
-        k_sweep<0><<<h.ntiles, SW_WARPS * 32, 0, s>>>(d_net);
 }
 
-void launch_step_parts(const NetDev &h, const NetDev *d_net, cudaStream_t s, cudaEvent_t ev[4])
+void launch_deliver(const NetDev &h, const NetDev *d_net, cudaStream_t s)
 {
-    cudaEventRecord(ev[0], s);
-    if (h.noise_mode == 1)
-        k_neurons_inject<<<1, 1024, 0, s>>>(d_net);
-    else
-        k_neurons_device<<<(h.N + 255) / 256, 256, 0, s>>>(d_net);
-    cudaEventRecord(ev[1], s);
-    k_fanout<<<fanout_blocks(), 256, 0, s>>>(d_net);
-    cudaEventRecord(ev[2], s);
     if (h.syn_kind == 1)
-        k_sweep<1><<<h.ntiles, SW_WARPS * 32, 0, s>>>(d_net);
+        k_deliver<1><<<deliver_blocks(), 256, 0, s>>>(d_net);
     else
-        k_sweep<0><<<h.ntiles, SW_WARPS * 32, 0, s>>>(d_net);
-    cudaEventRecord(ev[3], s);
+        k_deliver<0><<<deliver_blocks(), 256, 0, s>>>(d_net);
+}
+
+void launch_sweep(const NetDev &h, const NetDev *d_net, const CUtensorMap &tp,
+                  const CUtensorMap &tc, bool fuse, cudaStream_t s)
+{
+    if (h.syn_kind == 1) {
+        if (fuse) k_sweep<1, true><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
+        else k_sweep<1, false><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
+    } else {
+        if (fuse) k_sweep<0, true><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
+        else k_sweep<0, false><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
+    }
 }
 
 }  // namespace bg3
