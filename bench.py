@@ -166,7 +166,8 @@ def run_bg3(args):
     spec, net = build_network()
     N = spec["N"]
     S = net.total_synapses()
-    # warm-up
+    # warm-up: W benchmark steps plus ~0.1 s of plain steps so that clocks have ramped
+    net.step(2000)
     net.bench_steps(args.warmup, FLUSH_BYTES)
     c0 = net.download_lif(fields=("spikeCount",))["spikeCount"].astype(np.int64)
     maps = net.download_maps()
@@ -174,7 +175,7 @@ def run_bg3(args):
         dist.barrier()
     torch.cuda.synchronize()
     clk = ClockSampler(local) if rank == 0 else None
-    ms = net.bench_steps(args.steps, FLUSH_BYTES)
+    ms, km = net.bench_steps(args.steps, FLUSH_BYTES, per_kernel=True)
     torch.cuda.synchronize()
     clocks = clk.stop() if clk else None
     if world > 1:
@@ -188,9 +189,7 @@ def run_bg3(args):
     deliveries = float(((c1 - c0) * maps["outgoingSynapseCount"].astype(np.int64)).sum()) / args.steps
     rate_hz = float((c1 - c0).mean()) / (args.steps * 1e-4)
     value = S * args.steps * world / t_total
-    # roofline of the dominant kernel (the sweep), per-kernel events
-    nk = min(args.steps, 300)
-    _, km = net.bench_steps(nk, FLUSH_BYTES, per_kernel=True)
+    # roofline of the dominant kernel (the sweep): its CUDA-event duration in the timed region
     sweep_ms = float(np.mean(km[:, 2]))
     shares = np.sum(km, axis=0) / np.sum(km)
     peak, peak_kind = peaks()
@@ -310,7 +309,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="bg3", choices=["bg3", "reference"])
     args = ap.parse_args()

@@ -281,11 +281,27 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
         float *ps = s_psr[s];
         const uint8_t *cl = s_cls[s];
         const int rows = cnt - c * SW_ROWS;  // this lane's in-use rows in the chunk
-#pragma unroll 16
-        for (int kk = 0; kk < SW_ROWS; kk++) {
-            float v = ps[kk * SW_DESTS + lane] * s_dtab[cl[kk * SW_DESTS + lane]];
-            ps[kk * SW_DESTS + lane] = v;
-            if (kk < rows) acc = acc + v;
+        // batches of 16 rows: every shared-memory load of a batch is issued before its stores
+        // (the byte loads could alias the float stores, which would serialise each row)
+#pragma unroll 1
+        for (int kb = 0; kb < SW_ROWS; kb += 16) {
+            float pv[16], dv[16];
+            uint32_t cv[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                pv[j] = ps[(kb + j) * SW_DESTS + lane];
+                cv[j] = cl[(kb + j) * SW_DESTS + lane];
+            }
+#pragma unroll
+            for (int j = 0; j < 16; j++) dv[j] = s_dtab[cv[j]];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                float v = pv[j] * dv[j];
+                pv[j] = v;
+                if (kb + j < rows) acc = acc + v;
+            }
+#pragma unroll
+            for (int j = 0; j < 16; j++) ps[(kb + j) * SW_DESTS + lane] = pv[j];
         }
         fence_async_smem();
         __syncwarp();
@@ -338,7 +354,7 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
 }
 
 // ---- launchers -------------------------------------------------------------------------------
-int deliver_blocks() { return 2 * 152; }
+int deliver_blocks() { return 152; }
 
 void launch_neurons(const NetDev &h, const NetDev *d_net, cudaStream_t s)
 {
