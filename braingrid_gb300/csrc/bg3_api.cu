@@ -137,16 +137,19 @@ static int make_tensor_maps(bg3_net *n)
         return BG3_ECUDA;
     auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
     const NetDev &h = n->h;
-    cuuint64_t dims[2] = {(cuuint64_t)h.N, (cuuint64_t)std::max(h.max_syn, 1)};
-    cuuint32_t box[2] = {32, 64};
+    // psr: [Mq quads][N dests x 4 rows] floats, box 16 quads x (32 dests x 4 rows)
+    // class: [Mq quads][N dests] 32-bit words (4 one-byte classes), box 16 quads x 32 dests
+    cuuint64_t dims_f[2] = {(cuuint64_t)h.N * 4, (cuuint64_t)std::max(h.Mq, 1)};
+    cuuint64_t dims_b[2] = {(cuuint64_t)h.N, (cuuint64_t)std::max(h.Mq, 1)};
+    cuuint32_t box_f[2] = {128, 16}, box_b[2] = {32, 16};
     cuuint32_t es[2] = {1, 1};
-    cuuint64_t st_f[1] = {(cuuint64_t)h.Np * 4};
-    cuuint64_t st_b[1] = {(cuuint64_t)h.Np};
-    if (encode(&n->tm_psr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, h.psr, dims, st_f, box, es,
+    cuuint64_t st_f[1] = {(cuuint64_t)h.Np * 16};
+    cuuint64_t st_b[1] = {(cuuint64_t)h.Np * 4};
+    if (encode(&n->tm_psr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, h.psr, dims_f, st_f, box_f, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return BG3_ECUDA;
-    if (encode(&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, h.dcls, dims, st_b, box, es,
+    if (encode(&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, h.dcls, dims_b, st_b, box_b, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return BG3_ECUDA;
@@ -176,7 +179,9 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     const bg3_net_desc &D = *desc;
     if (D.n_neurons <= 0 || D.max_syn_per_neuron < 0 || D.delta_t <= 0 || D.epoch_duration <= 0)
         return BG3_EINVAL;
-    if ((size_t)D.n_neurons * (size_t)D.max_syn_per_neuron >= (1ull << 32)) return BG3_EINVAL;
+    if ((((size_t)D.n_neurons + 31) / 32 * 32) * (((size_t)D.max_syn_per_neuron + 3) / 4 * 4) >=
+        (1ull << 32))
+        return BG3_EINVAL;  // plane positions are 32-bit
     if (D.neuron_kind != BG3_NEURON_LIF) return BG3_EUNSUPPORTED;
     if (D.synapse_kind != BG3_SYN_DS && D.synapse_kind != BG3_SYN_SPIKING) return BG3_EUNSUPPORTED;
     if (D.noise_mode != BG3_NOISE_DEVICE && D.noise_mode != BG3_NOISE_INJECT) return BG3_EINVAL;
@@ -194,10 +199,12 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     memset(&h, 0, sizeof(h));
     const size_t N = (size_t)D.n_neurons;
     const size_t Np = (N + 31) / 32 * 32;
-    const size_t S = Np * (size_t)D.max_syn_per_neuron;
+    const size_t Mq = ((size_t)D.max_syn_per_neuron + 3) / 4;
+    const size_t S = Np * Mq * 4;
     h.N = D.n_neurons;
     h.Np = (int)Np;
     h.max_syn = D.max_syn_per_neuron;
+    h.Mq = (int)Mq;
     h.max_spikes = max_spikes;
     h.neuron_kind = D.neuron_kind;
     h.syn_kind = D.synapse_kind;
@@ -234,8 +241,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
                     F[4] = {0.06f, 0.02f, 1.2f, 0.05f};
         for (int t = 0; t < 4; t++) {
             h.t_tau[t] = tau[t];
-            n->dtab.push_back(expf(-D.delta_t / tau[t]));
-            h.t_dcls[t] = t;
+            h.t_dcls[t] = decay_class(n, expf(-D.delta_t / tau[t]));
             h.t_lcls[t] = delay_class(n, (int)(dly[t] / D.delta_t) + 1);
             if (h.t_lcls[t] < 0) { rc = BG3_EINVAL; goto fail; }
             h.t_U[t] = U[t];
@@ -343,7 +349,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
         !a->delayQueue || !a->delayIdx || !a->total_delay)
         return BG3_EINVAL;
     if (step >= 0xffffff00ull) return BG3_EINVAL;
-    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * M;
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * (size_t)n->h.Mq * 4;
     const bool ds = n->h.syn_kind == BG3_SYN_DS;
     if (ds && (!a->U || !a->D || !a->F || !a->u || !a->r || !a->lastSpike)) return BG3_EINVAL;
     std::vector<float> psr(S, 0.f);
@@ -363,7 +369,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
         if (a->counts && a->counts[d] != c) return BG3_EINVAL;
         count[d] = (uint32_t)c;
         for (size_t k = 0; k < c; k++) {
-            size_t i = d * M + k, p = k * Np + d;
+            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
             int D = a->total_delay[i], di = a->delayIdx[i];
             if (a->src[i] < 0 || (size_t)a->src[i] >= N || a->type[i] < 0 || a->type[i] > 3 ||
                 D < 1 || D > 31 || di < 0 || di > 31)
@@ -397,7 +403,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
     }
     for (size_t d = 0; d < N; d++) {
         for (size_t k = 0; k < count[d]; k++) {
-            size_t i = d * M + k, p = k * Np + d;
+            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
             int D = a->total_delay[i], di = a->delayIdx[i];
             uint32_t f = fired[a->src[i]], q = a->delayQueue[i];
             for (int j = 0; j < D; j++) {
@@ -456,14 +462,14 @@ int bg3_upload_growth(bg3_net *n, const bg3_growth_params *p, const float *radii
 int bg3_upload_weights(bg3_net *n, const float *Wref)
 {
     if (!n || !Wref) return BG3_EINVAL;
-    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * M;
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * (size_t)n->h.Mq * 4;
     std::vector<uint32_t> count(N);
     std::vector<EvSlot> ev(S);
     int rc;
     if ((rc = d2h(n, count.data(), n->h.count, N)) || (rc = d2h(n, ev.data(), n->h.ev, S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     for (size_t d = 0; d < N; d++)
-        for (size_t k = 0; k < count[d]; k++) ev[k * Np + d].W = Wref[d * M + k];
+        for (size_t k = 0; k < count[d]; k++) ev[slot_pos((int)k, (int)d, (int)Np)].W = Wref[d * M + k];
     if ((rc = h2d(n, n->h.ev, ev.data(), S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
@@ -615,7 +621,7 @@ int bg3_download_lif(bg3_net *n, bg3_lif_arrays *a)
 int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
 {
     if (!n || !a) return BG3_EINVAL;
-    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * M;
+    const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * (size_t)n->h.Mq * 4;
     NetDev &h = n->h;
     std::vector<float> psr(S);
     std::vector<uint8_t> dc(S), lc(S);
@@ -643,7 +649,7 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
     for (size_t d = 0; d < N; d++) {
         if (a->counts) a->counts[d] = count[d];
         for (size_t k = 0; k < M; k++) {
-            size_t i = d * M + k, p = k * Np + d;
+            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
             bool used = k < count[d];
             if (a->in_use) a->in_use[i] = used ? 1 : 0;
             if (!used) continue;
@@ -714,8 +720,9 @@ int bg3_download_maps(bg3_net *n, bg3_index_maps *m)
         std::vector<uint32_t> ids;
         for (size_t c = 0; c < C; c++)
             for (uint32_t j = 0; j < oc[c * N + i]; j++) {
-                uint32_t p = om[ob[c * N + i] + j];
-                ids.push_back((uint32_t)((p % Np) * M + p / Np));
+                int k, d;
+                pos_slot(om[ob[c * N + i] + j], (int)Np, k, d);
+                ids.push_back((uint32_t)((size_t)d * M + (size_t)k));
             }
         std::sort(ids.begin(), ids.end());
         if (m->outgoingSynapseBegin) m->outgoingSynapseBegin[i] = acc;

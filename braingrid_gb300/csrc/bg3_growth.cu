@@ -65,10 +65,11 @@ __device__ __forceinline__ float syn_sign(int type) { return (type <= 1) ? -1.0f
 __global__ void k_growth_existing(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    size_t total = (size_t)n.Np * n.max_syn;
+    size_t total = (size_t)n.Np * n.Mq * 4;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
-        int d = (int)(p % n.Np), k = (int)(p / n.Np);
+        int d, k;
+        pos_slot(p, n.Np, k, d);
         if (d >= n.N || k >= (int)n.count[d]) continue;
         int s = n.src[p];
         float a = pair_area(n.xloc[s], n.yloc[s], n.radii[s], n.xloc[d], n.yloc[d], n.radii[d]);
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
     __syncthreads();
     const int c0 = s_count;
     for (int k = threadIdx.x; k < c0; k += blockDim.x) {
-        int s = n.src[(size_t)k * n.Np + d];
+        int s = n.src[slot_pos(k, d, n.Np)];
         atomicOr(&existing[s >> 5], 1u << (s & 31));
     }
     __syncthreads();
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
         if (add) {
             int k = cur + before + __popc(m & ((1u << lane) - 1));
             if (k < n.max_syn) {
-                size_t p = (size_t)k * n.Np + d;
+                size_t p = slot_pos(k, d, n.Np);
                 int type = syn_type(n.ntype[s], td);
                 n.src[p] = s;
                 n.stype[p] = (int8_t)type;
@@ -165,10 +166,11 @@ __global__ void k_out_zero(const NetDev *nets)
 __global__ void k_out_count(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    size_t total = (size_t)n.Np * n.max_syn;
+    size_t total = (size_t)n.Np * n.Mq * 4;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
-        int d = (int)(p % n.Np), k = (int)(p / n.Np);
+        int d, k;
+        pos_slot(p, n.Np, k, d);
         if (d < n.N && k < (int)n.count[d])
             atomicAdd(&n.outCount[(size_t)n.lcls[p] * n.N + n.src[p]], 1u);
     }
@@ -214,10 +216,11 @@ __global__ void __launch_bounds__(1024) k_out_scan(const NetDev *nets)
 __global__ void k_out_fill(const NetDev *nets)
 {
     const NetDev &n = nets[0];
-    size_t total = (size_t)n.Np * n.max_syn;
+    size_t total = (size_t)n.Np * n.Mq * 4;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
-        int d = (int)(p % n.Np), k = (int)(p / n.Np);
+        int d, k;
+        pos_slot(p, n.Np, k, d);
         if (d >= n.N || k >= (int)n.count[d]) continue;
         size_t key = (size_t)n.lcls[p] * n.N + n.src[p];
         uint32_t slot = n.outBegin[key] + atomicAdd(&n.outFill[key], 1u);

@@ -3,10 +3,12 @@
 // HBM layout of one network (arrays owned by bg3_net, allocated once at bg3_create):
 //
 //   neurons               SoA float/int arrays, neuron index contiguous.
-//   synapse slot planes   slot (dest d, row k) lives at p = k * Np + d, Np = N rounded up to 32
-//                         ("ELL" order): one row of a 32-dest tile is 128 contiguous bytes of psr,
-//                         so the sweep moves [64 rows x 32 dests] tiles with 2-D TMA copies.  The
-//                         reference slot id of (d, k) is d * maxSyn + k.
+//   synapse slot planes   slot (dest d, row k) lives at p = ((k / 4) * Np + d) * 4 + k % 4,
+//                         Np = N rounded up to 32: ELL order with each dest's rows interleaved in
+//                         groups of four ("row quads"), so one 16-byte load gives a lane four
+//                         consecutive rows of its dest, and a 32-dest tile of 64 rows is a
+//                         [16 quads x 512 B] box for a 2-D TMA copy.  The reference slot id of
+//                         (d, k) is d * maxSyn + k.
 //   hot per-slot state    psr (f32) and a one-byte decay class (index into a per-network table
 //                         of decay factors): 9 bytes per synapse per step.
 //   event per-slot state  EvSlot (32 B, one sector): W, U, D, F, u, r, last spike step, birth
@@ -35,8 +37,21 @@ struct __align__(32) EvSlot {
     uint32_t born;   // step at which the synapse was created (low 32 bits)
 };
 
+// plane position of slot (dest d, row k) and its inverse
+__host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Np)
+{
+    return ((((size_t)(k >> 2)) * (size_t)Np + (size_t)d) << 2) | (size_t)(k & 3);
+}
+__host__ __device__ __forceinline__ void pos_slot(size_t p, int Np, int &k, int &d)
+{
+    size_t q = p >> 2;
+    d = (int)(q % (size_t)Np);
+    k = (int)((q / (size_t)Np) << 2) | (int)(p & 3);
+}
+
 struct NetDev {
     int32_t N, Np, max_syn, max_spikes, neuron_kind, syn_kind, noise_mode;
+    int32_t Mq;                    // row quads per dest: ceil(max_syn / 4)
     float dt, epoch_duration;
     uint32_t noise_seed;
     int32_t ntiles;                // sweep tiles of 32 dests
@@ -52,7 +67,7 @@ struct NetDev {
     int8_t *ntype;                 // 1 INH, 2 EXC
     // spike ring: ids of the neurons that fired at step t are ring[(t & 63) * N + i]
     int32_t *ring, *ring_n;
-    // synapse planes (index k * Np + d)
+    // synapse planes (index slot_pos(k, d, Np), Mq * Np * 4 entries)
     float *psr;
     uint8_t *dcls;                 // decay class
     uint8_t *lcls;                 // delay class

@@ -212,15 +212,18 @@ __global__ void __launch_bounds__(256) k_deliver(const NetDev *nets)
 // ---- synapse sweep ---------------------------------------------------------------------------
 constexpr int SW_DESTS = 32;   // dests per tile (one per consumer lane)
 constexpr int SW_ROWS = 64;    // slot rows per TMA chunk
+constexpr int SW_QUADS = SW_ROWS / 4;
 constexpr int SW_STAGES = 4;   // chunks in flight per tile
 constexpr uint32_t SW_CHUNK_BYTES = SW_ROWS * SW_DESTS * (4 + 1);
 
 // AllSpikingSynapses::advanceSynapse's "psr *= decay" for every in-use synapse, and the
 // summation of AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331):
 // sp[d] = ((0 + psr_0) + psr_1) + ... in slot order, the reference's accumulation order.
-// Warp 0 lane 0 streams [64 rows x 32 dests] chunks of psr and of the decay class into a 4-stage
-// shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales each chunk in place,
-// adds it in row order, and writes it back with a TMA store.  FUSE: the epilogue integrates the
+// Warp 0 lane 0 streams chunks of 64 rows x 32 dests (16 row quads) of psr and of the decay
+// class into a 4-stage shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales
+// each chunk in place, adds it in row order, and writes it back with a TMA store.  Rows past a
+// dest's in-use count hold +0.0f (never written otherwise), and adding +0.0f leaves a sum that
+// started at +0.0f unchanged, so every lane adds all 64 rows.  FUSE: the epilogue integrates the
 // tile's neurons for step t + 1 (device-noise mode).
 template <int SYN, bool FUSE>
 __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
@@ -261,8 +264,8 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
                     break;
                 }
                 mbar_expect_tx(&full[s], SW_CHUNK_BYTES);
-                tma_load_2d(s_psr[s], &tm_psr, d0, c * SW_ROWS, &full[s]);
-                tma_load_2d(s_cls[s], &tm_cls, d0, c * SW_ROWS, &full[s]);
+                tma_load_2d(s_psr[s], &tm_psr, d0 * 4, c * SW_QUADS, &full[s]);
+                tma_load_2d(s_cls[s], &tm_cls, d0, c * SW_QUADS, &full[s]);
                 *(volatile int *)&s_issued = c + 1;
             }
         }
@@ -278,35 +281,41 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
             break;
         }
         done = c + 1;
-        float *ps = s_psr[s];
-        const uint8_t *cl = s_cls[s];
-        const int rows = cnt - c * SW_ROWS;  // this lane's in-use rows in the chunk
-        // batches of 16 rows: every shared-memory load of a batch is issued before its stores
-        // (the byte loads could alias the float stores, which would serialise each row)
+        float4 *ps4 = reinterpret_cast<float4 *>(s_psr[s]);                 // [16 quads][32]
+        const uint32_t *cw = reinterpret_cast<const uint32_t *>(s_cls[s]);  // [16 quads][32]
+        // batches of 4 quads (16 rows): all loads of a batch, then the math, then the stores
 #pragma unroll 1
-        for (int kb = 0; kb < SW_ROWS; kb += 16) {
-            float pv[16], dv[16];
-            uint32_t cv[16];
+        for (int gb = 0; gb < SW_QUADS; gb += 4) {
+            float4 pv[4];
+            uint32_t cv[4];
+            float dv[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                pv[j] = ps[(kb + j) * SW_DESTS + lane];
-                cv[j] = cl[(kb + j) * SW_DESTS + lane];
+            for (int j = 0; j < 4; j++) {
+                pv[j] = ps4[(gb + j) * SW_DESTS + lane];
+                cv[j] = cw[(gb + j) * SW_DESTS + lane];
             }
 #pragma unroll
-            for (int j = 0; j < 16; j++) dv[j] = s_dtab[cv[j]];
+            for (int j = 0; j < 4; j++)
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                float v = pv[j] * dv[j];
-                pv[j] = v;
-                if (kb + j < rows) acc = acc + v;
+                for (int b = 0; b < 4; b++) dv[4 * j + b] = s_dtab[(cv[j] >> (8 * b)) & 0xffu];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                pv[j].x = pv[j].x * dv[4 * j + 0];
+                acc = acc + pv[j].x;
+                pv[j].y = pv[j].y * dv[4 * j + 1];
+                acc = acc + pv[j].y;
+                pv[j].z = pv[j].z * dv[4 * j + 2];
+                acc = acc + pv[j].z;
+                pv[j].w = pv[j].w * dv[4 * j + 3];
+                acc = acc + pv[j].w;
             }
 #pragma unroll
-            for (int j = 0; j < 16; j++) ps[(kb + j) * SW_DESTS + lane] = pv[j];
+            for (int j = 0; j < 4; j++) ps4[(gb + j) * SW_DESTS + lane] = pv[j];
         }
         fence_async_smem();
         __syncwarp();
         if (lane == 0) {
-            tma_store_2d(&tm_psr, d0, c * SW_ROWS, ps);
+            tma_store_2d(&tm_psr, d0 * 4, c * SW_QUADS, s_psr[s]);
             bulk_commit();
             if (c >= 1) {
                 bulk_wait_read1();
