@@ -795,7 +795,7 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
     }
     const NetDev &h = n->h;
     const bool inject = h.noise_mode == BG3_NOISE_INJECT;
-    std::vector<cudaEvent_t> ev((size_t)nsteps * 4);
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 3);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     for (int64_t s = 0; s < nsteps; s++) {
         if (flush_bytes > 0) {
@@ -806,24 +806,29 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
                                                    (size_t)flush_bytes / 16,
                                                    (float *)((char *)n->scrub_buf + flush_bytes));
         }
-        cudaEvent_t *e = &ev[(size_t)s * 4];
+        // three events per step: [neurons (injected-noise mode)] deliver | sweep; in device-noise
+        // mode the neuron pass runs in the previous sweep's epilogue (standalone before step 0)
+        cudaEvent_t *e = &ev[(size_t)s * 3];
         const bool last = s == nsteps - 1;
+        if (!inject && s == 0) bg3::launch_neurons(h, n->d, n->stream);
         CK(cudaEventRecord(e[0], n->stream));
-        if (inject || s == 0) bg3::launch_neurons(h, n->d, n->stream);
-        CK(cudaEventRecord(e[1], n->stream));
+        if (inject) bg3::launch_neurons(h, n->d, n->stream);
         bg3::launch_deliver(h, n->d, n->stream);
-        CK(cudaEventRecord(e[2], n->stream));
+        CK(cudaEventRecord(e[1], n->stream));
         bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, !inject && !last, n->stream);
-        CK(cudaEventRecord(e[3], n->stream));
+        CK(cudaEventRecord(e[2], n->stream));
     }
     n->launches += (inject ? 3 : 2) * nsteps + (inject ? 0 : 1);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(n->stream));
     for (int64_t s = 0; s < nsteps; s++) {
-        cudaEvent_t *e = &ev[(size_t)s * 4];
-        CK(cudaEventElapsedTime(&step_ms[s], e[0], e[3]));
-        if (kernel_ms)
-            for (int k = 0; k < 3; k++) CK(cudaEventElapsedTime(&kernel_ms[3 * s + k], e[k], e[k + 1]));
+        cudaEvent_t *e = &ev[(size_t)s * 3];
+        CK(cudaEventElapsedTime(&step_ms[s], e[0], e[2]));
+        if (kernel_ms) {
+            kernel_ms[3 * s] = 0.0f;
+            CK(cudaEventElapsedTime(&kernel_ms[3 * s + 1], e[0], e[1]));
+            CK(cudaEventElapsedTime(&kernel_ms[3 * s + 2], e[1], e[2]));
+        }
     }
     for (auto &e : ev) cudaEventDestroy(e);
     return BG3_OK;

@@ -186,8 +186,10 @@ int bg3_kernel_times(bg3_net *net, float *ms_neurons, float *ms_fanout, float *m
 /* Benchmark helper: runs nsteps steps on the handle's stream.  Before each step, when
  * flush_bytes > 0, a scratch buffer of that size is overwritten so that the step starts with a
  * cold L2.  The device time of each step (CUDA events on the handle's stream, flush excluded) is
- * written to step_ms[nsteps]; when kernel_ms is not NULL, the three kernels of each step are
- * timed separately into kernel_ms[3 * nsteps] (neurons, fan-out, sweep). */
+ * written to step_ms[nsteps]; when kernel_ms is not NULL, each step's phases go to
+ * kernel_ms[3 * s .. 3 * s + 2]: 0, spike delivery (plus the neuron pass in injected-noise mode),
+ * and the sweep (whose epilogue runs the next step's neuron pass in device-noise mode).  The
+ * standalone neuron pass before step 0 is not timed. */
 int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *step_ms,
                     float *kernel_ms);
 
