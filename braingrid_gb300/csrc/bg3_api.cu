@@ -13,10 +13,10 @@
 #include "bg3_internal.cuh"
 
 namespace bg3 {
-void launch_neurons(const NetDev &h, const NetDev *d_net, cudaStream_t s);
-void launch_deliver(const NetDev &h, const NetDev *d_net, cudaStream_t s);
-void launch_sweep(const NetDev &h, const NetDev *d_net, const CUtensorMap &tp,
-                  const CUtensorMap &tc, bool fuse, cudaStream_t s);
+void launch_neurons(const NetDev &h, cudaStream_t s);
+void launch_deliver(const NetDev &h, cudaStream_t s);
+void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
+                  cudaStream_t s);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
@@ -67,8 +67,12 @@ static int dalloc(bg3_net *n, T **p, size_t count, int fill = 0)
     return BG3_OK;
 }
 
+static void drop_graph(bg3_net *n);
+// The step kernels take the descriptor by value (captured into the step graph); the growth
+// kernels read the device copy.  Any change drops the captured graph.
 static int push_desc(bg3_net *n)
 {
+    drop_graph(n);
     CK(cudaMemcpyAsync(n->d, &n->h, sizeof(NetDev), cudaMemcpyHostToDevice, n->stream));
     return BG3_OK;
 }
@@ -518,22 +522,22 @@ static int run_steps(bg3_net *n, int64_t nsteps)
     const NetDev &h = n->h;
     if (h.noise_mode == BG3_NOISE_INJECT) {
         for (int64_t s = 0; s < nsteps; s++) {
-            bg3::launch_neurons(h, n->d, n->stream);
-            bg3::launch_deliver(h, n->d, n->stream);
-            bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, false, n->stream);
+            bg3::launch_neurons(h, n->stream);
+            bg3::launch_deliver(h, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->stream);
         }
         n->launches += 3 * nsteps;
         CK(cudaGetLastError());
         return BG3_OK;
     }
-    bg3::launch_neurons(h, n->d, n->stream);
+    bg3::launch_neurons(h, n->stream);
     int64_t interior = nsteps - 1;
     if (interior >= GRAPH_STEPS && !n->graph) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < GRAPH_STEPS; i++) {
-            bg3::launch_deliver(h, n->d, n->stream);
-            bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, true, n->stream);
+            bg3::launch_deliver(h, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->stream);
         }
         CK(cudaStreamEndCapture(n->stream, &g));
         cudaError_t e = cudaGraphInstantiate(&n->graph, g, 0);
@@ -545,11 +549,11 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         interior -= GRAPH_STEPS;
     }
     for (int64_t i = 0; i < interior; i++) {
-        bg3::launch_deliver(h, n->d, n->stream);
-        bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, true, n->stream);
+        bg3::launch_deliver(h, n->stream);
+        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->stream);
     }
-    bg3::launch_deliver(h, n->d, n->stream);
-    bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, false, n->stream);
+    bg3::launch_deliver(h, n->stream);
+    bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->stream);
     n->launches += 1 + 2 * nsteps;
     CK(cudaGetLastError());
     return BG3_OK;
@@ -810,12 +814,12 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
         // mode the neuron pass runs in the previous sweep's epilogue (standalone before step 0)
         cudaEvent_t *e = &ev[(size_t)s * 3];
         const bool last = s == nsteps - 1;
-        if (!inject && s == 0) bg3::launch_neurons(h, n->d, n->stream);
+        if (!inject && s == 0) bg3::launch_neurons(h, n->stream);
         CK(cudaEventRecord(e[0], n->stream));
-        if (inject) bg3::launch_neurons(h, n->d, n->stream);
-        bg3::launch_deliver(h, n->d, n->stream);
-        CK(cudaEventRecord(e[1], n->stream));
-        bg3::launch_sweep(h, n->d, n->tm_psr, n->tm_cls, !inject && !last, n->stream);
+        if (inject) bg3::launch_neurons(h, n->stream);
+        bg3::launch_deliver(h, n->stream);
+        if (kernel_ms) CK(cudaEventRecord(e[1], n->stream));
+        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, !inject && !last, n->stream);
         CK(cudaEventRecord(e[2], n->stream));
     }
     n->launches += (inject ? 3 : 2) * nsteps + (inject ? 0 : 1);

@@ -11,6 +11,7 @@
 //   k_neurons_*  (t)  standalone neuron integration: the first step of a bg3_step call and every
 //                     step in injected-noise mode (the noise order needs a scan over all neurons).
 #include <cuda.h>
+#include <utility>
 #include "bg3_internal.cuh"
 
 namespace bg3 {
@@ -79,12 +80,15 @@ __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Programmatic dependent launch: wait for the preceding kernel of the stream (and its memory),
+// and allow the next kernel of the stream to be scheduled early.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // ---- standalone neuron kernels ---------------------------------------------------------------
 // Device-noise mode: one N(0,1) draw per neuron per step, keyed by (seed, step, neuron).
-__global__ void __launch_bounds__(256) k_neurons_device(const NetDev *nets)
+__global__ void __launch_bounds__(256) k_neurons_device(const __grid_constant__ NetDev n)
 {
-    const NetDev &n = nets[0];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long t = *n.step;
     bool fired = false;
@@ -101,9 +105,8 @@ __global__ void __launch_bounds__(256) k_neurons_device(const NetDev *nets)
 // neurons from N-1 down to 0 (Neurons/AllSpikingNeurons.cpp:104).  One CTA walks the neurons in
 // chunks of 1024 from the top; a block scan of the "integrates" flags gives each neuron the
 // number of integrating neurons above it, i.e. its position in the stream.
-__global__ void __launch_bounds__(1024) k_neurons_inject(const NetDev *nets)
+__global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__ NetDev n)
 {
-    const NetDev &n = nets[0];
     __shared__ int warp_tot[32];
     __shared__ long long s_running;
     unsigned long long t = *n.step;
@@ -184,9 +187,10 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
 // of the class.  Each synapse has one source, which fires at most once per step, so no two
 // lanes touch one slot.  Block 0 also clears ring slot t + 1 for the next neuron pass.
 template <int SYN>
-__global__ void __launch_bounds__(256) k_deliver(const NetDev *nets)
+__global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev n)
 {
-    const NetDev &n = nets[0];
+    pdl_wait();  // the previous sweep (step counter, spike ring, psr) must be complete
+    pdl_trigger();
     const unsigned long long t = *n.step;
     if (blockIdx.x == 0 && threadIdx.x == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
     const int lane = threadIdx.x & 31;
@@ -213,34 +217,41 @@ __global__ void __launch_bounds__(256) k_deliver(const NetDev *nets)
 constexpr int SW_DESTS = 32;   // dests per tile (one per consumer lane)
 constexpr int SW_ROWS = 64;    // slot rows per TMA chunk
 constexpr int SW_QUADS = SW_ROWS / 4;
-constexpr int SW_STAGES = 4;   // chunks in flight per tile
-constexpr uint32_t SW_CHUNK_BYTES = SW_ROWS * SW_DESTS * (4 + 1);
+constexpr int SW_STAGES = 8;   // chunks in flight per tile
+constexpr uint32_t SW_PSR_BYTES = SW_ROWS * SW_DESTS * 4;
+constexpr uint32_t SW_CLS_BYTES = SW_ROWS * SW_DESTS;
+constexpr uint32_t SW_CHUNK_BYTES = SW_PSR_BYTES + SW_CLS_BYTES;
+// dynamic shared memory: stages (psr | class), decay table, barriers; +128 for alignment
+constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4 +
+                           2 * SW_STAGES * 8 + 16 + 128;
 
 // AllSpikingSynapses::advanceSynapse's "psr *= decay" for every in-use synapse, and the
 // summation of AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331):
 // sp[d] = ((0 + psr_0) + psr_1) + ... in slot order, the reference's accumulation order.
 // Warp 0 lane 0 streams chunks of 64 rows x 32 dests (16 row quads) of psr and of the decay
-// class into a 4-stage shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales
+// class into an 8-stage shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales
 // each chunk in place, adds it in row order, and writes it back with a TMA store.  Rows past a
 // dest's in-use count hold +0.0f (never written otherwise), and adding +0.0f leaves a sum that
 // started at +0.0f unchanged, so every lane adds all 64 rows.  FUSE: the epilogue integrates the
-// tile's neurons for step t + 1 (device-noise mode).
+// tile's neurons for step t + 1 (device-noise mode).  The prologue (barriers, decay table, row
+// counts) overlaps the previous kernel's tail; the step's data is touched after pdl_wait().
 template <int SYN, bool FUSE>
-__global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
+__global__ void __launch_bounds__(64) k_sweep(const __grid_constant__ NetDev n,
                                               const __grid_constant__ CUtensorMap tm_psr,
                                               const __grid_constant__ CUtensorMap tm_cls)
 {
-    const NetDev &n = nets[0];
-    __shared__ __align__(128) float s_psr[SW_STAGES][SW_ROWS * SW_DESTS];
-    __shared__ __align__(128) uint8_t s_cls[SW_STAGES][SW_ROWS * SW_DESTS];
-    __shared__ float s_dtab[BG3_MAX_DCLS];
-    __shared__ __align__(8) uint64_t full[SW_STAGES], empty[SW_STAGES];
-    __shared__ int s_issued;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+    float *s_dtab = (float *)(smem + (size_t)SW_STAGES * SW_CHUNK_BYTES);
+    uint64_t *full = (uint64_t *)(s_dtab + BG3_MAX_DCLS);
+    uint64_t *empty = full + SW_STAGES;
+    int *s_issued = (int *)(empty + SW_STAGES);
+    auto st_psr = [&](int s) { return (float *)(smem + (size_t)s * SW_CHUNK_BYTES); };
+    auto st_cls = [&](int s) { return smem + (size_t)s * SW_CHUNK_BYTES + SW_PSR_BYTES; };
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int d0 = blockIdx.x * SW_DESTS;
     const int d = d0 + lane;
     const bool valid = d < n.N;
-    const unsigned long long t = *n.step;
     for (int i = threadIdx.x; i < n.n_dcls; i += blockDim.x) s_dtab[i] = n.dtab[i];
     const int cnt = valid ? (int)n.count[d] : 0;
     const int kmax = __reduce_max_sync(0xffffffffu, cnt);
@@ -251,9 +262,12 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
             mbar_init(&empty[s], 1);
         }
         fence_mbar_init();
-        s_issued = 0;
+        *s_issued = 0;
     }
     __syncthreads();
+    pdl_wait();  // spike delivery for this step has finished writing psr
+    pdl_trigger();
+    const unsigned long long t = *n.step;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -264,9 +278,9 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
                     break;
                 }
                 mbar_expect_tx(&full[s], SW_CHUNK_BYTES);
-                tma_load_2d(s_psr[s], &tm_psr, d0 * 4, c * SW_QUADS, &full[s]);
-                tma_load_2d(s_cls[s], &tm_cls, d0, c * SW_QUADS, &full[s]);
-                *(volatile int *)&s_issued = c + 1;
+                tma_load_2d(st_psr(s), &tm_psr, d0 * 4, c * SW_QUADS, &full[s]);
+                tma_load_2d(st_cls(s), &tm_cls, d0, c * SW_QUADS, &full[s]);
+                *(volatile int *)s_issued = c + 1;
             }
         }
         return;
@@ -281,8 +295,8 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
             break;
         }
         done = c + 1;
-        float4 *ps4 = reinterpret_cast<float4 *>(s_psr[s]);                 // [16 quads][32]
-        const uint32_t *cw = reinterpret_cast<const uint32_t *>(s_cls[s]);  // [16 quads][32]
+        float4 *ps4 = reinterpret_cast<float4 *>(st_psr(s));                 // [16 quads][32]
+        const uint32_t *cw = reinterpret_cast<const uint32_t *>(st_cls(s));  // [16 quads][32]
         // batches of 4 quads (16 rows): all loads of a batch, then the math, then the stores
 #pragma unroll 1
         for (int gb = 0; gb < SW_QUADS; gb += 4) {
@@ -315,7 +329,7 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
         fence_async_smem();
         __syncwarp();
         if (lane == 0) {
-            tma_store_2d(&tm_psr, d0 * 4, c * SW_QUADS, s_psr[s]);
+            tma_store_2d(&tm_psr, d0 * 4, c * SW_QUADS, st_psr(s));
             bulk_commit();
             if (c >= 1) {
                 bulk_wait_read1();
@@ -329,7 +343,7 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
     if (done < nch) {
         // error path: wait (bounded) for the loads already issued before the smem goes away
         if (lane == 0) {
-            int issued = *(volatile int *)&s_issued;
+            int issued = *(volatile int *)s_issued;
             for (int c = done; c < issued; c++)
                 if (!mbar_wait(&full[c % SW_STAGES], (uint32_t)((c / SW_STAGES) & 1))) break;
         }
@@ -365,31 +379,57 @@ __global__ void __launch_bounds__(64) k_sweep(const NetDev *nets,
 // ---- launchers -------------------------------------------------------------------------------
 int deliver_blocks() { return 152; }
 
-void launch_neurons(const NetDev &h, const NetDev *d_net, cudaStream_t s)
+void launch_neurons(const NetDev &h, cudaStream_t s)
 {
     if (h.noise_mode == 1)
-        k_neurons_inject<<<1, 1024, 0, s>>>(d_net);
+        k_neurons_inject<<<1, 1024, 0, s>>>(h);
     else
-        k_neurons_device<<<(h.N + 255) / 256, 256, 0, s>>>(d_net);
+        k_neurons_device<<<(h.N + 255) / 256, 256, 0, s>>>(h);
 }
 
-void launch_deliver(const NetDev &h, const NetDev *d_net, cudaStream_t s)
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                       Args &&...args)
 {
-    if (h.syn_kind == 1)
-        k_deliver<1><<<deliver_blocks(), 256, 0, s>>>(d_net);
-    else
-        k_deliver<0><<<deliver_blocks(), 256, 0, s>>>(d_net);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
-void launch_sweep(const NetDev &h, const NetDev *d_net, const CUtensorMap &tp,
-                  const CUtensorMap &tc, bool fuse, cudaStream_t s)
+void launch_deliver(const NetDev &h, cudaStream_t s)
+{
+    if (h.syn_kind == 1) launch_pdl(k_deliver<1>, deliver_blocks(), 256, 0, s, h);
+    else launch_pdl(k_deliver<0>, deliver_blocks(), 256, 0, s, h);
+}
+
+template <int SYN, bool FUSE>
+static void launch_sweep_t(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, cudaStream_t s)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sweep<SYN, FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
+        attr_set = true;
+    }
+    launch_pdl(k_sweep<SYN, FUSE>, h.ntiles, 64, SW_SMEM, s, h, tp, tc);
+}
+
+void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
+                  cudaStream_t s)
 {
     if (h.syn_kind == 1) {
-        if (fuse) k_sweep<1, true><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
-        else k_sweep<1, false><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
+        if (fuse) launch_sweep_t<1, true>(h, tp, tc, s);
+        else launch_sweep_t<1, false>(h, tp, tc, s);
     } else {
-        if (fuse) k_sweep<0, true><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
-        else k_sweep<0, false><<<h.ntiles, 64, 0, s>>>(d_net, tp, tc);
+        if (fuse) launch_sweep_t<0, true>(h, tp, tc, s);
+        else launch_sweep_t<0, false>(h, tp, tc, s);
     }
 }
 

@@ -188,7 +188,8 @@ int bg3_kernel_times(bg3_net *net, float *ms_neurons, float *ms_fanout, float *m
  * cold L2.  The device time of each step (CUDA events on the handle's stream, flush excluded) is
  * written to step_ms[nsteps]; when kernel_ms is not NULL, each step's phases go to
  * kernel_ms[3 * s .. 3 * s + 2]: 0, spike delivery (plus the neuron pass in injected-noise mode),
- * and the sweep (whose epilogue runs the next step's neuron pass in device-noise mode).  The
+ * and the sweep (whose epilogue runs the next step's neuron pass in device-noise mode); that
+ * extra event between the two phases is recorded only when kernel_ms is not NULL.  The
  * standalone neuron pass before step 0 is not timed. */
 int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *step_ms,
                     float *kernel_ms);
