@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev 
 constexpr int SW_DESTS = 32;   // dests per tile (one per consumer lane)
 constexpr int SW_ROWS = 64;    // slot rows per TMA chunk
 constexpr int SW_QUADS = SW_ROWS / 4;
-constexpr int SW_STAGES = 8;   // chunks in flight per tile
+constexpr int SW_STAGES = 6;   // chunks in flight per tile (63 KB: three CTAs per SM)
 constexpr uint32_t SW_PSR_BYTES = SW_ROWS * SW_DESTS * 4;
 constexpr uint32_t SW_CLS_BYTES = SW_ROWS * SW_DESTS;
 constexpr uint32_t SW_CHUNK_BYTES = SW_PSR_BYTES + SW_CLS_BYTES;
@@ -229,7 +229,7 @@ constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4
 // summation of AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331):
 // sp[d] = ((0 + psr_0) + psr_1) + ... in slot order, the reference's accumulation order.
 // Warp 0 lane 0 streams chunks of 64 rows x 32 dests (16 row quads) of psr and of the decay
-// class into an 8-stage shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales
+// class into a 6-stage shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales
 // each chunk in place, adds it in row order, and writes it back with a TMA store.  Rows past a
 // dest's in-use count hold +0.0f (never written otherwise), and adding +0.0f leaves a sum that
 // started at +0.0f unchanged, so every lane adds all 64 rows.  FUSE: the epilogue integrates the
