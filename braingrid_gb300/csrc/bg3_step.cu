@@ -214,37 +214,45 @@ __global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev 
 }
 
 // ---- synapse sweep ---------------------------------------------------------------------------
-constexpr int SW_DESTS = 32;   // dests per tile (one per consumer lane)
+constexpr int SW_DESTS = 32;   // dests per tile (one per lane)
 constexpr int SW_ROWS = 64;    // slot rows per TMA chunk
 constexpr int SW_QUADS = SW_ROWS / 4;
 constexpr int SW_STAGES = 6;   // chunks in flight per tile (63 KB: three CTAs per SM)
+constexpr int SW_SCALE_WARPS = 4;
+constexpr int SW_THREADS = 32 * (2 + SW_SCALE_WARPS);
 constexpr uint32_t SW_PSR_BYTES = SW_ROWS * SW_DESTS * 4;
 constexpr uint32_t SW_CLS_BYTES = SW_ROWS * SW_DESTS;
 constexpr uint32_t SW_CHUNK_BYTES = SW_PSR_BYTES + SW_CLS_BYTES;
 // dynamic shared memory: stages (psr | class), decay table, barriers; +128 for alignment
 constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4 +
-                           2 * SW_STAGES * 8 + 16 + 128;
+                           3 * SW_STAGES * 8 + 16 + 128;
 
 // AllSpikingSynapses::advanceSynapse's "psr *= decay" for every in-use synapse, and the
 // summation of AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331):
 // sp[d] = ((0 + psr_0) + psr_1) + ... in slot order, the reference's accumulation order.
-// Warp 0 lane 0 streams chunks of 64 rows x 32 dests (16 row quads) of psr and of the decay
-// class into a 6-stage shared-memory ring with 2-D TMA loads; warp 1 (one lane per dest) scales
-// each chunk in place, adds it in row order, and writes it back with a TMA store.  Rows past a
-// dest's in-use count hold +0.0f (never written otherwise), and adding +0.0f leaves a sum that
-// started at +0.0f unchanged, so every lane adds all 64 rows.  FUSE: the epilogue integrates the
-// tile's neurons for step t + 1 (device-noise mode).  The prologue (barriers, decay table, row
-// counts) overlaps the previous kernel's tail; the step's data is touched after pdl_wait().
+//
+// One CTA per tile of 32 dests, three warp roles over a 6-stage shared-memory ring of chunks
+// (64 rows x 32 dests = 16 row quads of psr and of the decay class):
+//   warp 0      lane 0 issues the 2-D TMA loads of each chunk (mbarrier full[s]);
+//   warps 1-4   scale 4 quads each in place, psr *= decay[class] (then arrive on scaled[s]);
+//   warp 5      adds the 64 rows of each chunk in row order (one lane per dest), writes the chunk
+//               back with a TMA store and releases the stage (empty[s]); its epilogue stores the
+//               sums, or with FUSE integrates the tile's neurons for step t + 1.
+// Rows past a dest's in-use count hold +0.0f (never written otherwise), and adding +0.0f leaves
+// a sum that started at +0.0f unchanged, so the sum warp adds all 64 rows of every chunk.  The
+// prologue overlaps the previous kernel's tail; the step's data is touched after pdl_wait().
+// Every mbarrier wait is bounded (about 1 s); on expiry the error word is set and the CTA drains.
 template <int SYN, bool FUSE>
-__global__ void __launch_bounds__(64) k_sweep(const __grid_constant__ NetDev n,
-                                              const __grid_constant__ CUtensorMap tm_psr,
-                                              const __grid_constant__ CUtensorMap tm_cls)
+__global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ NetDev n,
+                                                      const __grid_constant__ CUtensorMap tm_psr,
+                                                      const __grid_constant__ CUtensorMap tm_cls)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     float *s_dtab = (float *)(smem + (size_t)SW_STAGES * SW_CHUNK_BYTES);
     uint64_t *full = (uint64_t *)(s_dtab + BG3_MAX_DCLS);
-    uint64_t *empty = full + SW_STAGES;
+    uint64_t *scaled = full + SW_STAGES;
+    uint64_t *empty = scaled + SW_STAGES;
     int *s_issued = (int *)(empty + SW_STAGES);
     auto st_psr = [&](int s) { return (float *)(smem + (size_t)s * SW_CHUNK_BYTES); };
     auto st_cls = [&](int s) { return smem + (size_t)s * SW_CHUNK_BYTES + SW_PSR_BYTES; };
@@ -259,6 +267,7 @@ __global__ void __launch_bounds__(64) k_sweep(const __grid_constant__ NetDev n,
     if (threadIdx.x == 0) {
         for (int s = 0; s < SW_STAGES; s++) {
             mbar_init(&full[s], 1);
+            mbar_init(&scaled[s], SW_SCALE_WARPS);
             mbar_init(&empty[s], 1);
         }
         fence_mbar_init();
@@ -269,7 +278,7 @@ __global__ void __launch_bounds__(64) k_sweep(const __grid_constant__ NetDev n,
     pdl_trigger();
     const unsigned long long t = *n.step;
 
-    if (warp == 0) {
+    if (warp == 0) {  // ---------------------------------------------------------- producer
         if (lane == 0) {
             for (int c = 0; c < nch; c++) {
                 const int s = c % SW_STAGES;
@@ -286,47 +295,60 @@ __global__ void __launch_bounds__(64) k_sweep(const __grid_constant__ NetDev n,
         return;
     }
 
+    if (warp <= SW_SCALE_WARPS) {  // --------------------------------------------- scale warps
+        const int q0 = (warp - 1) * (SW_QUADS / SW_SCALE_WARPS);
+        for (int c = 0; c < nch; c++) {
+            const int s = c % SW_STAGES;
+            if (!mbar_wait(&full[s], (uint32_t)((c / SW_STAGES) & 1))) {
+                set_err(n, ERR_TIMEOUT);
+                break;
+            }
+            float4 *ps4 = reinterpret_cast<float4 *>(st_psr(s));                 // [16 quads][32]
+            const uint32_t *cw = reinterpret_cast<const uint32_t *>(st_cls(s));  // [16 quads][32]
+            float4 pv[SW_QUADS / SW_SCALE_WARPS];
+            uint32_t cv[SW_QUADS / SW_SCALE_WARPS];
+#pragma unroll
+            for (int j = 0; j < SW_QUADS / SW_SCALE_WARPS; j++) {
+                pv[j] = ps4[(q0 + j) * SW_DESTS + lane];
+                cv[j] = cw[(q0 + j) * SW_DESTS + lane];
+            }
+#pragma unroll
+            for (int j = 0; j < SW_QUADS / SW_SCALE_WARPS; j++) {
+                pv[j].x = pv[j].x * s_dtab[cv[j] & 0xffu];
+                pv[j].y = pv[j].y * s_dtab[(cv[j] >> 8) & 0xffu];
+                pv[j].z = pv[j].z * s_dtab[(cv[j] >> 16) & 0xffu];
+                pv[j].w = pv[j].w * s_dtab[cv[j] >> 24];
+            }
+#pragma unroll
+            for (int j = 0; j < SW_QUADS / SW_SCALE_WARPS; j++) ps4[(q0 + j) * SW_DESTS + lane] = pv[j];
+            fence_async_smem();  // the TMA store (async proxy) must see these writes
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&scaled[s]);
+        }
+        return;
+    }
+
+    // ------------------------------------------------------------------------------- sum warp
     float acc = 0.0f;
     int done = 0;
     for (int c = 0; c < nch; c++) {
         const int s = c % SW_STAGES;
-        if (!mbar_wait(&full[s], (uint32_t)((c / SW_STAGES) & 1))) {
+        if (!mbar_wait(&scaled[s], (uint32_t)((c / SW_STAGES) & 1))) {
             set_err(n, ERR_TIMEOUT);
             break;
         }
         done = c + 1;
-        float4 *ps4 = reinterpret_cast<float4 *>(st_psr(s));                 // [16 quads][32]
-        const uint32_t *cw = reinterpret_cast<const uint32_t *>(st_cls(s));  // [16 quads][32]
-        // batches of 4 quads (16 rows): all loads of a batch, then the math, then the stores
-#pragma unroll 1
-        for (int gb = 0; gb < SW_QUADS; gb += 4) {
-            float4 pv[4];
-            uint32_t cv[4];
-            float dv[16];
+        const float4 *ps4 = reinterpret_cast<const float4 *>(st_psr(s));
+        float4 pv[SW_QUADS];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                pv[j] = ps4[(gb + j) * SW_DESTS + lane];
-                cv[j] = cw[(gb + j) * SW_DESTS + lane];
-            }
+        for (int q = 0; q < SW_QUADS; q++) pv[q] = ps4[q * SW_DESTS + lane];
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) dv[4 * j + b] = s_dtab[(cv[j] >> (8 * b)) & 0xffu];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                pv[j].x = pv[j].x * dv[4 * j + 0];
-                acc = acc + pv[j].x;
-                pv[j].y = pv[j].y * dv[4 * j + 1];
-                acc = acc + pv[j].y;
-                pv[j].z = pv[j].z * dv[4 * j + 2];
-                acc = acc + pv[j].z;
-                pv[j].w = pv[j].w * dv[4 * j + 3];
-                acc = acc + pv[j].w;
-            }
-#pragma unroll
-            for (int j = 0; j < 4; j++) ps4[(gb + j) * SW_DESTS + lane] = pv[j];
+        for (int q = 0; q < SW_QUADS; q++) {
+            acc = acc + pv[q].x;
+            acc = acc + pv[q].y;
+            acc = acc + pv[q].z;
+            acc = acc + pv[q].w;
         }
-        fence_async_smem();
         __syncwarp();
         if (lane == 0) {
             tma_store_2d(&tm_psr, d0 * 4, c * SW_QUADS, st_psr(s));
@@ -418,7 +440,7 @@ static void launch_sweep_t(const NetDev &h, const CUtensorMap &tp, const CUtenso
         cudaFuncSetAttribute(k_sweep<SYN, FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
         attr_set = true;
     }
-    launch_pdl(k_sweep<SYN, FUSE>, h.ntiles, 64, SW_SMEM, s, h, tp, tc);
+    launch_pdl(k_sweep<SYN, FUSE>, h.ntiles, SW_THREADS, SW_SMEM, s, h, tp, tc);
 }
 
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
