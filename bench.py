@@ -224,6 +224,7 @@ def run_bg3(args):
     e2e = {"value": S * E2E_STEPS * e2e_iters * world / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS}
     err = net.error_word
+    batched = run_batched(min(args.steps, 500), max(args.warmup, 20)) if world == 1 else None
     if rank == 0:
         cpu = cpu_baseline_port(net, spec)
         tr = traffic_per_launch(S)
@@ -251,6 +252,7 @@ def run_bg3(args):
                                            "sweep": float(shares[2])}},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "batched": batched,
             "gpu_launches": 2 * args.steps + 1,
             "clocks": clocks,
             "error_word": err,
@@ -258,6 +260,54 @@ def run_bg3(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_batched(steps, warmup):
+    """config[2]: the 36-network sweep as one batch (one launch per kernel per step) against the
+    same networks run one network at a time with bg3_step (each on its own CUDA graph)."""
+    import time as _t
+    from braingrid_gb300 import lib as bg
+    from braingrid_gb300 import workloads
+    members = workloads.c2_members()
+    nets = [workloads.build_member(w)[1] for w in members]
+    S = sum(n.total_synapses() for n in nets)
+    N = sum(n.N for n in nets)
+    batch = bg.Batch(nets)
+    batch.step(warmup)
+    batch.sync()
+    # batched: device time per step with CUDA events (the working set, ~1 GB, exceeds L2)
+    ms = batch.bench_steps(steps)
+    t_batch = float(np.sum(ms)) / 1e3
+    # plain: every network advanced on its own for the same number of steps, back to back
+    for n in nets:
+        n.step(warmup)
+    for n in nets:
+        n.sync()
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = _t.perf_counter()
+    for n in nets:
+        n.step(steps)
+    for n in nets:
+        n.sync()
+    t_plain = _t.perf_counter() - t0
+    err = max(n.error_word for n in nets)
+    out = {"workload": "config[2]: 36 networks (9 each of 30x30, 50x50, 70x70, 100x100; targetRate "
+                       "x excitatory fraction x 4 seeds), pre-grown as config[1]",
+           "networks": len(nets), "neurons": N, "synapses": S, "steps": steps,
+           "batched_synapse_updates_per_s": S * steps / t_batch,
+           "batched_neuron_steps_per_s": N * steps / t_batch,
+           "batched_ms_per_step": t_batch * 1e3 / steps,
+           "batched_sweep_gbs": 9.0 * S / (t_batch / steps) / 1e9,
+           "plain_synapse_updates_per_s": S * steps / t_plain,
+           "plain_neuron_steps_per_s": N * steps / t_plain,
+           "plain_ms_per_step": t_plain * 1e3 / steps,
+           "plain_timing": "host wall clock around 36 sequential bg3_step runs (each a CUDA graph)",
+           "batched_over_plain": t_plain / t_batch, "error_word": int(err)}
+    batch.close()
+    for n in nets:
+        n.close()
+    return out
 
 
 def run_reference(args):

@@ -17,6 +17,10 @@ void launch_neurons(const NetDev &h, cudaStream_t s);
 void launch_deliver(const NetDev &h, cudaStream_t s);
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
                   cudaStream_t s);
+void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s);
+void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s);
+void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int ntiles,
+                        bool fuse, cudaStream_t s);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
@@ -769,6 +773,181 @@ int bg3_download_histories(bg3_net *n, float *burst, float *spikes, float *rh, f
     return BG3_OK;
 }
 
+// ---- batched form ---------------------------------------------------------------------------
+// Many networks advanced together: per step one delivery launch and one sweep launch cover every
+// network (per-network descriptors and tensor maps in device tables, a (network, tile) table
+// ordered heaviest tile first).  Member handles keep their own state and remain usable on their
+// own; the batch orders its stream after theirs and theirs after its own.
+struct bg3_batch {
+    std::vector<bg3_net *> nets;
+    NetDev *d_nets = nullptr;
+    CUtensorMap *d_maps = nullptr;
+    int2 *d_tiles = nullptr;
+    int ntiles = 0, max_n = 0, syn_kind = 1;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev = nullptr;
+    void *flush_buf = nullptr, *scrub_buf = nullptr;
+    size_t flush_size = 0;
+    long long launches = 0;
+};
+
+static int batch_refresh(bg3_batch *b)
+{
+    std::vector<NetDev> hd;
+    std::vector<CUtensorMap> maps;
+    std::vector<std::pair<int, int2>> tiles;  // (rows, (net, tile))
+    for (size_t k = 0; k < b->nets.size(); k++) {
+        bg3_net *n = b->nets[k];
+        hd.push_back(n->h);
+        maps.push_back(n->tm_psr);
+        maps.push_back(n->tm_cls);
+        std::vector<uint32_t> count(n->h.N);
+        CK(cudaMemcpy(count.data(), n->h.count, count.size() * 4, cudaMemcpyDeviceToHost));
+        for (int t = 0; t < n->h.ntiles; t++) {
+            uint32_t m = 0;
+            for (int d = t * 32; d < std::min(n->h.N, t * 32 + 32); d++) m = std::max(m, count[d]);
+            tiles.push_back(std::make_pair((int)m, make_int2((int)k, t)));
+        }
+    }
+    std::stable_sort(tiles.begin(), tiles.end(),
+                     [](const std::pair<int, int2> &a, const std::pair<int, int2> &c) { return a.first > c.first; });
+    std::vector<int2> tl;
+    for (auto &t : tiles) tl.push_back(t.second);
+    if ((int)tl.size() != b->ntiles) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->d_tiles = nullptr;
+        if (cudaMalloc(&b->d_tiles, std::max<size_t>(tl.size(), 1) * sizeof(int2)) != cudaSuccess) {
+            cudaGetLastError();
+            return BG3_ENOMEM;
+        }
+        b->ntiles = (int)tl.size();
+    }
+    CK(cudaMemcpyAsync(b->d_nets, hd.data(), hd.size() * sizeof(NetDev), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    return BG3_OK;
+}
+
+// order the batch stream after every member stream (enter) or every member after it (leave)
+static int batch_order(bg3_batch *b, bool enter)
+{
+    for (bg3_net *n : b->nets) {
+        CK(cudaEventRecord(b->ev, enter ? n->stream : b->stream));
+        CK(cudaStreamWaitEvent(enter ? b->stream : n->stream, b->ev, 0));
+    }
+    return BG3_OK;
+}
+
+int bg3_batch_create(bg3_net *const *nets, int32_t count, bg3_batch **out)
+{
+    if (!nets || count <= 0 || !out) return BG3_EINVAL;
+    *out = nullptr;
+    for (int k = 0; k < count; k++) {
+        if (!nets[k] || nets[k]->h.noise_mode != BG3_NOISE_DEVICE ||
+            nets[k]->h.syn_kind != nets[0]->h.syn_kind)
+            return BG3_EINVAL;
+        for (int j = 0; j < k; j++)
+            if (nets[j] == nets[k]) return BG3_EINVAL;
+    }
+    bg3_batch *b = new (std::nothrow) bg3_batch();
+    if (!b) return BG3_ENOMEM;
+    b->nets.assign(nets, nets + count);
+    b->syn_kind = nets[0]->h.syn_kind;
+    for (bg3_net *n : b->nets) b->max_n = std::max(b->max_n, n->h.N);
+    int rc = BG3_ECUDA;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess)
+        goto fail;
+    rc = BG3_ENOMEM;
+    if (cudaMalloc(&b->d_nets, count * sizeof(NetDev)) != cudaSuccess ||
+        cudaMalloc(&b->d_maps, 2 * count * sizeof(CUtensorMap)) != cudaSuccess)
+        goto fail;
+    for (bg3_net *n : b->nets) cudaStreamSynchronize(n->stream);
+    if ((rc = batch_refresh(b)) != 0) goto fail;
+    *out = b;
+    return BG3_OK;
+fail:
+    cudaGetLastError();
+    bg3_batch_destroy(b);
+    return rc;
+}
+
+int bg3_batch_destroy(bg3_batch *b)
+{
+    if (!b) return BG3_EINVAL;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->d_nets) cudaFree(b->d_nets);
+    if (b->d_maps) cudaFree(b->d_maps);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->flush_buf) cudaFree(b->flush_buf);
+    if (b->scrub_buf) cudaFree(b->scrub_buf);
+    if (b->ev) cudaEventDestroy(b->ev);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return BG3_OK;
+}
+
+int bg3_batch_refresh(bg3_batch *b)
+{
+    if (!b) return BG3_EINVAL;
+    int rc = batch_order(b, true);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    return batch_refresh(b);
+}
+
+static void batch_interior(bg3_batch *b, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) {
+        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, (int)b->nets.size(), b->stream);
+        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, true, b->stream);
+    }
+}
+
+int bg3_batch_step(bg3_batch *b, int64_t nsteps)
+{
+    if (!b || nsteps < 0) return BG3_EINVAL;
+    if (nsteps == 0) return BG3_OK;
+    int rc = batch_order(b, true);
+    if (rc) return rc;
+    const int M = (int)b->nets.size();
+    bg3::launch_neurons_batch(b->d_nets, M, b->max_n, b->stream);
+    int64_t interior = nsteps - 1;
+    if (interior >= GRAPH_STEPS && !b->graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        batch_interior(b, GRAPH_STEPS);
+        CK(cudaStreamEndCapture(b->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { b->graph = nullptr; return BG3_ECUDA; }
+    }
+    while (b->graph && interior >= GRAPH_STEPS) {
+        CK(cudaGraphLaunch(b->graph, b->stream));
+        interior -= GRAPH_STEPS;
+    }
+    batch_interior(b, interior);
+    bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
+    bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, false, b->stream);
+    b->launches += 1 + 2 * nsteps;
+    CK(cudaGetLastError());
+    return batch_order(b, false);
+}
+
+int bg3_batch_sync(bg3_batch *b)
+{
+    if (!b) return BG3_EINVAL;
+    CK(cudaStreamSynchronize(b->stream));
+    return BG3_OK;
+}
+
+int64_t bg3_batch_launches(bg3_batch *b) { return b ? b->launches : BG3_EINVAL; }
+
 // ---- benchmarking ---------------------------------------------------------------------------
 __global__ void k_scrub(const float4 *p, size_t n4, float *sink)
 {
@@ -836,6 +1015,47 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
     }
     for (auto &e : ev) cudaEventDestroy(e);
     return BG3_OK;
+}
+
+int bg3_batch_bench_steps(bg3_batch *b, int64_t nsteps, int64_t flush_bytes, float *step_ms)
+{
+    if (!b || nsteps < 0 || !step_ms) return BG3_EINVAL;
+    if (flush_bytes > 0 && (size_t)flush_bytes > b->flush_size) {
+        if (b->flush_buf) cudaFree(b->flush_buf);
+        if (b->scrub_buf) cudaFree(b->scrub_buf);
+        b->flush_buf = b->scrub_buf = nullptr;
+        b->flush_size = 0;
+        if (cudaMalloc(&b->flush_buf, (size_t)flush_bytes) != cudaSuccess ||
+            cudaMalloc(&b->scrub_buf, (size_t)flush_bytes + 16) != cudaSuccess) {
+            cudaGetLastError();
+            return BG3_ENOMEM;
+        }
+        CK(cudaMemsetAsync(b->scrub_buf, 0, (size_t)flush_bytes + 16, b->stream));
+        b->flush_size = (size_t)flush_bytes;
+    }
+    int rc = batch_order(b, true);
+    if (rc) return rc;
+    const int M = (int)b->nets.size();
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 2);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    bg3::launch_neurons_batch(b->d_nets, M, b->max_n, b->stream);
+    for (int64_t s = 0; s < nsteps; s++) {
+        if (flush_bytes > 0) {
+            CK(cudaMemsetAsync(b->flush_buf, (int)(s & 0xff), (size_t)flush_bytes, b->stream));
+            k_scrub<<<2 * 152, 512, 0, b->stream>>>((const float4 *)b->scrub_buf, (size_t)flush_bytes / 16,
+                                                   (float *)((char *)b->scrub_buf + flush_bytes));
+        }
+        CK(cudaEventRecord(ev[2 * s], b->stream));
+        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
+        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, s < nsteps - 1, b->stream);
+        CK(cudaEventRecord(ev[2 * s + 1], b->stream));
+    }
+    b->launches += 1 + 2 * nsteps;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(b->stream));
+    for (int64_t s = 0; s < nsteps; s++) CK(cudaEventElapsedTime(&step_ms[s], ev[2 * s], ev[2 * s + 1]));
+    for (auto &e : ev) cudaEventDestroy(e);
+    return batch_order(b, false);
 }
 
 int bg3_enable_timing(bg3_net *n, int on)

@@ -185,17 +185,13 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
 
 // One warp per (delay class, spiking neuron) pair; lanes walk that neuron's outgoing synapses
 // of the class.  Each synapse has one source, which fires at most once per step, so no two
-// lanes touch one slot.  Block 0 also clears ring slot t + 1 for the next neuron pass.
+// lanes touch one slot.  One thread also clears ring slot t + 1 for the next neuron pass.
 template <int SYN>
-__global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev n)
+__device__ __forceinline__ void deliver_net(const NetDev &n, int gw, int nw, bool clear_next)
 {
-    pdl_wait();  // the previous sweep (step counter, spike ring, psr) must be complete
-    pdl_trigger();
     const unsigned long long t = *n.step;
-    if (blockIdx.x == 0 && threadIdx.x == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
+    if (clear_next) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
     const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int c = 0; c < n.n_delays; c++) {
         const int D = n.ltab[c];
         if (D <= 0 || (unsigned long long)D > t) continue;
@@ -211,6 +207,48 @@ __global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev 
                 deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, (uint32_t)t);
         }
     }
+}
+
+template <int SYN>
+__global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev n)
+{
+    pdl_wait();  // the previous sweep (step counter, spike ring, psr) must be complete
+    pdl_trigger();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    deliver_net<SYN>(n, gw, nw, blockIdx.x == 0 && threadIdx.x == 0);
+}
+
+// Batched form: the warps of one launch take turns over the networks of the batch.
+template <int SYN>
+__global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets, int count)
+{
+    pdl_wait();
+    pdl_trigger();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int k = 0; k < count; k++) {
+        // rotate the starting warp per network so small networks do not all land on warp 0
+        const int rw = (gw + k * 37) % nw;
+        deliver_net<SYN>(nets[k], rw, nw, blockIdx.x == 0 && threadIdx.x == 0);
+    }
+}
+
+// Batched standalone neuron pass (device noise): grid.y indexes the network.
+__global__ void __launch_bounds__(256) k_neurons_device_batch(const NetDev *nets)
+{
+    const NetDev &n = nets[blockIdx.y];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x >= (unsigned)n.N) return;  // whole warp-aligned block beyond N
+    unsigned long long t = *n.step;
+    bool fired = false;
+    if (i < n.N) {
+        int br = lif_branch(n, i);
+        float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
+        fired = lif_apply(n, i, br, n.sp[i], noise, t);
+        n.sp[i] = 0.0f;
+    }
+    ring_push(n, t, fired, i);
 }
 
 // ---- synapse sweep ---------------------------------------------------------------------------
@@ -242,12 +280,11 @@ constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4
 // a sum that started at +0.0f unchanged, so the sum warp adds all 64 rows of every chunk.  The
 // prologue overlaps the previous kernel's tail; the step's data is touched after pdl_wait().
 // Every mbarrier wait is bounded (about 1 s); on expiry the error word is set and the CTA drains.
-template <int SYN, bool FUSE>
-__global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ NetDev n,
-                                                      const __grid_constant__ CUtensorMap tm_psr,
-                                                      const __grid_constant__ CUtensorMap tm_cls)
+template <bool FUSE>
+__device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *tm_psr,
+                                           const CUtensorMap *tm_cls, const int tile,
+                                           uint8_t *smem_raw)
 {
-    extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     float *s_dtab = (float *)(smem + (size_t)SW_STAGES * SW_CHUNK_BYTES);
     uint64_t *full = (uint64_t *)(s_dtab + BG3_MAX_DCLS);
@@ -257,7 +294,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ Ne
     auto st_psr = [&](int s) { return (float *)(smem + (size_t)s * SW_CHUNK_BYTES); };
     auto st_cls = [&](int s) { return smem + (size_t)s * SW_CHUNK_BYTES + SW_PSR_BYTES; };
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int d0 = blockIdx.x * SW_DESTS;
+    const int d0 = tile * SW_DESTS;
     const int d = d0 + lane;
     const bool valid = d < n.N;
     for (int i = threadIdx.x; i < n.n_dcls; i += blockDim.x) s_dtab[i] = n.dtab[i];
@@ -287,8 +324,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ Ne
                     break;
                 }
                 mbar_expect_tx(&full[s], SW_CHUNK_BYTES);
-                tma_load_2d(st_psr(s), &tm_psr, d0 * 4, c * SW_QUADS, &full[s]);
-                tma_load_2d(st_cls(s), &tm_cls, d0, c * SW_QUADS, &full[s]);
+                tma_load_2d(st_psr(s), tm_psr, d0 * 4, c * SW_QUADS, &full[s]);
+                tma_load_2d(st_cls(s), tm_cls, d0, c * SW_QUADS, &full[s]);
                 *(volatile int *)s_issued = c + 1;
             }
         }
@@ -351,7 +388,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ Ne
         }
         __syncwarp();
         if (lane == 0) {
-            tma_store_2d(&tm_psr, d0 * 4, c * SW_QUADS, st_psr(s));
+            tma_store_2d(tm_psr, d0 * 4, c * SW_QUADS, st_psr(s));
             bulk_commit();
             if (c >= 1) {
                 bulk_wait_read1();
@@ -385,17 +422,38 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ Ne
     } else if (valid) {
         n.sp[d] = acc;
     }
-    // the last tile to finish advances the step counter
+    // the network's last tile to finish advances its step counter
     if (lane == 0) {
         __threadfence();
         unsigned prev = atomicAdd(n.sweep_done, 1u);
-        if (prev == gridDim.x - 1) {
+        if (prev == (unsigned)n.ntiles - 1) {
             *n.step = t + 1;
             *n.sweep_done = 0;
             if (t + 1 >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
             __threadfence();
         }
     }
+}
+
+template <int SYN, bool FUSE>
+__global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ NetDev n,
+                                                      const __grid_constant__ CUtensorMap tm_psr,
+                                                      const __grid_constant__ CUtensorMap tm_cls)
+{
+    extern __shared__ uint8_t smem_raw[];
+    sweep_tile<FUSE>(n, &tm_psr, &tm_cls, blockIdx.x, smem_raw);
+}
+
+// Batched form: one launch sweeps every tile of every network of a batch.  tiles[b] = (network,
+// tile); maps holds each network's two tensor maps (psr, class) in global memory.
+template <bool FUSE>
+__global__ void __launch_bounds__(SW_THREADS) k_sweep_batch(const NetDev *nets,
+                                                            const CUtensorMap *maps,
+                                                            const int2 *tiles)
+{
+    extern __shared__ uint8_t smem_raw[];
+    const int2 tr = tiles[blockIdx.x];
+    sweep_tile<FUSE>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
 }
 
 // ---- launchers -------------------------------------------------------------------------------
@@ -441,6 +499,36 @@ static void launch_sweep_t(const NetDev &h, const CUtensorMap &tp, const CUtenso
         attr_set = true;
     }
     launch_pdl(k_sweep<SYN, FUSE>, h.ntiles, SW_THREADS, SW_SMEM, s, h, tp, tc);
+}
+
+template <bool FUSE>
+static void launch_sweep_batch_t(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles,
+                                 int ntiles, cudaStream_t s)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sweep_batch<FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
+        attr_set = true;
+    }
+    launch_pdl(k_sweep_batch<FUSE>, ntiles, SW_THREADS, SW_SMEM, s, nets, maps, tiles);
+}
+
+void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s)
+{
+    k_neurons_device_batch<<<dim3((max_n + 255) / 256, count), 256, 0, s>>>(nets);
+}
+
+void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s)
+{
+    if (syn_kind == 1) launch_pdl(k_deliver_batch<1>, 2 * deliver_blocks(), 256, 0, s, nets, count);
+    else launch_pdl(k_deliver_batch<0>, 2 * deliver_blocks(), 256, 0, s, nets, count);
+}
+
+void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int ntiles,
+                        bool fuse, cudaStream_t s)
+{
+    if (fuse) launch_sweep_batch_t<true>(nets, maps, tiles, ntiles, s);
+    else launch_sweep_batch_t<false>(nets, maps, tiles, ntiles, s);
 }
 
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,

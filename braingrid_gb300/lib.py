@@ -110,6 +110,13 @@ def load(build_if_missing=True):
         "bg3_status_string": ([ctypes.c_int], ctypes.c_char_p),
         "bg3_enable_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "bg3_bench_steps": ([vp, ctypes.c_int64, ctypes.c_int64, c_f32p, c_f32p], ctypes.c_int),
+        "bg3_batch_create": ([ctypes.POINTER(vp), ctypes.c_int32, ctypes.POINTER(vp)], ctypes.c_int),
+        "bg3_batch_destroy": ([vp], ctypes.c_int),
+        "bg3_batch_refresh": ([vp], ctypes.c_int),
+        "bg3_batch_step": ([vp, ctypes.c_int64], ctypes.c_int),
+        "bg3_batch_sync": ([vp], ctypes.c_int),
+        "bg3_batch_launches": ([vp], ctypes.c_int64),
+        "bg3_batch_bench_steps": ([vp, ctypes.c_int64, ctypes.c_int64, c_f32p], ctypes.c_int),
         "bg3_kernel_times": ([vp, c_f32p, c_f32p, c_f32p, ctypes.POINTER(ctypes.c_int64)],
                              ctypes.c_int),
     }
@@ -343,3 +350,45 @@ class Network:
         check(self.L.bg3_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                       ctypes.byref(n)), "bg3_kernel_times")
         return a.value, b.value, c.value, n.value
+
+
+class Batch:
+    """Several Networks advanced together, one launch per kernel per step (bg3_batch_*)."""
+
+    def __init__(self, nets):
+        self.L = load()
+        self.nets = list(nets)
+        arr = (ctypes.c_void_p * len(self.nets))(*[n.h.value for n in self.nets])
+        h = ctypes.c_void_p()
+        check(self.L.bg3_batch_create(arr, len(self.nets), ctypes.byref(h)), "bg3_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.bg3_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def refresh(self):
+        check(self.L.bg3_batch_refresh(self.h), "bg3_batch_refresh")
+
+    def step(self, n=1):
+        check(self.L.bg3_batch_step(self.h, int(n)), "bg3_batch_step")
+
+    def sync(self):
+        check(self.L.bg3_batch_sync(self.h), "bg3_batch_sync")
+
+    @property
+    def launches(self):
+        return int(self.L.bg3_batch_launches(self.h))
+
+    def bench_steps(self, nsteps, flush_bytes=0):
+        ms = np.zeros(max(int(nsteps), 1), np.float32)
+        check(self.L.bg3_batch_bench_steps(self.h, int(nsteps), int(flush_bytes), _p(ms)),
+              "bg3_batch_bench_steps")
+        return ms[:nsteps]

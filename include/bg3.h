@@ -183,6 +183,24 @@ int bg3_enable_timing(bg3_net *net, int on);
 int bg3_kernel_times(bg3_net *net, float *ms_neurons, float *ms_fanout, float *ms_sweep,
                      int64_t *launches);
 
+/* ---- batched form ---------------------------------------------------------------------- */
+/* Many networks of uneven size advanced together: each step is one spike-delivery launch and
+ * one sweep launch over every network (per-network descriptor and tensor-map tables, tiles
+ * ordered heaviest first), with runs of steps replayed from a CUDA graph.  The reference has no
+ * counterpart (it runs one network per process, Core/BGDriver.cpp:49-158); each member network
+ * is a bg3_net created and loaded as usual, which stays usable on its own.  Members must share
+ * the synapse kind and use BG3_NOISE_DEVICE; results are identical to running each member with
+ * bg3_step.  After bg3_epoch_growth on a member, call bg3_batch_refresh. */
+typedef struct bg3_batch bg3_batch;
+int bg3_batch_create(bg3_net *const *nets, int32_t count, bg3_batch **out);
+int bg3_batch_destroy(bg3_batch *batch);
+int bg3_batch_refresh(bg3_batch *batch);
+int bg3_batch_step(bg3_batch *batch, int64_t nsteps);
+int bg3_batch_sync(bg3_batch *batch);
+int64_t bg3_batch_launches(bg3_batch *batch);
+/* Same as bg3_bench_steps for a batch (step_ms[nsteps], CUDA events on the batch stream). */
+int bg3_batch_bench_steps(bg3_batch *batch, int64_t nsteps, int64_t flush_bytes, float *step_ms);
+
 /* Benchmark helper: runs nsteps steps on the handle's stream.  Before each step, when
  * flush_bytes > 0, a scratch buffer of that size is overwritten so that the step starts with a
  * cold L2.  The device time of each step (CUDA events on the handle's stream, flush excluded) is
