@@ -291,6 +291,15 @@ def run_batched(steps, warmup):
     for n in nets:
         n.sync()
     t_plain = _t.perf_counter() - t0
+    # plain lock-step: every step, each network advanced by its own bg3_step(1) call
+    lock = min(steps, 100)
+    t0 = _t.perf_counter()
+    for _ in range(lock):
+        for n in nets:
+            n.step(1)
+    for n in nets:
+        n.sync()
+    t_lock = (_t.perf_counter() - t0) / lock
     err = max(n.error_word for n in nets)
     out = {"workload": "config[2]: 36 networks (9 each of 30x30, 50x50, 70x70, 100x100; targetRate "
                        "x excitatory fraction x 4 seeds), pre-grown as config[1]",
@@ -303,7 +312,11 @@ def run_batched(steps, warmup):
            "plain_neuron_steps_per_s": N * steps / t_plain,
            "plain_ms_per_step": t_plain * 1e3 / steps,
            "plain_timing": "host wall clock around 36 sequential bg3_step runs (each a CUDA graph)",
-           "batched_over_plain": t_plain / t_batch, "error_word": int(err)}
+           "plain_lockstep_synapse_updates_per_s": S / t_lock,
+           "plain_lockstep_ms_per_step": t_lock * 1e3,
+           "plain_lockstep_timing": "host wall clock, %d steps of 36 bg3_step(1) calls" % lock,
+           "batched_over_plain": t_plain / t_batch,
+           "batched_over_plain_lockstep": t_lock * steps / t_batch, "error_word": int(err)}
     batch.close()
     for n in nets:
         n.close()

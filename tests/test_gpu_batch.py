@@ -18,7 +18,7 @@ def make_set():
         spec = netgen.lif_network(w, h, seed=seed)
         net = netgen.make_gpu_network(spec, 40, epoch_duration=0.5, max_firing_rate=400,
                                       noise_seed=seed)
-        netgen.pregrow(net, spec, r, weight_scale=0.05, seed=seed)
+        netgen.pregrow(net, spec, r, weight_scale=0.2, seed=seed)
         nets.append(net)
     return nets
 
@@ -34,7 +34,7 @@ def test_batch_matches_plain_networks_bit_exact():
     batched = make_set()
     assert all(n.total_synapses() > 0 for n in plain)
     b = bg.Batch(batched)
-    for chunk in (1, 37, 200, 3):
+    for chunk in (1, 37, 1500, 3, 800):
         for n in plain:
             n.step(chunk)
         b.step(chunk)
