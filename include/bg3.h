@@ -175,6 +175,30 @@ int bg3_download_growth(bg3_net *net, float *radii, float *rates);
 int bg3_download_histories(bg3_net *net, float *burstiness, float *spikes, float *rates_hist,
                            float *radii_hist);
 
+/* ---- allocation-free variant -------------------------------------------------------------- */
+/* No counterpart in the reference: an extra entry point for callers that cannot allocate device
+ * memory when they need the map (code running under CUDA stream capture, where cudaMalloc is
+ * not allowed; host runtimes that own every device allocation through their own pool; real-time
+ * loops that must not enter the allocator).  Builds the outgoing synapse map in the reference's
+ * order (Core/SynapseIndexMap.h: per source neuron, the slot ids d * max_syn + k in ascending
+ * order) from caller-owned DEVICE buffers and allocates nothing:
+ *   src_dev     [n_neurons * max_syn] int32, reference slot layout (sourceNeuronIndex)
+ *   counts_dev  [n_neurons] uint32, in-use prefix length of each row (synapse_counts)
+ *   begin_dev, count_dev  [n_neurons] uint32 out;  map_dev [sum of counts] uint32 out
+ *   status_dev  one uint32 out: bit 0 a source index out of range, bit 1 a source with more than
+ *               BG3_NOALLOC_MAX_FANOUT synapses (its run is left unsorted)
+ *   stream      cudaStream_t (NULL: the legacy default stream); the call only enqueues work.
+ * Its scratch (one counter per neuron) is a fixed array inside the library, shared by all calls
+ * on a device and kept until the process exits: calls that overlap on the GPU race on it.  More
+ * than BG3_NOALLOC_MAX_NEURONS neurons is rejected with BG3_EINVAL.  The first call on each
+ * device resolves the array's address with that device current; make it before any capture. */
+#define BG3_NOALLOC_MAX_NEURONS 65536
+#define BG3_NOALLOC_MAX_FANOUT 4096
+int bg3_outgoing_map_noalloc(const int32_t *src_dev, const uint32_t *counts_dev,
+                             int32_t n_neurons, int32_t max_syn, uint32_t *begin_dev,
+                             uint32_t *count_dev, uint32_t *map_dev, uint32_t *status_dev,
+                             void *stream);
+
 /* ---- diagnostics ---------------------------------------------------------------------- */
 const char *bg3_status_string(int status);
 /* Per-launch timing of the last bg3_step call's kernels: fills up to n entries of
