@@ -131,6 +131,19 @@ struct bgo_net {
     float epsilon, beta, rho, target_rate, min_radius, start_radius, max_rate;
     /* recorder histories (Recorders/XmlRecorder.cpp, XmlGrowthRecorder.cpp) */
     float *burstinessHist, *spikesHistory, *ratesHistory, *radiiHistory;
+    /* inputs: 0 none, 1 regular, 2 poisson */
+    int input_kind;
+    int reg_dur, reg_cycle, reg_in_cycle;
+    float *reg_values;
+    int *reg_shift;
+    float pois_lambda;
+    uint8_t *pois_mask;
+    int *pois_nisi;
+    /* the Poisson input synapses: one DS synapse per neuron (SInputPoisson::init) */
+    float *in_W, *in_psr, *in_decay, *in_U, *in_D, *in_F, *in_u, *in_r;
+    int *in_delay, *in_delayIdx;
+    uint32_t *in_queue;
+    uint64_t *in_last;
 };
 
 #define ALLOC(p, cnt) ((p) = calloc((size_t)(cnt) ? (size_t)(cnt) : 1, sizeof(*(p))))
@@ -184,6 +197,10 @@ void bgo_destroy(bgo_net *n)
                     n->outBegin, n->outCount, n->radii, n->rates, n->burstinessHist,
                     n->spikesHistory, n->ratesHistory, n->radiiHistory, n->noise_rec};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
+    void *inp[] = {n->reg_values, n->reg_shift, n->pois_mask, n->pois_nisi, n->in_W, n->in_psr,
+                   n->in_decay, n->in_U, n->in_D, n->in_F, n->in_u, n->in_r, n->in_delay,
+                   n->in_delayIdx, n->in_queue, n->in_last};
+    for (size_t i = 0; i < sizeof(inp) / sizeof(inp[0]); i++) free(inp[i]);
     free(n);
 }
 
@@ -211,6 +228,14 @@ void *bgo_array(bgo_net *n, const char *name, int64_t *count, int *esz)
     A("ratesHistory", n->ratesHistory, (int64_t)(n->max_epochs + 1) * N)
     A("radiiHistory", n->radiiHistory, (int64_t)(n->max_epochs + 1) * N)
     A("noise", n->noise_rec, n->noise_n)
+    A("reg_values", n->reg_values, n->reg_values ? N : 0) A("reg_shift", n->reg_shift, n->reg_shift ? N : 0)
+    A("pois_nisi", n->pois_nisi, n->pois_nisi ? N : 0) A("pois_mask", n->pois_mask, n->pois_mask ? N : 0)
+    A("in_psr", n->in_psr, n->in_psr ? N : 0) A("in_u", n->in_u, n->in_u ? N : 0)
+    A("in_r", n->in_r, n->in_r ? N : 0) A("in_last", n->in_last, n->in_last ? N : 0)
+    A("in_queue", n->in_queue, n->in_queue ? N : 0) A("in_delayIdx", n->in_delayIdx, n->in_delayIdx ? N : 0)
+    A("in_W", n->in_W, n->in_W ? N : 0) A("in_decay", n->in_decay, n->in_decay ? N : 0)
+    A("in_delay", n->in_delay, n->in_delay ? N : 0) A("in_U", n->in_U, n->in_U ? N : 0)
+    A("in_D", n->in_D, n->in_D ? N : 0) A("in_F", n->in_F, n->in_F ? N : 0)
 #undef A
     *count = 0; *esz = 0;
     return NULL;
@@ -384,6 +409,162 @@ int bgo_rebuild_maps(bgo_net *n)
     return (nin == total) ? 0 : -1;
 }
 
+/* ============================== inputs ============================== */
+/* SInputRegular::SInputRegular (Inputs/SInputRegular.cpp:20-112): step counts, the 10x10 value
+ * pattern tiled over the grid, and per-neuron phase shifts. */
+int bgo_input_regular(bgo_net *n, float duration, float interval, int sync, const float *v100)
+{
+    n->input_kind = 1;
+    n->reg_dur = (int)((double)(duration / n->delta_t) + 0.5);
+    int nint = (int)((double)(interval / n->delta_t) + 0.5);
+    n->reg_cycle = n->reg_dur + nint;
+    n->reg_in_cycle = 0;
+    ALLOC(n->reg_values, n->N);
+    ALLOC(n->reg_shift, n->N);
+    for (int i = 0; i < n->height; i++)
+        for (int j = 0; j < n->width; j++)
+            n->reg_values[i * n->width + j] = v100[(i % 10) * 10 + j % 10];
+    if (sync == 1) {
+        for (int i = 0; i < n->height; i++)
+            for (int j = 0; j < n->width; j++)
+                n->reg_shift[i * n->width + j] =
+                    (int)bgo_mt_inrange(&n->rng, 0.0f, (float)(n->reg_cycle - 1));
+    } else if (sync == 2) {
+        for (int i = 0; i < n->height; i++)
+            for (int j = 0; j < n->width; j++)
+                n->reg_shift[i * n->width + j] = (n->reg_cycle / n->width) * j;
+    }
+    return 0;
+}
+
+/* SInputPoisson::SInputPoisson / init (Inputs/SInputPoisson.cpp:19-146): lambda, masks, and one
+ * DS input synapse per neuron (type EI onto inhibitory, EE onto excitatory neurons), created at
+ * the current step with W = weight x 1e-8.  The reference indexes its one-slot-per-neuron
+ * synapse object with maxSynapsesPerNeuron * neuron (SInputPoisson.cpp:141,
+ * HostSInputPoisson.cpp:77), out of bounds whenever maxSynapsesPerNeuron > 1; slot = neuron here
+ * (and in the reference harness that pins this code). */
+int bgo_input_poisson(bgo_net *n, float fr_mean, float weight, const uint8_t *masks)
+{
+    int N = n->N;
+    n->input_kind = 2;
+    fr_mean = fr_mean / 1000.0f;
+    n->pois_lambda = 1.0f / fr_mean;
+    ALLOC(n->pois_mask, N); ALLOC(n->pois_nisi, N);
+    ALLOC(n->in_W, N); ALLOC(n->in_psr, N); ALLOC(n->in_decay, N); ALLOC(n->in_U, N);
+    ALLOC(n->in_D, N); ALLOC(n->in_F, N); ALLOC(n->in_u, N); ALLOC(n->in_r, N);
+    ALLOC(n->in_delay, N); ALLOC(n->in_delayIdx, N); ALLOC(n->in_queue, N); ALLOC(n->in_last, N);
+    for (int i = 0; i < N; i++) {
+        n->pois_mask[i] = masks ? masks[i] : 1;
+        int type = (n->ntype[i] == BGO_INH) ? BGO_EI : BGO_EE;
+        float tau = (float)3e-3, delay = (type == BGO_EE) ? (float)1.5e-3 : (float)0.8e-3;
+        n->in_delay[i] = (int)(delay / n->delta_t) + 1;
+        n->in_queue[i] = 0;
+        n->in_delayIdx[i] = 0;
+        n->in_psr[i] = 0.0f;
+        n->in_decay[i] = expf(-n->delta_t / tau);
+        n->in_u[i] = (float)0.4;
+        n->in_r[i] = 1.0f;
+        n->in_last[i] = ULONG_MAX_U64;
+        n->in_U[i] = (type == BGO_EE) ? (float)0.5 : (float)0.05;
+        n->in_D[i] = (type == BGO_EE) ? (float)1.1 : (float)0.125;
+        n->in_F[i] = (type == BGO_EE) ? (float)0.05 : (float)1.2;
+        n->in_W[i] = weight * (float)1.0e-8;
+    }
+    return 0;
+}
+
+/* One ISI draw (HostSInputPoisson.cpp:81-84): exponential with mean lambda ms, rejection
+ * U <= exp(-isi^2 / 32), converted to steps. */
+static int poisson_draw(bgo_mt *rng, float lambda, float dt)
+{
+    float isi = -lambda * logf(bgo_mt_inrange(rng, 0.0f, 1.0f));
+    while (bgo_mt_inrange(rng, 0.0f, 1.0f) <= expf(-(isi * isi) / 32.0f))
+        isi = -lambda * logf(bgo_mt_inrange(rng, 0.0f, 1.0f));
+    return (int)((double)((isi / 1000.0f) / dt) + 0.5);
+}
+
+/* HostSInputRegular::inputStimulus (Inputs/HostSInputRegular.cpp:59-80). */
+static void input_regular(bgo_net *n)
+{
+    for (int i = n->N - 1; i >= 0; --i)
+        if (n->reg_in_cycle >= n->reg_shift[i] &&
+            n->reg_in_cycle < (n->reg_shift[i] + n->reg_dur) % n->reg_cycle)
+            n->sp[i] += n->reg_values[i];
+    n->reg_in_cycle = (n->reg_in_cycle + 1) % n->reg_cycle;
+}
+
+/* HostSInputPoisson::inputStimulus (Inputs/HostSInputPoisson.cpp:60-94): counter expiry fires
+ * the input synapse and draws the next ISI; the synapse then advances like any DS synapse. */
+static void input_poisson(bgo_net *n)
+{
+    for (int i = 0; i < n->N; i++) {
+        if (!n->pois_mask[i]) continue;
+        if (--n->pois_nisi[i] <= 0) {
+            int idx = n->in_delayIdx[i] + n->in_delay[i];
+            if (idx >= LDELAYQUEUE) idx -= LDELAYQUEUE;
+            n->in_queue[i] |= (1u << idx);
+            n->pois_nisi[i] = poisson_draw(&n->rng, n->pois_lambda, n->delta_t);
+        }
+        uint32_t bit = 1u << n->in_delayIdx[i];
+        int hit = (n->in_queue[i] & bit) != 0;
+        n->in_queue[i] &= ~bit;
+        if (++n->in_delayIdx[i] >= LDELAYQUEUE) n->in_delayIdx[i] = 0;
+        if (hit) {
+            if (n->in_last[i] != ULONG_MAX_U64) {
+                float isi = (float)(n->step - n->in_last[i]) * n->delta_t;
+                n->in_r[i] = 1.0f + (n->in_r[i] * (1.0f - n->in_u[i]) - 1.0f) * expf(-isi / n->in_D[i]);
+                n->in_u[i] = n->in_U[i] + n->in_u[i] * (1.0f - n->in_U[i]) * expf(-isi / n->in_F[i]);
+            }
+            n->in_psr[i] += ((n->in_W[i] / n->in_decay[i]) * n->in_u[i] * n->in_r[i]);
+            n->in_last[i] = n->step;
+        }
+        n->in_psr[i] *= n->in_decay[i];
+        n->sp[i] += n->in_psr[i];
+    }
+}
+
+int64_t bgo_poisson_isi_draws(bgo_net *n, int nsteps, int32_t *begin, int32_t *out, int64_t cap)
+{
+    if (n->input_kind != 2) return -1;
+    /* replay the counters on copies: per neuron, draws happen in step order, neurons ascending
+     * within a step; the rng is copied so the real run is unaffected */
+    bgo_mt rng = n->rng;
+    int N = n->N;
+    int *cnt = calloc((size_t)N, sizeof(int));
+    int *nisi = malloc((size_t)N * sizeof(int));
+    memcpy(nisi, n->pois_nisi, (size_t)N * sizeof(int));
+    /* first pass: count draws per neuron, recording them in step order into a temp buffer */
+    int64_t total = 0, tcap = 1024;
+    int32_t *tn = malloc((size_t)tcap * sizeof(int32_t)), *tv = malloc((size_t)tcap * sizeof(int32_t));
+    for (int t = 0; t < nsteps; t++)
+        for (int i = 0; i < N; i++) {
+            if (!n->pois_mask[i]) continue;
+            if (--nisi[i] <= 0) {
+                int v = poisson_draw(&rng, n->pois_lambda, n->delta_t);
+                nisi[i] = v;
+                if (total == tcap) {
+                    tcap *= 2;
+                    tn = realloc(tn, (size_t)tcap * sizeof(int32_t));
+                    tv = realloc(tv, (size_t)tcap * sizeof(int32_t));
+                }
+                tn[total] = i;
+                tv[total] = v;
+                total++;
+                cnt[i]++;
+            }
+        }
+    int64_t rc = total;
+    if (total > cap) rc = -1;
+    else {
+        begin[0] = 0;
+        for (int i = 0; i < N; i++) begin[i + 1] = begin[i] + cnt[i];
+        memset(cnt, 0, (size_t)N * sizeof(int));
+        for (int64_t k = 0; k < total; k++) out[begin[tn[k]] + cnt[tn[k]]++] = tv[k];
+    }
+    free(cnt); free(nisi); free(tn); free(tv);
+    return rc;
+}
+
 /* ============================== step ============================== */
 /* AllSpikingNeurons::fire (Neurons/AllSpikingNeurons.cpp:155-172) + AllLIFNeurons::fire
  * (Neurons/AllLIFNeurons.cpp:67-77). */
@@ -473,6 +654,9 @@ static void advance_synapses(bgo_net *n)
 void bgo_step(bgo_net *n, int nsteps)
 {
     for (int t = 0; t < nsteps; t++) {
+        /* Simulator::advanceUntilGrowth: inputStimulus, then advance (Core/Simulator.cpp:178-182) */
+        if (n->input_kind == 1) input_regular(n);
+        else if (n->input_kind == 2) input_poisson(n);
         advance_neurons(n);
         advance_synapses(n);
         n->step++;

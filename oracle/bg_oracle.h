@@ -67,6 +67,17 @@ int bgo_rebuild_maps(bgo_net *n);
 /* Fill per-type synapse constants of an in-use slot as createSynapse does. */
 void bgo_create_synapse(bgo_net *n, int dest, int src, int type, float W);
 
+/* External inputs (Inputs/).  Regular: values100 is the 10x10 pattern of <Values><I>, sync 0 =
+ * "yes", 1 = "no" (random shifts from the global rng), 2 = "wave".  Poisson: fr_mean (Hz),
+ * weight (x 1e-8 A), masks (N bytes, NULL = all).  Returns 0 on success. */
+int bgo_input_regular(bgo_net *n, float duration, float interval, int sync, const float *values100);
+int bgo_input_poisson(bgo_net *n, float fr_mean, float weight, const uint8_t *masks);
+/* Poisson input spike schedule as the reference would draw it over the next nsteps steps, without
+ * running the network (the draws depend only on the counters): per neuron, the ISI values (steps)
+ * in draw order.  isi_out must hold max_isis entries; returns the number written, or -1. */
+int64_t bgo_poisson_isi_draws(bgo_net *n, int nsteps, int32_t *isi_begin /* N+1 */,
+                              int32_t *isi_out, int64_t max_isis);
+
 /* Record every consumed noise value (bounded buffer) for inspection. */
 void bgo_record_noise(bgo_net *n, int64_t capacity);
 int64_t bgo_noise_recorded(const bgo_net *n);

@@ -16,10 +16,12 @@ LIB = os.path.join(BUILD, "libbgoracle.so")
 _NP = {1: np.uint8, 4: None, 8: None}
 # element type per array name (ambiguous sizes resolved by name)
 _INT32 = {"ntype", "starter", "refr", "spikeCount", "spikeCountOffset", "src", "dest", "type",
-          "total_delay", "delayIdx", "ldelayQueue"}
-_UINT32 = {"queue", "counts", "inMap", "outMap", "inBegin", "inCount", "outBegin", "outCount"}
-_UINT64 = {"history", "lastSpike"}
-_UINT8 = {"hasFired", "in_use"}
+          "total_delay", "delayIdx", "ldelayQueue", "reg_shift", "pois_nisi", "in_delay",
+          "in_delayIdx"}
+_UINT32 = {"queue", "counts", "inMap", "outMap", "inBegin", "inCount", "outBegin", "outCount",
+           "in_queue"}
+_UINT64 = {"history", "lastSpike", "in_last"}
+_UINT8 = {"hasFired", "in_use", "pois_mask"}
 
 LIF_CONFIG0_RANGES = [13.5e-9, 13.5e-9, 1.0e-9, 1.5e-9, 15.0e-3, 15.0e-3, 0.0, 0.0,
                       13.5e-3, 13.5e-3, 13.0e-3, 13.0e-3, 13.565e-3, 13.655e-3, 13.0e-3, 13.0e-3]
@@ -75,6 +77,13 @@ def lib():
         L.bgo_flags.restype = i
         L.bgo_flags.argtypes = [vp]
         L.bgo_norm_fill.argtypes = [u32, ctypes.POINTER(f), i64]
+        L.bgo_input_regular.argtypes = [vp, f, f, i, ctypes.POINTER(f)]
+        L.bgo_input_regular.restype = i
+        L.bgo_input_poisson.argtypes = [vp, f, f, ctypes.c_void_p]
+        L.bgo_input_poisson.restype = i
+        L.bgo_poisson_isi_draws.argtypes = [vp, i, ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.POINTER(ctypes.c_int32), i64]
+        L.bgo_poisson_isi_draws.restype = i64
         _lib = L
     return _lib
 
@@ -173,6 +182,31 @@ class OracleNet:
 
     def create_synapse(self, dest, src, type_, W):
         self.L.bgo_create_synapse(self.h, dest, src, type_, W)
+
+    # inputs (call input_regular before create_lif: with sync="no" it draws from the same rng)
+    def input_regular(self, duration, interval, sync, values100):
+        v = np.ascontiguousarray(values100, dtype=np.float32)
+        mode = {"yes": 0, "no": 1, "wave": 2}[sync]
+        assert self.L.bgo_input_regular(self.h, duration, interval, mode,
+                                        v.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+
+    def input_poisson(self, fr_mean, weight, masks=None):
+        m = None
+        if masks is not None:
+            self._mask = np.zeros(self.N, np.uint8)
+            self._mask[np.asarray(masks, dtype=np.int64)] = 1
+            m = self._mask.ctypes.data
+        assert self.L.bgo_input_poisson(self.h, fr_mean, weight, m) == 0
+
+    def poisson_isi_draws(self, nsteps, cap=None):
+        cap = cap or self.N * (nsteps // 5 + 4)
+        begin = np.zeros(self.N + 1, np.int32)
+        out = np.zeros(cap, np.int32)
+        k = self.L.bgo_poisson_isi_draws(self.h, int(nsteps),
+                                         begin.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap)
+        assert k >= 0
+        return begin, out[:k]
 
     # hot path
     def step_n(self, n):

@@ -37,6 +37,7 @@
 #include "Layout.h"
 #include "IRecorder.h"
 #include "tinyxml.h"
+#include "HostSInputPoisson.h"
 
 // ---------------------------------------------------------------------------------------------
 static FILE *g_out = NULL;
@@ -72,6 +73,69 @@ public:
     virtual BGFLOAT operator()() { BGFLOAT v = Norm::operator()(); drawn.push_back(v); return v; }
     std::vector<BGFLOAT> drawn;
 };
+
+// The reference's HostSInputPoisson (Inputs/HostSInputPoisson.cpp:60-94, SInputPoisson.cpp:129-146)
+// with one documented fix: its one-slot-per-neuron synapse object is indexed by neuron, not by
+// maxSynapsesPerNeuron * neuron (out of bounds whenever maxSynapsesPerNeuron > 1).  Everything
+// else — rng draws, rejection rule, synapse creation, the DS advance — is the reference's code.
+class FixedPoissonInput : public HostSInputPoisson {
+public:
+    FixedPoissonInput(SimulationInfo *psi, TiXmlElement *parms) : HostSInputPoisson(psi, parms) {}
+    virtual void init(SimulationInfo *psi)
+    {
+        if (!fSInput) return;
+        m_synapses = new AllDSSynapses(psi->totalNeurons, 1);
+        for (int i = 0; i < psi->totalNeurons; i++) {
+            synapseType type = (psi->model->getLayout()->neuron_type_map[i] == INH) ? EI : EE;
+            BGFLOAT *sum_point = &(psi->pSummationMap[i]);
+            m_synapses->createSynapse((BGSIZE)i, 0, i, sum_point, psi->deltaT, type);
+            dynamic_cast<AllSynapses *>(m_synapses)->W[i] = weight * AllSynapses::SYNAPSE_STRENGTH_ADJUSTMENT;
+        }
+    }
+    virtual void inputStimulus(SimulationInfo *psi)
+    {
+        if (!fSInput) return;
+        for (int i = 0; i < psi->totalNeurons; i++) {
+            if (!masks[i]) continue;
+            if (--nISIs[i] <= 0) {
+                dynamic_cast<AllSpikingSynapses *>(m_synapses)->preSpikeHit((BGSIZE)i);
+                BGFLOAT isi = -lambda * log(rng.inRange(0, 1));
+                while (rng.inRange(0, 1) <= exp(-(isi * isi) / 32))
+                    isi = -lambda * log(rng.inRange(0, 1));
+                nISIs[i] = static_cast<int>((isi / 1000) / psi->deltaT + 0.5);
+            }
+            m_synapses->advanceSynapse((BGSIZE)i, psi, NULL);
+        }
+    }
+    int *isis() { return nISIs; }
+    AllDSSynapses *syn() { return dynamic_cast<AllDSSynapses *>(m_synapses); }
+};
+
+static ISInput *make_input(SimulationInfo *si)
+{
+    if (si->stimulusInputFileName.empty()) return NULL;
+    TiXmlDocument doc(si->stimulusInputFileName.c_str());
+    if (!doc.LoadFile()) return NULL;
+    TiXmlElement *parms = doc.FirstChildElement("InputParams");
+    if (!parms) return NULL;
+    TiXmlElement *m = parms->FirstChildElement("IMethod");
+    std::string name;
+    if (m && m->QueryValueAttribute("name", &name) == TIXML_SUCCESS && name == "SInputPoisson")
+        return new FixedPoissonInput(si, parms);
+    return FSInput::get()->CreateInstance(si);
+}
+
+static void dump_input(SimulationInfo *si, uint64_t t)
+{
+    FixedPoissonInput *p = dynamic_cast<FixedPoissonInput *>(si->pInput);
+    if (!p || !p->syn()) return;
+    int N = si->totalNeurons;
+    AllDSSynapses *s = p->syn();
+    rec("in.nisi", t, p->isis(), N);
+    rec("in.psr", t, s->psr, N); rec("in.u", t, s->u, N); rec("in.r", t, s->r, N);
+    rec("in.lastSpike", t, s->lastSpike, N); rec("in.queue", t, s->delayQueue, N);
+    rec("in.delayIdx", t, s->delayIdx, N);
+}
 
 // Exposes the protected members of Core/Model.h:134-169.
 class HarnessModel : public SingleThreadedSpikingModel {
@@ -268,7 +332,7 @@ int main(int argc, char **argv)
     if (!FClassOfCategory::get()->readParameters(&doc)) { fprintf(stderr, "param read failed\n"); return 1; }
     si->stateOutputFileName = out + ".xml";
     si->simRecorder = si->model->getConnections()->createRecorder(si);
-    si->pInput = FSInput::get()->CreateInstance(si);
+    si->pInput = make_input(si);
 
     Simulator *sim = new Simulator();
     sim->setup(si);
@@ -304,7 +368,10 @@ int main(int argc, char **argv)
                 rec("n.count", t, &cnt, 1);
                 if (cnt) rec("n.vals", t, &rn->drawn[before], (uint64_t)cnt);
             }
-            if (dump_every > 0 && (t % dump_every) == 0) dump_neurons_step(m, si, t);
+            if (dump_every > 0 && (t % dump_every) == 0) {
+                dump_neurons_step(m, si, t);
+                dump_input(si, t);
+            }
             if (dump_syn_every > 0 && (t % dump_syn_every) == 0) dump_synapses(m, si, t, "s.");
             steps_done++;
             if (steps_limit > 0 && steps_done >= steps_limit) break;

@@ -28,9 +28,12 @@ def site_lists(width, height, frac_inh=0.10, n_starters=10, seed=1):
     return [int(x) for x in inh], [int(x) for x in starters]
 
 
+REG_VALUES = [1.5e-8 if ((i // 10) + (i % 10)) % 3 == 0 else 0.0 for i in range(100)]
+
+
 def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, radii=None,
           max_firing_rate=200, frac_inh=0.10, n_starters=10, site_seed=1, keep_steps_every=None,
-          fp64=False, config=None, inh=None, starters=None, syn_keep=None):
+          fp64=False, config=None, inh=None, starters=None, syn_keep=None, stim=None):
     if inh is None:
         inh, starters = site_lists(width, height, frac_inh, n_starters, site_seed)
     c = dict(name=name, width=width, height=height, N=width * height, tsim=tsim, epochs=epochs,
@@ -38,9 +41,12 @@ def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, r
              starters=starters, growth=dict(epsilon=0.60, beta=0.10, rho=1e-4,
                                             target_rate=target_rate, min_radius=0.1,
                                             start_radius=0.4),
-             radii=radii, keep_steps_every=keep_steps_every, fp64=fp64, syn_keep=syn_keep)
+             radii=radii, keep_steps_every=keep_steps_every, fp64=fp64, syn_keep=syn_keep,
+             stim=stim)
     c["config"] = config or "configfiles/bg3/%s.xml" % name
     args = []
+    if stim is not None:
+        args += ["-s", "configfiles/bg3/%s-stim.xml" % name]
     if radii is not None:
         args += ["--radii", repr(radii)]
     if keep_steps_every:
@@ -64,7 +70,33 @@ CASES = [
           keep_steps_every=1000, syn_keep=(9,)),
     # FP64 reference on config[0] (long-run comparison base)
     _case("c0_fp64", 10, 10, 1.0, 10, 100, fp64=True),
+    # Regular pulse input, random per-neuron phase (sync="no": shifts drawn before the neurons)
+    _case("c0_regular", 10, 10, 0.5, 2, 100, keep_steps_every=250,
+          stim=dict(kind="regular", duration=0.005, interval=0.045, sync="no", values=REG_VALUES)),
+    # Poisson input on the pre-grown network (10 Hz, weight 0.5 -> 5 nA), masked subset
+    _case("c0_poisson", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=100,
+          stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=list(range(0, 100, 3)))),
+    # Poisson input at the reference files' strength (10 Hz, weight 25), all neurons
+    _case("c0_poisson25", 10, 10, 0.2, 5, 100, max_firing_rate=1000, keep_steps_every=100,
+          stim=dict(kind="poisson", fr_mean=10.0, weight=25.0, masks=None)),
 ]
+
+
+def stim_xml(stim):
+    if stim["kind"] == "regular":
+        vals = " ".join(repr(v) for v in stim["values"])
+        return ('<?xml version="1.0" standalone="no"?>\n<InputParams>\n'
+                '  <IMethod name="SInputRegular"/>\n'
+                '  <IntParams duration="%r" interval="%r" sync="%s"/>\n'
+                '  <Values><I>%s</I></Values>\n</InputParams>\n'
+                % (stim["duration"], stim["interval"], stim["sync"], vals))
+    masks = ""
+    if stim.get("masks") is not None:
+        masks = "  <Masks><M>%s</M></Masks>\n" % " ".join(str(i) for i in stim["masks"])
+    return ('<?xml version="1.0" standalone="no"?>\n<InputParams>\n'
+            '  <IMethod name="SInputPoisson"/>\n'
+            '  <IntParams fr_mean="%r" weight="%r"/>\n%s</InputParams>\n'
+            % (stim["fr_mean"], stim["weight"], masks))
 
 
 def case(name):
@@ -134,3 +166,6 @@ def write_config_tree(cfgdir):
         with open(os.path.join(d, c["name"] + "-inh.xml"), "w") as f:
             f.write('<?xml version="1.0" encoding="UTF-8"?>\n<I>%s</I>\n'
                     % " ".join(str(i) for i in c["inh"]))
+        if c.get("stim") is not None:
+            with open(os.path.join(d, c["name"] + "-stim.xml"), "w") as f:
+                f.write(stim_xml(c["stim"]))

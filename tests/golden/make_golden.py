@@ -48,7 +48,7 @@ def compact(d, keep_steps_every=None, syn_keep=None):
     for name, recs in d.items():
         if name.startswith(("n.",)):
             continue
-        if name.startswith("s."):
+        if name.startswith(("s.", "in.")):
             for step, a in recs:
                 if keep_steps_every and step % keep_steps_every == 0:
                     out["%s@%d" % (name, step)] = a

@@ -26,7 +26,14 @@ def oracle_from_case(c, record_noise=0):
                      c["max_firing_rate"], c["epochs"])
     o.layout_grid()
     o.set_types(c["inh"], c["starters"])
+    stim = c.get("stim")
+    # FSInput::CreateInstance runs before setupSim (Core/BGDriver.cpp:72-74), so a regular
+    # input's random phases are drawn from the global rng before the neuron parameters
+    if stim and stim["kind"] == "regular":
+        o.input_regular(stim["duration"], stim["interval"], stim["sync"], stim["values"])
     o.create_lif(LIF_RANGES)
+    if stim and stim["kind"] == "poisson":
+        o.input_poisson(stim["fr_mean"], stim["weight"], stim.get("masks"))
     g = c["growth"]
     o.growth_init(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
                   g["start_radius"])

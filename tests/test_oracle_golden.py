@@ -33,7 +33,10 @@ def replay_against_fixture(name):
             o.step_n(1)
             if K and t % K == 0:
                 for f, g in (("s.Vm", "Vm"), ("s.refr", "refr"), ("s.sp", "sp"),
-                             ("s.spikeCount", "spikeCount")):
+                             ("s.spikeCount", "spikeCount"), ("in.nisi", "pois_nisi"),
+                             ("in.psr", "in_psr"), ("in.u", "in_u"), ("in.r", "in_r"),
+                             ("in.lastSpike", "in_last"), ("in.queue", "in_queue"),
+                             ("in.delayIdx", "in_delayIdx")):
                     key = "%s@%d" % (f, t)
                     if key in fx:
                         assert_same(key, o.arr(g), fx[key])
@@ -77,7 +80,8 @@ def test_norm_stream_matches_reference_tiny():
     assert np.all(np.isfinite(s)) and abs(float(np.mean(s))) < 1.5
 
 
-@pytest.mark.parametrize("name", ["ref_tiny", "c0", "c0_grown"])
+@pytest.mark.parametrize("name", ["ref_tiny", "c0", "c0_grown", "c0_regular", "c0_poisson",
+                                  "c0_poisson25"])
 def test_oracle_matches_reference_dump(name):
     o = replay_against_fixture(name)
     if name == "c0_grown":
