@@ -515,6 +515,144 @@ int bg3_push_noise(bg3_net *n, const float *v, int64_t cnt)
     return BG3_OK;
 }
 
+// ---- external input -------------------------------------------------------------------------
+int bg3_input_regular(bg3_net *n, const float *values, const int32_t *shifts, int32_t dur,
+                      int32_t cycle, int32_t in_cycle)
+{
+    if (!n || !values || !shifts || dur < 0 || cycle <= 0 || in_cycle < 0 || in_cycle >= cycle)
+        return BG3_EINVAL;
+    NetDev &h = n->h;
+    const size_t N = h.N;
+    int rc;
+    if (!h.reg_values) {
+        if ((rc = dalloc(n, &h.reg_values, N)) || (rc = dalloc(n, &h.reg_shift, N))) return rc;
+    }
+    if ((rc = h2d(n, h.reg_values, values, N)) || (rc = h2d(n, h.reg_shift, shifts, N))) return rc;
+    unsigned long long step = 0;
+    CK(cudaMemcpyAsync(&step, h.step, sizeof(step), cudaMemcpyDeviceToHost, n->stream));
+    CK(cudaStreamSynchronize(n->stream));
+    h.input_kind = 1;
+    h.reg_dur = dur;
+    h.reg_cycle = cycle;
+    h.reg_c0 = in_cycle;
+    h.reg_t0 = step;
+    if ((rc = push_desc(n))) return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+static inline uint32_t rotl32(uint32_t x, unsigned r) { r &= 31u; return r ? (x << r) | (x >> (32 - r)) : x; }
+static inline uint32_t rotr32(uint32_t x, unsigned r) { r &= 31u; return r ? (x >> r) | (x << (32 - r)) : x; }
+
+int bg3_input_poisson(bg3_net *n, const bg3_poisson_arrays *a, float lambda, uint32_t seed,
+                      uint64_t step)
+{
+    if (!n || !a || !a->nISIs || !a->total_delay || !a->delayIdx || !a->delayQueue || !a->W ||
+        !a->psr || !a->decay || !a->U || !a->D || !a->F || !a->u || !a->r || !a->lastSpike ||
+        lambda <= 0 || step >= 0xffffff00ull)
+        return BG3_EINVAL;
+    NetDev &h = n->h;
+    const size_t N = h.N;
+    int rc;
+    if (!h.pois_mask) {
+        if ((rc = dalloc(n, &h.pois_mask, N)) || (rc = dalloc(n, &h.pois_nisi, N)) ||
+            (rc = dalloc(n, &h.in_psr, N)) || (rc = dalloc(n, &h.in_decay, N)) ||
+            (rc = dalloc(n, &h.in_queue, N)) || (rc = dalloc(n, &h.in_delay, N)) ||
+            (rc = dalloc(n, &h.in_ev, N)) || (rc = dalloc(n, &h.isi_cursor, N)))
+            return rc;
+    }
+    std::vector<uint8_t> mask(N), dl(N);
+    std::vector<uint32_t> q(N);
+    std::vector<EvSlot> ev(N);
+    for (size_t i = 0; i < N; i++) {
+        if (a->total_delay[i] < 1 || a->total_delay[i] > 31 || a->delayIdx[i] < 0 || a->delayIdx[i] > 31)
+            return BG3_EINVAL;
+        uint64_t ls = a->lastSpike[i];
+        if (ls != BG3_ULONG_MAX && ls >= BG3_NO_SPIKE32) return BG3_EINVAL;
+        mask[i] = a->masks ? (a->masks[i] ? 1 : 0) : 1;
+        dl[i] = (uint8_t)a->total_delay[i];
+        unsigned phase = (unsigned)((step - (uint64_t)a->delayIdx[i]) & 31u);
+        q[i] = rotl32(a->delayQueue[i], phase);
+        EvSlot &e = ev[i];
+        e.W = a->W[i]; e.U = a->U[i]; e.D = a->D[i]; e.F = a->F[i]; e.u = a->u[i]; e.r = a->r[i];
+        e.last = (ls == BG3_ULONG_MAX) ? BG3_NO_SPIKE32 : (uint32_t)ls;
+        e.born = (uint32_t)(step - (uint64_t)a->delayIdx[i]);
+    }
+    if ((rc = h2d(n, h.pois_mask, mask.data(), N)) || (rc = h2d(n, h.pois_nisi, a->nISIs, N)) ||
+        (rc = h2d(n, h.in_psr, a->psr, N)) || (rc = h2d(n, h.in_decay, a->decay, N)) ||
+        (rc = h2d(n, h.in_queue, q.data(), N)) || (rc = h2d(n, h.in_delay, dl.data(), N)) ||
+        (rc = h2d(n, h.in_ev, ev.data(), N)))
+        return rc;
+    CK(cudaMemsetAsync(h.isi_cursor, 0, N * sizeof(int32_t), n->stream));
+    h.input_kind = 2;
+    h.pois_lambda = lambda;
+    h.pois_seed = seed;
+    if ((rc = push_desc(n))) return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_push_poisson_isis(bg3_net *n, const int32_t *begin, const int32_t *isis)
+{
+    if (!n || !begin || (!isis && begin[n->h.N] > 0) || n->h.input_kind != 2) return BG3_EINVAL;
+    NetDev &h = n->h;
+    const size_t N = h.N;
+    const size_t total = (size_t)begin[N];
+    int rc;
+    if (!h.isi_begin && (rc = dalloc(n, &h.isi_begin, N + 1))) return rc;
+    if (h.isi_vals) {  // replace the previous draws
+        cudaStreamSynchronize(n->stream);
+        for (auto &p : n->allocs)
+            if (p == (void *)h.isi_vals) { cudaFree(p); p = nullptr; }
+        h.isi_vals = nullptr;
+    }
+    if ((rc = dalloc(n, &h.isi_vals, std::max<size_t>(total, 1)))) return rc;
+    if ((rc = h2d(n, h.isi_begin, begin, N + 1)) || (rc = h2d(n, h.isi_vals, isis, total))) return rc;
+    CK(cudaMemsetAsync(h.isi_cursor, 0, N * sizeof(int32_t), n->stream));
+    if ((rc = push_desc(n))) return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_download_poisson(bg3_net *n, bg3_poisson_arrays *a)
+{
+    if (!n || !a || n->h.input_kind != 2) return BG3_EINVAL;
+    NetDev &h = n->h;
+    const size_t N = h.N;
+    std::vector<uint8_t> mask(N), dl(N);
+    std::vector<uint32_t> q(N);
+    std::vector<EvSlot> ev(N);
+    std::vector<float> psr(N), dec(N);
+    std::vector<int32_t> nisi(N);
+    unsigned long long step = 0;
+    int rc;
+    if ((rc = d2h(n, mask.data(), h.pois_mask, N)) || (rc = d2h(n, nisi.data(), h.pois_nisi, N)) ||
+        (rc = d2h(n, psr.data(), h.in_psr, N)) || (rc = d2h(n, dec.data(), h.in_decay, N)) ||
+        (rc = d2h(n, q.data(), h.in_queue, N)) || (rc = d2h(n, dl.data(), h.in_delay, N)) ||
+        (rc = d2h(n, ev.data(), h.in_ev, N)) || (rc = d2h(n, &step, h.step, 1)))
+        return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    for (size_t i = 0; i < N; i++) {
+        const EvSlot &e = ev[i];
+        uint32_t phase = e.born & 31u;
+        if (a->masks) a->masks[i] = mask[i];
+        if (a->nISIs) a->nISIs[i] = nisi[i];
+        if (a->total_delay) a->total_delay[i] = dl[i];
+        if (a->delayIdx) a->delayIdx[i] = (int32_t)(((uint32_t)step - e.born) & 31u);
+        if (a->delayQueue) a->delayQueue[i] = rotr32(q[i], phase);
+        if (a->W) a->W[i] = e.W;
+        if (a->psr) a->psr[i] = psr[i];
+        if (a->decay) a->decay[i] = dec[i];
+        if (a->U) a->U[i] = e.U;
+        if (a->D) a->D[i] = e.D;
+        if (a->F) a->F[i] = e.F;
+        if (a->u) a->u[i] = e.u;
+        if (a->r) a->r[i] = e.r;
+        if (a->lastSpike) a->lastSpike[i] = (e.last == BG3_NO_SPIKE32) ? BG3_ULONG_MAX : (uint64_t)e.last;
+    }
+    return BG3_OK;
+}
+
 // ---- hot path -------------------------------------------------------------------------------
 // Device-noise mode: neurons(t0), then per step deliver + sweep whose epilogue integrates the
 // next step's neurons, the last sweep without that epilogue.  Runs of interior steps replay a

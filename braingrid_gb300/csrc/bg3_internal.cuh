@@ -92,6 +92,21 @@ struct NetDev {
     // per-type constants for synapses created on the device
     float t_tau[4], t_U[4], t_D[4], t_F[4], t_u0, t_r0;
     int32_t t_dcls[4], t_lcls[4];
+    // external input: 0 none, 1 regular (Inputs/SInputRegular), 2 Poisson (Inputs/SInputPoisson)
+    int32_t input_kind;
+    float *reg_values;
+    int32_t *reg_shift;
+    int32_t reg_dur, reg_cycle, reg_c0;    // cycle position reg_c0 at step reg_t0
+    unsigned long long reg_t0;
+    uint8_t *pois_mask;
+    int32_t *pois_nisi;
+    float pois_lambda;
+    uint32_t pois_seed;
+    float *in_psr, *in_decay;
+    uint32_t *in_queue;                    // global-phase delay queue of the input synapse
+    uint8_t *in_delay;
+    EvSlot *in_ev;
+    int32_t *isi_begin, *isi_vals, *isi_cursor;  // injected ISI draws (NULL: device generator)
 };
 
 // device error word bits (mirrored in include/bg3.h)
@@ -103,6 +118,7 @@ enum : uint32_t {
     ERR_SPIKE_LIST = 1u << 5,
     ERR_TIMEOUT = 1u << 6,
     ERR_STEP_RANGE = 1u << 7,
+    ERR_ISI_EXHAUSTED = 1u << 8,
 };
 
 // ---- exact-rounding helpers -----------------------------------------------------------------
@@ -177,6 +193,73 @@ __device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float 
     sp = sp + noise * n.Inoise[i];
     n.Vm[i] = n.C1[i] * n.Vm[i] + n.C2[i] * sp;
     return false;
+}
+
+// ---- external input, applied to the summation point before the neuron update ----------------
+// One Poisson inter-spike interval in steps (HostSInputPoisson.cpp:81-84): exponential with mean
+// lambda ms, rejected while U <= exp(-isi^2 / 32).  Injected draws replay the reference's own
+// sequence; otherwise a Philox stream keyed by (seed, neuron, draw index).
+__device__ __forceinline__ int32_t next_isi(const NetDev &n, int i)
+{
+    const int32_t k = n.isi_cursor[i];
+    n.isi_cursor[i] = k + 1;
+    if (n.isi_begin) {
+        const int32_t p = n.isi_begin[i] + k;
+        if (p < n.isi_begin[i + 1]) return n.isi_vals[p];
+        set_err(n, ERR_ISI_EXHAUSTED);
+        return 0x3fffffff;
+    }
+    for (uint32_t a = 0; a < 64; a++) {
+        uint32_t c[4] = {(uint32_t)i, (uint32_t)k, a, 0x9e3779b9u};
+        philox4x32_10(c, n.pois_seed, n.pois_seed ^ 0x85ebca6bu);
+        float u1 = ((float)(c[0] >> 8) + 1.0f) * (1.0f / 16777216.0f);  // (0,1]
+        float u2 = (float)(c[1] >> 8) * (1.0f / 16777216.0f);
+        float isi = -n.pois_lambda * logf(u1);
+        if (u2 > expf(-(isi * isi) / 32.0f)) return (int32_t)((double)((isi / 1000.0f) / n.dt) + 0.5);
+    }
+    return (int32_t)((double)((n.pois_lambda / 1000.0f) / n.dt) + 0.5);
+}
+
+// HostSInputRegular::inputStimulus (Inputs/HostSInputRegular.cpp:59-80) and
+// HostSInputPoisson::inputStimulus (Inputs/HostSInputPoisson.cpp:60-94) for neuron i at step t:
+// returns the summation point after the input.
+__device__ __forceinline__ float input_apply(const NetDev &n, int i, unsigned long long t, float sp)
+{
+    if (n.input_kind == 1) {
+        const int cyc = (int)(((unsigned long long)n.reg_c0 + (t - n.reg_t0)) % (unsigned long long)n.reg_cycle);
+        const int sh = n.reg_shift[i];
+        if (cyc >= sh && cyc < (sh + n.reg_dur) % n.reg_cycle) sp = sp + n.reg_values[i];
+    } else if (n.input_kind == 2 && n.pois_mask[i]) {
+        int32_t c = n.pois_nisi[i] - 1;
+        uint32_t q = n.in_queue[i];
+        if (c <= 0) {
+            q |= 1u << ((uint32_t)(t + n.in_delay[i]) & 31u);
+            c = next_isi(n, i);
+        }
+        n.pois_nisi[i] = c;
+        const uint32_t bit = 1u << ((uint32_t)t & 31u);
+        float psr = n.in_psr[i];
+        const float dec = n.in_decay[i];
+        if (q & bit) {
+            q &= ~bit;
+            EvSlot e = n.in_ev[i];
+            float u = e.u, r = e.r;
+            if (e.last != BG3_NO_SPIKE32) {
+                float isi = (float)((uint32_t)t - e.last) * n.dt;
+                r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_cr(-isi / e.D);
+                u = e.U + u * (1.0f - e.U) * exp_cr(-isi / e.F);
+            }
+            psr = psr + ((e.W / dec) * u * r);
+            n.in_ev[i].u = u;
+            n.in_ev[i].r = r;
+            n.in_ev[i].last = (uint32_t)t;
+        }
+        n.in_queue[i] = q;
+        psr = psr * dec;
+        n.in_psr[i] = psr;
+        sp = sp + psr;
+    }
+    return sp;
 }
 
 // Append the firing lanes' neuron ids to ring slot (t & 63) (warp-aggregated atomic).

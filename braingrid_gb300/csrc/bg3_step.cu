@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_neurons_device(const __grid_constant__ 
     if (i < n.N) {
         int br = lif_branch(n, i);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = lif_apply(n, i, br, n.sp[i], noise, t);
+        fired = lif_apply(n, i, br, input_apply(n, i, t, n.sp[i]), noise, t);
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__
                 if (pos < n.noise_len) noise = n.noise_buf[pos];
                 else set_err(n, ERR_NOISE_EXHAUSTED);
             }
-            fired = lif_apply(n, i, br, n.sp[i], noise, t);
+            fired = lif_apply(n, i, br, input_apply(n, i, t, n.sp[i]), noise, t);
             n.sp[i] = 0.0f;
         }
         ring_push(n, t, fired, i);
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256) k_neurons_device_batch(const NetDev *nets
     if (i < n.N) {
         int br = lif_branch(n, i);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = lif_apply(n, i, br, n.sp[i], noise, t);
+        fired = lif_apply(n, i, br, input_apply(n, i, t, n.sp[i]), noise, t);
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -415,7 +415,7 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         if (valid) {
             int br = lif_branch(n, d);
             float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t1, d) : 0.0f;
-            fired = lif_apply(n, d, br, acc, noise, t1);
+            fired = lif_apply(n, d, br, input_apply(n, d, t1, acc), noise, t1);
             n.sp[d] = 0.0f;
         }
         ring_push(n, t1, fired, d);

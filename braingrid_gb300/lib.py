@@ -49,6 +49,21 @@ class SynArrays(ctypes.Structure):
                [("lastSpike", c_u64p)]
 
 
+class PoissonArrays(ctypes.Structure):
+    _fields_ = [("masks", c_u8p)] + \
+               [(k, c_i32p) for k in ("nISIs", "total_delay", "delayIdx")] + \
+               [("delayQueue", c_u32p)] + \
+               [(k, c_f32p) for k in ("W", "psr", "decay", "U", "D", "F", "u", "r")] + \
+               [("lastSpike", c_u64p)]
+
+
+POISSON_FIELDS = [("masks", np.uint8), ("nISIs", np.int32), ("total_delay", np.int32),
+                  ("delayIdx", np.int32), ("delayQueue", np.uint32), ("W", np.float32),
+                  ("psr", np.float32), ("decay", np.float32), ("U", np.float32),
+                  ("D", np.float32), ("F", np.float32), ("u", np.float32), ("r", np.float32),
+                  ("lastSpike", np.uint64)]
+
+
 class TypeConstants(ctypes.Structure):
     _fields_ = [("tau", ctypes.c_float * 4), ("decay", ctypes.c_float * 4),
                 ("total_delay", ctypes.c_int32 * 4), ("U", ctypes.c_float * 4),
@@ -96,6 +111,12 @@ def load(build_if_missing=True):
         "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
         "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
         "bg3_upload_weights": ([vp, c_f32p], ctypes.c_int),
+        "bg3_input_regular": ([vp, c_f32p, c_i32p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
+                              ctypes.c_int),
+        "bg3_input_poisson": ([vp, ctypes.POINTER(PoissonArrays), ctypes.c_float, ctypes.c_uint32,
+                               ctypes.c_uint64], ctypes.c_int),
+        "bg3_push_poisson_isis": ([vp, c_i32p, c_i32p], ctypes.c_int),
+        "bg3_download_poisson": ([vp, ctypes.POINTER(PoissonArrays)], ctypes.c_int),
         "bg3_step": ([vp, ctypes.c_int64], ctypes.c_int),
         "bg3_epoch_growth": ([vp, ctypes.c_int32], ctypes.c_int),
         "bg3_sync": ([vp], ctypes.c_int),
@@ -239,6 +260,34 @@ class Network:
         w = np.ascontiguousarray(W, np.float32)
         assert w.size == self.N * self.max_syn
         check(self.L.bg3_upload_weights(self.h, _p(w)), "bg3_upload_weights")
+
+    def input_regular(self, values, shifts, n_steps_duration, n_steps_cycle, steps_in_cycle=0):
+        v = np.ascontiguousarray(values, np.float32)
+        sh = np.ascontiguousarray(shifts, np.int32)
+        check(self.L.bg3_input_regular(self.h, _p(v), _p(sh), int(n_steps_duration),
+                                       int(n_steps_cycle), int(steps_in_cycle)),
+              "bg3_input_regular")
+
+    def input_poisson(self, lam, seed=0, step=0, **arrs):
+        keep = {}
+        s = PoissonArrays()
+        for k, dt in POISSON_FIELDS:
+            if arrs.get(k) is not None:
+                keep[k] = np.ascontiguousarray(arrs[k], dtype=dt)
+                setattr(s, k, _p(keep[k]))
+        check(self.L.bg3_input_poisson(self.h, ctypes.byref(s), float(lam), int(seed), int(step)),
+              "bg3_input_poisson")
+
+    def push_poisson_isis(self, begin, isis):
+        b = np.ascontiguousarray(begin, np.int32)
+        v = np.ascontiguousarray(isis if len(isis) else np.zeros(1), np.int32)
+        check(self.L.bg3_push_poisson_isis(self.h, _p(b), _p(v)), "bg3_push_poisson_isis")
+
+    def download_poisson(self):
+        out = {k: np.zeros(self.N, dt) for k, dt in POISSON_FIELDS}
+        s = PoissonArrays(*[_p(out[k]) for k, _ in POISSON_FIELDS])
+        check(self.L.bg3_download_poisson(self.h, ctypes.byref(s)), "bg3_download_poisson")
+        return out
 
     def push_noise(self, values):
         v = np.ascontiguousarray(values, np.float32)

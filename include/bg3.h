@@ -44,7 +44,10 @@ enum {
     BG3_ERR_ROW_FULL = 1u << 2,         /* growth wanted a synapse in a full row (AllSynapses.cpp:360) */
     BG3_ERR_NOISE_EXHAUSTED = 1u << 3,  /* injected noise stream shorter than needed                */
     BG3_ERR_NEGATIVE_AREA = 1u << 4,    /* growth saw a negative weight (the reference would erase) */
-    BG3_ERR_SPIKE_LIST = 1u << 5        /* more spikes in one step than neurons (internal check)    */
+    BG3_ERR_SPIKE_LIST = 1u << 5,       /* more spikes in one step than neurons (internal check)    */
+    BG3_ERR_TIMEOUT = 1u << 6,          /* a bounded device wait expired (the kernel drained)       */
+    BG3_ERR_STEP_RANGE = 1u << 7,       /* step counter beyond 2^32 - 256 (32-bit spike times)      */
+    BG3_ERR_ISI_EXHAUSTED = 1u << 8     /* injected Poisson ISI draws ran out                        */
 };
 
 enum { BG3_NEURON_LIF = 0, BG3_NEURON_IZH = 1 };
@@ -144,6 +147,30 @@ int bg3_upload_growth(bg3_net *net, const bg3_growth_params *p, const float *rad
 int bg3_upload_weights(bg3_net *net, const float *W);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
+
+/* ---- external input (one per network, as ISInput) --------------------------------------- */
+/* Regular pulses (Inputs/SInputRegular.cpp:20-112, HostSInputRegular.cpp:59-80): per-neuron
+ * values and phase shifts as the reference's constructor computed them, the pulse and cycle
+ * lengths in steps, and the cycle position (nStepsInCycle) at the current step. */
+int bg3_input_regular(bg3_net *net, const float *values, const int32_t *shifts,
+                      int32_t n_steps_duration, int32_t n_steps_cycle, int32_t steps_in_cycle);
+/* Poisson drive (Inputs/SInputPoisson.cpp:19-146, HostSInputPoisson.cpp:60-94): one DS input
+ * synapse per neuron (arrays of n_neurons, reference semantics), the ISI counters nISIs, masks,
+ * lambda (ms).  ISIs come from bg3_push_poisson_isis when given, else from a device generator
+ * keyed by seed.  current_step is g_simulationStep. */
+typedef struct {
+    uint8_t *masks;
+    int32_t *nISIs, *total_delay, *delayIdx;
+    uint32_t *delayQueue;
+    float *W, *psr, *decay, *U, *D, *F, *u, *r;
+    uint64_t *lastSpike;
+} bg3_poisson_arrays;
+int bg3_input_poisson(bg3_net *net, const bg3_poisson_arrays *a, float lambda, uint32_t seed,
+                      uint64_t current_step);
+/* The reference's own ISI draws per neuron in draw order (begin: n_neurons + 1 offsets), e.g.
+ * replayed from its MTRand stream; consumed from the next expiry of each neuron's counter. */
+int bg3_push_poisson_isis(bg3_net *net, const int32_t *begin, const int32_t *isis);
+int bg3_download_poisson(bg3_net *net, bg3_poisson_arrays *a);
 
 /* ---- hot path ------------------------------------------------------------------------- */
 /* nsteps of GPUSpikingModel::advance (Core/GPUSpikingModel.cu:188-230): neuron integration,

@@ -15,7 +15,43 @@ SYN_MAP = [("in_use", "in_use"), ("src", "src"), ("type", "type"), ("delayIdx", 
            ("lastSpike", "lastSpike")]
 
 
-def gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_INJECT, n_noise=0, noise_seed=None):
+POIS_MAP = [("masks", "pois_mask"), ("nISIs", "pois_nisi"), ("total_delay", "in_delay"),
+            ("delayIdx", "in_delayIdx"), ("delayQueue", "in_queue"), ("W", "in_W"),
+            ("psr", "in_psr"), ("decay", "in_decay"), ("U", "in_U"), ("D", "in_D"),
+            ("F", "in_F"), ("u", "in_u"), ("r", "in_r"), ("lastSpike", "in_last")]
+
+
+def f32_steps(seconds, dt=1e-4):
+    """static_cast<int>(seconds / deltaT + 0.5) with the float division of the reference."""
+    return int(float(np.float32(seconds) / np.float32(dt)) + 0.5)
+
+
+def setup_input(net, o, c, isi_steps=0):
+    stim = c.get("stim")
+    if not stim:
+        return
+    if stim["kind"] == "regular":
+        dur = f32_steps(stim["duration"])
+        cyc = dur + f32_steps(stim["interval"])
+        net.input_regular(o.arr("reg_values"), o.arr("reg_shift"), dur, cyc, 0)
+    else:
+        lam = np.float32(1.0) / (np.float32(stim["fr_mean"]) / np.float32(1000.0))
+        net.input_poisson(float(lam), seed=7, step=o.step,
+                          **{k: o.arr(v) for k, v in POIS_MAP})
+        if isi_steps:
+            begin, isis = o.poisson_isi_draws(isi_steps)
+            net.push_poisson_isis(begin, isis)
+
+
+def compare_input(net, o, where):
+    if o.arr("pois_nisi").size == 0:
+        return
+    g = net.download_poisson()
+    for k, v in POIS_MAP[1:]:
+        assert_same("%s input %s" % (where, k), g[k], o.arr(v))
+
+
+def gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_INJECT, n_noise=0, noise_seed=None, isi_steps=0):
     net = bg.Network(c["N"], c["max_syn"], c["width"], c["height"], c["tsim"], 1e-4,
                      c["max_firing_rate"], c["epochs"], bg.BG3_SYN_DS, noise_mode,
                      noise_seed if noise_seed is not None else c["seed"])
@@ -30,6 +66,7 @@ def gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_INJECT, n_noise=0, noise_seed=
                       g["start_radius"], o.arr("radii"), o.arr("rates"))
     if noise_mode == bg.BG3_NOISE_INJECT and n_noise:
         net.push_noise(po.norm_stream(c["seed"], n_noise))
+    setup_input(net, o, c, isi_steps)
     return net
 
 

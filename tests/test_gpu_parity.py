@@ -16,7 +16,7 @@ import pytest
 
 from braingrid_gb300 import lib as bg
 from tests.golden.configs import case
-from tests.gpu_helpers import (compare_history, compare_maps, compare_neurons,
+from tests.gpu_helpers import (compare_history, compare_input, compare_maps, compare_neurons,
                                compare_synapses, gpu_from_oracle)
 from tests.netcases import (assert_same, load_fixture, oracle_from_case, raster_from_history,
                             steps_per_epoch)
@@ -42,7 +42,7 @@ def run_locked(name, epochs=None, check_every=1, syn_every=None):
     E = epochs or c["epochs"]
     spe = steps_per_epoch(c)
     o = oracle_from_case(c)
-    net = gpu_from_oracle(o, c, n_noise=c["N"] * spe * E + 64)
+    net = gpu_from_oracle(o, c, n_noise=c["N"] * spe * E + 64, isi_steps=spe * E + 2)
     t = 0
     for e in range(E):
         for _ in range(spe):
@@ -51,6 +51,7 @@ def run_locked(name, epochs=None, check_every=1, syn_every=None):
             t += 1
             if t % check_every == 0:
                 compare_neurons(net, o, "step %d" % t)
+                compare_input(net, o, "step %d" % t)
             if syn_every and t % syn_every == 0 and o.total:
                 compare_synapses(net, o, "step %d" % t)
         compare_neurons(net, o, "epoch %d end" % e)
@@ -100,6 +101,18 @@ def test_c0_grown_gpu_raster_matches_reference_dump():
         net.growth(e + 1)
         net.upload_weights(o.arr("W"))
     assert net.error_word == 0
+
+
+def test_regular_input_bit_exact():
+    """Regular pulses with random per-neuron phases (config[0] network, 2 x 0.5 s)."""
+    o, net = run_locked("c0_regular", check_every=50)
+    assert int(o.arr("spikeCount").sum()) >= 0
+
+
+@pytest.mark.parametrize("name", ["c0_poisson", "c0_poisson25"])
+def test_poisson_input_bit_exact(name):
+    """Poisson drive with the reference's own ISI draws (masked / all neurons, growth wiring)."""
+    o, net = run_locked(name, check_every=20, syn_every=500)
 
 
 @pytest.mark.slow
