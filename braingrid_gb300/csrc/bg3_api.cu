@@ -587,6 +587,7 @@ int bg3_input_poisson(bg3_net *n, const bg3_poisson_arrays *a, float lambda, uin
     h.input_kind = 2;
     h.pois_lambda = lambda;
     h.pois_seed = seed;
+    h.pois_t0 = step;
     if ((rc = push_desc(n))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
@@ -638,7 +639,9 @@ int bg3_download_poisson(bg3_net *n, bg3_poisson_arrays *a)
         if (a->masks) a->masks[i] = mask[i];
         if (a->nISIs) a->nISIs[i] = nisi[i];
         if (a->total_delay) a->total_delay[i] = dl[i];
-        if (a->delayIdx) a->delayIdx[i] = (int32_t)(((uint32_t)step - e.born) & 31u);
+        // the reference advances the read index only of masked-in neurons' input synapses
+        const uint32_t now = mask[i] ? (uint32_t)step : (uint32_t)h.pois_t0;
+        if (a->delayIdx) a->delayIdx[i] = (int32_t)((now - e.born) & 31u);
         if (a->delayQueue) a->delayQueue[i] = rotr32(q[i], phase);
         if (a->W) a->W[i] = e.W;
         if (a->psr) a->psr[i] = psr[i];

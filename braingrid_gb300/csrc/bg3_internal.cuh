@@ -102,6 +102,7 @@ struct NetDev {
     int32_t *pois_nisi;
     float pois_lambda;
     uint32_t pois_seed;
+    unsigned long long pois_t0;            // step of bg3_input_poisson (masked-out synapses stay)
     float *in_psr, *in_decay;
     uint32_t *in_queue;                    // global-phase delay queue of the input synapse
     uint8_t *in_delay;

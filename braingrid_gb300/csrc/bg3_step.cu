@@ -11,6 +11,7 @@
 //   k_neurons_*  (t)  standalone neuron integration: the first step of a bg3_step call and every
 //                     step in injected-noise mode (the noise order needs a scan over all neurons).
 #include <cuda.h>
+#include <algorithm>
 #include <utility>
 #include "bg3_internal.cuh"
 
@@ -219,19 +220,16 @@ __global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev 
     deliver_net<SYN>(n, gw, nw, blockIdx.x == 0 && threadIdx.x == 0);
 }
 
-// Batched form: the warps of one launch take turns over the networks of the batch.
+// Batched form: grid.y indexes the network, so the networks' (short, latency-bound) delivery
+// passes run side by side.
 template <int SYN>
-__global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets, int count)
+__global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets)
 {
     pdl_wait();
     pdl_trigger();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int k = 0; k < count; k++) {
-        // rotate the starting warp per network so small networks do not all land on warp 0
-        const int rw = (gw + k * 37) % nw;
-        deliver_net<SYN>(nets[k], rw, nw, blockIdx.x == 0 && threadIdx.x == 0);
-    }
+    deliver_net<SYN>(nets[blockIdx.y], gw, nw, blockIdx.x == 0 && threadIdx.x == 0);
 }
 
 // Batched standalone neuron pass (device noise): grid.y indexes the network.
@@ -468,14 +466,14 @@ void launch_neurons(const NetDev &h, cudaStream_t s)
 }
 
 template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+static void launch_pdl(void (*kern)(KArgs...), dim3 grid, int block, size_t smem, cudaStream_t s,
                        Args &&...args)
 {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.gridDim = dim3(grid);
+    cfg.gridDim = grid;
     cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
@@ -520,8 +518,10 @@ void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t
 
 void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s)
 {
-    if (syn_kind == 1) launch_pdl(k_deliver_batch<1>, 2 * deliver_blocks(), 256, 0, s, nets, count);
-    else launch_pdl(k_deliver_batch<0>, 2 * deliver_blocks(), 256, 0, s, nets, count);
+    // per network: enough warps for a burst, few enough that the grid stays small
+    const int per_net = std::max(2, std::min(16, 608 / std::max(count, 1)));
+    if (syn_kind == 1) launch_pdl(k_deliver_batch<1>, dim3(per_net, count), 256, 0, s, nets);
+    else launch_pdl(k_deliver_batch<0>, dim3(per_net, count), 256, 0, s, nets);
 }
 
 void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int ntiles,
