@@ -114,6 +114,7 @@ struct bgo_net {
     /* IF neurons (Neurons/AllIFNeurons.h:279-362) */
     float *Vm, *Vthresh, *Vreset, *Vrest, *Vinit, *I0, *Inoise, *Iinject, *C1, *C2, *Trefract;
     float *Rm, *Cm, *Tau, *sp;
+    float *Aconst, *Bconst, *Cconst, *Dconst, *u_izh, *C3; /* Neurons/AllIZHNeurons.h:380-472 */
     int *refr, *spikeCount, *spikeCountOffset;
     uint8_t *hasFired;
     uint64_t *history; /* [N][max_spikes] */
@@ -166,6 +167,8 @@ bgo_net *bgo_create(int N, int max_syn, int width, int height, float epoch_durat
     ALLOC(n->C1, N); ALLOC(n->C2, N); ALLOC(n->Trefract, N); ALLOC(n->Rm, N); ALLOC(n->Cm, N);
     ALLOC(n->Tau, N); ALLOC(n->sp, N); ALLOC(n->refr, N); ALLOC(n->spikeCount, N);
     ALLOC(n->spikeCountOffset, N); ALLOC(n->hasFired, N);
+    ALLOC(n->Aconst, N); ALLOC(n->Bconst, N); ALLOC(n->Cconst, N); ALLOC(n->Dconst, N);
+    ALLOC(n->u_izh, N); ALLOC(n->C3, N);
     ALLOC(n->history, (size_t)N * n->max_spikes);
     for (size_t i = 0; i < (size_t)N * n->max_spikes; i++) n->history[i] = ULONG_MAX_U64;
     ALLOC(n->in_use, S); ALLOC(n->src, S); ALLOC(n->dest, S); ALLOC(n->type, S);
@@ -197,6 +200,8 @@ void bgo_destroy(bgo_net *n)
                     n->outBegin, n->outCount, n->radii, n->rates, n->burstinessHist,
                     n->spikesHistory, n->ratesHistory, n->radiiHistory, n->noise_rec};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
+    void *izh[] = {n->Aconst, n->Bconst, n->Cconst, n->Dconst, n->u_izh, n->C3};
+    for (size_t i = 0; i < sizeof(izh) / sizeof(izh[0]); i++) free(izh[i]);
     void *inp[] = {n->reg_values, n->reg_shift, n->pois_mask, n->pois_nisi, n->in_W, n->in_psr,
                    n->in_decay, n->in_U, n->in_D, n->in_F, n->in_u, n->in_r, n->in_delay,
                    n->in_delayIdx, n->in_queue, n->in_last};
@@ -228,6 +233,8 @@ void *bgo_array(bgo_net *n, const char *name, int64_t *count, int *esz)
     A("ratesHistory", n->ratesHistory, (int64_t)(n->max_epochs + 1) * N)
     A("radiiHistory", n->radiiHistory, (int64_t)(n->max_epochs + 1) * N)
     A("noise", n->noise_rec, n->noise_n)
+    A("Aconst", n->Aconst, N) A("Bconst", n->Bconst, N) A("Cconst", n->Cconst, N)
+    A("Dconst", n->Dconst, N) A("u_izh", n->u_izh, N) A("C3", n->C3, N)
     A("reg_values", n->reg_values, n->reg_values ? N : 0) A("reg_shift", n->reg_shift, n->reg_shift ? N : 0)
     A("pois_nisi", n->pois_nisi, n->pois_nisi ? N : 0) A("pois_mask", n->pois_mask, n->pois_mask ? N : 0)
     A("in_psr", n->in_psr, n->in_psr ? N : 0) A("in_u", n->in_u, n->in_u ? N : 0)
@@ -275,9 +282,32 @@ void bgo_set_types(bgo_net *n, const int *inh, int n_inh, const int *st, int n_s
  * initNeuronConstsFromParamValues (Neurons/AllIFNeurons.cpp:380-503).  The draws come from the
  * global rng in neuron order: Iinject, Inoise, Vthresh, Vrest, Vreset, Vinit, then for starters
  * Vthresh and Vreset again. */
+static void create_if_neuron(bgo_net *n, const float *g, int i);
 void bgo_create_lif(bgo_net *n, const float *g)
 {
+    for (int i = 0; i < n->N; i++) create_if_neuron(n, g, i);
+}
+
+/* AllIZHNeurons::setNeuronDefaults / createNeuron / initNeuronConstsFromParamValues: the IF
+ * draws first (AllIFNeurons::createNeuron), then a, b, c, d by neuron type, u = 0,
+ * C3 = deltaT * 1000. */
+void bgo_create_izh(bgo_net *n, const float *g, const float *z)
+{
     for (int i = 0; i < n->N; i++) {
+        create_if_neuron(n, g, i);
+        n->C3[i] = n->delta_t * 1000.0f;
+        int inh = n->ntype[i] != BGO_EXC;
+        n->Aconst[i] = bgo_mt_inrange(&n->rng, z[0 + 2 * inh], z[1 + 2 * inh]);
+        n->Bconst[i] = bgo_mt_inrange(&n->rng, z[4 + 2 * inh], z[5 + 2 * inh]);
+        n->Cconst[i] = bgo_mt_inrange(&n->rng, z[8 + 2 * inh], z[9 + 2 * inh]);
+        n->Dconst[i] = bgo_mt_inrange(&n->rng, z[12 + 2 * inh], z[13 + 2 * inh]);
+        n->u_izh[i] = 0.0f;
+    }
+}
+
+static void create_if_neuron(bgo_net *n, const float *g, int i)
+{
+    {
         n->Cm[i] = (float)3e-8;     /* DEFAULT_Cm (Utils/Global.h:103) */
         n->Rm[i] = (float)1e6;      /* DEFAULT_Rm */
         n->Tau[i] = (float)(3e-8 * 1e6);
@@ -603,11 +633,42 @@ static void pre_spike_hit(bgo_net *n, uint32_t s)
     n->queue[s] |= (1u << idx);
 }
 
+/* AllIZHNeurons::advanceNeuron / fire (Neurons/AllIZHNeurons.cpp:570-655): the Euler step in
+ * mV with the reference's double literals (0.04, 0.001) promoting parts of it to double. */
+static void izh_advance(bgo_net *n, int i)
+{
+    if (n->refr[i] > 0) {
+        --n->refr[i];
+    } else if (n->Vm[i] >= n->Vthresh[i]) {
+        n->hasFired[i] = 1;
+        int idxSp = (n->spikeCount[i] + n->spikeCountOffset[i]) % n->max_spikes;
+        n->history[(size_t)i * n->max_spikes + idxSp] = n->step;
+        n->spikeCount[i]++;
+        n->refr[i] = (int)((double)(n->Trefract[i] / n->delta_t) + 0.5);
+        n->Vm[i] = (float)((double)n->Cconst[i] * 0.001);
+        n->u_izh[i] = n->u_izh[i] + n->Dconst[i];
+    } else {
+        n->sp[i] += n->I0[i];
+        float noise = bgo_norm_next(&n->noise);
+        if (n->noise_rec && n->noise_n < n->noise_cap) n->noise_rec[n->noise_n++] = noise;
+        n->sp[i] += noise * n->Inoise[i];
+        float Vint = n->Vm[i] * 1000.0f;
+        float u = n->u_izh[i], C3 = n->C3[i];
+        float Vb = (float)((double)Vint +
+                           (double)C3 * (0.04 * (double)Vint * (double)Vint + (double)(5.0f * Vint) +
+                                         140.0 - (double)u));
+        n->u_izh[i] = u + C3 * n->Aconst[i] * (n->Bconst[i] * Vint - u);
+        n->Vm[i] = (float)((double)Vb * 0.001 + (double)(n->C2[i] * n->sp[i]));
+    }
+    n->sp[i] = 0.0f;
+}
+
 /* AllSpikingNeurons::advanceNeurons (Neurons/AllSpikingNeurons.cpp:98-147): descending index. */
 static void advance_neurons(bgo_net *n)
 {
     for (int i = n->N - 1; i >= 0; --i) {
-        lif_advance(n, i);
+        if (n->neuron_kind == BGO_IZH) izh_advance(n, i);
+        else lif_advance(n, i);
         if (n->hasFired[i]) {
             if (n->total > 0) {
                 uint32_t c = n->outCount[i], b = n->outBegin[i];

@@ -59,6 +59,9 @@ void bgo_set_types(bgo_net *n, const int *inh, int n_inh, const int *starters, i
 /* LIF ranges, in order: Iinject, Inoise, Vthresh, Vresting, Vreset, Vinit, starter_Vthresh,
  * starter_Vreset — each as (min, max): 16 floats.  Draws from the global rng seeded 1. */
 void bgo_create_lif(bgo_net *n, const float *ranges16);
+/* Izhikevich neurons (Neurons/AllIZHNeurons.cpp:405-476): the 16 IF ranges as for LIF, then
+ * for each of a, b, c, d: (minExc, maxExc, minInh, maxInh) — 16 floats. */
+void bgo_create_izh(bgo_net *n, const float *ranges16, const float *izh16);
 void bgo_growth_init(bgo_net *n, float epsilon, float beta, float rho, float target_rate,
                      float min_radius, float start_radius);
 void bgo_seed_noise(bgo_net *n, uint32_t seed);

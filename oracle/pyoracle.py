@@ -63,6 +63,7 @@ def lib():
         L.bgo_layout_grid.argtypes = [vp]
         L.bgo_set_types.argtypes = [vp, ctypes.POINTER(i), i, ctypes.POINTER(i), i]
         L.bgo_create_lif.argtypes = [vp, ctypes.POINTER(f)]
+        L.bgo_create_izh.argtypes = [vp, ctypes.POINTER(f), ctypes.POINTER(f)]
         L.bgo_growth_init.argtypes = [vp, f, f, f, f, f, f]
         L.bgo_seed_noise.argtypes = [vp, u32]
         L.bgo_rebuild_maps.restype = i
@@ -111,6 +112,7 @@ class OracleNet:
         self.N, self.max_syn = N, max_syn
         self.epoch_duration, self.delta_t = epoch_duration, delta_t
         self.max_epochs = max_epochs
+        self.neuron_kind, self.synapse_kind = neuron_kind, synapse_kind
 
     def close(self):
         if self.h:
@@ -167,6 +169,12 @@ class OracleNet:
     def create_lif(self, ranges16=LIF_CONFIG0_RANGES):
         g = np.asarray(ranges16, dtype=np.float32)
         self.L.bgo_create_lif(self.h, g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+
+    def create_izh(self, ranges16, izh16):
+        g = np.asarray(ranges16, dtype=np.float32)
+        z = np.asarray(izh16, dtype=np.float32)
+        self.L.bgo_create_izh(self.h, g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                              z.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
 
     def growth_init(self, epsilon, beta, rho, target_rate, min_radius, start_radius):
         self.L.bgo_growth_init(self.h, epsilon, beta, rho, target_rate, min_radius, start_radius)

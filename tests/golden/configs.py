@@ -28,12 +28,21 @@ def site_lists(width, height, frac_inh=0.10, n_starters=10, seed=1):
     return [int(x) for x in inh], [int(x) for x in starters]
 
 
+# static_izh_1000-style Izhikevich parameters: IF ranges, then a, b, c, d (minExc, maxExc,
+# minInh, maxInh)
+IZH_IF_RANGES = [13.5e-9, 13.5e-9, 0.5e-6, 0.7329e-6, 30.0e-3, 30.0e-3, 0.0, 0.0,
+                 -0.065, -0.065, -0.065, -0.065, 13.565e-3, 13.655e-3, 13.0e-3, 13.0e-3]
+IZH_RANGES = [0.02, 0.02, 0.02, 0.1, 0.2, 0.2, 0.2, 0.25, -65.0, -50.0, -65.0, -65.0,
+              2.0, 8.0, 2.0, 2.0]
+SYN_CLASS = {1: "AllDSSynapses", 0: "AllSpikingSynapses"}
+
 REG_VALUES = [1.5e-8 if ((i // 10) + (i % 10)) % 3 == 0 else 0.0 for i in range(100)]
 
 
 def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, radii=None,
           max_firing_rate=200, frac_inh=0.10, n_starters=10, site_seed=1, keep_steps_every=None,
-          fp64=False, config=None, inh=None, starters=None, syn_keep=None, stim=None):
+          fp64=False, config=None, inh=None, starters=None, syn_keep=None, stim=None,
+          neuron="lif", synapse=1):
     if inh is None:
         inh, starters = site_lists(width, height, frac_inh, n_starters, site_seed)
     c = dict(name=name, width=width, height=height, N=width * height, tsim=tsim, epochs=epochs,
@@ -42,7 +51,7 @@ def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, r
                                             target_rate=target_rate, min_radius=0.1,
                                             start_radius=0.4),
              radii=radii, keep_steps_every=keep_steps_every, fp64=fp64, syn_keep=syn_keep,
-             stim=stim)
+             stim=stim, neuron=neuron, synapse=synapse)
     c["config"] = config or "configfiles/bg3/%s.xml" % name
     args = []
     if stim is not None:
@@ -79,6 +88,12 @@ CASES = [
     # Poisson input at the reference files' strength (10 Hz, weight 25), all neurons
     _case("c0_poisson25", 10, 10, 0.2, 5, 100, max_firing_rate=1000, keep_steps_every=100,
           stim=dict(kind="poisson", fr_mean=10.0, weight=25.0, masks=None)),
+    # Izhikevich neurons, DS synapses, pre-grown 12x12 network
+    _case("izh_grown", 12, 12, 0.2, 5, 100, radii=1.3, max_firing_rate=1000, site_seed=4,
+          keep_steps_every=100, neuron="izh"),
+    # LIF neurons with plain spiking synapses (AllSpikingSynapses), pre-grown
+    _case("c0_spiking", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=100,
+          synapse=0),
 ]
 
 
@@ -119,17 +134,10 @@ _XML = """<?xml version="1.0" encoding="UTF-8" standalone="no"?>
     <OutputParams name="OutputParams"><stateOutputFileName name="stateOutputFileName">results/{name}-out.xml</stateOutputFileName></OutputParams>
   </SimInfoParams>
   <ModelParams>
-    <NeuronsParams class="AllLIFNeurons" name="NeuronsParams">
-      <Iinject name="Iinject"><min name="min">13.5e-09</min><max name="max">13.5e-09</max></Iinject>
-      <Inoise name="Inoise"><min name="min">1.0e-09</min><max name="max">1.5e-09</max></Inoise>
-      <Vthresh name="Vthresh"><min name="min">15.0e-03</min><max name="max">15.0e-03</max></Vthresh>
-      <Vresting name="Vresting"><min name="min">0.0</min><max name="max">0.0</max></Vresting>
-      <Vreset name="Vreset"><min name="min">13.5e-03</min><max name="max">13.5e-03</max></Vreset>
-      <Vinit name="Vinit"><min name="min">13.0e-03</min><max name="max">13.0e-03</max></Vinit>
-      <starter_vthresh name="starter_vthresh"><min name="min">13.565e-3</min><max name="max">13.655e-3</max></starter_vthresh>
-      <starter_vreset name="starter_vreset"><min name="min">13.0e-3</min><max name="max">13.0e-3</max></starter_vreset>
+    <NeuronsParams class="{neuron_class}" name="NeuronsParams">
+{neuron_params}
     </NeuronsParams>
-    <SynapsesParams class="AllDSSynapses" name="SynapsesParams"></SynapsesParams>
+    <SynapsesParams class="{synapse_class}" name="SynapsesParams"></SynapsesParams>
     <ConnectionsParams class="ConnGrowth" name="ConnectionsParams">
       <GrowthParams name="GrowthParams">
         <epsilon name="epsilon">{epsilon}</epsilon><beta name="beta">{beta}</beta><rho name="rho">{rho}</rho>
@@ -149,6 +157,25 @@ _XML = """<?xml version="1.0" encoding="UTF-8" standalone="no"?>
 """
 
 
+def _range_xml(ranges):
+    names = ["Iinject", "Inoise", "Vthresh", "Vresting", "Vreset", "Vinit", "starter_vthresh",
+             "starter_vreset"]
+    return "\n".join('      <%s name="%s"><min name="min">%r</min><max name="max">%r</max></%s>'
+                     % (nm, nm, ranges[2 * k], ranges[2 * k + 1], nm)
+                     for k, nm in enumerate(names))
+
+
+def _izh_xml(z):
+    return "\n".join('      <%s name="%s"><minExc name="minExc">%r</minExc><maxExc name="maxExc">%r'
+                     '</maxExc><minInh name="minInh">%r</minInh><maxInh name="maxInh">%r</maxInh>'
+                     '</%s>' % (nm, nm, z[4 * k], z[4 * k + 1], z[4 * k + 2], z[4 * k + 3], nm)
+                     for k, nm in enumerate(["Aconst", "Bconst", "Cconst", "Dconst"]))
+
+
+def neuron_ranges(c):
+    return IZH_IF_RANGES if c.get("neuron") == "izh" else LIF_RANGES
+
+
 def write_config_tree(cfgdir):
     """Write configfiles/bg3/<case>.xml and its NLists for every generated case."""
     d = os.path.join(cfgdir, "bg3")
@@ -158,6 +185,13 @@ def write_config_tree(cfgdir):
             continue
         p = dict(c)
         p.update(c["growth"])
+        p["synapse_class"] = SYN_CLASS[c.get("synapse", 1)]
+        if c.get("neuron") == "izh":
+            p["neuron_class"] = "AllIZHNeurons"
+            p["neuron_params"] = _range_xml(IZH_IF_RANGES) + "\n" + _izh_xml(IZH_RANGES)
+        else:
+            p["neuron_class"] = "AllLIFNeurons"
+            p["neuron_params"] = _range_xml(LIF_RANGES)
         with open(os.path.join(d, c["name"] + ".xml"), "w") as f:
             f.write(_XML.format(**p))
         with open(os.path.join(d, c["name"] + "-active.xml"), "w") as f:

@@ -4,7 +4,7 @@ import os
 import numpy as np
 
 from oracle import pyoracle as po
-from tests.golden.configs import LIF_RANGES, case
+from tests.golden.configs import IZH_IF_RANGES, IZH_RANGES, LIF_RANGES, case
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -22,8 +22,10 @@ def load_fixture(name):
 
 def oracle_from_case(c, record_noise=0):
     """Set up an oracle network exactly as Model::setupSim does for this case."""
+    izh = c.get("neuron") == "izh"
     o = po.OracleNet(c["N"], c["max_syn"], c["width"], c["height"], c["tsim"], 1e-4,
-                     c["max_firing_rate"], c["epochs"])
+                     c["max_firing_rate"], c["epochs"], neuron_kind=1 if izh else 0,
+                     synapse_kind=c.get("synapse", 1))
     o.layout_grid()
     o.set_types(c["inh"], c["starters"])
     stim = c.get("stim")
@@ -31,7 +33,10 @@ def oracle_from_case(c, record_noise=0):
     # input's random phases are drawn from the global rng before the neuron parameters
     if stim and stim["kind"] == "regular":
         o.input_regular(stim["duration"], stim["interval"], stim["sync"], stim["values"])
-    o.create_lif(LIF_RANGES)
+    if izh:
+        o.create_izh(IZH_IF_RANGES, IZH_RANGES)
+    else:
+        o.create_lif(LIF_RANGES)
     if stim and stim["kind"] == "poisson":
         o.input_poisson(stim["fr_mean"], stim["weight"], stim.get("masks"))
     g = c["growth"]

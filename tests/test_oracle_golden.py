@@ -23,6 +23,10 @@ def replay_against_fixture(name):
     N, ms = c["N"], int(fx["hdr"][4])
     for k in SETUP:
         assert_same(k, o.arr(k), fx[k])
+    for k, g in (("Aconst", "Aconst"), ("Bconst", "Bconst"), ("Cconst", "Cconst"),
+                 ("Dconst", "Dconst"), ("u", "u_izh"), ("C3", "C3")):
+        if k in fx:
+            assert_same(k, o.arr(g), fx[k])
     assert_same("ntype", o.arr("ntype"), fx["ntype"])
     assert_same("radii0", o.arr("radii"), fx["radii"])
     K = c.get("keep_steps_every")
@@ -32,7 +36,7 @@ def replay_against_fixture(name):
         for _ in range(spe):
             o.step_n(1)
             if K and t % K == 0:
-                for f, g in (("s.Vm", "Vm"), ("s.refr", "refr"), ("s.sp", "sp"),
+                for f, g in (("s.Vm", "Vm"), ("s.refr", "refr"), ("s.sp", "sp"), ("s.u", "u_izh"),
                              ("s.spikeCount", "spikeCount"), ("in.nisi", "pois_nisi"),
                              ("in.psr", "in_psr"), ("in.u", "in_u"), ("in.r", "in_r"),
                              ("in.lastSpike", "in_last"), ("in.queue", "in_queue"),
@@ -81,7 +85,7 @@ def test_norm_stream_matches_reference_tiny():
 
 
 @pytest.mark.parametrize("name", ["ref_tiny", "c0", "c0_grown", "c0_regular", "c0_poisson",
-                                  "c0_poisson25"])
+                                  "c0_poisson25", "izh_grown", "c0_spiking"])
 def test_oracle_matches_reference_dump(name):
     o = replay_against_fixture(name)
     if name == "c0_grown":
