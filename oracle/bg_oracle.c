@@ -124,6 +124,14 @@ struct bgo_net {
     float *W, *psr, *decay, *tau, *r, *u, *D, *U, *F;
     uint32_t *queue, *counts;
     uint64_t *lastSpike;
+    /* STDP slots (Synapses/AllSTDPSynapses.h:330-420), allocated for the STDP kinds only */
+    int *total_delayPost, *delayIdxPost, *ldelayQueuePost;
+    uint32_t *queuePost;
+    float *tauspost, *tauspre, *taupos, *tauneg, *STDPgap, *Wex, *Aneg, *Apos, *mupos, *muneg;
+    uint8_t *useFD;
+    int stdp_signed; /* 0: host build's arithmetic, 1: device build's (signed spike times) */
+    int stdp_override;
+    float stdp_p[11]; /* Apos, Aneg, STDPgap, tauspost, tauspre, taupos, tauneg, WexE, WexI, mupos, muneg */
     /* SynapseIndexMap (Core/SynapseIndexMap.h:38-104) */
     uint32_t *inMap, *inBegin, *inCount, *outMap, *outBegin, *outCount;
     int64_t total;
@@ -177,6 +185,12 @@ bgo_net *bgo_create(int N, int max_syn, int width, int height, float epoch_durat
     ALLOC(n->u, S); ALLOC(n->D, S); ALLOC(n->U, S); ALLOC(n->F, S); ALLOC(n->queue, S);
     ALLOC(n->lastSpike, S); ALLOC(n->counts, N);
     for (size_t i = 0; i < S; i++) n->type[i] = -1;
+    if (synapse_kind == BGO_SYN_STDP || synapse_kind == BGO_SYN_DSTDP) {
+        ALLOC(n->total_delayPost, S); ALLOC(n->delayIdxPost, S); ALLOC(n->ldelayQueuePost, S);
+        ALLOC(n->queuePost, S); ALLOC(n->tauspost, S); ALLOC(n->tauspre, S); ALLOC(n->taupos, S);
+        ALLOC(n->tauneg, S); ALLOC(n->STDPgap, S); ALLOC(n->Wex, S); ALLOC(n->Aneg, S);
+        ALLOC(n->Apos, S); ALLOC(n->mupos, S); ALLOC(n->muneg, S); ALLOC(n->useFD, S);
+    }
     ALLOC(n->inMap, S); ALLOC(n->outMap, S);
     ALLOC(n->inBegin, N); ALLOC(n->inCount, N); ALLOC(n->outBegin, N); ALLOC(n->outCount, N);
     ALLOC(n->radii, N); ALLOC(n->rates, N);
@@ -206,6 +220,10 @@ void bgo_destroy(bgo_net *n)
                    n->in_decay, n->in_U, n->in_D, n->in_F, n->in_u, n->in_r, n->in_delay,
                    n->in_delayIdx, n->in_queue, n->in_last};
     for (size_t i = 0; i < sizeof(inp) / sizeof(inp[0]); i++) free(inp[i]);
+    void *stdp[] = {n->total_delayPost, n->delayIdxPost, n->ldelayQueuePost, n->queuePost,
+                    n->tauspost, n->tauspre, n->taupos, n->tauneg, n->STDPgap, n->Wex, n->Aneg,
+                    n->Apos, n->mupos, n->muneg, n->useFD};
+    for (size_t i = 0; i < sizeof(stdp) / sizeof(stdp[0]); i++) free(stdp[i]);
     free(n);
 }
 
@@ -243,6 +261,15 @@ void *bgo_array(bgo_net *n, const char *name, int64_t *count, int *esz)
     A("in_W", n->in_W, n->in_W ? N : 0) A("in_decay", n->in_decay, n->in_decay ? N : 0)
     A("in_delay", n->in_delay, n->in_delay ? N : 0) A("in_U", n->in_U, n->in_U ? N : 0)
     A("in_D", n->in_D, n->in_D ? N : 0) A("in_F", n->in_F, n->in_F ? N : 0)
+    {
+        int64_t P = n->queuePost ? S : 0;
+        A("queuePost", n->queuePost, P) A("delayIdxPost", n->delayIdxPost, P)
+        A("total_delayPost", n->total_delayPost, P) A("ldelayQueuePost", n->ldelayQueuePost, P)
+        A("tauspost", n->tauspost, P) A("tauspre", n->tauspre, P) A("taupos", n->taupos, P)
+        A("tauneg", n->tauneg, P) A("STDPgap", n->STDPgap, P) A("Wex", n->Wex, P)
+        A("Aneg", n->Aneg, P) A("Apos", n->Apos, P) A("mupos", n->mupos, P)
+        A("muneg", n->muneg, P) A("useFD", n->useFD, P)
+    }
 #undef A
     *count = 0; *esz = 0;
     return NULL;
@@ -252,6 +279,12 @@ uint64_t bgo_get_step(const bgo_net *n) { return n->step; }
 void bgo_set_step(bgo_net *n, uint64_t s) { n->step = s; }
 int64_t bgo_total_synapses(const bgo_net *n) { return n->total; }
 int bgo_flags(const bgo_net *n) { return n->flags; }
+void bgo_stdp_signed(bgo_net *n, int on) { n->stdp_signed = on ? 1 : 0; }
+void bgo_stdp_params(bgo_net *n, const float *p11)
+{
+    n->stdp_override = 1;
+    memcpy(n->stdp_p, p11, sizeof(n->stdp_p));
+}
 
 void bgo_record_noise(bgo_net *n, int64_t cap)
 {
@@ -385,6 +418,32 @@ static void create_synapse_slot(bgo_net *n, size_t iSyn, int src, int dest, int 
         default:     U = (float)0.5; D = (float)1.1; F = (float)0.05; break;
         }
         n->U[iSyn] = U; n->D[iSyn] = D; n->F[iSyn] = F;
+    }
+    if (n->queuePost) {
+        /* AllSTDPSynapses::initSpikeQueue (:125-138) and createSynapse (:252-273) */
+        n->queuePost[iSyn] = 0;
+        n->delayIdxPost[iSyn] = 0;
+        n->ldelayQueuePost[iSyn] = LDELAYQUEUE;
+        n->Apos[iSyn] = (float)0.5;
+        n->Aneg[iSyn] = (float)-0.5;
+        n->STDPgap[iSyn] = (float)2e-3;
+        n->total_delayPost[iSyn] = 0;
+        n->tauspost[iSyn] = (float)75e-3;
+        n->tauspre[iSyn] = (float)34e-3;
+        n->taupos[iSyn] = (float)15e-3;
+        n->tauneg[iSyn] = (float)35e-3;
+        n->Wex[iSyn] = (float)1.0;
+        n->mupos[iSyn] = 0.0f;
+        n->muneg[iSyn] = 0.0f;
+        n->useFD[iSyn] = 1;
+        if (n->stdp_override) {
+            const float *p = n->stdp_p;
+            n->Apos[iSyn] = p[0]; n->Aneg[iSyn] = p[1]; n->STDPgap[iSyn] = p[2];
+            n->tauspost[iSyn] = p[3]; n->tauspre[iSyn] = p[4]; n->taupos[iSyn] = p[5];
+            n->tauneg[iSyn] = p[6];
+            n->Wex[iSyn] = (type == BGO_II || type == BGO_IE) ? p[8] : p[7];
+            n->mupos[iSyn] = p[9]; n->muneg[iSyn] = p[10];
+        }
     }
 }
 
@@ -626,6 +685,7 @@ static void lif_advance(bgo_net *n, int i)
 }
 
 /* AllSpikingSynapses::preSpikeHit (Synapses/AllSpikingSynapses.cpp:261-279). */
+static void post_spike_hit(bgo_net *n, size_t s);
 static void pre_spike_hit(bgo_net *n, uint32_t s)
 {
     int idx = n->delayIdx[s] + n->total_delay[s];
@@ -674,6 +734,14 @@ static void advance_neurons(bgo_net *n)
                 uint32_t c = n->outCount[i], b = n->outBegin[i];
                 for (uint32_t k = 0; k < c; k++) pre_spike_hit(n, n->outMap[b + k]);
             }
+            if (n->queuePost) {
+                /* back propagation to the in-use incoming synapses (:128-138) */
+                uint32_t notified = 0;
+                for (int z = 0; notified < n->counts[i]; z++) {
+                    size_t s = (size_t)n->max_syn * i + z;
+                    if (n->in_use[s]) { post_spike_hit(n, s); notified++; }
+                }
+            }
             n->hasFired[i] = 0;
         }
     }
@@ -691,22 +759,150 @@ static void ds_change_psr(bgo_net *n, size_t s)
     n->lastSpike[s] = n->step;
 }
 
+/* ---- STDP (Synapses/AllSTDPSynapses.cpp:283-517, device form AllSynapsesDeviceFuncs_d.cu:100-380).
+ * The host build keeps spike times as uint64_t, so (spikeHistory - step) in the pre-spike walk
+ * wraps to a huge positive interval and that walk only applies the sign and |Wex| clamps; the
+ * device build holds them in int64_t and depresses.  stdp_signed selects the device form.  A
+ * history walk that would pass the oldest entry of a full ring (where the host build reads
+ * outside the ring) stops there and raises flag 4. */
+
+/* AllSpikingNeurons::getSpikeHistory (Neurons/AllSpikingNeurons.cpp:182-188); returns 0 when the
+ * ring index would be negative. */
+static int spike_history(const bgo_net *n, int idx, int off, uint64_t *out)
+{
+    int x = n->spikeCount[idx] + n->spikeCountOffset[idx] + n->max_spikes + off;
+    if (x < 0) return 0;
+    *out = n->history[(size_t)idx * n->max_spikes + x % n->max_spikes];
+    return 1;
+}
+
+/* AllSTDPSynapses::stdpLearning (:432-472) */
+static void stdp_learning(bgo_net *n, size_t s, double delta, double epost, double epre)
+{
+    float gap = n->STDPgap[s], Wex = n->Wex[s];
+    float W = n->W[s];
+    float dw;
+    if (delta < -gap)
+        dw = (float)((double)(powf(W, n->muneg[s]) * n->Aneg[s]) * exp(delta / n->tauneg[s]));
+    else if (delta > gap)
+        dw = (float)((double)(powf(Wex - W, n->mupos[s]) * n->Apos[s]) * exp(-delta / n->taupos[s]));
+    else
+        return;
+    W = (float)((double)W + epost * epre * dw);
+    if ((Wex < 0 && W > 0) || (Wex > 0 && W < 0)) W = 0;
+    if (fabsf(W) > fabsf(Wex)) W = Wex;
+    n->W[s] = W;
+}
+
+/* Interval in seconds between spike times a - b as the chosen build computes it. */
+static float stdp_interval(const bgo_net *n, uint64_t a, uint64_t b)
+{
+    if (n->stdp_signed) return (float)(int64_t)(a - b) * n->delta_t;
+    return (float)(a - b) * n->delta_t;
+}
+
+static void stdp_pre(bgo_net *n, size_t s)
+{
+    int pre = n->src[s], post = n->dest[s];
+    uint64_t sh, sh2;
+    float delta, epre, epost;
+    int have = spike_history(n, pre, -2, &sh);
+    int ok = have && (n->stdp_signed ? ((int64_t)sh > 0) : (sh != ULONG_MAX_U64));
+    if (ok && n->useFD[s]) {
+        delta = stdp_interval(n, n->step, sh);
+        epre = (float)(1.0 - (double)expf(-delta / n->tauspre[s]));
+    } else {
+        epre = 1.0f;
+    }
+    for (int off = -1;; --off) {
+        if (off < -n->max_spikes || !spike_history(n, post, off, &sh)) { n->flags |= 4; break; }
+        if (sh == ULONG_MAX_U64) break;
+        delta = stdp_interval(n, sh, n->step);
+        if ((double)delta <= -3.0 * (double)n->tauneg[s]) break;
+        if (n->useFD[s]) {
+            if (off - 1 < -n->max_spikes || !spike_history(n, post, off - 1, &sh2)) {
+                n->flags |= 4;
+                break;
+            }
+            if (sh2 == ULONG_MAX_U64) break;
+            epost = (float)(1.0 - (double)expf(-stdp_interval(n, sh, sh2) / n->tauspost[s]));
+        } else {
+            epost = 1.0f;
+        }
+        stdp_learning(n, s, delta, epost, epre);
+    }
+}
+
+static void stdp_post(bgo_net *n, size_t s)
+{
+    int pre = n->src[s], post = n->dest[s];
+    uint64_t sh, sh2;
+    float delta, epre, epost;
+    int have = spike_history(n, post, -2, &sh);
+    int ok = have && (n->stdp_signed ? ((int64_t)sh > 0) : (sh != ULONG_MAX_U64));
+    if (ok && n->useFD[s]) {
+        delta = stdp_interval(n, n->step, sh);
+        epost = (float)(1.0 - (double)expf(-delta / n->tauspost[s]));
+    } else {
+        epost = 1.0f;
+    }
+    for (int off = -1;; --off) {
+        if (off < -n->max_spikes || !spike_history(n, pre, off, &sh)) { n->flags |= 4; break; }
+        if (sh == ULONG_MAX_U64) break;
+        /* ((int64_t)step - spikeHistory - total_delay) */
+        delta = stdp_interval(n, n->step - (uint64_t)(int64_t)n->total_delay[s], sh);
+        if (delta <= 0 || (double)delta >= 3.0 * (double)n->taupos[s]) break;
+        if (n->useFD[s]) {
+            if (off - 1 < -n->max_spikes || !spike_history(n, pre, off - 1, &sh2)) {
+                n->flags |= 4;
+                break;
+            }
+            if (sh2 == ULONG_MAX_U64) break;
+            epre = (float)(1.0 - (double)expf(-stdp_interval(n, sh, sh2) / n->tauspre[s]));
+        } else {
+            epre = 1.0f;
+        }
+        stdp_learning(n, s, delta, epost, epre);
+    }
+}
+
+/* AllSTDPSynapses::postSpikeHit (:499-517) */
+static void post_spike_hit(bgo_net *n, size_t s)
+{
+    int idx = n->delayIdxPost[s] + n->total_delayPost[s];
+    if (idx >= n->ldelayQueuePost[s]) idx -= n->ldelayQueuePost[s];
+    if (n->queuePost[s] & (1u << idx)) n->flags |= 8;
+    n->queuePost[s] |= (1u << idx);
+}
+
 /* AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331) over the incoming map, with
- * AllSpikingSynapses::advanceSynapse / isSpikeQueue (AllSpikingSynapses.cpp:242-319). */
+ * AllSpikingSynapses::advanceSynapse / isSpikeQueue (AllSpikingSynapses.cpp:242-319) and, for
+ * the STDP kinds, AllSTDPSynapses::advanceSynapse / isSpikeQueuePost (:283-421, :480-492). */
 static void advance_synapses(bgo_net *n)
 {
+    const int stdp = n->queuePost != NULL;
+    const int ds = n->syn_kind == BGO_SYN_DS || n->syn_kind == BGO_SYN_DSTDP;
     for (int64_t q = 0; q < n->total; q++) {
         uint32_t s = n->inMap[q];
         uint32_t bit = 1u << n->delayIdx[s];
         int hit = (n->queue[s] & bit) != 0;
         n->queue[s] &= ~bit;
         if (++n->delayIdx[s] >= n->ldelayQueue[s]) n->delayIdx[s] = 0;
+        int post = 0;
+        if (stdp) {
+            uint32_t pb = 1u << n->delayIdxPost[s];
+            post = (n->queuePost[s] & pb) != 0;
+            n->queuePost[s] &= ~pb;
+            if (++n->delayIdxPost[s] >= n->ldelayQueuePost[s]) n->delayIdxPost[s] = 0;
+        }
         if (hit) {
-            if (n->syn_kind == BGO_SYN_DS)
+            if (stdp) stdp_pre(n, s);
+            if (ds)
                 ds_change_psr(n, s);
             else
                 n->psr[s] += (n->W[s] / n->decay[s]); /* AllSpikingSynapses::changePSR :327-334 */
         }
+        if (post) stdp_post(n, s);
         n->psr[s] *= n->decay[s];
         n->sp[n->dest[s]] += n->psr[s];
     }

@@ -89,7 +89,14 @@ int64_t bgo_noise_recorded(const bgo_net *n);
 void bgo_step(bgo_net *n, int nsteps);        /* advanceNeurons + advanceSynapses, nsteps times */
 void bgo_growth(bgo_net *n);                  /* updateConnections (ConnGrowth) + maps rebuild  */
 void bgo_record_epoch(bgo_net *n, int epoch); /* XmlGrowthRecorder::compileHistories            */
-int bgo_flags(const bgo_net *n);              /* bit0: a row hit maxSynapsesPerNeuron          */
+int bgo_flags(const bgo_net *n);
+/* STDP arithmetic: 0 = the reference's host build (uint64_t spike times), 1 = its device build
+ * (int64_t spike times, AllSynapsesDeviceFuncs_d.cu:239-380). */
+void bgo_stdp_signed(bgo_net *n, int on);
+/* STDP constants of synapses created from now on (the reference hard-codes them in
+ * AllSTDPSynapses::createSynapse): Apos, Aneg, STDPgap, tauspost, tauspre, taupos, tauneg,
+ * WexE (excitatory source), WexI (inhibitory source), mupos, muneg. */
+void bgo_stdp_params(bgo_net *n, const float *p11);              /* bit0: a row hit maxSynapsesPerNeuron          */
 
 #ifdef __cplusplus
 }

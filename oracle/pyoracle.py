@@ -17,11 +17,11 @@ _NP = {1: np.uint8, 4: None, 8: None}
 # element type per array name (ambiguous sizes resolved by name)
 _INT32 = {"ntype", "starter", "refr", "spikeCount", "spikeCountOffset", "src", "dest", "type",
           "total_delay", "delayIdx", "ldelayQueue", "reg_shift", "pois_nisi", "in_delay",
-          "in_delayIdx"}
+          "in_delayIdx", "delayIdxPost", "total_delayPost", "ldelayQueuePost"}
 _UINT32 = {"queue", "counts", "inMap", "outMap", "inBegin", "inCount", "outBegin", "outCount",
-           "in_queue"}
+           "in_queue", "queuePost"}
 _UINT64 = {"history", "lastSpike", "in_last"}
-_UINT8 = {"hasFired", "in_use", "pois_mask"}
+_UINT8 = {"hasFired", "in_use", "pois_mask", "useFD"}
 
 LIF_CONFIG0_RANGES = [13.5e-9, 13.5e-9, 1.0e-9, 1.5e-9, 15.0e-3, 15.0e-3, 0.0, 0.0,
                       13.5e-3, 13.5e-3, 13.0e-3, 13.0e-3, 13.565e-3, 13.655e-3, 13.0e-3, 13.0e-3]
@@ -77,6 +77,8 @@ def lib():
         L.bgo_record_epoch.argtypes = [vp, i]
         L.bgo_flags.restype = i
         L.bgo_flags.argtypes = [vp]
+        L.bgo_stdp_signed.argtypes = [vp, i]
+        L.bgo_stdp_params.argtypes = [vp, ctypes.POINTER(f)]
         L.bgo_norm_fill.argtypes = [u32, ctypes.POINTER(f), i64]
         L.bgo_input_regular.argtypes = [vp, f, f, i, ctypes.POINTER(f)]
         L.bgo_input_regular.restype = i
@@ -225,6 +227,14 @@ class OracleNet:
 
     def record_epoch(self, epoch):
         self.L.bgo_record_epoch(self.h, int(epoch))
+
+    def stdp_signed(self, on=True):
+        """STDP arithmetic of the reference's device build (signed spike-time differences)."""
+        self.L.bgo_stdp_signed(self.h, 1 if on else 0)
+
+    def stdp_params(self, p11):
+        self._stdp = np.asarray(p11, dtype=np.float32)
+        self.L.bgo_stdp_params(self.h, self._stdp.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
 
     @property
     def flags(self):

@@ -295,9 +295,30 @@ static void dump_epoch(HarnessModel *m, SimulationInfo *si, uint64_t t, const ch
 #undef NM
 }
 
+// Parameter override (a documented deviation): the reference hard-codes its STDP constants in
+// AllSTDPSynapses::createSynapse (Synapses/AllSTDPSynapses.cpp:252-273) and reads none from the
+// configuration.  Synapses are only created by growth here, so setting the constants of every
+// in-use synapse right after each growth pass is the same as creating them with these values.
+// Wex takes the source's sign: WexE for EI/EE synapses, WexI for II/IE.
+static void override_stdp(HarnessModel *m, SimulationInfo *si, const BGFLOAT *p)
+{
+    AllSTDPSynapses *sp = dynamic_cast<AllSTDPSynapses *>(m->synapses());
+    if (!sp) return;
+    uint64_t S = (uint64_t)si->totalNeurons * si->maxSynapsesPerNeuron;
+    for (uint64_t i = 0; i < S; i++) {
+        if (!sp->in_use[i]) continue;
+        sp->Apos[i] = p[0]; sp->Aneg[i] = p[1]; sp->STDPgap[i] = p[2];
+        sp->tauspost[i] = p[3]; sp->tauspre[i] = p[4]; sp->taupos[i] = p[5]; sp->tauneg[i] = p[6];
+        sp->Wex[i] = (sp->type[i] == II || sp->type[i] == IE) ? p[8] : p[7];
+        sp->mupos[i] = p[9]; sp->muneg[i] = p[10];
+    }
+}
+
 int main(int argc, char **argv)
 {
     std::string cfg, out, stim;
+    BGFLOAT stdp_p[11];
+    int n_stdp = 0;
     int epochs = -1, dump_every = 0, dump_syn_every = 0, maxsyn = -1;
     long steps_limit = -1;
     double tsim = -1, radii = -1;
@@ -315,6 +336,18 @@ int main(int argc, char **argv)
         else if (a == "--maxsyn") maxsyn = atoi(argv[++i]);
         else if (a == "--record-noise") record_noise = true;
         else if (a == "--steps-limit") steps_limit = atol(argv[++i]);
+        else if (a == "--stdp") {
+            // Apos,Aneg,STDPgap,tauspost,tauspre,taupos,tauneg,WexE,WexI,mupos,muneg
+            std::string v = argv[++i];
+            n_stdp = 0;
+            for (size_t p = 0; n_stdp < 11 && p <= v.size();) {
+                size_t q = v.find(',', p);
+                if (q == std::string::npos) q = v.size();
+                stdp_p[n_stdp++] = (BGFLOAT)atof(v.substr(p, q - p).c_str());
+                p = q + 1;
+            }
+            if (n_stdp != 11) { fprintf(stderr, "--stdp wants 11 values\n"); return 2; }
+        }
         else { fprintf(stderr, "unknown arg %s\n", a.c_str()); return 2; }
     }
     if (cfg.empty() || out.empty()) { fprintf(stderr, "usage: -t cfg -o out\n"); return 2; }
@@ -380,6 +413,7 @@ int main(int argc, char **argv)
         // record spike history and counts before the recorder consumes them
         dump_epoch(m, si, g_simulationStep, "pre.");
         si->model->updateConnections(si);
+        if (n_stdp) override_stdp(m, si, stdp_p);
         dump_epoch(m, si, g_simulationStep, "grow.");   // after growth, before the recorder
         si->model->updateHistory(si);
         dump_epoch(m, si, g_simulationStep, "post.");   // after the recorder (radius clamp, count roll)

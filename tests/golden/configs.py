@@ -34,7 +34,14 @@ IZH_IF_RANGES = [13.5e-9, 13.5e-9, 0.5e-6, 0.7329e-6, 30.0e-3, 30.0e-3, 0.0, 0.0
                  -0.065, -0.065, -0.065, -0.065, 13.565e-3, 13.655e-3, 13.0e-3, 13.0e-3]
 IZH_RANGES = [0.02, 0.02, 0.02, 0.1, 0.2, 0.2, 0.2, 0.25, -65.0, -50.0, -65.0, -65.0,
               2.0, 8.0, 2.0, 2.0]
-SYN_CLASS = {1: "AllDSSynapses", 0: "AllSpikingSynapses"}
+SYN_CLASS = {0: "AllSpikingSynapses", 1: "AllDSSynapses", 2: "AllSTDPSynapses",
+             3: "AllDynamicSTDPSynapses"}
+
+# Additive STDP after Song, Miller and Abbott (2000): increments of 0.005 / -0.00525 of the 30 nA
+# weight bound, tau+ = tau- = 20 ms; Wex +30 nA for excitatory sources, -40 nA for inhibitory
+# ones.  Order: Apos, Aneg, STDPgap, tauspost, tauspre, taupos, tauneg, WexE, WexI, mupos, muneg.
+STDP_SOFT = [0.005 * 30e-9, -0.00525 * 30e-9, 2e-3, 75e-3, 34e-3, 20e-3, 20e-3, 30e-9, -40e-9,
+             0.0, 0.0]
 
 REG_VALUES = [1.5e-8 if ((i // 10) + (i % 10)) % 3 == 0 else 0.0 for i in range(100)]
 
@@ -42,7 +49,7 @@ REG_VALUES = [1.5e-8 if ((i // 10) + (i % 10)) % 3 == 0 else 0.0 for i in range(
 def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, radii=None,
           max_firing_rate=200, frac_inh=0.10, n_starters=10, site_seed=1, keep_steps_every=None,
           fp64=False, config=None, inh=None, starters=None, syn_keep=None, stim=None,
-          neuron="lif", synapse=1):
+          neuron="lif", synapse=1, stdp=None):
     if inh is None:
         inh, starters = site_lists(width, height, frac_inh, n_starters, site_seed)
     c = dict(name=name, width=width, height=height, N=width * height, tsim=tsim, epochs=epochs,
@@ -51,7 +58,7 @@ def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, r
                                             target_rate=target_rate, min_radius=0.1,
                                             start_radius=0.4),
              radii=radii, keep_steps_every=keep_steps_every, fp64=fp64, syn_keep=syn_keep,
-             stim=stim, neuron=neuron, synapse=synapse)
+             stim=stim, neuron=neuron, synapse=synapse, stdp=stdp)
     c["config"] = config or "configfiles/bg3/%s.xml" % name
     args = []
     if stim is not None:
@@ -60,6 +67,8 @@ def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, r
         args += ["--radii", repr(radii)]
     if keep_steps_every:
         args += ["--dump-every", str(keep_steps_every)]
+    if stdp is not None:
+        args += ["--stdp", ",".join(repr(float(v)) for v in stdp)]
     c["args"] = args
     return c
 
@@ -91,6 +100,17 @@ CASES = [
     # Izhikevich neurons, DS synapses, pre-grown 12x12 network
     _case("izh_grown", 12, 12, 0.2, 5, 100, radii=1.3, max_firing_rate=1000, site_seed=4,
           keep_steps_every=100, neuron="izh"),
+    # STDP with the reference's built-in constants (Apos 0.5 A: one potentiation saturates the
+    # network), two epochs so that the spike rings never fill
+    _case("c0_stdp", 10, 10, 0.5, 2, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=50,
+          synapse=2),
+    _case("c0_dstdp", 10, 10, 0.5, 2, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=50,
+          synapse=3),
+    # Izhikevich neurons, dynamic STDP synapses with bounded additive constants and Poisson
+    # drive (10 Hz, 5 nA), as in the 512-network Izhikevich + STDP sweep
+    _case("izh_dstdp", 12, 12, 0.5, 2, 100, radii=1.3, max_firing_rate=1000, site_seed=4,
+          keep_steps_every=50, neuron="izh", synapse=3, stdp=STDP_SOFT,
+          stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=None)),
     # LIF neurons with plain spiking synapses (AllSpikingSynapses), pre-grown
     _case("c0_spiking", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=100,
           synapse=0),

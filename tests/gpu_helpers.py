@@ -15,6 +15,8 @@ SYN_MAP = [("in_use", "in_use"), ("src", "src"), ("type", "type"), ("delayIdx", 
            ("lastSpike", "lastSpike")]
 
 
+IZH_MAP = [("Aconst", "Aconst"), ("Bconst", "Bconst"), ("Cconst", "Cconst"),
+           ("Dconst", "Dconst"), ("u", "u_izh"), ("C3", "C3")]
 POIS_MAP = [("masks", "pois_mask"), ("nISIs", "pois_nisi"), ("total_delay", "in_delay"),
             ("delayIdx", "in_delayIdx"), ("delayQueue", "in_queue"), ("W", "in_W"),
             ("psr", "in_psr"), ("decay", "in_decay"), ("U", "in_U"), ("D", "in_D"),
@@ -52,13 +54,17 @@ def compare_input(net, o, where):
 
 
 def gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_INJECT, n_noise=0, noise_seed=None, isi_steps=0):
+    izh = c.get("neuron") == "izh"
     net = bg.Network(c["N"], c["max_syn"], c["width"], c["height"], c["tsim"], 1e-4,
-                     c["max_firing_rate"], c["epochs"], bg.BG3_SYN_DS, noise_mode,
-                     noise_seed if noise_seed is not None else c["seed"])
+                     c["max_firing_rate"], c["epochs"], c.get("synapse", bg.BG3_SYN_DS),
+                     noise_mode, noise_seed if noise_seed is not None else c["seed"],
+                     neuron_kind=bg.BG3_NEURON_IZH if izh else bg.BG3_NEURON_LIF)
     net.upload_layout(o.arr("xloc"), o.arr("yloc"), o.arr("ntype"))
     kw = {k: o.arr(v) for k, v in LIF_MAP}
     kw["history"] = o.arr("history")
     net.upload_lif(**kw)
+    if izh:
+        net.upload_izh(**{k: o.arr(v) for k, v in IZH_MAP})
     skw = {k: o.arr(v) for k, v in SYN_MAP}
     net.upload_synapses(o.step, counts=o.arr("counts"), **skw)
     g = c["growth"]
@@ -76,6 +82,8 @@ def compare_neurons(net, o, where, fields=("Vm", "summation", "nStepsInRefr", "s
     m = dict(LIF_MAP)
     for f in fields:
         assert_same("%s %s" % (where, f), g[f], o.arr(m[f]))
+    if o.neuron_kind == 1:
+        assert_same(where + " u", net.download_izh()["u"], o.arr("u_izh"))
     return g
 
 

@@ -39,6 +39,8 @@ def oracle_from_case(c, record_noise=0):
         o.create_lif(LIF_RANGES)
     if stim and stim["kind"] == "poisson":
         o.input_poisson(stim["fr_mean"], stim["weight"], stim.get("masks"))
+    if c.get("stdp") is not None:
+        o.stdp_params(c["stdp"])
     g = c["growth"]
     o.growth_init(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
                   g["start_radius"])
@@ -92,4 +94,6 @@ def raster_from_history(history, counts, offsets, N, ms):
 
 
 SYN_FIELDS = ("W", "src", "dest", "type", "psr", "decay", "tau", "total_delay", "queue",
-              "delayIdx", "ldelayQueue", "lastSpike", "r", "u", "D", "U", "F")
+              "delayIdx", "ldelayQueue", "lastSpike", "r", "u", "D", "U", "F", "queuePost",
+              "delayIdxPost", "total_delayPost", "tauspost", "tauspre", "taupos", "tauneg",
+              "STDPgap", "Wex", "Aneg", "Apos", "mupos", "muneg")

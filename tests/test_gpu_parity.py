@@ -115,6 +115,19 @@ def test_poisson_input_bit_exact(name):
     o, net = run_locked(name, check_every=20, syn_every=500)
 
 
+def test_izhikevich_bit_exact():
+    """Izhikevich neurons (AllIZHNeurons) on a pre-grown 12x12 DS network: Vm, u, spikes and
+    synapses step-locked with the oracle over 5 epochs with growth."""
+    o, net = run_locked("izh_grown", check_every=10, syn_every=500)
+    assert o.total > 0 and int(o.arr("spikeCount").sum()) > 0
+
+
+def test_spiking_synapses_bit_exact():
+    """Plain AllSpikingSynapses (no facilitation / depression) on a pre-grown 10x10 network."""
+    o, net = run_locked("c0_spiking", check_every=10, syn_every=500)
+    assert o.total > 0
+
+
 @pytest.mark.slow
 def test_m30_grown_bit_exact():
     run_locked("m30_grown", check_every=100, syn_every=1000)
