@@ -1,9 +1,13 @@
 // C-ABI of libbg3: handle lifetime, conversion between the reference's slot layout and the
 // device plane layout, and the launch sequences of a step and of an epoch.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include <cuda.h>
@@ -45,6 +49,7 @@ struct bg3_net {
     void *flush_buf = nullptr, *scrub_buf = nullptr;
     size_t flush_size = 0;
     cudaGraphExec_t graph = nullptr;
+    std::vector<std::tuple<int, int, uint32_t, uint32_t>> exp_keys;  // exp tables this net holds
 };
 
 #define CK(x)                                                                            \
@@ -127,6 +132,116 @@ static int decay_class(bg3_net *n, float v)
     n->dtab.push_back(v);
     return (int)n->dtab.size() - 1;
 }
+// ---- exp tables ------------------------------------------------------------------------------
+// expf(-((float)k * dt) / tau) for k < BG3_EXP_LEN, evaluated by this host's libm in the order
+// the reference's DS and STDP code evaluates it (AllDSSynapses.cpp:239-240,
+// AllSTDPSynapses.cpp:322,345,370,394).  One device table per (device, dt, tau), shared by all
+// networks of the process and freed with the last one.
+struct ExpTable {
+    void *dev = nullptr;
+    int refs = 0;
+};
+// key: (device, kind, dt bits, tau bits); kind 0 = float expf table, 1 = double exp table
+using ExpKey = std::tuple<int, int, uint32_t, uint32_t>;
+static std::mutex g_exp_mu;
+static std::map<ExpKey, ExpTable> g_exp;
+
+static uint32_t fbits(float v)
+{
+    uint32_t b;
+    memcpy(&b, &v, 4);
+    return b;
+}
+
+// Registers tau with the network; returns 0, or BG3_ENOMEM / BG3_ECUDA.  A tau that is not
+// positive and finite, or one past BG3_MAX_EXPC classes, is left to the device fallback.
+// Returns the shared device table of (kind, dt, tau), creating it on first use; the caller
+// records the key in n->exp_keys.
+template <typename T>
+static int exp_table(bg3_net *n, int kind, float tau, int len, const T **out)
+{
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    const float dt = n->h.dt;
+    ExpKey key = std::make_tuple(dev, kind, fbits(dt), fbits(tau));
+    std::lock_guard<std::mutex> lock(g_exp_mu);
+    ExpTable &t = g_exp[key];
+    if (!t.dev) {
+        std::vector<T> v(len);
+        for (int k = 0; k < len; k++) {
+            const float x = (float)k * dt;
+            if (kind == 0) v[k] = (T)expf(-x / tau);            // expf(-isi / tau), float isi
+            else v[k] = (T)exp(-(double)x / (double)tau);     // exp(-delta / tau), double delta
+        }
+        if (cudaMalloc(&t.dev, v.size() * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            g_exp.erase(key);
+            return BG3_ENOMEM;
+        }
+        if (cudaMemcpy(t.dev, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(t.dev);
+            g_exp.erase(key);
+            return BG3_ECUDA;
+        }
+    }
+    t.refs++;
+    n->exp_keys.push_back(key);
+    *out = (const T *)t.dev;
+    return BG3_OK;
+}
+
+static int exp_class(bg3_net *n, float tau)
+{
+    NetDev &h = n->h;
+    if (!(tau > 0.0f) || !std::isfinite(tau)) return BG3_OK;
+    for (int c = 0; c < h.n_expc; c++)
+        if (fbits(h.expc_tau[c]) == fbits(tau)) return BG3_OK;
+    if (h.n_expc >= BG3_MAX_EXPC) return BG3_OK;
+    const float *tab = nullptr;
+    int rc = exp_table<float>(n, 0, tau, BG3_EXP_LEN, &tab);
+    if (rc) return rc;
+    h.expc_tau[h.n_expc] = tau;
+    h.expc_tab[h.n_expc] = tab;
+    h.n_expc++;
+    return push_desc(n);
+}
+
+// Per-type STDP constants: the float tables of tauspre / tauspost and the double tables of
+// taupos / tauneg (exp(-delta / taupos), exp(delta / tauneg) over a 3 tau window).
+static int set_stdp_type(bg3_net *n, int type, const StdpConst &in)
+{
+    StdpConst c = in;
+    int rc;
+    if ((rc = exp_class(n, c.tauspre)) || (rc = exp_class(n, c.tauspost))) return rc;
+    c.dpos = c.dneg = nullptr;
+    c.dlen_pos = c.dlen_neg = 0;
+    if (c.taupos > 0.0f && std::isfinite(c.taupos)) {
+        if ((rc = exp_table<double>(n, 1, c.taupos, BG3_DEXP_LEN, &c.dpos))) return rc;
+        c.dlen_pos = BG3_DEXP_LEN;
+    }
+    if (c.tauneg > 0.0f && std::isfinite(c.tauneg)) {
+        if ((rc = exp_table<double>(n, 1, c.tauneg, BG3_DEXP_LEN, &c.dneg))) return rc;
+        c.dlen_neg = BG3_DEXP_LEN;
+    }
+    n->h.stdp[type] = c;
+    return push_desc(n);
+}
+
+static void exp_release(bg3_net *n)
+{
+    std::lock_guard<std::mutex> lock(g_exp_mu);
+    for (auto &key : n->exp_keys) {
+        auto it = g_exp.find(key);
+        if (it == g_exp.end()) continue;
+        if (--it->second.refs == 0) {
+            cudaFree(it->second.dev);
+            g_exp.erase(it);
+        }
+    }
+    n->exp_keys.clear();
+    n->h.n_expc = 0;
+}
+
 static int delay_class(bg3_net *n, int D)
 {
     for (size_t i = 0; i < n->ltab.size(); i++)
@@ -190,8 +305,8 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     if ((((size_t)D.n_neurons + 31) / 32 * 32) * (((size_t)D.max_syn_per_neuron + 3) / 4 * 4) >=
         (1ull << 32))
         return BG3_EINVAL;  // plane positions are 32-bit
-    if (D.neuron_kind != BG3_NEURON_LIF) return BG3_EUNSUPPORTED;
-    if (D.synapse_kind != BG3_SYN_DS && D.synapse_kind != BG3_SYN_SPIKING) return BG3_EUNSUPPORTED;
+    if (D.neuron_kind != BG3_NEURON_LIF && D.neuron_kind != BG3_NEURON_IZH) return BG3_EUNSUPPORTED;
+    if (D.synapse_kind < BG3_SYN_SPIKING || D.synapse_kind > BG3_SYN_DYNSTDP) return BG3_EUNSUPPORTED;
     if (D.noise_mode != BG3_NOISE_DEVICE && D.noise_mode != BG3_NOISE_INJECT) return BG3_EINVAL;
     int max_spikes = (int)(D.epoch_duration * (float)D.max_firing_rate);
     if (max_spikes <= 0) return BG3_EINVAL;
@@ -237,6 +352,9 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     A(radii, N) A(rates, N) A(xloc, N) A(yloc, N)
     A(burstiness, (size_t)std::max(h.n_burst_bins, 1)) A(spikes_hist, (size_t)std::max(h.n_spike_bins, 1))
     A(rates_hist, (size_t)(D.max_epochs + 1) * N) A(radii_hist, (size_t)(D.max_epochs + 1) * N)
+    if (D.neuron_kind == BG3_NEURON_IZH) {
+        A(Aconst, N) A(Bconst, N) A(Cconst, N) A(Dconst, N) A(u_izh, N) A(C3, N)
+    }
 #undef A
     if ((rc = dalloc(n, &h.history, N * (size_t)max_spikes, 0xff)) != 0) goto fail;
     if (cudaMalloc((void **)&n->d, sizeof(NetDev)) != cudaSuccess) { rc = BG3_ENOMEM; goto fail; }
@@ -260,6 +378,20 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
         h.t_r0 = 1.0f;
     }
     if ((rc = make_tensor_maps(n)) != 0) goto fail;
+    if (cudaMemcpy(n->d, &h, sizeof(NetDev), cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = BG3_ECUDA;
+        goto fail;
+    }
+    for (int t = 0; t < 4 && (h.syn_kind == BG3_SYN_DS || h.syn_kind == BG3_SYN_DYNSTDP); t++)
+        if ((rc = exp_class(n, h.t_D[t])) || (rc = exp_class(n, h.t_F[t]))) goto fail;
+    // AllSTDPSynapses::createSynapse constants (Synapses/AllSTDPSynapses.cpp:256-272)
+    for (int t = 0; t < 4 && h.syn_kind >= BG3_SYN_STDP; t++) {
+        StdpConst c = {};
+        c.Apos = 0.5f; c.Aneg = -0.5f; c.gap = 2e-3f;
+        c.tauspost = 75e-3f; c.tauspre = 34e-3f; c.taupos = 15e-3f; c.tauneg = 35e-3f;
+        c.Wex = 1.0f; c.mupos = 0.0f; c.muneg = 0.0f; c.useFD = 1;
+        if ((rc = set_stdp_type(n, t, c))) goto fail;
+    }
     if ((rc = push_tables(n)) != 0) goto fail;
     if (cudaStreamSynchronize(n->stream) != cudaSuccess) { rc = BG3_ECUDA; goto fail; }
     *out = n;
@@ -275,6 +407,7 @@ int bg3_destroy(bg3_net *n)
     if (!n) return BG3_EINVAL;
     if (n->stream) cudaStreamSynchronize(n->stream);
     drop_graph(n);
+    exp_release(n);
     for (void *p : n->allocs) cudaFree(p);
     if (n->d) cudaFree(n->d);
     if (n->noise_dev) cudaFree(n->noise_dev);
@@ -302,6 +435,21 @@ int bg3_upload_lif(bg3_net *n, const bg3_lif_arrays *a)
         (rc = h2d(n, h.spikeCount, a->spikeCount, N)) ||
         (rc = h2d(n, h.spikeCountOffset, a->spikeCountOffset, N)) ||
         (rc = h2d(n, (uint64_t *)h.history, a->history, N * (size_t)h.max_spikes)))
+        return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_upload_izh(bg3_net *n, const bg3_izh_arrays *a)
+{
+    if (!n || !a) return BG3_EINVAL;
+    if (n->h.neuron_kind != BG3_NEURON_IZH) return BG3_EUNSUPPORTED;
+    size_t N = n->h.N;
+    NetDev &h = n->h;
+    int rc;
+    if ((rc = h2d(n, h.Aconst, a->Aconst, N)) || (rc = h2d(n, h.Bconst, a->Bconst, N)) ||
+        (rc = h2d(n, h.Cconst, a->Cconst, N)) || (rc = h2d(n, h.Dconst, a->Dconst, N)) ||
+        (rc = h2d(n, h.u_izh, a->u, N)) || (rc = h2d(n, h.C3, a->C3, N)))
         return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
@@ -337,6 +485,10 @@ int bg3_set_type_constants(bg3_net *n, const bg3_type_constants *c)
         n->h.t_U[t] = c->U[t];
         n->h.t_D[t] = c->D[t];
         n->h.t_F[t] = c->F[t];
+        int rc;
+        if ((n->h.syn_kind == BG3_SYN_DS || n->h.syn_kind == BG3_SYN_DYNSTDP) &&
+            ((rc = exp_class(n, c->D[t])) || (rc = exp_class(n, c->F[t]))))
+            return rc;
     }
     n->h.t_u0 = c->u0;
     n->h.t_r0 = c->r0;
@@ -358,7 +510,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
         return BG3_EINVAL;
     if (step >= 0xffffff00ull) return BG3_EINVAL;
     const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * (size_t)n->h.Mq * 4;
-    const bool ds = n->h.syn_kind == BG3_SYN_DS;
+    const bool ds = n->h.syn_kind == BG3_SYN_DS || n->h.syn_kind == BG3_SYN_DYNSTDP;
     if (ds && (!a->U || !a->D || !a->F || !a->u || !a->r || !a->lastSpike)) return BG3_EINVAL;
     std::vector<float> psr(S, 0.f);
     std::vector<uint8_t> dc(S, 0), lc(S, 0);
@@ -369,6 +521,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
     memset(ev.data(), 0, S * sizeof(EvSlot));
     // fired[s] bit j: neuron s fired at step - 1 - j (j < 32), from the queues
     std::vector<uint32_t> fired(N, 0u);
+    uint32_t seenD = 0xffffffffu, seenF = 0xffffffffu;  // last time constants registered
     for (size_t d = 0; d < N; d++) {
         size_t c = 0;
         while (c < M && a->in_use[d * M + c]) c++;
@@ -394,6 +547,12 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
             e.born = (uint32_t)(step - (uint64_t)di - 32u);
             if (ds) {
                 e.U = a->U[i]; e.D = a->D[i]; e.F = a->F[i]; e.u = a->u[i]; e.r = a->r[i];
+                if (fbits(e.D) != seenD || fbits(e.F) != seenF) {
+                    int erc;
+                    if ((erc = exp_class(n, e.D)) || (erc = exp_class(n, e.F))) return erc;
+                    seenD = fbits(e.D);
+                    seenF = fbits(e.F);
+                }
                 uint64_t ls = a->lastSpike[i];
                 if (ls != BG3_ULONG_MAX && ls >= BG3_NO_SPIKE32) return BG3_EINVAL;
                 e.last = (ls == BG3_ULONG_MAX) ? BG3_NO_SPIKE32 : (uint32_t)ls;
@@ -577,6 +736,7 @@ int bg3_input_poisson(bg3_net *n, const bg3_poisson_arrays *a, float lambda, uin
         e.W = a->W[i]; e.U = a->U[i]; e.D = a->D[i]; e.F = a->F[i]; e.u = a->u[i]; e.r = a->r[i];
         e.last = (ls == BG3_ULONG_MAX) ? BG3_NO_SPIKE32 : (uint32_t)ls;
         e.born = (uint32_t)(step - (uint64_t)a->delayIdx[i]);
+        if ((rc = exp_class(n, e.D)) || (rc = exp_class(n, e.F))) return rc;
     }
     if ((rc = h2d(n, h.pois_mask, mask.data(), N)) || (rc = h2d(n, h.pois_nisi, a->nISIs, N)) ||
         (rc = h2d(n, h.in_psr, a->psr, N)) || (rc = h2d(n, h.in_decay, a->decay, N)) ||
@@ -764,6 +924,21 @@ int bg3_download_lif(bg3_net *n, bg3_lif_arrays *a)
     return BG3_OK;
 }
 
+int bg3_download_izh(bg3_net *n, bg3_izh_arrays *a)
+{
+    if (!n || !a) return BG3_EINVAL;
+    if (n->h.neuron_kind != BG3_NEURON_IZH) return BG3_EUNSUPPORTED;
+    size_t N = n->h.N;
+    NetDev &h = n->h;
+    int rc;
+    if ((rc = d2h(n, a->Aconst, h.Aconst, N)) || (rc = d2h(n, a->Bconst, h.Bconst, N)) ||
+        (rc = d2h(n, a->Cconst, h.Cconst, N)) || (rc = d2h(n, a->Dconst, h.Dconst, N)) ||
+        (rc = d2h(n, a->u, h.u_izh, N)) || (rc = d2h(n, a->C3, h.C3, N)))
+        return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
 // Rebuilds the reference's delayQueue / delayIdx from the spike ring and birth steps: a spike
 // emitted at tf >= birth is due at tf + D; at step t it sits at bit (delayIdx + tf + D - t) & 31
 // with delayIdx = (t - birth) & 31.
@@ -779,6 +954,7 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
     std::vector<int8_t> st(S);
     std::vector<uint32_t> count(N);
     unsigned long long step = 0;
+    const bool ds = h.syn_kind == BG3_SYN_DS || h.syn_kind == BG3_SYN_DYNSTDP;
     int rc;
     if ((rc = d2h(n, psr.data(), h.psr, S)) || (rc = d2h(n, dc.data(), h.dcls, S)) ||
         (rc = d2h(n, lc.data(), h.lcls, S)) || (rc = d2h(n, ev.data(), h.ev, S)) ||
@@ -821,12 +997,132 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
             if (a->delayIdx) a->delayIdx[i] = (int32_t)di;
             if (a->delayQueue) a->delayQueue[i] = q;
             if (a->tau) a->tau[i] = h.t_tau[st[p] & 3];
+            if (!ds) continue;  // the DS fields exist for DS and dynamic STDP synapses only
             if (a->U) a->U[i] = e.U;
             if (a->D) a->D[i] = e.D;
             if (a->F) a->F[i] = e.F;
             if (a->u) a->u[i] = e.u;
             if (a->r) a->r[i] = e.r;
             if (a->lastSpike) a->lastSpike[i] = (e.last == BG3_NO_SPIKE32) ? BG3_ULONG_MAX : (uint64_t)e.last;
+        }
+    }
+    return BG3_OK;
+}
+
+// ---- STDP --------------------------------------------------------------------------------------
+static StdpConst stdp_from(const bg3_stdp_constants *c, int t)
+{
+    StdpConst s = {};
+    s.Apos = c->Apos[t]; s.Aneg = c->Aneg[t]; s.gap = c->STDPgap[t];
+    s.tauspost = c->tauspost[t]; s.tauspre = c->tauspre[t];
+    s.taupos = c->taupos[t]; s.tauneg = c->tauneg[t];
+    s.Wex = c->Wex[t]; s.mupos = c->mupos[t]; s.muneg = c->muneg[t];
+    s.useFD = c->useFroemkeDanSTDP[t] ? 1 : 0;
+    return s;
+}
+
+int bg3_set_stdp_constants(bg3_net *n, const bg3_stdp_constants *c)
+{
+    if (!n || !c) return BG3_EINVAL;
+    if (n->h.syn_kind < BG3_SYN_STDP) return BG3_EUNSUPPORTED;
+    for (int t = 0; t < 4; t++) {
+        int rc = set_stdp_type(n, t, stdp_from(c, t));
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_set_stdp_arithmetic(bg3_net *n, int mode)
+{
+    if (!n || (mode != BG3_STDP_HOST && mode != BG3_STDP_DEVICE)) return BG3_EINVAL;
+    if (n->h.syn_kind < BG3_SYN_STDP) return BG3_EUNSUPPORTED;
+    n->h.stdp_signed = mode == BG3_STDP_DEVICE;
+    int rc = push_desc(n);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+// The reference's STDP fields per slot; every in-use synapse of one type must carry the same
+// constants, an empty post queue, total_delayPost 0 and delayIdxPost == delayIdx (what
+// createSynapse and the step produce).  Anything else is BG3_EUNSUPPORTED.
+int bg3_upload_stdp(bg3_net *n, const bg3_synapse_arrays *syn, const bg3_stdp_arrays *a)
+{
+    if (!n || !syn || !a || !syn->in_use || !syn->type || !syn->delayIdx || !a->delayQueuePost ||
+        !a->delayIdxPost || !a->total_delayPost || !a->tauspost || !a->tauspre || !a->taupos ||
+        !a->tauneg || !a->STDPgap || !a->Wex || !a->Aneg || !a->Apos || !a->mupos || !a->muneg ||
+        !a->useFroemkeDanSTDP)
+        return BG3_EINVAL;
+    if (n->h.syn_kind < BG3_SYN_STDP) return BG3_EUNSUPPORTED;
+    const size_t S = (size_t)n->h.N * n->h.max_syn;
+    bool seen[4] = {false, false, false, false};
+    bg3_stdp_constants c;
+    memset(&c, 0, sizeof(c));
+    for (size_t i = 0; i < S; i++) {
+        if (!syn->in_use[i]) continue;
+        const int t = syn->type[i];
+        if (t < 0 || t > 3) return BG3_EINVAL;
+        if (a->delayQueuePost[i] != 0 || a->total_delayPost[i] != 0 ||
+            a->delayIdxPost[i] != syn->delayIdx[i])
+            return BG3_EUNSUPPORTED;
+        const float v[10] = {a->Apos[i], a->Aneg[i], a->STDPgap[i], a->tauspost[i], a->tauspre[i],
+                             a->taupos[i], a->tauneg[i], a->Wex[i], a->mupos[i], a->muneg[i]};
+        float *dst[10] = {&c.Apos[t], &c.Aneg[t], &c.STDPgap[t], &c.tauspost[t], &c.tauspre[t],
+                          &c.taupos[t], &c.tauneg[t], &c.Wex[t], &c.mupos[t], &c.muneg[t]};
+        const int fd = a->useFroemkeDanSTDP[i] ? 1 : 0;
+        if (!seen[t]) {
+            for (int k = 0; k < 10; k++) *dst[k] = v[k];
+            c.useFroemkeDanSTDP[t] = fd;
+            seen[t] = true;
+            continue;
+        }
+        for (int k = 0; k < 10; k++)
+            if (fbits(*dst[k]) != fbits(v[k])) return BG3_EUNSUPPORTED;
+        if (c.useFroemkeDanSTDP[t] != fd) return BG3_EUNSUPPORTED;
+    }
+    for (int t = 0; t < 4; t++) {
+        if (!seen[t]) continue;
+        int rc = set_stdp_type(n, t, stdp_from(&c, t));
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_download_stdp(bg3_net *n, bg3_stdp_arrays *a)
+{
+    if (!n || !a) return BG3_EINVAL;
+    if (n->h.syn_kind < BG3_SYN_STDP) return BG3_EUNSUPPORTED;
+    const NetDev &h = n->h;
+    const size_t N = h.N, Np = h.Np, M = h.max_syn, S = Np * (size_t)h.Mq * 4;
+    std::vector<EvSlot> ev(S);
+    std::vector<int8_t> st(S);
+    std::vector<uint32_t> count(N);
+    unsigned long long step = 0;
+    int rc;
+    if ((rc = d2h(n, ev.data(), h.ev, S)) || (rc = d2h(n, st.data(), h.stype, S)) ||
+        (rc = d2h(n, count.data(), h.count, N)) || (rc = d2h(n, &step, h.step, 1)))
+        return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    for (size_t d = 0; d < N; d++) {
+        for (size_t k = 0; k < M && k < count[d]; k++) {
+            const size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
+            const StdpConst &c = h.stdp[st[p] & 3];
+            if (a->delayQueuePost) a->delayQueuePost[i] = 0;
+            if (a->delayIdxPost) a->delayIdxPost[i] = (int32_t)(((uint32_t)step - ev[p].born) & 31u);
+            if (a->total_delayPost) a->total_delayPost[i] = 0;
+            if (a->tauspost) a->tauspost[i] = c.tauspost;
+            if (a->tauspre) a->tauspre[i] = c.tauspre;
+            if (a->taupos) a->taupos[i] = c.taupos;
+            if (a->tauneg) a->tauneg[i] = c.tauneg;
+            if (a->STDPgap) a->STDPgap[i] = c.gap;
+            if (a->Wex) a->Wex[i] = c.Wex;
+            if (a->Aneg) a->Aneg[i] = c.Aneg;
+            if (a->Apos) a->Apos[i] = c.Apos;
+            if (a->mupos) a->mupos[i] = c.mupos;
+            if (a->muneg) a->muneg[i] = c.muneg;
+            if (a->useFroemkeDanSTDP) a->useFroemkeDanSTDP[i] = (uint8_t)c.useFD;
         }
     }
     return BG3_OK;

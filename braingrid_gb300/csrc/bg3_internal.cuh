@@ -30,6 +30,18 @@
 #define BG3_RING 64          // spike-list ring depth (steps); delays must be < 32
 #define BG3_MAX_DCLS 256     // decay classes
 #define BG3_MAX_DELAYS 8     // delay classes
+#define BG3_MAX_EXPC 16      // time constants with an exp table
+#define BG3_EXP_LEN 262144   // steps covered by an exp table (26 s at dt = 0.1 ms)
+#define BG3_DEXP_LEN 8192    // steps covered by a double exp table (STDP windows)
+
+// STDP constants of one synapse type (AllSTDPSynapses.h:350-420); createSynapse gives every
+// synapse the same values (AllSTDPSynapses.cpp:252-273), so they are held per type.
+struct StdpConst {
+    float Apos, Aneg, gap, tauspost, tauspre, taupos, tauneg, Wex, mupos, muneg;
+    int32_t useFD;
+    int32_t dlen_pos, dlen_neg;      // entries of the double tables (0: none)
+    const double *dpos, *dneg;       // exp(-(k dt) / taupos), exp(-(k dt) / tauneg)
+};
 
 struct __align__(32) EvSlot {
     float W, U, D, F, u, r;
@@ -65,6 +77,8 @@ struct NetDev {
     int32_t *refr, *spikeCount, *spikeCountOffset;
     unsigned long long *history;   // [N][max_spikes]
     int8_t *ntype;                 // 1 INH, 2 EXC
+    // Izhikevich neurons only (NULL for LIF): a, b, c, d, recovery variable u, C3 = dt * 1000
+    float *Aconst, *Bconst, *Cconst, *Dconst, *u_izh, *C3;
     // spike ring: ids of the neurons that fired at step t are ring[(t & 63) * N + i]
     int32_t *ring, *ring_n;
     // synapse planes (index slot_pos(k, d, Np), Mq * Np * 4 entries)
@@ -108,6 +122,15 @@ struct NetDev {
     uint8_t *in_delay;
     EvSlot *in_ev;
     int32_t *isi_begin, *isi_vals, *isi_cursor;  // injected ISI draws (NULL: device generator)
+    // exp(-(k dt) / tau) for k < BG3_EXP_LEN, one table per time constant, filled by the host's
+    // libm expf (the function the reference's host build calls for these factors)
+    int32_t n_expc;
+    float expc_tau[BG3_MAX_EXPC];
+    const float *expc_tab[BG3_MAX_EXPC];
+    // STDP kinds: per-type constants; stdp_signed selects the reference device build's signed
+    // spike-time arithmetic instead of its host build's unsigned one
+    StdpConst stdp[4];
+    int32_t stdp_signed;
 };
 
 // device error word bits (mirrored in include/bg3.h)
@@ -120,6 +143,7 @@ enum : uint32_t {
     ERR_TIMEOUT = 1u << 6,
     ERR_STEP_RANGE = 1u << 7,
     ERR_ISI_EXHAUSTED = 1u << 8,
+    ERR_STDP_RING = 1u << 9,
 };
 
 // ---- exact-rounding helpers -----------------------------------------------------------------
@@ -129,6 +153,30 @@ enum : uint32_t {
 __device__ __forceinline__ float exp_cr(float x) { return (float)exp((double)x); }
 __device__ __forceinline__ float acos_cr(float x) { return (float)acos((double)x); }
 __device__ __forceinline__ float sin_cr(float x) { return (float)sin((double)x); }
+
+// expf(-((float)k * dt) / tau): the DS facilitation / depression factors and the STDP
+// efficacies all take this form with k a whole number of steps.  Time constants registered by
+// the host are read from their table, so the value is the host library's own rounding; others
+// (and k beyond the table) fall back to the correctly rounded value.
+__device__ __forceinline__ float exp_steps(const NetDev &n, uint32_t k, float tau)
+{
+    if (k < (uint32_t)BG3_EXP_LEN) {
+        for (int c = 0; c < n.n_expc; c++)
+            if (n.expc_tau[c] == tau) return __ldg(n.expc_tab[c] + k);
+    }
+    const float x = (float)k * n.dt;
+    return exp_cr(-x / tau);
+}
+
+// expf(-(x dt) / tau) for a spike-time difference u held as uint64 (host build) or int64
+// (device build): x = (float)u or (float)(int64)u.
+__device__ __forceinline__ float exp_interval(const NetDev &n, unsigned long long u, bool sgn,
+                                              float tau)
+{
+    if (u < (unsigned long long)BG3_EXP_LEN) return exp_steps(n, (uint32_t)u, tau);
+    const float x = (sgn ? (float)(long long)u : (float)u) * n.dt;
+    return exp_cr(-x / tau);
+}
 
 // ---- counter-based normal generator (device noise mode) --------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
@@ -169,12 +217,15 @@ __device__ __forceinline__ int lif_branch(const NetDev &n, int i)
 }
 
 // AllLIFNeurons::advanceNeuron / fire and AllSpikingNeurons::fire
-// (Neurons/AllLIFNeurons.cpp:20-77, Neurons/AllSpikingNeurons.cpp:155-172) with the summation
-// point value passed in.  Each float operation rounds on its own (-fmad=false).  Returns true
-// when the neuron fired.  The caller stores sp = 0 afterwards.
+// (Neurons/AllLIFNeurons.cpp:20-77, Neurons/AllSpikingNeurons.cpp:155-172), and for Izhikevich
+// neurons AllIZHNeurons::advanceNeuron / fire (Neurons/AllIZHNeurons.cpp:570-655), with the
+// summation point value passed in.  Each float operation rounds on its own (-fmad=false) and the
+// double promotions of the reference's expressions are kept.  Returns true when the neuron
+// fired.  The caller stores sp = 0 afterwards.
 __device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float sp, float noise,
                                           unsigned long long t)
 {
+    const bool izh = n.neuron_kind == 1;
     if (br == BR_REFRACTORY) {
         n.refr[i] = n.refr[i] - 1;
         return false;
@@ -187,12 +238,28 @@ __device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float 
         n.spikeCount[i] = cnt;
         if (cnt >= n.max_spikes) set_err(n, ERR_HISTORY_OVERFLOW);
         n.refr[i] = (int)((double)(n.Trefract[i] / n.dt) + 0.5);
-        n.Vm[i] = n.Vreset[i];
+        if (izh) {
+            n.Vm[i] = (float)((double)n.Cconst[i] * 0.001);
+            n.u_izh[i] = n.u_izh[i] + n.Dconst[i];
+        } else {
+            n.Vm[i] = n.Vreset[i];
+        }
         return true;
     }
     sp = sp + n.I0[i];
     sp = sp + noise * n.Inoise[i];
-    n.Vm[i] = n.C1[i] * n.Vm[i] + n.C2[i] * sp;
+    if (izh) {
+        // Vm in mV; dv = C3 (0.04 v^2 + 5 v + 140 - u) evaluated in double, du = C3 a (b v - u)
+        const float Vint = n.Vm[i] * 1000.0f;
+        const float u = n.u_izh[i], C3 = n.C3[i];
+        const double vd = (double)Vint;
+        const float Vb = (float)(vd + (double)C3 * (0.04 * vd * vd + (double)(5.0f * Vint) +
+                                                    140.0 - (double)u));
+        n.u_izh[i] = u + C3 * n.Aconst[i] * (n.Bconst[i] * Vint - u);
+        n.Vm[i] = (float)((double)Vb * 0.001 + (double)(n.C2[i] * sp));
+    } else {
+        n.Vm[i] = n.C1[i] * n.Vm[i] + n.C2[i] * sp;
+    }
     return false;
 }
 
@@ -246,9 +313,9 @@ __device__ __forceinline__ float input_apply(const NetDev &n, int i, unsigned lo
             EvSlot e = n.in_ev[i];
             float u = e.u, r = e.r;
             if (e.last != BG3_NO_SPIKE32) {
-                float isi = (float)((uint32_t)t - e.last) * n.dt;
-                r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_cr(-isi / e.D);
-                u = e.U + u * (1.0f - e.U) * exp_cr(-isi / e.F);
+                const uint32_t k = (uint32_t)t - e.last;
+                r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_steps(n, k, e.D);
+                u = e.U + u * (1.0f - e.U) * exp_steps(n, k, e.F);
             }
             psr = psr + ((e.W / dec) * u * r);
             n.in_ev[i].u = u;

@@ -155,23 +155,155 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__
     if (threadIdx.x == 0) *n.noise_cursor = cursor + (unsigned long long)s_running;
 }
 
+// ---- STDP ------------------------------------------------------------------------------------
+// AllSTDPSynapses::advanceSynapse / stdpLearning (Synapses/AllSTDPSynapses.cpp:283-472) and the
+// device form advanceSTDPSynapsesDevice (AllSynapsesDeviceFuncs_d.cu:100-380).  The only
+// difference between the two builds is the type of the spike times in the interval arithmetic:
+// uint64_t on the host (a pre-spike walk interval wraps to a huge positive value), int64_t on
+// the device.  Each float / double operation rounds as in the reference; the exp factors come
+// from the host library's tables.
+
+// getSpikeHistory (Neurons/AllSpikingNeurons.cpp:182-188) for off in [-max_spikes, -1];
+// co = spikeCount + spikeCountOffset.
+__device__ __forceinline__ unsigned long long hist_at(const NetDev &n, int i, int co, int off)
+{
+    const int x = (co + n.max_spikes + off) % n.max_spikes;
+    return n.history[(size_t)i * n.max_spikes + x];
+}
+
+__device__ __forceinline__ float pow_mu(float x, float mu) { return mu == 0.0f ? 1.0f : powf(x, mu); }
+
+// stdpLearning with delta = dk steps (dk the signed interval; 0 when not a small count)
+__device__ __forceinline__ float stdp_learn(const StdpConst &c, float W, float delta, float epost,
+                                            float epre, long long dk)
+{
+    const double d = (double)delta;
+    float dw;
+    if (d < (double)(-c.gap)) {
+        const double e = (dk < 0 && -dk < (long long)c.dlen_neg) ? c.dneg[-dk] : exp(d / (double)c.tauneg);
+        dw = (float)((double)(pow_mu(W, c.muneg) * c.Aneg) * e);
+    } else if (d > (double)c.gap) {
+        const double e = (dk > 0 && dk < (long long)c.dlen_pos) ? c.dpos[dk] : exp(-d / (double)c.taupos);
+        dw = (float)((double)(pow_mu(c.Wex - W, c.mupos) * c.Apos) * e);
+    } else {
+        return W;
+    }
+    W = (float)((double)W + (double)epost * (double)epre * (double)dw);
+    if ((c.Wex < 0.0f && W > 0.0f) || (c.Wex > 0.0f && W < 0.0f)) W = 0.0f;
+    if (fabsf(W) > fabsf(c.Wex)) W = c.Wex;
+    return W;
+}
+
+// The fPre branch: a spike from pre arrives at the synapse onto post at step t.  Returns W.
+__device__ float stdp_pre(const NetDev &n, const StdpConst &c, float W, int pre, int post,
+                          unsigned long long t)
+{
+    const int ms = n.max_spikes;
+    const int cpost = n.spikeCount[post] + n.spikeCountOffset[post];
+    if (!n.stdp_signed) {
+        // Every interval (spikeHistory - step) wraps to ~1.8e15 s (or is 0 at step t): each
+        // learning call potentiates by exactly zero and applies the clamps, so only whether one
+        // happens matters: the walk runs while entries -k and -(k+1) are valid.
+        const unsigned long long h1 = hist_at(n, post, cpost, -1);
+        const unsigned long long h2 = hist_at(n, post, cpost, -2);
+        if (hist_at(n, post, cpost, -ms) != BG3_ULONG_MAX) set_err(n, ERR_STDP_RING);
+        bool learn;
+        if (c.useFD) {
+            const unsigned long long h3 = hist_at(n, post, cpost, -3);
+            learn = h1 != BG3_ULONG_MAX && h2 != BG3_ULONG_MAX && (h1 != t || h3 != BG3_ULONG_MAX);
+        } else {
+            learn = h1 != BG3_ULONG_MAX && (h1 != t || h2 != BG3_ULONG_MAX);
+        }
+        if (learn) {
+            // potentiation by (float)(x * exp(-huge)) = +-0; epost * epre >= 0 keeps dw's sign
+            const float dw = (float)((double)(pow_mu(c.Wex - W, c.mupos) * c.Apos) * 0.0);
+            W = (float)((double)W + (double)dw);
+            if ((c.Wex < 0.0f && W > 0.0f) || (c.Wex > 0.0f && W < 0.0f)) W = 0.0f;
+            if (fabsf(W) > fabsf(c.Wex)) W = c.Wex;
+        }
+        return W;
+    }
+    const int cpre = n.spikeCount[pre] + n.spikeCountOffset[pre];
+    float epre = 1.0f;
+    const unsigned long long sp2 = hist_at(n, pre, cpre, -2);
+    if ((long long)sp2 > 0 && c.useFD)
+        epre = (float)(1.0 - (double)exp_interval(n, t - sp2, true, c.tauspre));
+    for (int off = -1;; --off) {
+        if (off < -ms) { set_err(n, ERR_STDP_RING); break; }
+        const unsigned long long sh = hist_at(n, post, cpost, off);
+        if (sh == BG3_ULONG_MAX) break;
+        const long long dk = (long long)(sh - t);
+        const float delta = (float)dk * n.dt;
+        if ((double)delta <= -3.0 * (double)c.tauneg) break;
+        float epost = 1.0f;
+        if (c.useFD) {
+            if (off - 1 < -ms) { set_err(n, ERR_STDP_RING); break; }
+            const unsigned long long sh2 = hist_at(n, post, cpost, off - 1);
+            if (sh2 == BG3_ULONG_MAX) break;
+            epost = (float)(1.0 - (double)exp_interval(n, sh - sh2, true, c.tauspost));
+        }
+        W = stdp_learn(c, W, delta, epost, epre, dk);
+    }
+    return W;
+}
+
+// The fPost branch: post fired at step t; walk the pre history (both builds agree here).
+__device__ float stdp_post(const NetDev &n, const StdpConst &c, float W, int pre, int post,
+                           int total_delay, unsigned long long t)
+{
+    const int ms = n.max_spikes;
+    const bool sgn = n.stdp_signed != 0;
+    const int cpost = n.spikeCount[post] + n.spikeCountOffset[post];
+    const int cpre = n.spikeCount[pre] + n.spikeCountOffset[pre];
+    float epost = 1.0f;
+    const unsigned long long q2 = hist_at(n, post, cpost, -2);
+    const bool ok = sgn ? ((long long)q2 > 0) : (q2 != BG3_ULONG_MAX);
+    if (ok && c.useFD) epost = (float)(1.0 - (double)exp_interval(n, t - q2, sgn, c.tauspost));
+    for (int off = -1;; --off) {
+        if (off < -ms) { set_err(n, ERR_STDP_RING); break; }
+        const unsigned long long sh = hist_at(n, pre, cpre, off);
+        if (sh == BG3_ULONG_MAX) break;
+        const unsigned long long dd = t - (unsigned long long)(long long)total_delay - sh;
+        const float delta = (sgn ? (float)(long long)dd : (float)dd) * n.dt;
+        if (delta <= 0.0f || (double)delta >= 3.0 * (double)c.taupos) break;
+        float epre = 1.0f;
+        if (c.useFD) {
+            if (off - 1 < -ms) { set_err(n, ERR_STDP_RING); break; }
+            const unsigned long long sh2 = hist_at(n, pre, cpre, off - 1);
+            if (sh2 == BG3_ULONG_MAX) break;
+            epre = (float)(1.0 - (double)exp_interval(n, sh - sh2, sgn, c.tauspre));
+        }
+        W = stdp_learn(c, W, delta, epost, epre, (long long)dd);
+    }
+    return W;
+}
+
 // ---- spike arrival ---------------------------------------------------------------------------
 // Arrival of a spike emitted at step tf on plane slot p at step t: the isSpikeQueue hit of
 // AllSpikingSynapses::advanceSynapse (Synapses/AllSpikingSynapses.cpp:297-319) followed by
-// changePSR — AllDSSynapses.cpp:227-247 for DS, AllSpikingSynapses.cpp:327-334 otherwise.
+// changePSR — AllDSSynapses.cpp:227-247 for DS and dynamic STDP, AllSpikingSynapses.cpp:327-334
+// for spiking and STDP synapses; the STDP kinds (2, 3) first run the fPre learning walk.
 template <int SYN>
-__device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_t tf, uint32_t t)
+__device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_t tf,
+                                            unsigned long long t64, int src)
 {
+    const uint32_t t = (uint32_t)t64;
     EvSlot e = n.ev[p];
     if ((int32_t)(tf - e.born) < 0) return;  // the synapse did not exist when the spike left
     float dec = n.dtab[n.dcls[p]];
     float ps = n.psr[p];
-    if (SYN == 1) {
+    if (SYN >= 2) {
+        int k, d;
+        pos_slot(p, n.Np, k, d);
+        e.W = stdp_pre(n, n.stdp[n.stype[p]], e.W, src, d, t64);
+        n.ev[p].W = e.W;
+    }
+    if (SYN == 1 || SYN == 3) {
         float u = e.u, r = e.r;
         if (e.last != BG3_NO_SPIKE32) {
-            float isi = (float)(t - e.last) * n.dt;
-            r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_cr(-isi / e.D);
-            u = e.U + u * (1.0f - e.U) * exp_cr(-isi / e.F);
+            const uint32_t k = t - e.last;
+            r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_steps(n, k, e.D);
+            u = e.U + u * (1.0f - e.U) * exp_steps(n, k, e.F);
         }
         ps = ps + ((e.W / dec) * u * r);
         EvSlot *q = &n.ev[p];
@@ -205,7 +337,7 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int gw, int nw, boo
             const int i = ids[s];
             const uint32_t b = beg[i], k = cnt[i];
             for (uint32_t j = lane; j < k; j += 32)
-                deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, (uint32_t)t);
+                deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, t, i);
         }
     }
 }
@@ -230,6 +362,45 @@ __global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets)
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     deliver_net<SYN>(nets[blockIdx.y], gw, nw, blockIdx.x == 0 && threadIdx.x == 0);
+}
+
+// The fPost branch (AllSTDPSynapses.cpp:368-418) for every in-use synapse onto a neuron that
+// fired at step t (postSpikeHit marks them all, AllSpikingNeurons.cpp:128-138, with
+// total_delayPost 0, so the post queue is read in the same step).  One warp per fired neuron,
+// one lane per incoming synapse; runs after the arrivals of step t (the fPre branch comes first
+// in the reference) and before the sweep.
+__device__ __forceinline__ void stdp_post_net(const NetDev &n, int gw, int nw)
+{
+    const unsigned long long t = *n.step;
+    const int slot = (int)(t & (BG3_RING - 1));
+    const int m = min(n.ring_n[slot], n.N);
+    const int32_t *ids = n.ring + (size_t)slot * n.N;
+    const int lane = threadIdx.x & 31;
+    for (int s = gw; s < m; s += nw) {
+        const int d = ids[s];
+        const int cnt = (int)n.count[d];
+        for (int k = lane; k < cnt; k += 32) {
+            const size_t p = slot_pos(k, d, n.Np);
+            const float W = n.ev[p].W;
+            const float W2 = stdp_post(n, n.stdp[n.stype[p]], W, n.src[p], d, n.ltab[n.lcls[p]], t);
+            n.ev[p].W = W2;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_stdp_post(const __grid_constant__ NetDev n)
+{
+    pdl_wait();
+    pdl_trigger();
+    stdp_post_net(n, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+}
+
+__global__ void __launch_bounds__(256) k_stdp_post_batch(const NetDev *nets)
+{
+    pdl_wait();
+    pdl_trigger();
+    stdp_post_net(nets[blockIdx.y], (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                  (gridDim.x * blockDim.x) >> 5);
 }
 
 // Batched standalone neuron pass (device noise): grid.y indexes the network.
@@ -482,10 +653,16 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, int block, size_t smem
     cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
+// Spike arrivals of the step, then (STDP kinds) the post-spike learning pass.
 void launch_deliver(const NetDev &h, cudaStream_t s)
 {
-    if (h.syn_kind == 1) launch_pdl(k_deliver<1>, deliver_blocks(), 256, 0, s, h);
-    else launch_pdl(k_deliver<0>, deliver_blocks(), 256, 0, s, h);
+    switch (h.syn_kind) {
+    case 1: launch_pdl(k_deliver<1>, deliver_blocks(), 256, 0, s, h); break;
+    case 2: launch_pdl(k_deliver<2>, deliver_blocks(), 256, 0, s, h); break;
+    case 3: launch_pdl(k_deliver<3>, deliver_blocks(), 256, 0, s, h); break;
+    default: launch_pdl(k_deliver<0>, deliver_blocks(), 256, 0, s, h); break;
+    }
+    if (h.syn_kind >= 2) launch_pdl(k_stdp_post, deliver_blocks(), 256, 0, s, h);
 }
 
 template <int SYN, bool FUSE>
@@ -520,8 +697,14 @@ void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStrea
 {
     // per network: enough warps for a burst, few enough that the grid stays small
     const int per_net = std::max(2, std::min(16, 608 / std::max(count, 1)));
-    if (syn_kind == 1) launch_pdl(k_deliver_batch<1>, dim3(per_net, count), 256, 0, s, nets);
-    else launch_pdl(k_deliver_batch<0>, dim3(per_net, count), 256, 0, s, nets);
+    const dim3 grid(per_net, count);
+    switch (syn_kind) {
+    case 1: launch_pdl(k_deliver_batch<1>, grid, 256, 0, s, nets); break;
+    case 2: launch_pdl(k_deliver_batch<2>, grid, 256, 0, s, nets); break;
+    case 3: launch_pdl(k_deliver_batch<3>, grid, 256, 0, s, nets); break;
+    default: launch_pdl(k_deliver_batch<0>, grid, 256, 0, s, nets); break;
+    }
+    if (syn_kind >= 2) launch_pdl(k_stdp_post_batch, grid, 256, 0, s, nets);
 }
 
 void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int ntiles,
@@ -534,7 +717,7 @@ void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
                   cudaStream_t s)
 {
-    if (h.syn_kind == 1) {
+    if (h.syn_kind == 1 || h.syn_kind == 3) {
         if (fuse) launch_sweep_t<1, true>(h, tp, tc, s);
         else launch_sweep_t<1, false>(h, tp, tc, s);
     } else {

@@ -20,6 +20,7 @@ c_u8p = ctypes.POINTER(ctypes.c_uint8)
 BG3_NEURON_LIF, BG3_NEURON_IZH = 0, 1
 BG3_SYN_SPIKING, BG3_SYN_DS, BG3_SYN_STDP, BG3_SYN_DYNSTDP = 0, 1, 2, 3
 BG3_NOISE_DEVICE, BG3_NOISE_INJECT = 0, 1
+BG3_STDP_HOST, BG3_STDP_DEVICE = 0, 1
 ERR_BITS = {1: "history overflow", 2: "double spike in a queue slot", 4: "synapse row full",
             8: "injected noise exhausted", 16: "negative growth weight"}
 
@@ -38,6 +39,25 @@ class LifArrays(ctypes.Structure):
                                       "Trefract", "summation")] + \
                [(k, c_i32p) for k in ("nStepsInRefr", "spikeCount", "spikeCountOffset")] + \
                [("history", c_u64p)]
+
+
+class IzhArrays(ctypes.Structure):
+    _fields_ = [(k, c_f32p) for k in ("Aconst", "Bconst", "Cconst", "Dconst", "u", "C3")]
+
+
+STDP_FLOATS = ("tauspost", "tauspre", "taupos", "tauneg", "STDPgap", "Wex", "Aneg", "Apos",
+               "mupos", "muneg")
+
+
+class StdpArrays(ctypes.Structure):
+    _fields_ = [("delayQueuePost", c_u32p), ("delayIdxPost", c_i32p), ("total_delayPost", c_i32p)] + \
+               [(k, c_f32p) for k in STDP_FLOATS] + [("useFroemkeDanSTDP", c_u8p)]
+
+
+class StdpConstants(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_float * 4) for k in ("Apos", "Aneg", "STDPgap", "tauspost", "tauspre",
+                                                  "taupos", "tauneg", "Wex", "mupos", "muneg")] + \
+               [("useFroemkeDanSTDP", ctypes.c_int32 * 4)]
 
 
 class SynArrays(ctypes.Structure):
@@ -105,6 +125,12 @@ def load(build_if_missing=True):
         "bg3_create": ([ctypes.POINTER(NetDesc), ctypes.POINTER(vp)], ctypes.c_int),
         "bg3_destroy": ([vp], ctypes.c_int),
         "bg3_upload_lif": ([vp, ctypes.POINTER(LifArrays)], ctypes.c_int),
+        "bg3_upload_izh": ([vp, ctypes.POINTER(IzhArrays)], ctypes.c_int),
+        "bg3_download_izh": ([vp, ctypes.POINTER(IzhArrays)], ctypes.c_int),
+        "bg3_upload_stdp": ([vp, ctypes.POINTER(SynArrays), ctypes.POINTER(StdpArrays)], ctypes.c_int),
+        "bg3_download_stdp": ([vp, ctypes.POINTER(StdpArrays)], ctypes.c_int),
+        "bg3_set_stdp_constants": ([vp, ctypes.POINTER(StdpConstants)], ctypes.c_int),
+        "bg3_set_stdp_arithmetic": ([vp, ctypes.c_int], ctypes.c_int),
         "bg3_upload_layout": ([vp, c_f32p, c_f32p, c_i32p], ctypes.c_int),
         "bg3_upload_synapses": ([vp, ctypes.POINTER(SynArrays), ctypes.c_uint64], ctypes.c_int),
         "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
@@ -180,6 +206,10 @@ LIF_FIELDS = [("Vm", np.float32), ("Vthresh", np.float32), ("Vreset", np.float32
               ("I0", np.float32), ("Inoise", np.float32), ("C1", np.float32), ("C2", np.float32),
               ("Trefract", np.float32), ("summation", np.float32), ("nStepsInRefr", np.int32),
               ("spikeCount", np.int32), ("spikeCountOffset", np.int32)]
+STDP_FIELDS = [("delayQueuePost", np.uint32), ("delayIdxPost", np.int32),
+               ("total_delayPost", np.int32)] + [(k, np.float32) for k in STDP_FLOATS] + \
+              [("useFroemkeDanSTDP", np.uint8)]
+IZH_FIELDS = ("Aconst", "Bconst", "Cconst", "Dconst", "u", "C3")
 SYN_FIELDS = [("in_use", np.uint8), ("src", np.int32), ("type", np.int32),
               ("delayIdx", np.int32), ("total_delay", np.int32), ("W", np.float32),
               ("psr", np.float32), ("decay", np.float32), ("tau", np.float32),
@@ -228,6 +258,52 @@ class Network:
             keep["history"] = np.ascontiguousarray(arrs["history"], dtype=np.uint64)
             s.history = _p(keep["history"])
         check(self.L.bg3_upload_lif(self.h, ctypes.byref(s)), "bg3_upload_lif")
+
+    def upload_izh(self, **arrs):
+        """Izhikevich arrays Aconst, Bconst, Cconst, Dconst, u, C3 (all required)."""
+        keep = {k: np.ascontiguousarray(arrs[k], dtype=np.float32) for k in IZH_FIELDS}
+        s = IzhArrays(*[_p(keep[k]) for k in IZH_FIELDS])
+        check(self.L.bg3_upload_izh(self.h, ctypes.byref(s)), "bg3_upload_izh")
+
+    def download_izh(self):
+        out = {k: np.zeros(self.N, np.float32) for k in IZH_FIELDS}
+        s = IzhArrays(*[_p(out[k]) for k in IZH_FIELDS])
+        check(self.L.bg3_download_izh(self.h, ctypes.byref(s)), "bg3_download_izh")
+        return out
+
+    def upload_stdp(self, in_use, type, delayIdx, **arrs):
+        """STDP fields of the slots (reference layout); in_use, type and delayIdx as uploaded."""
+        keep = {"in_use": np.ascontiguousarray(in_use, np.uint8),
+                "type": np.ascontiguousarray(type, np.int32),
+                "delayIdx": np.ascontiguousarray(delayIdx, np.int32)}
+        syn = SynArrays()
+        for k in keep:
+            setattr(syn, k, _p(keep[k]))
+        st = StdpArrays()
+        for k, dt in STDP_FIELDS:
+            keep["s_" + k] = np.ascontiguousarray(arrs[k], dt)
+            setattr(st, k, _p(keep["s_" + k]))
+        check(self.L.bg3_upload_stdp(self.h, ctypes.byref(syn), ctypes.byref(st)), "bg3_upload_stdp")
+
+    def download_stdp(self):
+        S = self.N * self.max_syn
+        out = {k: np.zeros(S, dt) for k, dt in STDP_FIELDS}
+        st = StdpArrays()
+        for k, _ in STDP_FIELDS:
+            setattr(st, k, _p(out[k]))
+        check(self.L.bg3_download_stdp(self.h, ctypes.byref(st)), "bg3_download_stdp")
+        return out
+
+    def set_stdp_constants(self, **per_type):
+        """Per-type (II, IE, EI, EE) constants: each keyword a scalar or 4 values."""
+        c = StdpConstants()
+        for k, _ in StdpConstants._fields_:
+            v = np.broadcast_to(np.asarray(per_type[k]), (4,))
+            getattr(c, k)[:] = [float(x) if k != "useFroemkeDanSTDP" else int(x) for x in v]
+        check(self.L.bg3_set_stdp_constants(self.h, ctypes.byref(c)), "bg3_set_stdp_constants")
+
+    def set_stdp_arithmetic(self, mode):
+        check(self.L.bg3_set_stdp_arithmetic(self.h, int(mode)), "bg3_set_stdp_arithmetic")
 
     def upload_layout(self, xloc, yloc, ntype):
         x = np.ascontiguousarray(xloc, np.float32)

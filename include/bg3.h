@@ -47,7 +47,9 @@ enum {
     BG3_ERR_SPIKE_LIST = 1u << 5,       /* more spikes in one step than neurons (internal check)    */
     BG3_ERR_TIMEOUT = 1u << 6,          /* a bounded device wait expired (the kernel drained)       */
     BG3_ERR_STEP_RANGE = 1u << 7,       /* step counter beyond 2^32 - 256 (32-bit spike times)      */
-    BG3_ERR_ISI_EXHAUSTED = 1u << 8     /* injected Poisson ISI draws ran out                        */
+    BG3_ERR_ISI_EXHAUSTED = 1u << 8,    /* injected Poisson ISI draws ran out                        */
+    BG3_ERR_STDP_RING = 1u << 9         /* an STDP walk reached the oldest entry of a full spike ring
+                                           (the reference reads outside the ring there)              */
 };
 
 enum { BG3_NEURON_LIF = 0, BG3_NEURON_IZH = 1 };
@@ -85,6 +87,13 @@ typedef struct {
     uint64_t *history;
 } bg3_lif_arrays;
 
+/* Izhikevich arrays, each n_neurons long (Neurons/AllIZHNeurons.h:439-471): a, b, c, d, the
+ * recovery variable u and C3 = deltaT * 1000.  The IF fields (Vm, Vthresh, I0, Inoise, C2,
+ * Trefract, ...) travel in bg3_lif_arrays; C1 and Vreset are unused by this model. */
+typedef struct {
+    float *Aconst, *Bconst, *Cconst, *Dconst, *u, *C3;
+} bg3_izh_arrays;
+
 /* Synapse slot arrays in the reference layout, n_neurons * max_syn_per_neuron long
  * (Synapses/AllSynapses.h:188-232, AllSpikingSynapses.h:342-355, AllDSSynapses.h:269-336).
  * in_use uses one byte per slot; counts is n_neurons long (synapse_counts).  On upload the
@@ -98,6 +107,31 @@ typedef struct {
     float *U, *D, *F, *u, *r;
     uint64_t *lastSpike;
 } bg3_synapse_arrays;
+
+/* STDP slot arrays (Synapses/AllSTDPSynapses.h:330-420), n_neurons * max_syn_per_neuron long,
+ * used with BG3_SYN_STDP and BG3_SYN_DYNSTDP. */
+typedef struct {
+    uint32_t *delayQueuePost;
+    int32_t *delayIdxPost, *total_delayPost;
+    float *tauspost, *tauspre, *taupos, *tauneg, *STDPgap, *Wex, *Aneg, *Apos, *mupos, *muneg;
+    uint8_t *useFroemkeDanSTDP;
+} bg3_stdp_arrays;
+
+/* STDP constants per synapse type II, IE, EI, EE.  AllSTDPSynapses::createSynapse gives every
+ * synapse the same values (Synapses/AllSTDPSynapses.cpp:252-273: Apos 0.5, Aneg -0.5, STDPgap
+ * 2 ms, tauspost 75 ms, tauspre 34 ms, taupos 15 ms, tauneg 35 ms, Wex 1, mu 0, Froemke-Dan on),
+ * which are the defaults of a new network. */
+typedef struct {
+    float Apos[4], Aneg[4], STDPgap[4], tauspost[4], tauspre[4], taupos[4], tauneg[4], Wex[4];
+    float mupos[4], muneg[4];
+    int32_t useFroemkeDanSTDP[4];
+} bg3_stdp_constants;
+
+/* Spike-time arithmetic of the STDP walks.  HOST: the reference's host build
+ * (Synapses/AllSTDPSynapses.cpp:283-421, uint64_t spike times: the pre-spike walk's interval
+ * wraps, so pre-after-post pairs only apply the weight clamps).  DEVICE: its device build
+ * (Synapses/AllSynapsesDeviceFuncs_d.cu:239-380, int64_t spike times: depression applies). */
+enum { BG3_STDP_HOST = 0, BG3_STDP_DEVICE = 1 };
 
 /* Synapse constants per synapse type II, IE, EI, EE (Utils/Global.h:100), as the reference's
  * createSynapse computes them on the host (Synapses/AllSpikingSynapses.cpp:192-240,
@@ -132,6 +166,9 @@ int bg3_destroy(bg3_net *net);
 /* ---- host -> device ------------------------------------------------------------------- */
 /* IAllNeurons::copyNeuronHostToDevice (Neurons/IAllNeurons.h:114). */
 int bg3_upload_lif(bg3_net *net, const bg3_lif_arrays *a);
+/* AllIZHNeurons::copyNeuronHostToDevice (Neurons/AllIZHNeurons_d.cu:91-121): the Izhikevich
+ * arrays of a BG3_NEURON_IZH network (the IF arrays go through bg3_upload_lif). */
+int bg3_upload_izh(bg3_net *net, const bg3_izh_arrays *a);
 /* Layout arrays (Layouts/Layout.h: xloc, yloc, neuron_type_map as INH=1 / EXC=2). */
 int bg3_upload_layout(bg3_net *net, const float *xloc, const float *yloc, const int32_t *ntype);
 /* IAllSynapses::copySynapseHostToDevice (Synapses/IAllSynapses.h:160) plus the index-map copy of
@@ -184,12 +221,26 @@ int bg3_step(bg3_net *net, int64_t nsteps);
  * epoch number (SimulationInfo::currentStep). */
 int bg3_epoch_growth(bg3_net *net, int32_t epoch);
 
+/* AllSTDPSynapses::copySynapseHostToDevice (Synapses/AllSTDPSynapses_d.cu:125-195): the STDP
+ * fields of the slots given by syn (in_use, type, delayIdx).  Constants must be uniform per
+ * synapse type; post queues must be empty with total_delayPost 0 (BG3_EUNSUPPORTED otherwise). */
+int bg3_upload_stdp(bg3_net *net, const bg3_synapse_arrays *syn, const bg3_stdp_arrays *a);
+/* Constants for synapses created by the device growth pass from now on. */
+int bg3_set_stdp_constants(bg3_net *net, const bg3_stdp_constants *c);
+/* BG3_STDP_HOST (default) or BG3_STDP_DEVICE. */
+int bg3_set_stdp_arithmetic(bg3_net *net, int mode);
+
 /* ---- device -> host ------------------------------------------------------------------- */
 int bg3_sync(bg3_net *net);
 int bg3_get_step(bg3_net *net, uint64_t *step);
 int bg3_error_word(bg3_net *net, uint32_t *err);
 /* IAllNeurons::copyNeuronDeviceToHost (Neurons/IAllNeurons.h:122); history included. */
 int bg3_download_lif(bg3_net *net, bg3_lif_arrays *a);
+/* AllIZHNeurons::copyNeuronDeviceToHost (Neurons/AllIZHNeurons_d.cu:125-150). */
+int bg3_download_izh(bg3_net *net, bg3_izh_arrays *a);
+/* AllSTDPSynapses::copySynapseDeviceToHost (Synapses/AllSTDPSynapses_d.cu:198-250): STDP fields
+ * of the in-use slots in the reference layout. */
+int bg3_download_stdp(bg3_net *net, bg3_stdp_arrays *a);
 /* IAllSynapses::copySynapseDeviceToHost (Synapses/IAllSynapses.h:177), reference layout, with
  * delayIdx and delayQueue in the reference's per-synapse phase. */
 int bg3_download_synapses(bg3_net *net, bg3_synapse_arrays *a);

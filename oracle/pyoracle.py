@@ -230,6 +230,7 @@ class OracleNet:
 
     def stdp_signed(self, on=True):
         """STDP arithmetic of the reference's device build (signed spike-time differences)."""
+        self._signed = bool(on)
         self.L.bgo_stdp_signed(self.h, 1 if on else 0)
 
     def stdp_params(self, p11):

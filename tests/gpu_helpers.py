@@ -45,6 +45,33 @@ def setup_input(net, o, c, isi_steps=0):
             net.push_poisson_isis(begin, isis)
 
 
+STDP_MAP = [("delayQueuePost", "queuePost"), ("delayIdxPost", "delayIdxPost"),
+            ("total_delayPost", "total_delayPost"), ("tauspost", "tauspost"),
+            ("tauspre", "tauspre"), ("taupos", "taupos"), ("tauneg", "tauneg"),
+            ("STDPgap", "STDPgap"), ("Wex", "Wex"), ("Aneg", "Aneg"), ("Apos", "Apos"),
+            ("mupos", "mupos"), ("muneg", "muneg"), ("useFroemkeDanSTDP", "useFD")]
+
+
+def stdp_constants(c):
+    """Per-type constants of the synapses growth creates (the case's override, or the
+    reference's createSynapse values)."""
+    p = c.get("stdp")
+    if p is None:
+        p = [0.5, -0.5, 2e-3, 75e-3, 34e-3, 15e-3, 35e-3, 1.0, 1.0, 0.0, 0.0]
+    wex = [p[8], p[8], p[7], p[7]]  # II, IE (inhibitory source), EI, EE
+    return dict(Apos=p[0], Aneg=p[1], STDPgap=p[2], tauspost=p[3], tauspre=p[4], taupos=p[5],
+                tauneg=p[6], Wex=wex, mupos=p[9], muneg=p[10], useFroemkeDanSTDP=1)
+
+
+def setup_stdp(net, o, c):
+    net.set_stdp_constants(**stdp_constants(c))
+    if getattr(o, "_signed", False):
+        net.set_stdp_arithmetic(bg.BG3_STDP_DEVICE)
+    if o.total:
+        net.upload_stdp(o.arr("in_use"), o.arr("type"), o.arr("delayIdx"),
+                        **{k: o.arr(v) for k, v in STDP_MAP})
+
+
 def compare_input(net, o, where):
     if o.arr("pois_nisi").size == 0:
         return
@@ -67,6 +94,8 @@ def gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_INJECT, n_noise=0, noise_seed=
         net.upload_izh(**{k: o.arr(v) for k, v in IZH_MAP})
     skw = {k: o.arr(v) for k, v in SYN_MAP}
     net.upload_synapses(o.step, counts=o.arr("counts"), **skw)
+    if c.get("synapse", 1) >= 2:
+        setup_stdp(net, o, c)
     g = c["growth"]
     net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
                       g["start_radius"], o.arr("radii"), o.arr("rates"))
@@ -92,17 +121,27 @@ def compare_history(net, o, where):
     assert_same(where + " history", g["history"], o.arr("history"))
 
 
+DS_ONLY = {"U", "D", "F", "u", "r", "lastSpike"}
+
+
 def compare_synapses(net, o, where, tol_fields=()):
     g = net.download_synapses()
     used = o.arr("in_use").astype(bool)
+    ds = o.synapse_kind in (1, 3)
     assert_same(where + " in_use", g["in_use"], o.arr("in_use"))
     assert_same(where + " counts", g["counts"], o.arr("counts"))
     for k, v in SYN_MAP[1:]:
+        if k in DS_ONLY and not ds:
+            continue
         a, b = g[k][used], o.arr(v)[used]
         if k in tol_fields:
             np.testing.assert_allclose(a, b, rtol=1e-5, atol=0, err_msg=where + " " + k)
         else:
             assert_same("%s %s" % (where, k), a, b)
+    if o.synapse_kind >= 2:
+        st = net.download_stdp()
+        for k, v in STDP_MAP:
+            assert_same("%s %s" % (where, k), st[k][used], o.arr(v)[used])
     return g
 
 

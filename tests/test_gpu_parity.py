@@ -37,11 +37,13 @@ def _growth_both(o, net, e, resync=True):
         net.upload_weights(o.arr("W"))
 
 
-def run_locked(name, epochs=None, check_every=1, syn_every=None):
+def run_locked(name, epochs=None, check_every=1, syn_every=None, stdp_signed=False):
     c = case(name)
     E = epochs or c["epochs"]
     spe = steps_per_epoch(c)
     o = oracle_from_case(c)
+    if stdp_signed:
+        o.stdp_signed(True)
     net = gpu_from_oracle(o, c, n_noise=c["N"] * spe * E + 64, isi_steps=spe * E + 2)
     t = 0
     for e in range(E):
@@ -119,12 +121,33 @@ def test_izhikevich_bit_exact():
     """Izhikevich neurons (AllIZHNeurons) on a pre-grown 12x12 DS network: Vm, u, spikes and
     synapses step-locked with the oracle over 5 epochs with growth."""
     o, net = run_locked("izh_grown", check_every=10, syn_every=500)
-    assert o.total > 0 and int(o.arr("spikeCount").sum()) > 0
+    fired = int((o.arr("history") != np.uint64(0xFFFFFFFFFFFFFFFF)).sum())
+    assert o.total > 0 and fired > 0
 
 
 def test_spiking_synapses_bit_exact():
     """Plain AllSpikingSynapses (no facilitation / depression) on a pre-grown 10x10 network."""
     o, net = run_locked("c0_spiking", check_every=10, syn_every=500)
+    assert o.total > 0
+
+
+@pytest.mark.parametrize("name", ["c0_stdp", "c0_dstdp"])
+def test_stdp_bit_exact(name):
+    """STDP / dynamic STDP with the reference's createSynapse constants (host-build arithmetic):
+    weights, PSRs and the reconstructed post queues step-locked with the oracle."""
+    o, net = run_locked(name, check_every=10, syn_every=250)
+    assert o.total > 0
+
+
+def test_izhikevich_dynamic_stdp_poisson_bit_exact():
+    """Izhikevich neurons, dynamic STDP with bounded additive constants, Poisson drive."""
+    o, net = run_locked("izh_dstdp", check_every=10, syn_every=250)
+    assert o.total > 0
+
+
+def test_stdp_device_arithmetic_bit_exact():
+    """The reference device build's signed spike-time arithmetic (depression applies)."""
+    o, net = run_locked("izh_dstdp", check_every=10, syn_every=250, stdp_signed=True)
     assert o.total > 0
 
 
