@@ -27,6 +27,7 @@ void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 
                         bool fuse, cudaStream_t s);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
+void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
 
 static const int GRAPH_STEPS = 32;  // fused steps captured per CUDA graph replay
@@ -349,7 +350,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     A(dtab, BG3_MAX_DCLS) A(ltab, BG3_MAX_DELAYS)
     A(outBegin, N * BG3_MAX_DELAYS) A(outCount, N * BG3_MAX_DELAYS) A(outFill, N * BG3_MAX_DELAYS)
     A(outMap, S)
-    A(radii, N) A(rates, N) A(xloc, N) A(yloc, N)
+    A(radii, N) A(rates, N) A(xloc, N) A(yloc, N) A(grow_exp, (size_t)max_spikes + 1)
     A(burstiness, (size_t)std::max(h.n_burst_bins, 1)) A(spikes_hist, (size_t)std::max(h.n_spike_bins, 1))
     A(rates_hist, (size_t)(D.max_epochs + 1) * N) A(radii_hist, (size_t)(D.max_epochs + 1) * N)
     if (D.neuron_kind == BG3_NEURON_IZH) {
@@ -618,6 +619,14 @@ int bg3_upload_growth(bg3_net *n, const bg3_growth_params *p, const float *radii
     h.g_start_radius = p->start_radius; h.g_max_rate = p->max_rate;
     size_t N = h.N;
     int rc;
+    // ConnGrowth::updateConns' exp((epsilon - rate / maxRate) / beta) for rate = count / T
+    // (Connections/ConnGrowth.cpp:300-306), one value per possible spike count
+    std::vector<float> ge((size_t)h.max_spikes + 1);
+    for (int c = 0; c <= h.max_spikes; c++) {
+        const float rate = (float)c / h.epoch_duration;
+        ge[c] = expf((h.g_epsilon - rate / h.g_max_rate) / h.g_beta);
+    }
+    if ((rc = h2d(n, h.grow_exp, ge.data(), ge.size()))) return rc;
     if ((rc = h2d(n, h.radii, radii, N)) || (rc = h2d(n, h.rates, rates, N))) return rc;
     // recorder row 0 holds the start values (XmlGrowthRecorder::initDefaultValues / initValues)
     if ((rc = h2d(n, h.radii_hist, radii, N)) || (rc = h2d(n, h.rates_hist, rates, N))) return rc;
@@ -875,6 +884,15 @@ int bg3_epoch_growth(bg3_net *n, int32_t epoch)
     if (!n || epoch < 0) return BG3_EINVAL;
     bg3::launch_growth(n->h, n->d, epoch, n->stream);
     n->launches += 8;
+    CK(cudaGetLastError());
+    return BG3_OK;
+}
+
+int bg3_epoch_record(bg3_net *n)
+{
+    if (!n) return BG3_EINVAL;
+    bg3::launch_record(n->h, n->d, n->stream);
+    n->launches += 1;
     CK(cudaGetLastError());
     return BG3_OK;
 }

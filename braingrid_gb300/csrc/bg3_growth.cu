@@ -19,9 +19,12 @@ __global__ void k_growth_radii(const NetDev *nets)
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n.N) return;
     float T = n.epoch_duration;
-    float rate = (float)n.spikeCount[i] / T;
+    const int cnt = n.spikeCount[i];
+    float rate = (float)cnt / T;
     n.rates[i] = rate;
-    float e = exp_cr((n.g_epsilon - rate / n.g_max_rate) / n.g_beta);
+    // expf of the host library for every possible count, evaluated there in this order
+    float e = (cnt >= 0 && cnt <= n.max_spikes) ? n.grow_exp[cnt]
+                                                : exp_cr((n.g_epsilon - rate / n.g_max_rate) / n.g_beta);
     float og = 1.0f - 2.0f / (e + 1.0f);
     float trho = T * n.g_rho;
     n.radii[i] = n.radii[i] + trho * og;
@@ -230,7 +233,9 @@ __global__ void k_out_fill(const NetDev *nets)
 
 // ---- recorder (Recorders/XmlRecorder.cpp:71-104, XmlGrowthRecorder.cpp:72-97,
 //      Neurons/AllSpikingNeurons.cpp:77-86) ----------------------------------------------------
-__global__ void k_record_epoch(const NetDev *nets, int epoch)
+// XmlRecorder::compileHistories (Recorders/XmlRecorder.cpp:71-104) and, with growth, the
+// XmlGrowthRecorder additions (XmlGrowthRecorder.cpp:72-97).
+__global__ void k_record_epoch(const NetDev *nets, int epoch, bool growth)
 {
     const NetDev &n = nets[0];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -245,7 +250,7 @@ __global__ void k_record_epoch(const NetDev *nets, int epoch)
         if (b1 >= 0 && b1 < n.n_burst_bins) atomicAdd(&n.burstiness[b1], 1.0f);
         if (b2 >= 0 && b2 < n.n_spike_bins) atomicAdd(&n.spikes_hist[b2], 1.0f);
     }
-    if (epoch >= 0 && epoch <= n.max_epochs) {
+    if (growth && epoch >= 0 && epoch <= n.max_epochs) {
         n.rates_hist[(size_t)epoch * n.N + i] = n.rates[i];
         float r = n.radii[i];
         if (r < n.g_min_radius) r = n.g_min_radius;
@@ -268,7 +273,12 @@ void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t
     k_out_count<<<sb, 256, 0, s>>>(d_net);
     k_out_scan<<<1, 1024, 0, s>>>(d_net);
     k_out_fill<<<sb, 256, 0, s>>>(d_net);
-    k_record_epoch<<<nb, 256, 0, s>>>(d_net, epoch);
+    k_record_epoch<<<nb, 256, 0, s>>>(d_net, epoch, true);
+}
+
+void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s)
+{
+    k_record_epoch<<<(h.N + 255) / 256, 256, 0, s>>>(d_net, -1, false);
 }
 
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s)

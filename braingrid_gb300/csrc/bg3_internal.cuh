@@ -96,6 +96,7 @@ struct NetDev {
     // growth
     float *radii, *rates, *xloc, *yloc;
     float g_epsilon, g_beta, g_rho, g_target_rate, g_min_radius, g_start_radius, g_max_rate;
+    float *grow_exp;   // [max_spikes + 1]: the outgrowth exp for each spike count (host libm)
     // recorder
     float *burstiness, *spikes_hist, *rates_hist, *radii_hist;
     int32_t n_burst_bins, n_spike_bins, max_epochs;

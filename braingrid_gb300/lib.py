@@ -131,6 +131,7 @@ def load(build_if_missing=True):
         "bg3_download_stdp": ([vp, ctypes.POINTER(StdpArrays)], ctypes.c_int),
         "bg3_set_stdp_constants": ([vp, ctypes.POINTER(StdpConstants)], ctypes.c_int),
         "bg3_set_stdp_arithmetic": ([vp, ctypes.c_int], ctypes.c_int),
+        "bg3_epoch_record": ([vp], ctypes.c_int),
         "bg3_upload_layout": ([vp, c_f32p, c_f32p, c_i32p], ctypes.c_int),
         "bg3_upload_synapses": ([vp, ctypes.POINTER(SynArrays), ctypes.c_uint64], ctypes.c_int),
         "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
@@ -375,6 +376,10 @@ class Network:
 
     def growth(self, epoch):
         check(self.L.bg3_epoch_growth(self.h, int(epoch)), "bg3_epoch_growth")
+
+    def record(self):
+        """Epoch end of a network without growth (recorder histograms, spike-count roll)."""
+        check(self.L.bg3_epoch_record(self.h), "bg3_epoch_record")
 
     def sync(self):
         check(self.L.bg3_sync(self.h), "bg3_sync")

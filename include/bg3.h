@@ -220,6 +220,10 @@ int bg3_step(bg3_net *net, int64_t nsteps);
  * histograms, rates/radii history, radius clamp, spike-count roll).  epoch is the 1-based
  * epoch number (SimulationInfo::currentStep). */
 int bg3_epoch_growth(bg3_net *net, int32_t epoch);
+/* updateHistory of a network without growth (ConnStatic: Connections/ConnStatic.h has no
+ * updateConnections work): XmlRecorder::compileHistories (Recorders/XmlRecorder.cpp:71-104),
+ * burstiness and 10 ms spike histograms plus the spike-count roll. */
+int bg3_epoch_record(bg3_net *net);
 
 /* AllSTDPSynapses::copySynapseHostToDevice (Synapses/AllSTDPSynapses_d.cu:125-195): the STDP
  * fields of the slots given by syn (in_use, type, delayIdx).  Constants must be uniform per

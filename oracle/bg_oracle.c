@@ -280,6 +280,10 @@ void bgo_set_step(bgo_net *n, uint64_t s) { n->step = s; }
 int64_t bgo_total_synapses(const bgo_net *n) { return n->total; }
 int bgo_flags(const bgo_net *n) { return n->flags; }
 void bgo_stdp_signed(bgo_net *n, int on) { n->stdp_signed = on ? 1 : 0; }
+void bgo_rng_skip(bgo_net *n, int64_t draws)
+{
+    for (int64_t k = 0; k < draws; k++) (void)bgo_mt_inrange(&n->rng, 0.0f, 1.0f);
+}
 void bgo_stdp_params(bgo_net *n, const float *p11)
 {
     n->stdp_override = 1;
@@ -1012,7 +1016,33 @@ void bgo_growth(bgo_net *n)
 /* XmlRecorder::compileHistories (Recorders/XmlRecorder.cpp:71-104) followed by the growth part
  * (Recorders/XmlGrowthRecorder.cpp:72-97: rates/radii history, radius clamp) and
  * AllSpikingNeurons::clearSpikeCounts (Neurons/AllSpikingNeurons.cpp:77-86). */
+static void record_spikes(bgo_net *n);
 void bgo_record_epoch(bgo_net *n, int epoch)
+{
+    record_spikes(n);
+    for (int i = 0; i < n->N; i++) {
+        n->ratesHistory[(size_t)epoch * n->N + i] = n->rates[i];
+        if (n->radii[i] < n->min_radius) n->radii[i] = n->min_radius;
+        n->radiiHistory[(size_t)epoch * n->N + i] = n->radii[i];
+    }
+    for (int i = 0; i < n->N; i++) {
+        n->spikeCountOffset[i] = (n->spikeCount[i] + n->spikeCountOffset[i]) % n->max_spikes;
+        n->spikeCount[i] = 0;
+    }
+}
+
+/* XmlRecorder::compileHistories alone (Recorders/XmlRecorder.cpp:71-104): the recorder of a
+ * network without growth (ConnStatic). */
+void bgo_record_static(bgo_net *n)
+{
+    record_spikes(n);
+    for (int i = 0; i < n->N; i++) {
+        n->spikeCountOffset[i] = (n->spikeCount[i] + n->spikeCountOffset[i]) % n->max_spikes;
+        n->spikeCount[i] = 0;
+    }
+}
+
+static void record_spikes(bgo_net *n)
 {
     int ms = n->max_spikes;
     for (int i = 0; i < n->N; i++) {
@@ -1024,14 +1054,5 @@ void bgo_record_epoch(bgo_net *n, int epoch)
             int b2 = (int)((double)h[idx] * (double)n->delta_t * 100);
             n->spikesHistory[b2] = n->spikesHistory[b2] + 1.0f;
         }
-    }
-    for (int i = 0; i < n->N; i++) {
-        n->ratesHistory[(size_t)epoch * n->N + i] = n->rates[i];
-        if (n->radii[i] < n->min_radius) n->radii[i] = n->min_radius;
-        n->radiiHistory[(size_t)epoch * n->N + i] = n->radii[i];
-    }
-    for (int i = 0; i < n->N; i++) {
-        n->spikeCountOffset[i] = (n->spikeCount[i] + n->spikeCountOffset[i]) % ms;
-        n->spikeCount[i] = 0;
     }
 }

@@ -89,10 +89,16 @@ int64_t bgo_noise_recorded(const bgo_net *n);
 void bgo_step(bgo_net *n, int nsteps);        /* advanceNeurons + advanceSynapses, nsteps times */
 void bgo_growth(bgo_net *n);                  /* updateConnections (ConnGrowth) + maps rebuild  */
 void bgo_record_epoch(bgo_net *n, int epoch); /* XmlGrowthRecorder::compileHistories            */
+/* XmlRecorder::compileHistories alone (Recorders/XmlRecorder.cpp:71-104), for ConnStatic. */
+void bgo_record_static(bgo_net *n);
 int bgo_flags(const bgo_net *n);
 /* STDP arithmetic: 0 = the reference's host build (uint64_t spike times), 1 = its device build
  * (int64_t spike times, AllSynapsesDeviceFuncs_d.cu:239-380). */
 void bgo_stdp_signed(bgo_net *n, int on);
+/* Advance the global rng by the given number of rand() draws (e.g. the weight draws of
+ * ConnStatic::setupConnections, Connections/ConnStatic.cpp:74-79, when its synapses are loaded
+ * from a reference dump). */
+void bgo_rng_skip(bgo_net *n, int64_t draws);
 /* STDP constants of synapses created from now on (the reference hard-codes them in
  * AllSTDPSynapses::createSynapse): Apos, Aneg, STDPgap, tauspost, tauspre, taupos, tauneg,
  * WexE (excitatory source), WexI (inhibitory source), mupos, muneg. */

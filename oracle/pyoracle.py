@@ -75,9 +75,11 @@ def lib():
         L.bgo_step.argtypes = [vp, i]
         L.bgo_growth.argtypes = [vp]
         L.bgo_record_epoch.argtypes = [vp, i]
+        L.bgo_record_static.argtypes = [vp]
         L.bgo_flags.restype = i
         L.bgo_flags.argtypes = [vp]
         L.bgo_stdp_signed.argtypes = [vp, i]
+        L.bgo_rng_skip.argtypes = [vp, i64]
         L.bgo_stdp_params.argtypes = [vp, ctypes.POINTER(f)]
         L.bgo_norm_fill.argtypes = [u32, ctypes.POINTER(f), i64]
         L.bgo_input_regular.argtypes = [vp, f, f, i, ctypes.POINTER(f)]
@@ -228,10 +230,17 @@ class OracleNet:
     def record_epoch(self, epoch):
         self.L.bgo_record_epoch(self.h, int(epoch))
 
+    def record_static(self):
+        """The recorder of a network without growth (XmlRecorder::compileHistories)."""
+        self.L.bgo_record_static(self.h)
+
     def stdp_signed(self, on=True):
         """STDP arithmetic of the reference's device build (signed spike-time differences)."""
         self._signed = bool(on)
         self.L.bgo_stdp_signed(self.h, 1 if on else 0)
+
+    def rng_skip(self, draws):
+        self.L.bgo_rng_skip(self.h, int(draws))
 
     def stdp_params(self, p11):
         self._stdp = np.asarray(p11, dtype=np.float32)

@@ -377,6 +377,7 @@ int main(int argc, char **argv)
     delete rgNormrnd[0];
     rgNormrnd[0] = rn;
 
+    if (n_stdp) override_stdp(m, si, stdp_p);  // synapses made by setupConnections (ConnStatic)
     ConnGrowth *g = dynamic_cast<ConnGrowth *>(m->conns());
     if (g && radii > 0)
         for (int i = 0; i < si->totalNeurons; i++) (*g->radii)[i] = (BGFLOAT)radii;

@@ -49,7 +49,7 @@ REG_VALUES = [1.5e-8 if ((i // 10) + (i % 10)) % 3 == 0 else 0.0 for i in range(
 def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, radii=None,
           max_firing_rate=200, frac_inh=0.10, n_starters=10, site_seed=1, keep_steps_every=None,
           fp64=False, config=None, inh=None, starters=None, syn_keep=None, stim=None,
-          neuron="lif", synapse=1, stdp=None):
+          neuron="lif", synapse=1, stdp=None, static=None):
     if inh is None:
         inh, starters = site_lists(width, height, frac_inh, n_starters, site_seed)
     c = dict(name=name, width=width, height=height, N=width * height, tsim=tsim, epochs=epochs,
@@ -58,7 +58,7 @@ def _case(name, width, height, tsim, epochs, max_syn, seed=1, target_rate=1.0, r
                                             target_rate=target_rate, min_radius=0.1,
                                             start_radius=0.4),
              radii=radii, keep_steps_every=keep_steps_every, fp64=fp64, syn_keep=syn_keep,
-             stim=stim, neuron=neuron, synapse=synapse, stdp=stdp)
+             stim=stim, neuron=neuron, synapse=synapse, stdp=stdp, static=static)
     c["config"] = config or "configfiles/bg3/%s.xml" % name
     args = []
     if stim is not None:
@@ -111,6 +111,13 @@ CASES = [
     _case("izh_dstdp", 12, 12, 0.5, 2, 100, radii=1.3, max_firing_rate=1000, site_seed=4,
           keep_steps_every=50, neuron="izh", synapse=3, stdp=STDP_SOFT,
           stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=None)),
+    # ConnStatic: 10 nearest neighbours within radius 5, weights U[10, 20] nA / U[-40, -20] nA
+    # (pRewiring 0.1 is read but never applied by the reference); Izhikevich neurons, dynamic
+    # STDP and Poisson drive as in the 512-network sweep
+    _case("izh_static", 12, 12, 0.5, 2, 100, max_firing_rate=1000, site_seed=5,
+          keep_steps_every=50, neuron="izh", synapse=3, stdp=STDP_SOFT,
+          stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=None),
+          static=dict(n=10, radius=5.0, rewire=0.1, exc=(10e-9, 20e-9), inh=(-40e-9, -20e-9))),
     # LIF neurons with plain spiking synapses (AllSpikingSynapses), pre-grown
     _case("c0_spiking", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=100,
           synapse=0),
@@ -158,13 +165,7 @@ _XML = """<?xml version="1.0" encoding="UTF-8" standalone="no"?>
 {neuron_params}
     </NeuronsParams>
     <SynapsesParams class="{synapse_class}" name="SynapsesParams"></SynapsesParams>
-    <ConnectionsParams class="ConnGrowth" name="ConnectionsParams">
-      <GrowthParams name="GrowthParams">
-        <epsilon name="epsilon">{epsilon}</epsilon><beta name="beta">{beta}</beta><rho name="rho">{rho}</rho>
-        <targetRate name="targetRate">{target_rate}</targetRate><minRadius name="minRadius">{min_radius}</minRadius>
-        <startRadius name="startRadius">{start_radius}</startRadius>
-      </GrowthParams>
-    </ConnectionsParams>
+{connections}
     <LayoutParams class="FixedLayout" name="LayoutParams">
       <LayoutFiles name="LayoutFiles">
         <activeNListFileName name="activeNListFileName" type="InputFile">configfiles/bg3/{name}-active.xml</activeNListFileName>
@@ -175,6 +176,27 @@ _XML = """<?xml version="1.0" encoding="UTF-8" standalone="no"?>
   </ModelParams>
 </BGSimParams>
 """
+
+
+GROWTH_XML = """    <ConnectionsParams class="ConnGrowth" name="ConnectionsParams">
+      <GrowthParams name="GrowthParams">
+        <epsilon name="epsilon">{epsilon}</epsilon><beta name="beta">{beta}</beta><rho name="rho">{rho}</rho>
+        <targetRate name="targetRate">{target_rate}</targetRate><minRadius name="minRadius">{min_radius}</minRadius>
+        <startRadius name="startRadius">{start_radius}</startRadius>
+      </GrowthParams>
+    </ConnectionsParams>"""
+
+STATIC_XML = """    <ConnectionsParams class="ConnStatic" name="ConnectionsParams">
+      <StaticConnectionsParams name="StaticConnectionsParams">
+        <nConnsPerNeuron name="nConnsPerNeuron">{n}</nConnsPerNeuron>
+        <threshConnsRadius name="threshConnsRadius">{radius!r}</threshConnsRadius>
+        <pRewiring name="pRewiring">{rewire!r}</pRewiring>
+      </StaticConnectionsParams>
+      <StaticConnectionsWeight name="StaticConnectionsWeight">
+        <minExc name="minExc">{exc[0]!r}</minExc><maxExc name="maxExc">{exc[1]!r}</maxExc>
+        <minInh name="minInh">{inh[0]!r}</minInh><maxInh name="maxInh">{inh[1]!r}</maxInh>
+      </StaticConnectionsWeight>
+    </ConnectionsParams>"""
 
 
 def _range_xml(ranges):
@@ -206,6 +228,10 @@ def write_config_tree(cfgdir):
         p = dict(c)
         p.update(c["growth"])
         p["synapse_class"] = SYN_CLASS[c.get("synapse", 1)]
+        if c.get("static"):
+            p["connections"] = STATIC_XML.format(**c["static"])
+        else:
+            p["connections"] = GROWTH_XML.format(**c["growth"])
         if c.get("neuron") == "izh":
             p["neuron_class"] = "AllIZHNeurons"
             p["neuron_params"] = _range_xml(IZH_IF_RANGES) + "\n" + _izh_xml(IZH_RANGES)

@@ -37,10 +37,12 @@ def oracle_from_case(c, record_noise=0):
         o.create_izh(IZH_IF_RANGES, IZH_RANGES)
     else:
         o.create_lif(LIF_RANGES)
-    if stim and stim["kind"] == "poisson":
-        o.input_poisson(stim["fr_mean"], stim["weight"], stim.get("masks"))
     if c.get("stdp") is not None:
         o.stdp_params(c["stdp"])
+    if c.get("static"):
+        load_static_synapses(o, c)
+    if stim and stim["kind"] == "poisson":
+        o.input_poisson(stim["fr_mean"], stim["weight"], stim.get("masks"))
     g = c["growth"]
     o.growth_init(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
                   g["start_radius"])
@@ -50,6 +52,20 @@ def oracle_from_case(c, record_noise=0):
     if c.get("radii") is not None:
         o.arr("radii")[:] = np.float32(c["radii"])
     return o
+
+
+def load_static_synapses(o, c):
+    """ConnStatic::setupConnections' synapses (Connections/ConnStatic.cpp:33-88) taken from the
+    reference's own dump of the case (its neighbour sort breaks distance ties in libstdc++'s
+    order), added in slot order so every row fills as in the reference; the global rng then
+    skips the one weight draw per synapse."""
+    fx = load_fixture(c["name"])
+    slots = fx["i.slots"].astype(np.int64)
+    for k, s in enumerate(slots):
+        o.create_synapse(int(s // c["max_syn"]), int(fx["i.src"][k]), int(fx["i.type"][k]),
+                         float(fx["i.W"][k]))
+    assert o.rebuild_maps() == 0
+    o.rng_skip(len(slots))
 
 
 def steps_per_epoch(c):

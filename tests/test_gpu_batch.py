@@ -73,3 +73,45 @@ def test_batch_then_member_step_and_growth():
     for k, (p, q) in enumerate(zip(plain, batched)):
         assert_same("net %d Vm" % k, q.download_lif()["Vm"], p.download_lif()["Vm"])
         assert p.sim_step == q.sim_step
+
+
+def make_mixed_stdp():
+    """An Izhikevich network with Poisson drive and a LIF network (device-build STDP
+    arithmetic), both dynamic STDP, wired by one device growth pass."""
+    from tests.golden.configs import case
+    from tests.gpu_helpers import gpu_from_oracle
+    from tests.netcases import oracle_from_case
+    nets = []
+    for name, seed, signed in (("izh_dstdp", 3, False), ("c0_dstdp", 5, True)):
+        c = case(name)
+        o = oracle_from_case(c)
+        if signed:
+            o.stdp_signed(True)
+        net = gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_DEVICE, noise_seed=seed)
+        net.growth(1)
+        nets.append(net)
+    return nets
+
+
+def test_batch_izhikevich_stdp_matches_plain_bit_exact():
+    plain = make_mixed_stdp()
+    batched = make_mixed_stdp()
+    assert all(n.total_synapses() > 0 for n in plain)
+    b = bg.Batch(batched)
+    for chunk in (1, 250, 2000):
+        for n in plain:
+            n.step(chunk)
+        b.step(chunk)
+        b.sync()
+        for k, (p, q) in enumerate(zip(plain, batched)):
+            gp, sp = state(p)
+            gq, sq = state(q)
+            for f in ("Vm", "nStepsInRefr", "spikeCount", "history"):
+                assert_same("net %d %s" % (k, f), gq[f], gp[f])
+            used = sp["in_use"].astype(bool)
+            for f in ("W", "psr", "u", "r", "lastSpike"):
+                assert_same("net %d %s" % (k, f), sq[f][used], sp[f][used])
+        assert_same("izh u", batched[0].download_izh()["u"], plain[0].download_izh()["u"])
+    assert all(int(n.download_lif()["spikeCount"].sum()) > 0 for n in plain)
+    errs = [n.error_word for n in plain + batched]
+    assert all(e == 0 for e in errs), errs

@@ -60,7 +60,12 @@ def run_locked(name, epochs=None, check_every=1, syn_every=None, stdp_signed=Fal
         compare_history(net, o, "epoch %d" % e)
         if o.total:
             compare_synapses(net, o, "epoch %d end" % e)
-        _growth_both(o, net, e + 1)
+        if c.get("static"):
+            o.record_static()
+            net.record()
+            compare_neurons(net, o, "record %d" % e)
+        else:
+            _growth_both(o, net, e + 1)
     assert net.error_word == 0
     return o, net
 
@@ -143,6 +148,16 @@ def test_izhikevich_dynamic_stdp_poisson_bit_exact():
     """Izhikevich neurons, dynamic STDP with bounded additive constants, Poisson drive."""
     o, net = run_locked("izh_dstdp", check_every=10, syn_every=250)
     assert o.total > 0
+
+
+def test_static_connections_izhikevich_stdp_bit_exact():
+    """ConnStatic network (the reference's own setupConnections output) with Izhikevich
+    neurons, dynamic STDP and Poisson drive; the epoch end runs the plain recorder."""
+    o, net = run_locked("izh_static", check_every=10, syn_every=250)
+    assert o.total > 1000
+    b, s, rh, ra = net.download_histories()
+    assert_same("burstiness", b, o.arr("burstinessHist"))
+    assert_same("spikes history", s, o.arr("spikesHistory"))
 
 
 def test_stdp_device_arithmetic_bit_exact():

@@ -28,7 +28,8 @@ def replay_against_fixture(name):
         if k in fx:
             assert_same(k, o.arr(g), fx[k])
     assert_same("ntype", o.arr("ntype"), fx["ntype"])
-    assert_same("radii0", o.arr("radii"), fx["radii"])
+    if "radii" in fx:
+        assert_same("radii0", o.arr("radii"), fx["radii"])
     K = c.get("keep_steps_every")
     spe = steps_per_epoch(c)
     t = 0
@@ -56,16 +57,21 @@ def replay_against_fixture(name):
                 key = "pre.%s#%d" % (f, e)
                 if key in fx:
                     assert_same(key, o.arr(f)[slots], fx[key])
-        o.growth()
+        if not c.get("static"):
+            o.growth()
         for f in ("radii", "rates", "counts", "inMap", "outMap", "inCount", "outCount",
                   "outBegin", "inBegin"):
             key = "grow.%s#%d" % (f, e) if c["epochs"] > 1 else "grow.%s" % f
             if key in fx:
                 assert_same(key, o.arr(f), fx[key])
-        o.record_epoch(e + 1)
+        if c.get("static"):
+            o.record_static()
+        else:
+            o.record_epoch(e + 1)
         suffix = "#%d" % e if c["epochs"] > 1 else ""
         for f in ("radii", "rates", "spikeCountOffset", "spikeCount"):
-            assert_same("post." + f + suffix, o.arr(f), fx["post." + f + suffix])
+            if ("post." + f + suffix) in fx:
+                assert_same("post." + f + suffix, o.arr(f), fx["post." + f + suffix])
         if ("post.slots" + suffix) in fx:
             slots = np.nonzero(o.arr("in_use"))[0]
             assert_same("post.slots" + suffix, slots, fx["post.slots" + suffix])
@@ -86,7 +92,7 @@ def test_norm_stream_matches_reference_tiny():
 
 @pytest.mark.parametrize("name", ["ref_tiny", "c0", "c0_grown", "c0_regular", "c0_poisson",
                                   "c0_poisson25", "izh_grown", "c0_spiking", "c0_stdp",
-                                  "c0_dstdp", "izh_dstdp"])
+                                  "c0_dstdp", "izh_dstdp", "izh_static"])
 def test_oracle_matches_reference_dump(name):
     o = replay_against_fixture(name)
     if name == "c0_grown":
