@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libbg3.so")
 ROOT = os.path.dirname(HERE)
 
-SOURCES = ["bg3_step.cu", "bg3_growth.cu", "bg3_api.cu", "bg3_noalloc.cu"]
+SOURCES = ["bg3_step.cu", "bg3_growth.cu", "bg3_api.cu", "bg3_noalloc.cu", "bg3_serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
@@ -40,7 +40,7 @@ def _stale(out, deps):
 def build(verbose=False, extra=()):
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(ROOT, "include", "bg3.h"))
+    headers += [os.path.join(ROOT, "include", f) for f in ("bg3.h", "bg3_serve.h")]
     objs = []
     jobs = []
     for s in SOURCES:

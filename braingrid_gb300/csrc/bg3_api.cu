@@ -32,6 +32,9 @@ void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 
 static const int GRAPH_STEPS = 32;  // fused steps captured per CUDA graph replay
 
+// kernels one step launches after its neuron pass: delivery (+ post-spike STDP) and the sweep
+static inline int step_kernels(int syn_kind) { return syn_kind >= BG3_SYN_STDP ? 3 : 2; }
+
 struct bg3_net {
     bg3_net_desc desc;
     NetDev h;                 // host copy of the device descriptor
@@ -51,6 +54,7 @@ struct bg3_net {
     size_t flush_size = 0;
     cudaGraphExec_t graph = nullptr;
     std::vector<std::tuple<int, int, uint32_t, uint32_t>> exp_keys;  // exp tables this net holds
+    uint64_t bytes = 0;                                                 // device bytes allocated
 };
 
 #define CK(x)                                                                            \
@@ -72,6 +76,7 @@ static int dalloc(bg3_net *n, T **p, size_t count, int fill = 0)
         return BG3_ENOMEM;
     }
     n->allocs.push_back(q);
+    n->bytes += bytes;
     if (cudaMemsetAsync(q, fill, bytes, n->stream) != cudaSuccess) return BG3_ECUDA;
     *p = (T *)q;
     return BG3_OK;
@@ -402,6 +407,37 @@ fail:
     bg3_destroy(n);
     return rc;
 }
+
+// Device bytes bg3_create allocates for desc, plus an external input's arrays (Poisson 54 B or
+// regular 8 B per neuron); mirrors the allocation list of bg3_create.
+int64_t bg3_net_footprint(const bg3_net_desc *desc)
+{
+    if (!desc || desc->n_neurons <= 0 || desc->max_syn_per_neuron < 0 || desc->delta_t <= 0 ||
+        desc->epoch_duration <= 0)
+        return BG3_EINVAL;
+    const bg3_net_desc &D = *desc;
+    const uint64_t N = (uint64_t)D.n_neurons;
+    const uint64_t Np = (N + 31) / 32 * 32;
+    const uint64_t S = Np * (((uint64_t)D.max_syn_per_neuron + 3) / 4) * 4;
+    const int64_t ms = (int64_t)(D.epoch_duration * (float)D.max_firing_rate);
+    if (ms <= 0) return BG3_EINVAL;
+    const uint64_t nb = (uint64_t)std::max((int)((float)D.max_epochs * D.epoch_duration), 1);
+    const uint64_t ns = (uint64_t)std::max((int)((float)D.max_epochs * D.epoch_duration * 100.0f), 1);
+    const uint64_t E1 = (uint64_t)D.max_epochs + 1;
+    uint64_t b = 8 + 4 + 4 + 8;                                   // step, sweep_done, err, cursor
+    b += N * (9 * 4 + 3 * 4 + 1);                                  // neuron SoA + ntype
+    b += N * BG3_RING * 4 + BG3_RING * 4;                          // spike ring
+    b += S * (4 + 1 + 1 + sizeof(EvSlot) + 4 + 1 + 4) + N * 4;     // planes, outMap, count
+    b += BG3_MAX_DCLS * 4 + BG3_MAX_DELAYS * 4 + 3 * N * BG3_MAX_DELAYS * 4;
+    b += 4 * N * 4 + ((uint64_t)ms + 1) * 4;                       // growth arrays, grow_exp
+    b += (nb + ns) * 4 + 2 * E1 * N * 4;                           // recorder
+    if (D.neuron_kind == BG3_NEURON_IZH) b += 6 * N * 4;
+    b += N * (uint64_t)ms * 8;                                     // spike history
+    b += sizeof(NetDev) + 54 * N;                                  // descriptor, input
+    return (int64_t)b;
+}
+
+uint64_t bg3_net_bytes(bg3_net *n) { return n ? n->bytes + sizeof(NetDev) : 0; }
 
 int bg3_destroy(bg3_net *n)
 {
@@ -840,7 +876,7 @@ static int run_steps(bg3_net *n, int64_t nsteps)
             bg3::launch_deliver(h, n->stream);
             bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->stream);
         }
-        n->launches += 3 * nsteps;
+        n->launches += (1 + step_kernels(h.syn_kind)) * nsteps;
         CK(cudaGetLastError());
         return BG3_OK;
     }
@@ -868,7 +904,7 @@ static int run_steps(bg3_net *n, int64_t nsteps)
     }
     bg3::launch_deliver(h, n->stream);
     bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->stream);
-    n->launches += 1 + 2 * nsteps;
+    n->launches += 1 + step_kernels(h.syn_kind) * nsteps;
     CK(cudaGetLastError());
     return BG3_OK;
 }
@@ -1389,7 +1425,7 @@ int bg3_batch_step(bg3_batch *b, int64_t nsteps)
     batch_interior(b, interior);
     bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
     bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, false, b->stream);
-    b->launches += 1 + 2 * nsteps;
+    b->launches += 1 + step_kernels(b->syn_kind) * nsteps;
     CK(cudaGetLastError());
     return batch_order(b, false);
 }
@@ -1456,7 +1492,7 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
         bg3::launch_sweep(h, n->tm_psr, n->tm_cls, !inject && !last, n->stream);
         CK(cudaEventRecord(e[2], n->stream));
     }
-    n->launches += (inject ? 3 : 2) * nsteps + (inject ? 0 : 1);
+    n->launches += (step_kernels(h.syn_kind) + (inject ? 1 : 0)) * nsteps + (inject ? 0 : 1);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(n->stream));
     for (int64_t s = 0; s < nsteps; s++) {
@@ -1505,7 +1541,7 @@ int bg3_batch_bench_steps(bg3_batch *b, int64_t nsteps, int64_t flush_bytes, flo
         bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, s < nsteps - 1, b->stream);
         CK(cudaEventRecord(ev[2 * s + 1], b->stream));
     }
-    b->launches += 1 + 2 * nsteps;
+    b->launches += 1 + step_kernels(b->syn_kind) * nsteps;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(b->stream));
     for (int64_t s = 0; s < nsteps; s++) CK(cudaEventElapsedTime(&step_ms[s], ev[2 * s], ev[2 * s + 1]));

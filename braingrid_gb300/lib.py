@@ -132,6 +132,8 @@ def load(build_if_missing=True):
         "bg3_set_stdp_constants": ([vp, ctypes.POINTER(StdpConstants)], ctypes.c_int),
         "bg3_set_stdp_arithmetic": ([vp, ctypes.c_int], ctypes.c_int),
         "bg3_epoch_record": ([vp], ctypes.c_int),
+        "bg3_net_footprint": ([ctypes.POINTER(NetDesc)], ctypes.c_int64),
+        "bg3_net_bytes": ([vp], ctypes.c_uint64),
         "bg3_upload_layout": ([vp, c_f32p, c_f32p, c_i32p], ctypes.c_int),
         "bg3_upload_synapses": ([vp, ctypes.POINTER(SynArrays), ctypes.c_uint64], ctypes.c_int),
         "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
@@ -218,6 +220,14 @@ SYN_FIELDS = [("in_use", np.uint8), ("src", np.int32), ("type", np.int32),
               ("F", np.float32), ("u", np.float32), ("r", np.float32), ("lastSpike", np.uint64)]
 
 
+def footprint(desc):
+    """Device bytes a network of this NetDesc holds (bg3_net_footprint; no GPU needed)."""
+    v = int(load().bg3_net_footprint(ctypes.byref(desc)))
+    if v < 0:
+        check(v, "bg3_net_footprint")
+    return v
+
+
 class Network:
     """One network on the GPU, driven through the C-ABI."""
 
@@ -235,10 +245,26 @@ class Network:
         h = ctypes.c_void_p()
         check(self.L.bg3_create(ctypes.byref(self.desc), ctypes.byref(h)), "bg3_create")
         self.h = h
+        self._owned = True
+
+    @classmethod
+    def borrow(cls, handle, desc):
+        """Wraps a bg3_net* created elsewhere (e.g. by the job server); close() leaves it."""
+        self = cls.__new__(cls)
+        self.L = load()
+        self.desc = desc
+        self.N, self.max_syn = desc.n_neurons, desc.max_syn_per_neuron
+        self.max_spikes = int(np.float32(desc.epoch_duration) * np.float32(desc.max_firing_rate))
+        self.max_epochs = desc.max_epochs
+        self.epoch_duration = desc.epoch_duration
+        self.h = ctypes.c_void_p(handle)
+        self._owned = False
+        return self
 
     def close(self):
         if getattr(self, "h", None):
-            self.L.bg3_destroy(self.h)
+            if getattr(self, "_owned", True):
+                self.L.bg3_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -376,6 +402,10 @@ class Network:
 
     def growth(self, epoch):
         check(self.L.bg3_epoch_growth(self.h, int(epoch)), "bg3_epoch_growth")
+
+    @property
+    def device_bytes(self):
+        return int(self.L.bg3_net_bytes(self.h))
 
     def record(self):
         """Epoch end of a network without growth (recorder histograms, spike-count roll)."""

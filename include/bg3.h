@@ -162,6 +162,11 @@ typedef struct {
 int bg3_create(const bg3_net_desc *desc, bg3_net **out);
 /* Replaces GPUSpikingModel::cleanupSim / delete*DeviceStruct (Core/GPUSpikingModel.cu:82-99). */
 int bg3_destroy(bg3_net *net);
+/* Device bytes a network of this shape holds (bg3_create plus an external input); no GPU work.
+ * Negative status for an invalid desc.  No counterpart in the reference (admission control). */
+int64_t bg3_net_footprint(const bg3_net_desc *desc);
+/* Device bytes this network has allocated so far. */
+uint64_t bg3_net_bytes(bg3_net *net);
 
 /* ---- host -> device ------------------------------------------------------------------- */
 /* IAllNeurons::copyNeuronHostToDevice (Neurons/IAllNeurons.h:114). */

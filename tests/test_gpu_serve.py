@@ -1,0 +1,111 @@
+"""Served form (bg3_serve_*): continuous batching must not change any job's results.
+
+Each job's arithmetic is independent of the others (its own noise seed, its own step counter),
+and the batched kernels are bit-exact with the single-network ones, so a job's recorder
+histories and final state are identical whether it runs alone, in a mix that joins and leaves
+around it, or through the plain single-network API."""
+import numpy as np
+import pytest
+
+from braingrid_gb300 import lib as bg
+from braingrid_gb300 import serve
+from tests.netcases import assert_same
+
+pytestmark = pytest.mark.gpu
+
+T = 0.2  # epoch duration of the test jobs (2000 steps)
+
+
+def make_jobs():
+    return [serve.lif_growth_job(12, 2, seed=1, radius=2.0, epoch_duration=T),
+            serve.izh_static_job(20, 15, 2, seed=2, epoch_duration=T),
+            serve.lif_growth_job(20, 3, seed=3, radius=2.5, epoch_duration=T),
+            serve.izh_static_job(10, 10, 1, seed=4, epoch_duration=T),
+            serve.lif_growth_job(16, 1, seed=5, radius=1.6, epoch_duration=T)]
+
+
+def run_alone(job):
+    srv = serve.Server(max_resident=1, chunk_steps=700)
+    srv.submit(job)
+    done = srv.run_all()
+    srv.close()
+    assert done[0] is job and job.result.status == 0, job.error
+    return job.outputs()
+
+
+def check_same(a, b, name):
+    for k in a:
+        assert_same("%s %s" % (name, k), b[k], a[k])
+
+
+def test_served_results_identical_alone_and_in_mix():
+    alone = [run_alone(j) for j in make_jobs()]
+    jobs = make_jobs()
+    srv = serve.Server(max_resident=3, chunk_steps=300)
+    for j in jobs[:2]:
+        srv.submit(j)
+    srv.pump()
+    srv.pump()
+    st = srv.stats()
+    assert st["resident"] == 2 and st["rounds"] >= 1
+    for j in jobs[2:]:          # arrive while the first two are on the GPU
+        srv.submit(j)
+    done = srv.run_all()
+    st = srv.stats()
+    srv.close()
+    assert len(done) == len(jobs) and st["done"] == len(jobs) and st["failed"] == 0
+    assert st["peak_resident"] == 3
+    for j, a in zip(jobs, alone):
+        assert j.result.status == 0 and j.result.error_word == 0, (j.name, j.error)
+        assert j.result.synapse_steps > 0 or j.growth
+        check_same(a, j.outputs(), j.name)
+    assert sum(float(j.spikes_hist.sum()) for j in jobs) > 0
+
+
+def test_admission_respects_the_device_budget():
+    jobs = make_jobs()
+    budget = max(j.footprint for j in jobs)
+    srv = serve.Server(hbm_budget_bytes=budget, max_resident=8, chunk_steps=500)
+    for j in jobs:
+        srv.submit(j)
+    done, waited = [], 0
+    while len(done) < len(jobs):
+        srv.pump()
+        done += srv.take()
+        st = srv.stats()
+        assert st["bytes_resident"] <= budget
+        waited = max(waited, st["queued"])
+    srv.close()
+    assert waited > 0 and st["peak_resident"] < len(jobs)
+    assert all(j.result.status == 0 for j in jobs)
+
+
+def test_job_larger_than_budget_is_rejected():
+    j = make_jobs()[0]
+    srv = serve.Server(hbm_budget_bytes=j.footprint - 1, max_resident=4)
+    with pytest.raises(RuntimeError):
+        srv.submit(j)
+    srv.close()
+
+
+def test_served_job_matches_plain_network():
+    """The served job against the same network stepped epoch by epoch with bg3_step."""
+    job = serve.lif_growth_job(20, 3, seed=3, radius=2.5, epoch_duration=T)
+    served = run_alone(job)
+    ref = serve.lif_growth_job(20, 3, seed=3, radius=2.5, epoch_duration=T)
+    d = ref.desc
+    net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height, d.epoch_duration,
+                     d.delta_t, d.max_firing_rate, d.max_epochs, d.synapse_kind, d.noise_mode,
+                     d.noise_seed, neuron_kind=d.neuron_kind)
+    ref.setup(net)
+    assert net.device_bytes <= ref.footprint
+    spe = int(np.float32(d.epoch_duration) / np.float32(d.delta_t))
+    for e in range(ref.epochs):
+        net.step(spe)
+        net.growth(e + 1)
+    b, s, rh, ra = net.download_histories()
+    plain = dict(burstiness=b, spikes_hist=s, rates_hist=rh, radii_hist=ra,
+                 Vm=net.download_lif(fields=("Vm",))["Vm"])
+    for k in served:
+        assert_same("plain vs served " + k, served[k][:len(plain[k])], plain[k])
+    assert net.error_word == 0
