@@ -323,6 +323,141 @@ def run_batched(steps, warmup):
     return out
 
 
+def run_c3(steps, warmup):
+    """config[3]: 512 Izhikevich + dynamic STDP networks (static wiring, Poisson drive) advanced
+    as one batch against the same networks run one at a time with bg3_step."""
+    import time as _t
+    from braingrid_gb300 import lib as bg
+    from braingrid_gb300 import workloads
+    t0 = _t.perf_counter()
+    nets = workloads.build_c3()
+    t_build = _t.perf_counter() - t0
+    S = sum(n.total_synapses() for n in nets)
+    N = sum(n.N for n in nets)
+    batch = bg.Batch(nets)
+    batch.step(warmup)
+    batch.sync()
+    ms = batch.bench_steps(steps)
+    t_batch = float(np.sum(ms)) / 1e3
+    for n in nets:
+        n.step(warmup)
+    for n in nets:
+        n.sync()
+    t0 = _t.perf_counter()
+    for n in nets:
+        n.step(steps)
+    for n in nets:
+        n.sync()
+    t_plain = _t.perf_counter() - t0
+    spikes = sum(int(n.download_lif(fields=("spikeCount",))["spikeCount"].sum()) for n in nets)
+    err = max(n.error_word for n in nets)
+    out = {"workload": "config[3]: %d Izhikevich + dynamic STDP networks, N ~ U[500, 8000] "
+                       "(grids), static wiring 10 nearest within radius 5 + 10%% rewired, "
+                       "Poisson 10 Hz x 5 nA" % len(nets),
+           "networks": len(nets), "neurons": N, "synapses": S, "steps": steps,
+           "build_s": t_build,
+           "batched_synapse_updates_per_s": S * steps / t_batch,
+           "batched_neuron_steps_per_s": N * steps / t_batch,
+           "batched_ms_per_step": t_batch * 1e3 / steps,
+           "plain_synapse_updates_per_s": S * steps / t_plain,
+           "plain_neuron_steps_per_s": N * steps / t_plain,
+           "plain_ms_per_step": t_plain * 1e3 / steps,
+           "plain_timing": "host wall clock around %d sequential bg3_step runs" % len(nets),
+           "batched_over_plain": t_plain / t_batch,
+           "mean_rate_hz": spikes / float(N) / ((steps + 2 * warmup) * 1e-4),
+           "error_word": int(err)}
+    batch.close()
+    for n in nets:
+        n.close()
+    return out
+
+
+def run_served(n_jobs, chunk_steps=2000):
+    """config[4]: a seeded open-loop Poisson trace (20 jobs/s) through the job server
+    (continuous batching, footprint admission, 150 GB budget), then the same jobs one at a
+    time through the plain API.  Latency = completion - arrival, host wall clock."""
+    import time as _t
+    from braingrid_gb300 import lib as bg
+    from braingrid_gb300 import serve, workloads
+    trace = workloads.c4_trace(n_jobs)
+    srv = serve.Server(hbm_budget_bytes=workloads.C4_BUDGET, max_resident=64,
+                       chunk_steps=chunk_steps)
+    pending = list(trace)
+    arrival = {}
+    lat, finish = {}, {}
+    t0 = _t.perf_counter()
+    while pending or srv.jobs:
+        now = _t.perf_counter() - t0
+        while pending and pending[0][0] <= now:
+            a, job = pending.pop(0)
+            srv.submit(job)
+            arrival[job.id] = a
+        if not srv.jobs:
+            _t.sleep(max(0.0, pending[0][0] - (_t.perf_counter() - t0)))
+            continue
+        srv.pump()
+        now = _t.perf_counter() - t0
+        for job in srv.take():
+            lat[job.id] = now - arrival[job.id]
+            finish[job.id] = now
+    st = srv.stats()
+    srv.close()
+    jobs = [j for _, j in trace]
+    ok = all(j.result.status == 0 for j in jobs)
+    syn_steps = sum(int(j.result.synapse_steps) for j in jobs)
+    span = max(finish.values()) - trace[0][0]
+    L = np.array([lat[j.id] for j in jobs])
+    # plain: the same jobs, one at a time, each on its own network with bg3_step + epoch passes
+    durations, setups = [], []
+    for _, job in workloads.c4_trace(n_jobs):
+        d = job.desc
+        t1 = _t.perf_counter()
+        net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height, d.epoch_duration,
+                         d.delta_t, d.max_firing_rate, d.max_epochs, d.synapse_kind,
+                         d.noise_mode, d.noise_seed, neuron_kind=d.neuron_kind)
+        job.setup(net)
+        net.sync()
+        setups.append(_t.perf_counter() - t1)
+        spe = int(np.float32(d.epoch_duration) / np.float32(d.delta_t))
+        for e in range(job.epochs):
+            net.step(spe)
+            if job.growth:
+                net.growth(e + 1)
+            else:
+                net.record()
+        net.download_histories()
+        net.close()
+        durations.append(_t.perf_counter() - t1)
+    t_free, plat = 0.0, []
+    for (a, _), dur in zip(trace, durations):
+        start = max(a, t_free)
+        t_free = start + dur
+        plat.append(t_free - a)
+    plat = np.array(plat)
+    pct = lambda x, q: float(np.percentile(x, q))
+    return {"workload": "config[4]: %d-job seeded Poisson trace at 20 jobs/s from the config[1]-[3] "
+                        "families (LIF sides U[10,200] pre-grown, Izhikevich N U[500,8000]), 1-20 "
+                        "epochs of 1 s, 150 GB admission budget" % n_jobs,
+            "jobs": n_jobs, "all_ok": ok, "synapse_steps": syn_steps,
+            "served_p50_s": pct(L, 50), "served_p95_s": pct(L, 95), "served_p99_s": pct(L, 99),
+            "served_makespan_s": span, "served_synapse_updates_per_s": syn_steps / span,
+            "peak_resident": int(st["peak_resident"]), "rounds": int(st["rounds"]),
+            "server_host_s": {k: round(float(st[k]), 3) for k in ("admit_s", "wait_s", "epoch_s",
+                                                                   "rebuild_s")},
+            "per_job": [{"name": j.name, "neurons": int(j.desc.n_neurons), "epochs": int(j.epochs),
+                         "synapse_steps": int(j.result.synapse_steps),
+                         "served_latency_s": round(float(lat[j.id]), 3),
+                         "plain_duration_s": round(float(dur), 3),
+                         "plain_setup_s": round(float(su), 3)}
+                        for j, dur, su in zip(jobs, durations, setups)],
+            "plain_p50_s": pct(plat, 50), "plain_p95_s": pct(plat, 95),
+            "plain_p99_s": pct(plat, 99), "plain_makespan_s": float(t_free - trace[0][0]),
+            "plain_synapse_updates_per_s": syn_steps / float(t_free - trace[0][0]),
+            "plain_timing": "jobs run back to back (each with its own setup); latencies from the "
+                            "measured durations and the same arrival times",
+            "served_over_plain_throughput": float(t_free - trace[0][0]) / span}
+
+
 def run_reference(args):
     """The reference algorithm's CPU path (oracle C port), single-threaded like the reference."""
     rank, world, _ = dist_env()
@@ -377,9 +512,19 @@ def main():
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="bg3", choices=["bg3", "reference"])
+    ap.add_argument("--serve-jobs", type=int, default=8,
+                    help="jobs of the served-stream trace (config[4])")
+    ap.add_argument("--only", choices=["c3", "serve"], default=None,
+                    help="run one secondary workload alone and print its JSON")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.only == "c3":
+        print(json.dumps(run_c3(min(args.steps, 1000), max(args.warmup, 20))), flush=True)
+        return
+    if args.only == "serve":
+        print(json.dumps(run_served(args.serve_jobs)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -23,8 +23,9 @@ void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
                   cudaStream_t s);
 void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s);
 void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s);
-void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int ntiles,
-                        bool fuse, cudaStream_t s);
+void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int n_thick,
+                        int n_thin, bool fuse, cudaStream_t s);
+bool sweep_is_thin(const NetDev &h);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s);
@@ -1274,7 +1275,7 @@ struct bg3_batch {
     NetDev *d_nets = nullptr;
     CUtensorMap *d_maps = nullptr;
     int2 *d_tiles = nullptr;
-    int ntiles = 0, max_n = 0, syn_kind = 1;
+    int ntiles = 0, n_thick = 0, max_n = 0, syn_kind = 1;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev = nullptr;
@@ -1301,10 +1302,15 @@ static int batch_refresh(bg3_batch *b)
             tiles.push_back(std::make_pair((int)m, make_int2((int)k, t)));
         }
     }
+    // TMA-swept tiles first, heaviest first; then the tiles of thin networks (one warp each)
     std::stable_sort(tiles.begin(), tiles.end(),
                      [](const std::pair<int, int2> &a, const std::pair<int, int2> &c) { return a.first > c.first; });
     std::vector<int2> tl;
-    for (auto &t : tiles) tl.push_back(t.second);
+    for (auto &t : tiles)
+        if (!bg3::sweep_is_thin(b->nets[t.second.x]->h)) tl.push_back(t.second);
+    b->n_thick = (int)tl.size();
+    for (auto &t : tiles)
+        if (bg3::sweep_is_thin(b->nets[t.second.x]->h)) tl.push_back(t.second);
     if ((int)tl.size() != b->ntiles) {
         if (b->d_tiles) cudaFree(b->d_tiles);
         b->d_tiles = nullptr;
@@ -1396,7 +1402,7 @@ static void batch_interior(bg3_batch *b, int64_t n)
 {
     for (int64_t i = 0; i < n; i++) {
         bg3::launch_deliver_batch(b->syn_kind, b->d_nets, (int)b->nets.size(), b->stream);
-        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, true, b->stream);
+        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, true, b->stream);
     }
 }
 
@@ -1424,8 +1430,9 @@ int bg3_batch_step(bg3_batch *b, int64_t nsteps)
     }
     batch_interior(b, interior);
     bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
-    bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, false, b->stream);
-    b->launches += 1 + step_kernels(b->syn_kind) * nsteps;
+    bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, false, b->stream);
+    const int sweeps = (b->n_thick > 0) + (b->ntiles > b->n_thick);
+    b->launches += 1 + (step_kernels(b->syn_kind) - 1 + sweeps) * nsteps;
     CK(cudaGetLastError());
     return batch_order(b, false);
 }
@@ -1538,10 +1545,11 @@ int bg3_batch_bench_steps(bg3_batch *b, int64_t nsteps, int64_t flush_bytes, flo
         }
         CK(cudaEventRecord(ev[2 * s], b->stream));
         bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
-        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->ntiles, s < nsteps - 1, b->stream);
+        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, s < nsteps - 1, b->stream);
         CK(cudaEventRecord(ev[2 * s + 1], b->stream));
     }
-    b->launches += 1 + step_kernels(b->syn_kind) * nsteps;
+    const int sweeps = (b->n_thick > 0) + (b->ntiles > b->n_thick);
+    b->launches += 1 + (step_kernels(b->syn_kind) - 1 + sweeps) * nsteps;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(b->stream));
     for (int64_t s = 0; s < nsteps; s++) CK(cudaEventElapsedTime(&step_ms[s], ev[2 * s], ev[2 * s + 1]));

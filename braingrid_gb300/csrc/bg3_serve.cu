@@ -2,6 +2,7 @@
 // batching of the resident jobs through the batched step (bg3_batch_*), per-job epoch ends.
 // Host code only; it drives the GPU through the public C-ABI.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <deque>
 #include <new>
@@ -26,6 +27,11 @@ struct Job {
 };
 
 const int KINDS = 4;  // one batch group per synapse kind
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 }  // namespace
 
@@ -180,7 +186,10 @@ int bg3_serve_submit(bg3_server *s, const bg3_job_desc *job, int64_t *job_id)
 int bg3_serve_pump(bg3_server *s)
 {
     if (!s) return BG3_EINVAL;
+    double t0 = now_s();
     int rc = rebuild_groups(s);
+    double t1 = now_s();
+    s->st.rebuild_s += t1 - t0;
     if (rc) return rc;
     // 1. launch one chunk for the resident jobs
     int64_t chunk = 0;
@@ -192,10 +201,15 @@ int bg3_serve_pump(bg3_server *s)
         s->st.rounds++;
     }
     // 2. admit arrivals while the chunk runs
+    t0 = now_s();
     admit(s);
+    t1 = now_s();
+    s->st.admit_s += t1 - t0;
     // 3. wait for the chunk, then epoch ends and completions
     for (int k = 0; k < KINDS; k++)
         if (s->group[k] && (rc = bg3_batch_sync(s->group[k]))) return rc;
+    t0 = now_s();
+    s->st.wait_s += t0 - t1;
     std::vector<Job *> keep;
     for (Job *j : s->resident) {
         const int64_t ss = j->syn * chunk, ns = (int64_t)j->d.desc.n_neurons * chunk;
@@ -233,6 +247,7 @@ int bg3_serve_pump(bg3_server *s)
         keep.push_back(j);
     }
     s->resident.swap(keep);
+    s->st.epoch_s += now_s() - t0;
     for (Job *j : s->joining) {
         s->resident.push_back(j);
         s->dirty[j->d.desc.synapse_kind] = true;

@@ -316,29 +316,141 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
     n.psr[p] = ps;
 }
 
-// One warp per (delay class, spiking neuron) pair; lanes walk that neuron's outgoing synapses
-// of the class.  Each synapse has one source, which fires at most once per step, so no two
-// lanes touch one slot.  One thread also clears ring slot t + 1 for the next neuron pass.
+// Spike arrivals of one step.  The work items are (delay class c, neuron that fired at t - D_c)
+// pairs; each item's outgoing synapses of the class are cut into chunks of DLV_CHUNK that one warp
+// delivers, four per lane with their loads issued together.  A block takes up to DLV_GROUP items
+// at a time (fewer when the step has few spikes, so that they spread over the blocks), scans their
+// chunk counts and lets its warps take the chunks in turn; so a burst of high-fan-out neurons
+// keeps every warp of the grid busy instead of one warp per neuron walking its synapses 32 at a
+// time.  Each synapse has one source, which fires at most once per step, so no two lanes touch
+// one slot.  Block 0 also clears ring slot t + 1 for the next neuron pass.
+constexpr int DLV_CHUNK = 128;
+constexpr int DLV_GROUP = 32;
+
 template <int SYN>
-__device__ __forceinline__ void deliver_net(const NetDev &n, int gw, int nw, bool clear_next)
+__device__ __forceinline__ void deliver_chunk(const NetDev &n, uint32_t b, uint32_t k,
+                                              uint32_t base, uint32_t tf, unsigned long long t64,
+                                              int src, int lane)
 {
-    const unsigned long long t = *n.step;
-    if (clear_next) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
-    const int lane = threadIdx.x & 31;
-    for (int c = 0; c < n.n_delays; c++) {
-        const int D = n.ltab[c];
-        if (D <= 0 || (unsigned long long)D > t) continue;
-        const unsigned long long tf = t - (unsigned long long)D;
-        const int slot = (int)(tf & (BG3_RING - 1));
-        const int m = min(n.ring_n[slot], n.N);
-        const int32_t *ids = n.ring + (size_t)slot * n.N;
-        const uint32_t *beg = n.outBegin + (size_t)c * n.N, *cnt = n.outCount + (size_t)c * n.N;
-        for (int s = gw; s < m; s += nw) {
-            const int i = ids[s];
-            const uint32_t b = beg[i], k = cnt[i];
-            for (uint32_t j = lane; j < k; j += 32)
-                deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, t, i);
+    if (SYN >= 2) {  // STDP: the pre-spike walks go one synapse at a time
+        const uint32_t end = min(k, base + (uint32_t)DLV_CHUNK);
+        for (uint32_t j = base + lane; j < end; j += 32) deliver_hit<SYN>(n, n.outMap[b + j], tf, t64, src);
+        return;
+    }
+    const uint32_t t = (uint32_t)t64;
+    uint32_t p[4];
+    bool ok[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const uint32_t j = base + (uint32_t)lane + 32u * u;
+        ok[u] = j < k;
+        p[u] = ok[u] ? n.outMap[b + j] : 0u;
+    }
+    EvSlot e[4];
+    float ps[4], dec[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        if (ok[u]) {
+            e[u] = n.ev[p[u]];
+            ps[u] = n.psr[p[u]];
+            dec[u] = n.dtab[n.dcls[p[u]]];
         }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) ok[u] = ok[u] && (int32_t)(tf - e[u].born) >= 0;
+    float xr[4], xu[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        if (SYN == 1 && ok[u] && e[u].last != BG3_NO_SPIKE32) {
+            const uint32_t ki = t - e[u].last;
+            xr[u] = exp_steps(n, ki, e[u].D);
+            xu[u] = exp_steps(n, ki, e[u].F);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        if (!ok[u]) continue;
+        float q = ps[u];
+        if (SYN == 1) {
+            float uu = e[u].u, r = e[u].r;
+            if (e[u].last != BG3_NO_SPIKE32) {
+                r = 1.0f + (r * (1.0f - uu) - 1.0f) * xr[u];
+                uu = e[u].U + uu * (1.0f - e[u].U) * xu[u];
+            }
+            q = q + ((e[u].W / dec[u]) * uu * r);
+            EvSlot *w = &n.ev[p[u]];
+            w->u = uu;
+            w->r = r;
+            w->last = t;
+        } else {
+            q = q + e[u].W / dec[u];
+        }
+        n.psr[p[u]] = q;
+    }
+}
+
+template <int SYN>
+__device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb)
+{
+    __shared__ uint32_t s_pref[DLV_GROUP], s_beg[DLV_GROUP], s_cnt[DLV_GROUP], s_tf[DLV_GROUP];
+    __shared__ int32_t s_src[DLV_GROUP];
+    __shared__ int s_moff[BG3_MAX_DELAYS + 1];
+    const unsigned long long t = *n.step;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (bid == 0 && threadIdx.x == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
+    if (threadIdx.x == 0) {
+        int off = 0;
+        for (int c = 0; c < n.n_delays; c++) {
+            s_moff[c] = off;
+            const int D = n.ltab[c];
+            if (D > 0 && (unsigned long long)D <= t)
+                off += min(n.ring_n[(t - (unsigned long long)D) & (BG3_RING - 1)], n.N);
+        }
+        s_moff[n.n_delays] = off;
+    }
+    __syncthreads();
+    const int M = s_moff[n.n_delays];
+    const int G = max(1, min(DLV_GROUP, (M + nb - 1) / nb));
+    for (int g0 = bid * G; g0 < M; g0 += nb * G) {
+        const int items = min(G, M - g0);
+        if (warp == 0) {
+            uint32_t chunks = 0;
+            if (lane < items) {
+                const int idx = g0 + lane;
+                int c = 0;
+                while (idx >= s_moff[c + 1]) c++;
+                const unsigned long long tf = t - (unsigned long long)n.ltab[c];
+                const int slot = (int)(tf & (BG3_RING - 1));
+                const int i = n.ring[(size_t)slot * n.N + (idx - s_moff[c])];
+                const size_t ci = (size_t)c * n.N + i;
+                const uint32_t k = n.outCount[ci];
+                s_beg[lane] = n.outBegin[ci];
+                s_cnt[lane] = k;
+                s_src[lane] = i;
+                s_tf[lane] = (uint32_t)tf;
+                chunks = (k + DLV_CHUNK - 1) / DLV_CHUNK;
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, chunks, o);
+                if (lane >= o) chunks += v;
+            }
+            s_pref[lane] = chunks;
+        }
+        __syncthreads();
+        const uint32_t total = s_pref[31];
+        for (uint32_t ch = warp; ch < total; ch += nwarps) {
+            int lo = 0, hi = items - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s_pref[mid] > ch) hi = mid;
+                else lo = mid + 1;
+            }
+            const uint32_t first = lo ? s_pref[lo - 1] : 0u;
+            deliver_chunk<SYN>(n, s_beg[lo], s_cnt[lo], (ch - first) * DLV_CHUNK, s_tf[lo], t,
+                               s_src[lo], lane);
+        }
+        __syncthreads();
     }
 }
 
@@ -347,21 +459,16 @@ __global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev 
 {
     pdl_wait();  // the previous sweep (step counter, spike ring, psr) must be complete
     pdl_trigger();
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    deliver_net<SYN>(n, gw, nw, blockIdx.x == 0 && threadIdx.x == 0);
+    deliver_net<SYN>(n, blockIdx.x, gridDim.x);
 }
 
-// Batched form: grid.y indexes the network, so the networks' (short, latency-bound) delivery
-// passes run side by side.
+// Batched form: grid.y indexes the network, so the networks' delivery passes run side by side.
 template <int SYN>
 __global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets)
 {
     pdl_wait();
     pdl_trigger();
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    deliver_net<SYN>(nets[blockIdx.y], gw, nw, blockIdx.x == 0 && threadIdx.x == 0);
+    deliver_net<SYN>(nets[blockIdx.y], blockIdx.x, gridDim.x);
 }
 
 // The fPost branch (AllSTDPSynapses.cpp:368-418) for every in-use synapse onto a neuron that
@@ -449,6 +556,37 @@ constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4
 // a sum that started at +0.0f unchanged, so the sum warp adds all 64 rows of every chunk.  The
 // prologue overlaps the previous kernel's tail; the step's data is touched after pdl_wait().
 // Every mbarrier wait is bounded (about 1 s); on expiry the error word is set and the CTA drains.
+// Tile epilogue: the sums go to the summation points or, with FUSE, straight into the neuron
+// update of step t + 1 (device noise); the network's last tile advances its step counter.
+template <bool FUSE>
+__device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid, float acc,
+                                             unsigned long long t, int lane)
+{
+    if (FUSE) {
+        const unsigned long long t1 = t + 1;
+        bool fired = false;
+        if (valid) {
+            int br = lif_branch(n, d);
+            float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t1, d) : 0.0f;
+            fired = lif_apply(n, d, br, input_apply(n, d, t1, acc), noise, t1);
+            n.sp[d] = 0.0f;
+        }
+        ring_push(n, t1, fired, d);
+    } else if (valid) {
+        n.sp[d] = acc;
+    }
+    if (lane == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(n.sweep_done, 1u);
+        if (prev == (unsigned)n.ntiles - 1) {
+            *n.step = t + 1;
+            *n.sweep_done = 0;
+            if (t + 1 >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
+            __threadfence();
+        }
+    }
+}
+
 template <bool FUSE>
 __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *tm_psr,
                                            const CUtensorMap *tm_cls, const int tile,
@@ -578,30 +716,56 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         __syncwarp();
     }
 
-    if (FUSE) {
-        const unsigned long long t1 = t + 1;
-        bool fired = false;
-        if (valid) {
-            int br = lif_branch(n, d);
-            float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t1, d) : 0.0f;
-            fired = lif_apply(n, d, br, input_apply(n, d, t1, acc), noise, t1);
-            n.sp[d] = 0.0f;
+    sweep_finish<FUSE>(n, d, valid, acc, t, lane);
+}
+
+// Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
+// of a tile is 512 contiguous bytes of the plane (and 128 of the class plane), so the warp reads
+// it with one coalesced 16-byte load per lane, scales it, writes it back and adds it in row
+// order; the same epilogue as sweep_tile.  Lanes past N sit in the plane padding (Np), whose
+// slots stay +0.0f.  For these networks a TMA pipeline per 32 dests would spend most of its time
+// in set-up.
+template <bool FUSE>
+__device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
+{
+    const int lane = threadIdx.x & 31;
+    const int d = tile * SW_DESTS + lane;
+    const bool valid = d < n.N;
+    const int cnt = valid ? (int)n.count[d] : 0;
+    const int nq = (__reduce_max_sync(0xffffffffu, cnt) + 3) >> 2;
+    pdl_wait();  // spike delivery for this step has finished writing psr
+    pdl_trigger();
+    const unsigned long long t = *n.step;
+    float4 *P = reinterpret_cast<float4 *>(n.psr);
+    const uint32_t *C = reinterpret_cast<const uint32_t *>(n.dcls);
+    const size_t Np = (size_t)n.Np;
+    float acc = 0.0f;
+    for (int q = 0; q < nq; q += 4) {
+        float4 v[4];
+        uint32_t c[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (q + j < nq) {
+                v[j] = P[(size_t)(q + j) * Np + d];
+                c[j] = C[(size_t)(q + j) * Np + d];
+            }
         }
-        ring_push(n, t1, fired, d);
-    } else if (valid) {
-        n.sp[d] = acc;
-    }
-    // the network's last tile to finish advances its step counter
-    if (lane == 0) {
-        __threadfence();
-        unsigned prev = atomicAdd(n.sweep_done, 1u);
-        if (prev == (unsigned)n.ntiles - 1) {
-            *n.step = t + 1;
-            *n.sweep_done = 0;
-            if (t + 1 >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
-            __threadfence();
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (q + j < nq) {
+                v[j].x = v[j].x * __ldg(&n.dtab[c[j] & 0xffu]);
+                v[j].y = v[j].y * __ldg(&n.dtab[(c[j] >> 8) & 0xffu]);
+                v[j].z = v[j].z * __ldg(&n.dtab[(c[j] >> 16) & 0xffu]);
+                v[j].w = v[j].w * __ldg(&n.dtab[c[j] >> 24]);
+                P[(size_t)(q + j) * Np + d] = v[j];
+                acc = acc + v[j].x;
+                acc = acc + v[j].y;
+                acc = acc + v[j].z;
+                acc = acc + v[j].w;
+            }
         }
     }
+    sweep_finish<FUSE>(n, d, valid, acc, t, lane);
 }
 
 template <int SYN, bool FUSE>
@@ -625,8 +789,32 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_batch(const NetDev *nets,
     sweep_tile<FUSE>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
 }
 
+constexpr int THIN_QUADS = 16;   // networks with max_syn <= 64 take the thin sweep
+constexpr int THIN_WARPS = 8;
+
+template <bool FUSE>
+__global__ void __launch_bounds__(32 * THIN_WARPS) k_sweep_thin(const __grid_constant__ NetDev n)
+{
+    const int tile = blockIdx.x * THIN_WARPS + (threadIdx.x >> 5);
+    if (tile >= n.ntiles) return;
+    sweep_thin_tile<FUSE>(n, tile);
+}
+
+// Batched thin tiles: tiles[i] = (network, tile), one warp each.
+template <bool FUSE>
+__global__ void __launch_bounds__(32 * THIN_WARPS) k_sweep_thin_batch(const NetDev *nets,
+                                                                      const int2 *tiles, int count)
+{
+    const int i = blockIdx.x * THIN_WARPS + (threadIdx.x >> 5);
+    if (i >= count) return;
+    const int2 tr = tiles[i];
+    sweep_thin_tile<FUSE>(nets[tr.x], tr.y);
+}
+
+bool sweep_is_thin(const NetDev &h) { return h.Mq <= THIN_QUADS; }
+
 // ---- launchers -------------------------------------------------------------------------------
-int deliver_blocks() { return 152; }
+int deliver_blocks() { return 304; }
 
 void launch_neurons(const NetDev &h, cudaStream_t s)
 {
@@ -678,14 +866,17 @@ static void launch_sweep_t(const NetDev &h, const CUtensorMap &tp, const CUtenso
 
 template <bool FUSE>
 static void launch_sweep_batch_t(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles,
-                                 int ntiles, cudaStream_t s)
+                                 int n_thick, int n_thin, cudaStream_t s)
 {
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_sweep_batch<FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
         attr_set = true;
     }
-    launch_pdl(k_sweep_batch<FUSE>, ntiles, SW_THREADS, SW_SMEM, s, nets, maps, tiles);
+    if (n_thick > 0) launch_pdl(k_sweep_batch<FUSE>, n_thick, SW_THREADS, SW_SMEM, s, nets, maps, tiles);
+    if (n_thin > 0)
+        launch_pdl(k_sweep_thin_batch<FUSE>, (n_thin + THIN_WARPS - 1) / THIN_WARPS, 32 * THIN_WARPS,
+                   0, s, nets, (const int2 *)(tiles + n_thick), n_thin);
 }
 
 void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s)
@@ -696,7 +887,7 @@ void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t
 void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s)
 {
     // per network: enough warps for a burst, few enough that the grid stays small
-    const int per_net = std::max(2, std::min(16, 608 / std::max(count, 1)));
+    const int per_net = std::max(2, std::min(32, 608 / std::max(count, 1)));
     const dim3 grid(per_net, count);
     switch (syn_kind) {
     case 1: launch_pdl(k_deliver_batch<1>, grid, 256, 0, s, nets); break;
@@ -707,16 +898,22 @@ void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStrea
     if (syn_kind >= 2) launch_pdl(k_stdp_post_batch, grid, 256, 0, s, nets);
 }
 
-void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int ntiles,
-                        bool fuse, cudaStream_t s)
+void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int n_thick,
+                        int n_thin, bool fuse, cudaStream_t s)
 {
-    if (fuse) launch_sweep_batch_t<true>(nets, maps, tiles, ntiles, s);
-    else launch_sweep_batch_t<false>(nets, maps, tiles, ntiles, s);
+    if (fuse) launch_sweep_batch_t<true>(nets, maps, tiles, n_thick, n_thin, s);
+    else launch_sweep_batch_t<false>(nets, maps, tiles, n_thick, n_thin, s);
 }
 
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
                   cudaStream_t s)
 {
+    if (sweep_is_thin(h)) {
+        const int blocks = (h.ntiles + THIN_WARPS - 1) / THIN_WARPS;
+        if (fuse) launch_pdl(k_sweep_thin<true>, blocks, 32 * THIN_WARPS, 0, s, h);
+        else launch_pdl(k_sweep_thin<false>, blocks, 32 * THIN_WARPS, 0, s, h);
+        return;
+    }
     if (h.syn_kind == 1 || h.syn_kind == 3) {
         if (fuse) launch_sweep_t<1, true>(h, tp, tc, s);
         else launch_sweep_t<1, false>(h, tp, tc, s);

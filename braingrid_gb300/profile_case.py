@@ -1,6 +1,9 @@
 """Run a benchmark workload for a few steps, for profilers (ncu) to capture its kernels.
 
-    python -m braingrid_gb300.profile_case [--workload c1|c2] [--steps 20] [--flush]
+    python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big] [--steps 20] [--flush]
+
+c3 is the 512-network Izhikevich + STDP batch; big is three pre-grown LIF networks of the
+served stream's largest sizes (170x170, 176x176, 180x180) batched together.
 """
 import argparse
 
@@ -11,7 +14,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big"])
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
     if a.workload == "c1":
@@ -21,7 +24,25 @@ def main():
         assert net.error_word == 0
     else:
         from . import lib as bg
-        nets = [workloads.build_member(w)[1] for w in workloads.c2_members()]
+        if a.workload == "c2":
+            nets = [workloads.build_member(w)[1] for w in workloads.c2_members()]
+        elif a.workload == "c3":
+            nets = workloads.build_c3()
+        else:
+            from . import serve
+            nets = []
+            for k, side in enumerate((170, 176, 180)):
+                job = serve.lif_growth_job(side, 1, seed=60 + k)
+                d = job.desc
+                net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height,
+                                 d.epoch_duration, d.delta_t, d.max_firing_rate, d.max_epochs,
+                                 d.synapse_kind, d.noise_mode, d.noise_seed)
+                job.setup(net)
+                net.step(1000)
+                c = net.download_lif(fields=("spikeCount",))["spikeCount"]
+                print("net", side, "synapses", net.total_synapses(), "rate_hz",
+                      float(c.sum()) / c.size / 0.1)
+                nets.append(net)
         batch = bg.Batch(nets)
         batch.bench_steps(a.steps, flush)
         S = sum(n.total_synapses() for n in nets)

@@ -37,7 +37,9 @@ class ServeStats(ctypes.Structure):
     _fields_ = [("queued", ctypes.c_int64), ("resident", ctypes.c_int64), ("done", ctypes.c_int64),
                 ("failed", ctypes.c_int64), ("bytes_resident", ctypes.c_uint64),
                 ("rounds", ctypes.c_int64), ("synapse_steps", ctypes.c_int64),
-                ("neuron_steps", ctypes.c_int64), ("peak_resident", ctypes.c_int64)]
+                ("neuron_steps", ctypes.c_int64), ("peak_resident", ctypes.c_int64),
+                ("admit_s", ctypes.c_double), ("wait_s", ctypes.c_double),
+                ("epoch_s", ctypes.c_double), ("rebuild_s", ctypes.c_double)]
 
 
 _BOUND = False

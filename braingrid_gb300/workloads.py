@@ -1,4 +1,6 @@
 """Benchmark workloads (synthetic networks with the stated configs' shapes and distributions)."""
+import numpy as np
+
 from . import netgen
 
 # config[1]: plain single network, 100x100 LIF + DS + ConnGrowth, max 1000 synapses per neuron.
@@ -44,3 +46,64 @@ def build_member(w):
                                   growth=dict(target_rate=w.get("target_rate", 1.0)))
     netgen.pregrow(net, spec, w["radius"], weight_scale=w["weight_scale"], seed=w["seed"] + 11)
     return spec, net
+
+
+# config[3]: 512 independent Izhikevich + dynamic STDP networks, sizes ~ U[500, 8000] neurons on
+# near-square grids, 20 % inhibitory, static wiring (10 nearest within radius 5, 10 % rewired),
+# weights U[10, 20] nA / U[-40, -20] nA, additive STDP (Apos 0.005, Aneg -0.00525 of the 30 nA
+# bound, tau 20 ms), Poisson drive 10 Hz x 5 nA, dt 0.1 ms.
+C3_NETWORKS = 512
+
+
+def c3_shapes(count=C3_NETWORKS, seed=3):
+    rs = np.random.RandomState(seed)
+    out = []
+    for n in rs.randint(500, 8001, size=count):
+        w = int(round(np.sqrt(n)))
+        out.append((w, max(1, int(round(n / w)))))
+    return out
+
+
+def build_c3(count=C3_NETWORKS, seed=3, max_epochs=10):
+    nets = []
+    for k, (w, h) in enumerate(c3_shapes(count, seed)):
+        nets.append(netgen.make_izh_static(w, h, seed=1000 + k, max_epochs=max_epochs)[1])
+    return nets
+
+
+# config[4]: served stream.  Open-loop Poisson arrivals at 20 jobs/s (seeded trace); each job
+# drawn from the config[1]-[3] families: LIF + DS + ConnGrowth pre-grown like config[1]
+# (side ~ U[10, 200], radius min(8.4, 0.45 side)), the config[2] parameter sweep (targetRate,
+# excitatory fraction), or the config[3] Izhikevich + STDP network (N ~ U[500, 8000]);
+# 1-20 epochs of 1 s; admission against a 150 GB footprint budget.
+C4_RATE = 20.0
+C4_BUDGET = 150 << 30
+
+
+def c4_trace(n_jobs, seed=4, rate=C4_RATE, epoch_duration=1.0):
+    """[(arrival_s, job)] for n_jobs jobs of the served stream."""
+    from . import serve
+    rs = np.random.RandomState(seed)
+    t = 0.0
+    out = []
+    for k in range(n_jobs):
+        t += rs.exponential(1.0 / rate)
+        fam = rs.randint(3)
+        epochs = int(rs.randint(1, 21))
+        js = 50 + k
+        if fam == 0:
+            side = int(rs.randint(10, 201))
+            job = serve.lif_growth_job(side, epochs, seed=js, epoch_duration=epoch_duration)
+        elif fam == 1:
+            side = int(rs.randint(10, 201))
+            tr = float(rs.choice([0.1, 1.0, 1.9]))
+            fe = float(rs.choice([0.80, 0.90, 0.98]))
+            job = serve.lif_growth_job(side, epochs, seed=js, target_rate=tr,
+                                       frac_inh=round(1.0 - fe, 2), epoch_duration=epoch_duration)
+        else:
+            n = int(rs.randint(500, 8001))
+            w = int(round(np.sqrt(n)))
+            job = serve.izh_static_job(w, max(1, int(round(n / w))), epochs, seed=js,
+                                       epoch_duration=epoch_duration)
+        out.append((t, job))
+    return out

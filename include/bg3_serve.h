@@ -69,6 +69,9 @@ typedef struct {
     int64_t rounds;              /* pump rounds that advanced at least one job                 */
     int64_t synapse_steps, neuron_steps;
     int64_t peak_resident;
+    /* host wall-clock seconds spent in: admission (create + setup), waiting for chunks,
+     * epoch passes and completions, batch rebuilds */
+    double admit_s, wait_s, epoch_s, rebuild_s;
 } bg3_serve_stats;
 
 int bg3_serve_create(const bg3_serve_desc *desc, bg3_server **out);

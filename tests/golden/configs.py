@@ -114,7 +114,8 @@ CASES = [
     # ConnStatic: 10 nearest neighbours within radius 5, weights U[10, 20] nA / U[-40, -20] nA
     # (pRewiring 0.1 is read but never applied by the reference); Izhikevich neurons, dynamic
     # STDP and Poisson drive as in the 512-network sweep
-    _case("izh_static", 12, 12, 0.5, 2, 100, max_firing_rate=1000, site_seed=5,
+    # (max 32 synapses per neuron: the thin sweep path)
+    _case("izh_static", 12, 12, 0.5, 2, 32, max_firing_rate=1000, site_seed=5,
           keep_steps_every=50, neuron="izh", synapse=3, stdp=STDP_SOFT,
           stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=None),
           static=dict(n=10, radius=5.0, rewire=0.1, exc=(10e-9, 20e-9), inh=(-40e-9, -20e-9))),

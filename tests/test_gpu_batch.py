@@ -77,18 +77,21 @@ def test_batch_then_member_step_and_growth():
 
 def make_mixed_stdp():
     """An Izhikevich network with Poisson drive and a LIF network (device-build STDP
-    arithmetic), both dynamic STDP, wired by one device growth pass."""
+    arithmetic), both dynamic STDP and wired by one device growth pass, and a statically wired
+    Izhikevich network of at most 32 synapses per neuron (thin sweep tiles in the same batch)."""
     from tests.golden.configs import case
     from tests.gpu_helpers import gpu_from_oracle
     from tests.netcases import oracle_from_case
     nets = []
-    for name, seed, signed in (("izh_dstdp", 3, False), ("c0_dstdp", 5, True)):
+    for name, seed, signed in (("izh_dstdp", 3, False), ("c0_dstdp", 5, True),
+                               ("izh_static", 7, False)):
         c = case(name)
         o = oracle_from_case(c)
         if signed:
             o.stdp_signed(True)
         net = gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_DEVICE, noise_seed=seed)
-        net.growth(1)
+        if not c.get("static"):
+            net.growth(1)
         nets.append(net)
     return nets
 

@@ -193,6 +193,33 @@ def test_large_pregrown_network_bit_exact():
     assert net.error_word == 0
 
 
+def test_high_fanout_bursts_bit_exact():
+    """60x60 network wired at radius 8 (~700 synapses per neuron, unscaled growth weights): the
+    network bursts, so steps carry many spiking sources whose fan-out spans several delivery
+    chunks; 400 steps step-locked."""
+    c = dict(case("c0"), name="burst", width=60, height=60, N=3600, max_syn=1000, tsim=0.1,
+             epochs=1, max_firing_rate=1000, radii=8.0)
+    from tests.golden.configs import site_lists
+    c["inh"], c["starters"] = site_lists(60, 60, 0.10, 60, seed=9)
+    o = oracle_from_case(c)
+    o.growth()
+    o.record_epoch(1)
+    assert o.total > 2000000
+    # start every membrane near threshold so that the network bursts at once
+    rs = np.random.RandomState(5)
+    o.arr("Vm")[:] = rs.uniform(13.0e-3, 15.5e-3, c["N"]).astype(np.float32)
+    net = gpu_from_oracle(o, c, n_noise=c["N"] * 500)
+    for t in range(400):
+        o.step_n(1)
+        net.step(1)
+        if (t + 1) % 25 == 0:
+            compare_neurons(net, o, "step %d" % (t + 1))
+    fired = int(o.arr("spikeCount").sum())
+    assert fired > 20000, fired
+    compare_synapses(net, o, "after 400 steps")
+    assert net.error_word == 0
+
+
 def test_device_noise_mode_runs_and_is_deterministic():
     c = case("c0_grown")
     outs = []
