@@ -45,6 +45,8 @@ METRIC = "synapse-updates/s"
 SWEEP_BYTES_PER_SYN = 9
 SWEEP_BYTES_PER_NEURON = 48
 SURVEY_BYTES_PER_SYN = 28
+# served form: resident work cap, about two and a half of the largest jobs' synapse slots
+SERVE_SLOTS = 100e6
 
 
 def peaks():
@@ -372,7 +374,7 @@ def run_c3(steps, warmup):
     return out
 
 
-def run_served(n_jobs, chunk_steps=2000):
+def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     """config[4]: a seeded open-loop Poisson trace (20 jobs/s) through the job server
     (continuous batching, footprint admission, 150 GB budget), then the same jobs one at a
     time through the plain API.  Latency = completion - arrival, host wall clock."""
@@ -381,7 +383,7 @@ def run_served(n_jobs, chunk_steps=2000):
     from braingrid_gb300 import serve, workloads
     trace = workloads.c4_trace(n_jobs)
     srv = serve.Server(hbm_budget_bytes=workloads.C4_BUDGET, max_resident=64,
-                       chunk_steps=chunk_steps)
+                       chunk_steps=chunk_steps, max_resident_slots=slots_cap)
     pending = list(trace)
     arrival = {}
     lat, finish = {}, {}
@@ -439,6 +441,7 @@ def run_served(n_jobs, chunk_steps=2000):
                         "families (LIF sides U[10,200] pre-grown, Izhikevich N U[500,8000]), 1-20 "
                         "epochs of 1 s, 150 GB admission budget" % n_jobs,
             "jobs": n_jobs, "all_ok": ok, "synapse_steps": syn_steps,
+            "max_resident_slots": int(slots_cap), "chunk_steps": chunk_steps,
             "served_p50_s": pct(L, 50), "served_p95_s": pct(L, 95), "served_p99_s": pct(L, 99),
             "served_makespan_s": span, "served_synapse_updates_per_s": syn_steps / span,
             "peak_resident": int(st["peak_resident"]), "rounds": int(st["rounds"]),
@@ -514,6 +517,8 @@ def main():
     ap.add_argument("--impl", default="bg3", choices=["bg3", "reference"])
     ap.add_argument("--serve-jobs", type=int, default=8,
                     help="jobs of the served-stream trace (config[4])")
+    ap.add_argument("--serve-slots", type=float, default=SERVE_SLOTS,
+                    help="served form: cap on the resident jobs' synapse slots (0 = none)")
     ap.add_argument("--only", choices=["c3", "serve"], default=None,
                     help="run one secondary workload alone and print its JSON")
     args = ap.parse_args()
@@ -523,7 +528,7 @@ def main():
         print(json.dumps(run_c3(min(args.steps, 1000), max(args.warmup, 20))), flush=True)
         return
     if args.only == "serve":
-        print(json.dumps(run_served(args.serve_jobs)), flush=True)
+        print(json.dumps(run_served(args.serve_jobs, int(args.serve_slots))), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -24,6 +24,8 @@ struct Job {
     int64_t to_boundary = 0;  // steps left in the current epoch
     int32_t epoch = 0;        // epochs finished
     int64_t syn = 0;          // current synapse count
+    uint64_t slots = 0;       // n_neurons x max_syn_per_neuron (work estimate)
+    int32_t bypassed = 0;     // times a later job was admitted ahead of it
 };
 
 const int KINDS = 4;  // one batch group per synapse kind
@@ -42,7 +44,7 @@ struct bg3_server {
     std::vector<int64_t> finished;
     bg3_batch *group[KINDS] = {nullptr, nullptr, nullptr, nullptr};
     bool dirty[KINDS] = {false, false, false, false};
-    uint64_t bytes = 0;
+    uint64_t bytes = 0, slots = 0;
     int64_t next_id = 1;
     bg3_serve_stats st;
 };
@@ -78,6 +80,7 @@ static void finish(bg3_server *s, Job *j, int status)
     if (j->net) {
         bg3_destroy(j->net);
         s->bytes -= (uint64_t)j->footprint;
+        s->slots -= j->slots;
     }
     j->net = nullptr;
     if (status == BG3_OK) s->st.done++;
@@ -104,16 +107,31 @@ static int rebuild_groups(bg3_server *s)
     return BG3_OK;
 }
 
-// Admits queued jobs in arrival order while the budget and the slot count allow.
+static bool fits(const bg3_server *s, const Job *j)
+{
+    if (s->bytes + (uint64_t)j->footprint > s->cfg.hbm_budget_bytes) return false;
+    if (s->cfg.max_resident_slots && s->slots > 0 &&
+        s->slots + j->slots > s->cfg.max_resident_slots)
+        return false;
+    return true;
+}
+
+// Admits queued jobs in arrival order while the budgets and the job count allow; later jobs
+// may pass one that does not fit until it has been passed max_bypass times.
 static void admit(bg3_server *s)
 {
-    while (!s->queue.empty()) {
-        Job *j = s->queue.front();
-        const int64_t slots = (int64_t)s->resident.size() + (int64_t)s->joining.size();
-        if (slots >= s->cfg.max_resident) break;
-        if (s->bytes + (uint64_t)j->footprint > s->cfg.hbm_budget_bytes) break;
-        s->queue.pop_front();
+    for (size_t qi = 0; qi < s->queue.size();) {
+        if ((int64_t)(s->resident.size() + s->joining.size()) >= s->cfg.max_resident) break;
+        Job *j = s->queue[qi];
+        if (qi > 0 && s->queue[0]->bypassed >= s->cfg.max_bypass) break;  // the head's turn
+        if (!fits(s, j)) {
+            qi++;
+            continue;
+        }
+        for (size_t k = 0; k < qi; k++) s->queue[k]->bypassed++;
+        s->queue.erase(s->queue.begin() + qi);
         s->bytes += (uint64_t)j->footprint;
+        s->slots += j->slots;
         int rc = bg3_create(&j->d.desc, &j->net);
         if (rc == BG3_OK && j->d.setup) rc = j->d.setup(j->net, j->d.user);
         if (rc == BG3_OK) rc = bg3_sync(j->net);
@@ -123,7 +141,10 @@ static void admit(bg3_server *s)
             else j->syn = t;
         }
         if (rc != BG3_OK) {
-            if (!j->net) s->bytes -= (uint64_t)j->footprint;
+            if (!j->net) {
+                s->bytes -= (uint64_t)j->footprint;
+                s->slots -= j->slots;
+            }
             finish(s, j, rc);
             continue;
         }
@@ -137,7 +158,8 @@ extern "C" {
 
 int bg3_serve_create(const bg3_serve_desc *desc, bg3_server **out)
 {
-    if (!desc || !out || desc->max_resident <= 0 || desc->chunk_steps <= 0) return BG3_EINVAL;
+    if (!desc || !out || desc->max_resident <= 0 || desc->chunk_steps <= 0 || desc->max_bypass < 0)
+        return BG3_EINVAL;
     bg3_server *s = new (std::nothrow) bg3_server();
     if (!s) return BG3_ENOMEM;
     s->cfg = *desc;
@@ -172,6 +194,7 @@ int bg3_serve_submit(bg3_server *s, const bg3_job_desc *job, int64_t *job_id)
     j->id = s->next_id++;
     j->d = *job;
     j->footprint = fp;
+    j->slots = (uint64_t)job->desc.n_neurons * (uint64_t)job->desc.max_syn_per_neuron;
     if (j->d.result) {
         j->d.result->status = BG3_OK;
         j->d.result->synapse_steps = 0;

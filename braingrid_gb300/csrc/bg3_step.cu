@@ -886,8 +886,9 @@ void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t
 
 void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s)
 {
-    // per network: enough warps for a burst, few enough that the grid stays small
-    const int per_net = std::max(2, std::min(32, 608 / std::max(count, 1)));
+    // per network: a plain network's grid shared out over the batch (blocks without items
+    // exit at once, so a quiet network costs little)
+    const int per_net = std::max(2, std::min(deliver_blocks(), 1216 / std::max(count, 1)));
     const dim3 grid(per_net, count);
     switch (syn_kind) {
     case 1: launch_pdl(k_deliver_batch<1>, grid, 256, 0, s, nets); break;

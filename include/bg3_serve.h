@@ -12,9 +12,11 @@
  *      advances with one batched launch per kernel per step (bg3_batch_*), groups on their own
  *      streams;
  *   2. while that runs, queued jobs are admitted in arrival order as long as the device bytes of
- *      the resident jobs plus the next job's bg3_net_footprint stay within hbm_budget_bytes and
- *      fewer than max_resident jobs are resident; admission creates the network and calls the
- *      job's setup callback; the job joins the batch in the next round;
+ *      the resident jobs plus the job's bg3_net_footprint stay within hbm_budget_bytes, its
+ *      synapse slots within max_resident_slots and fewer than max_resident jobs are resident;
+ *      a job that does not fit may be passed by later ones that do, max_bypass times at most;
+ *      admission creates the network and calls the job's setup callback; the job joins the
+ *      batch in the next round;
  *   3. after the chunk, jobs at an epoch end run their epoch pass; finished jobs copy their
  *      results out, free their device memory and are reported by bg3_serve_take.
  * Every job's arithmetic is independent of the others (device noise is keyed by the job's own
@@ -37,6 +39,13 @@ typedef struct {
     uint64_t hbm_budget_bytes;   /* admission budget: sum of resident bg3_net_footprint       */
     int32_t max_resident;        /* jobs on the GPU at once                                    */
     int32_t chunk_steps;         /* cap on the steps of one scheduling round                   */
+    /* work budget: sum of the resident jobs' synapse slots (n_neurons x max_syn_per_neuron);
+     * 0 = none.  Past the point where one step's sweep saturates HBM, more resident work only
+     * stretches every job's latency, so jobs wait instead. */
+    uint64_t max_resident_slots;
+    /* a job that does not fit may be passed by later jobs that do (backfill) at most this many
+     * times; then admission waits for it */
+    int32_t max_bypass;
 } bg3_serve_desc;
 
 /* Where a finished job's results go (host memory owned by the caller, valid until the job has

@@ -109,3 +109,26 @@ def test_served_job_matches_plain_network():
     for k in served:
         assert_same("plain vs served " + k, served[k][:len(plain[k])], plain[k])
     assert net.error_word == 0
+
+
+def test_work_budget_backfills_small_jobs_past_a_large_one():
+    """With a synapse-slot budget, a job that does not fit waits while later small jobs pass it,
+    up to max_bypass times; every result is still the job's own."""
+    big = [serve.lif_growth_job(20, 2, seed=11, radius=2.5, epoch_duration=T),
+           serve.lif_growth_job(22, 2, seed=12, radius=2.5, epoch_duration=T)]
+    small = [serve.izh_static_job(10, 10, 1, seed=13 + k, epoch_duration=T) for k in range(3)]
+    alone = [run_alone(j) for j in (serve.lif_growth_job(20, 2, seed=11, radius=2.5, epoch_duration=T),
+                                    serve.lif_growth_job(22, 2, seed=12, radius=2.5, epoch_duration=T))]
+    cap = big[0].desc.n_neurons * big[0].desc.max_syn_per_neuron + 10000
+    srv = serve.Server(max_resident=8, chunk_steps=400, max_resident_slots=cap, max_bypass=2)
+    for j in big + small:
+        srv.submit(j)
+    srv.pump()
+    st = srv.stats()
+    # big[0] admitted; big[1] does not fit, the small jobs pass it (at most twice)
+    assert st["resident"] == 3 and st["queued"] == 2
+    done = srv.run_all()
+    srv.close()
+    assert len(done) == 5 and all(j.result.status == 0 for j in big + small)
+    for j, a in zip(big, alone):
+        check_same(a, j.outputs(), j.name)
