@@ -12,6 +12,11 @@ of step t + 1 runs in the epilogue of sweep t; the first step's runs standalone)
 before every timed step; device time per step comes from CUDA events on the library's stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bg3|reference]
+                    [--serve-jobs J] [--serve-slots S] [--only c3|serve]
+
+Beside the headline (config[1]) the line carries the batched forms of config[2] (36 LIF
+networks) and config[3] (512 Izhikevich + STDP networks), and the served stream of config[4]
+(a J-job trace through the job server, against the same jobs one at a time).
 
 --impl reference times the reference algorithm's CPU path (the C restatement in oracle/, the
 reference's own sources are not on the GPU host) on the same network, single-threaded as the
@@ -45,8 +50,8 @@ METRIC = "synapse-updates/s"
 SWEEP_BYTES_PER_SYN = 9
 SWEEP_BYTES_PER_NEURON = 48
 SURVEY_BYTES_PER_SYN = 28
-# served form: resident work cap, about two and a half of the largest jobs' synapse slots
-SERVE_SLOTS = 100e6
+# served form: resident work cap, about one and a half of the largest jobs' synapse slots
+SERVE_SLOTS = 60e6
 
 
 def peaks():
@@ -226,7 +231,12 @@ def run_bg3(args):
     e2e = {"value": S * E2E_STEPS * e2e_iters * world / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS}
     err = net.error_word
-    batched = run_batched(min(args.steps, 500), max(args.warmup, 20)) if world == 1 else None
+    batched = izh_stdp = served = None
+    if world == 1:
+        batched = run_batched(min(args.steps, 500), max(args.warmup, 20))
+        izh_stdp = run_c3(min(args.steps, 1000), max(args.warmup, 20))
+        if args.serve_jobs > 0:
+            served = run_served(args.serve_jobs, int(args.serve_slots))
     if rank == 0:
         cpu = cpu_baseline_port(net, spec)
         tr = traffic_per_launch(S)
@@ -255,6 +265,8 @@ def run_bg3(args):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "batched": batched,
+            "batched_izh_stdp": izh_stdp,
+            "served": served,
             "gpu_launches": 2 * args.steps + 1,
             "clocks": clocks,
             "error_word": err,
