@@ -75,6 +75,27 @@ def test_c0_first_epoch_bit_exact():
     run_locked("c0", epochs=1, check_every=1)
 
 
+def test_c0_ten_epochs_epoch_ends_bit_exact():
+    """config[0] in full (10 x 1 s, 100,000 steps): radii, rates, spike histories and recorder
+    histograms equal the oracle's at every epoch end, hence the FP32 reference's (whose gap to the
+    FP64 build is pinned in test_oracle_golden)."""
+    c = case("c0")
+    spe = steps_per_epoch(c)
+    o = oracle_from_case(c)
+    net = gpu_from_oracle(o, c, n_noise=c["N"] * spe * c["epochs"] + 64)
+    for e in range(c["epochs"]):
+        o.step_n(spe)
+        net.step(spe)
+        compare_history(net, o, "epoch %d" % e)
+        _growth_both(o, net, e + 1)
+    b, s, rh, ra = net.download_histories()
+    assert_same("burstiness", b, o.arr("burstinessHist"))
+    assert_same("spikes history", s, o.arr("spikesHistory"))
+    assert_same("radii history", ra, o.arr("radiiHistory"))
+    assert_same("rates history", rh, o.arr("ratesHistory"))
+    assert net.error_word == 0
+
+
 def test_ref_tiny_bit_exact_vs_reference_fixture():
     o, net = run_locked("ref_tiny", check_every=1)
     fx = load_fixture("ref_tiny")
