@@ -234,6 +234,29 @@ static int set_stdp_type(bg3_net *n, int type, const StdpConst &in)
     return push_desc(n);
 }
 
+// DS parameter class of (U, D, F): index into the network's table, adding it (with the exp
+// tables of D and F) on first use.  Returns the class, or a negative status.
+static int param_class(bg3_net *n, float U, float D, float F)
+{
+    NetDev &h = n->h;
+    for (int c = 0; c < h.n_pcls; c++)
+        if (fbits(h.p_U[c]) == fbits(U) && fbits(h.p_D[c]) == fbits(D) && fbits(h.p_F[c]) == fbits(F))
+            return c;
+    if (h.n_pcls >= BG3_MAX_PCLS) return BG3_EUNSUPPORTED;
+    const float *xd = nullptr, *xf = nullptr;
+    int rc;
+    if (D > 0.0f && std::isfinite(D) && (rc = exp_table<float>(n, 0, D, BG3_EXP_LEN, &xd))) return rc;
+    if (F > 0.0f && std::isfinite(F) && (rc = exp_table<float>(n, 0, F, BG3_EXP_LEN, &xf))) return rc;
+    const int c = h.n_pcls++;
+    h.p_U[c] = U;
+    h.p_D[c] = D;
+    h.p_F[c] = F;
+    h.p_xD[c] = xd;
+    h.p_xF[c] = xf;
+    if ((rc = push_desc(n))) return rc;
+    return c;
+}
+
 static void exp_release(bg3_net *n)
 {
     std::lock_guard<std::mutex> lock(g_exp_mu);
@@ -389,8 +412,11 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
         rc = BG3_ECUDA;
         goto fail;
     }
-    for (int t = 0; t < 4 && (h.syn_kind == BG3_SYN_DS || h.syn_kind == BG3_SYN_DYNSTDP); t++)
-        if ((rc = exp_class(n, h.t_D[t])) || (rc = exp_class(n, h.t_F[t]))) goto fail;
+    for (int t = 0; t < 4 && (h.syn_kind == BG3_SYN_DS || h.syn_kind == BG3_SYN_DYNSTDP); t++) {
+        const int c = param_class(n, h.t_U[t], h.t_D[t], h.t_F[t]);
+        if (c < 0) { rc = c; goto fail; }
+        h.t_pcls[t] = c;
+    }
     // AllSTDPSynapses::createSynapse constants (Synapses/AllSTDPSynapses.cpp:256-272)
     for (int t = 0; t < 4 && h.syn_kind >= BG3_SYN_STDP; t++) {
         StdpConst c = {};
@@ -523,10 +549,11 @@ int bg3_set_type_constants(bg3_net *n, const bg3_type_constants *c)
         n->h.t_U[t] = c->U[t];
         n->h.t_D[t] = c->D[t];
         n->h.t_F[t] = c->F[t];
-        int rc;
-        if ((n->h.syn_kind == BG3_SYN_DS || n->h.syn_kind == BG3_SYN_DYNSTDP) &&
-            ((rc = exp_class(n, c->D[t])) || (rc = exp_class(n, c->F[t]))))
-            return rc;
+        if (n->h.syn_kind == BG3_SYN_DS || n->h.syn_kind == BG3_SYN_DYNSTDP) {
+            const int pc = param_class(n, c->U[t], c->D[t], c->F[t]);
+            if (pc < 0) return pc;
+            n->h.t_pcls[t] = pc;
+        }
     }
     n->h.t_u0 = c->u0;
     n->h.t_r0 = c->r0;
@@ -559,7 +586,8 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
     memset(ev.data(), 0, S * sizeof(EvSlot));
     // fired[s] bit j: neuron s fired at step - 1 - j (j < 32), from the queues
     std::vector<uint32_t> fired(N, 0u);
-    uint32_t seenD = 0xffffffffu, seenF = 0xffffffffu;  // last time constants registered
+    uint32_t seenU = 0xffffffffu, seenD = 0xffffffffu, seenF = 0xffffffffu;  // last (U, D, F)
+    int seenC = 0;
     for (size_t d = 0; d < N; d++) {
         size_t c = 0;
         while (c < M && a->in_use[d * M + c]) c++;
@@ -583,14 +611,18 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
             EvSlot &e = ev[p];
             e.W = a->W[i];
             e.born = (uint32_t)(step - (uint64_t)di - 32u);
+            e.dcls = (uint8_t)dcl;
             if (ds) {
-                e.U = a->U[i]; e.D = a->D[i]; e.F = a->F[i]; e.u = a->u[i]; e.r = a->r[i];
-                if (fbits(e.D) != seenD || fbits(e.F) != seenF) {
-                    int erc;
-                    if ((erc = exp_class(n, e.D)) || (erc = exp_class(n, e.F))) return erc;
-                    seenD = fbits(e.D);
-                    seenF = fbits(e.F);
+                e.u = a->u[i];
+                e.r = a->r[i];
+                if (fbits(a->U[i]) != seenU || fbits(a->D[i]) != seenD || fbits(a->F[i]) != seenF) {
+                    seenC = param_class(n, a->U[i], a->D[i], a->F[i]);
+                    if (seenC < 0) return seenC;
+                    seenU = fbits(a->U[i]);
+                    seenD = fbits(a->D[i]);
+                    seenF = fbits(a->F[i]);
                 }
+                e.pcls = (uint8_t)seenC;
                 uint64_t ls = a->lastSpike[i];
                 if (ls != BG3_ULONG_MAX && ls >= BG3_NO_SPIKE32) return BG3_EINVAL;
                 e.last = (ls == BG3_ULONG_MAX) ? BG3_NO_SPIKE32 : (uint32_t)ls;
@@ -779,10 +811,12 @@ int bg3_input_poisson(bg3_net *n, const bg3_poisson_arrays *a, float lambda, uin
         unsigned phase = (unsigned)((step - (uint64_t)a->delayIdx[i]) & 31u);
         q[i] = rotl32(a->delayQueue[i], phase);
         EvSlot &e = ev[i];
-        e.W = a->W[i]; e.U = a->U[i]; e.D = a->D[i]; e.F = a->F[i]; e.u = a->u[i]; e.r = a->r[i];
+        e.W = a->W[i]; e.u = a->u[i]; e.r = a->r[i];
         e.last = (ls == BG3_ULONG_MAX) ? BG3_NO_SPIKE32 : (uint32_t)ls;
         e.born = (uint32_t)(step - (uint64_t)a->delayIdx[i]);
-        if ((rc = exp_class(n, e.D)) || (rc = exp_class(n, e.F))) return rc;
+        const int pc = param_class(n, a->U[i], a->D[i], a->F[i]);
+        if (pc < 0) return pc;
+        e.pcls = (uint8_t)pc;
     }
     if ((rc = h2d(n, h.pois_mask, mask.data(), N)) || (rc = h2d(n, h.pois_nisi, a->nISIs, N)) ||
         (rc = h2d(n, h.in_psr, a->psr, N)) || (rc = h2d(n, h.in_decay, a->decay, N)) ||
@@ -852,9 +886,9 @@ int bg3_download_poisson(bg3_net *n, bg3_poisson_arrays *a)
         if (a->W) a->W[i] = e.W;
         if (a->psr) a->psr[i] = psr[i];
         if (a->decay) a->decay[i] = dec[i];
-        if (a->U) a->U[i] = e.U;
-        if (a->D) a->D[i] = e.D;
-        if (a->F) a->F[i] = e.F;
+        if (a->U) a->U[i] = h.p_U[e.pcls];
+        if (a->D) a->D[i] = h.p_D[e.pcls];
+        if (a->F) a->F[i] = h.p_F[e.pcls];
         if (a->u) a->u[i] = e.u;
         if (a->r) a->r[i] = e.r;
         if (a->lastSpike) a->lastSpike[i] = (e.last == BG3_NO_SPIKE32) ? BG3_ULONG_MAX : (uint64_t)e.last;
@@ -1053,9 +1087,9 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
             if (a->delayQueue) a->delayQueue[i] = q;
             if (a->tau) a->tau[i] = h.t_tau[st[p] & 3];
             if (!ds) continue;  // the DS fields exist for DS and dynamic STDP synapses only
-            if (a->U) a->U[i] = e.U;
-            if (a->D) a->D[i] = e.D;
-            if (a->F) a->F[i] = e.F;
+            if (a->U) a->U[i] = h.p_U[e.pcls];
+            if (a->D) a->D[i] = h.p_D[e.pcls];
+            if (a->F) a->F[i] = h.p_F[e.pcls];
             if (a->u) a->u[i] = e.u;
             if (a->r) a->r[i] = e.r;
             if (a->lastSpike) a->lastSpike[i] = (e.last == BG3_NO_SPIKE32) ? BG3_ULONG_MAX : (uint64_t)e.last;

@@ -136,9 +136,10 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
                 n.lcls[p] = (uint8_t)n.t_lcls[type];
                 EvSlot e;
                 e.W = a * syn_sign(type) * 1.0e-8f;
-                e.U = n.t_U[type];
-                e.D = n.t_D[type];
-                e.F = n.t_F[type];
+                e.dcls = (uint8_t)n.t_dcls[type];
+                e.pcls = (uint8_t)n.t_pcls[type];
+                e.pad0 = 0;
+                e.pad1 = e.pad2 = 0u;
                 e.u = n.t_u0;
                 e.r = n.t_r0;
                 e.last = BG3_NO_SPIKE32;

@@ -11,8 +11,10 @@
 //                         (d, k) is d * maxSyn + k.
 //   hot per-slot state    psr (f32) and a one-byte decay class (index into a per-network table
 //                         of decay factors): 9 bytes per synapse per step.
-//   event per-slot state  EvSlot (32 B, one sector): W, U, D, F, u, r, last spike step, birth
-//                         step — read only when a spike is delivered.
+//   event per-slot state  EvSlot (32 B, one sector): W, u, r, last spike step, birth step, and
+//                         the slot's decay class and DS parameter class (U, D, F and their exp
+//                         tables live in a per-network table) — read only when a spike is
+//                         delivered, so a delivery touches two lines: its EvSlot and its psr.
 //   spike propagation     instead of a 32-bit delay queue per synapse, the ids of the neurons
 //                         that fired at each of the last 64 steps are kept in a ring; the
 //                         outgoing map is grouped by delay class, so at step t the synapses of
@@ -33,6 +35,7 @@
 #define BG3_MAX_EXPC 16      // time constants with an exp table
 #define BG3_EXP_LEN 262144   // steps covered by an exp table (26 s at dt = 0.1 ms)
 #define BG3_DEXP_LEN 8192    // steps covered by a double exp table (STDP windows)
+#define BG3_MAX_PCLS 16      // distinct (U, D, F) triples of DS synapses
 
 // STDP constants of one synapse type (AllSTDPSynapses.h:350-420); createSynapse gives every
 // synapse the same values (AllSTDPSynapses.cpp:252-273), so they are held per type.
@@ -44,9 +47,13 @@ struct StdpConst {
 };
 
 struct __align__(32) EvSlot {
-    float W, U, D, F, u, r;
+    float W, u, r;
     uint32_t last;   // step of the last delivered spike, BG3_NO_SPIKE32 = none (ULONG_MAX)
     uint32_t born;   // step at which the synapse was created (low 32 bits)
+    uint8_t dcls;    // decay class (the plane's class byte, for the delivery)
+    uint8_t pcls;    // (U, D, F) class
+    uint16_t pad0;
+    uint32_t pad1, pad2;
 };
 
 // plane position of slot (dest d, row k) and its inverse
@@ -132,6 +139,11 @@ struct NetDev {
     // spike-time arithmetic instead of its host build's unsigned one
     StdpConst stdp[4];
     int32_t stdp_signed;
+    // DS parameter classes: (U, D, F) and the exp tables of D and F (NULL past the limit)
+    int32_t n_pcls;
+    int32_t t_pcls[4];               // class of the per-type constants (synapses growth creates)
+    float p_U[BG3_MAX_PCLS], p_D[BG3_MAX_PCLS], p_F[BG3_MAX_PCLS];
+    const float *p_xD[BG3_MAX_PCLS], *p_xF[BG3_MAX_PCLS];
 };
 
 // device error word bits (mirrored in include/bg3.h)
@@ -167,6 +179,25 @@ __device__ __forceinline__ float exp_steps(const NetDev &n, uint32_t k, float ta
     }
     const float x = (float)k * n.dt;
     return exp_cr(-x / tau);
+}
+
+// expf(-((float)k * dt) / tau) from the table of a DS parameter class.
+__device__ __forceinline__ float exp_tab(const NetDev &n, const float *tab, uint32_t k, float tau)
+{
+    if (tab && k < (uint32_t)BG3_EXP_LEN) return __ldg(tab + k);
+    const float x = (float)k * n.dt;
+    return exp_cr(-x / tau);
+}
+
+// AllDSSynapses::changePSR's facilitation / depression update of u and r
+// (Synapses/AllDSSynapses.cpp:235-241) for a spike k steps after the previous one.
+__device__ __forceinline__ void ds_update(const NetDev &n, const EvSlot &e, uint32_t k,
+                                          float &u, float &r)
+{
+    const int c = e.pcls;
+    const float U = n.p_U[c];
+    r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_tab(n, n.p_xD[c], k, n.p_D[c]);
+    u = U + u * (1.0f - U) * exp_tab(n, n.p_xF[c], k, n.p_F[c]);
 }
 
 // expf(-(x dt) / tau) for a spike-time difference u held as uint64 (host build) or int64
@@ -313,11 +344,7 @@ __device__ __forceinline__ float input_apply(const NetDev &n, int i, unsigned lo
             q &= ~bit;
             EvSlot e = n.in_ev[i];
             float u = e.u, r = e.r;
-            if (e.last != BG3_NO_SPIKE32) {
-                const uint32_t k = (uint32_t)t - e.last;
-                r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_steps(n, k, e.D);
-                u = e.U + u * (1.0f - e.U) * exp_steps(n, k, e.F);
-            }
+            if (e.last != BG3_NO_SPIKE32) ds_update(n, e, (uint32_t)t - e.last, u, r);
             psr = psr + ((e.W / dec) * u * r);
             n.in_ev[i].u = u;
             n.in_ev[i].r = r;

@@ -290,7 +290,7 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
     const uint32_t t = (uint32_t)t64;
     EvSlot e = n.ev[p];
     if ((int32_t)(tf - e.born) < 0) return;  // the synapse did not exist when the spike left
-    float dec = n.dtab[n.dcls[p]];
+    float dec = n.dtab[e.dcls];
     float ps = n.psr[p];
     if (SYN >= 2) {
         int k, d;
@@ -300,11 +300,7 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
     }
     if (SYN == 1 || SYN == 3) {
         float u = e.u, r = e.r;
-        if (e.last != BG3_NO_SPIKE32) {
-            const uint32_t k = t - e.last;
-            r = 1.0f + (r * (1.0f - u) - 1.0f) * exp_steps(n, k, e.D);
-            u = e.U + u * (1.0f - e.U) * exp_steps(n, k, e.F);
-        }
+        if (e.last != BG3_NO_SPIKE32) ds_update(n, e, t - e.last, u, r);
         ps = ps + ((e.W / dec) * u * r);
         EvSlot *q = &n.ev[p];
         q->u = u;
@@ -347,24 +343,26 @@ __device__ __forceinline__ void deliver_chunk(const NetDev &n, uint32_t b, uint3
         p[u] = ok[u] ? n.outMap[b + j] : 0u;
     }
     EvSlot e[4];
-    float ps[4], dec[4];
+    float ps[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
         if (ok[u]) {
             e[u] = n.ev[p[u]];
             ps[u] = n.psr[p[u]];
-            dec[u] = n.dtab[n.dcls[p[u]]];
         }
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) ok[u] = ok[u] && (int32_t)(tf - e[u].born) >= 0;
-    float xr[4], xu[4];
+    float xr[4], xu[4], dec[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-        if (SYN == 1 && ok[u] && e[u].last != BG3_NO_SPIKE32) {
+        if (!ok[u]) continue;
+        dec[u] = n.dtab[e[u].dcls];
+        if (SYN == 1 && e[u].last != BG3_NO_SPIKE32) {
             const uint32_t ki = t - e[u].last;
-            xr[u] = exp_steps(n, ki, e[u].D);
-            xu[u] = exp_steps(n, ki, e[u].F);
+            const int c = e[u].pcls;
+            xr[u] = exp_tab(n, n.p_xD[c], ki, n.p_D[c]);
+            xu[u] = exp_tab(n, n.p_xF[c], ki, n.p_F[c]);
         }
     }
 #pragma unroll
@@ -374,8 +372,9 @@ __device__ __forceinline__ void deliver_chunk(const NetDev &n, uint32_t b, uint3
         if (SYN == 1) {
             float uu = e[u].u, r = e[u].r;
             if (e[u].last != BG3_NO_SPIKE32) {
+                const float U = n.p_U[e[u].pcls];
                 r = 1.0f + (r * (1.0f - uu) - 1.0f) * xr[u];
-                uu = e[u].U + uu * (1.0f - e[u].U) * xu[u];
+                uu = U + uu * (1.0f - U) * xu[u];
             }
             q = q + ((e[u].W / dec[u]) * uu * r);
             EvSlot *w = &n.ev[p[u]];

@@ -2,8 +2,10 @@
 
     python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big] [--steps 20] [--flush]
 
-c3 is the 512-network Izhikevich + STDP batch; big is three pre-grown LIF networks of the
-served stream's largest sizes (170x170, 176x176, 180x180) batched together.
+c3 is the Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
+networks of the served stream's largest sizes (166x166, 176x176, 180x180) after one epoch and a
+growth pass (which restores the unscaled growth weights: the networks then fire at ~300 Hz),
+batched together.
 """
 import argparse
 
@@ -15,6 +17,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
     ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big"])
+    ap.add_argument("--count", type=int, default=512, help="networks of the c3 workload")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
     if a.workload == "c1":
@@ -27,17 +30,19 @@ def main():
         if a.workload == "c2":
             nets = [workloads.build_member(w)[1] for w in workloads.c2_members()]
         elif a.workload == "c3":
-            nets = workloads.build_c3()
+            nets = workloads.build_c3(count=a.count)
         else:
             from . import serve
             nets = []
-            for k, side in enumerate((170, 176, 180)):
-                job = serve.lif_growth_job(side, 1, seed=60 + k)
+            for k, side in enumerate((166, 176, 180)):
+                job = serve.lif_growth_job(side, 2, seed=60 + k)
                 d = job.desc
                 net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height,
                                  d.epoch_duration, d.delta_t, d.max_firing_rate, d.max_epochs,
                                  d.synapse_kind, d.noise_mode, d.noise_seed)
                 job.setup(net)
+                net.step(10000)
+                net.growth(1)
                 net.step(1000)
                 c = net.download_lif(fields=("spikeCount",))["spikeCount"]
                 print("net", side, "synapses", net.total_synapses(), "rate_hz",

@@ -98,7 +98,9 @@ typedef struct {
  * (Synapses/AllSynapses.h:188-232, AllSpikingSynapses.h:342-355, AllDSSynapses.h:269-336).
  * in_use uses one byte per slot; counts is n_neurons long (synapse_counts).  On upload the
  * in-use slots of every row must form a prefix (what AllSynapses::addSynapse produces when no
- * synapse was ever erased).  DS fields may be NULL for BG3_SYN_SPIKING. */
+ * synapse was ever erased).  DS fields may be NULL for BG3_SYN_SPIKING; a network holds at most
+ * 16 distinct (U, D, F) triples (createSynapse makes four, one per synapse type), more is
+ * BG3_EUNSUPPORTED. */
 typedef struct {
     uint8_t *in_use;
     int32_t *src, *type, *delayIdx, *total_delay;
