@@ -173,6 +173,8 @@ def run_bg3(args):
     spec, net = build_network()
     N = spec["N"]
     S = net.total_synapses()
+    # launch configuration chosen by the autotuner on this network's state (left unchanged)
+    launch, _ = net.autotune(steps_per_trial=200)
     # warm-up: W benchmark steps plus ~0.1 s of plain steps so that clocks have ramped
     net.step(2000)
     net.bench_steps(args.warmup, FLUSH_BYTES)
@@ -251,6 +253,7 @@ def run_bg3(args):
                        "neurons": N, "synapses": S, "dt_s": 1e-4, "noise": "device",
                        "l2": "flushed (256 MiB write) before every timed step",
                        "mean_rate_hz": rate_hz, "deliveries_per_step": deliveries,
+                       "launch": launch,
                        "parallelism": "replicas" if world > 1 else "single"},
             "neuron_steps_per_s": N * args.steps * world / t_total,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -287,6 +290,7 @@ def run_batched(steps, warmup):
     S = sum(n.total_synapses() for n in nets)
     N = sum(n.N for n in nets)
     batch = bg.Batch(nets)
+    launch, _ = batch.autotune(steps_per_trial=100)
     batch.step(warmup)
     batch.sync()
     # batched: device time per step with CUDA events (the working set, ~1 GB, exceeds L2)
@@ -330,7 +334,8 @@ def run_batched(steps, warmup):
            "plain_lockstep_ms_per_step": t_lock * 1e3,
            "plain_lockstep_timing": "host wall clock, %d steps of 36 bg3_step(1) calls" % lock,
            "batched_over_plain": t_plain / t_batch,
-           "batched_over_plain_lockstep": t_lock * steps / t_batch, "error_word": int(err)}
+           "batched_over_plain_lockstep": t_lock * steps / t_batch, "error_word": int(err),
+           "launch": launch}
     batch.close()
     for n in nets:
         n.close()
@@ -349,6 +354,7 @@ def run_c3(steps, warmup):
     S = sum(n.total_synapses() for n in nets)
     N = sum(n.N for n in nets)
     batch = bg.Batch(nets)
+    launch, _ = batch.autotune(steps_per_trial=100)
     batch.step(warmup)
     batch.sync()
     ms = batch.bench_steps(steps)
@@ -379,7 +385,7 @@ def run_c3(steps, warmup):
            "plain_timing": "host wall clock around %d sequential bg3_step runs" % len(nets),
            "batched_over_plain": t_plain / t_batch,
            "mean_rate_hz": spikes / float(N) / ((steps + 2 * warmup) * 1e-4),
-           "error_word": int(err)}
+           "error_word": int(err), "launch": launch}
     batch.close()
     for n in nets:
         n.close()

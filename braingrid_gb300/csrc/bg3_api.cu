@@ -18,15 +18,17 @@
 
 namespace bg3 {
 void launch_neurons(const NetDev &h, cudaStream_t s);
-void launch_deliver(const NetDev &h, cudaStream_t s);
+void launch_deliver(const NetDev &h, const LaunchCfg &c, cudaStream_t s);
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
+                  const LaunchCfg &c,
                   cudaStream_t s);
 void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s);
-void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s);
+void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, const LaunchCfg &c,
+                          cudaStream_t s);
 void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int n_thick,
-                        int n_thin, bool fuse, cudaStream_t s);
-bool sweep_is_thin(const NetDev &h);
-void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s);
+                        int n_thin, bool fuse, const LaunchCfg &c, cudaStream_t s);
+bool sweep_is_thin(const NetDev &h, const LaunchCfg &c);
+void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, int add_threads, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
@@ -41,7 +43,8 @@ struct bg3_net {
     NetDev h;                 // host copy of the device descriptor
     NetDev *d = nullptr;      // device copy
     cudaStream_t stream = nullptr;
-    std::vector<void *> allocs;
+    std::vector<std::pair<void *, size_t>> allocs;  // device allocations and their sizes
+    LaunchCfg cfg = LAUNCH_DEFAULT;
     CUtensorMap tm_psr, tm_cls;
     std::vector<float> dtab;  // decay factor per decay class
     std::vector<int> ltab;    // delay per delay class
@@ -76,7 +79,7 @@ static int dalloc(bg3_net *n, T **p, size_t count, int fill = 0)
         cudaGetLastError();
         return BG3_ENOMEM;
     }
-    n->allocs.push_back(q);
+    n->allocs.push_back(std::make_pair(q, bytes));
     n->bytes += bytes;
     if (cudaMemsetAsync(q, fill, bytes, n->stream) != cudaSuccess) return BG3_ECUDA;
     *p = (T *)q;
@@ -472,7 +475,8 @@ int bg3_destroy(bg3_net *n)
     if (n->stream) cudaStreamSynchronize(n->stream);
     drop_graph(n);
     exp_release(n);
-    for (void *p : n->allocs) cudaFree(p);
+    for (auto &a : n->allocs)
+        if (a.first) cudaFree(a.first);
     if (n->d) cudaFree(n->d);
     if (n->noise_dev) cudaFree(n->noise_dev);
     if (n->flush_buf) cudaFree(n->flush_buf);
@@ -844,7 +848,11 @@ int bg3_push_poisson_isis(bg3_net *n, const int32_t *begin, const int32_t *isis)
     if (h.isi_vals) {  // replace the previous draws
         cudaStreamSynchronize(n->stream);
         for (auto &p : n->allocs)
-            if (p == (void *)h.isi_vals) { cudaFree(p); p = nullptr; }
+            if (p.first == (void *)h.isi_vals) {
+                cudaFree(p.first);
+                n->bytes -= p.second;
+                p = std::make_pair((void *)nullptr, (size_t)0);
+            }
         h.isi_vals = nullptr;
     }
     if ((rc = dalloc(n, &h.isi_vals, std::max<size_t>(total, 1)))) return rc;
@@ -908,8 +916,8 @@ static int run_steps(bg3_net *n, int64_t nsteps)
     if (h.noise_mode == BG3_NOISE_INJECT) {
         for (int64_t s = 0; s < nsteps; s++) {
             bg3::launch_neurons(h, n->stream);
-            bg3::launch_deliver(h, n->stream);
-            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->stream);
+            bg3::launch_deliver(h, n->cfg, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->cfg, n->stream);
         }
         n->launches += (1 + step_kernels(h.syn_kind)) * nsteps;
         CK(cudaGetLastError());
@@ -921,8 +929,8 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < GRAPH_STEPS; i++) {
-            bg3::launch_deliver(h, n->stream);
-            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->stream);
+            bg3::launch_deliver(h, n->cfg, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->cfg, n->stream);
         }
         CK(cudaStreamEndCapture(n->stream, &g));
         cudaError_t e = cudaGraphInstantiate(&n->graph, g, 0);
@@ -934,11 +942,11 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         interior -= GRAPH_STEPS;
     }
     for (int64_t i = 0; i < interior; i++) {
-        bg3::launch_deliver(h, n->stream);
-        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->stream);
+        bg3::launch_deliver(h, n->cfg, n->stream);
+        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->cfg, n->stream);
     }
-    bg3::launch_deliver(h, n->stream);
-    bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->stream);
+    bg3::launch_deliver(h, n->cfg, n->stream);
+    bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->cfg, n->stream);
     n->launches += 1 + step_kernels(h.syn_kind) * nsteps;
     CK(cudaGetLastError());
     return BG3_OK;
@@ -953,7 +961,7 @@ int bg3_step(bg3_net *n, int64_t nsteps)
 int bg3_epoch_growth(bg3_net *n, int32_t epoch)
 {
     if (!n || epoch < 0) return BG3_EINVAL;
-    bg3::launch_growth(n->h, n->d, epoch, n->stream);
+    bg3::launch_growth(n->h, n->d, epoch, n->cfg.growth_threads, n->stream);
     n->launches += 8;
     CK(cudaGetLastError());
     return BG3_OK;
@@ -1316,6 +1324,7 @@ struct bg3_batch {
     void *flush_buf = nullptr, *scrub_buf = nullptr;
     size_t flush_size = 0;
     long long launches = 0;
+    LaunchCfg cfg = LAUNCH_DEFAULT;
 };
 
 static int batch_refresh(bg3_batch *b)
@@ -1341,10 +1350,10 @@ static int batch_refresh(bg3_batch *b)
                      [](const std::pair<int, int2> &a, const std::pair<int, int2> &c) { return a.first > c.first; });
     std::vector<int2> tl;
     for (auto &t : tiles)
-        if (!bg3::sweep_is_thin(b->nets[t.second.x]->h)) tl.push_back(t.second);
+        if (!bg3::sweep_is_thin(b->nets[t.second.x]->h, b->cfg)) tl.push_back(t.second);
     b->n_thick = (int)tl.size();
     for (auto &t : tiles)
-        if (bg3::sweep_is_thin(b->nets[t.second.x]->h)) tl.push_back(t.second);
+        if (bg3::sweep_is_thin(b->nets[t.second.x]->h, b->cfg)) tl.push_back(t.second);
     if ((int)tl.size() != b->ntiles) {
         if (b->d_tiles) cudaFree(b->d_tiles);
         b->d_tiles = nullptr;
@@ -1435,8 +1444,8 @@ int bg3_batch_refresh(bg3_batch *b)
 static void batch_interior(bg3_batch *b, int64_t n)
 {
     for (int64_t i = 0; i < n; i++) {
-        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, (int)b->nets.size(), b->stream);
-        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, true, b->stream);
+        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, (int)b->nets.size(), b->cfg, b->stream);
+        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, true, b->cfg, b->stream);
     }
 }
 
@@ -1463,8 +1472,8 @@ int bg3_batch_step(bg3_batch *b, int64_t nsteps)
         interior -= GRAPH_STEPS;
     }
     batch_interior(b, interior);
-    bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
-    bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, false, b->stream);
+    bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
+    bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, false, b->cfg, b->stream);
     const int sweeps = (b->n_thick > 0) + (b->ntiles > b->n_thick);
     b->launches += 1 + (step_kernels(b->syn_kind) - 1 + sweeps) * nsteps;
     CK(cudaGetLastError());
@@ -1528,9 +1537,9 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
         if (!inject && s == 0) bg3::launch_neurons(h, n->stream);
         CK(cudaEventRecord(e[0], n->stream));
         if (inject) bg3::launch_neurons(h, n->stream);
-        bg3::launch_deliver(h, n->stream);
+        bg3::launch_deliver(h, n->cfg, n->stream);
         if (kernel_ms) CK(cudaEventRecord(e[1], n->stream));
-        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, !inject && !last, n->stream);
+        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, !inject && !last, n->cfg, n->stream);
         CK(cudaEventRecord(e[2], n->stream));
     }
     n->launches += (step_kernels(h.syn_kind) + (inject ? 1 : 0)) * nsteps + (inject ? 0 : 1);
@@ -1578,8 +1587,8 @@ int bg3_batch_bench_steps(bg3_batch *b, int64_t nsteps, int64_t flush_bytes, flo
                                                    (float *)((char *)b->scrub_buf + flush_bytes));
         }
         CK(cudaEventRecord(ev[2 * s], b->stream));
-        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->stream);
-        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, s < nsteps - 1, b->stream);
+        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
+        bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, s < nsteps - 1, b->cfg, b->stream);
         CK(cudaEventRecord(ev[2 * s + 1], b->stream));
     }
     const int sweeps = (b->n_thick > 0) + (b->ntiles > b->n_thick);
@@ -1609,3 +1618,253 @@ int bg3_kernel_times(bg3_net *n, float *a, float *b, float *c, int64_t *launches
 }
 
 }  // extern "C"
+
+// ---- launch configuration and autotuning ------------------------------------------------------
+static bool cfg_valid(const bg3_launch_cfg *c)
+{
+    return c && (c->sweep_stages == 4 || c->sweep_stages == 6 || c->sweep_stages == 8) &&
+           c->thin_max_quads >= 1 && c->thin_max_quads <= 4096 && c->thin_warps >= 1 &&
+           c->thin_warps <= 32 && c->deliver_blocks >= 1 && c->deliver_blocks <= 65535 &&
+           (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512);
+}
+static LaunchCfg cfg_from(const bg3_launch_cfg &c)
+{
+    return LaunchCfg{c.sweep_stages, c.thin_max_quads, c.thin_warps, c.deliver_blocks, c.growth_threads};
+}
+static bg3_launch_cfg cfg_to(const LaunchCfg &c)
+{
+    bg3_launch_cfg o;
+    o.sweep_stages = c.sweep_stages;
+    o.thin_max_quads = c.thin_max_quads;
+    o.thin_warps = c.thin_warps;
+    o.deliver_blocks = c.deliver_blocks;
+    o.growth_threads = c.growth_threads;
+    return o;
+}
+
+int bg3_get_launch(bg3_net *n, bg3_launch_cfg *c)
+{
+    if (!n || !c) return BG3_EINVAL;
+    *c = cfg_to(n->cfg);
+    return BG3_OK;
+}
+
+int bg3_set_launch(bg3_net *n, const bg3_launch_cfg *c)
+{
+    if (!n || !cfg_valid(c)) return BG3_EINVAL;
+    CK(cudaStreamSynchronize(n->stream));
+    n->cfg = cfg_from(*c);
+    drop_graph(n);
+    return BG3_OK;
+}
+
+int bg3_batch_get_launch(bg3_batch *b, bg3_launch_cfg *c)
+{
+    if (!b || !c) return BG3_EINVAL;
+    *c = cfg_to(b->cfg);
+    return BG3_OK;
+}
+
+int bg3_batch_set_launch(bg3_batch *b, const bg3_launch_cfg *c)
+{
+    if (!b || !cfg_valid(c)) return BG3_EINVAL;
+    CK(cudaStreamSynchronize(b->stream));
+    b->cfg = cfg_from(*c);
+    return batch_refresh(b);  // the thin / TMA split of the tiles depends on the configuration
+}
+
+// A device-side copy of a network's whole state (every allocation plus the injected-noise
+// buffer), for trials that must leave the network as it was.
+struct StateCopy {
+    void *buf = nullptr;
+    std::vector<std::pair<void *, size_t>> parts;
+};
+
+static int state_save(bg3_net *n, StateCopy &sc)
+{
+    sc.parts.clear();
+    for (auto &a : n->allocs)
+        if (a.first) sc.parts.push_back(a);
+    if (n->noise_dev) sc.parts.push_back(std::make_pair((void *)n->noise_dev, (size_t)n->noise_cap * sizeof(float)));
+    size_t tot = 0;
+    for (auto &p : sc.parts) tot += p.second;
+    CK(cudaStreamSynchronize(n->stream));
+    if (cudaMalloc(&sc.buf, std::max<size_t>(tot, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        sc.buf = nullptr;
+        return BG3_ENOMEM;
+    }
+    size_t off = 0;
+    for (auto &p : sc.parts) {
+        CK(cudaMemcpyAsync((char *)sc.buf + off, p.first, p.second, cudaMemcpyDeviceToDevice, n->stream));
+        off += p.second;
+    }
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+static int state_load(bg3_net *n, const StateCopy &sc)
+{
+    size_t off = 0;
+    for (auto &p : sc.parts) {
+        CK(cudaMemcpyAsync(p.first, (const char *)sc.buf + off, p.second, cudaMemcpyDeviceToDevice, n->stream));
+        off += p.second;
+    }
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+static void state_free(StateCopy &sc)
+{
+    if (sc.buf) cudaFree(sc.buf);
+    sc.buf = nullptr;
+}
+
+// Coordinate search over the launch parameters; trial(cfg) returns a time (ms) or < 0 on error.
+template <typename Trial>
+static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool growth, Trial trial, float &best_ms)
+{
+    float t = trial(cur);
+    if (t < 0) return (int)t;
+    best_ms = t;
+    auto try_param = [&](int LaunchCfg::*field, std::initializer_list<int> values) -> int {
+        const int keep = cur.*field;
+        int best_v = keep;
+        for (int v : values) {
+            if (v == keep) continue;
+            cur.*field = v;
+            const float tv = trial(cur);
+            if (tv < 0) return (int)tv;
+            if (tv < best_ms) { best_ms = tv; best_v = v; }
+        }
+        cur.*field = best_v;
+        return BG3_OK;
+    };
+    int rc;
+    if (thick && (rc = try_param(&LaunchCfg::sweep_stages, {4, 6, 8}))) return rc;
+    if (mq > 4 && mq <= 64 && (rc = try_param(&LaunchCfg::thin_max_quads, {mq - 1, mq}))) return rc;
+    if ((thin || mq <= 64) && (rc = try_param(&LaunchCfg::thin_warps, {4, 8, 16}))) return rc;
+    if ((rc = try_param(&LaunchCfg::deliver_blocks, {152, 304, 608}))) return rc;
+    (void)growth;
+    return BG3_OK;
+}
+
+// Warm-up long enough to capture the step graph outside the timed region, then steps timed.
+static float time_steps(bg3_net *n, int32_t steps)
+{
+    if (bg3_step(n, GRAPH_STEPS + 3) != BG3_OK) return -1.0f;
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return -1.0f;
+    cudaEventRecord(a, n->stream);
+    int rc = bg3_step(n, steps);
+    cudaEventRecord(b, n->stream);
+    float ms = -1.0f;
+    if (rc == BG3_OK && cudaEventSynchronize(b) == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms < 0 ? -1.0f : ms / (float)steps;
+}
+
+int bg3_autotune(bg3_net *n, int32_t steps, int32_t tune_growth, bg3_launch_cfg *best,
+                 float *best_ms)
+{
+    if (!n || steps < 1) return BG3_EINVAL;
+    StateCopy sc;
+    int rc = state_save(n, sc);
+    if (rc) return rc;
+    const NetDev &h = n->h;
+    LaunchCfg cur = n->cfg;
+    auto trial = [&](const LaunchCfg &c) -> float {
+        if (state_load(n, sc) != BG3_OK) return -1.0f;
+        n->cfg = c;
+        drop_graph(n);
+        return time_steps(n, steps);
+    };
+    float ms = 0.0f;
+    rc = tune(cur, !bg3::sweep_is_thin(h, cur), bg3::sweep_is_thin(h, cur), h.Mq, false, trial, ms);
+    if (rc == BG3_OK && tune_growth) {
+        // the overlap pass: one growth pass per candidate block size from the saved state
+        float best_g = -1.0f;
+        int best_t = cur.growth_threads;
+        for (int t : {128, 256, 512}) {
+            if (state_load(n, sc) != BG3_OK) { rc = BG3_ECUDA; break; }
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, n->stream);
+            bg3::launch_growth(h, n->d, 0, t, n->stream);
+            cudaEventRecord(b, n->stream);
+            float g = -1.0f;
+            if (cudaEventSynchronize(b) == cudaSuccess) cudaEventElapsedTime(&g, a, b);
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            if (g >= 0 && (best_g < 0 || g < best_g)) { best_g = g; best_t = t; }
+        }
+        cur.growth_threads = best_t;
+    }
+    int rc2 = state_load(n, sc);
+    state_free(sc);
+    n->cfg = cur;
+    drop_graph(n);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (best) *best = cfg_to(cur);
+    if (best_ms) *best_ms = ms;
+    return BG3_OK;
+}
+
+static float time_batch_steps(bg3_batch *b, int32_t steps)
+{
+    if (bg3_batch_step(b, GRAPH_STEPS + 3) != BG3_OK) return -1.0f;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1.0f;
+    cudaEventRecord(e0, b->stream);
+    int rc = bg3_batch_step(b, steps);
+    cudaEventRecord(e1, b->stream);
+    float ms = -1.0f;
+    if (rc == BG3_OK && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms < 0 ? -1.0f : ms / (float)steps;
+}
+
+int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float *best_ms)
+{
+    if (!b || steps < 1) return BG3_EINVAL;
+    std::vector<StateCopy> sc(b->nets.size());
+    int rc = BG3_OK;
+    for (size_t k = 0; k < b->nets.size() && rc == BG3_OK; k++) rc = state_save(b->nets[k], sc[k]);
+    bool thick = false, thin = false;
+    int mq = 1 << 30;
+    for (bg3_net *n : b->nets) {
+        if (bg3::sweep_is_thin(n->h, b->cfg)) thin = true;
+        else thick = true;
+        mq = std::min(mq, n->h.Mq);
+    }
+    LaunchCfg cur = b->cfg;
+    auto trial = [&](const LaunchCfg &c) -> float {
+        for (size_t k = 0; k < b->nets.size(); k++)
+            if (state_load(b->nets[k], sc[k]) != BG3_OK) return -1.0f;
+        const bool split = b->cfg.thin_max_quads != c.thin_max_quads;
+        b->cfg = c;
+        if (split && batch_refresh(b) != BG3_OK) return -1.0f;
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        return time_batch_steps(b, steps);
+    };
+    float ms = 0.0f;
+    if (rc == BG3_OK) rc = tune(cur, thick, thin, thin ? 1 << 30 : mq, false, trial, ms);
+    int rc2 = BG3_OK;
+    for (size_t k = 0; k < b->nets.size(); k++) {
+        if (sc[k].buf && state_load(b->nets[k], sc[k]) != BG3_OK) rc2 = BG3_ECUDA;
+        state_free(sc[k]);
+    }
+    b->cfg = cur;
+    int rc3 = batch_refresh(b);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (rc3) return rc3;
+    if (best) *best = cfg_to(cur);
+    if (best_ms) *best_ms = ms;
+    return BG3_OK;
+}

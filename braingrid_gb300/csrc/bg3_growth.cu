@@ -83,7 +83,7 @@ __global__ void k_growth_existing(const NetDev *nets)
 
 // New synapses (ConnGrowth.cpp:441-454, AllSynapses::addSynapse :357-377, create* of
 // AllSpikingSynapses.cpp:192-240 / AllDSSynapses.cpp:180-218).  One CTA per destination.
-constexpr int ADD_THREADS = 256;
+template <int ADD_THREADS>
 __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
 {
     const NetDev &n = nets[0];
@@ -262,14 +262,16 @@ __global__ void k_record_epoch(const NetDev *nets, int epoch, bool growth)
     n.spikeCount[i] = 0;
 }
 
-void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, cudaStream_t s)
+void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, int add_threads, cudaStream_t s)
 {
     int nb = (h.N + 255) / 256;
     k_growth_radii<<<nb, 256, 0, s>>>(d_net);
     int sb = 152 * 8;
     k_growth_existing<<<sb, 256, 0, s>>>(d_net);
     size_t smem = (size_t)((h.N + 31) / 32) * sizeof(uint32_t);
-    k_growth_add<<<h.N, ADD_THREADS, smem, s>>>(d_net);
+    if (add_threads == 128) k_growth_add<128><<<h.N, 128, smem, s>>>(d_net);
+    else if (add_threads == 512) k_growth_add<512><<<h.N, 512, smem, s>>>(d_net);
+    else k_growth_add<256><<<h.N, 256, smem, s>>>(d_net);
     k_out_zero<<<nb, 256, 0, s>>>(d_net);
     k_out_count<<<sb, 256, 0, s>>>(d_net);
     k_out_scan<<<1, 1024, 0, s>>>(d_net);

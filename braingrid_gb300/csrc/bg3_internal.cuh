@@ -56,6 +56,17 @@ struct __align__(32) EvSlot {
     uint32_t pad1, pad2;
 };
 
+// Launch configuration of the step and growth kernels (bg3_launch_cfg of the C-ABI; chosen by
+// the autotuner or set by the caller).
+struct LaunchCfg {
+    int32_t sweep_stages;     // chunks in flight per TMA sweep tile: 4, 6 or 8
+    int32_t thin_max_quads;   // networks with at most this many row quads take the thin sweep
+    int32_t thin_warps;       // warps per block of the thin sweep (1 .. 32)
+    int32_t deliver_blocks;   // blocks of the delivery grid (a batch shares 4x this out)
+    int32_t growth_threads;   // threads per block of the overlap pass: 128, 256 or 512
+};
+constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256};
+
 // plane position of slot (dest d, row k) and its inverse
 __host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Np)
 {
@@ -237,14 +248,94 @@ __device__ __forceinline__ float normal_device(uint32_t seed, unsigned long long
 
 __device__ __forceinline__ void set_err(const NetDev &n, uint32_t bit) { atomicOr(n.err, bit); }
 
-// ---- LIF neuron update (shared by the standalone kernels and the sweep epilogue) -------------
+// ---- exact float <-> double conversions on the integer pipe ---------------------------------
+// GB300's FP64 pipe is narrow and the Izhikevich update (which the reference evaluates partly in
+// double) is bound by it; its conversions are done with integer operations instead.  Both are
+// exact restatements of IEEE 754: widening a normal float only re-biases the exponent (+896) and
+// shifts the mantissa; narrowing rounds the 52-bit mantissa to 23 bits, to nearest, ties to even,
+// with the carry into the exponent.  Zero, subnormal, infinite and NaN inputs, and results
+// outside the normal float range, take the hardware conversion.
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const uint32_t lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float d2f_rn(double d)
+{
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e < 1 || e > 254) return (float)d;
+    // 52-bit mantissa m = [hi 20 bits][lo 32 bits]; keep the top 23, round on the other 29
+    const uint32_t mhi = hi & 0xfffffu;
+    uint32_t m23 = (mhi << 3) | (lo >> 29);
+    const uint32_t rest = lo & 0x1fffffffu;  // 29 dropped bits
+    const uint32_t half = 0x10000000u;
+    uint32_t bits = (hi & 0x80000000u) | ((uint32_t)e << 23) | m23;
+    if (rest > half || (rest == half && (m23 & 1u))) bits += 1u;  // may carry into the exponent
+    if (((bits >> 23) & 0xffu) == 0xffu) return (float)d;           // rounded up to infinity
+    return __uint_as_float(bits);
+}
+
+// ---- neuron update (shared by the standalone kernels and the sweep epilogues) ---------------
 enum { BR_REFRACTORY = 0, BR_FIRE = 1, BR_INTEGRATE = 2 };
 
-// AllLIFNeurons::advanceNeuron branch selection (Neurons/AllLIFNeurons.cpp:31-35).
-__device__ __forceinline__ int lif_branch(const NetDev &n, int i)
+// The values one neuron's update reads, loaded together with independent loads (neuron_load) so
+// that their latency overlaps other work — in the sweeps, the synapse loads of the same step.
+struct NeuronIn {
+    float Vm, Vthresh, Trefract, I0, Inoise, C1, C2;
+    int32_t refr;
+    float A, B, Cc, Dd, u, C3;          // Izhikevich
+    int32_t reg_shift;                  // regular input
+    float reg_value;
+    int32_t nisi;                       // Poisson input
+    uint32_t q;
+    float ipsr, idec;
+    uint8_t pmask, idelay;
+};
+
+__device__ __forceinline__ void neuron_load(const NetDev &n, int i, NeuronIn &x)
 {
-    if (n.refr[i] > 0) return BR_REFRACTORY;
-    if (n.Vm[i] >= n.Vthresh[i]) return BR_FIRE;
+    x.Vm = n.Vm[i];
+    x.Vthresh = n.Vthresh[i];
+    x.refr = n.refr[i];
+    x.Trefract = n.Trefract[i];
+    x.I0 = n.I0[i];
+    x.Inoise = n.Inoise[i];
+    x.C2 = n.C2[i];
+    if (n.neuron_kind == 1) {
+        x.A = n.Aconst[i];
+        x.B = n.Bconst[i];
+        x.Cc = n.Cconst[i];
+        x.Dd = n.Dconst[i];
+        x.u = n.u_izh[i];
+        x.C3 = n.C3[i];
+    } else {
+        x.C1 = n.C1[i];
+    }
+    if (n.input_kind == 1) {
+        x.reg_shift = n.reg_shift[i];
+        x.reg_value = n.reg_values[i];
+    } else if (n.input_kind == 2) {
+        x.pmask = n.pois_mask[i];
+        x.nisi = n.pois_nisi[i];
+        x.q = n.in_queue[i];
+        x.ipsr = n.in_psr[i];
+        x.idec = n.in_decay[i];
+        x.idelay = n.in_delay[i];
+    }
+}
+
+// AllLIFNeurons::advanceNeuron branch selection (Neurons/AllLIFNeurons.cpp:31-35; the same for
+// AllIZHNeurons, Neurons/AllIZHNeurons.cpp:577-583).
+__device__ __forceinline__ int neuron_branch(const NeuronIn &x)
+{
+    if (x.refr > 0) return BR_REFRACTORY;
+    if (x.Vm >= x.Vthresh) return BR_FIRE;
     return BR_INTEGRATE;
 }
 
@@ -254,12 +345,12 @@ __device__ __forceinline__ int lif_branch(const NetDev &n, int i)
 // summation point value passed in.  Each float operation rounds on its own (-fmad=false) and the
 // double promotions of the reference's expressions are kept.  Returns true when the neuron
 // fired.  The caller stores sp = 0 afterwards.
-__device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float sp, float noise,
-                                          unsigned long long t)
+__device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const NeuronIn &x, int br,
+                                             float sp, float noise, unsigned long long t)
 {
     const bool izh = n.neuron_kind == 1;
     if (br == BR_REFRACTORY) {
-        n.refr[i] = n.refr[i] - 1;
+        n.refr[i] = x.refr - 1;
         return false;
     }
     if (br == BR_FIRE) {
@@ -269,28 +360,28 @@ __device__ __forceinline__ bool lif_apply(const NetDev &n, int i, int br, float 
         cnt += 1;
         n.spikeCount[i] = cnt;
         if (cnt >= n.max_spikes) set_err(n, ERR_HISTORY_OVERFLOW);
-        n.refr[i] = (int)((double)(n.Trefract[i] / n.dt) + 0.5);
+        n.refr[i] = (int)((double)(x.Trefract / n.dt) + 0.5);
         if (izh) {
-            n.Vm[i] = (float)((double)n.Cconst[i] * 0.001);
-            n.u_izh[i] = n.u_izh[i] + n.Dconst[i];
+            n.Vm[i] = (float)((double)x.Cc * 0.001);
+            n.u_izh[i] = x.u + x.Dd;
         } else {
             n.Vm[i] = n.Vreset[i];
         }
         return true;
     }
-    sp = sp + n.I0[i];
-    sp = sp + noise * n.Inoise[i];
+    sp = sp + x.I0;
+    sp = sp + noise * x.Inoise;
     if (izh) {
         // Vm in mV; dv = C3 (0.04 v^2 + 5 v + 140 - u) evaluated in double, du = C3 a (b v - u)
-        const float Vint = n.Vm[i] * 1000.0f;
-        const float u = n.u_izh[i], C3 = n.C3[i];
-        const double vd = (double)Vint;
-        const float Vb = (float)(vd + (double)C3 * (0.04 * vd * vd + (double)(5.0f * Vint) +
-                                                    140.0 - (double)u));
-        n.u_izh[i] = u + C3 * n.Aconst[i] * (n.Bconst[i] * Vint - u);
-        n.Vm[i] = (float)((double)Vb * 0.001 + (double)(n.C2[i] * sp));
+        const float Vint = x.Vm * 1000.0f;
+        const float u = x.u, C3 = x.C3;
+        const double vd = f2d_exact(Vint);
+        const float Vb = d2f_rn(vd + f2d_exact(C3) * (0.04 * vd * vd + f2d_exact(5.0f * Vint) +
+                                                      140.0 - f2d_exact(u)));
+        n.u_izh[i] = u + C3 * x.A * (x.B * Vint - u);
+        n.Vm[i] = d2f_rn(f2d_exact(Vb) * 0.001 + f2d_exact(x.C2 * sp));
     } else {
-        n.Vm[i] = n.C1[i] * n.Vm[i] + n.C2[i] * sp;
+        n.Vm[i] = x.C1 * x.Vm + x.C2 * sp;
     }
     return false;
 }
@@ -323,23 +414,24 @@ __device__ __forceinline__ int32_t next_isi(const NetDev &n, int i)
 // HostSInputRegular::inputStimulus (Inputs/HostSInputRegular.cpp:59-80) and
 // HostSInputPoisson::inputStimulus (Inputs/HostSInputPoisson.cpp:60-94) for neuron i at step t:
 // returns the summation point after the input.
-__device__ __forceinline__ float input_apply(const NetDev &n, int i, unsigned long long t, float sp)
+__device__ __forceinline__ float input_apply(const NetDev &n, int i, const NeuronIn &x,
+                                             unsigned long long t, float sp)
 {
     if (n.input_kind == 1) {
         const int cyc = (int)(((unsigned long long)n.reg_c0 + (t - n.reg_t0)) % (unsigned long long)n.reg_cycle);
-        const int sh = n.reg_shift[i];
-        if (cyc >= sh && cyc < (sh + n.reg_dur) % n.reg_cycle) sp = sp + n.reg_values[i];
-    } else if (n.input_kind == 2 && n.pois_mask[i]) {
-        int32_t c = n.pois_nisi[i] - 1;
-        uint32_t q = n.in_queue[i];
+        const int sh = x.reg_shift;
+        if (cyc >= sh && cyc < (sh + n.reg_dur) % n.reg_cycle) sp = sp + x.reg_value;
+    } else if (n.input_kind == 2 && x.pmask) {
+        int32_t c = x.nisi - 1;
+        uint32_t q = x.q;
         if (c <= 0) {
-            q |= 1u << ((uint32_t)(t + n.in_delay[i]) & 31u);
+            q |= 1u << ((uint32_t)(t + x.idelay) & 31u);
             c = next_isi(n, i);
         }
         n.pois_nisi[i] = c;
         const uint32_t bit = 1u << ((uint32_t)t & 31u);
-        float psr = n.in_psr[i];
-        const float dec = n.in_decay[i];
+        float psr = x.ipsr;
+        const float dec = x.idec;
         if (q & bit) {
             q &= ~bit;
             EvSlot e = n.in_ev[i];

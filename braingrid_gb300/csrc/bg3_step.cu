@@ -94,9 +94,11 @@ __global__ void __launch_bounds__(256) k_neurons_device(const __grid_constant__ 
     unsigned long long t = *n.step;
     bool fired = false;
     if (i < n.N) {
-        int br = lif_branch(n, i);
+        NeuronIn x;
+        neuron_load(n, i, x);
+        const int br = neuron_branch(x);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = lif_apply(n, i, br, input_apply(n, i, t, n.sp[i]), noise, t);
+        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -117,7 +119,9 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__
     __syncthreads();
     for (int top = n.N - 1; top >= 0; top -= 1024) {
         int i = top - (int)threadIdx.x;
-        int br = (i >= 0) ? lif_branch(n, i) : BR_REFRACTORY;
+        NeuronIn x;
+        if (i >= 0) neuron_load(n, i, x);
+        int br = (i >= 0) ? neuron_branch(x) : BR_REFRACTORY;
         bool integ = (i >= 0) && br == BR_INTEGRATE;
         unsigned m = __ballot_sync(0xffffffffu, integ);
         int in_warp = __popc(m & ((1u << lane) - 1));
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__
                 if (pos < n.noise_len) noise = n.noise_buf[pos];
                 else set_err(n, ERR_NOISE_EXHAUSTED);
             }
-            fired = lif_apply(n, i, br, input_apply(n, i, t, n.sp[i]), noise, t);
+            fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
             n.sp[i] = 0.0f;
         }
         ring_push(n, t, fired, i);
@@ -518,9 +522,11 @@ __global__ void __launch_bounds__(256) k_neurons_device_batch(const NetDev *nets
     unsigned long long t = *n.step;
     bool fired = false;
     if (i < n.N) {
-        int br = lif_branch(n, i);
+        NeuronIn x;
+        neuron_load(n, i, x);
+        const int br = neuron_branch(x);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = lif_apply(n, i, br, input_apply(n, i, t, n.sp[i]), noise, t);
+        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -530,15 +536,18 @@ __global__ void __launch_bounds__(256) k_neurons_device_batch(const NetDev *nets
 constexpr int SW_DESTS = 32;   // dests per tile (one per lane)
 constexpr int SW_ROWS = 64;    // slot rows per TMA chunk
 constexpr int SW_QUADS = SW_ROWS / 4;
-constexpr int SW_STAGES = 6;   // chunks in flight per tile (63 KB: three CTAs per SM)
+
 constexpr int SW_SCALE_WARPS = 4;
 constexpr int SW_THREADS = 32 * (2 + SW_SCALE_WARPS);
 constexpr uint32_t SW_PSR_BYTES = SW_ROWS * SW_DESTS * 4;
 constexpr uint32_t SW_CLS_BYTES = SW_ROWS * SW_DESTS;
 constexpr uint32_t SW_CHUNK_BYTES = SW_PSR_BYTES + SW_CLS_BYTES;
 // dynamic shared memory: stages (psr | class), decay table, barriers; +128 for alignment
-constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4 +
-                           3 * SW_STAGES * 8 + 16 + 128;
+// ST chunks in flight per tile: 4 (42 KB, five CTAs per SM), 6 (63 KB, three), 8 (83 KB, two)
+constexpr size_t sw_smem(int st)
+{
+    return (size_t)st * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4 + 3 * (size_t)st * 8 + 16 + 128;
+}
 
 // AllSpikingSynapses::advanceSynapse's "psr *= decay" for every in-use synapse, and the
 // summation of AllSynapses::advanceSynapses (Synapses/AllSynapses.cpp:325-331):
@@ -557,17 +566,19 @@ constexpr size_t SW_SMEM = (size_t)SW_STAGES * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4
 // Every mbarrier wait is bounded (about 1 s); on expiry the error word is set and the CTA drains.
 // Tile epilogue: the sums go to the summation points or, with FUSE, straight into the neuron
 // update of step t + 1 (device noise); the network's last tile advances its step counter.
+// x: the dest's neuron values (neuron_load after pdl_wait), noise: its N(0,1) draw for step t+1.
 template <bool FUSE>
 __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid, float acc,
-                                             unsigned long long t, int lane)
+                                             unsigned long long t, int lane, const NeuronIn &x,
+                                             float noise)
 {
     if (FUSE) {
         const unsigned long long t1 = t + 1;
         bool fired = false;
         if (valid) {
-            int br = lif_branch(n, d);
-            float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t1, d) : 0.0f;
-            fired = lif_apply(n, d, br, input_apply(n, d, t1, acc), noise, t1);
+            const int br = neuron_branch(x);
+            fired = neuron_apply(n, d, x, br, input_apply(n, d, x, t1, acc),
+                                 br == BR_INTEGRATE ? noise : 0.0f, t1);
             n.sp[d] = 0.0f;
         }
         ring_push(n, t1, fired, d);
@@ -586,7 +597,7 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
     }
 }
 
-template <bool FUSE>
+template <bool FUSE, int SW_STAGES>
 __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *tm_psr,
                                            const CUtensorMap *tm_cls, const int tile,
                                            uint8_t *smem_raw)
@@ -672,6 +683,12 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
     }
 
     // ------------------------------------------------------------------------------- sum warp
+    NeuronIn x;
+    float noise = 0.0f;
+    if (FUSE && valid) {
+        neuron_load(n, d, x);  // in flight while the chunks stream
+        noise = normal_device(n.noise_seed, t + 1, d);
+    }
     float acc = 0.0f;
     int done = 0;
     for (int c = 0; c < nch; c++) {
@@ -715,7 +732,7 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         __syncwarp();
     }
 
-    sweep_finish<FUSE>(n, d, valid, acc, t, lane);
+    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise);
 }
 
 // Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
@@ -735,6 +752,12 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
     pdl_wait();  // spike delivery for this step has finished writing psr
     pdl_trigger();
     const unsigned long long t = *n.step;
+    NeuronIn x;
+    float noise = 0.0f;
+    if (FUSE && valid) {
+        neuron_load(n, d, x);  // in flight with the row loads below
+        noise = normal_device(n.noise_seed, t + 1, d);
+    }
     float4 *P = reinterpret_cast<float4 *>(n.psr);
     const uint32_t *C = reinterpret_cast<const uint32_t *>(n.dcls);
     const size_t Np = (size_t)n.Np;
@@ -764,56 +787,52 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
             }
         }
     }
-    sweep_finish<FUSE>(n, d, valid, acc, t, lane);
+    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise);
 }
 
-template <int SYN, bool FUSE>
+template <int SYN, bool FUSE, int ST>
 __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ NetDev n,
                                                       const __grid_constant__ CUtensorMap tm_psr,
                                                       const __grid_constant__ CUtensorMap tm_cls)
 {
     extern __shared__ uint8_t smem_raw[];
-    sweep_tile<FUSE>(n, &tm_psr, &tm_cls, blockIdx.x, smem_raw);
+    sweep_tile<FUSE, ST>(n, &tm_psr, &tm_cls, blockIdx.x, smem_raw);
 }
 
 // Batched form: one launch sweeps every tile of every network of a batch.  tiles[b] = (network,
 // tile); maps holds each network's two tensor maps (psr, class) in global memory.
-template <bool FUSE>
+template <bool FUSE, int ST>
 __global__ void __launch_bounds__(SW_THREADS) k_sweep_batch(const NetDev *nets,
                                                             const CUtensorMap *maps,
                                                             const int2 *tiles)
 {
     extern __shared__ uint8_t smem_raw[];
     const int2 tr = tiles[blockIdx.x];
-    sweep_tile<FUSE>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
+    sweep_tile<FUSE, ST>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
 }
 
-constexpr int THIN_QUADS = 16;   // networks with max_syn <= 64 take the thin sweep
-constexpr int THIN_WARPS = 8;
-
 template <bool FUSE>
-__global__ void __launch_bounds__(32 * THIN_WARPS) k_sweep_thin(const __grid_constant__ NetDev n)
+__global__ void __launch_bounds__(1024) k_sweep_thin(const __grid_constant__ NetDev n)
 {
-    const int tile = blockIdx.x * THIN_WARPS + (threadIdx.x >> 5);
+    const int tile = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
     if (tile >= n.ntiles) return;
     sweep_thin_tile<FUSE>(n, tile);
 }
 
 // Batched thin tiles: tiles[i] = (network, tile), one warp each.
 template <bool FUSE>
-__global__ void __launch_bounds__(32 * THIN_WARPS) k_sweep_thin_batch(const NetDev *nets,
-                                                                      const int2 *tiles, int count)
+__global__ void __launch_bounds__(1024) k_sweep_thin_batch(const NetDev *nets, const int2 *tiles,
+                                                           int count)
 {
-    const int i = blockIdx.x * THIN_WARPS + (threadIdx.x >> 5);
+    const int i = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
     if (i >= count) return;
     const int2 tr = tiles[i];
     sweep_thin_tile<FUSE>(nets[tr.x], tr.y);
 }
 
-bool sweep_is_thin(const NetDev &h) { return h.Mq <= THIN_QUADS; }
+bool sweep_is_thin(const NetDev &h, const LaunchCfg &c) { return h.Mq <= c.thin_max_quads; }
 
 // ---- launchers -------------------------------------------------------------------------------
-int deliver_blocks() { return 304; }
 
 void launch_neurons(const NetDev &h, cudaStream_t s)
 {
@@ -841,41 +860,61 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, int block, size_t smem
 }
 
 // Spike arrivals of the step, then (STDP kinds) the post-spike learning pass.
-void launch_deliver(const NetDev &h, cudaStream_t s)
+void launch_deliver(const NetDev &h, const LaunchCfg &c, cudaStream_t s)
 {
+    const int g = c.deliver_blocks;
     switch (h.syn_kind) {
-    case 1: launch_pdl(k_deliver<1>, deliver_blocks(), 256, 0, s, h); break;
-    case 2: launch_pdl(k_deliver<2>, deliver_blocks(), 256, 0, s, h); break;
-    case 3: launch_pdl(k_deliver<3>, deliver_blocks(), 256, 0, s, h); break;
-    default: launch_pdl(k_deliver<0>, deliver_blocks(), 256, 0, s, h); break;
+    case 1: launch_pdl(k_deliver<1>, g, 256, 0, s, h); break;
+    case 2: launch_pdl(k_deliver<2>, g, 256, 0, s, h); break;
+    case 3: launch_pdl(k_deliver<3>, g, 256, 0, s, h); break;
+    default: launch_pdl(k_deliver<0>, g, 256, 0, s, h); break;
     }
-    if (h.syn_kind >= 2) launch_pdl(k_stdp_post, deliver_blocks(), 256, 0, s, h);
+    if (h.syn_kind >= 2) launch_pdl(k_stdp_post, g, 256, 0, s, h);
 }
 
-template <int SYN, bool FUSE>
+template <typename K>
+static void allow_smem(K kern, int st)
+{
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sw_smem(st));
+}
+
+template <int SYN, bool FUSE, int ST>
 static void launch_sweep_t(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, cudaStream_t s)
 {
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_sweep<SYN, FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
+        allow_smem(k_sweep<SYN, FUSE, ST>, ST);
         attr_set = true;
     }
-    launch_pdl(k_sweep<SYN, FUSE>, h.ntiles, SW_THREADS, SW_SMEM, s, h, tp, tc);
+    launch_pdl(k_sweep<SYN, FUSE, ST>, h.ntiles, SW_THREADS, sw_smem(ST), s, h, tp, tc);
+}
+
+template <bool FUSE, int ST>
+static void launch_sweep_batch_thick(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles,
+                                     int n_thick, cudaStream_t s)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        allow_smem(k_sweep_batch<FUSE, ST>, ST);
+        attr_set = true;
+    }
+    launch_pdl(k_sweep_batch<FUSE, ST>, n_thick, SW_THREADS, sw_smem(ST), s, nets, maps, tiles);
 }
 
 template <bool FUSE>
 static void launch_sweep_batch_t(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles,
-                                 int n_thick, int n_thin, cudaStream_t s)
+                                 int n_thick, int n_thin, const LaunchCfg &c, cudaStream_t s)
 {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_sweep_batch<FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
-        attr_set = true;
+    if (n_thick > 0) {
+        if (c.sweep_stages == 4) launch_sweep_batch_thick<FUSE, 4>(nets, maps, tiles, n_thick, s);
+        else if (c.sweep_stages == 8) launch_sweep_batch_thick<FUSE, 8>(nets, maps, tiles, n_thick, s);
+        else launch_sweep_batch_thick<FUSE, 6>(nets, maps, tiles, n_thick, s);
     }
-    if (n_thick > 0) launch_pdl(k_sweep_batch<FUSE>, n_thick, SW_THREADS, SW_SMEM, s, nets, maps, tiles);
-    if (n_thin > 0)
-        launch_pdl(k_sweep_thin_batch<FUSE>, (n_thin + THIN_WARPS - 1) / THIN_WARPS, 32 * THIN_WARPS,
-                   0, s, nets, (const int2 *)(tiles + n_thick), n_thin);
+    if (n_thin > 0) {
+        const int w = c.thin_warps;
+        launch_pdl(k_sweep_thin_batch<FUSE>, (n_thin + w - 1) / w, 32 * w, 0, s, nets,
+                   (const int2 *)(tiles + n_thick), n_thin);
+    }
 }
 
 void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s)
@@ -883,11 +922,12 @@ void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t
     k_neurons_device_batch<<<dim3((max_n + 255) / 256, count), 256, 0, s>>>(nets);
 }
 
-void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStream_t s)
+void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, const LaunchCfg &c,
+                          cudaStream_t s)
 {
-    // per network: a plain network's grid shared out over the batch (blocks without items
-    // exit at once, so a quiet network costs little)
-    const int per_net = std::max(2, std::min(deliver_blocks(), 1216 / std::max(count, 1)));
+    // per network: four plain grids shared out over the batch (blocks without items exit at
+    // once, so a quiet network costs little)
+    const int per_net = std::max(2, std::min(c.deliver_blocks, 4 * c.deliver_blocks / std::max(count, 1)));
     const dim3 grid(per_net, count);
     switch (syn_kind) {
     case 1: launch_pdl(k_deliver_batch<1>, grid, 256, 0, s, nets); break;
@@ -899,28 +939,34 @@ void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, cudaStrea
 }
 
 void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int n_thick,
-                        int n_thin, bool fuse, cudaStream_t s)
+                        int n_thin, bool fuse, const LaunchCfg &c, cudaStream_t s)
 {
-    if (fuse) launch_sweep_batch_t<true>(nets, maps, tiles, n_thick, n_thin, s);
-    else launch_sweep_batch_t<false>(nets, maps, tiles, n_thick, n_thin, s);
+    if (fuse) launch_sweep_batch_t<true>(nets, maps, tiles, n_thick, n_thin, c, s);
+    else launch_sweep_batch_t<false>(nets, maps, tiles, n_thick, n_thin, c, s);
+}
+
+template <int SYN, bool FUSE>
+static void launch_sweep_st(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
+                            const LaunchCfg &c, cudaStream_t s)
+{
+    if (c.sweep_stages == 4) launch_sweep_t<SYN, FUSE, 4>(h, tp, tc, s);
+    else if (c.sweep_stages == 8) launch_sweep_t<SYN, FUSE, 8>(h, tp, tc, s);
+    else launch_sweep_t<SYN, FUSE, 6>(h, tp, tc, s);
 }
 
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
-                  cudaStream_t s)
+                  const LaunchCfg &c, cudaStream_t s)
 {
-    if (sweep_is_thin(h)) {
-        const int blocks = (h.ntiles + THIN_WARPS - 1) / THIN_WARPS;
-        if (fuse) launch_pdl(k_sweep_thin<true>, blocks, 32 * THIN_WARPS, 0, s, h);
-        else launch_pdl(k_sweep_thin<false>, blocks, 32 * THIN_WARPS, 0, s, h);
+    if (sweep_is_thin(h, c)) {
+        const int w = c.thin_warps;
+        const int blocks = (h.ntiles + w - 1) / w;
+        if (fuse) launch_pdl(k_sweep_thin<true>, blocks, 32 * w, 0, s, h);
+        else launch_pdl(k_sweep_thin<false>, blocks, 32 * w, 0, s, h);
         return;
     }
-    if (h.syn_kind == 1 || h.syn_kind == 3) {
-        if (fuse) launch_sweep_t<1, true>(h, tp, tc, s);
-        else launch_sweep_t<1, false>(h, tp, tc, s);
-    } else {
-        if (fuse) launch_sweep_t<0, true>(h, tp, tc, s);
-        else launch_sweep_t<0, false>(h, tp, tc, s);
-    }
+    // the synapse kind does not change the sweep: one instantiation serves all kinds
+    if (fuse) launch_sweep_st<1, true>(h, tp, tc, c, s);
+    else launch_sweep_st<1, false>(h, tp, tc, c, s);
 }
 
 }  // namespace bg3

@@ -60,6 +60,14 @@ class StdpConstants(ctypes.Structure):
                [("useFroemkeDanSTDP", ctypes.c_int32 * 4)]
 
 
+class LaunchCfg(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int32) for k in ("sweep_stages", "thin_max_quads", "thin_warps",
+                                              "deliver_blocks", "growth_threads")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SynArrays(ctypes.Structure):
     _fields_ = [("in_use", c_u8p)] + \
                [(k, c_i32p) for k in ("src", "type", "delayIdx", "total_delay")] + \
@@ -132,6 +140,14 @@ def load(build_if_missing=True):
         "bg3_set_stdp_constants": ([vp, ctypes.POINTER(StdpConstants)], ctypes.c_int),
         "bg3_set_stdp_arithmetic": ([vp, ctypes.c_int], ctypes.c_int),
         "bg3_epoch_record": ([vp], ctypes.c_int),
+        "bg3_get_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
+        "bg3_set_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
+        "bg3_batch_get_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
+        "bg3_batch_set_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
+        "bg3_autotune": ([vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(LaunchCfg),
+                          ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+        "bg3_batch_autotune": ([vp, ctypes.c_int32, ctypes.POINTER(LaunchCfg),
+                                ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "bg3_net_footprint": ([ctypes.POINTER(NetDesc)], ctypes.c_int64),
         "bg3_net_bytes": ([vp], ctypes.c_uint64),
         "bg3_upload_layout": ([vp, c_f32p, c_f32p, c_i32p], ctypes.c_int),
@@ -403,6 +419,25 @@ class Network:
     def growth(self, epoch):
         check(self.L.bg3_epoch_growth(self.h, int(epoch)), "bg3_epoch_growth")
 
+    # launch configuration
+    @property
+    def launch(self):
+        c = LaunchCfg()
+        check(self.L.bg3_get_launch(self.h, ctypes.byref(c)), "bg3_get_launch")
+        return c.as_dict()
+
+    def set_launch(self, **kw):
+        c = LaunchCfg(**dict(self.launch, **kw))
+        check(self.L.bg3_set_launch(self.h, ctypes.byref(c)), "bg3_set_launch")
+
+    def autotune(self, steps_per_trial=200, growth=False):
+        """Times launch configurations on this network's state (left unchanged) and keeps the
+        fastest; returns (config dict, ms per step)."""
+        c, ms = LaunchCfg(), ctypes.c_float()
+        check(self.L.bg3_autotune(self.h, int(steps_per_trial), 1 if growth else 0,
+                                  ctypes.byref(c), ctypes.byref(ms)), "bg3_autotune")
+        return c.as_dict(), ms.value
+
     @property
     def device_bytes(self):
         return int(self.L.bg3_net_bytes(self.h))
@@ -546,6 +581,23 @@ class Batch:
     @property
     def launches(self):
         return int(self.L.bg3_batch_launches(self.h))
+
+    @property
+    def launch(self):
+        c = LaunchCfg()
+        check(self.L.bg3_batch_get_launch(self.h, ctypes.byref(c)), "bg3_batch_get_launch")
+        return c.as_dict()
+
+    def set_launch(self, **kw):
+        c = LaunchCfg(**dict(self.launch, **kw))
+        check(self.L.bg3_batch_set_launch(self.h, ctypes.byref(c)), "bg3_batch_set_launch")
+
+    def autotune(self, steps_per_trial=100):
+        """Times launch configurations on the members' state (left unchanged); keeps the fastest."""
+        c, ms = LaunchCfg(), ctypes.c_float()
+        check(self.L.bg3_batch_autotune(self.h, int(steps_per_trial), ctypes.byref(c),
+                                        ctypes.byref(ms)), "bg3_batch_autotune")
+        return c.as_dict(), ms.value
 
     def bench_steps(self, nsteps, flush_bytes=0):
         ms = np.zeros(max(int(nsteps), 1), np.float32)

@@ -325,6 +325,32 @@ int bg3_batch_bench_steps(bg3_batch *batch, int64_t nsteps, int64_t flush_bytes,
 int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *step_ms,
                     float *kernel_ms);
 
+/* ---- launch configuration and autotuning (no counterpart in the reference) ----------------- */
+typedef struct {
+    int32_t sweep_stages;     /* chunks in flight per TMA sweep tile: 4, 6 or 8 (default 6)          */
+    int32_t thin_max_quads;   /* networks with at most 4 x this many slots per neuron take the thin
+                                 sweep, one warp per 32 dests: 1 .. 4096 (default 16)               */
+    int32_t thin_warps;       /* warps per block of the thin sweep: 1 .. 32 (default 8)              */
+    int32_t deliver_blocks;   /* blocks of the spike-delivery grid: 1 .. 65535 (default 304); a
+                                 batch shares four such grids out over its networks                 */
+    int32_t growth_threads;   /* threads per block of the overlap pass: 128, 256 or 512 (256)       */
+} bg3_launch_cfg;
+int bg3_get_launch(bg3_net *net, bg3_launch_cfg *cfg);
+int bg3_set_launch(bg3_net *net, const bg3_launch_cfg *cfg);
+int bg3_batch_get_launch(bg3_batch *batch, bg3_launch_cfg *cfg);
+int bg3_batch_set_launch(bg3_batch *batch, const bg3_launch_cfg *cfg);
+/* Chooses the launch configuration by timing candidates on the handle's own state: the device
+ * state is copied aside, each candidate runs from that copy (warm-up steps, then
+ * steps_per_trial timed steps; with tune_growth also one growth pass for the overlap block
+ * size), one parameter at a time, and the state is put back, so the network is afterwards
+ * exactly as before.  The fastest configuration is kept and returned with its time per step.
+ * (Each trial first runs 35 untimed steps, so that its CUDA graph is captured before timing.)
+ * Needs free device memory for one copy of the state (BG3_ENOMEM otherwise). */
+int bg3_autotune(bg3_net *net, int32_t steps_per_trial, int32_t tune_growth, bg3_launch_cfg *best,
+                 float *best_ms_per_step);
+int bg3_batch_autotune(bg3_batch *batch, int32_t steps_per_trial, bg3_launch_cfg *best,
+                       float *best_ms_per_step);
+
 #ifdef __cplusplus
 }
 #endif
