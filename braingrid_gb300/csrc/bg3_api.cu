@@ -19,8 +19,8 @@
 namespace bg3 {
 void launch_neurons(const NetDev &h, cudaStream_t s);
 void launch_deliver(const NetDev &h, const LaunchCfg &c, cudaStream_t s);
-void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
-                  const LaunchCfg &c,
+void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
+                  const CUtensorMap &tp16, const CUtensorMap &tc16, bool fuse, const LaunchCfg &c,
                   cudaStream_t s);
 void launch_neurons_batch(const NetDev *nets, int count, int max_n, cudaStream_t s);
 void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, const LaunchCfg &c,
@@ -45,7 +45,7 @@ struct bg3_net {
     cudaStream_t stream = nullptr;
     std::vector<std::pair<void *, size_t>> allocs;  // device allocations and their sizes
     LaunchCfg cfg = LAUNCH_DEFAULT;
-    CUtensorMap tm_psr, tm_cls;
+    CUtensorMap tm_psr, tm_cls, tm_psr16, tm_cls16;  // 32- and 16-dest sweep boxes
     std::vector<float> dtab;  // decay factor per decay class
     std::vector<int> ltab;    // delay per delay class
     long long noise_cap = 0;
@@ -293,22 +293,25 @@ static int make_tensor_maps(bg3_net *n)
         return BG3_ECUDA;
     auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
     const NetDev &h = n->h;
-    // psr: [Mq quads][N dests x 4 rows] floats, box 16 quads x (32 dests x 4 rows)
-    // class: [Mq quads][N dests] 32-bit words (4 one-byte classes), box 16 quads x 32 dests
-    cuuint64_t dims_f[2] = {(cuuint64_t)h.N * 4, (cuuint64_t)std::max(h.Mq, 1)};
-    cuuint64_t dims_b[2] = {(cuuint64_t)h.N, (cuuint64_t)std::max(h.Mq, 1)};
-    cuuint32_t box_f[2] = {128, 16}, box_b[2] = {32, 16};
-    cuuint32_t es[2] = {1, 1};
-    cuuint64_t st_f[1] = {(cuuint64_t)h.Np * 16};
-    cuuint64_t st_b[1] = {(cuuint64_t)h.Np * 4};
-    if (encode(&n->tm_psr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, h.psr, dims_f, st_f, box_f, es,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return BG3_ECUDA;
-    if (encode(&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, h.dcls, dims_b, st_b, box_b, es,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return BG3_ECUDA;
+    // tile-major planes as 3-D tensors [tiles][Mq quads][32 dests x 4 rows] (psr, floats) and
+    // [tiles][Mq quads][32 dests] (classes, 32-bit words of four bytes); a box is 16 quads of one
+    // tile (32 or 16 dests); quads past Mq read as zero and are not written
+    const cuuint64_t T = (cuuint64_t)h.ntiles, Q = (cuuint64_t)std::max(h.Mq, 1);
+    cuuint64_t dims_f[3] = {128, Q, T}, dims_b[3] = {32, Q, T};
+    cuuint64_t st_f[2] = {512, Q * 512}, st_b[2] = {128, Q * 128};
+    cuuint32_t box_f[3] = {128, 16, 1}, box_b[3] = {32, 16, 1};
+    cuuint32_t box_f16[3] = {64, 16, 1}, box_b16[3] = {16, 16, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    struct { CUtensorMap *m; CUtensorMapDataType ty; void *base; cuuint64_t *dims, *st; cuuint32_t *box; } maps[4] = {
+        {&n->tm_psr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, h.psr, dims_f, st_f, box_f},
+        {&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT32, h.dcls, dims_b, st_b, box_b},
+        {&n->tm_psr16, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, h.psr, dims_f, st_f, box_f16},
+        {&n->tm_cls16, CU_TENSOR_MAP_DATA_TYPE_UINT32, h.dcls, dims_b, st_b, box_b16}};
+    for (auto &m : maps)
+        if (encode(m.m, m.ty, 3, m.base, m.dims, m.st, m.box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return BG3_ECUDA;
     return BG3_OK;
 }
 
@@ -600,7 +603,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
         if (a->counts && a->counts[d] != c) return BG3_EINVAL;
         count[d] = (uint32_t)c;
         for (size_t k = 0; k < c; k++) {
-            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
+            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)n->h.Mq);
             int D = a->total_delay[i], di = a->delayIdx[i];
             if (a->src[i] < 0 || (size_t)a->src[i] >= N || a->type[i] < 0 || a->type[i] > 3 ||
                 D < 1 || D > 31 || di < 0 || di > 31)
@@ -644,7 +647,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
     }
     for (size_t d = 0; d < N; d++) {
         for (size_t k = 0; k < count[d]; k++) {
-            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
+            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)n->h.Mq);
             int D = a->total_delay[i], di = a->delayIdx[i];
             uint32_t f = fired[a->src[i]], q = a->delayQueue[i];
             for (int j = 0; j < D; j++) {
@@ -718,7 +721,7 @@ int bg3_upload_weights(bg3_net *n, const float *Wref)
     if ((rc = d2h(n, count.data(), n->h.count, N)) || (rc = d2h(n, ev.data(), n->h.ev, S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     for (size_t d = 0; d < N; d++)
-        for (size_t k = 0; k < count[d]; k++) ev[slot_pos((int)k, (int)d, (int)Np)].W = Wref[d * M + k];
+        for (size_t k = 0; k < count[d]; k++) ev[slot_pos((int)k, (int)d, (int)n->h.Mq)].W = Wref[d * M + k];
     if ((rc = h2d(n, n->h.ev, ev.data(), S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
@@ -917,7 +920,7 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         for (int64_t s = 0; s < nsteps; s++) {
             bg3::launch_neurons(h, n->stream);
             bg3::launch_deliver(h, n->cfg, n->stream);
-            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->cfg, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, false, n->cfg, n->stream);
         }
         n->launches += (1 + step_kernels(h.syn_kind)) * nsteps;
         CK(cudaGetLastError());
@@ -930,7 +933,7 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         CK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < GRAPH_STEPS; i++) {
             bg3::launch_deliver(h, n->cfg, n->stream);
-            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->cfg, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, true, n->cfg, n->stream);
         }
         CK(cudaStreamEndCapture(n->stream, &g));
         cudaError_t e = cudaGraphInstantiate(&n->graph, g, 0);
@@ -943,10 +946,10 @@ static int run_steps(bg3_net *n, int64_t nsteps)
     }
     for (int64_t i = 0; i < interior; i++) {
         bg3::launch_deliver(h, n->cfg, n->stream);
-        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, true, n->cfg, n->stream);
+        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, true, n->cfg, n->stream);
     }
     bg3::launch_deliver(h, n->cfg, n->stream);
-    bg3::launch_sweep(h, n->tm_psr, n->tm_cls, false, n->cfg, n->stream);
+    bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, false, n->cfg, n->stream);
     n->launches += 1 + step_kernels(h.syn_kind) * nsteps;
     CK(cudaGetLastError());
     return BG3_OK;
@@ -1071,7 +1074,7 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
     for (size_t d = 0; d < N; d++) {
         if (a->counts) a->counts[d] = count[d];
         for (size_t k = 0; k < M; k++) {
-            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
+            size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)n->h.Mq);
             bool used = k < count[d];
             if (a->in_use) a->in_use[i] = used ? 1 : 0;
             if (!used) continue;
@@ -1204,7 +1207,7 @@ int bg3_download_stdp(bg3_net *n, bg3_stdp_arrays *a)
     CK(cudaStreamSynchronize(n->stream));
     for (size_t d = 0; d < N; d++) {
         for (size_t k = 0; k < M && k < count[d]; k++) {
-            const size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)Np);
+            const size_t i = d * M + k, p = slot_pos((int)k, (int)d, (int)n->h.Mq);
             const StdpConst &c = h.stdp[st[p] & 3];
             if (a->delayQueuePost) a->delayQueuePost[i] = 0;
             if (a->delayIdxPost) a->delayIdxPost[i] = (int32_t)(((uint32_t)step - ev[p].born) & 31u);
@@ -1263,7 +1266,7 @@ int bg3_download_maps(bg3_net *n, bg3_index_maps *m)
         for (size_t c = 0; c < C; c++)
             for (uint32_t j = 0; j < oc[c * N + i]; j++) {
                 int k, d;
-                pos_slot(om[ob[c * N + i] + j], (int)Np, k, d);
+                pos_slot(om[ob[c * N + i] + j], (int)n->h.Mq, k, d);
                 ids.push_back((uint32_t)((size_t)d * M + (size_t)k));
             }
         std::sort(ids.begin(), ids.end());
@@ -1539,7 +1542,7 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
         if (inject) bg3::launch_neurons(h, n->stream);
         bg3::launch_deliver(h, n->cfg, n->stream);
         if (kernel_ms) CK(cudaEventRecord(e[1], n->stream));
-        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, !inject && !last, n->cfg, n->stream);
+        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, !inject && !last, n->cfg, n->stream);
         CK(cudaEventRecord(e[2], n->stream));
     }
     n->launches += (step_kernels(h.syn_kind) + (inject ? 1 : 0)) * nsteps + (inject ? 0 : 1);
@@ -1625,11 +1628,13 @@ static bool cfg_valid(const bg3_launch_cfg *c)
     return c && (c->sweep_stages == 4 || c->sweep_stages == 6 || c->sweep_stages == 8) &&
            c->thin_max_quads >= 1 && c->thin_max_quads <= 4096 && c->thin_warps >= 1 &&
            c->thin_warps <= 32 && c->deliver_blocks >= 1 && c->deliver_blocks <= 65535 &&
-           (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512);
+           (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512) &&
+           (c->sweep_dests == 16 || c->sweep_dests == 32);
 }
 static LaunchCfg cfg_from(const bg3_launch_cfg &c)
 {
-    return LaunchCfg{c.sweep_stages, c.thin_max_quads, c.thin_warps, c.deliver_blocks, c.growth_threads};
+    return LaunchCfg{c.sweep_stages, c.thin_max_quads, c.thin_warps, c.deliver_blocks,
+                     c.growth_threads, c.sweep_dests};
 }
 static bg3_launch_cfg cfg_to(const LaunchCfg &c)
 {
@@ -1639,6 +1644,7 @@ static bg3_launch_cfg cfg_to(const LaunchCfg &c)
     o.thin_warps = c.thin_warps;
     o.deliver_blocks = c.deliver_blocks;
     o.growth_threads = c.growth_threads;
+    o.sweep_dests = c.sweep_dests;
     return o;
 }
 
@@ -1722,7 +1728,7 @@ static void state_free(StateCopy &sc)
 
 // Coordinate search over the launch parameters; trial(cfg) returns a time (ms) or < 0 on error.
 template <typename Trial>
-static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool growth, Trial trial, float &best_ms)
+static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool batch, Trial trial, float &best_ms)
 {
     float t = trial(cur);
     if (t < 0) return (int)t;
@@ -1741,11 +1747,11 @@ static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool growth, Tria
         return BG3_OK;
     };
     int rc;
+    if (thick && !batch && (rc = try_param(&LaunchCfg::sweep_dests, {16, 32}))) return rc;
     if (thick && (rc = try_param(&LaunchCfg::sweep_stages, {4, 6, 8}))) return rc;
     if (mq > 4 && mq <= 64 && (rc = try_param(&LaunchCfg::thin_max_quads, {mq - 1, mq}))) return rc;
     if ((thin || mq <= 64) && (rc = try_param(&LaunchCfg::thin_warps, {4, 8, 16}))) return rc;
     if ((rc = try_param(&LaunchCfg::deliver_blocks, {152, 304, 608}))) return rc;
-    (void)growth;
     return BG3_OK;
 }
 
@@ -1853,7 +1859,7 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
         return time_batch_steps(b, steps);
     };
     float ms = 0.0f;
-    if (rc == BG3_OK) rc = tune(cur, thick, thin, thin ? 1 << 30 : mq, false, trial, ms);
+    if (rc == BG3_OK) rc = tune(cur, thick, thin, thin ? 1 << 30 : mq, true, trial, ms);
     int rc2 = BG3_OK;
     for (size_t k = 0; k < b->nets.size(); k++) {
         if (sc[k].buf && state_load(b->nets[k], sc[k]) != BG3_OK) rc2 = BG3_ECUDA;

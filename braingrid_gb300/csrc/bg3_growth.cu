@@ -72,7 +72,7 @@ __global__ void k_growth_existing(const NetDev *nets)
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
         int d, k;
-        pos_slot(p, n.Np, k, d);
+        pos_slot(p, n.Mq, k, d);
         if (d >= n.N || k >= (int)n.count[d]) continue;
         int s = n.src[p];
         float a = pair_area(n.xloc[s], n.yloc[s], n.radii[s], n.xloc[d], n.yloc[d], n.radii[d]);
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
     __syncthreads();
     const int c0 = s_count;
     for (int k = threadIdx.x; k < c0; k += blockDim.x) {
-        int s = n.src[slot_pos(k, d, n.Np)];
+        int s = n.src[slot_pos(k, d, n.Mq)];
         atomicOr(&existing[s >> 5], 1u << (s & 31));
     }
     __syncthreads();
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
         if (add) {
             int k = cur + before + __popc(m & ((1u << lane) - 1));
             if (k < n.max_syn) {
-                size_t p = slot_pos(k, d, n.Np);
+                size_t p = slot_pos(k, d, n.Mq);
                 int type = syn_type(n.ntype[s], td);
                 n.src[p] = s;
                 n.stype[p] = (int8_t)type;
@@ -174,7 +174,7 @@ __global__ void k_out_count(const NetDev *nets)
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
         int d, k;
-        pos_slot(p, n.Np, k, d);
+        pos_slot(p, n.Mq, k, d);
         if (d < n.N && k < (int)n.count[d])
             atomicAdd(&n.outCount[(size_t)n.lcls[p] * n.N + n.src[p]], 1u);
     }
@@ -224,7 +224,7 @@ __global__ void k_out_fill(const NetDev *nets)
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total;
          p += (size_t)gridDim.x * blockDim.x) {
         int d, k;
-        pos_slot(p, n.Np, k, d);
+        pos_slot(p, n.Mq, k, d);
         if (d >= n.N || k >= (int)n.count[d]) continue;
         size_t key = (size_t)n.lcls[p] * n.N + n.src[p];
         uint32_t slot = n.outBegin[key] + atomicAdd(&n.outFill[key], 1u);

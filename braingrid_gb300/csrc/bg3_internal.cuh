@@ -3,12 +3,14 @@
 // HBM layout of one network (arrays owned by bg3_net, allocated once at bg3_create):
 //
 //   neurons               SoA float/int arrays, neuron index contiguous.
-//   synapse slot planes   slot (dest d, row k) lives at p = ((k / 4) * Np + d) * 4 + k % 4,
-//                         Np = N rounded up to 32: ELL order with each dest's rows interleaved in
-//                         groups of four ("row quads"), so one 16-byte load gives a lane four
-//                         consecutive rows of its dest, and a 32-dest tile of 64 rows is a
-//                         [16 quads x 512 B] box for a 2-D TMA copy.  The reference slot id of
-//                         (d, k) is d * maxSyn + k.
+//   synapse slot planes   tile-major ELL with row quads: dests are grouped in tiles of 32; slot
+//                         (dest d, row k) of tile T = d / 32 lives at
+//                         p = ((T * Mq + k / 4) * 32 + d % 32) * 4 + k % 4, Mq = max_syn / 4
+//                         rounded up.  One 16-byte load gives a lane four consecutive rows of its
+//                         dest; a tile's row quads are one contiguous stream of Mq x 512 bytes,
+//                         so the sweep reads long sequential runs (a 64-row chunk of a tile is
+//                         8 KB of psr and 2 KB of classes, one 3-D TMA box each).  The reference
+//                         slot id of (d, k) is d * maxSyn + k.
 //   hot per-slot state    psr (f32) and a one-byte decay class (index into a per-network table
 //                         of decay factors): 9 bytes per synapse per step.
 //   event per-slot state  EvSlot (32 B, one sector): W, u, r, last spike step, birth step, and
@@ -64,19 +66,22 @@ struct LaunchCfg {
     int32_t thin_warps;       // warps per block of the thin sweep (1 .. 32)
     int32_t deliver_blocks;   // blocks of the delivery grid (a batch shares 4x this out)
     int32_t growth_threads;   // threads per block of the overlap pass: 128, 256 or 512
+    int32_t sweep_dests;      // dests per TMA sweep tile of a single network: 16 or 32
 };
-constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256};
+constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32};
 
-// plane position of slot (dest d, row k) and its inverse
-__host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Np)
+// plane position of slot (dest d, row k) and its inverse (Mq row quads per dest)
+__host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Mq)
 {
-    return ((((size_t)(k >> 2)) * (size_t)Np + (size_t)d) << 2) | (size_t)(k & 3);
+    const size_t t = (size_t)(d >> 5) * (size_t)Mq + (size_t)(k >> 2);  // tile row quad
+    return (((t << 5) | (size_t)(d & 31)) << 2) | (size_t)(k & 3);
 }
-__host__ __device__ __forceinline__ void pos_slot(size_t p, int Np, int &k, int &d)
+__host__ __device__ __forceinline__ void pos_slot(size_t p, int Mq, int &k, int &d)
 {
-    size_t q = p >> 2;
-    d = (int)(q % (size_t)Np);
-    k = (int)((q / (size_t)Np) << 2) | (int)(p & 3);
+    const size_t q = p >> 2;
+    const size_t t = q >> 5;
+    d = (int)((t / (size_t)Mq) << 5) | (int)(q & 31);
+    k = (int)((t % (size_t)Mq) << 2) | (int)(p & 3);
 }
 
 struct NetDev {
@@ -99,7 +104,7 @@ struct NetDev {
     float *Aconst, *Bconst, *Cconst, *Dconst, *u_izh, *C3;
     // spike ring: ids of the neurons that fired at step t are ring[(t & 63) * N + i]
     int32_t *ring, *ring_n;
-    // synapse planes (index slot_pos(k, d, Np), Mq * Np * 4 entries)
+    // synapse planes (index slot_pos(k, d, Mq), Np * Mq * 4 entries)
     float *psr;
     uint8_t *dcls;                 // decay class
     uint8_t *lcls;                 // delay class

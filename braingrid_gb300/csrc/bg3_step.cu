@@ -61,19 +61,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
         if (global_ns() - t0 > 1000000000ull) return false;
     }
 }
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
                                             uint64_t *bar)
 {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-        "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int y, const void *src)
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, int x, int y, int z,
+                                             const void *src)
 {
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(map),
-                 "r"(x), "r"(y), "r"(smem_u32(src))
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map),
+                 "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
                  : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
@@ -298,7 +299,7 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
     float ps = n.psr[p];
     if (SYN >= 2) {
         int k, d;
-        pos_slot(p, n.Np, k, d);
+        pos_slot(p, n.Mq, k, d);
         e.W = stdp_pre(n, n.stdp[n.stype[p]], e.W, src, d, t64);
         n.ev[p].W = e.W;
     }
@@ -490,7 +491,7 @@ __device__ __forceinline__ void stdp_post_net(const NetDev &n, int gw, int nw)
         const int d = ids[s];
         const int cnt = (int)n.count[d];
         for (int k = lane; k < cnt; k += 32) {
-            const size_t p = slot_pos(k, d, n.Np);
+            const size_t p = slot_pos(k, d, n.Mq);
             const float W = n.ev[p].W;
             const float W2 = stdp_post(n, n.stdp[n.stype[p]], W, n.src[p], d, n.ltab[n.lcls[p]], t);
             n.ev[p].W = W2;
@@ -539,14 +540,15 @@ constexpr int SW_QUADS = SW_ROWS / 4;
 
 constexpr int SW_SCALE_WARPS = 4;
 constexpr int SW_THREADS = 32 * (2 + SW_SCALE_WARPS);
-constexpr uint32_t SW_PSR_BYTES = SW_ROWS * SW_DESTS * 4;
-constexpr uint32_t SW_CLS_BYTES = SW_ROWS * SW_DESTS;
-constexpr uint32_t SW_CHUNK_BYTES = SW_PSR_BYTES + SW_CLS_BYTES;
+// a chunk of a D-dest tile: 64 rows of psr and of the decay class
+__host__ __device__ constexpr uint32_t sw_psr_bytes(int D) { return (uint32_t)(SW_ROWS * D * 4); }
+__host__ __device__ constexpr uint32_t sw_chunk_bytes(int D) { return (uint32_t)(SW_ROWS * D * 5); }
 // dynamic shared memory: stages (psr | class), decay table, barriers; +128 for alignment
-// ST chunks in flight per tile: 4 (42 KB, five CTAs per SM), 6 (63 KB, three), 8 (83 KB, two)
-constexpr size_t sw_smem(int st)
+// ST chunks in flight per D-dest tile; for D = 32: 4 (42 KB, five CTAs per SM), 6 (63 KB,
+// three), 8 (83 KB, two); D = 16 halves the stages
+constexpr size_t sw_smem(int st, int D)
 {
-    return (size_t)st * SW_CHUNK_BYTES + BG3_MAX_DCLS * 4 + 3 * (size_t)st * 8 + 16 + 128;
+    return (size_t)st * sw_chunk_bytes(D) + BG3_MAX_DCLS * 4 + 3 * (size_t)st * 8 + 16 + 128;
 }
 
 // AllSpikingSynapses::advanceSynapse's "psr *= decay" for every in-use synapse, and the
@@ -570,7 +572,7 @@ constexpr size_t sw_smem(int st)
 template <bool FUSE>
 __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid, float acc,
                                              unsigned long long t, int lane, const NeuronIn &x,
-                                             float noise)
+                                             float noise, int tiles)
 {
     if (FUSE) {
         const unsigned long long t1 = t + 1;
@@ -588,7 +590,7 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
     if (lane == 0) {
         __threadfence();
         unsigned prev = atomicAdd(n.sweep_done, 1u);
-        if (prev == (unsigned)n.ntiles - 1) {
+        if (prev == (unsigned)tiles - 1) {
             *n.step = t + 1;
             *n.sweep_done = 0;
             if (t + 1 >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
@@ -597,23 +599,25 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
     }
 }
 
-template <bool FUSE, int SW_STAGES>
+template <bool FUSE, int SW_STAGES, int D>
 __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *tm_psr,
                                            const CUtensorMap *tm_cls, const int tile,
                                            uint8_t *smem_raw)
 {
+    constexpr uint32_t CH = sw_chunk_bytes(D), PB = sw_psr_bytes(D);
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
-    float *s_dtab = (float *)(smem + (size_t)SW_STAGES * SW_CHUNK_BYTES);
+    float *s_dtab = (float *)(smem + (size_t)SW_STAGES * CH);
     uint64_t *full = (uint64_t *)(s_dtab + BG3_MAX_DCLS);
     uint64_t *scaled = full + SW_STAGES;
     uint64_t *empty = scaled + SW_STAGES;
     int *s_issued = (int *)(empty + SW_STAGES);
-    auto st_psr = [&](int s) { return (float *)(smem + (size_t)s * SW_CHUNK_BYTES); };
-    auto st_cls = [&](int s) { return smem + (size_t)s * SW_CHUNK_BYTES + SW_PSR_BYTES; };
+    auto st_psr = [&](int s) { return (float *)(smem + (size_t)s * CH); };
+    auto st_cls = [&](int s) { return smem + (size_t)s * CH + PB; };
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int d0 = tile * SW_DESTS;
+    const int d0 = tile * D;
     const int d = d0 + lane;
-    const bool valid = d < n.N;
+    const bool valid = lane < D && d < n.N;
+    const int t32 = d0 >> 5, lx = d0 & 31;  // 32-dest plane tile and the first lane within it
     for (int i = threadIdx.x; i < n.n_dcls; i += blockDim.x) s_dtab[i] = n.dtab[i];
     const int cnt = valid ? (int)n.count[d] : 0;
     const int kmax = __reduce_max_sync(0xffffffffu, cnt);
@@ -640,9 +644,9 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
                     set_err(n, ERR_TIMEOUT);
                     break;
                 }
-                mbar_expect_tx(&full[s], SW_CHUNK_BYTES);
-                tma_load_2d(st_psr(s), tm_psr, d0 * 4, c * SW_QUADS, &full[s]);
-                tma_load_2d(st_cls(s), tm_cls, d0, c * SW_QUADS, &full[s]);
+                mbar_expect_tx(&full[s], CH);
+                tma_load_3d(st_psr(s), tm_psr, lx * 4, c * SW_QUADS, t32, &full[s]);
+                tma_load_3d(st_cls(s), tm_cls, lx, c * SW_QUADS, t32, &full[s]);
                 *(volatile int *)s_issued = c + 1;
             }
         }
@@ -650,31 +654,34 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
     }
 
     if (warp <= SW_SCALE_WARPS) {  // --------------------------------------------- scale warps
-        const int q0 = (warp - 1) * (SW_QUADS / SW_SCALE_WARPS);
+        // a chunk is [16 quads][D dests] entries of (float4 psr, uint32 class quad); each scale
+        // warp takes a quarter of them, J per lane
+        constexpr int E = SW_QUADS * D / SW_SCALE_WARPS, J = E / 32;
+        const int e0 = (warp - 1) * E;
         for (int c = 0; c < nch; c++) {
             const int s = c % SW_STAGES;
             if (!mbar_wait(&full[s], (uint32_t)((c / SW_STAGES) & 1))) {
                 set_err(n, ERR_TIMEOUT);
                 break;
             }
-            float4 *ps4 = reinterpret_cast<float4 *>(st_psr(s));                 // [16 quads][32]
-            const uint32_t *cw = reinterpret_cast<const uint32_t *>(st_cls(s));  // [16 quads][32]
-            float4 pv[SW_QUADS / SW_SCALE_WARPS];
-            uint32_t cv[SW_QUADS / SW_SCALE_WARPS];
+            float4 *ps4 = reinterpret_cast<float4 *>(st_psr(s));                 // [16 quads][D]
+            const uint32_t *cw = reinterpret_cast<const uint32_t *>(st_cls(s));  // [16 quads][D]
+            float4 pv[J];
+            uint32_t cv[J];
 #pragma unroll
-            for (int j = 0; j < SW_QUADS / SW_SCALE_WARPS; j++) {
-                pv[j] = ps4[(q0 + j) * SW_DESTS + lane];
-                cv[j] = cw[(q0 + j) * SW_DESTS + lane];
+            for (int j = 0; j < J; j++) {
+                pv[j] = ps4[e0 + j * 32 + lane];
+                cv[j] = cw[e0 + j * 32 + lane];
             }
 #pragma unroll
-            for (int j = 0; j < SW_QUADS / SW_SCALE_WARPS; j++) {
+            for (int j = 0; j < J; j++) {
                 pv[j].x = pv[j].x * s_dtab[cv[j] & 0xffu];
                 pv[j].y = pv[j].y * s_dtab[(cv[j] >> 8) & 0xffu];
                 pv[j].z = pv[j].z * s_dtab[(cv[j] >> 16) & 0xffu];
                 pv[j].w = pv[j].w * s_dtab[cv[j] >> 24];
             }
 #pragma unroll
-            for (int j = 0; j < SW_QUADS / SW_SCALE_WARPS; j++) ps4[(q0 + j) * SW_DESTS + lane] = pv[j];
+            for (int j = 0; j < J; j++) ps4[e0 + j * 32 + lane] = pv[j];
             fence_async_smem();  // the TMA store (async proxy) must see these writes
             __syncwarp();
             if (lane == 0) mbar_arrive(&scaled[s]);
@@ -699,19 +706,21 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         }
         done = c + 1;
         const float4 *ps4 = reinterpret_cast<const float4 *>(st_psr(s));
-        float4 pv[SW_QUADS];
+        if (lane < D) {
+            float4 pv[SW_QUADS];
 #pragma unroll
-        for (int q = 0; q < SW_QUADS; q++) pv[q] = ps4[q * SW_DESTS + lane];
+            for (int q = 0; q < SW_QUADS; q++) pv[q] = ps4[q * D + lane];
 #pragma unroll
-        for (int q = 0; q < SW_QUADS; q++) {
-            acc = acc + pv[q].x;
-            acc = acc + pv[q].y;
-            acc = acc + pv[q].z;
-            acc = acc + pv[q].w;
+            for (int q = 0; q < SW_QUADS; q++) {
+                acc = acc + pv[q].x;
+                acc = acc + pv[q].y;
+                acc = acc + pv[q].z;
+                acc = acc + pv[q].w;
+            }
         }
         __syncwarp();
         if (lane == 0) {
-            tma_store_2d(tm_psr, d0 * 4, c * SW_QUADS, st_psr(s));
+            tma_store_3d(tm_psr, lx * 4, c * SW_QUADS, t32, st_psr(s));
             bulk_commit();
             if (c >= 1) {
                 bulk_wait_read1();
@@ -732,13 +741,13 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         __syncwarp();
     }
 
-    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise);
+    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise, n.ntiles * (SW_DESTS / D));
 }
 
 // Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
 // of a tile is 512 contiguous bytes of the plane (and 128 of the class plane), so the warp reads
 // it with one coalesced 16-byte load per lane, scales it, writes it back and adds it in row
-// order; the same epilogue as sweep_tile.  Lanes past N sit in the plane padding (Np), whose
+// order; the same epilogue as sweep_tile.  Lanes past N sit in the last tile's padding, whose
 // slots stay +0.0f.  For these networks a TMA pipeline per 32 dests would spend most of its time
 // in set-up.
 template <bool FUSE>
@@ -758,9 +767,9 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
         neuron_load(n, d, x);  // in flight with the row loads below
         noise = normal_device(n.noise_seed, t + 1, d);
     }
-    float4 *P = reinterpret_cast<float4 *>(n.psr);
-    const uint32_t *C = reinterpret_cast<const uint32_t *>(n.dcls);
-    const size_t Np = (size_t)n.Np;
+    // this tile's row quads: [Mq][32 lanes] float4 of psr, uint32 of class bytes
+    float4 *P = reinterpret_cast<float4 *>(n.psr) + (size_t)tile * n.Mq * 32 + lane;
+    const uint32_t *C = reinterpret_cast<const uint32_t *>(n.dcls) + (size_t)tile * n.Mq * 32 + lane;
     float acc = 0.0f;
     for (int q = 0; q < nq; q += 4) {
         float4 v[4];
@@ -768,8 +777,8 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (q + j < nq) {
-                v[j] = P[(size_t)(q + j) * Np + d];
-                c[j] = C[(size_t)(q + j) * Np + d];
+                v[j] = P[(size_t)(q + j) * 32];
+                c[j] = C[(size_t)(q + j) * 32];
             }
         }
 #pragma unroll
@@ -779,7 +788,7 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
                 v[j].y = v[j].y * __ldg(&n.dtab[(c[j] >> 8) & 0xffu]);
                 v[j].z = v[j].z * __ldg(&n.dtab[(c[j] >> 16) & 0xffu]);
                 v[j].w = v[j].w * __ldg(&n.dtab[c[j] >> 24]);
-                P[(size_t)(q + j) * Np + d] = v[j];
+                P[(size_t)(q + j) * 32] = v[j];
                 acc = acc + v[j].x;
                 acc = acc + v[j].y;
                 acc = acc + v[j].z;
@@ -787,16 +796,16 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
             }
         }
     }
-    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise);
+    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise, n.ntiles);
 }
 
-template <int SYN, bool FUSE, int ST>
+template <int SYN, bool FUSE, int ST, int D>
 __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ NetDev n,
                                                       const __grid_constant__ CUtensorMap tm_psr,
                                                       const __grid_constant__ CUtensorMap tm_cls)
 {
     extern __shared__ uint8_t smem_raw[];
-    sweep_tile<FUSE, ST>(n, &tm_psr, &tm_cls, blockIdx.x, smem_raw);
+    sweep_tile<FUSE, ST, D>(n, &tm_psr, &tm_cls, blockIdx.x, smem_raw);
 }
 
 // Batched form: one launch sweeps every tile of every network of a batch.  tiles[b] = (network,
@@ -808,7 +817,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_batch(const NetDev *nets,
 {
     extern __shared__ uint8_t smem_raw[];
     const int2 tr = tiles[blockIdx.x];
-    sweep_tile<FUSE, ST>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
+    sweep_tile<FUSE, ST, SW_DESTS>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
 }
 
 template <bool FUSE>
@@ -873,20 +882,21 @@ void launch_deliver(const NetDev &h, const LaunchCfg &c, cudaStream_t s)
 }
 
 template <typename K>
-static void allow_smem(K kern, int st)
+static void allow_smem(K kern, int st, int D)
 {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sw_smem(st));
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sw_smem(st, D));
 }
 
-template <int SYN, bool FUSE, int ST>
+template <int SYN, bool FUSE, int ST, int D>
 static void launch_sweep_t(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, cudaStream_t s)
 {
     static bool attr_set = false;
     if (!attr_set) {
-        allow_smem(k_sweep<SYN, FUSE, ST>, ST);
+        allow_smem(k_sweep<SYN, FUSE, ST, D>, ST, D);
         attr_set = true;
     }
-    launch_pdl(k_sweep<SYN, FUSE, ST>, h.ntiles, SW_THREADS, sw_smem(ST), s, h, tp, tc);
+    launch_pdl(k_sweep<SYN, FUSE, ST, D>, h.ntiles * (SW_DESTS / D), SW_THREADS, sw_smem(ST, D), s,
+               h, tp, tc);
 }
 
 template <bool FUSE, int ST>
@@ -895,10 +905,10 @@ static void launch_sweep_batch_thick(const NetDev *nets, const CUtensorMap *maps
 {
     static bool attr_set = false;
     if (!attr_set) {
-        allow_smem(k_sweep_batch<FUSE, ST>, ST);
+        allow_smem(k_sweep_batch<FUSE, ST>, ST, SW_DESTS);
         attr_set = true;
     }
-    launch_pdl(k_sweep_batch<FUSE, ST>, n_thick, SW_THREADS, sw_smem(ST), s, nets, maps, tiles);
+    launch_pdl(k_sweep_batch<FUSE, ST>, n_thick, SW_THREADS, sw_smem(ST, SW_DESTS), s, nets, maps, tiles);
 }
 
 template <bool FUSE>
@@ -945,16 +955,18 @@ void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 
     else launch_sweep_batch_t<false>(nets, maps, tiles, n_thick, n_thin, c, s);
 }
 
-template <int SYN, bool FUSE>
+template <int SYN, bool FUSE, int D>
 static void launch_sweep_st(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
                             const LaunchCfg &c, cudaStream_t s)
 {
-    if (c.sweep_stages == 4) launch_sweep_t<SYN, FUSE, 4>(h, tp, tc, s);
-    else if (c.sweep_stages == 8) launch_sweep_t<SYN, FUSE, 8>(h, tp, tc, s);
-    else launch_sweep_t<SYN, FUSE, 6>(h, tp, tc, s);
+    if (c.sweep_stages == 4) launch_sweep_t<SYN, FUSE, 4, D>(h, tp, tc, s);
+    else if (c.sweep_stages == 8) launch_sweep_t<SYN, FUSE, 8, D>(h, tp, tc, s);
+    else launch_sweep_t<SYN, FUSE, 6, D>(h, tp, tc, s);
 }
 
-void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc, bool fuse,
+// tp/tc: the tensor maps of 32-dest boxes, tp16/tc16 those of 16-dest boxes
+void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
+                  const CUtensorMap &tp16, const CUtensorMap &tc16, bool fuse,
                   const LaunchCfg &c, cudaStream_t s)
 {
     if (sweep_is_thin(h, c)) {
@@ -965,8 +977,13 @@ void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
         return;
     }
     // the synapse kind does not change the sweep: one instantiation serves all kinds
-    if (fuse) launch_sweep_st<1, true>(h, tp, tc, c, s);
-    else launch_sweep_st<1, false>(h, tp, tc, c, s);
+    if (c.sweep_dests == 16) {
+        if (fuse) launch_sweep_st<1, true, 16>(h, tp16, tc16, c, s);
+        else launch_sweep_st<1, false, 16>(h, tp16, tc16, c, s);
+    } else {
+        if (fuse) launch_sweep_st<1, true, SW_DESTS>(h, tp, tc, c, s);
+        else launch_sweep_st<1, false, SW_DESTS>(h, tp, tc, c, s);
+    }
 }
 
 }  // namespace bg3

@@ -1,6 +1,6 @@
 """Run a benchmark workload for a few steps, for profilers (ncu) to capture its kernels.
 
-    python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big] [--steps 20] [--flush]
+    python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big|growth] [--steps 20] [--flush]
 
 c3 is the Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
 networks of the served stream's largest sizes (166x166, 176x176, 180x180) after one epoch and a
@@ -16,10 +16,17 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big", "growth"])
     ap.add_argument("--count", type=int, default=512, help="networks of the c3 workload")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
+    if a.workload == "growth":
+        # config[1]'s growth pass at the pre-grown radii: creation, then an updating pass
+        spec, net = workloads.build()
+        net.growth(2)
+        net.sync()
+        print("synapses", net.total_synapses(), "error_word", net.error_word)
+        return
     if a.workload == "c1":
         spec, net = workloads.build()
         net.bench_steps(a.steps, flush)

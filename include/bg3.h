@@ -334,6 +334,9 @@ typedef struct {
     int32_t deliver_blocks;   /* blocks of the spike-delivery grid: 1 .. 65535 (default 304); a
                                  batch shares four such grids out over its networks                 */
     int32_t growth_threads;   /* threads per block of the overlap pass: 128, 256 or 512 (256)       */
+    int32_t sweep_dests;      /* dests per TMA sweep tile of a single network: 16 or 32 (32); more,
+                                 smaller tiles spread a network over the SMs more evenly (a batch
+                                 always uses 32)                                                    */
 } bg3_launch_cfg;
 int bg3_get_launch(bg3_net *net, bg3_launch_cfg *cfg);
 int bg3_set_launch(bg3_net *net, const bg3_launch_cfg *cfg);
