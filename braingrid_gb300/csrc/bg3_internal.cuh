@@ -286,6 +286,158 @@ __device__ __forceinline__ float d2f_rn(double d)
     return __uint_as_float(bits);
 }
 
+// ---- IEEE 754 binary64 add and multiply on the integer pipe ---------------------------------
+// The Izhikevich update evaluates part of its expression in double (as the reference does);
+// GB300's FP64 pipe is a small fraction of its FP32 rate, so these few operations are restated
+// in integer arithmetic: a finite nonzero double is (-1)^s * m * 2^(e - 52) with a 53-bit
+// m in [2^52, 2^53); products are formed exactly (106 bits) and sums with 10 guard bits plus a
+// sticky bit, then rounded to nearest, ties to even — the definition of IEEE 754 rounding, so the
+// results are the hardware's bit for bit.  Zero is m = 0.  Anything else (subnormal, infinite,
+// NaN, or an exponent leaving the normal range) sets ok = false and the caller recomputes with
+// hardware doubles.
+struct SoftD {
+    uint64_t m;
+    int32_t e;
+    uint32_t s;
+};
+
+__device__ __forceinline__ SoftD sd_from_float(float f, bool &ok)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t ex = (b >> 23) & 0xffu, fr = b & 0x7fffffu;
+    SoftD r;
+    r.s = b >> 31;
+    if (ex == 0u) {
+        if (fr) ok = false;  // subnormal
+        r.m = 0;
+        r.e = 0;
+        return r;
+    }
+    if (ex == 0xffu) ok = false;
+    r.m = (uint64_t)(fr | 0x800000u) << 29;
+    r.e = (int32_t)ex - 127;
+    return r;
+}
+
+__device__ __forceinline__ SoftD sd_from_double(double x, bool &ok)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const uint32_t ex = (uint32_t)(b >> 52) & 0x7ffu;
+    const uint64_t fr = b & 0xfffffffffffffull;
+    SoftD r;
+    r.s = (uint32_t)(b >> 63);
+    if (ex == 0u) {
+        if (fr) ok = false;
+        r.m = 0;
+        r.e = 0;
+        return r;
+    }
+    if (ex == 0x7ffu) ok = false;
+    r.m = fr | (1ull << 52);
+    r.e = (int32_t)ex - 1023;
+    return r;
+}
+
+__device__ __forceinline__ void sd_round(SoftD &r, uint64_t rem, uint64_t half, bool &ok)
+{
+    if (rem > half || (rem == half && (r.m & 1ull))) {
+        r.m += 1ull;
+        if (r.m == (1ull << 53)) {
+            r.m >>= 1;
+            r.e += 1;
+        }
+    }
+    if (r.e > 1023 || r.e < -1022) ok = false;
+}
+
+__device__ __forceinline__ SoftD sd_mul(SoftD a, SoftD b, bool &ok)
+{
+    SoftD r;
+    r.s = a.s ^ b.s;
+    if (a.m == 0 || b.m == 0) {
+        r.m = 0;
+        r.e = 0;
+        return r;
+    }
+    const uint64_t lo = a.m * b.m, hi = __umul64hi(a.m, b.m);  // product in [2^104, 2^106)
+    const int sh = (hi >> 41) ? 53 : 52;
+    r.e = a.e + b.e + (sh - 52);
+    r.m = (hi << (64 - sh)) | (lo >> sh);
+    const uint64_t rem = lo & ((1ull << sh) - 1ull);
+    sd_round(r, rem, 1ull << (sh - 1), ok);
+    return r;
+}
+
+__device__ __forceinline__ SoftD sd_add(SoftD a, SoftD b, bool &ok)
+{
+    if (b.m == 0) {
+        if (a.m == 0) a.s &= b.s;  // +0 + -0 = +0, -0 + -0 = -0
+        return a;
+    }
+    if (a.m == 0) return b;
+    // A: the operand of larger magnitude
+    if (b.e > a.e || (b.e == a.e && b.m > a.m)) {
+        const SoftD t = a;
+        a = b;
+        b = t;
+    }
+    const int d = a.e - b.e;
+    const uint64_t ma = a.m << 10;  // leading bit at 62
+    uint64_t mb = b.m << 10;
+    if (d >= 63) {
+        mb = 1ull;  // only the sticky bit survives
+    } else if (d > 0) {
+        const uint64_t lost = mb & ((1ull << d) - 1ull);
+        mb = (mb >> d) | (lost ? 1ull : 0ull);
+    }
+    SoftD r;
+    r.s = a.s;
+    r.e = a.e;
+    uint64_t S;
+    if (a.s == b.s) {
+        S = ma + mb;
+        if (S >> 63) {
+            S = (S >> 1) | (S & 1ull);
+            r.e += 1;
+        }
+    } else {
+        S = ma - mb;
+        if (S == 0) {  // exact cancellation gives +0 in round-to-nearest
+            r.m = 0;
+            r.e = 0;
+            r.s = 0;
+            return r;
+        }
+        const int k = __clzll((long long)S) - 1;  // bring the leading bit back to 62
+        S <<= k;
+        r.e -= k;
+    }
+    r.m = S >> 10;
+    sd_round(r, S & 0x3ffull, 0x200ull, ok);
+    return r;
+}
+
+// (float) of the double, rounded to nearest, ties to even.
+__device__ __forceinline__ float sd_to_float(SoftD a, bool &ok)
+{
+    if (a.m == 0) return __uint_as_float(a.s << 31);
+    uint32_t m = (uint32_t)(a.m >> 29);
+    const uint64_t rem = a.m & ((1ull << 29) - 1ull);
+    int e = a.e;
+    if (rem > (1ull << 28) || (rem == (1ull << 28) && (m & 1u))) {
+        m += 1u;
+        if (m == (1u << 24)) {
+            m >>= 1;
+            e += 1;
+        }
+    }
+    if (e < -126 || e > 127) {
+        ok = false;
+        return 0.0f;
+    }
+    return __uint_as_float((a.s << 31) | ((uint32_t)(e + 127) << 23) | (m & 0x7fffffu));
+}
+
 // ---- neuron update (shared by the standalone kernels and the sweep epilogues) ---------------
 enum { BR_REFRACTORY = 0, BR_FIRE = 1, BR_INTEGRATE = 2 };
 
@@ -380,11 +532,34 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
         // Vm in mV; dv = C3 (0.04 v^2 + 5 v + 140 - u) evaluated in double, du = C3 a (b v - u)
         const float Vint = x.Vm * 1000.0f;
         const float u = x.u, C3 = x.C3;
-        const double vd = f2d_exact(Vint);
-        const float Vb = d2f_rn(vd + f2d_exact(C3) * (0.04 * vd * vd + f2d_exact(5.0f * Vint) +
-                                                      140.0 - f2d_exact(u)));
+        // Vb = (float)(v + C3 * (0.04 v v + (double)(5 v) + 140 - u)), then
+        // Vm = (float)((double)Vb * 0.001 + (double)(C2 sp)), each double operation rounded once
+        // the double constants 0.04, 140.0 and 0.001 as (mantissa, exponent, sign)
+        constexpr SoftD K004 = {0x147ae147ae147bull, -5, 0u};
+        constexpr SoftD K140 = {0x11800000000000ull, 7, 0u};
+        constexpr SoftD K0001 = {0x10624dd2f1a9fcull, -10, 0u};
+        bool ok = true;
+        const SoftD vd = sd_from_float(Vint, ok);
+        SoftD t = sd_mul(K004, vd, ok);
+        t = sd_mul(t, vd, ok);
+        t = sd_add(t, sd_from_float(5.0f * Vint, ok), ok);
+        t = sd_add(t, K140, ok);
+        SoftD nu = sd_from_float(u, ok);
+        nu.s ^= 1u;
+        t = sd_add(t, nu, ok);
+        t = sd_mul(sd_from_float(C3, ok), t, ok);
+        const float Vb = sd_to_float(sd_add(vd, t, ok), ok);
+        SoftD w = sd_mul(sd_from_float(Vb, ok), K0001, ok);
+        w = sd_add(w, sd_from_float(x.C2 * sp, ok), ok);
+        float Vnew = sd_to_float(w, ok);
+        if (!ok) {  // outside the restated range: the same expression in hardware doubles
+            const double v = (double)Vint;
+            const float Vh = (float)(v + (double)C3 * (0.04 * v * v + (double)(5.0f * Vint) +
+                                                       140.0 - (double)u));
+            Vnew = (float)((double)Vh * 0.001 + (double)(x.C2 * sp));
+        }
         n.u_izh[i] = u + C3 * x.A * (x.B * Vint - u);
-        n.Vm[i] = d2f_rn(f2d_exact(Vb) * 0.001 + f2d_exact(x.C2 * sp));
+        n.Vm[i] = Vnew;
     } else {
         n.Vm[i] = x.C1 * x.Vm + x.C2 * sp;
     }

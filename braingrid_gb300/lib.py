@@ -140,6 +140,8 @@ def load(build_if_missing=True):
         "bg3_set_stdp_constants": ([vp, ctypes.POINTER(StdpConstants)], ctypes.c_int),
         "bg3_set_stdp_arithmetic": ([vp, ctypes.c_int], ctypes.c_int),
         "bg3_epoch_record": ([vp], ctypes.c_int),
+        "bg3_selftest_binary64": ([ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+                                  ctypes.c_int),
         "bg3_get_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
         "bg3_set_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
         "bg3_batch_get_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
@@ -604,3 +606,11 @@ class Batch:
         check(self.L.bg3_batch_bench_steps(self.h, int(nsteps), int(flush_bytes), _p(ms)),
               "bg3_batch_bench_steps")
         return ms[:nsteps]
+
+
+def selftest_binary64(samples=1 << 26, seed=1):
+    """(add, multiply, conversion mismatches, out-of-range cases) of the integer-pipe binary64
+    arithmetic against the hardware."""
+    c = (ctypes.c_uint64 * 4)()
+    check(load().bg3_selftest_binary64(int(samples), int(seed), c), "bg3_selftest_binary64")
+    return tuple(int(x) for x in c)

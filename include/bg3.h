@@ -325,6 +325,12 @@ int bg3_batch_bench_steps(bg3_batch *batch, int64_t nsteps, int64_t flush_bytes,
 int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *step_ms,
                     float *kernel_ms);
 
+/* Self-test of the library's integer-pipe binary64 add / multiply / conversion (used by the
+ * Izhikevich update) against the hardware on `samples` random operand pairs: counts[0..3] =
+ * add mismatches, multiply mismatches, conversion mismatches, cases outside the restated range
+ * (which the update recomputes in hardware).  No counterpart in the reference. */
+int bg3_selftest_binary64(uint64_t samples, uint64_t seed, uint64_t *counts);
+
 /* ---- launch configuration and autotuning (no counterpart in the reference) ----------------- */
 typedef struct {
     int32_t sweep_stages;     /* chunks in flight per TMA sweep tile: 4, 6 or 8 (default 6)          */
