@@ -233,8 +233,9 @@ def run_bg3(args):
     e2e = {"value": S * E2E_STEPS * e2e_iters * world / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS}
     err = net.error_word
-    batched = izh_stdp = served = None
+    batched = izh_stdp = served = growth = None
     if world == 1:
+        growth = run_growth()
         batched = run_batched(min(args.steps, 500), max(args.warmup, 20))
         izh_stdp = run_c3(min(args.steps, 1000), max(args.warmup, 20))
         if args.serve_jobs > 0:
@@ -267,6 +268,7 @@ def run_bg3(args):
                                            "sweep": float(shares[2])}},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "growth": growth,
             "batched": batched,
             "batched_izh_stdp": izh_stdp,
             "served": served,
@@ -339,6 +341,42 @@ def run_batched(steps, warmup):
     batch.close()
     for n in nets:
         n.close()
+    return out
+
+
+def run_growth():
+    """ConnGrowth epoch pass (radii update, O(N^2) overlap scan, weight update / synapse
+    creation, map rebuild, recorder) on config[1]: at the stated start radius 0.4 (every pair
+    rejected), at the pre-grown radii U[8.35, 8.45] creating ~7.6 M synapses, and once more at
+    those radii updating them.  Host wall clock around a synchronised pass."""
+    import time as _t
+    from braingrid_gb300 import netgen
+    spec = netgen.lif_network(WIDTH, HEIGHT, frac_inh=0.10, seed=SEED)
+    net = netgen.make_gpu_network(spec, MAX_SYN, noise_seed=SEED)
+    N = spec["N"]
+    out = {"pairs": N * N}
+
+    def timed(epoch):
+        net.sync()
+        t0 = _t.perf_counter()
+        net.growth(epoch)
+        net.sync()
+        return _t.perf_counter() - t0
+    timed(1)  # first pass loads the module's kernels
+    t_reject = timed(2)
+    rs = np.random.RandomState(11)
+    r = rs.uniform(RADIUS - 0.05, RADIUS + 0.05, N).astype(np.float32)
+    g = netgen.GROWTH
+    net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
+                      g["start_radius"], r)
+    t_create = timed(3)
+    S = net.total_synapses()
+    t_update = timed(4)
+    out.update({"radius_0.4_s": t_reject, "radius_0.4_pairs_per_s": N * N / t_reject,
+                "grown_create_s": t_create, "grown_update_s": t_update,
+                "grown_pairs_per_s": N * N / t_update, "synapses": S,
+                "error_word": net.error_word})
+    net.close()
     return out
 
 
@@ -537,13 +575,16 @@ def main():
                     help="jobs of the served-stream trace (config[4])")
     ap.add_argument("--serve-slots", type=float, default=SERVE_SLOTS,
                     help="served form: cap on the resident jobs' synapse slots (0 = none)")
-    ap.add_argument("--only", choices=["c3", "serve"], default=None,
+    ap.add_argument("--only", choices=["c3", "serve", "growth"], default=None,
                     help="run one secondary workload alone and print its JSON")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.only == "c3":
         print(json.dumps(run_c3(min(args.steps, 1000), max(args.warmup, 20))), flush=True)
+        return
+    if args.only == "growth":
+        print(json.dumps(run_growth()), flush=True)
         return
     if args.only == "serve":
         print(json.dumps(run_served(args.serve_jobs, int(args.serve_slots))), flush=True)
