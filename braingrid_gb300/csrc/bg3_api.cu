@@ -472,6 +472,13 @@ int64_t bg3_net_footprint(const bg3_net_desc *desc)
 
 uint64_t bg3_net_bytes(bg3_net *n) { return n ? n->bytes + sizeof(NetDev) : 0; }
 
+int bg3_get_desc(bg3_net *n, bg3_net_desc *desc)
+{
+    if (!n || !desc) return BG3_EINVAL;
+    *desc = n->desc;
+    return BG3_OK;
+}
+
 int bg3_destroy(bg3_net *n)
 {
     if (!n) return BG3_EINVAL;
@@ -688,21 +695,23 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
 int bg3_upload_growth(bg3_net *n, const bg3_growth_params *p, const float *radii,
                       const float *rates)
 {
-    if (!n || !p) return BG3_EINVAL;
+    if (!n || (!p && !radii && !rates)) return BG3_EINVAL;
     NetDev &h = n->h;
-    h.g_epsilon = p->epsilon; h.g_beta = p->beta; h.g_rho = p->rho;
-    h.g_target_rate = p->target_rate; h.g_min_radius = p->min_radius;
-    h.g_start_radius = p->start_radius; h.g_max_rate = p->max_rate;
     size_t N = h.N;
     int rc;
-    // ConnGrowth::updateConns' exp((epsilon - rate / maxRate) / beta) for rate = count / T
-    // (Connections/ConnGrowth.cpp:300-306), one value per possible spike count
-    std::vector<float> ge((size_t)h.max_spikes + 1);
-    for (int c = 0; c <= h.max_spikes; c++) {
-        const float rate = (float)c / h.epoch_duration;
-        ge[c] = expf((h.g_epsilon - rate / h.g_max_rate) / h.g_beta);
+    if (p) {
+        h.g_epsilon = p->epsilon; h.g_beta = p->beta; h.g_rho = p->rho;
+        h.g_target_rate = p->target_rate; h.g_min_radius = p->min_radius;
+        h.g_start_radius = p->start_radius; h.g_max_rate = p->max_rate;
+        // ConnGrowth::updateConns' exp((epsilon - rate / maxRate) / beta) for rate = count / T
+        // (Connections/ConnGrowth.cpp:300-306), one value per possible spike count
+        std::vector<float> ge((size_t)h.max_spikes + 1);
+        for (int c = 0; c <= h.max_spikes; c++) {
+            const float rate = (float)c / h.epoch_duration;
+            ge[c] = expf((h.g_epsilon - rate / h.g_max_rate) / h.g_beta);
+        }
+        if ((rc = h2d(n, h.grow_exp, ge.data(), ge.size()))) return rc;
     }
-    if ((rc = h2d(n, h.grow_exp, ge.data(), ge.size()))) return rc;
     if ((rc = h2d(n, h.radii, radii, N)) || (rc = h2d(n, h.rates, rates, N))) return rc;
     // recorder row 0 holds the start values (XmlGrowthRecorder::initDefaultValues / initValues)
     if ((rc = h2d(n, h.radii_hist, radii, N)) || (rc = h2d(n, h.rates_hist, rates, N))) return rc;
@@ -1874,3 +1883,222 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
     if (best_ms) *best_ms = ms;
     return BG3_OK;
 }
+
+// ---- checkpoints ------------------------------------------------------------------------------
+// Every device array of a network, by its NetDev field.  A checkpoint holds each one's bytes with
+// the size of its allocation; bg3_checkpoint_save refuses a network holding an allocation that
+// this list does not name, so a new array cannot be left out silently.
+#define BG3_NET_ARRAYS(X)                                                                         \
+    X(step) X(sweep_done) X(err) X(noise_cursor) X(Vm) X(Vthresh) X(Vreset) X(I0) X(Inoise)       \
+    X(C1) X(C2) X(Trefract) X(sp) X(refr) X(spikeCount) X(spikeCountOffset) X(history) X(ntype)   \
+    X(Aconst) X(Bconst) X(Cconst) X(Dconst) X(u_izh) X(C3) X(ring) X(ring_n) X(psr) X(dcls)       \
+    X(lcls) X(ev) X(src) X(stype) X(count) X(dtab) X(ltab) X(outBegin) X(outCount) X(outMap)      \
+    X(outFill) X(radii) X(rates) X(xloc) X(yloc) X(grow_exp) X(burstiness) X(spikes_hist)         \
+    X(rates_hist) X(radii_hist) X(reg_values) X(reg_shift) X(pois_mask) X(pois_nisi) X(in_psr)    \
+    X(in_decay) X(in_queue) X(in_delay) X(in_ev) X(isi_begin) X(isi_vals) X(isi_cursor)
+
+#define BG3_COUNT_ONE(f) +1
+static const uint32_t CKPT_ARRAYS = 0 BG3_NET_ARRAYS(BG3_COUNT_ONE);
+#undef BG3_COUNT_ONE
+
+struct CkptHeader {
+    char magic[8];             // "BG3CKPT"
+    uint32_t version;          // CKPT_VERSION
+    uint32_t netdev_bytes;     // sizeof(NetDev) of the writing library
+    uint64_t total_bytes;      // whole checkpoint
+    bg3_net_desc desc;
+    LaunchCfg cfg;
+    int64_t noise_count;       // injected noise values held (consumed ones included)
+    uint32_t n_dtab, n_ltab;   // decay / delay class tables
+    uint32_t n_arrays;         // CKPT_ARRAYS
+    uint32_t pad;
+};
+static const uint32_t CKPT_VERSION = 1;
+static const char CKPT_MAGIC[8] = {'B', 'G', '3', 'C', 'K', 'P', 'T', 0};
+
+static size_t alloc_size(const bg3_net *n, const void *p)
+{
+    if (!p) return 0;
+    for (auto &a : n->allocs)
+        if (a.first == p) return a.second;
+    return 0;
+}
+
+static void afree(bg3_net *n, const void *p)
+{
+    for (auto &a : n->allocs)
+        if (a.first && a.first == p) {
+            cudaFree(a.first);
+            n->bytes -= a.second;
+            a = std::make_pair((void *)nullptr, (size_t)0);
+        }
+}
+
+// Gives field an allocation of exactly `bytes` (none for 0), keeping one of that size.
+template <typename T>
+static int aresize(bg3_net *n, T *&field, size_t bytes)
+{
+    if (field && alloc_size(n, field) == bytes) return BG3_OK;
+    if (field) afree(n, field);
+    field = nullptr;
+    if (!bytes) return BG3_OK;
+    if (bytes % sizeof(T)) return BG3_EINVAL;
+    return dalloc(n, &field, bytes / sizeof(T));
+}
+
+extern "C" {
+
+int bg3_checkpoint_save(bg3_net *n, void *buf, uint64_t cap, uint64_t *len)
+{
+    if (!n || !len) return BG3_EINVAL;
+    CK(cudaStreamSynchronize(n->stream));
+    const NetDev &h = n->h;
+    uint64_t arrays = 0, named = 0;
+#define BG3_SIZE_ONE(f) { const size_t s = alloc_size(n, h.f); arrays += 8 + s; named += s; }
+    BG3_NET_ARRAYS(BG3_SIZE_ONE)
+#undef BG3_SIZE_ONE
+    if (named != n->bytes) return BG3_EUNSUPPORTED;  // an allocation outside the list
+    const int64_t noise = (n->noise_dev && h.noise_len > 0) ? h.noise_len : 0;
+    const uint64_t total = sizeof(CkptHeader) + sizeof(NetDev) + n->dtab.size() * sizeof(float) +
+                           n->ltab.size() * sizeof(int32_t) + (uint64_t)noise * sizeof(float) + arrays;
+    *len = total;
+    if (!buf) return BG3_OK;
+    if (cap < total) return BG3_EINVAL;
+    char *p = (char *)buf;
+    CkptHeader hd;
+    memset(&hd, 0, sizeof(hd));
+    memcpy(hd.magic, CKPT_MAGIC, 8);
+    hd.version = CKPT_VERSION;
+    hd.netdev_bytes = (uint32_t)sizeof(NetDev);
+    hd.total_bytes = total;
+    hd.desc = n->desc;
+    hd.cfg = n->cfg;
+    hd.noise_count = noise;
+    hd.n_dtab = (uint32_t)n->dtab.size();
+    hd.n_ltab = (uint32_t)n->ltab.size();
+    hd.n_arrays = CKPT_ARRAYS;
+    memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    memcpy(p, &h, sizeof(NetDev));  // scalars; its pointers mean nothing to a reader
+    p += sizeof(NetDev);
+    memcpy(p, n->dtab.data(), n->dtab.size() * sizeof(float));
+    p += n->dtab.size() * sizeof(float);
+    memcpy(p, n->ltab.data(), n->ltab.size() * sizeof(int32_t));
+    p += n->ltab.size() * sizeof(int32_t);
+    if (noise) {
+        CK(cudaMemcpy(p, n->noise_dev, (size_t)noise * sizeof(float), cudaMemcpyDeviceToHost));
+        p += (size_t)noise * sizeof(float);
+    }
+#define BG3_SAVE_ONE(f)                                                                           \
+    {                                                                                             \
+        const uint64_t s = alloc_size(n, h.f);                                                    \
+        memcpy(p, &s, 8);                                                                         \
+        p += 8;                                                                                   \
+        if (s) CK(cudaMemcpy(p, h.f, s, cudaMemcpyDeviceToHost));                                 \
+        p += s;                                                                                   \
+    }
+    BG3_NET_ARRAYS(BG3_SAVE_ONE)
+#undef BG3_SAVE_ONE
+    return BG3_OK;
+}
+
+int bg3_checkpoint_load(bg3_net *n, const void *buf, uint64_t len)
+{
+    if (!n || !buf || len < sizeof(CkptHeader) + sizeof(NetDev)) return BG3_EINVAL;
+    const char *p = (const char *)buf, *end = p + len;
+    CkptHeader hd;
+    memcpy(&hd, p, sizeof(hd));
+    if (memcmp(hd.magic, CKPT_MAGIC, 8) || hd.version != CKPT_VERSION ||
+        hd.netdev_bytes != sizeof(NetDev) || hd.total_bytes != len || hd.n_arrays != CKPT_ARRAYS ||
+        memcmp(&hd.desc, &n->desc, sizeof(bg3_net_desc)) || hd.n_dtab > BG3_MAX_DCLS ||
+        hd.n_ltab > BG3_MAX_DELAYS || hd.noise_count < 0)
+        return BG3_EINVAL;
+    const bg3_launch_cfg lc = cfg_to(hd.cfg);
+    if (!cfg_valid(&lc)) return BG3_EINVAL;
+    p += sizeof(hd);
+    NetDev saved;
+    memcpy(&saved, p, sizeof(NetDev));
+    p += sizeof(NetDev);
+    const uint64_t fixed = hd.n_dtab * sizeof(float) + hd.n_ltab * sizeof(int32_t) +
+                           (uint64_t)hd.noise_count * sizeof(float);
+    if ((uint64_t)(end - p) < fixed) return BG3_EINVAL;
+    const char *dtab = p, *ltab = p + hd.n_dtab * sizeof(float);
+    const char *noise = p + hd.n_dtab * sizeof(float) + hd.n_ltab * sizeof(int32_t);
+    p += fixed;
+    // walk the array list once to check it before anything changes
+    const char *arr = p;
+    for (uint32_t i = 0; i < CKPT_ARRAYS; i++) {
+        uint64_t s;
+        if ((uint64_t)(end - p) < 8) return BG3_EINVAL;
+        memcpy(&s, p, 8);
+        p += 8;
+        if ((uint64_t)(end - p) < s) return BG3_EINVAL;
+        p += s;
+    }
+    if (p != end) return BG3_EINVAL;
+    CK(cudaStreamSynchronize(n->stream));
+    NetDev &h = n->h;
+    int rc;
+    p = arr;
+#define BG3_LOAD_ONE(f)                                                                           \
+    {                                                                                             \
+        uint64_t s;                                                                               \
+        memcpy(&s, p, 8);                                                                         \
+        p += 8;                                                                                   \
+        if ((rc = aresize(n, h.f, (size_t)s))) return rc;                                         \
+        if (s) CK(cudaMemcpy((void *)h.f, p, (size_t)s, cudaMemcpyHostToDevice));                 \
+        p += s;                                                                                   \
+    }
+    BG3_NET_ARRAYS(BG3_LOAD_ONE)
+#undef BG3_LOAD_ONE
+    if (n->noise_dev) cudaFree(n->noise_dev);
+    n->noise_dev = nullptr;
+    n->noise_cap = 0;
+    if (hd.noise_count) {
+        if (cudaMalloc(&n->noise_dev, (size_t)hd.noise_count * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            n->noise_dev = nullptr;
+            return BG3_ENOMEM;
+        }
+        CK(cudaMemcpy(n->noise_dev, noise, (size_t)hd.noise_count * sizeof(float),
+                      cudaMemcpyHostToDevice));
+        n->noise_cap = hd.noise_count;
+    }
+    // scalars from the checkpoint, pointers of this network; exp tables looked up again
+    exp_release(n);
+    const NetDev live = h;
+    h = saved;
+#define BG3_KEEP_ONE(f) h.f = live.f;
+    BG3_NET_ARRAYS(BG3_KEEP_ONE)
+#undef BG3_KEEP_ONE
+    h.noise_buf = n->noise_dev;
+    if (h.n_expc < 0 || h.n_expc > BG3_MAX_EXPC || h.n_pcls < 0 || h.n_pcls > BG3_MAX_PCLS)
+        return BG3_EINVAL;
+    for (int c = 0; c < h.n_expc; c++)
+        if ((rc = exp_table<float>(n, 0, h.expc_tau[c], BG3_EXP_LEN, &h.expc_tab[c]))) return rc;
+    for (int t = 0; t < 4; t++) {
+        StdpConst &s = h.stdp[t];
+        s.dpos = s.dneg = nullptr;
+        if (s.dlen_pos && (rc = exp_table<double>(n, 1, s.taupos, BG3_DEXP_LEN, &s.dpos))) return rc;
+        if (s.dlen_neg && (rc = exp_table<double>(n, 1, s.tauneg, BG3_DEXP_LEN, &s.dneg))) return rc;
+    }
+    for (int c = 0; c < h.n_pcls; c++) {
+        h.p_xD[c] = h.p_xF[c] = nullptr;
+        if (h.p_D[c] > 0.0f && std::isfinite(h.p_D[c]) &&
+            (rc = exp_table<float>(n, 0, h.p_D[c], BG3_EXP_LEN, &h.p_xD[c])))
+            return rc;
+        if (h.p_F[c] > 0.0f && std::isfinite(h.p_F[c]) &&
+            (rc = exp_table<float>(n, 0, h.p_F[c], BG3_EXP_LEN, &h.p_xF[c])))
+            return rc;
+    }
+    n->dtab.resize(hd.n_dtab);
+    n->ltab.resize(hd.n_ltab);
+    if (hd.n_dtab) memcpy(n->dtab.data(), dtab, hd.n_dtab * sizeof(float));
+    if (hd.n_ltab) memcpy(n->ltab.data(), ltab, hd.n_ltab * sizeof(int32_t));
+    n->cfg = hd.cfg;
+    if ((rc = push_desc(n))) return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+}  // extern "C"

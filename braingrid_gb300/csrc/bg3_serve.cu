@@ -73,6 +73,9 @@ static void finish(bg3_server *s, Job *j, int status)
                     a.Vm = r->Vm;
                     rc = bg3_download_lif(j->net, &a);
                 }
+                if (rc == BG3_OK && r->checkpoint)
+                    rc = bg3_checkpoint_save(j->net, r->checkpoint, r->checkpoint_cap,
+                                             &r->checkpoint_len);
                 r->status = rc;
             }
         }
@@ -134,7 +137,10 @@ static void admit(bg3_server *s)
         s->slots += j->slots;
         int rc = bg3_create(&j->d.desc, &j->net);
         if (rc == BG3_OK && j->d.setup) rc = j->d.setup(j->net, j->d.user);
+        if (rc == BG3_OK && j->d.resume) rc = bg3_checkpoint_load(j->net, j->d.resume, j->d.resume_len);
         if (rc == BG3_OK) rc = bg3_sync(j->net);
+        uint64_t step = 0;
+        if (rc == BG3_OK) rc = bg3_get_step(j->net, &step);
         if (rc == BG3_OK) {
             int64_t t = bg3_total_synapses(j->net);
             if (t < 0) rc = (int)t;
@@ -149,7 +155,13 @@ static void admit(bg3_server *s)
             continue;
         }
         j->spe = steps_per_epoch(j->d.desc);
-        j->to_boundary = j->spe;
+        // a resumed job continues its epoch count from its step counter
+        j->epoch = (int32_t)(step / (uint64_t)j->spe);
+        j->to_boundary = j->spe - (int64_t)(step % (uint64_t)j->spe);
+        if (j->epoch >= j->d.epochs) {
+            finish(s, j, BG3_EINVAL);  // nothing left to run
+            continue;
+        }
         s->joining.push_back(j);
     }
 }
@@ -183,6 +195,7 @@ int bg3_serve_destroy(bg3_server *s)
 int bg3_serve_submit(bg3_server *s, const bg3_job_desc *job, int64_t *job_id)
 {
     if (!s || !job || job->epochs <= 0 || job->epochs > job->desc.max_epochs ||
+        (job->resume && !job->resume_len) ||
         job->desc.noise_mode != BG3_NOISE_DEVICE || job->desc.synapse_kind < 0 ||
         job->desc.synapse_kind >= KINDS)
         return BG3_EINVAL;
@@ -200,6 +213,7 @@ int bg3_serve_submit(bg3_server *s, const bg3_job_desc *job, int64_t *job_id)
         j->d.result->synapse_steps = 0;
         j->d.result->neuron_steps = 0;
         j->d.result->error_word = 0;
+        j->d.result->checkpoint_len = 0;
     }
     s->queue.push_back(j);
     if (job_id) *job_id = j->id;

@@ -21,6 +21,8 @@ BG3_NEURON_LIF, BG3_NEURON_IZH = 0, 1
 BG3_SYN_SPIKING, BG3_SYN_DS, BG3_SYN_STDP, BG3_SYN_DYNSTDP = 0, 1, 2, 3
 BG3_NOISE_DEVICE, BG3_NOISE_INJECT = 0, 1
 BG3_STDP_HOST, BG3_STDP_DEVICE = 0, 1
+(BG3_OK, BG3_EINVAL, BG3_ENOMEM, BG3_ECUDA, BG3_ENOISE, BG3_EDEVICE,
+ BG3_EUNSUPPORTED) = 0, -1, -2, -3, -4, -5, -6
 ERR_BITS = {1: "history overflow", 2: "double spike in a queue slot", 4: "synapse row full",
             8: "injected noise exhausted", 16: "negative growth weight"}
 
@@ -113,6 +115,16 @@ class IndexMaps(ctypes.Structure):
 _LIB = None
 
 
+IF_FIELDS = ("Cm", "Rm", "Vrest", "Vinit", "Iinject", "Isyn", "Tau")
+
+
+class IfFields(ctypes.Structure):
+    _fields_ = [(k, ctypes.POINTER(ctypes.c_float)) for k in IF_FIELDS]
+
+
+BG3_CONN_STATIC, BG3_CONN_GROWTH = 0, 1
+
+
 def lib_path():
     return _build.LIB
 
@@ -150,6 +162,13 @@ def load(build_if_missing=True):
                           ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "bg3_batch_autotune": ([vp, ctypes.c_int32, ctypes.POINTER(LaunchCfg),
                                 ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+        "bg3_serialize": ([vp, ctypes.POINTER(IfFields), ctypes.c_int32, ctypes.c_char_p,
+                           ctypes.c_uint64, c_u64p], ctypes.c_int),
+        "bg3_deserialize": ([vp, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_uint64,
+                             ctypes.POINTER(IfFields)], ctypes.c_int),
+        "bg3_get_desc": ([vp, ctypes.POINTER(NetDesc)], ctypes.c_int),
+        "bg3_checkpoint_save": ([vp, ctypes.c_void_p, ctypes.c_uint64, c_u64p], ctypes.c_int),
+        "bg3_checkpoint_load": ([vp, ctypes.c_void_p, ctypes.c_uint64], ctypes.c_int),
         "bg3_net_footprint": ([ctypes.POINTER(NetDesc)], ctypes.c_int64),
         "bg3_net_bytes": ([vp], ctypes.c_uint64),
         "bg3_upload_layout": ([vp, c_f32p, c_f32p, c_i32p], ctypes.c_int),
@@ -264,6 +283,14 @@ class Network:
         check(self.L.bg3_create(ctypes.byref(self.desc), ctypes.byref(h)), "bg3_create")
         self.h = h
         self._owned = True
+
+    @classmethod
+    def from_desc(cls, desc):
+        """A new network of the same shape as desc (a NetDesc)."""
+        d = desc
+        return cls(d.n_neurons, d.max_syn_per_neuron, d.width, d.height, d.epoch_duration,
+                   d.delta_t, d.max_firing_rate, d.max_epochs, d.synapse_kind, d.noise_mode,
+                   d.noise_seed, neuron_kind=d.neuron_kind)
 
     @classmethod
     def borrow(cls, handle, desc):
@@ -443,6 +470,43 @@ class Network:
     @property
     def device_bytes(self):
         return int(self.L.bg3_net_bytes(self.h))
+
+    def checkpoint(self):
+        """The network's whole state (bg3_checkpoint_save) as a numpy uint8 array."""
+        n = ctypes.c_uint64()
+        check(self.L.bg3_checkpoint_save(self.h, None, 0, ctypes.byref(n)), "bg3_checkpoint_save")
+        buf = np.empty(n.value, np.uint8)
+        check(self.L.bg3_checkpoint_save(self.h, buf.ctypes.data, buf.size, ctypes.byref(n)),
+              "bg3_checkpoint_save")
+        return buf
+
+    def load_checkpoint(self, buf):
+        b = np.ascontiguousarray(np.frombuffer(buf, np.uint8))
+        check(self.L.bg3_checkpoint_load(self.h, b.ctypes.data, b.size), "bg3_checkpoint_load")
+
+    def serialize(self, growth=True, **if_fields):
+        """The reference's checkpoint stream (bg3_serialize) as bytes; if_fields gives the IF
+        neuron arrays the library does not keep (Cm, Rm, Vrest, Vinit, Iinject, Isyn, Tau)."""
+        keep = {k: np.ascontiguousarray(v, np.float32) for k, v in if_fields.items()}
+        f = IfFields(*[_p(keep[k]) if k in keep else None for k in IF_FIELDS])
+        conn = BG3_CONN_GROWTH if growth else BG3_CONN_STATIC
+        n = ctypes.c_uint64()
+        check(self.L.bg3_serialize(self.h, ctypes.byref(f), conn, None, 0, ctypes.byref(n)),
+              "bg3_serialize")
+        buf = ctypes.create_string_buffer(max(n.value, 1))
+        check(self.L.bg3_serialize(self.h, ctypes.byref(f), conn, buf, n.value, ctypes.byref(n)),
+              "bg3_serialize")
+        return buf.raw[:n.value]
+
+    def deserialize(self, data, growth=True, step=0):
+        """Loads a reference checkpoint stream (bg3_deserialize); returns the IF arrays it held
+        that the library does not keep."""
+        out = {k: np.zeros(self.N, np.float32) for k in IF_FIELDS}
+        f = IfFields(*[_p(out[k]) for k in IF_FIELDS])
+        conn = BG3_CONN_GROWTH if growth else BG3_CONN_STATIC
+        check(self.L.bg3_deserialize(self.h, bytes(data), len(data), conn, int(step),
+                                     ctypes.byref(f)), "bg3_deserialize")
+        return out
 
     def record(self):
         """Epoch end of a network without growth (recorder histograms, spike-count roll)."""

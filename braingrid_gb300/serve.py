@@ -24,14 +24,17 @@ class ServeDesc(ctypes.Structure):
 class JobResult(ctypes.Structure):
     _fields_ = [(k, ctypes.POINTER(ctypes.c_float)) for k in
                 ("burstiness", "spikes_hist", "rates_hist", "radii_hist", "Vm")] + \
-               [("synapse_steps", ctypes.c_int64), ("neuron_steps", ctypes.c_int64),
+               [("checkpoint", ctypes.c_void_p), ("checkpoint_cap", ctypes.c_uint64),
+                ("checkpoint_len", ctypes.c_uint64),
+                ("synapse_steps", ctypes.c_int64), ("neuron_steps", ctypes.c_int64),
                 ("status", ctypes.c_int32), ("error_word", ctypes.c_uint32)]
 
 
 class JobDesc(ctypes.Structure):
     _fields_ = [("desc", bg.NetDesc), ("epochs", ctypes.c_int32), ("growth", ctypes.c_int32),
                 ("setup", SETUP_FN), ("user", ctypes.c_void_p),
-                ("result", ctypes.POINTER(JobResult))]
+                ("result", ctypes.POINTER(JobResult)),
+                ("resume", ctypes.c_void_p), ("resume_len", ctypes.c_uint64)]
 
 
 class ServeStats(ctypes.Structure):
@@ -70,9 +73,11 @@ def _bind():
 
 
 class Job:
-    """One simulation: desc (bg.NetDesc), epochs, growth flag and setup(net) filling it."""
+    """One simulation: desc (bg.NetDesc), epochs, growth flag and setup(net) filling it.
+    export=True keeps the finished job's whole state (checkpoint()); resume=<checkpoint> starts
+    the job from an exported state (after setup), continuing its epoch count."""
 
-    def __init__(self, desc, epochs, growth, setup, name=""):
+    def __init__(self, desc, epochs, growth, setup, name="", export=False, resume=None):
         self.desc, self.epochs, self.growth, self.setup, self.name = desc, epochs, growth, setup, name
         N, E, T = desc.n_neurons, desc.max_epochs, desc.epoch_duration
         nb = int(np.float32(E) * np.float32(T))
@@ -84,8 +89,22 @@ class Job:
         self.Vm = np.zeros(N, np.float32)
         self.result = JobResult(*[bg._p(a) for a in (self.burstiness, self.spikes_hist,
                                                       self.rates_hist, self.radii_hist, self.Vm)])
+        self._ckpt = None
+        if export:
+            # the state is the job's device arrays plus a small header
+            self._ckpt = np.empty(bg.footprint(desc) + (1 << 20), np.uint8)
+            self.result.checkpoint = self._ckpt.ctypes.data
+            self.result.checkpoint_cap = self._ckpt.size
+        self._resume = None if resume is None else np.ascontiguousarray(
+            np.frombuffer(resume, np.uint8))
         self.id = None
         self.error = None
+
+    def checkpoint(self):
+        """The exported state of a finished job (export=True)."""
+        if self._ckpt is None:
+            return None
+        return self._ckpt[:self.result.checkpoint_len].copy()
 
     @property
     def footprint(self):
@@ -130,6 +149,9 @@ class Server:
         fn = SETUP_FN(cb)
         jd = JobDesc(job.desc, job.epochs, 1 if job.growth else 0, fn, None,
                      ctypes.pointer(job.result))
+        if job._resume is not None:
+            jd.resume = job._resume.ctypes.data
+            jd.resume_len = job._resume.size
         jid = ctypes.c_int64()
         bg.check(self.L.bg3_serve_submit(self.h, ctypes.byref(jd), ctypes.byref(jid)),
                  "bg3_serve_submit")
@@ -170,7 +192,8 @@ class Server:
 
 # ---- job families of the served stream -------------------------------------------------------
 def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_rate=1.0,
-                   frac_inh=0.10, max_syn=None, epoch_duration=1.0, max_epochs=None, name=""):
+                   frac_inh=0.10, max_syn=None, epoch_duration=1.0, max_epochs=None, name="",
+                   **job_kw):
     """The config[1]/[2] family: LIF + DS + ConnGrowth on a side x side grid, pre-grown to
     radius (mean in-degree ~ pi (2 radius)^2, capped by max_syn), growth at every epoch end."""
     spec_args = dict(frac_inh=frac_inh, seed=seed)
@@ -188,10 +211,11 @@ def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_r
         spec = netgen.lif_network(side, side, **spec_args)
         netgen.configure_lif(net, spec, dict(target_rate=target_rate))
         netgen.pregrow(net, spec, radius, weight_scale=weight_scale, seed=seed + 11)
-    return Job(desc, epochs, True, setup, name or "lif%dx%d" % (side, side))
+    return Job(desc, epochs, True, setup, name or "lif%dx%d" % (side, side), **job_kw)
 
 
-def izh_static_job(width, height, epochs, seed, epoch_duration=1.0, max_epochs=None, name=""):
+def izh_static_job(width, height, epochs, seed, epoch_duration=1.0, max_epochs=None, name="",
+                   **job_kw):
     """The config[3] family: Izhikevich neurons, static wiring (10 nearest within radius 5,
     10 % rewired), dynamic STDP, Poisson drive at 10 Hz / 5 nA; epochs end in the recorder."""
     spec, syn, counts, M = netgen.izh_static_spec(width, height, seed)
@@ -201,4 +225,4 @@ def izh_static_job(width, height, epochs, seed, epoch_duration=1.0, max_epochs=N
 
     def setup(net):
         netgen.configure_izh_static(net, spec, syn, counts, input_seed=seed)
-    return Job(desc, epochs, False, setup, name or "izh%dx%d" % (width, height))
+    return Job(desc, epochs, False, setup, name or "izh%dx%d" % (width, height), **job_kw)

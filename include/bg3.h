@@ -169,6 +169,8 @@ int bg3_destroy(bg3_net *net);
 int64_t bg3_net_footprint(const bg3_net_desc *desc);
 /* Device bytes this network has allocated so far. */
 uint64_t bg3_net_bytes(bg3_net *net);
+/* The shape the network was created with. */
+int bg3_get_desc(bg3_net *net, bg3_net_desc *desc);
 
 /* ---- host -> device ------------------------------------------------------------------- */
 /* IAllNeurons::copyNeuronHostToDevice (Neurons/IAllNeurons.h:114). */
@@ -183,7 +185,9 @@ int bg3_upload_layout(bg3_net *net, const float *xloc, const float *yloc, const 
  * rebuilt on the device.  current_step is g_simulationStep (Utils/Global.h:85). */
 int bg3_upload_synapses(bg3_net *net, const bg3_synapse_arrays *a, uint64_t current_step);
 int bg3_set_type_constants(bg3_net *net, const bg3_type_constants *c);
-/* ConnGrowth state (radii, rates) and parameters (Connections/ConnGrowth.h:219+). */
+/* ConnGrowth state (radii, rates) and parameters (Connections/ConnGrowth.h:219+).  p NULL keeps
+ * the parameters; radii and rates also become row 0 of the recorder's histories
+ * (XmlGrowthRecorder::initValues); NULL arrays are left as they are. */
 int bg3_upload_growth(bg3_net *net, const bg3_growth_params *p, const float *radii,
                       const float *rates);
 /* Sets W of every in-use slot from a reference-layout array (n_neurons * max_syn_per_neuron),
@@ -359,6 +363,59 @@ int bg3_autotune(bg3_net *net, int32_t steps_per_trial, int32_t tune_growth, bg3
                  float *best_ms_per_step);
 int bg3_batch_autotune(bg3_batch *batch, int32_t steps_per_trial, bg3_launch_cfg *best,
                        float *best_ms_per_step);
+
+/* ---- checkpoints (bit-exact resume; no counterpart in the reference) --------------------------
+ * The reference's own checkpoint (Model::serialize, Core/Model.cpp:85-98) prints six significant
+ * digits per value and holds neither the step counter, the noise generator nor the spike
+ * history, so a run restarted from it does not continue the original one.  These two calls save
+ * and restore a network's entire state instead: every device array, the step counter, the
+ * injected noise still to be consumed, the Poisson and regular input state, the tables and the
+ * launch configuration.  A network loaded from a checkpoint continues exactly as the saved one
+ * would have (same spikes, same float bits); device noise is keyed by (seed, step, neuron), so
+ * restoring the step restores the generator.
+ *
+ * bg3_checkpoint_save: with buf == NULL only *len is set (the bytes needed); with cap < *len it
+ * returns BG3_EINVAL and writes nothing.  The format is this library build's own (host byte order,
+ * checked by a header); it is not meant for other programs.
+ * bg3_checkpoint_load: into a network made by bg3_create with the same bg3_net_desc (BG3_EINVAL
+ * otherwise, before anything changes).  Arrays the checkpoint holds that the network lacks (an
+ * input set up before the save) are allocated.  A network that is a member of a batch needs
+ * bg3_batch_refresh afterwards.  If the load fails part way (a CUDA or allocation error), destroy
+ * the network. */
+int bg3_checkpoint_save(bg3_net *net, void *buf, uint64_t cap, uint64_t *len);
+int bg3_checkpoint_load(bg3_net *net, const void *buf, uint64_t len);
+
+/* ---- the reference's checkpoint stream ---------------------------------------------------- */
+enum { BG3_CONN_STATIC = 0, BG3_CONN_GROWTH = 1 };  /* ConnStatic / ConnGrowth */
+/* IF-neuron fields that only the reference's host objects hold: set by AllIFNeurons::
+ * createNeuron and never read by the step (Neurons/AllIFNeurons.h:279-362), so the library does
+ * not keep them.  Each array n_neurons long; NULL arrays are written as 0 and skipped on reading. */
+typedef struct {
+    float *Cm, *Rm, *Vrest, *Vinit, *Iinject, *Isyn, *Tau;
+} bg3_if_fields;
+/* The bytes Model::serialize writes (Core/Model.cpp:85-98; the -w file of Core/BGDriver.cpp:
+ * 110-116): totalNeurons; per neuron the AllIFNeurons::writeNeuron fields (plus the six of
+ * AllIZHNeurons); the synapse count and every in-use synapse, dest row by dest row, with the
+ * writeSynapse fields of the network's synapse class; with BG3_CONN_GROWTH the radii and rates
+ * (ConnGrowth::serialize; ConnStatic writes nothing).  Every value is printed as std::ostream
+ * prints it (floats with six significant digits) and followed by a NUL.  hasFired is written as 0:
+ * the step that sets it also clears it (Neurons/AllSpikingNeurons.cpp:144).  With buf NULL only
+ * *len is set; with cap < *len nothing is written and BG3_EINVAL returned. */
+int bg3_serialize(bg3_net *net, const bg3_if_fields *setup, int32_t conn, char *buf, uint64_t cap,
+                  uint64_t *len);
+/* Loads such a stream into the network (Model::deserialize, Core/Model.cpp:62-76, then the
+ * recorder's initValues as Core/Simulator.cpp:206-214 does: radii and rates become row 0 of the
+ * histories).  The reference's own reader cannot read its writer's layout: AllSynapses::
+ * deserialize (Synapses/AllSynapses.cpp:123-155) reads a neuron index before every synapse that
+ * writeSynapse never writes.  This reader follows the writer: each synapse goes to the next slot of
+ * its dest row, which reproduces the written slots.  current_step is the g_simulationStep the state
+ * belongs to (delay queues, delayIdx and lastSpike are relative to it; the reference's driver
+ * restarts at 0).  Values the library keeps per synapse type or as classes (tau, U/D/F, the STDP
+ * constants) must be representable: BG3_EUNSUPPORTED otherwise, and so for a hasFired of 1 or a
+ * queue length other than 32.  A malformed stream is BG3_EINVAL.  setup_out, when given, receives
+ * the fields of bg3_if_fields. */
+int bg3_deserialize(bg3_net *net, const char *buf, uint64_t len, int32_t conn,
+                    uint64_t current_step, bg3_if_fields *setup_out);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,11 @@
  *      admission creates the network and calls the job's setup callback; the job joins the
  *      batch in the next round;
  *   3. after the chunk, jobs at an epoch end run their epoch pass; finished jobs copy their
- *      results out, free their device memory and are reported by bg3_serve_take.
+ *      results out (and their whole state, when asked: bg3_job_result.checkpoint), free their
+ *      device memory and are reported by bg3_serve_take.
+ * A job may start from an exported state (bg3_job_desc.resume): it continues bit for bit as the
+ * job it came from would have, so long jobs can be split, moved between servers or GPUs, or
+ * preempted and requeued.
  * Every job's arithmetic is independent of the others (device noise is keyed by the job's own
  * seed and step), so a job's results are the same alone and in any mix.
  */
@@ -53,6 +57,11 @@ typedef struct {
  * bg3_download_histories; Vm is the final membrane potential (n_neurons). */
 typedef struct {
     float *burstiness, *spikes_hist, *rates_hist, *radii_hist, *Vm;
+    /* export of the finished job's state (bg3_checkpoint_save) into checkpoint[checkpoint_cap];
+     * NULL: none.  checkpoint_len gets the bytes needed; too small a buffer fails the job with
+     * BG3_EINVAL. */
+    void *checkpoint;
+    uint64_t checkpoint_cap, checkpoint_len;
     /* filled by the server */
     int64_t synapse_steps;       /* sum over the job's steps of its synapse count             */
     int64_t neuron_steps;
@@ -70,6 +79,11 @@ typedef struct {
     bg3_job_setup_fn setup;
     void *user;
     bg3_job_result *result;
+    /* import: a checkpoint (bg3_checkpoint_save of a network with this desc) loaded after setup;
+     * the job continues from its step, its epochs counted from step 0 (a job exported after k
+     * epochs and resumed with `epochs` = n runs n - k more).  NULL: start from setup's state. */
+    const void *resume;
+    uint64_t resume_len;
 } bg3_job_desc;
 
 typedef struct {

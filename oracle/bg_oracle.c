@@ -1056,3 +1056,94 @@ static void record_spikes(bgo_net *n)
         }
     }
 }
+
+/* ---- checkpoint stream ----------------------------------------------------------------------
+ * Model::serialize (Core/Model.cpp:85-98) prints each value with std::ostream's defaults (a float
+ * is printed as the double it converts to, "%.6g"; integers in decimal; bool as 0/1; the synapse
+ * type enum as its int value) and ends it with `ends` (a NUL). */
+typedef struct {
+    char *buf;
+    int64_t cap, len;
+} ser_out;
+
+static void ser_put(ser_out *o, const char *txt)
+{
+    const int64_t k = (int64_t)strlen(txt) + 1; /* with the NUL */
+    if (o->buf && o->len + k <= o->cap) memcpy(o->buf + o->len, txt, (size_t)k);
+    o->len += k;
+}
+static void ser_f(ser_out *o, float v)
+{
+    char t[64];
+    snprintf(t, sizeof t, "%.*g", 6, (double)v);
+    ser_put(o, t);
+}
+static void ser_i(ser_out *o, long long v)
+{
+    char t[32];
+    snprintf(t, sizeof t, "%lld", v);
+    ser_put(o, t);
+}
+static void ser_u(ser_out *o, unsigned long long v)
+{
+    char t[32];
+    snprintf(t, sizeof t, "%llu", v);
+    ser_put(o, t);
+}
+
+int64_t bgo_serialize(const bgo_net *n, int conn_growth, char *buf, int64_t cap)
+{
+    ser_out o = {buf, cap, 0};
+    const int N = n->N;
+    ser_i(&o, N); /* Model::serialize: totalNeurons */
+    for (int i = 0; i < N; i++) {
+        /* AllIFNeurons::writeNeuron (Neurons/AllIFNeurons.cpp:594-613) */
+        ser_f(&o, n->Cm[i]); ser_f(&o, n->Rm[i]); ser_f(&o, n->Vthresh[i]); ser_f(&o, n->Vrest[i]);
+        ser_f(&o, n->Vreset[i]); ser_f(&o, n->Vinit[i]); ser_f(&o, n->Trefract[i]);
+        ser_f(&o, n->Inoise[i]); ser_f(&o, n->Iinject[i]); ser_f(&o, 0.0f /* Isyn */);
+        ser_i(&o, n->refr[i]); ser_f(&o, n->C1[i]); ser_f(&o, n->C2[i]); ser_f(&o, n->I0[i]);
+        ser_f(&o, n->Vm[i]); ser_i(&o, n->hasFired[i] ? 1 : 0); ser_f(&o, n->Tau[i]);
+        if (n->neuron_kind == 1) {
+            /* AllIZHNeurons::writeNeuron (Neurons/AllIZHNeurons.cpp:551-561) */
+            ser_f(&o, n->Aconst[i]); ser_f(&o, n->Bconst[i]); ser_f(&o, n->Cconst[i]);
+            ser_f(&o, n->Dconst[i]); ser_f(&o, n->u_izh[i]); ser_f(&o, n->C3[i]);
+        }
+    }
+    /* AllSynapses::serialize (Synapses/AllSynapses.cpp:163-177): dest rows in order, the first
+     * synapse_counts[dest] slots of each */
+    long long total = 0;
+    for (int d = 0; d < N; d++) total += n->counts[d];
+    ser_i(&o, total);
+    const int dyn = n->syn_kind == 1 || n->syn_kind == 3, stdp = n->syn_kind >= 2;
+    for (int d = 0; d < N; d++)
+        for (uint32_t k = 0; k < n->counts[d]; k++) {
+            const size_t s = (size_t)d * (size_t)n->max_syn + k;
+            /* AllSynapses::writeSynapse (:207-215) */
+            ser_i(&o, n->src[s]); ser_i(&o, n->dest[s]); ser_f(&o, n->W[s]); ser_f(&o, n->psr[s]);
+            ser_i(&o, n->type[s]); ser_i(&o, n->in_use[s] ? 1 : 0);
+            /* AllSpikingSynapses::writeSynapse (Synapses/AllSpikingSynapses.cpp:168-178) */
+            ser_f(&o, n->decay[s]); ser_i(&o, n->total_delay[s]); ser_u(&o, n->queue[s]);
+            ser_i(&o, n->delayIdx[s]); ser_i(&o, n->ldelayQueue[s]); ser_f(&o, n->tau[s]);
+            if (stdp) {
+                /* AllSTDPSynapses::writeSynapse (Synapses/AllSTDPSynapses.cpp:209-228) */
+                ser_i(&o, n->total_delayPost[s]); ser_u(&o, n->queuePost[s]);
+                ser_i(&o, n->delayIdxPost[s]); ser_i(&o, n->ldelayQueuePost[s]);
+                ser_f(&o, n->tauspost[s]); ser_f(&o, n->tauspre[s]); ser_f(&o, n->taupos[s]);
+                ser_f(&o, n->tauneg[s]); ser_f(&o, n->STDPgap[s]); ser_f(&o, n->Wex[s]);
+                ser_f(&o, n->Aneg[s]); ser_f(&o, n->Apos[s]); ser_f(&o, n->mupos[s]);
+                ser_f(&o, n->muneg[s]); ser_i(&o, n->useFD[s] ? 1 : 0);
+            }
+            if (dyn) {
+                /* AllDSSynapses::writeSynapse (Synapses/AllDSSynapses.cpp:142-152),
+                 * AllDynamicSTDPSynapses::writeSynapse (AllDynamicSTDPSynapses.cpp:142-152) */
+                ser_u(&o, n->lastSpike[s]); ser_f(&o, n->r[s]); ser_f(&o, n->u[s]);
+                ser_f(&o, n->D[s]); ser_f(&o, n->U[s]); ser_f(&o, n->F[s]);
+            }
+        }
+    if (conn_growth) {
+        /* ConnGrowth::serialize (Connections/ConnGrowth.cpp:254-265) */
+        for (int i = 0; i < N; i++) ser_f(&o, n->radii[i]);
+        for (int i = 0; i < N; i++) ser_f(&o, n->rates[i]);
+    }
+    return o.len;
+}

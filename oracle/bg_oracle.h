@@ -102,7 +102,12 @@ void bgo_rng_skip(bgo_net *n, int64_t draws);
 /* STDP constants of synapses created from now on (the reference hard-codes them in
  * AllSTDPSynapses::createSynapse): Apos, Aneg, STDPgap, tauspost, tauspre, taupos, tauneg,
  * WexE (excitatory source), WexI (inhibitory source), mupos, muneg. */
-void bgo_stdp_params(bgo_net *n, const float *p11);              /* bit0: a row hit maxSynapsesPerNeuron          */
+void bgo_stdp_params(bgo_net *n, const float *p11);
+/* The reference's checkpoint stream (Model::serialize, Core/Model.cpp:85-98): totalNeurons, the
+ * neurons, the in-use synapses, and with conn_growth the ConnGrowth radii and rates; every value
+ * printed as std::ostream prints it and followed by a NUL.  Isyn, which the reference allocates
+ * and never sets, is written as 0.  Returns the stream's length; writes it when cap suffices. */
+int64_t bgo_serialize(const bgo_net *n, int conn_growth, char *buf, int64_t cap);              /* bit0: a row hit maxSynapsesPerNeuron          */
 
 #ifdef __cplusplus
 }

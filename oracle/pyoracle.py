@@ -81,6 +81,8 @@ def lib():
         L.bgo_stdp_signed.argtypes = [vp, i]
         L.bgo_rng_skip.argtypes = [vp, i64]
         L.bgo_stdp_params.argtypes = [vp, ctypes.POINTER(f)]
+        L.bgo_serialize.restype = i64
+        L.bgo_serialize.argtypes = [vp, i, ctypes.c_char_p, i64]
         L.bgo_norm_fill.argtypes = [u32, ctypes.POINTER(f), i64]
         L.bgo_input_regular.argtypes = [vp, f, f, i, ctypes.POINTER(f)]
         L.bgo_input_regular.restype = i
@@ -241,6 +243,13 @@ class OracleNet:
 
     def rng_skip(self, draws):
         self.L.bgo_rng_skip(self.h, int(draws))
+
+    def serialize(self, conn_growth=True):
+        """The reference's checkpoint stream (Model::serialize) of the current state, as bytes."""
+        n = self.L.bgo_serialize(self.h, 1 if conn_growth else 0, None, 0)
+        buf = ctypes.create_string_buffer(int(n))
+        assert self.L.bgo_serialize(self.h, 1 if conn_growth else 0, buf, n) == n
+        return buf.raw
 
     def stdp_params(self, p11):
         self._stdp = np.asarray(p11, dtype=np.float32)

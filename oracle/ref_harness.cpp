@@ -7,13 +7,17 @@
 //
 //   bg_ref_harness -t config.xml -o dump.bin [-s stim.xml] [--epochs E] [--tsim SECONDS]
 //                  [--dump-every K] [--dump-syn-every K] [--radii R] [--maxsyn M]
-//                  [--record-noise] [--steps-limit S]
+//                  [--record-noise] [--steps-limit S] [--serialize FILE]
+//
+// --serialize writes the reference's checkpoint stream (Simulator::serialize, Core/
+// Simulator.cpp:225-232) at the end of the run, where Core/BGDriver.cpp:110-116 writes it.
 //
 // Dump format: "BGR1", then records: name[24] (NUL padded), dtype char ('f' float32,
 // 'd' float64, 'i' int32, 'I' uint32, 'Q' uint64, 'B' uint8), 7 pad bytes, uint64 count,
 // uint64 step, then count elements.  A record named "end" closes the file.
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -316,7 +320,7 @@ static void override_stdp(HarnessModel *m, SimulationInfo *si, const BGFLOAT *p)
 
 int main(int argc, char **argv)
 {
-    std::string cfg, out, stim;
+    std::string cfg, out, stim, ser;
     BGFLOAT stdp_p[11];
     int n_stdp = 0;
     int epochs = -1, dump_every = 0, dump_syn_every = 0, maxsyn = -1;
@@ -335,6 +339,7 @@ int main(int argc, char **argv)
         else if (a == "--radii") radii = atof(argv[++i]);
         else if (a == "--maxsyn") maxsyn = atoi(argv[++i]);
         else if (a == "--record-noise") record_noise = true;
+        else if (a == "--serialize") ser = argv[++i];
         else if (a == "--steps-limit") steps_limit = atol(argv[++i]);
         else if (a == "--stdp") {
             // Apos,Aneg,STDPgap,tauspost,tauspre,taupos,tauneg,WexE,WexI,mupos,muneg
@@ -423,6 +428,11 @@ int main(int argc, char **argv)
     fclose(g_out);
     if (si->pInput) { si->pInput->term(si); }
     sim->saveData(si);
+    if (!ser.empty()) {
+        std::ofstream mo(ser.c_str(), std::ofstream::binary | std::ofstream::trunc);
+        sim->serialize(mo, si);
+        mo.close();
+    }
     if (si->simRecorder) si->simRecorder->term();
     return 0;
 }

@@ -8,7 +8,9 @@ It (1) writes the network configs and NLists under tests/golden/configs/, (2) bu
 reference single-threaded simulator and oracle/ref_harness.cpp with oracle/ref.mk, (3) runs the
 harness on each case, and (4) keeps a compact subset of each dump as tests/golden/<case>.npz.
 The reference's own CPU golden outputs for test-tiny and test-small
-(old/validation/4-2016/growth/test-{tiny,small}-out.xml) are parsed into ref_goldens.npz.
+(old/validation/4-2016/growth/test-{tiny,small}-out.xml) are parsed into ref_goldens.npz, and the
+reference's checkpoint stream at the end of a few cases (Simulator::serialize) goes to
+serialize.npz (--only-serialize rewrites that file alone).
 
 Nothing at test time reads the reference tree: the tests only read the .npz files written here.
 """
@@ -36,10 +38,16 @@ def build_reference(ref, fp64=False):
     return os.path.join(ROOT, "oracle", "_ref64" if fp64 else "_ref", "bg_ref_harness")
 
 
-def run_harness(harness, workdir, cfg, args, out):
+def run_harness(harness, workdir, cfg, args, out, serialize=None):
     cmd = [harness, "-t", cfg, "-o", out] + args
+    if serialize:
+        cmd += ["--serialize", serialize]
     subprocess.check_call(cmd, cwd=workdir, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return read_dump(out)
+
+
+# cases whose end-of-run checkpoint stream (Simulator::serialize) is kept in serialize.npz
+SERIALIZE_CASES = ("c0_grown", "c0_spiking", "c0_stdp", "izh_dstdp", "izh_static")
 
 
 def compact(d, keep_steps_every=None, syn_keep=None):
@@ -118,6 +126,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--cases", default="")
+    ap.add_argument("--only-serialize", action="store_true",
+                    help="write serialize.npz only (the other fixtures stay as they are)")
     a = ap.parse_args()
     harness = build_reference(a.ref)
     harness64 = build_reference(a.ref, fp64=True)
@@ -127,6 +137,17 @@ def main():
         shutil.copytree(os.path.join(a.ref, "configfiles"), cfgdir)
         write_config_tree(cfgdir)
         os.makedirs(os.path.join(work, "results"), exist_ok=True)
+        ser = {}
+        for case in CASES:
+            if case["name"] in SERIALIZE_CASES:
+                path = os.path.join(work, case["name"] + ".ser")
+                run_harness(harness, work, case["config"], case["args"],
+                            os.path.join(work, case["name"] + ".sbin"), serialize=path)
+                ser[case["name"]] = np.frombuffer(open(path, "rb").read(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, "serialize.npz"), **ser)
+        print("wrote serialize", sorted(ser))
+        if a.only_serialize:
+            return
         selected = [c for c in CASES if not a.cases or c["name"] in a.cases.split(",")]
         for case in selected:
             h = harness64 if case.get("fp64") else harness

@@ -3,7 +3,8 @@ import numpy as np
 
 from braingrid_gb300 import lib as bg
 from oracle import pyoracle as po
-from tests.netcases import assert_same
+from tests.golden.configs import case
+from tests.netcases import assert_same, oracle_from_case, steps_per_epoch
 
 LIF_MAP = [("Vm", "Vm"), ("Vthresh", "Vthresh"), ("Vreset", "Vreset"), ("I0", "I0"),
            ("Inoise", "Inoise"), ("C1", "C1"), ("C2", "C2"), ("Trefract", "Trefract"),
@@ -152,3 +153,49 @@ def compare_maps(net, o, where):
     assert_same(where + " outCount", m["outgoingSynapseCount"], o.arr("outCount"))
     assert_same(where + " inMap", m["incomingSynapseIndexMap"], o.arr("inMap"))
     assert_same(where + " inCount", m["incomingSynapseCount"], o.arr("inCount"))
+
+
+def _growth_both(o, net, e, resync=True):
+    o.growth()
+    o.record_epoch(e)
+    net.growth(e)
+    r, q = net.download_growth()
+    assert_same("radii after growth %d" % e, r, o.arr("radii"))
+    assert_same("rates after growth %d" % e, q, o.arr("rates"))
+    compare_synapses(net, o, "growth %d" % e, tol_fields=("W",))
+    compare_maps(net, o, "growth %d" % e)
+    if resync:
+        net.upload_weights(o.arr("W"))
+
+
+def run_locked(name, epochs=None, check_every=1, syn_every=None, stdp_signed=False):
+    c = case(name)
+    E = epochs or c["epochs"]
+    spe = steps_per_epoch(c)
+    o = oracle_from_case(c)
+    if stdp_signed:
+        o.stdp_signed(True)
+    net = gpu_from_oracle(o, c, n_noise=c["N"] * spe * E + 64, isi_steps=spe * E + 2)
+    t = 0
+    for e in range(E):
+        for _ in range(spe):
+            o.step_n(1)
+            net.step(1)
+            t += 1
+            if t % check_every == 0:
+                compare_neurons(net, o, "step %d" % t)
+                compare_input(net, o, "step %d" % t)
+            if syn_every and t % syn_every == 0 and o.total:
+                compare_synapses(net, o, "step %d" % t)
+        compare_neurons(net, o, "epoch %d end" % e)
+        compare_history(net, o, "epoch %d" % e)
+        if o.total:
+            compare_synapses(net, o, "epoch %d end" % e)
+        if c.get("static"):
+            o.record_static()
+            net.record()
+            compare_neurons(net, o, "record %d" % e)
+        else:
+            _growth_both(o, net, e + 1)
+    assert net.error_word == 0
+    return o, net

@@ -132,3 +132,35 @@ def test_work_budget_backfills_small_jobs_past_a_large_one():
     assert len(done) == 5 and all(j.result.status == 0 for j in big + small)
     for j, a in zip(big, alone):
         check_same(a, j.outputs(), j.name)
+
+
+@pytest.mark.parametrize("family", ["lif", "izh"])
+def test_exported_job_resumes_bit_exact(family):
+    """A job exported after 2 of 4 epochs and resumed as a new job, in another server and among
+    other jobs, ends with the results of the same job run for 4 epochs in one go."""
+    def job(epochs, **kw):
+        if family == "lif":
+            return serve.lif_growth_job(14, epochs, seed=7, radius=2.0, epoch_duration=T,
+                                        max_epochs=4, **kw)
+        return serve.izh_static_job(16, 12, epochs, seed=8, epoch_duration=T, max_epochs=4, **kw)
+    want = run_alone(job(4))
+    first = job(2, export=True)
+    run_alone(first)
+    ck = first.checkpoint()
+    assert ck is not None and ck.size > 0
+    second = job(4, resume=ck)
+    srv = serve.Server(max_resident=3, chunk_steps=300)
+    srv.submit(second)
+    for j in make_jobs()[:2]:
+        srv.submit(j)
+    srv.run_all()
+    srv.close()
+    assert second.result.status == 0, second.error
+    check_same(want, second.outputs(), "resumed " + family)
+    # a checkpoint already at its last epoch leaves nothing to run: the job fails, no GPU work
+    done = job(2, resume=ck)
+    srv = serve.Server(max_resident=1, chunk_steps=300)
+    srv.submit(done)
+    srv.run_all()
+    srv.close()
+    assert done.result.status == bg.BG3_EINVAL
