@@ -170,6 +170,7 @@ def run_bg3(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     from braingrid_gb300 import lib as bg
+    from braingrid_gb300 import shard
     spec, net = build_network()
     N = spec["N"]
     S = net.total_synapses()
@@ -191,10 +192,8 @@ def run_bg3(args):
         dist.barrier()
     c1 = net.download_lif(fields=("spikeCount",))["spikeCount"].astype(np.int64)
     t_total = float(np.sum(ms)) / 1e3
-    if world > 1:
-        t = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
+    # whole job: units of every replica over the slowest replica's time (no-op at N = 1)
+    _, t_total = shard.reduce_timing(S * args.steps, t_total, device="cuda")
     deliveries = float(((c1 - c0) * maps["outgoingSynapseCount"].astype(np.int64)).sum()) / args.steps
     rate_hz = float((c1 - c0).mean()) / (args.steps * 1e-4)
     value = S * args.steps * world / t_total
@@ -230,6 +229,7 @@ def run_bg3(args):
         net.download_lif(fields=("spikeCount",), out={"spikeCount": out_counts})
     net.sync()
     e2e_s = time.perf_counter() - t0
+    _, e2e_s = shard.reduce_timing(0, e2e_s, device="cuda")
     e2e = {"value": S * E2E_STEPS * e2e_iters * world / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS}
     err = net.error_word
@@ -240,6 +240,15 @@ def run_bg3(args):
         izh_stdp = run_c3(min(args.steps, 1000), max(args.warmup, 20))
         if args.serve_jobs > 0:
             served = run_served(args.serve_jobs, int(args.serve_slots))
+    else:
+        # the batched and served forms spread over the ranks by instance (bin packed, no
+        # collective); whole-job figures over the slowest rank
+        batched = run_batch_sharded("config[2]", rank, world, min(args.steps, 500),
+                                    max(args.warmup, 20))
+        izh_stdp = run_batch_sharded("config[3]", rank, world, min(args.steps, 1000),
+                                     max(args.warmup, 20))
+        if args.serve_jobs > 0:
+            served = run_served_sharded(args.serve_jobs, int(args.serve_slots), rank, world)
     if rank == 0:
         cpu = cpu_baseline_port(net, spec)
         tr = traffic_per_launch(S)
@@ -344,6 +353,71 @@ def run_batched(steps, warmup):
     return out
 
 
+def run_batch_sharded(which, rank, world, steps, warmup):
+    """config[2] or config[3] over N GPUs: each rank builds and batches its share of the networks
+    (bin packed by synapse slots, the same split on every rank) and times its own batch; the
+    whole-job rate is every rank's synapse-steps over the slowest rank's time."""
+    from braingrid_gb300 import lib as bg
+    from braingrid_gb300 import netgen, shard, workloads
+    if which == "config[2]":
+        members = workloads.c2_members()
+        weights = [m["width"] * m["height"] * m["max_syn"] for m in members]
+        mine = shard.share(list(range(len(members))), weights, rank, world)
+        nets = [workloads.build_member(members[i])[1] for i in mine]
+    else:
+        shapes = workloads.c3_shapes()
+        weights = [w * h for w, h in shapes]
+        mine = shard.share(list(range(len(shapes))), weights, rank, world)
+        nets = [netgen.make_izh_static(shapes[k][0], shapes[k][1], seed=1000 + k,
+                                       max_epochs=10)[1] for k in mine]
+    S = sum(n.total_synapses() for n in nets)
+    N = sum(n.N for n in nets)
+    t = 0.0
+    if nets:
+        batch = bg.Batch(nets)
+        batch.autotune(steps_per_trial=100)
+        batch.step(warmup)
+        batch.sync()
+        t = float(np.sum(batch.bench_steps(steps))) / 1e3
+        batch.close()
+    for n in nets:
+        n.close()
+    units, t_max = shard.reduce_timing(S * steps, t, device="cuda")
+    neuron_units, _ = shard.reduce_timing(N * steps, t, device="cuda")
+    return {"workload": "%s sharded over %d GPUs by instance (%d networks on rank %d)"
+                        % (which, world, len(mine), rank),
+            "batched_synapse_updates_per_s": units / t_max if t_max > 0 else None,
+            "batched_neuron_steps_per_s": neuron_units / t_max if t_max > 0 else None,
+            "batched_ms_per_step": t_max * 1e3 / steps, "steps": steps}
+
+
+def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
+    """config[4] over N GPUs: every rank serves its share of the same trace (jobs bin packed by
+    work, arrival times kept) with its own job server; latencies are gathered on rank 0."""
+    from braingrid_gb300 import serve, shard, workloads
+    trace = serve.sharded_trace(workloads.c4_trace(n_jobs), rank, world)
+    srv = serve.Server(hbm_budget_bytes=workloads.C4_BUDGET, max_resident=64,
+                       chunk_steps=chunk_steps, max_resident_slots=slots_cap)
+    shard.barrier()  # one trace clock for all ranks
+    times = serve.run_trace(srv, trace) if trace else {}
+    srv.close()
+    mine = [(job.name, times[job.id][0], times[job.id][1], int(job.result.synapse_steps),
+             int(job.result.status)) for _, job in trace]
+    every = shard.gather(mine)
+    if every is None:
+        return None
+    rows = [r for part in every for r in part]
+    lat = [f - a for _, a, f, _, _ in rows]
+    span = max(f for _, _, f, _, _ in rows) - min(a for _, a, _, _, _ in rows)
+    pct = shard.latency_percentiles(lat)
+    syn = sum(r[3] for r in rows)
+    return {"workload": "config[4]: %d-job trace sharded over %d GPUs by job work" % (n_jobs, world),
+            "jobs": len(rows), "all_ok": all(r[4] == 0 for r in rows),
+            "served_p50_s": pct["p50"], "served_p95_s": pct["p95"], "served_p99_s": pct["p99"],
+            "served_makespan_s": span, "served_synapse_updates_per_s": syn / span,
+            "jobs_per_rank": [len(part) for part in every]}
+
+
 def run_growth():
     """ConnGrowth epoch pass (radii update, O(N^2) overlap scan, weight update / synapse
     creation, map rebuild, recorder) on config[1]: at the stated start radius 0.4 (every pair
@@ -440,24 +514,9 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     trace = workloads.c4_trace(n_jobs)
     srv = serve.Server(hbm_budget_bytes=workloads.C4_BUDGET, max_resident=64,
                        chunk_steps=chunk_steps, max_resident_slots=slots_cap)
-    pending = list(trace)
-    arrival = {}
-    lat, finish = {}, {}
-    t0 = _t.perf_counter()
-    while pending or srv.jobs:
-        now = _t.perf_counter() - t0
-        while pending and pending[0][0] <= now:
-            a, job = pending.pop(0)
-            srv.submit(job)
-            arrival[job.id] = a
-        if not srv.jobs:
-            _t.sleep(max(0.0, pending[0][0] - (_t.perf_counter() - t0)))
-            continue
-        srv.pump()
-        now = _t.perf_counter() - t0
-        for job in srv.take():
-            lat[job.id] = now - arrival[job.id]
-            finish[job.id] = now
+    times = serve.run_trace(srv, trace)
+    lat = {k: f - a for k, (a, f) in times.items()}
+    finish = {k: f for k, (_, f) in times.items()}
     st = srv.stats()
     srv.close()
     jobs = [j for _, j in trace]

@@ -190,6 +190,41 @@ class Server:
         return done
 
 
+# ---- arrival traces ---------------------------------------------------------------------------
+def run_trace(srv, trace, clock=None, sleep=None):
+    """Serves an open-loop arrival trace [(arrival_s, job)] (ascending arrivals) on srv in real
+    time: each job is submitted once the clock passes its arrival.  Returns {job.id: (arrival_s,
+    finish_s)} on the trace's clock (finish = when bg3_serve_take reported it)."""
+    import time
+    clock = clock or time.perf_counter
+    sleep = sleep or time.sleep
+    pending = list(trace)
+    arrival, out = {}, {}
+    t0 = clock()
+    while pending or srv.jobs:
+        now = clock() - t0
+        while pending and pending[0][0] <= now:
+            a, job = pending.pop(0)
+            srv.submit(job)
+            arrival[job.id] = a
+        if not srv.jobs:
+            sleep(max(0.0, pending[0][0] - (clock() - t0)))
+            continue
+        srv.pump()
+        now = clock() - t0
+        for job in srv.take():
+            out[job.id] = (arrival[job.id], now)
+    return out
+
+
+def sharded_trace(trace, rank, world):
+    """The part of a trace that rank `rank` of `world` serves: jobs bin packed by work (synapse
+    slots x simulated seconds), arrival times kept.  Every rank computes the same split."""
+    from . import shard
+    w = [shard.job_weight(job.desc, job.epochs) for _, job in trace]
+    return [trace[i] for i in shard.partition(w, world)[rank]]
+
+
 # ---- job families of the served stream -------------------------------------------------------
 def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_rate=1.0,
                    frac_inh=0.10, max_syn=None, epoch_duration=1.0, max_epochs=None, name="",

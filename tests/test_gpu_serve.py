@@ -164,3 +164,26 @@ def test_exported_job_resumes_bit_exact(family):
     srv.run_all()
     srv.close()
     assert done.result.status == bg.BG3_EINVAL
+
+
+def test_sharded_trace_serves_every_job_once_with_unchanged_results():
+    """The served stream split over two ranks (run here one after the other on one GPU): every
+    job is served by exactly one rank and its results equal the job run alone."""
+    alone = [run_alone(j) for j in make_jobs()]
+    trace = [(0.02 * i, j) for i, j in enumerate(make_jobs())]
+    index = {id(j): i for i, (_, j) in enumerate(trace)}
+    seen = []
+    for rank in range(2):
+        part = serve.sharded_trace(trace, rank, 2)
+        assert part, "both ranks get work"
+        srv = serve.Server(max_resident=3, chunk_steps=300)
+        times = serve.run_trace(srv, part)
+        srv.close()
+        for a, j in part:
+            assert j.result.status == 0, (j.name, j.error)
+            arrival, finish = times[j.id]
+            assert arrival == a and finish >= a
+            i = index[id(j)]
+            check_same(alone[i], j.outputs(), "rank %d %s" % (rank, j.name))
+            seen.append(i)
+    assert sorted(seen) == list(range(len(trace)))
