@@ -377,7 +377,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     h.n_spike_bins = (int)((float)D.max_epochs * D.epoch_duration * 100.0f);
     int rc = 0;
 #define A(ptr, cnt) if ((rc = dalloc(n, &h.ptr, (cnt))) != 0) goto fail;
-    A(step, 1) A(sweep_done, 1) A(err, 1) A(noise_cursor, 1)
+    A(step, 1) A(sweep_done, 1) A(dstep, 1) A(dlv_done, 1) A(err, 1) A(noise_cursor, 1)
     A(Vm, N) A(Vthresh, N) A(Vreset, N) A(I0, N) A(Inoise, N) A(C1, N) A(C2, N) A(Trefract, N)
     A(sp, N) A(refr, N) A(spikeCount, N) A(spikeCountOffset, N) A(ntype, N)
     A(ring, N * BG3_RING) A(ring_n, BG3_RING)
@@ -457,7 +457,8 @@ int64_t bg3_net_footprint(const bg3_net_desc *desc)
     const uint64_t nb = (uint64_t)std::max((int)((float)D.max_epochs * D.epoch_duration), 1);
     const uint64_t ns = (uint64_t)std::max((int)((float)D.max_epochs * D.epoch_duration * 100.0f), 1);
     const uint64_t E1 = (uint64_t)D.max_epochs + 1;
-    uint64_t b = 8 + 4 + 4 + 8;                                   // step, sweep_done, err, cursor
+    uint64_t b = 8 + 4 + 8 + 4 + 4 + 8;                   // step, sweep_done, dstep, dlv_done,
+                                                          // err, cursor
     b += N * (9 * 4 + 3 * 4 + 1);                                  // neuron SoA + ntype
     b += N * BG3_RING * 4 + BG3_RING * 4;                          // spike ring
     b += S * (4 + 1 + 1 + sizeof(EvSlot) + 4 + 1 + 4) + N * 4;     // planes, outMap, count
@@ -685,6 +686,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
         return rc;
     unsigned long long s64 = step;
     CK(cudaMemcpyAsync(h.step, &s64, sizeof(s64), cudaMemcpyHostToDevice, n->stream));
+    CK(cudaMemcpyAsync(h.dstep, &s64, sizeof(s64), cudaMemcpyHostToDevice, n->stream));
     CK(cudaStreamSynchronize(n->stream));
     bg3::launch_rebuild_maps(h, n->d, n->stream);
     CK(cudaGetLastError());
@@ -935,14 +937,17 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         CK(cudaGetLastError());
         return BG3_OK;
     }
+    // neuron pass and arrivals of the first step, then (fused sweep of step t, arrivals of step
+    // t + 1) pairs, so that each delivery pass overlaps the sweep before it, then the last sweep
     bg3::launch_neurons(h, n->stream);
+    bg3::launch_deliver(h, n->cfg, n->stream);
     int64_t interior = nsteps - 1;
     if (interior >= GRAPH_STEPS && !n->graph) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < GRAPH_STEPS; i++) {
-            bg3::launch_deliver(h, n->cfg, n->stream);
             bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, true, n->cfg, n->stream);
+            bg3::launch_deliver(h, n->cfg, n->stream);
         }
         CK(cudaStreamEndCapture(n->stream, &g));
         cudaError_t e = cudaGraphInstantiate(&n->graph, g, 0);
@@ -954,10 +959,9 @@ static int run_steps(bg3_net *n, int64_t nsteps)
         interior -= GRAPH_STEPS;
     }
     for (int64_t i = 0; i < interior; i++) {
-        bg3::launch_deliver(h, n->cfg, n->stream);
         bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, true, n->cfg, n->stream);
+        bg3::launch_deliver(h, n->cfg, n->stream);
     }
-    bg3::launch_deliver(h, n->cfg, n->stream);
     bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, false, n->cfg, n->stream);
     n->launches += 1 + step_kernels(h.syn_kind) * nsteps;
     CK(cudaGetLastError());
@@ -1453,11 +1457,13 @@ int bg3_batch_refresh(bg3_batch *b)
     return batch_refresh(b);
 }
 
+// (fused sweep of step t, arrivals of step t + 1) pairs: each delivery pass overlaps the sweep
+// before it
 static void batch_interior(bg3_batch *b, int64_t n)
 {
     for (int64_t i = 0; i < n; i++) {
-        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, (int)b->nets.size(), b->cfg, b->stream);
         bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, true, b->cfg, b->stream);
+        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, (int)b->nets.size(), b->cfg, b->stream);
     }
 }
 
@@ -1469,6 +1475,7 @@ int bg3_batch_step(bg3_batch *b, int64_t nsteps)
     if (rc) return rc;
     const int M = (int)b->nets.size();
     bg3::launch_neurons_batch(b->d_nets, M, b->max_n, b->stream);
+    bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
     int64_t interior = nsteps - 1;
     if (interior >= GRAPH_STEPS && !b->graph) {
         cudaGraph_t g;
@@ -1484,7 +1491,6 @@ int bg3_batch_step(bg3_batch *b, int64_t nsteps)
         interior -= GRAPH_STEPS;
     }
     batch_interior(b, interior);
-    bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
     bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, false, b->cfg, b->stream);
     const int sweeps = (b->n_thick > 0) + (b->ntiles > b->n_thick);
     b->launches += 1 + (step_kernels(b->syn_kind) - 1 + sweeps) * nsteps;
@@ -1542,16 +1548,24 @@ int bg3_bench_steps(bg3_net *n, int64_t nsteps, int64_t flush_bytes, float *step
                                                    (size_t)flush_bytes / 16,
                                                    (float *)((char *)n->scrub_buf + flush_bytes));
         }
-        // three events per step: [neurons (injected-noise mode)] deliver | sweep; in device-noise
-        // mode the neuron pass runs in the previous sweep's epilogue (standalone before step 0)
         cudaEvent_t *e = &ev[(size_t)s * 3];
         const bool last = s == nsteps - 1;
         if (!inject && s == 0) bg3::launch_neurons(h, n->stream);
         CK(cudaEventRecord(e[0], n->stream));
-        if (inject) bg3::launch_neurons(h, n->stream);
-        bg3::launch_deliver(h, n->cfg, n->stream);
-        if (kernel_ms) CK(cudaEventRecord(e[1], n->stream));
-        bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, !inject && !last, n->cfg, n->stream);
+        if (inject || kernel_ms) {
+            // three events per step: [neurons (injected-noise mode)] deliver | sweep; in
+            // device-noise mode the neuron pass runs in the previous sweep's epilogue
+            if (inject) bg3::launch_neurons(h, n->stream);
+            bg3::launch_deliver(h, n->cfg, n->stream);
+            if (kernel_ms) CK(cudaEventRecord(e[1], n->stream));
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, !inject && !last, n->cfg, n->stream);
+        } else {
+            // as bg3_step runs them: the sweep of step s and the arrivals of step s + 1, which
+            // overlap it (the first step's arrivals open the first timed region)
+            if (s == 0) bg3::launch_deliver(h, n->cfg, n->stream);
+            bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, !last, n->cfg, n->stream);
+            if (!last) bg3::launch_deliver(h, n->cfg, n->stream);
+        }
         CK(cudaEventRecord(e[2], n->stream));
     }
     n->launches += (step_kernels(h.syn_kind) + (inject ? 1 : 0)) * nsteps + (inject ? 0 : 1);
@@ -1598,9 +1612,12 @@ int bg3_batch_bench_steps(bg3_batch *b, int64_t nsteps, int64_t flush_bytes, flo
             k_scrub<<<2 * 152, 512, 0, b->stream>>>((const float4 *)b->scrub_buf, (size_t)flush_bytes / 16,
                                                    (float *)((char *)b->scrub_buf + flush_bytes));
         }
+        // the sweep of step s and the arrivals of step s + 1, which overlap it, as bg3_batch_step
+        // runs them (the first step's arrivals open the first timed region)
         CK(cudaEventRecord(ev[2 * s], b->stream));
-        bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
+        if (s == 0) bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
         bg3::launch_sweep_batch(b->d_nets, b->d_maps, b->d_tiles, b->n_thick, b->ntiles - b->n_thick, s < nsteps - 1, b->cfg, b->stream);
+        if (s < nsteps - 1) bg3::launch_deliver_batch(b->syn_kind, b->d_nets, M, b->cfg, b->stream);
         CK(cudaEventRecord(ev[2 * s + 1], b->stream));
     }
     const int sweeps = (b->n_thick > 0) + (b->ntiles > b->n_thick);
@@ -1638,12 +1655,13 @@ static bool cfg_valid(const bg3_launch_cfg *c)
            c->thin_max_quads >= 1 && c->thin_max_quads <= 4096 && c->thin_warps >= 1 &&
            c->thin_warps <= 32 && c->deliver_blocks >= 1 && c->deliver_blocks <= 65535 &&
            (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512) &&
-           (c->sweep_dests == 16 || c->sweep_dests == 32);
+           (c->sweep_dests == 16 || c->sweep_dests == 32) &&
+           (c->deliver_early == 0 || c->deliver_early == 1);
 }
 static LaunchCfg cfg_from(const bg3_launch_cfg &c)
 {
     return LaunchCfg{c.sweep_stages, c.thin_max_quads, c.thin_warps, c.deliver_blocks,
-                     c.growth_threads, c.sweep_dests};
+                     c.growth_threads, c.sweep_dests, c.deliver_early};
 }
 static bg3_launch_cfg cfg_to(const LaunchCfg &c)
 {
@@ -1654,6 +1672,7 @@ static bg3_launch_cfg cfg_to(const LaunchCfg &c)
     o.deliver_blocks = c.deliver_blocks;
     o.growth_threads = c.growth_threads;
     o.sweep_dests = c.sweep_dests;
+    o.deliver_early = c.deliver_early;
     return o;
 }
 
@@ -1761,6 +1780,7 @@ static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool batch, Trial
     if (mq > 4 && mq <= 64 && (rc = try_param(&LaunchCfg::thin_max_quads, {mq - 1, mq}))) return rc;
     if ((thin || mq <= 64) && (rc = try_param(&LaunchCfg::thin_warps, {4, 8, 16}))) return rc;
     if ((rc = try_param(&LaunchCfg::deliver_blocks, {152, 304, 608}))) return rc;
+    if ((rc = try_param(&LaunchCfg::deliver_early, {0, 1}))) return rc;
     return BG3_OK;
 }
 
@@ -1889,7 +1909,7 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
 // the size of its allocation; bg3_checkpoint_save refuses a network holding an allocation that
 // this list does not name, so a new array cannot be left out silently.
 #define BG3_NET_ARRAYS(X)                                                                         \
-    X(step) X(sweep_done) X(err) X(noise_cursor) X(Vm) X(Vthresh) X(Vreset) X(I0) X(Inoise)       \
+    X(step) X(sweep_done) X(dstep) X(dlv_done) X(err) X(noise_cursor) X(Vm) X(Vthresh) X(Vreset) X(I0) X(Inoise)       \
     X(C1) X(C2) X(Trefract) X(sp) X(refr) X(spikeCount) X(spikeCountOffset) X(history) X(ntype)   \
     X(Aconst) X(Bconst) X(Cconst) X(Dconst) X(u_izh) X(C3) X(ring) X(ring_n) X(psr) X(dcls)       \
     X(lcls) X(ev) X(src) X(stype) X(count) X(dtab) X(ltab) X(outBegin) X(outCount) X(outMap)      \
@@ -1913,7 +1933,7 @@ struct CkptHeader {
     uint32_t n_arrays;         // CKPT_ARRAYS
     uint32_t pad;
 };
-static const uint32_t CKPT_VERSION = 1;
+static const uint32_t CKPT_VERSION = 2;
 static const char CKPT_MAGIC[8] = {'B', 'G', '3', 'C', 'K', 'P', 'T', 0};
 
 static size_t alloc_size(const bg3_net *n, const void *p)

@@ -67,8 +67,10 @@ struct LaunchCfg {
     int32_t deliver_blocks;   // blocks of the delivery grid (a batch shares 4x this out)
     int32_t growth_threads;   // threads per block of the overlap pass: 128, 256 or 512
     int32_t sweep_dests;      // dests per TMA sweep tile of a single network: 16 or 32
+    int32_t deliver_early;    // 1: spiking/DS delivery prepares its arrivals during the previous
+                              // sweep, 0: it starts after it
 };
-constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32};
+constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1};
 
 // plane position of slot (dest d, row k) and its inverse (Mq row quads per dest)
 __host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Mq)
@@ -94,6 +96,10 @@ struct NetDev {
     // step counter and the last-CTA barrier of the sweep
     unsigned long long *step;
     uint32_t *sweep_done;
+    // the delivery pass's own copy of the step counter and its last-block barrier: a delivery
+    // prepares its arrivals while the previous sweep, which advances `step`, is still running
+    unsigned long long *dstep;
+    uint32_t *dlv_done;
     uint32_t *err;
     // neurons
     float *Vm, *Vthresh, *Vreset, *I0, *Inoise, *C1, *C2, *Trefract, *sp;
@@ -173,6 +179,7 @@ enum : uint32_t {
     ERR_STEP_RANGE = 1u << 7,
     ERR_ISI_EXHAUSTED = 1u << 8,
     ERR_STDP_RING = 1u << 9,
+    ERR_STEP_SYNC = 1u << 10,
 };
 
 // ---- exact-rounding helpers -----------------------------------------------------------------

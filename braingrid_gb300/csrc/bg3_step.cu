@@ -325,43 +325,48 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
 // keeps every warp of the grid busy instead of one warp per neuron walking its synapses 32 at a
 // time.  Each synapse has one source, which fires at most once per step, so no two lanes touch
 // one slot.  Block 0 also clears ring slot t + 1 for the next neuron pass.
+//
+// Spiking and DS synapses: the pass starts while the previous sweep is still running (its launch
+// is a programmatic dependent of that sweep).  Everything an arrival needs except psr depends only
+// on spikes at least one step old (written by earlier sweeps), the outgoing map and the synapse's
+// event slot (written only by earlier delivery passes, which have finished: a sweep releases its
+// dependent only after its own wait on the delivery before it).  So the item table, the slot
+// positions, the DS update of u, r and the last-spike step, and the psr increment are done first;
+// pdl_wait() then waits for the sweep, and only the psr read-modify-write comes after it.  The
+// step comes from the pass's own counter (dstep), since the sweep advances `step` at its end.
+// STDP kinds wait first: their pre-spike walks read the post neurons' latest spikes.
 constexpr int DLV_CHUNK = 128;
 constexpr int DLV_GROUP = 32;
 
-template <int SYN>
-__device__ __forceinline__ void deliver_chunk(const NetDev &n, uint32_t b, uint32_t k,
-                                              uint32_t base, uint32_t tf, unsigned long long t64,
-                                              int src, int lane)
-{
-    if (SYN >= 2) {  // STDP: the pre-spike walks go one synapse at a time
-        const uint32_t end = min(k, base + (uint32_t)DLV_CHUNK);
-        for (uint32_t j = base + lane; j < end; j += 32) deliver_hit<SYN>(n, n.outMap[b + j], tf, t64, src);
-        return;
-    }
-    const uint32_t t = (uint32_t)t64;
+struct Arrivals {
     uint32_t p[4];
+    float add[4];
     bool ok[4];
+};
+
+// Event-state part of the arrivals of one chunk (lane's four synapses): slot positions, the
+// isSpikeQueue/changePSR arithmetic of the spiking and DS synapses up to the psr increment
+// (AllSpikingSynapses.cpp:327-334, AllDSSynapses.cpp:227-247), and the event-slot update.
+template <int SYN>
+__device__ __forceinline__ void deliver_prep(const NetDev &n, uint32_t b, uint32_t k, uint32_t base,
+                                             uint32_t tf, uint32_t t, int lane, Arrivals &a)
+{
 #pragma unroll
     for (int u = 0; u < 4; u++) {
         const uint32_t j = base + (uint32_t)lane + 32u * u;
-        ok[u] = j < k;
-        p[u] = ok[u] ? n.outMap[b + j] : 0u;
+        a.ok[u] = j < k;
+        a.p[u] = a.ok[u] ? n.outMap[b + j] : 0u;
     }
     EvSlot e[4];
-    float ps[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-        if (ok[u]) {
-            e[u] = n.ev[p[u]];
-            ps[u] = n.psr[p[u]];
-        }
-    }
+    for (int u = 0; u < 4; u++)
+        if (a.ok[u]) e[u] = n.ev[a.p[u]];
 #pragma unroll
-    for (int u = 0; u < 4; u++) ok[u] = ok[u] && (int32_t)(tf - e[u].born) >= 0;
+    for (int u = 0; u < 4; u++) a.ok[u] = a.ok[u] && (int32_t)(tf - e[u].born) >= 0;
     float xr[4], xu[4], dec[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-        if (!ok[u]) continue;
+        if (!a.ok[u]) continue;
         dec[u] = n.dtab[e[u].dcls];
         if (SYN == 1 && e[u].last != BG3_NO_SPIKE32) {
             const uint32_t ki = t - e[u].last;
@@ -372,8 +377,7 @@ __device__ __forceinline__ void deliver_chunk(const NetDev &n, uint32_t b, uint3
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-        if (!ok[u]) continue;
-        float q = ps[u];
+        if (!a.ok[u]) continue;
         if (SYN == 1) {
             float uu = e[u].u, r = e[u].r;
             if (e[u].last != BG3_NO_SPIKE32) {
@@ -381,27 +385,43 @@ __device__ __forceinline__ void deliver_chunk(const NetDev &n, uint32_t b, uint3
                 r = 1.0f + (r * (1.0f - uu) - 1.0f) * xr[u];
                 uu = U + uu * (1.0f - U) * xu[u];
             }
-            q = q + ((e[u].W / dec[u]) * uu * r);
-            EvSlot *w = &n.ev[p[u]];
+            a.add[u] = (e[u].W / dec[u]) * uu * r;
+            EvSlot *w = &n.ev[a.p[u]];
             w->u = uu;
             w->r = r;
             w->last = t;
         } else {
-            q = q + e[u].W / dec[u];
+            a.add[u] = e[u].W / dec[u];
         }
-        n.psr[p[u]] = q;
     }
 }
 
+// psr part: psr += increment (the four loads issued together).
+__device__ __forceinline__ void deliver_apply(const NetDev &n, const Arrivals &a)
+{
+    float ps[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+        if (a.ok[u]) ps[u] = n.psr[a.p[u]];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+        if (a.ok[u]) n.psr[a.p[u]] = ps[u] + a.add[u];
+}
+
 template <int SYN>
-__device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb)
+__device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb, bool early_cfg)
 {
     __shared__ uint32_t s_pref[DLV_GROUP], s_beg[DLV_GROUP], s_cnt[DLV_GROUP], s_tf[DLV_GROUP];
     __shared__ int32_t s_src[DLV_GROUP];
     __shared__ int s_moff[BG3_MAX_DELAYS + 1];
-    const unsigned long long t = *n.step;
+    const bool early = SYN <= 1 && early_cfg;
+    bool waited = !early;
+    if (!early) {
+        pdl_wait();
+        pdl_trigger();
+    }
+    const unsigned long long t = *n.dstep;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    if (bid == 0 && threadIdx.x == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
     if (threadIdx.x == 0) {
         int off = 0;
         for (int c = 0; c < n.n_delays; c++) {
@@ -451,28 +471,55 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb)
                 else lo = mid + 1;
             }
             const uint32_t first = lo ? s_pref[lo - 1] : 0u;
-            deliver_chunk<SYN>(n, s_beg[lo], s_cnt[lo], (ch - first) * DLV_CHUNK, s_tf[lo], t,
-                               s_src[lo], lane);
+            const uint32_t base = (ch - first) * DLV_CHUNK;
+            if (SYN >= 2) {  // STDP: the pre-spike walks go one synapse at a time
+                const uint32_t end = min(s_cnt[lo], base + (uint32_t)DLV_CHUNK);
+                for (uint32_t j = base + lane; j < end; j += 32)
+                    deliver_hit<SYN>(n, n.outMap[s_beg[lo] + j], s_tf[lo], t, s_src[lo]);
+            } else {
+                Arrivals a;
+                deliver_prep<SYN>(n, s_beg[lo], s_cnt[lo], base, s_tf[lo], (uint32_t)t, lane, a);
+                if (!waited) {
+                    pdl_wait();  // the previous sweep has finished with psr
+                    pdl_trigger();
+                    waited = true;
+                }
+                deliver_apply(n, a);
+            }
         }
         __syncthreads();
+    }
+    if (!waited) {
+        pdl_wait();
+        pdl_trigger();
+    }
+    if (threadIdx.x == 0) {
+        if (bid == 0) {
+            if (*n.step != t) set_err(n, ERR_STEP_SYNC);  // internal check
+            n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
+        }
+        // the pass's last block advances the delivery step counter
+        __threadfence();
+        const unsigned prev = atomicAdd(n.dlv_done, 1u);
+        if (prev == (unsigned)nb - 1) {
+            *n.dlv_done = 0;
+            *n.dstep = t + 1;
+            __threadfence();
+        }
     }
 }
 
 template <int SYN>
-__global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev n)
+__global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev n, int early)
 {
-    pdl_wait();  // the previous sweep (step counter, spike ring, psr) must be complete
-    pdl_trigger();
-    deliver_net<SYN>(n, blockIdx.x, gridDim.x);
+    deliver_net<SYN>(n, blockIdx.x, gridDim.x, early != 0);
 }
 
 // Batched form: grid.y indexes the network, so the networks' delivery passes run side by side.
 template <int SYN>
-__global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets)
+__global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets, int early)
 {
-    pdl_wait();
-    pdl_trigger();
-    deliver_net<SYN>(nets[blockIdx.y], blockIdx.x, gridDim.x);
+    deliver_net<SYN>(nets[blockIdx.y], blockIdx.x, gridDim.x, early != 0);
 }
 
 // The fPost branch (AllSTDPSynapses.cpp:368-418) for every in-use synapse onto a neuron that
@@ -871,12 +918,12 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, int block, size_t smem
 // Spike arrivals of the step, then (STDP kinds) the post-spike learning pass.
 void launch_deliver(const NetDev &h, const LaunchCfg &c, cudaStream_t s)
 {
-    const int g = c.deliver_blocks;
+    const int g = c.deliver_blocks, e = c.deliver_early;
     switch (h.syn_kind) {
-    case 1: launch_pdl(k_deliver<1>, g, 256, 0, s, h); break;
-    case 2: launch_pdl(k_deliver<2>, g, 256, 0, s, h); break;
-    case 3: launch_pdl(k_deliver<3>, g, 256, 0, s, h); break;
-    default: launch_pdl(k_deliver<0>, g, 256, 0, s, h); break;
+    case 1: launch_pdl(k_deliver<1>, g, 256, 0, s, h, e); break;
+    case 2: launch_pdl(k_deliver<2>, g, 256, 0, s, h, e); break;
+    case 3: launch_pdl(k_deliver<3>, g, 256, 0, s, h, e); break;
+    default: launch_pdl(k_deliver<0>, g, 256, 0, s, h, e); break;
     }
     if (h.syn_kind >= 2) launch_pdl(k_stdp_post, g, 256, 0, s, h);
 }
@@ -939,11 +986,12 @@ void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, const Lau
     // once, so a quiet network costs little)
     const int per_net = std::max(2, std::min(c.deliver_blocks, 4 * c.deliver_blocks / std::max(count, 1)));
     const dim3 grid(per_net, count);
+    const int e = c.deliver_early;
     switch (syn_kind) {
-    case 1: launch_pdl(k_deliver_batch<1>, grid, 256, 0, s, nets); break;
-    case 2: launch_pdl(k_deliver_batch<2>, grid, 256, 0, s, nets); break;
-    case 3: launch_pdl(k_deliver_batch<3>, grid, 256, 0, s, nets); break;
-    default: launch_pdl(k_deliver_batch<0>, grid, 256, 0, s, nets); break;
+    case 1: launch_pdl(k_deliver_batch<1>, grid, 256, 0, s, nets, e); break;
+    case 2: launch_pdl(k_deliver_batch<2>, grid, 256, 0, s, nets, e); break;
+    case 3: launch_pdl(k_deliver_batch<3>, grid, 256, 0, s, nets, e); break;
+    default: launch_pdl(k_deliver_batch<0>, grid, 256, 0, s, nets, e); break;
     }
     if (syn_kind >= 2) launch_pdl(k_stdp_post_batch, grid, 256, 0, s, nets);
 }

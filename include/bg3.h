@@ -48,8 +48,10 @@ enum {
     BG3_ERR_TIMEOUT = 1u << 6,          /* a bounded device wait expired (the kernel drained)       */
     BG3_ERR_STEP_RANGE = 1u << 7,       /* step counter beyond 2^32 - 256 (32-bit spike times)      */
     BG3_ERR_ISI_EXHAUSTED = 1u << 8,    /* injected Poisson ISI draws ran out                        */
-    BG3_ERR_STDP_RING = 1u << 9         /* an STDP walk reached the oldest entry of a full spike ring
+    BG3_ERR_STDP_RING = 1u << 9,        /* an STDP walk reached the oldest entry of a full spike ring
                                            (the reference reads outside the ring there)              */
+    BG3_ERR_STEP_SYNC = 1u << 10        /* internal check: the delivery and sweep step counters
+                                           disagreed (that step's arrivals were not applied)         */
 };
 
 enum { BG3_NEURON_LIF = 0, BG3_NEURON_IZH = 1 };
@@ -321,10 +323,12 @@ int bg3_batch_bench_steps(bg3_batch *batch, int64_t nsteps, int64_t flush_bytes,
 /* Benchmark helper: runs nsteps steps on the handle's stream.  Before each step, when
  * flush_bytes > 0, a scratch buffer of that size is overwritten so that the step starts with a
  * cold L2.  The device time of each step (CUDA events on the handle's stream, flush excluded) is
- * written to step_ms[nsteps]; when kernel_ms is not NULL, each step's phases go to
- * kernel_ms[3 * s .. 3 * s + 2]: 0, spike delivery (plus the neuron pass in injected-noise mode),
- * and the sweep (whose epilogue runs the next step's neuron pass in device-noise mode); that
- * extra event between the two phases is recorded only when kernel_ms is not NULL.  The
+ * written to step_ms[nsteps].  In device-noise mode a timed step is, as bg3_step runs them, the
+ * sweep of step s followed by the spike delivery of step s + 1, which overlaps that sweep (the
+ * first timed step also holds step 0's delivery, the last none: nsteps of each in total).  When
+ * kernel_ms is not NULL the phases run one after the other instead, with an event between them:
+ * kernel_ms[3 * s .. 3 * s + 2] = 0, spike delivery (plus the neuron pass in injected-noise mode),
+ * and the sweep (whose epilogue runs the next step's neuron pass in device-noise mode).  The
  * standalone neuron pass before step 0 is not timed. */
 int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *step_ms,
                     float *kernel_ms);
@@ -347,6 +351,10 @@ typedef struct {
     int32_t sweep_dests;      /* dests per TMA sweep tile of a single network: 16 or 32 (32); more,
                                  smaller tiles spread a network over the SMs more evenly (a batch
                                  always uses 32)                                                    */
+    int32_t deliver_early;    /* 1 (default): the spike delivery of spiking and DS synapses starts
+                                 while the previous sweep runs and prepares its arrivals (slot
+                                 positions, event state), applying only the psr increments after it;
+                                 0: it starts after the sweep.  Same results either way.            */
 } bg3_launch_cfg;
 int bg3_get_launch(bg3_net *net, bg3_launch_cfg *cfg);
 int bg3_set_launch(bg3_net *net, const bg3_launch_cfg *cfg);
