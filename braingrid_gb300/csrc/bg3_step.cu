@@ -10,6 +10,10 @@
 //                     their own summation point), so a step costs two launches.
 //   k_neurons_*  (t)  standalone neuron integration: the first step of a bg3_step call and every
 //                     step in injected-noise mode (the noise order needs a scan over all neurons).
+// In device-noise mode a call runs neurons(t0), k_deliver(t0), then (k_sweep(t), k_deliver(t+1))
+// pairs, each delivery a programmatic dependent that overlaps the sweep before it, and a last
+// unfused sweep.  The step counter: an unfused sweep advances it; after a fused sweep the next
+// delivery does (it keeps its own copy, dstep, for the part it runs before the sweep ends).
 #include <cuda.h>
 #include <algorithm>
 #include <utility>
@@ -495,7 +499,14 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb, bo
     }
     if (threadIdx.x == 0) {
         if (bid == 0) {
-            if (*n.step != t) set_err(n, ERR_STEP_SYNC);  // internal check
+            // the step counter reaches t here: a fused sweep before this pass left it at t - 1
+            const unsigned long long st = *n.step;
+            if (st + 1 == t) {
+                *n.step = t;
+                if (t >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
+            } else if (st != t) {
+                set_err(n, ERR_STEP_SYNC);  // internal check
+            }
             n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
         }
         // the pass's last block advances the delivery step counter
@@ -614,7 +625,8 @@ constexpr size_t sw_smem(int st, int D)
 // prologue overlaps the previous kernel's tail; the step's data is touched after pdl_wait().
 // Every mbarrier wait is bounded (about 1 s); on expiry the error word is set and the CTA drains.
 // Tile epilogue: the sums go to the summation points or, with FUSE, straight into the neuron
-// update of step t + 1 (device noise); the network's last tile advances its step counter.
+// update of step t + 1 (device noise); the step counter advances here only when unfused (a fused
+// sweep's next delivery advances it).
 // x: the dest's neuron values (neuron_load after pdl_wait), noise: its N(0,1) draw for step t+1.
 template <bool FUSE>
 __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid, float acc,
@@ -634,7 +646,10 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
     } else if (valid) {
         n.sp[d] = acc;
     }
-    if (lane == 0) {
+    // A fused sweep is always followed by the next step's delivery, which advances the step
+    // counter after its wait; an unfused one (the last step of a call, injected noise) advances it
+    // here, from the network's last tile.
+    if (!FUSE && lane == 0) {
         __threadfence();
         unsigned prev = atomicAdd(n.sweep_done, 1u);
         if (prev == (unsigned)tiles - 1) {
