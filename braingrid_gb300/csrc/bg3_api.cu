@@ -377,7 +377,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     h.n_spike_bins = (int)((float)D.max_epochs * D.epoch_duration * 100.0f);
     int rc = 0;
 #define A(ptr, cnt) if ((rc = dalloc(n, &h.ptr, (cnt))) != 0) goto fail;
-    A(step, 1) A(sweep_done, 1) A(dstep, 1) A(dlv_done, 1) A(err, 1) A(noise_cursor, 1)
+    A(step, 1) A(sweep_done, 1) A(dstep, 1) A(err, 1) A(noise_cursor, 1)
     A(Vm, N) A(Vthresh, N) A(Vreset, N) A(I0, N) A(Inoise, N) A(C1, N) A(C2, N) A(Trefract, N)
     A(sp, N) A(refr, N) A(spikeCount, N) A(spikeCountOffset, N) A(ntype, N)
     A(ring, N * BG3_RING) A(ring_n, BG3_RING)
@@ -457,8 +457,7 @@ int64_t bg3_net_footprint(const bg3_net_desc *desc)
     const uint64_t nb = (uint64_t)std::max((int)((float)D.max_epochs * D.epoch_duration), 1);
     const uint64_t ns = (uint64_t)std::max((int)((float)D.max_epochs * D.epoch_duration * 100.0f), 1);
     const uint64_t E1 = (uint64_t)D.max_epochs + 1;
-    uint64_t b = 8 + 4 + 8 + 4 + 4 + 8;                   // step, sweep_done, dstep, dlv_done,
-                                                          // err, cursor
+    uint64_t b = 8 + 4 + 8 + 4 + 8;                       // step, sweep_done, dstep, err, cursor
     b += N * (9 * 4 + 3 * 4 + 1);                                  // neuron SoA + ntype
     b += N * BG3_RING * 4 + BG3_RING * 4;                          // spike ring
     b += S * (4 + 1 + 1 + sizeof(EvSlot) + 4 + 1 + 4) + N * 4;     // planes, outMap, count
@@ -1909,7 +1908,7 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
 // the size of its allocation; bg3_checkpoint_save refuses a network holding an allocation that
 // this list does not name, so a new array cannot be left out silently.
 #define BG3_NET_ARRAYS(X)                                                                         \
-    X(step) X(sweep_done) X(dstep) X(dlv_done) X(err) X(noise_cursor) X(Vm) X(Vthresh) X(Vreset) X(I0) X(Inoise)       \
+    X(step) X(sweep_done) X(dstep) X(err) X(noise_cursor) X(Vm) X(Vthresh) X(Vreset) X(I0) X(Inoise)       \
     X(C1) X(C2) X(Trefract) X(sp) X(refr) X(spikeCount) X(spikeCountOffset) X(history) X(ntype)   \
     X(Aconst) X(Bconst) X(Cconst) X(Dconst) X(u_izh) X(C3) X(ring) X(ring_n) X(psr) X(dcls)       \
     X(lcls) X(ev) X(src) X(stype) X(count) X(dtab) X(ltab) X(outBegin) X(outCount) X(outMap)      \
@@ -1933,7 +1932,7 @@ struct CkptHeader {
     uint32_t n_arrays;         // CKPT_ARRAYS
     uint32_t pad;
 };
-static const uint32_t CKPT_VERSION = 2;
+static const uint32_t CKPT_VERSION = 3;
 static const char CKPT_MAGIC[8] = {'B', 'G', '3', 'C', 'K', 'P', 'T', 0};
 
 static size_t alloc_size(const bg3_net *n, const void *p)

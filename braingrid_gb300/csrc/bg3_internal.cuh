@@ -96,10 +96,9 @@ struct NetDev {
     // step counter and the last-CTA barrier of the sweep
     unsigned long long *step;
     uint32_t *sweep_done;
-    // the delivery pass's own copy of the step counter and its last-block barrier: a delivery
-    // prepares its arrivals while the previous sweep, which advances `step`, is still running
+    // the delivery pass's own copy of the step counter: a delivery prepares its arrivals while
+    // the previous sweep, which may advance `step`, is still running
     unsigned long long *dstep;
-    uint32_t *dlv_done;
     uint32_t *err;
     // neurons
     float *Vm, *Vthresh, *Vreset, *I0, *Inoise, *C1, *C2, *Trefract, *sp;

@@ -13,7 +13,8 @@
 // In device-noise mode a call runs neurons(t0), k_deliver(t0), then (k_sweep(t), k_deliver(t+1))
 // pairs, each delivery a programmatic dependent that overlaps the sweep before it, and a last
 // unfused sweep.  The step counter: an unfused sweep advances it; after a fused sweep the next
-// delivery does (it keeps its own copy, dstep, for the part it runs before the sweep ends).
+// delivery does.  The delivery's own copy, dstep, which it reads before the sweep ahead of it
+// ends, is advanced by that sweep's first tile as soon as the sweep's wait is over.
 #include <cuda.h>
 #include <algorithm>
 #include <utility>
@@ -83,13 +84,28 @@ __device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, int x, int 
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// the stores' reads of shared memory are done (the stage may go); their global writes complete
+// by the end of the grid, which is all a later kernel needs
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 // Programmatic dependent launch: wait for the preceding kernel of the stream (and its memory),
 // and allow the next kernel of the stream to be scheduled early.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// The delivery pass of step t + 1 starts (programmatically) during the sweep of step t and reads
+// its step from dstep before that sweep ends.  The sweep's first tile advances dstep once the
+// delivery of step t has finished (after pdl_wait) and before any CTA of the sweep releases the
+// next launch (the fence makes the store visible first; the caller's barrier keeps the other
+// threads of the CTA from triggering before it).
+__device__ __forceinline__ void dstep_advance(const NetDev &n, bool me, unsigned long long t)
+{
+    if (me) {
+        *n.dstep = t + 1;
+        __threadfence();
+    }
+}
 
 // ---- standalone neuron kernels ---------------------------------------------------------------
 // Device-noise mode: one N(0,1) draw per neuron per step, keyed by (seed, step, neuron).
@@ -509,14 +525,6 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb, bo
             }
             n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;
         }
-        // the pass's last block advances the delivery step counter
-        __threadfence();
-        const unsigned prev = atomicAdd(n.dlv_done, 1u);
-        if (prev == (unsigned)nb - 1) {
-            *n.dlv_done = 0;
-            *n.dstep = t + 1;
-            __threadfence();
-        }
     }
 }
 
@@ -695,8 +703,10 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
     }
     __syncthreads();
     pdl_wait();  // spike delivery for this step has finished writing psr
-    pdl_trigger();
     const unsigned long long t = *n.step;
+    dstep_advance(n, tile == 0 && threadIdx.x == 0, t);
+    __syncthreads();
+    pdl_trigger();
 
     if (warp == 0) {  // ---------------------------------------------------------- producer
         if (lane == 0) {
@@ -791,7 +801,7 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         }
         __syncwarp();
     }
-    if (lane == 0) bulk_wait_all();
+    if (lane == 0) bulk_wait_read_all();
     __syncwarp();
     if (done < nch) {
         // error path: wait (bounded) for the loads already issued before the smem goes away
@@ -812,17 +822,15 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
 // order; the same epilogue as sweep_tile.  Lanes past N sit in the last tile's padding, whose
 // slots stay +0.0f.  For these networks a TMA pipeline per 32 dests would spend most of its time
 // in set-up.
+// Before it: the kernel's pdl_wait (spike delivery for this step has finished writing psr), the
+// dstep advance by the network's tile 0 and the block barrier, then pdl_trigger.
 template <bool FUSE>
-__device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile)
+__device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile, const int nq,
+                                                const unsigned long long t)
 {
     const int lane = threadIdx.x & 31;
     const int d = tile * SW_DESTS + lane;
     const bool valid = d < n.N;
-    const int cnt = valid ? (int)n.count[d] : 0;
-    const int nq = (__reduce_max_sync(0xffffffffu, cnt) + 3) >> 2;
-    pdl_wait();  // spike delivery for this step has finished writing psr
-    pdl_trigger();
-    const unsigned long long t = *n.step;
     NeuronIn x;
     float noise = 0.0f;
     if (FUSE && valid) {
@@ -882,12 +890,26 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_batch(const NetDev *nets,
     sweep_tile<FUSE, ST, SW_DESTS>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
 }
 
+// Row-quad count of a thin tile (read before pdl_wait: the counts change only between calls).
+__device__ __forceinline__ int thin_quads(const NetDev &n, int tile)
+{
+    const int d = tile * SW_DESTS + (int)(threadIdx.x & 31);
+    const int cnt = d < n.N ? (int)n.count[d] : 0;
+    return (__reduce_max_sync(0xffffffffu, cnt) + 3) >> 2;
+}
+
 template <bool FUSE>
 __global__ void __launch_bounds__(1024) k_sweep_thin(const __grid_constant__ NetDev n)
 {
     const int tile = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
-    if (tile >= n.ntiles) return;
-    sweep_thin_tile<FUSE>(n, tile);
+    const bool active = tile < n.ntiles;
+    const int nq = active ? thin_quads(n, tile) : 0;
+    pdl_wait();
+    const unsigned long long t = *n.step;
+    dstep_advance(n, tile == 0 && (threadIdx.x & 31) == 0, t);
+    __syncthreads();
+    pdl_trigger();
+    if (active) sweep_thin_tile<FUSE>(n, tile, nq, t);
 }
 
 // Batched thin tiles: tiles[i] = (network, tile), one warp each.
@@ -896,9 +918,16 @@ __global__ void __launch_bounds__(1024) k_sweep_thin_batch(const NetDev *nets, c
                                                            int count)
 {
     const int i = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
-    if (i >= count) return;
-    const int2 tr = tiles[i];
-    sweep_thin_tile<FUSE>(nets[tr.x], tr.y);
+    const bool active = i < count;
+    const int2 tr = active ? tiles[i] : make_int2(0, 0);
+    const NetDev &n = nets[tr.x];
+    const int nq = active ? thin_quads(n, tr.y) : 0;
+    pdl_wait();
+    const unsigned long long t = active ? *n.step : 0ull;
+    dstep_advance(n, active && tr.y == 0 && (threadIdx.x & 31) == 0, t);
+    __syncthreads();
+    pdl_trigger();
+    if (active) sweep_thin_tile<FUSE>(n, tr.y, nq, t);
 }
 
 bool sweep_is_thin(const NetDev &h, const LaunchCfg &c) { return h.Mq <= c.thin_max_quads; }
