@@ -327,6 +327,7 @@ const char *bg3_status_string(int s)
     case BG3_ENOISE: return "injected noise stream exhausted";
     case BG3_EDEVICE: return "device error word set";
     case BG3_EUNSUPPORTED: return "unsupported model combination";
+    case BG3_ECANCELED: return "job cancelled";
     default: return "unknown status";
     }
 }

@@ -1,8 +1,10 @@
-// Self-test of the integer-pipe binary64 arithmetic (SoftD, bg3_internal.cuh) against the
-// hardware: random operands (random signs, mantissas, exponents in [-300, 300]) and operand pairs
-// that nearly cancel, for add, multiply and the conversion to float.
+// Self-tests.  bg3_selftest_binary64: the integer-pipe binary64 arithmetic (SoftD,
+// bg3_internal.cuh) against the hardware on random operands (random signs, mantissas, exponents
+// in [-300, 300]) and operand pairs that nearly cancel, for add, multiply and the conversion to
+// float.  bg3_selftest_timeout: the bounded mbarrier wait of the step kernels, run out on purpose.
 #include "../../include/bg3.h"
 #include "bg3_internal.cuh"
+#include "bg3_ptx.cuh"
 
 namespace {
 
@@ -61,7 +63,44 @@ __global__ void k_softd_test(uint64_t n, uint64_t seed, unsigned long long *bad)
         if (local[k]) atomicAdd(&bad[k], local[k]);
 }
 
+// A wait that nothing ends: an mbarrier expecting one arrival that never comes, waited on by a
+// warp with the step kernels' bounded wait at limit_ns.  No copy targets the barrier, so the
+// block may leave it pending; the kernel records whether the wait gave up and how long it took,
+// and returns.
+__global__ void k_wait_test(unsigned long long limit_ns, unsigned long long *out)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        bg3::mbar_init(&bar, 1);
+        bg3::fence_mbar_init();
+    }
+    __syncthreads();
+    const unsigned long long t0 = bg3::global_ns();
+    const bool done = bg3::mbar_wait(&bar, 0u, limit_ns);
+    const unsigned long long t1 = bg3::global_ns();
+    if (threadIdx.x == 0) {
+        out[0] = done ? 0ull : (unsigned long long)BG3_ERR_TIMEOUT;
+        out[1] = t1 - t0;
+    }
+}
+
 }  // namespace
+
+extern "C" int bg3_selftest_timeout(uint64_t limit_ns, uint32_t *status, uint64_t *waited_ns)
+{
+    if (!status || !waited_ns || limit_ns == 0 || limit_ns > 2000000000ull) return BG3_EINVAL;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return BG3_ENOMEM;
+    k_wait_test<<<1, 32>>>((unsigned long long)limit_ns, d);
+    unsigned long long h[2] = {0, 0};
+    const cudaError_t e1 = cudaDeviceSynchronize();
+    const cudaError_t e2 = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) return BG3_ECUDA;
+    *status = (uint32_t)h[0];
+    *waited_ns = h[1];
+    return BG3_OK;
+}
 
 extern "C" int bg3_selftest_binary64(uint64_t samples, uint64_t seed, uint64_t *counts)
 {

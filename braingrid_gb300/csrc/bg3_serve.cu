@@ -87,6 +87,7 @@ static void finish(bg3_server *s, Job *j, int status)
     }
     j->net = nullptr;
     if (status == BG3_OK) s->st.done++;
+    else if (status == BG3_ECANCELED) s->st.cancelled++;
     else s->st.failed++;
     s->finished.push_back(j->id);
     delete j;
@@ -292,6 +293,29 @@ int bg3_serve_pump(bg3_server *s)
     s->joining.clear();
     s->st.peak_resident = std::max<int64_t>(s->st.peak_resident, (int64_t)s->resident.size());
     return BG3_OK;
+}
+
+int bg3_serve_cancel(bg3_server *s, int64_t job_id)
+{
+    if (!s) return BG3_EINVAL;
+    // between pump calls no chunk is in flight: the job can go at once
+    for (size_t i = 0; i < s->queue.size(); i++)
+        if (s->queue[i]->id == job_id) {
+            Job *j = s->queue[i];
+            s->queue.erase(s->queue.begin() + i);
+            finish(s, j, BG3_ECANCELED);
+            return BG3_OK;
+        }
+    for (std::vector<Job *> *v : {&s->resident, &s->joining})
+        for (size_t i = 0; i < v->size(); i++)
+            if ((*v)[i]->id == job_id) {
+                Job *j = (*v)[i];
+                v->erase(v->begin() + i);
+                if (v == &s->resident) s->dirty[j->d.desc.synapse_kind] = true;
+                finish(s, j, BG3_ECANCELED);
+                return BG3_OK;
+            }
+    return BG3_EINVAL;
 }
 
 int bg3_serve_take(bg3_server *s, int64_t *ids, int32_t cap, int32_t *n)

@@ -22,7 +22,8 @@ BG3_SYN_SPIKING, BG3_SYN_DS, BG3_SYN_STDP, BG3_SYN_DYNSTDP = 0, 1, 2, 3
 BG3_NOISE_DEVICE, BG3_NOISE_INJECT = 0, 1
 BG3_STDP_HOST, BG3_STDP_DEVICE = 0, 1
 (BG3_OK, BG3_EINVAL, BG3_ENOMEM, BG3_ECUDA, BG3_ENOISE, BG3_EDEVICE,
- BG3_EUNSUPPORTED) = 0, -1, -2, -3, -4, -5, -6
+ BG3_EUNSUPPORTED, BG3_ECANCELED) = 0, -1, -2, -3, -4, -5, -6, -7
+BG3_ERR_TIMEOUT = 1 << 6
 ERR_BITS = {1: "history overflow", 2: "double spike in a queue slot", 4: "synapse row full",
             8: "injected noise exhausted", 16: "negative growth weight"}
 

@@ -39,7 +39,8 @@ class JobDesc(ctypes.Structure):
 
 class ServeStats(ctypes.Structure):
     _fields_ = [("queued", ctypes.c_int64), ("resident", ctypes.c_int64), ("done", ctypes.c_int64),
-                ("failed", ctypes.c_int64), ("bytes_resident", ctypes.c_uint64),
+                ("failed", ctypes.c_int64), ("cancelled", ctypes.c_int64),
+                ("bytes_resident", ctypes.c_uint64),
                 ("rounds", ctypes.c_int64), ("synapse_steps", ctypes.c_int64),
                 ("neuron_steps", ctypes.c_int64), ("peak_resident", ctypes.c_int64),
                 ("admit_s", ctypes.c_double), ("wait_s", ctypes.c_double),
@@ -61,6 +62,7 @@ def _bind():
         "bg3_serve_submit": ([vp, ctypes.POINTER(JobDesc), ctypes.POINTER(ctypes.c_int64)],
                              ctypes.c_int),
         "bg3_serve_pump": ([vp], ctypes.c_int),
+        "bg3_serve_cancel": ([vp, ctypes.c_int64], ctypes.c_int),
         "bg3_serve_take": ([vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32,
                             ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
         "bg3_serve_stats_get": ([vp, ctypes.POINTER(ServeStats)], ctypes.c_int),
@@ -162,6 +164,11 @@ class Server:
 
     def pump(self):
         bg.check(self.L.bg3_serve_pump(self.h), "bg3_serve_pump")
+
+    def cancel(self, job):
+        """Cancels a queued or resident job (bg3_serve_cancel); take() then returns it with
+        status BG3_ECANCELED."""
+        bg.check(self.L.bg3_serve_cancel(self.h, int(job.id)), "bg3_serve_cancel")
 
     def take(self):
         ids = (ctypes.c_int64 * 256)()

@@ -34,7 +34,8 @@ enum {
     BG3_ECUDA = -3,       /* a CUDA call failed                                           */
     BG3_ENOISE = -4,      /* injected noise stream ran out                                */
     BG3_EDEVICE = -5,     /* the device error word is set (see bg3_error_word)            */
-    BG3_EUNSUPPORTED = -6 /* model combination not built                                  */
+    BG3_EUNSUPPORTED = -6, /* model combination not built                                 */
+    BG3_ECANCELED = -7     /* a served job was cancelled (bg3_serve_cancel)                */
 };
 
 /* device error word bits */
@@ -338,6 +339,12 @@ int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *st
  * add mismatches, multiply mismatches, conversion mismatches, cases outside the restated range
  * (which the update recomputes in hardware).  No counterpart in the reference. */
 int bg3_selftest_binary64(uint64_t samples, uint64_t seed, uint64_t *counts);
+/* Failure-detection self-test: one warp waits, with the bounded mbarrier wait the step kernels
+ * use, on a barrier that nothing completes, for at most limit_ns (1 .. 2e9).  The wait gives up,
+ * the kernel returns normally and the context stays usable: *status = BG3_ERR_TIMEOUT, and
+ * *waited_ns the time it waited.  (In the step kernels the same expiry sets BG3_ERR_TIMEOUT in the
+ * network's error word after about 1 s, and the CTA drains its copies in flight.) */
+int bg3_selftest_timeout(uint64_t limit_ns, uint32_t *status, uint64_t *waited_ns);
 
 /* ---- launch configuration and autotuning (no counterpart in the reference) ----------------- */
 typedef struct {

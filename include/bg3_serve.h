@@ -87,7 +87,7 @@ typedef struct {
 } bg3_job_desc;
 
 typedef struct {
-    int64_t queued, resident, done, failed;
+    int64_t queued, resident, done, failed, cancelled;
     uint64_t bytes_resident;     /* sum of the resident jobs' footprints                       */
     int64_t rounds;              /* pump rounds that advanced at least one job                 */
     int64_t synapse_steps, neuron_steps;
@@ -105,6 +105,11 @@ int bg3_serve_destroy(bg3_server *srv);
 int bg3_serve_submit(bg3_server *srv, const bg3_job_desc *job, int64_t *job_id);
 /* One scheduling round (above).  Returns after the round's chunk has finished on the GPU. */
 int bg3_serve_pump(bg3_server *srv);
+/* Cancels a job between rounds: a queued job leaves the queue, a resident one frees its device
+ * memory at once (its group's batch is rebuilt in the next round); the other jobs go on as if it
+ * had never been there.  Its result gets status BG3_ECANCELED (histories not filled) and
+ * bg3_serve_take reports it.  BG3_EINVAL for an id that is not queued or resident. */
+int bg3_serve_cancel(bg3_server *srv, int64_t job_id);
 /* Ids of jobs finished since the last call (results filled), up to cap; *n gets the count. */
 int bg3_serve_take(bg3_server *srv, int64_t *job_ids, int32_t cap, int32_t *n);
 int bg3_serve_stats_get(bg3_server *srv, bg3_serve_stats *stats);

@@ -4,6 +4,8 @@ Each job's arithmetic is independent of the others (its own noise seed, its own 
 and the batched kernels are bit-exact with the single-network ones, so a job's recorder
 histories and final state are identical whether it runs alone, in a mix that joins and leaves
 around it, or through the plain single-network API."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -187,3 +189,52 @@ def test_sharded_trace_serves_every_job_once_with_unchanged_results():
             check_same(alone[i], j.outputs(), "rank %d %s" % (rank, j.name))
             seen.append(i)
     assert sorted(seen) == list(range(len(trace)))
+
+
+def test_cancelled_jobs_leave_the_others_unchanged():
+    """A resident and a queued job cancelled between rounds: both come back with BG3_ECANCELED,
+    their memory is freed, and the remaining jobs end exactly as they do alone."""
+    alone = [run_alone(j) for j in make_jobs()]
+    jobs = make_jobs()
+    srv = serve.Server(max_resident=2, chunk_steps=300)
+    for j in jobs:
+        srv.submit(j)
+    srv.pump()
+    srv.pump()
+    st = srv.stats()
+    assert st["resident"] == 2 and st["queued"] == 3 and st["rounds"] == 1
+    before = st["bytes_resident"]
+    srv.cancel(jobs[1])  # resident, one chunk in
+    srv.cancel(jobs[3])  # still queued
+    assert srv.stats()["bytes_resident"] == before - bg.footprint(jobs[1].desc)
+    with pytest.raises(bg.Bg3Error):
+        srv.cancel(jobs[3])  # already gone
+    done = srv.run_all()
+    st = srv.stats()
+    srv.close()
+    assert len(done) == len(jobs) and st["cancelled"] == 2 and st["failed"] == 0
+    for k, (j, a) in enumerate(zip(jobs, alone)):
+        if k in (1, 3):
+            assert j.result.status == bg.BG3_ECANCELED
+        else:
+            assert j.result.status == 0, (j.name, j.error)
+            check_same(a, j.outputs(), j.name)
+
+
+def test_bounded_device_wait_expires_with_a_status_and_the_context_survives():
+    """The step kernels' bounded mbarrier wait, run on a barrier that nothing completes: it gives
+    up after its limit, the kernel returns BG3_ERR_TIMEOUT, and the GPU keeps working."""
+    L = bg.load()
+    L.bg3_selftest_timeout.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32),
+                                       ctypes.POINTER(ctypes.c_uint64)]
+    for limit in (1_000_000, 50_000_000):
+        status, waited = ctypes.c_uint32(), ctypes.c_uint64()
+        assert L.bg3_selftest_timeout(limit, ctypes.byref(status), ctypes.byref(waited)) == 0
+        assert status.value == bg.BG3_ERR_TIMEOUT
+        assert limit <= waited.value < limit + 200_000_000
+    status, waited = ctypes.c_uint32(), ctypes.c_uint64()
+    assert L.bg3_selftest_timeout(0, ctypes.byref(status), ctypes.byref(waited)) == bg.BG3_EINVAL
+    # the context is usable: a job runs as usual afterwards
+    job = make_jobs()[0]
+    out = run_alone(job)
+    assert job.result.error_word == 0 and np.isfinite(out["Vm"]).all()

@@ -102,3 +102,37 @@ def test_two_rank_gloo_sharding_and_reporting():
     every = sorted(x for part in r0[5] for x in part)
     assert every == sorted((a, j.name, int(j.desc.noise_seed)) for a, j in trace)
     assert all(len(part) > 0 for part in r0[5])
+
+
+def _rank_dies(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import datetime
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=world,
+                            timeout=datetime.timedelta(seconds=20))
+    if rank == 1:
+        os._exit(3)  # a rank lost before the end-of-run reporting
+    try:
+        shard.gather(["rank 0 results"])
+        q.put("no error")
+    except Exception as e:  # the loss surfaces as an error, not a hang
+        q.put("error: " + type(e).__name__)
+
+
+def test_a_lost_rank_is_reported_at_the_gather_not_hung():
+    world = 2
+    ctx = multiprocessing.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_dies, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    try:
+        msg = q.get(timeout=120)
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.kill()
+    assert msg.startswith("error"), msg
+    assert procs[1].exitcode == 3
