@@ -43,11 +43,11 @@ RADIUS, WEIGHT_SCALE, SEED = C1["radius"], C1["weight_scale"], C1["seed"]
 FLUSH_BYTES = 256 << 20
 METRIC = "synapse-updates/s"
 # Algorithmic bytes of the dominant kernel (k_sweep, with the next step's neuron pass fused in):
-# every in-use synapse's psr is read and written and its decay class (1 byte) read; every neuron
+# every in-use synapse's psr is read and written and its decay class (4 bits) read; every neuron
 # reads Vm, Vthresh, I0, Inoise, C1, C2, Trefract, refr and writes Vm, refr, sp (44 B, rounded
 # to 48 with the spike-ring entry).  The reference layout's per-synapse figure (psr, decay, queue
 # word, delay index read; psr, queue, delay index written: 28 B) is reported beside it.
-SWEEP_BYTES_PER_SYN = 9
+SWEEP_BYTES_PER_SYN = 8.5
 SWEEP_BYTES_PER_NEURON = 48
 SURVEY_BYTES_PER_SYN = 28
 # served form: resident work cap, about one and a half of the largest jobs' synapse slots

@@ -294,19 +294,19 @@ static int make_tensor_maps(bg3_net *n)
     auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
     const NetDev &h = n->h;
     // tile-major planes as 3-D tensors [tiles][Mq quads][32 dests x 4 rows] (psr, floats) and
-    // [tiles][Mq quads][32 dests] (classes, 32-bit words of four bytes); a box is 16 quads of one
-    // tile (32 or 16 dests); quads past Mq read as zero and are not written
+    // [tiles][Mq quads][32 dests] (classes, 16-bit words of four 4-bit codes); a box is 16 quads
+    // of one tile (32 or 16 dests); quads past Mq read as zero and are not written
     const cuuint64_t T = (cuuint64_t)h.ntiles, Q = (cuuint64_t)std::max(h.Mq, 1);
     cuuint64_t dims_f[3] = {128, Q, T}, dims_b[3] = {32, Q, T};
-    cuuint64_t st_f[2] = {512, Q * 512}, st_b[2] = {128, Q * 128};
+    cuuint64_t st_f[2] = {512, Q * 512}, st_b[2] = {64, Q * 64};
     cuuint32_t box_f[3] = {128, 16, 1}, box_b[3] = {32, 16, 1};
     cuuint32_t box_f16[3] = {64, 16, 1}, box_b16[3] = {16, 16, 1};
     cuuint32_t es[3] = {1, 1, 1};
     struct { CUtensorMap *m; CUtensorMapDataType ty; void *base; cuuint64_t *dims, *st; cuuint32_t *box; } maps[4] = {
         {&n->tm_psr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, h.psr, dims_f, st_f, box_f},
-        {&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT32, h.dcls, dims_b, st_b, box_b},
+        {&n->tm_cls, CU_TENSOR_MAP_DATA_TYPE_UINT16, h.dcls, dims_b, st_b, box_b},
         {&n->tm_psr16, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, h.psr, dims_f, st_f, box_f16},
-        {&n->tm_cls16, CU_TENSOR_MAP_DATA_TYPE_UINT32, h.dcls, dims_b, st_b, box_b16}};
+        {&n->tm_cls16, CU_TENSOR_MAP_DATA_TYPE_UINT16, h.dcls, dims_b, st_b, box_b16}};
     for (auto &m : maps)
         if (encode(m.m, m.ty, 3, m.base, m.dims, m.st, m.box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -382,7 +382,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     A(Vm, N) A(Vthresh, N) A(Vreset, N) A(I0, N) A(Inoise, N) A(C1, N) A(C2, N) A(Trefract, N)
     A(sp, N) A(refr, N) A(spikeCount, N) A(spikeCountOffset, N) A(ntype, N)
     A(ring, N * BG3_RING) A(ring_n, BG3_RING)
-    A(psr, S) A(dcls, S) A(lcls, S) A(ev, S) A(src, S) A(stype, S) A(count, N)
+    A(psr, S) A(dcls, S / 8) A(lcls, S) A(ev, S) A(src, S) A(stype, S) A(count, N)
     A(dtab, BG3_MAX_DCLS) A(ltab, BG3_MAX_DELAYS)
     A(outBegin, N * BG3_MAX_DELAYS) A(outCount, N * BG3_MAX_DELAYS) A(outFill, N * BG3_MAX_DELAYS)
     A(outMap, S)
@@ -461,7 +461,7 @@ int64_t bg3_net_footprint(const bg3_net_desc *desc)
     uint64_t b = 8 + 4 + 8 + 4 + 8;                       // step, sweep_done, dstep, err, cursor
     b += N * (9 * 4 + 3 * 4 + 1);                                  // neuron SoA + ntype
     b += N * BG3_RING * 4 + BG3_RING * 4;                          // spike ring
-    b += S * (4 + 1 + 1 + sizeof(EvSlot) + 4 + 1 + 4) + N * 4;     // planes, outMap, count
+    b += S * (4 + 1 + sizeof(EvSlot) + 4 + 1 + 4) + S / 2 + N * 4; // planes, outMap, count
     b += BG3_MAX_DCLS * 4 + BG3_MAX_DELAYS * 4 + 3 * N * BG3_MAX_DELAYS * 4;
     b += 4 * N * 4 + ((uint64_t)ms + 1) * 4;                       // growth arrays, grow_exp
     b += (nb + ns) * 4 + 2 * E1 * N * 4;                           // recorder
@@ -593,7 +593,8 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
     const bool ds = n->h.syn_kind == BG3_SYN_DS || n->h.syn_kind == BG3_SYN_DYNSTDP;
     if (ds && (!a->U || !a->D || !a->F || !a->u || !a->r || !a->lastSpike)) return BG3_EINVAL;
     std::vector<float> psr(S, 0.f);
-    std::vector<uint8_t> dc(S, 0), lc(S, 0);
+    std::vector<uint32_t> dc(S / 8, 0u);
+    std::vector<uint8_t> lc(S, 0);
     std::vector<EvSlot> ev(S);
     std::vector<int32_t> src(S, 0);
     std::vector<int8_t> st(S, 0);
@@ -617,9 +618,10 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
                 D < 1 || D > 31 || di < 0 || di > 31)
                 return BG3_EINVAL;
             int dcl = decay_class(n, a->decay[i]), lcl = delay_class(n, D);
-            if (dcl < 0 || lcl < 0) return BG3_EINVAL;
+            if (dcl < 0) return BG3_EUNSUPPORTED;  // more than BG3_MAX_DCLS decay factors
+            if (lcl < 0) return BG3_EINVAL;
             psr[p] = a->psr[i];
-            dc[p] = (uint8_t)dcl;
+            cls_put(dc.data(), p, (uint32_t)dcl);
             lc[p] = (uint8_t)lcl;
             src[p] = a->src[i];
             st[p] = (int8_t)a->type[i];
@@ -678,7 +680,7 @@ int bg3_upload_synapses(bg3_net *n, const bg3_synapse_arrays *a, uint64_t step)
     NetDev &h = n->h;
     int rc;
     if ((rc = push_tables(n))) return rc;
-    if ((rc = h2d(n, h.psr, psr.data(), S)) || (rc = h2d(n, h.dcls, dc.data(), S)) ||
+    if ((rc = h2d(n, h.psr, psr.data(), S)) || (rc = h2d(n, h.dcls, dc.data(), S / 8)) ||
         (rc = h2d(n, h.lcls, lc.data(), S)) || (rc = h2d(n, h.ev, ev.data(), S)) ||
         (rc = h2d(n, h.src, src.data(), S)) || (rc = h2d(n, h.stype, st.data(), S)) ||
         (rc = h2d(n, h.count, count.data(), N)) || (rc = h2d(n, h.ring, ring.data(), ring.size())) ||
@@ -1061,7 +1063,8 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
     const size_t N = n->h.N, Np = n->h.Np, M = n->h.max_syn, S = Np * (size_t)n->h.Mq * 4;
     NetDev &h = n->h;
     std::vector<float> psr(S);
-    std::vector<uint8_t> dc(S), lc(S);
+    std::vector<uint32_t> dc(S / 8);
+    std::vector<uint8_t> lc(S);
     std::vector<EvSlot> ev(S);
     std::vector<int32_t> src(S), ring(N * BG3_RING), ring_n(BG3_RING);
     std::vector<int8_t> st(S);
@@ -1069,7 +1072,7 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
     unsigned long long step = 0;
     const bool ds = h.syn_kind == BG3_SYN_DS || h.syn_kind == BG3_SYN_DYNSTDP;
     int rc;
-    if ((rc = d2h(n, psr.data(), h.psr, S)) || (rc = d2h(n, dc.data(), h.dcls, S)) ||
+    if ((rc = d2h(n, psr.data(), h.psr, S)) || (rc = d2h(n, dc.data(), h.dcls, S / 8)) ||
         (rc = d2h(n, lc.data(), h.lcls, S)) || (rc = d2h(n, ev.data(), h.ev, S)) ||
         (rc = d2h(n, src.data(), h.src, S)) || (rc = d2h(n, st.data(), h.stype, S)) ||
         (rc = d2h(n, count.data(), h.count, N)) || (rc = d2h(n, &step, h.step, 1)) ||
@@ -1105,7 +1108,7 @@ int bg3_download_synapses(bg3_net *n, bg3_synapse_arrays *a)
             if (a->type) a->type[i] = st[p];
             if (a->W) a->W[i] = e.W;
             if (a->psr) a->psr[i] = psr[p];
-            if (a->decay) a->decay[i] = n->dtab[dc[p]];
+            if (a->decay) a->decay[i] = n->dtab[cls_get(dc.data(), p)];
             if (a->total_delay) a->total_delay[i] = D;
             if (a->delayIdx) a->delayIdx[i] = (int32_t)di;
             if (a->delayQueue) a->delayQueue[i] = q;

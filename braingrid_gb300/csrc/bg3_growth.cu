@@ -132,7 +132,9 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
                 n.src[p] = s;
                 n.stype[p] = (int8_t)type;
                 n.psr[p] = 0.0f;
-                n.dcls[p] = (uint8_t)n.t_dcls[type];
+                // new slots hold class 0: set the slot's nibble (slots of other dests or rows
+                // may share the word)
+                atomicOr(&n.dcls[p >> 3], ((uint32_t)n.t_dcls[type] & 15u) << (4u * (uint32_t)(p & 7)));
                 n.lcls[p] = (uint8_t)n.t_lcls[type];
                 EvSlot e;
                 e.W = a * syn_sign(type) * 1.0e-8f;

@@ -32,7 +32,7 @@
 #define BG3_ULONG_MAX 0xffffffffffffffffull
 #define BG3_NO_SPIKE32 0xffffffffu
 #define BG3_RING 64          // spike-list ring depth (steps); delays must be < 32
-#define BG3_MAX_DCLS 256     // decay classes
+#define BG3_MAX_DCLS 16      // decay classes (4-bit codes in the class plane)
 #define BG3_MAX_DELAYS 8     // delay classes
 #define BG3_MAX_EXPC 16      // time constants with an exp table
 #define BG3_EXP_LEN 262144   // steps covered by an exp table (26 s at dt = 0.1 ms)
@@ -78,6 +78,16 @@ __host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Mq)
     const size_t t = (size_t)(d >> 5) * (size_t)Mq + (size_t)(k >> 2);  // tile row quad
     return (((t << 5) | (size_t)(d & 31)) << 2) | (size_t)(k & 3);
 }
+// The class plane holds a 4-bit decay class per slot position p: nibble p & 7 of word p >> 3,
+// so one 16-bit half-word carries the four rows of one dest's row quad.
+__host__ __device__ __forceinline__ uint32_t cls_get(const uint32_t *plane, size_t p)
+{
+    return (plane[p >> 3] >> (4u * (uint32_t)(p & 7))) & 15u;
+}
+__host__ __device__ __forceinline__ void cls_put(uint32_t *plane, size_t p, uint32_t c)
+{
+    plane[p >> 3] |= (c & 15u) << (4u * (uint32_t)(p & 7));  // the nibble must be 0 before
+}
 __host__ __device__ __forceinline__ void pos_slot(size_t p, int Mq, int &k, int &d)
 {
     const size_t q = p >> 2;
@@ -111,7 +121,7 @@ struct NetDev {
     int32_t *ring, *ring_n;
     // synapse planes (index slot_pos(k, d, Mq), Np * Mq * 4 entries)
     float *psr;
-    uint8_t *dcls;                 // decay class
+    uint32_t *dcls;                // decay class, 4 bits per slot: nibble p (cls_get / cls_or)
     uint8_t *lcls;                 // delay class
     EvSlot *ev;
     int32_t *src;

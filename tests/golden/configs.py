@@ -122,6 +122,14 @@ CASES = [
     # LIF neurons with plain spiking synapses (AllSpikingSynapses), pre-grown
     _case("c0_spiking", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000, keep_steps_every=100,
           synapse=0),
+    # ragged shapes: 63 neurons (a full 32-dest tile and one of 31), 30 slots per row (the last
+    # row quad half used), pre-grown DS network
+    _case("ragged", 7, 9, 0.25, 4, 30, radii=1.2, max_firing_rate=1000, site_seed=6,
+          keep_steps_every=100),
+    # 65 neurons (the last tile holds one), 18 slots per row, Izhikevich + dynamic STDP + Poisson
+    _case("ragged_izh", 5, 13, 0.5, 2, 18, radii=1.1, max_firing_rate=1000, site_seed=7,
+          keep_steps_every=50, neuron="izh", synapse=3, stdp=STDP_SOFT,
+          stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=None)),
 ]
 
 

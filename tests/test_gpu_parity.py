@@ -210,3 +210,11 @@ def test_device_noise_mode_runs_and_is_deterministic():
     assert_same("Vm", outs[0][0], outs[1][0])
     assert_same("spikes", outs[0][1], outs[1][1])
     assert outs[0][2] == outs[1][2] > 0
+
+
+@pytest.mark.parametrize("name", ["ragged", "ragged_izh"])
+def test_ragged_shapes_bit_exact(name):
+    """Neuron counts that leave a partial 32-dest tile (63, 65 neurons) and rows that end inside a
+    row quad (30, 18 slots), DS and Izhikevich + dynamic STDP + Poisson."""
+    o, net = run_locked(name, check_every=5, syn_every=50)
+    assert o.total > 0

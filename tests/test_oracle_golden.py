@@ -92,7 +92,7 @@ def test_norm_stream_matches_reference_tiny():
 
 @pytest.mark.parametrize("name", ["ref_tiny", "c0", "c0_grown", "c0_regular", "c0_poisson",
                                   "c0_poisson25", "izh_grown", "c0_spiking", "c0_stdp",
-                                  "c0_dstdp", "izh_dstdp", "izh_static"])
+                                  "c0_dstdp", "izh_dstdp", "izh_static", "ragged", "ragged_izh"])
 def test_oracle_matches_reference_dump(name):
     o = replay_against_fixture(name)
     if name == "c0_grown":
