@@ -1354,6 +1354,7 @@ static int batch_refresh(bg3_batch *b)
     for (size_t k = 0; k < b->nets.size(); k++) {
         bg3_net *n = b->nets[k];
         hd.push_back(n->h);
+        hd.back().izh_hw_every = b->cfg.izh_hw_every;
         maps.push_back(n->tm_psr);
         maps.push_back(n->tm_cls);
         std::vector<uint32_t> count(n->h.N);
@@ -1659,12 +1660,13 @@ static bool cfg_valid(const bg3_launch_cfg *c)
            c->thin_warps <= 32 && c->deliver_blocks >= 1 && c->deliver_blocks <= 65535 &&
            (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512) &&
            (c->sweep_dests == 16 || c->sweep_dests == 32) &&
-           (c->deliver_early == 0 || c->deliver_early == 1);
+           (c->deliver_early == 0 || c->deliver_early == 1) && c->izh_hw_every >= 0 &&
+           c->izh_hw_every <= 8;
 }
 static LaunchCfg cfg_from(const bg3_launch_cfg &c)
 {
     return LaunchCfg{c.sweep_stages, c.thin_max_quads, c.thin_warps, c.deliver_blocks,
-                     c.growth_threads, c.sweep_dests, c.deliver_early};
+                     c.growth_threads, c.sweep_dests, c.deliver_early, c.izh_hw_every};
 }
 static bg3_launch_cfg cfg_to(const LaunchCfg &c)
 {
@@ -1676,6 +1678,7 @@ static bg3_launch_cfg cfg_to(const LaunchCfg &c)
     o.growth_threads = c.growth_threads;
     o.sweep_dests = c.sweep_dests;
     o.deliver_early = c.deliver_early;
+    o.izh_hw_every = c.izh_hw_every;
     return o;
 }
 
@@ -1691,6 +1694,7 @@ int bg3_set_launch(bg3_net *n, const bg3_launch_cfg *c)
     if (!n || !cfg_valid(c)) return BG3_EINVAL;
     CK(cudaStreamSynchronize(n->stream));
     n->cfg = cfg_from(*c);
+    n->h.izh_hw_every = n->cfg.izh_hw_every;
     drop_graph(n);
     return BG3_OK;
 }
@@ -1759,7 +1763,8 @@ static void state_free(StateCopy &sc)
 
 // Coordinate search over the launch parameters; trial(cfg) returns a time (ms) or < 0 on error.
 template <typename Trial>
-static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool batch, Trial trial, float &best_ms)
+static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool batch, bool izh, Trial trial,
+                float &best_ms)
 {
     float t = trial(cur);
     if (t < 0) return (int)t;
@@ -1784,6 +1789,7 @@ static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool batch, Trial
     if ((thin || mq <= 64) && (rc = try_param(&LaunchCfg::thin_warps, {4, 8, 16}))) return rc;
     if ((rc = try_param(&LaunchCfg::deliver_blocks, {152, 304, 608}))) return rc;
     if ((rc = try_param(&LaunchCfg::deliver_early, {0, 1}))) return rc;
+    if (izh && (rc = try_param(&LaunchCfg::izh_hw_every, {0, 1, 2, 3, 4}))) return rc;
     return BG3_OK;
 }
 
@@ -1815,11 +1821,13 @@ int bg3_autotune(bg3_net *n, int32_t steps, int32_t tune_growth, bg3_launch_cfg 
     auto trial = [&](const LaunchCfg &c) -> float {
         if (state_load(n, sc) != BG3_OK) return -1.0f;
         n->cfg = c;
+        n->h.izh_hw_every = c.izh_hw_every;
         drop_graph(n);
         return time_steps(n, steps);
     };
     float ms = 0.0f;
-    rc = tune(cur, !bg3::sweep_is_thin(h, cur), bg3::sweep_is_thin(h, cur), h.Mq, false, trial, ms);
+    rc = tune(cur, !bg3::sweep_is_thin(h, cur), bg3::sweep_is_thin(h, cur), h.Mq, false,
+              h.neuron_kind == BG3_NEURON_IZH, trial, ms);
     if (rc == BG3_OK && tune_growth) {
         // the overlap pass: one growth pass per candidate block size from the saved state
         float best_g = -1.0f;
@@ -1843,6 +1851,7 @@ int bg3_autotune(bg3_net *n, int32_t steps, int32_t tune_growth, bg3_launch_cfg 
     int rc2 = state_load(n, sc);
     state_free(sc);
     n->cfg = cur;
+    n->h.izh_hw_every = cur.izh_hw_every;
     drop_graph(n);
     if (rc) return rc;
     if (rc2) return rc2;
@@ -1872,9 +1881,10 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
     std::vector<StateCopy> sc(b->nets.size());
     int rc = BG3_OK;
     for (size_t k = 0; k < b->nets.size() && rc == BG3_OK; k++) rc = state_save(b->nets[k], sc[k]);
-    bool thick = false, thin = false;
+    bool thick = false, thin = false, izh = false;
     int mq = 1 << 30;
     for (bg3_net *n : b->nets) {
+        izh = izh || n->h.neuron_kind == BG3_NEURON_IZH;
         if (bg3::sweep_is_thin(n->h, b->cfg)) thin = true;
         else thick = true;
         mq = std::min(mq, n->h.Mq);
@@ -1883,7 +1893,8 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
     auto trial = [&](const LaunchCfg &c) -> float {
         for (size_t k = 0; k < b->nets.size(); k++)
             if (state_load(b->nets[k], sc[k]) != BG3_OK) return -1.0f;
-        const bool split = b->cfg.thin_max_quads != c.thin_max_quads;
+        const bool split = b->cfg.thin_max_quads != c.thin_max_quads ||
+                           b->cfg.izh_hw_every != c.izh_hw_every;
         b->cfg = c;
         if (split && batch_refresh(b) != BG3_OK) return -1.0f;
         if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -1891,7 +1902,7 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
         return time_batch_steps(b, steps);
     };
     float ms = 0.0f;
-    if (rc == BG3_OK) rc = tune(cur, thick, thin, thin ? 1 << 30 : mq, true, trial, ms);
+    if (rc == BG3_OK) rc = tune(cur, thick, thin, thin ? 1 << 30 : mq, true, izh, trial, ms);
     int rc2 = BG3_OK;
     for (size_t k = 0; k < b->nets.size(); k++) {
         if (sc[k].buf && state_load(b->nets[k], sc[k]) != BG3_OK) rc2 = BG3_ECUDA;
@@ -1936,7 +1947,7 @@ struct CkptHeader {
     uint32_t n_arrays;         // CKPT_ARRAYS
     uint32_t pad;
 };
-static const uint32_t CKPT_VERSION = 3;
+static const uint32_t CKPT_VERSION = 4;
 static const char CKPT_MAGIC[8] = {'B', 'G', '3', 'C', 'K', 'P', 'T', 0};
 
 static size_t alloc_size(const bg3_net *n, const void *p)

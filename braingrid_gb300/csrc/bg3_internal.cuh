@@ -69,8 +69,10 @@ struct LaunchCfg {
     int32_t sweep_dests;      // dests per TMA sweep tile of a single network: 16 or 32
     int32_t deliver_early;    // 1: spiking/DS delivery prepares its arrivals during the previous
                               // sweep, 0: it starts after it
+    int32_t izh_hw_every;     // Izhikevich update: every k-th 32-neuron tile in hardware FP64,
+                              // the others on the integer pipe (0: all on the integer pipe)
 };
-constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1};
+constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1, 0};
 
 // plane position of slot (dest d, row k) and its inverse (Mq row quads per dest)
 __host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Mq)
@@ -102,6 +104,7 @@ struct NetDev {
     float dt, epoch_duration;
     uint32_t noise_seed;
     int32_t ntiles;                // sweep tiles of 32 dests
+    int32_t izh_hw_every;          // LaunchCfg::izh_hw_every, for the fused neuron pass
     int32_t n_dcls, n_delays;
     // step counter and the last-CTA barrier of the sweep
     unsigned long long *step;
@@ -518,8 +521,11 @@ __device__ __forceinline__ int neuron_branch(const NeuronIn &x)
 // summation point value passed in.  Each float operation rounds on its own (-fmad=false) and the
 // double promotions of the reference's expressions are kept.  Returns true when the neuron
 // fired.  The caller stores sp = 0 afterwards.
+// hw: evaluate the Izhikevich double expression with the hardware FP64 pipe instead of its
+// integer-pipe restatement (the same bits either way).
 __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const NeuronIn &x, int br,
-                                             float sp, float noise, unsigned long long t)
+                                             float sp, float noise, unsigned long long t,
+                                             bool hw = false)
 {
     const bool izh = n.neuron_kind == 1;
     if (br == BR_REFRACTORY) {
@@ -551,24 +557,27 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
         // Vb = (float)(v + C3 * (0.04 v v + (double)(5 v) + 140 - u)), then
         // Vm = (float)((double)Vb * 0.001 + (double)(C2 sp)), each double operation rounded once
         // the double constants 0.04, 140.0 and 0.001 as (mantissa, exponent, sign)
-        constexpr SoftD K004 = {0x147ae147ae147bull, -5, 0u};
-        constexpr SoftD K140 = {0x11800000000000ull, 7, 0u};
-        constexpr SoftD K0001 = {0x10624dd2f1a9fcull, -10, 0u};
-        bool ok = true;
-        const SoftD vd = sd_from_float(Vint, ok);
-        SoftD t = sd_mul(K004, vd, ok);
-        t = sd_mul(t, vd, ok);
-        t = sd_add(t, sd_from_float(5.0f * Vint, ok), ok);
-        t = sd_add(t, K140, ok);
-        SoftD nu = sd_from_float(u, ok);
-        nu.s ^= 1u;
-        t = sd_add(t, nu, ok);
-        t = sd_mul(sd_from_float(C3, ok), t, ok);
-        const float Vb = sd_to_float(sd_add(vd, t, ok), ok);
-        SoftD w = sd_mul(sd_from_float(Vb, ok), K0001, ok);
-        w = sd_add(w, sd_from_float(x.C2 * sp, ok), ok);
-        float Vnew = sd_to_float(w, ok);
-        if (!ok) {  // outside the restated range: the same expression in hardware doubles
+        float Vnew;
+        bool ok = !hw;
+        if (ok) {
+            constexpr SoftD K004 = {0x147ae147ae147bull, -5, 0u};
+            constexpr SoftD K140 = {0x11800000000000ull, 7, 0u};
+            constexpr SoftD K0001 = {0x10624dd2f1a9fcull, -10, 0u};
+            const SoftD vd = sd_from_float(Vint, ok);
+            SoftD t = sd_mul(K004, vd, ok);
+            t = sd_mul(t, vd, ok);
+            t = sd_add(t, sd_from_float(5.0f * Vint, ok), ok);
+            t = sd_add(t, K140, ok);
+            SoftD nu = sd_from_float(u, ok);
+            nu.s ^= 1u;
+            t = sd_add(t, nu, ok);
+            t = sd_mul(sd_from_float(C3, ok), t, ok);
+            const float Vb = sd_to_float(sd_add(vd, t, ok), ok);
+            SoftD w = sd_mul(sd_from_float(Vb, ok), K0001, ok);
+            w = sd_add(w, sd_from_float(x.C2 * sp, ok), ok);
+            Vnew = sd_to_float(w, ok);
+        }
+        if (!ok) {  // hardware doubles (chosen, or outside the restated range)
             const double v = (double)Vint;
             const float Vh = (float)(v + (double)C3 * (0.04 * v * v + (double)(5.0f * Vint) +
                                                        140.0 - (double)u));

@@ -617,8 +617,9 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
         bool fired = false;
         if (valid) {
             const int br = neuron_branch(x);
+            const bool hw = n.izh_hw_every > 0 && ((d >> 5) % n.izh_hw_every) == 0;
             fired = neuron_apply(n, d, x, br, input_apply(n, d, x, t1, acc),
-                                 br == BR_INTEGRATE ? noise : 0.0f, t1);
+                                 br == BR_INTEGRATE ? noise : 0.0f, t1, hw);
             n.sp[d] = 0.0f;
         }
         ring_push(n, t1, fired, d);

@@ -66,7 +66,7 @@ class StdpConstants(ctypes.Structure):
 class LaunchCfg(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int32) for k in ("sweep_stages", "thin_max_quads", "thin_warps",
                                               "deliver_blocks", "growth_threads", "sweep_dests",
-                                              "deliver_early")]
+                                              "deliver_early", "izh_hw_every")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
