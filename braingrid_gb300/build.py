@@ -49,7 +49,10 @@ def build(verbose=False, extra=()):
         obj = os.path.join(BUILD, s.replace(".cu", ".o"))
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc()] + ARCH + FLAGS + list(extra) + ["-c", src, "-o", obj])
+            # -Xptxas -v: ptxas's per-kernel registers and spills, kept beside the object
+            # (ptxas_report) for the no-spill check of the hot kernels
+            jobs.append(([nvcc()] + ARCH + FLAGS + list(extra) + ["-Xptxas", "-v", "-c", src, "-o", obj],
+                         obj + ".ptxas.txt"))
 
     def run(cmd):
         if verbose:
@@ -59,8 +62,15 @@ def build(verbose=False, extra=()):
             raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
         return r.stderr
 
+    def compile_one(job):
+        cmd, report = job
+        err = run(cmd)
+        with open(report, "w") as f:
+            f.write(err)
+        return err
+
     with ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
-        for err in ex.map(run, jobs):
+        for err in ex.map(compile_one, jobs):
             if verbose and err:
                 print(err)
     if jobs or _stale(LIB, objs):
@@ -68,6 +78,26 @@ def build(verbose=False, extra=()):
         run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
         os.replace(tmp, LIB)
     return LIB
+
+
+def ptxas_report(source="bg3_step.cu"):
+    """{kernel (mangled name): (registers, spill store bytes, spill load bytes)} from the last
+    compile of a source (build() keeps ptxas's -v output beside the object)."""
+    import re
+    path = os.path.join(BUILD, source.replace(".cu", ".o") + ".ptxas.txt")
+    out, name = {}, None
+    for line in open(path):
+        m = re.search(r"Compiling entry function '([^']+)'", line)
+        if m:
+            name = m.group(1)
+            continue
+        m = re.search(r"(\d+) bytes spill stores, (\d+) bytes spill loads", line)
+        if m and name:
+            out.setdefault(name, [0, 0, 0])[1:] = [int(m.group(1)), int(m.group(2))]
+        m = re.search(r"Used (\d+) registers", line)
+        if m and name:
+            out.setdefault(name, [0, 0, 0])[0] = int(m.group(1))
+    return {k: tuple(v) for k, v in out.items()}
 
 
 if __name__ == "__main__":

@@ -374,6 +374,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     h.epoch_duration = D.epoch_duration;
     h.ntiles = (int)(Np / 32);
     h.max_epochs = D.max_epochs;
+    h.izh_hw_every = n->cfg.izh_hw_every;
     h.n_burst_bins = (int)((float)D.max_epochs * D.epoch_duration);
     h.n_spike_bins = (int)((float)D.max_epochs * D.epoch_duration * 100.0f);
     int rc = 0;

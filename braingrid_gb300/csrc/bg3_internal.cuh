@@ -72,7 +72,7 @@ struct LaunchCfg {
     int32_t izh_hw_every;     // Izhikevich update: every k-th 32-neuron tile in hardware FP64,
                               // the others on the integer pipe (0: all on the integer pipe)
 };
-constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1, 0};
+constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1, 1};
 
 // plane position of slot (dest d, row k) and its inverse (Mq row quads per dest)
 __host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Mq)
@@ -521,6 +521,15 @@ __device__ __forceinline__ int neuron_branch(const NeuronIn &x)
 // summation point value passed in.  Each float operation rounds on its own (-fmad=false) and the
 // double promotions of the reference's expressions are kept.  Returns true when the neuron
 // fired.  The caller stores sp = 0 afterwards.
+// The Izhikevich update's double expression on the FP64 pipe: Vb = (float)(v + C3 (0.04 v v +
+// (double)(5 v) + 140 - u)), then (float)((double)Vb * 0.001 + (double)(C2 sp)).
+__device__ __forceinline__ float izh_v_fp64(float Vint, float u, float C3, float c2sp)
+{
+    const double v = (double)Vint;
+    const float Vh = (float)(v + (double)C3 * (0.04 * v * v + (double)(5.0f * Vint) + 140.0 - (double)u));
+    return (float)((double)Vh * 0.001 + (double)c2sp);
+}
+
 // hw: evaluate the Izhikevich double expression with the hardware FP64 pipe instead of its
 // integer-pipe restatement (the same bits either way).
 __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const NeuronIn &x, int br,
@@ -558,11 +567,13 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
         // Vm = (float)((double)Vb * 0.001 + (double)(C2 sp)), each double operation rounded once
         // the double constants 0.04, 140.0 and 0.001 as (mantissa, exponent, sign)
         float Vnew;
-        bool ok = !hw;
-        if (ok) {
+        if (hw) {
+            Vnew = izh_v_fp64(Vint, u, C3, x.C2 * sp);
+        } else {
             constexpr SoftD K004 = {0x147ae147ae147bull, -5, 0u};
             constexpr SoftD K140 = {0x11800000000000ull, 7, 0u};
             constexpr SoftD K0001 = {0x10624dd2f1a9fcull, -10, 0u};
+            bool ok = true;
             const SoftD vd = sd_from_float(Vint, ok);
             SoftD t = sd_mul(K004, vd, ok);
             t = sd_mul(t, vd, ok);
@@ -576,12 +587,7 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
             SoftD w = sd_mul(sd_from_float(Vb, ok), K0001, ok);
             w = sd_add(w, sd_from_float(x.C2 * sp, ok), ok);
             Vnew = sd_to_float(w, ok);
-        }
-        if (!ok) {  // hardware doubles (chosen, or outside the restated range)
-            const double v = (double)Vint;
-            const float Vh = (float)(v + (double)C3 * (0.04 * v * v + (double)(5.0f * Vint) +
-                                                       140.0 - (double)u));
-            Vnew = (float)((double)Vh * 0.001 + (double)(x.C2 * sp));
+            if (!ok) Vnew = izh_v_fp64(Vint, u, C3, x.C2 * sp);  // outside the restated range
         }
         n.u_izh[i] = u + C3 * x.A * (x.B * Vint - u);
         n.Vm[i] = Vnew;

@@ -36,3 +36,21 @@ def test_status_strings_without_gpu():
     lib.bg3_status_string.restype = ctypes.c_char_p
     assert lib.bg3_status_string(0) == b"ok"
     assert b"invalid" in lib.bg3_status_string(-1)
+
+
+def test_hot_kernels_do_not_spill():
+    """The per-step kernels of the default configuration keep everything in registers (a spill in
+    the fused 32-dest sweep once cost config[1] 10 % of its step time): ptxas's report of the last
+    build for the single-network TMA sweep with the fused neuron pass (32-dest tiles, every
+    pipeline depth), the thin sweeps and the spiking / DS delivery.  (The 16-dest and unfused
+    sweep variants, and the batched STDP passes, spill a few bytes and are not held to this.)"""
+    bgbuild.build()
+    rep = bgbuild.ptxas_report("bg3_step.cu")
+    hot = {k: v for k, v in rep.items()
+           if k.startswith(("_ZN3bg37k_sweepILi1ELb1ELi4ELi32E", "_ZN3bg37k_sweepILi1ELb1ELi6ELi32E",
+                            "_ZN3bg37k_sweepILi1ELb1ELi8ELi32E", "_ZN3bg312k_sweep_thin",
+                            "_ZN3bg39k_deliverILi0E", "_ZN3bg39k_deliverILi1E",
+                            "_ZN3bg315k_deliver_batchILi0E", "_ZN3bg315k_deliver_batchILi1E"))}
+    assert len(hot) == 9, sorted(rep)
+    spilling = {k: v for k, v in hot.items() if v[1] or v[2]}
+    assert not spilling, spilling

@@ -13,7 +13,8 @@ from tests.netcases import assert_same, oracle_from_case
 
 pytestmark = pytest.mark.gpu
 
-CONFIGS = [dict(sweep_stages=4, thin_warps=4, deliver_blocks=152, growth_threads=128),
+CONFIGS = [dict(sweep_stages=4, thin_warps=4, deliver_blocks=152, growth_threads=128,
+                izh_hw_every=0),
            dict(sweep_stages=8, thin_warps=16, deliver_blocks=608, growth_threads=512,
                 deliver_early=0),
            dict(sweep_dests=16, sweep_stages=6, izh_hw_every=1),
