@@ -47,7 +47,7 @@ def run_harness(harness, workdir, cfg, args, out, serialize=None):
 
 
 # cases whose end-of-run checkpoint stream (Simulator::serialize) is kept in serialize.npz
-SERIALIZE_CASES = ("c0_grown", "c0_spiking", "c0_stdp", "izh_dstdp", "izh_static")
+SERIALIZE_CASES = ("c0_grown", "c0_spiking", "c0_stdp", "izh_dstdp", "izh_static", "ragged", "ragged_izh")
 
 
 def compact(d, keep_steps_every=None, syn_keep=None):
