@@ -1,11 +1,13 @@
 """Run a benchmark workload for a few steps, for profilers (ncu) to capture its kernels.
 
-    python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big|growth] [--steps 20] [--flush]
+    python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big|growth|heavy] [--steps 20] [--flush]
 
 c3 is the Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
 networks of the served stream's largest sizes (166x166, 176x176, 180x180) after one epoch and a
 growth pass (which restores the unscaled growth weights: the networks then fire at ~300 Hz),
-batched together.
+batched together.  heavy is one of those jobs (180x180) alone: 10,000 steps, a growth pass, 1,000
+steps (it then fires at ~300 Hz), then --steps steps timed kernel by kernel; its delivery passes
+after launch 11,000 are heavy ones.
 """
 import argparse
 
@@ -16,7 +18,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big", "growth"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big", "growth", "heavy"])
     ap.add_argument("--count", type=int, default=512, help="networks of the c3 workload")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
@@ -26,6 +28,24 @@ def main():
         net.growth(2)
         net.sync()
         print("synapses", net.total_synapses(), "error_word", net.error_word)
+        return
+    if a.workload == "heavy":
+        import numpy as np
+        from . import lib as bg
+        from . import serve
+        job = serve.lif_growth_job(180, 3, seed=77)
+        d = job.desc
+        net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height, d.epoch_duration,
+                         d.delta_t, d.max_firing_rate, d.max_epochs, d.synapse_kind, d.noise_mode,
+                         d.noise_seed)
+        job.setup(net)
+        net.step(10000)
+        net.growth(1)
+        net.step(1000)
+        _, km = net.bench_steps(a.steps, flush, per_kernel=True)
+        print("steps", a.steps, "deliver_us %.1f sweep_us %.1f" % (np.mean(km[:, 1]) * 1e3,
+                                                                 np.mean(km[:, 2]) * 1e3),
+              "synapses", net.total_synapses(), "error_word", net.error_word)
         return
     if a.workload == "c1":
         spec, net = workloads.build()
