@@ -432,17 +432,17 @@ def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
     times = serve.run_trace(srv, trace) if trace else {}
     srv.close()
     mine = [(job.name, times[job.id][0], times[job.id][1], int(job.result.synapse_steps),
-             int(job.result.status)) for _, job in trace]
+             int(job.result.status), int(job.result.error_word)) for _, job in trace]
     every = shard.gather(mine)
     if every is None:
         return None
     rows = [r for part in every for r in part]
-    lat = [f - a for _, a, f, _, _ in rows]
-    span = max(f for _, _, f, _, _ in rows) - min(a for _, a, _, _, _ in rows)
+    lat = [r[2] - r[1] for r in rows]
+    span = max(r[2] for r in rows) - min(r[1] for r in rows)
     pct = shard.latency_percentiles(lat)
     syn = sum(r[3] for r in rows)
     return {"workload": "config[4]: %d-job trace sharded over %d GPUs by job work" % (n_jobs, world),
-            "jobs": len(rows), "all_ok": all(r[4] == 0 for r in rows),
+            "jobs": len(rows), "all_ok": all(r[4] == 0 and r[5] == 0 for r in rows),
             "served_p50_s": pct["p50"], "served_p95_s": pct["p95"], "served_p99_s": pct["p99"],
             "served_makespan_s": span, "served_synapse_updates_per_s": syn / span,
             "jobs_per_rank": [len(part) for part in every]}
@@ -550,7 +550,7 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     st = srv.stats()
     srv.close()
     jobs = [j for _, j in trace]
-    ok = all(j.result.status == 0 for j in jobs)
+    ok = all(j.result.status == 0 and j.result.error_word == 0 for j in jobs)
     syn_steps = sum(int(j.result.synapse_steps) for j in jobs)
     span = max(finish.values()) - trace[0][0]
     L = np.array([lat[j.id] for j in jobs])
@@ -594,6 +594,7 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
                                                                    "rebuild_s")},
             "per_job": [{"name": j.name, "neurons": int(j.desc.n_neurons), "epochs": int(j.epochs),
                          "synapse_steps": int(j.result.synapse_steps),
+                         "error_word": int(j.result.error_word),
                          "served_latency_s": round(float(lat[j.id]), 3),
                          "plain_duration_s": round(float(dur), 3),
                          "plain_setup_s": round(float(su), 3)}

@@ -235,9 +235,11 @@ def sharded_trace(trace, rank, world):
 # ---- job families of the served stream -------------------------------------------------------
 def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_rate=1.0,
                    frac_inh=0.10, max_syn=None, epoch_duration=1.0, max_epochs=None, name="",
-                   **job_kw):
+                   max_firing_rate=1000, **job_kw):
     """The config[1]/[2] family: LIF + DS + ConnGrowth on a side x side grid, pre-grown to
-    radius (mean in-degree ~ pi (2 radius)^2, capped by max_syn), growth at every epoch end."""
+    radius (mean in-degree ~ pi (2 radius)^2, capped by max_syn), growth at every epoch end.
+    The first growth pass sets the weights from the overlap areas unscaled, after which the
+    larger networks fire at ~300 Hz: the spike-history ring is sized for max_firing_rate."""
     spec_args = dict(frac_inh=frac_inh, seed=seed)
     N = side * side
     if radius is None:
@@ -246,8 +248,9 @@ def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_r
         # in-degree ~ pi (2 radius)^2; the slack keeps growth from filling a row
         max_syn = int(min(1000, N, np.ceil(np.pi * (2 * radius + 2.0) ** 2 / 4) * 4))
         max_syn = max(4, (max_syn + 3) // 4 * 4)
-    desc = bg.NetDesc(N, max_syn, side, side, epoch_duration, 1e-4, 200, max_epochs or epochs,
-                      bg.BG3_NEURON_LIF, bg.BG3_SYN_DS, bg.BG3_NOISE_DEVICE, seed + 101)
+    desc = bg.NetDesc(N, max_syn, side, side, epoch_duration, 1e-4, max_firing_rate,
+                      max_epochs or epochs, bg.BG3_NEURON_LIF, bg.BG3_SYN_DS, bg.BG3_NOISE_DEVICE,
+                      seed + 101)
 
     def setup(net):
         spec = netgen.lif_network(side, side, **spec_args)
