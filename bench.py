@@ -1,9 +1,9 @@
 """Benchmark of the spiking hot path on one GB300: synapse-updates/s (and neuron-steps/s).
 
-Workload (config[1] of the stated benchmark): the plain single-network step of a 100x100 = 10,000
-neuron LIF + AllDSSynapses + ConnGrowth network, max 1,000 synapses per neuron, dt 0.1 ms,
-excitatory fraction 0.90, targetRate 1.0 Hz, seed 7, synthetic parameters with the config's
-value distributions (braingrid_gb300.netgen).  Connectivity is pre-grown (at the stated 0.4 start
+Workload (the headline): the plain single-network step of a 100x100 = 10,000 neuron LIF +
+AllDSSynapses + ConnGrowth network, max 1,000 synapses per neuron, dt 0.1 ms, excitatory fraction
+0.90, targetRate 1.0 Hz, seed 7, synthetic parameters with the stated value distributions
+(braingrid_gb300.netgen).  Connectivity is pre-grown (at the stated 0.4 start
 radius no pair overlaps, so no synapse would ever form): radii ~ U[8.35, 8.45] and one device
 growth pass wire every overlapping pair (~7.6 M synapses, up to ~930 per neuron); weights =
 overlap area x 1e-8 x a fixed scale.  A "step" is one simulation time step of the whole network:
@@ -12,16 +12,17 @@ of step t + 1 runs in the epilogue of sweep t; the first step's runs standalone)
 before every timed step; device time per step comes from CUDA events on the library's stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bg3|reference]
-                    [--serve-jobs J] [--serve-slots S] [--only c3|serve]
+                    [--serve-jobs J] [--serve-slots S] [--only c3|serve|growth]
 
-Beside the headline (config[1]) the line carries the batched forms of config[2] (36 LIF
-networks) and config[3] (512 Izhikevich + STDP networks), and the served stream of config[4]
-(a J-job trace through the job server, against the same jobs one at a time).
+Beside the headline the line carries the batched forms of the 36-network growth sweep (36 LIF
+networks) and of the 512-network Izhikevich + STDP batch, the served stream (a J-job trace through
+the job server, against the same jobs one at a time) and the growth pass.
 
 --impl reference times the reference algorithm's CPU path (the C restatement in oracle/, the
 reference's own sources are not on the GPU host) on the same network, single-threaded as the
-reference is.  Under torchrun every rank runs an independent replica (the path does not shard);
-value is the sum over ranks.
+reference is.  Under torchrun every rank runs an independent replica of the headline (the path
+does not shard within a network) and a share of the batched and served work (shard.py); value is
+the sum over ranks.
 """
 import argparse
 import json
@@ -49,7 +50,7 @@ METRIC = "synapse-updates/s"
 # word, delay index read; psr, queue, delay index written: 28 B) is reported beside it.
 SWEEP_BYTES_PER_SYN = 8.5
 SWEEP_BYTES_PER_NEURON = 48
-SURVEY_BYTES_PER_SYN = 28
+REF_LAYOUT_BYTES_PER_SYN = 28
 # served form: resident work cap, about one and a half of the largest jobs' synapse slots
 SERVE_SLOTS = 60e6
 
@@ -205,7 +206,7 @@ def run_bg3(args):
     peak, peak_kind = peaks()
     alg_bytes = SWEEP_BYTES_PER_SYN * S + SWEEP_BYTES_PER_NEURON * N
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
-    survey_achieved = (SURVEY_BYTES_PER_SYN * S + 4 * N) / (sweep_ms * 1e-3) / 1e9
+    ref_layout_achieved = (REF_LAYOUT_BYTES_PER_SYN * S + 4 * N) / (sweep_ms * 1e-3) / 1e9
     size_matched = size_matched_copy(alg_bytes)
     # end to end through the C-ABI with pinned host buffers: every iteration uploads the neuron
     # state (H2D), advances E2E_STEPS steps and reads back the spike counts and history (D2H)
@@ -244,9 +245,9 @@ def run_bg3(args):
     else:
         # the batched and served forms spread over the ranks by instance (bin packed, no
         # collective); whole-job figures over the slowest rank
-        batched = run_batch_sharded("config[2]", rank, world, min(args.steps, 500),
+        batched = run_batch_sharded("sweep36", rank, world, min(args.steps, 500),
                                     max(args.warmup, 20))
-        izh_stdp = run_batch_sharded("config[3]", rank, world, min(args.steps, 1000),
+        izh_stdp = run_batch_sharded("izh512", rank, world, min(args.steps, 1000),
                                      max(args.warmup, 20))
         if args.serve_jobs > 0:
             served = run_served_sharded(args.serve_jobs, int(args.serve_slots), rank, world)
@@ -258,7 +259,7 @@ def run_bg3(args):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "config[1] plain single-network step: 100x100 LIF + DS + "
+            "config": {"workload": "plain single-network step: 100x100 LIF + DS + "
                                    "ConnGrowth, max 1000 synapses/neuron, pre-grown radius "
                                    "U[8.35,8.45], weight scale %g" % WEIGHT_SCALE,
                        "neurons": N, "synapses": S, "dt_s": 1e-4, "noise": "device",
@@ -272,8 +273,8 @@ def run_bg3(args):
                          "peak_kind": peak_kind, "launch_ms": sweep_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "bytes_per_synapse": SWEEP_BYTES_PER_SYN,
-                         "reference_layout_bytes_per_synapse": SURVEY_BYTES_PER_SYN,
-                         "reference_layout_equivalent_gbs": survey_achieved,
+                         "reference_layout_bytes_per_synapse": REF_LAYOUT_BYTES_PER_SYN,
+                         "reference_layout_equivalent_gbs": ref_layout_achieved,
                          "size_matched_copy": dict(size_matched,
                                                    frac=achieved / size_matched["gbs"]),
                          "kernel_shares": {"neurons": float(shares[0]), "deliver": float(shares[1]),
@@ -294,7 +295,7 @@ def run_bg3(args):
 
 
 def run_batched(steps, warmup):
-    """config[2]: the 36-network sweep as one batch (one launch per kernel per step) against the
+    """The 36-network growth sweep as one batch (one launch per kernel per step) against the
     same networks run one network at a time with bg3_step (each on its own CUDA graph)."""
     import time as _t
     from braingrid_gb300 import lib as bg
@@ -333,8 +334,9 @@ def run_batched(steps, warmup):
         n.sync()
     t_lock = (_t.perf_counter() - t0) / lock
     err = max(n.error_word for n in nets)
-    out = {"workload": "config[2]: 36 networks (9 each of 30x30, 50x50, 70x70, 100x100; targetRate "
-                       "x excitatory fraction x 4 seeds), pre-grown as config[1]",
+    out = {"workload": "36-network growth sweep: 9 each of 30x30, 50x50, 70x70, 100x100 "
+                       "(targetRate x excitatory fraction x 4 seeds), pre-grown as the headline "
+                       "network",
            "networks": len(nets), "neurons": N, "synapses": S, "steps": steps,
            "batched_synapse_updates_per_s": S * steps / t_batch,
            "batched_neuron_steps_per_s": N * steps / t_batch,
@@ -384,12 +386,12 @@ def size_matched_copy(traffic_bytes, reps=25):
 
 
 def run_batch_sharded(which, rank, world, steps, warmup):
-    """config[2] or config[3] over N GPUs: each rank builds and batches its share of the networks
+    """The 36-network sweep ("sweep36") or the 512-network Izhikevich batch ("izh512") over N GPUs: each rank builds and batches its share of the networks
     (bin packed by synapse slots, the same split on every rank) and times its own batch; the
     whole-job rate is every rank's synapse-steps over the slowest rank's time."""
     from braingrid_gb300 import lib as bg
     from braingrid_gb300 import netgen, shard, workloads
-    if which == "config[2]":
+    if which == "sweep36":
         members = workloads.c2_members()
         weights = [m["width"] * m["height"] * m["max_syn"] for m in members]
         mine = shard.share(list(range(len(members))), weights, rank, world)
@@ -422,7 +424,7 @@ def run_batch_sharded(which, rank, world, steps, warmup):
 
 
 def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
-    """config[4] over N GPUs: every rank serves its share of the same trace (jobs bin packed by
+    """The served stream over N GPUs: every rank serves its share of the same trace (jobs bin packed by
     work, arrival times kept) with its own job server; latencies are gathered on rank 0."""
     from braingrid_gb300 import serve, shard, workloads
     trace = serve.sharded_trace(workloads.c4_trace(n_jobs), rank, world)
@@ -441,7 +443,7 @@ def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
     span = max(r[2] for r in rows) - min(r[1] for r in rows)
     pct = shard.latency_percentiles(lat)
     syn = sum(r[3] for r in rows)
-    return {"workload": "config[4]: %d-job trace sharded over %d GPUs by job work" % (n_jobs, world),
+    return {"workload": "served stream: %d-job trace sharded over %d GPUs by job work" % (n_jobs, world),
             "jobs": len(rows), "all_ok": all(r[4] == 0 and r[5] == 0 for r in rows),
             "served_p50_s": pct["p50"], "served_p95_s": pct["p95"], "served_p99_s": pct["p99"],
             "served_makespan_s": span, "served_synapse_updates_per_s": syn / span,
@@ -450,7 +452,7 @@ def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
 
 def run_growth():
     """ConnGrowth epoch pass (radii update, O(N^2) overlap scan, weight update / synapse
-    creation, map rebuild, recorder) on config[1]: at the stated start radius 0.4 (every pair
+    creation, map rebuild, recorder) on the headline network: at the stated start radius 0.4 (every pair
     rejected), at the pre-grown radii U[8.35, 8.45] creating ~7.6 M synapses, and once more at
     those radii updating them.  Host wall clock around a synchronised pass."""
     import time as _t
@@ -485,7 +487,7 @@ def run_growth():
 
 
 def run_c3(steps, warmup):
-    """config[3]: 512 Izhikevich + dynamic STDP networks (static wiring, Poisson drive) advanced
+    """The 512-network batch: Izhikevich + dynamic STDP networks (static wiring, Poisson drive) advanced
     as one batch against the same networks run one at a time with bg3_step."""
     import time as _t
     from braingrid_gb300 import lib as bg
@@ -513,7 +515,7 @@ def run_c3(steps, warmup):
     t_plain = _t.perf_counter() - t0
     spikes = sum(int(n.download_lif(fields=("spikeCount",))["spikeCount"].sum()) for n in nets)
     err = max(n.error_word for n in nets)
-    out = {"workload": "config[3]: %d Izhikevich + dynamic STDP networks, N ~ U[500, 8000] "
+    out = {"workload": "%d Izhikevich + dynamic STDP networks, N ~ U[500, 8000] "
                        "(grids), static wiring 10 nearest within radius 5 + 10%% rewired, "
                        "Poisson 10 Hz x 5 nA" % len(nets),
            "networks": len(nets), "neurons": N, "synapses": S, "steps": steps,
@@ -535,7 +537,7 @@ def run_c3(steps, warmup):
 
 
 def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
-    """config[4]: a seeded open-loop Poisson trace (20 jobs/s) through the job server
+    """The served stream: a seeded open-loop Poisson trace (20 jobs/s) through the job server
     (continuous batching, footprint admission, 150 GB budget), then the same jobs one at a
     time through the plain API.  Latency = completion - arrival, host wall clock."""
     import time as _t
@@ -582,7 +584,7 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
         plat.append(t_free - a)
     plat = np.array(plat)
     pct = lambda x, q: float(np.percentile(x, q))
-    return {"workload": "config[4]: %d-job seeded Poisson trace at 20 jobs/s from the config[1]-[3] "
+    return {"workload": "served stream: %d-job seeded Poisson trace at 20 jobs/s from the three "
                         "families (LIF sides U[10,200] pre-grown, Izhikevich N U[500,8000]), 1-20 "
                         "epochs of 1 s, 150 GB admission budget" % n_jobs,
             "jobs": n_jobs, "all_ok": ok, "synapse_steps": syn_steps,
@@ -641,7 +643,7 @@ def run_reference(args):
             "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": dt * 1e3 / k,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "config[1] plain single-network step: 100x100 LIF + DS + "
+            "config": {"workload": "plain single-network step: 100x100 LIF + DS + "
                                    "ConnGrowth, max 1000 synapses/neuron, pre-grown radius "
                                    "U[8.35,8.45], weight scale %g" % WEIGHT_SCALE,
                        "neurons": N, "synapses": S},
@@ -662,7 +664,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="bg3", choices=["bg3", "reference"])
     ap.add_argument("--serve-jobs", type=int, default=8,
-                    help="jobs of the served-stream trace (config[4])")
+                    help="jobs of the served-stream trace")
     ap.add_argument("--serve-slots", type=float, default=SERVE_SLOTS,
                     help="served form: cap on the resident jobs' synapse slots (0 = none)")
     ap.add_argument("--only", choices=["c3", "serve", "growth"], default=None,

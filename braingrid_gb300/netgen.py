@@ -4,7 +4,7 @@ Builds what the reference's host setup would (Layouts/Layout.cpp:41-73 grid posi
 FixedLayout E/I and starter sites, AllIFNeurons::createNeuron parameter ranges and constants,
 Neurons/AllIFNeurons.cpp:398-503) from a seeded numpy generator, so that benchmark networks of
 any size can be made without the reference's MTRand draws.  The value distributions are the
-config[0] ones: Iinject 13.5 nA, Inoise U[1.0, 1.5] nA, Vthresh 15 mV (starters U[13.565,
+10x10 benchmark network's: Iinject 13.5 nA, Inoise U[1.0, 1.5] nA, Vthresh 15 mV (starters U[13.565,
 13.655] mV), Vreset 13.5 mV (starters 13.0 mV), Vrest 0, Vinit 13.0 mV, Cm 30 nF, Rm 1 MOhm,
 Trefract 3 ms (2 ms inhibitory), dt 0.1 ms.
 """

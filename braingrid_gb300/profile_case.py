@@ -23,7 +23,8 @@ def main():
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
     if a.workload == "growth":
-        # config[1]'s growth pass at the pre-grown radii: creation, then an updating pass
+        # the 10,000-neuron network's growth pass at the pre-grown radii: creation, then an
+        # updating pass
         spec, net = workloads.build()
         net.growth(2)
         net.sync()

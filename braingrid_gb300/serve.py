@@ -236,7 +236,7 @@ def sharded_trace(trace, rank, world):
 def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_rate=1.0,
                    frac_inh=0.10, max_syn=None, epoch_duration=1.0, max_epochs=None, name="",
                    max_firing_rate=1000, **job_kw):
-    """The config[1]/[2] family: LIF + DS + ConnGrowth on a side x side grid, pre-grown to
+    """The LIF growth family: LIF + DS + ConnGrowth on a side x side grid, pre-grown to
     radius (mean in-degree ~ pi (2 radius)^2, capped by max_syn), growth at every epoch end.
     The first growth pass sets the weights from the overlap areas unscaled, after which the
     larger networks fire at ~300 Hz: the spike-history ring is sized for max_firing_rate."""
@@ -261,7 +261,7 @@ def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_r
 
 def izh_static_job(width, height, epochs, seed, epoch_duration=1.0, max_epochs=None, name="",
                    **job_kw):
-    """The config[3] family: Izhikevich neurons, static wiring (10 nearest within radius 5,
+    """The Izhikevich + STDP family: Izhikevich neurons, static wiring (10 nearest within radius 5,
     10 % rewired), dynamic STDP, Poisson drive at 10 Hz / 5 nA; epochs end in the recorder."""
     spec, syn, counts, M = netgen.izh_static_spec(width, height, seed)
     desc = bg.NetDesc(spec["N"], M, width, height, epoch_duration, 1e-4, 1000,

@@ -3,7 +3,7 @@ import numpy as np
 
 from . import netgen
 
-# config[1]: plain single network, 100x100 LIF + DS + ConnGrowth, max 1000 synapses per neuron.
+# The plain single network: 100x100 LIF + DS + ConnGrowth, max 1000 synapses per neuron.
 # At the stated start radius (0.4) no pair overlaps, so throughput is measured on a pre-grown
 # state: radii ~ U[8.35, 8.45] wired by one device growth pass (~7.6 M synapses), weights scaled.
 C1 = dict(width=100, height=100, max_syn=1000, radius=8.4, weight_scale=0.003, seed=7,
@@ -19,8 +19,8 @@ def build(w=C1):
     return spec, net
 
 
-# config[2]: 36 networks, targetRate {0.1, 1.0, 1.9} Hz x excitatory fraction {0.80, 0.90, 0.98}
-# x 4 seeds, sizes cycling 30x30, 50x50, 70x70, 100x100; the config[1] model otherwise, with the
+# The 36-network growth sweep: targetRate {0.1, 1.0, 1.9} Hz x excitatory fraction {0.80, 0.90,
+# 0.98} x 4 seeds, sizes cycling 30x30, 50x50, 70x70, 100x100; the plain network's model otherwise, with the
 # same pre-grown radius and weight scale.
 C2_SIZES = [30, 50, 70, 100]
 
@@ -48,7 +48,7 @@ def build_member(w):
     return spec, net
 
 
-# config[3]: 512 independent Izhikevich + dynamic STDP networks, sizes ~ U[500, 8000] neurons on
+# The 512-network batch: independent Izhikevich + dynamic STDP networks, sizes ~ U[500, 8000] neurons on
 # near-square grids, 20 % inhibitory, static wiring (10 nearest within radius 5, 10 % rewired),
 # weights U[10, 20] nA / U[-40, -20] nA, additive STDP (Apos 0.005, Aneg -0.00525 of the 30 nA
 # bound, tau 20 ms), Poisson drive 10 Hz x 5 nA, dt 0.1 ms.
@@ -71,10 +71,10 @@ def build_c3(count=C3_NETWORKS, seed=3, max_epochs=10):
     return nets
 
 
-# config[4]: served stream.  Open-loop Poisson arrivals at 20 jobs/s (seeded trace); each job
-# drawn from the config[1]-[3] families: LIF + DS + ConnGrowth pre-grown like config[1]
-# (side ~ U[10, 200], radius min(8.4, 0.45 side)), the config[2] parameter sweep (targetRate,
-# excitatory fraction), or the config[3] Izhikevich + STDP network (N ~ U[500, 8000]);
+# The served stream.  Open-loop Poisson arrivals at 20 jobs/s (seeded trace); each job
+# drawn from the three families above: LIF + DS + ConnGrowth pre-grown like the plain network
+# (side ~ U[10, 200], radius min(8.4, 0.45 side)), the growth-sweep parameters (targetRate,
+# excitatory fraction), or the Izhikevich + STDP network (N ~ U[500, 8000]);
 # 1-20 epochs of 1 s; admission against a 150 GB footprint budget.
 C4_RATE = 20.0
 C4_BUDGET = 150 << 30

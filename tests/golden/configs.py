@@ -4,7 +4,7 @@ Each case is described twice, consistently: as a BrainGrid XML config (written b
 write_config_tree for the reference harness) and as plain parameters (read by the tests to set up
 the oracle and the CUDA path without the reference tree).
 
-The config[0]-style networks follow the stated model: LIF neurons, AllDSSynapses, ConnGrowth,
+The 10x10-style networks follow the stated model: LIF neurons, AllDSSynapses, ConnGrowth,
 FixedLayout with 10 % inhibitory and 10 endogenously active (starter) sites chosen by a seeded
 shuffle; Iinject 13.5 nA, Inoise U[1.0, 1.5] nA, Vthresh 15 mV (starters U[13.565, 13.655] mV),
 Vreset 13.5 mV (starters 13.0 mV), Vrest 0, Vinit 13.0 mV, dt 0.1 ms.
@@ -77,16 +77,16 @@ CASES = [
     # the reference's own tiny test (2x2, 1 epoch of 1 s), with its own NLists
     _case("ref_tiny", 2, 2, 1.0, 1, 200, target_rate=1.9, config="configfiles/test-tiny.xml",
           inh=[1], starters=[0], keep_steps_every=500),
-    # config[0]: 10x10, 10 epochs x 1 s, max 100 synapses per neuron, seed 1
+    # the 100-neuron benchmark network: 10x10, 10 epochs x 1 s, max 100 synapses per neuron, seed 1
     _case("c0", 10, 10, 1.0, 10, 100, keep_steps_every=5000),
-    # config[0] network with a pre-grown radius so that growth wires it after epoch 1
+    # the same network with a pre-grown radius so that growth wires it after epoch 1
     # (the reference recorder needs epoch duration x epochs >= 1 s)
     _case("c0_grown", 10, 10, 0.2, 5, 100, radii=1.2, max_firing_rate=1000,
           keep_steps_every=100),
     # 30x30 pre-grown network, larger fan-in and fan-out
     _case("m30_grown", 30, 30, 0.1, 10, 200, radii=2.0, max_firing_rate=1000, site_seed=3,
           keep_steps_every=1000, syn_keep=(9,)),
-    # FP64 reference on config[0] (long-run comparison base)
+    # FP64 reference on the 10x10 network (long-run comparison base)
     _case("c0_fp64", 10, 10, 1.0, 10, 100, fp64=True),
     # Regular pulse input, random per-neuron phase (sync="no": shifts drawn before the neurons)
     _case("c0_regular", 10, 10, 0.5, 2, 100, keep_steps_every=250,

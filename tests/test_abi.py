@@ -40,7 +40,7 @@ def test_status_strings_without_gpu():
 
 def test_hot_kernels_do_not_spill():
     """The per-step kernels of the default configuration keep everything in registers (a spill in
-    the fused 32-dest sweep once cost config[1] 10 % of its step time): ptxas's report of the last
+    the fused 32-dest sweep once cost the 10,000-neuron network 10 % of its step time): ptxas's report of the last
     build for the single-network TMA sweep with the fused neuron pass (32-dest tiles, every
     pipeline depth), the thin sweeps and the spiking / DS delivery.  (The 16-dest and unfused
     sweep variants, and the batched STDP passes, spill a few bytes and are not held to this.)"""

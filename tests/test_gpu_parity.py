@@ -25,12 +25,12 @@ pytestmark = pytest.mark.gpu
 
 
 def test_c0_first_epoch_bit_exact():
-    """config[0] (10x10, no synapses yet): every step of the first 1 s epoch."""
+    """The 10x10 network (no synapses yet): every step of the first 1 s epoch."""
     run_locked("c0", epochs=1, check_every=1)
 
 
 def test_c0_ten_epochs_epoch_ends_bit_exact():
-    """config[0] in full (10 x 1 s, 100,000 steps): radii, rates, spike histories and recorder
+    """The 10x10 network in full (10 x 1 s, 100,000 steps): radii, rates, spike histories and recorder
     histograms equal the oracle's at every epoch end, hence the FP32 reference's (whose gap to the
     FP64 build is pinned in test_oracle_golden)."""
     c = case("c0")
@@ -86,7 +86,7 @@ def test_c0_grown_gpu_raster_matches_reference_dump():
 
 
 def test_regular_input_bit_exact():
-    """Regular pulses with random per-neuron phases (config[0] network, 2 x 0.5 s)."""
+    """Regular pulses with random per-neuron phases (10x10 network, 2 x 0.5 s)."""
     o, net = run_locked("c0_regular", check_every=50)
     assert int(o.arr("spikeCount").sum()) >= 0
 

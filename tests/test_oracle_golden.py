@@ -135,7 +135,7 @@ def _check_xml_golden(c, g, nm):
 
 
 def test_fp32_vs_fp64_reference_long_run_gap():
-    """config[0] for 10 x 1 s against the reference built with BGFLOAT = double.  The FP32 path
+    """The 10x10 network for 10 x 1 s against the reference built with BGFLOAT = double.  The FP32 path
     (the oracle here, bit-exact with the FP32 reference and with the GPU) differs from the FP64
     build by the amounts below; they are properties of the model's FP32 arithmetic, measured:
     final radii 1.5e-3 relative, network spike count 5.2 %, per-neuron rates up to 60 % (the ten
