@@ -12,7 +12,7 @@ of step t + 1 runs in the epilogue of sweep t; the first step's runs standalone)
 before every timed step; device time per step comes from CUDA events on the library's stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bg3|reference]
-                    [--serve-jobs J] [--serve-slots S] [--only c3|serve|growth]
+                    [--serve-jobs J] [--serve-slots S] [--only izh512|serve|growth]
 
 Beside the headline the line carries the batched forms of the 36-network growth sweep (36 LIF
 networks) and of the 512-network Izhikevich + STDP batch, the served stream (a J-job trace through
@@ -37,10 +37,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from braingrid_gb300.workloads import C1  # noqa: E402
+from braingrid_gb300.workloads import PLAIN  # noqa: E402
 
-WIDTH, HEIGHT, MAX_SYN = C1["width"], C1["height"], C1["max_syn"]
-RADIUS, WEIGHT_SCALE, SEED = C1["radius"], C1["weight_scale"], C1["seed"]
+WIDTH, HEIGHT, MAX_SYN = PLAIN["width"], PLAIN["height"], PLAIN["max_syn"]
+RADIUS, WEIGHT_SCALE, SEED = PLAIN["radius"], PLAIN["weight_scale"], PLAIN["seed"]
 FLUSH_BYTES = 256 << 20
 METRIC = "synapse-updates/s"
 # Algorithmic bytes of the dominant kernel (k_sweep, with the next step's neuron pass fused in):
@@ -112,7 +112,7 @@ def dist_env():
 
 def build_network():
     from braingrid_gb300 import workloads
-    return workloads.build(workloads.C1)
+    return workloads.build(workloads.PLAIN)
 
 
 def traffic_per_launch(S):
@@ -239,7 +239,7 @@ def run_bg3(args):
     if world == 1:
         growth = run_growth()
         batched = run_batched(min(args.steps, 500), max(args.warmup, 20))
-        izh_stdp = run_c3(min(args.steps, 1000), max(args.warmup, 20))
+        izh_stdp = run_izh512(min(args.steps, 1000), max(args.warmup, 20))
         if args.serve_jobs > 0:
             served = run_served(args.serve_jobs, int(args.serve_slots))
     else:
@@ -300,7 +300,7 @@ def run_batched(steps, warmup):
     import time as _t
     from braingrid_gb300 import lib as bg
     from braingrid_gb300 import workloads
-    members = workloads.c2_members()
+    members = workloads.sweep36_members()
     nets = [workloads.build_member(w)[1] for w in members]
     S = sum(n.total_synapses() for n in nets)
     N = sum(n.N for n in nets)
@@ -392,12 +392,12 @@ def run_batch_sharded(which, rank, world, steps, warmup):
     from braingrid_gb300 import lib as bg
     from braingrid_gb300 import netgen, shard, workloads
     if which == "sweep36":
-        members = workloads.c2_members()
+        members = workloads.sweep36_members()
         weights = [m["width"] * m["height"] * m["max_syn"] for m in members]
         mine = shard.share(list(range(len(members))), weights, rank, world)
         nets = [workloads.build_member(members[i])[1] for i in mine]
     else:
-        shapes = workloads.c3_shapes()
+        shapes = workloads.izh512_shapes()
         weights = [w * h for w, h in shapes]
         mine = shard.share(list(range(len(shapes))), weights, rank, world)
         nets = [netgen.make_izh_static(shapes[k][0], shapes[k][1], seed=1000 + k,
@@ -427,8 +427,8 @@ def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
     """The served stream over N GPUs: every rank serves its share of the same trace (jobs bin packed by
     work, arrival times kept) with its own job server; latencies are gathered on rank 0."""
     from braingrid_gb300 import serve, shard, workloads
-    trace = serve.sharded_trace(workloads.c4_trace(n_jobs), rank, world)
-    srv = serve.Server(hbm_budget_bytes=workloads.C4_BUDGET, max_resident=64,
+    trace = serve.sharded_trace(workloads.served_trace(n_jobs), rank, world)
+    srv = serve.Server(hbm_budget_bytes=workloads.SERVED_BUDGET, max_resident=64,
                        chunk_steps=chunk_steps, max_resident_slots=slots_cap)
     shard.barrier()  # one trace clock for all ranks
     times = serve.run_trace(srv, trace) if trace else {}
@@ -486,14 +486,14 @@ def run_growth():
     return out
 
 
-def run_c3(steps, warmup):
+def run_izh512(steps, warmup):
     """The 512-network batch: Izhikevich + dynamic STDP networks (static wiring, Poisson drive) advanced
     as one batch against the same networks run one at a time with bg3_step."""
     import time as _t
     from braingrid_gb300 import lib as bg
     from braingrid_gb300 import workloads
     t0 = _t.perf_counter()
-    nets = workloads.build_c3()
+    nets = workloads.build_izh512()
     t_build = _t.perf_counter() - t0
     S = sum(n.total_synapses() for n in nets)
     N = sum(n.N for n in nets)
@@ -543,8 +543,8 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     import time as _t
     from braingrid_gb300 import lib as bg
     from braingrid_gb300 import serve, workloads
-    trace = workloads.c4_trace(n_jobs)
-    srv = serve.Server(hbm_budget_bytes=workloads.C4_BUDGET, max_resident=64,
+    trace = workloads.served_trace(n_jobs)
+    srv = serve.Server(hbm_budget_bytes=workloads.SERVED_BUDGET, max_resident=64,
                        chunk_steps=chunk_steps, max_resident_slots=slots_cap)
     times = serve.run_trace(srv, trace)
     lat = {k: f - a for k, (a, f) in times.items()}
@@ -558,7 +558,7 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     L = np.array([lat[j.id] for j in jobs])
     # plain: the same jobs, one at a time, each on its own network with bg3_step + epoch passes
     durations, setups = [], []
-    for _, job in workloads.c4_trace(n_jobs):
+    for _, job in workloads.served_trace(n_jobs):
         d = job.desc
         t1 = _t.perf_counter()
         net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height, d.epoch_duration,
@@ -667,13 +667,13 @@ def main():
                     help="jobs of the served-stream trace")
     ap.add_argument("--serve-slots", type=float, default=SERVE_SLOTS,
                     help="served form: cap on the resident jobs' synapse slots (0 = none)")
-    ap.add_argument("--only", choices=["c3", "serve", "growth"], default=None,
+    ap.add_argument("--only", choices=["izh512", "serve", "growth"], default=None,
                     help="run one secondary workload alone and print its JSON")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.only == "c3":
-        print(json.dumps(run_c3(min(args.steps, 1000), max(args.warmup, 20))), flush=True)
+    if args.only == "izh512":
+        print(json.dumps(run_izh512(min(args.steps, 1000), max(args.warmup, 20))), flush=True)
         return
     if args.only == "growth":
         print(json.dumps(run_growth()), flush=True)

@@ -1,8 +1,9 @@
 """Run a benchmark workload for a few steps, for profilers (ncu) to capture its kernels.
 
-    python -m braingrid_gb300.profile_case [--workload c1|c2|c3|big|growth|heavy] [--steps 20] [--flush]
+    python -m braingrid_gb300.profile_case [--workload plain|sweep36|izh512|big|growth|heavy] [--steps 20] [--flush]
 
-c3 is the Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
+plain is the 100x100 network of the headline, sweep36 the 36-network growth sweep, izh512 the
+Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
 networks of the served stream's largest sizes (166x166, 176x176, 180x180) after one epoch and a
 growth pass (which restores the unscaled growth weights: the networks then fire at ~300 Hz),
 batched together.  heavy is one of those jobs (180x180) alone: 10,000 steps, a growth pass, 1,000
@@ -18,8 +19,9 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "big", "growth", "heavy"])
-    ap.add_argument("--count", type=int, default=512, help="networks of the c3 workload")
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "sweep36", "izh512", "big", "growth", "heavy"])
+    ap.add_argument("--count", type=int, default=512, help="networks of the izh512 workload")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
     if a.workload == "growth":
@@ -48,17 +50,17 @@ def main():
                                                                  np.mean(km[:, 2]) * 1e3),
               "synapses", net.total_synapses(), "error_word", net.error_word)
         return
-    if a.workload == "c1":
+    if a.workload == "plain":
         spec, net = workloads.build()
         net.bench_steps(a.steps, flush)
         print("steps", a.steps, "synapses", net.total_synapses(), "error_word", net.error_word)
         assert net.error_word == 0
     else:
         from . import lib as bg
-        if a.workload == "c2":
-            nets = [workloads.build_member(w)[1] for w in workloads.c2_members()]
-        elif a.workload == "c3":
-            nets = workloads.build_c3(count=a.count)
+        if a.workload == "sweep36":
+            nets = [workloads.build_member(w)[1] for w in workloads.sweep36_members()]
+        elif a.workload == "izh512":
+            nets = workloads.build_izh512(count=a.count)
         else:
             from . import serve
             nets = []

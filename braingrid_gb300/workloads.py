@@ -6,11 +6,11 @@ from . import netgen
 # The plain single network: 100x100 LIF + DS + ConnGrowth, max 1000 synapses per neuron.
 # At the stated start radius (0.4) no pair overlaps, so throughput is measured on a pre-grown
 # state: radii ~ U[8.35, 8.45] wired by one device growth pass (~7.6 M synapses), weights scaled.
-C1 = dict(width=100, height=100, max_syn=1000, radius=8.4, weight_scale=0.003, seed=7,
+PLAIN = dict(width=100, height=100, max_syn=1000, radius=8.4, weight_scale=0.003, seed=7,
           frac_inh=0.10, epoch_duration=1.0, max_firing_rate=200, max_epochs=10)
 
 
-def build(w=C1):
+def build(w=PLAIN):
     spec = netgen.lif_network(w["width"], w["height"], frac_inh=w["frac_inh"], seed=w["seed"])
     net = netgen.make_gpu_network(spec, w["max_syn"], epoch_duration=w["epoch_duration"],
                                   max_firing_rate=w["max_firing_rate"],
@@ -22,17 +22,17 @@ def build(w=C1):
 # The 36-network growth sweep: targetRate {0.1, 1.0, 1.9} Hz x excitatory fraction {0.80, 0.90,
 # 0.98} x 4 seeds, sizes cycling 30x30, 50x50, 70x70, 100x100; the plain network's model otherwise, with the
 # same pre-grown radius and weight scale.
-C2_SIZES = [30, 50, 70, 100]
+SWEEP36_SIZES = [30, 50, 70, 100]
 
 
-def c2_members():
+def sweep36_members():
     out = []
     k = 0
     for tr in (0.1, 1.0, 1.9):
         for fe in (0.80, 0.90, 0.98):
             for seed in range(4):
-                side = C2_SIZES[k % 4]
-                out.append(dict(C1, width=side, height=side, frac_inh=round(1.0 - fe, 2),
+                side = SWEEP36_SIZES[k % 4]
+                out.append(dict(PLAIN, width=side, height=side, frac_inh=round(1.0 - fe, 2),
                                 seed=seed, target_rate=tr))
                 k += 1
     return out
@@ -52,10 +52,10 @@ def build_member(w):
 # near-square grids, 20 % inhibitory, static wiring (10 nearest within radius 5, 10 % rewired),
 # weights U[10, 20] nA / U[-40, -20] nA, additive STDP (Apos 0.005, Aneg -0.00525 of the 30 nA
 # bound, tau 20 ms), Poisson drive 10 Hz x 5 nA, dt 0.1 ms.
-C3_NETWORKS = 512
+IZH512_NETWORKS = 512
 
 
-def c3_shapes(count=C3_NETWORKS, seed=3):
+def izh512_shapes(count=IZH512_NETWORKS, seed=3):
     rs = np.random.RandomState(seed)
     out = []
     for n in rs.randint(500, 8001, size=count):
@@ -64,9 +64,9 @@ def c3_shapes(count=C3_NETWORKS, seed=3):
     return out
 
 
-def build_c3(count=C3_NETWORKS, seed=3, max_epochs=10):
+def build_izh512(count=IZH512_NETWORKS, seed=3, max_epochs=10):
     nets = []
-    for k, (w, h) in enumerate(c3_shapes(count, seed)):
+    for k, (w, h) in enumerate(izh512_shapes(count, seed)):
         nets.append(netgen.make_izh_static(w, h, seed=1000 + k, max_epochs=max_epochs)[1])
     return nets
 
@@ -76,11 +76,11 @@ def build_c3(count=C3_NETWORKS, seed=3, max_epochs=10):
 # (side ~ U[10, 200], radius min(8.4, 0.45 side)), the growth-sweep parameters (targetRate,
 # excitatory fraction), or the Izhikevich + STDP network (N ~ U[500, 8000]);
 # 1-20 epochs of 1 s; admission against a 150 GB footprint budget.
-C4_RATE = 20.0
-C4_BUDGET = 150 << 30
+SERVED_RATE = 20.0
+SERVED_BUDGET = 150 << 30
 
 
-def c4_trace(n_jobs, seed=4, rate=C4_RATE, epoch_duration=1.0):
+def served_trace(n_jobs, seed=4, rate=SERVED_RATE, epoch_duration=1.0):
     """[(arrival_s, job)] for n_jobs jobs of the served stream."""
     from . import serve
     rs = np.random.RandomState(seed)

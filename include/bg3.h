@@ -364,8 +364,8 @@ typedef struct {
                                  0: it starts after the sweep.  Same results either way.            */
     int32_t izh_hw_every;     /* Izhikevich networks: every k-th group of 32 neurons evaluates the
                                  update's double-precision expression on the FP64 pipe, the others
-                                 on the integer pipe (an exact restatement): 0 .. 8, 0 = none
-                                 (default).  Same results either way; the two pipes share the work. */
+                                 on the integer pipe (an exact restatement): 0 .. 8, 0 = none,
+                                 1 = all (default).  Same results either way.                        */
 } bg3_launch_cfg;
 int bg3_get_launch(bg3_net *net, bg3_launch_cfg *cfg);
 int bg3_set_launch(bg3_net *net, const bg3_launch_cfg *cfg);

@@ -55,12 +55,12 @@ def _rank_main(rank, world, port, q):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
         from braingrid_gb300 import serve, workloads
-        members = workloads.c2_members()
+        members = workloads.sweep36_members()
         weights = [m["width"] * m["height"] * m["max_syn"] for m in members]
         mine = shard.share(list(range(len(members))), weights, rank, world)
         units, t = shard.reduce_timing(float(sum(weights[i] for i in mine)), 1.0 + rank)
         nets = shard.gather(mine)
-        part = serve.sharded_trace(workloads.c4_trace(12), rank, world)
+        part = serve.sharded_trace(workloads.served_trace(12), rank, world)
         jobs = shard.gather([(a, job.name, int(job.desc.noise_seed)) for a, job in part])
         shard.barrier()
         q.put((rank, mine, units, t, nets, jobs))
@@ -88,7 +88,7 @@ def test_two_rank_gloo_sharding_and_reporting():
                 p.kill()
     assert all(p.exitcode == 0 for p in procs)
     from braingrid_gb300 import workloads
-    members = workloads.c2_members()
+    members = workloads.sweep36_members()
     weights = [m["width"] * m["height"] * m["max_syn"] for m in members]
     r0, r1 = got[0], got[1]
     # the networks: each rank's share, disjoint and complete, as rank 0 gathered them
@@ -98,7 +98,7 @@ def test_two_rank_gloo_sharding_and_reporting():
     assert r0[2] == r1[2] == float(sum(weights))
     assert r0[3] == r1[3] == 2.0
     # the served trace: every job on exactly one rank, arrival times kept
-    trace = workloads.c4_trace(12)
+    trace = workloads.served_trace(12)
     every = sorted(x for part in r0[5] for x in part)
     assert every == sorted((a, j.name, int(j.desc.noise_seed)) for a, j in trace)
     assert all(len(part) > 0 for part in r0[5])
