@@ -30,6 +30,7 @@ void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 
 bool sweep_is_thin(const NetDev &h, const LaunchCfg &c);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, int add_threads, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
+void launch_scale_weights(const NetDev &h, float f, cudaStream_t s);
 void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
 
@@ -738,6 +739,15 @@ int bg3_upload_weights(bg3_net *n, const float *Wref)
         for (size_t k = 0; k < count[d]; k++) ev[slot_pos((int)k, (int)d, (int)n->h.Mq)].W = Wref[d * M + k];
     if ((rc = h2d(n, n->h.ev, ev.data(), S))) return rc;
     CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
+int bg3_scale_weights(bg3_net *n, float factor)
+{
+    if (!n) return BG3_EINVAL;
+    bg3::launch_scale_weights(n->h, factor, n->stream);
+    n->launches += 1;
+    CK(cudaGetLastError());
     return BG3_OK;
 }
 

@@ -286,6 +286,23 @@ void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s)
     k_record_epoch<<<(h.N + 255) / 256, 256, 0, s>>>(d_net, -1, false);
 }
 
+// W *= f for every in-use slot (one float multiply each, as a host loop would do it).
+__global__ void k_scale_weights(const __grid_constant__ NetDev n, float f)
+{
+    const size_t S = (size_t)n.Np * (size_t)n.Mq * 4;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < S;
+         p += (size_t)gridDim.x * blockDim.x) {
+        int k, d;
+        pos_slot(p, n.Mq, k, d);
+        if (d < n.N && (uint32_t)k < n.count[d]) n.ev[p].W = n.ev[p].W * f;
+    }
+}
+
+void launch_scale_weights(const NetDev &h, float f, cudaStream_t s)
+{
+    k_scale_weights<<<152 * 8, 256, 0, s>>>(h, f);
+}
+
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s)
 {
     int nb = (h.N + 255) / 256;

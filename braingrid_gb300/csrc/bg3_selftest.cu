@@ -107,7 +107,10 @@ extern "C" int bg3_selftest_binary64(uint64_t samples, uint64_t seed, uint64_t *
     if (!counts) return BG3_EINVAL;
     unsigned long long *d = nullptr;
     if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return BG3_ENOMEM;
-    cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+    if (cudaMemset(d, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(d);
+        return BG3_ECUDA;
+    }
     k_softd_test<<<152 * 8, 256>>>(samples, seed, d);
     unsigned long long h[4];
     const cudaError_t e1 = cudaDeviceSynchronize();

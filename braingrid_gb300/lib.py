@@ -179,6 +179,7 @@ def load(build_if_missing=True):
         "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
         "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
         "bg3_upload_weights": ([vp, c_f32p], ctypes.c_int),
+        "bg3_scale_weights": ([vp, ctypes.c_float], ctypes.c_int),
         "bg3_input_regular": ([vp, c_f32p, c_i32p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
                               ctypes.c_int),
         "bg3_input_poisson": ([vp, ctypes.POINTER(PoissonArrays), ctypes.c_float, ctypes.c_uint32,
@@ -438,6 +439,10 @@ class Network:
         s = PoissonArrays(*[_p(out[k]) for k, _ in POISSON_FIELDS])
         check(self.L.bg3_download_poisson(self.h, ctypes.byref(s)), "bg3_download_poisson")
         return out
+
+    def scale_weights(self, factor):
+        """W *= factor for every in-use synapse, on the device (bg3_scale_weights)."""
+        check(self.L.bg3_scale_weights(self.h, float(factor)), "bg3_scale_weights")
 
     def push_noise(self, values):
         v = np.ascontiguousarray(values, np.float32)

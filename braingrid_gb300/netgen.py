@@ -80,10 +80,9 @@ def pregrow(net, spec, radius, spread=0.05, weight_scale=1.0, seed=11):
     net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
                       g["start_radius"], r)
     net.growth(0)
-    net.sync()
     if weight_scale != 1.0:
-        s = net.download_synapses()
-        net.upload_weights((s["W"] * np.float32(weight_scale)).astype(np.float32))
+        net.scale_weights(np.float32(weight_scale))
+    net.sync()
     return r
 
 

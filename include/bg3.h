@@ -196,6 +196,10 @@ int bg3_upload_growth(bg3_net *net, const bg3_growth_params *p, const float *rad
 /* Sets W of every in-use slot from a reference-layout array (n_neurons * max_syn_per_neuron),
  * the weight upload of the reference's GPU growth path (Connections/ConnGrowth_d.cu:37-45). */
 int bg3_upload_weights(bg3_net *net, const float *W);
+/* Multiplies the weight of every in-use synapse by factor, on the device (W = W * factor in
+ * float, the same bits as a host loop over the downloaded weights).  No counterpart in the
+ * reference: it builds benchmark networks from grown ones without moving the synapse arrays. */
+int bg3_scale_weights(bg3_net *net, float factor);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
 

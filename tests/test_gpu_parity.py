@@ -218,3 +218,22 @@ def test_ragged_shapes_bit_exact(name):
     row quad (30, 18 slots), DS and Izhikevich + dynamic STDP + Poisson."""
     o, net = run_locked(name, check_every=5, syn_every=50)
     assert o.total > 0
+
+
+def test_device_weight_scaling_matches_host_scaling():
+    """bg3_scale_weights gives the same bits as scaling the downloaded weights on the host."""
+    c = case("c0_grown")
+    o = oracle_from_case(c)
+    a = gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_DEVICE)
+    b = gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_DEVICE)
+    a.growth(1)
+    b.growth(1)
+    f = np.float32(0.003)
+    a.scale_weights(f)
+    s = b.download_synapses()
+    b.upload_weights((s["W"] * f).astype(np.float32))
+    sa, sb = a.download_synapses(), b.download_synapses()
+    assert int(sa["in_use"].sum()) > 0
+    assert_same("W", sa["W"], sb["W"])
+    a.close()
+    b.close()
