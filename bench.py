@@ -450,6 +450,14 @@ def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
             "jobs_per_rank": [len(part) for part in every]}
 
 
+def _sm_max_mhz():
+    """Maximum SM clock from MEASURED_PEAKS.json (2070 MHz on GB300 if absent)."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["sm_max_mhz"])
+    except (OSError, KeyError, ValueError):
+        return 2070.0
+
+
 def run_growth():
     """ConnGrowth epoch pass (radii update, O(N^2) overlap scan, weight update / synapse
     creation, map rebuild, recorder) on the headline network: at the stated start radius 0.4 (every pair
@@ -478,9 +486,20 @@ def run_growth():
     t_create = timed(3)
     S = net.total_synapses()
     t_update = timed(4)
+    # FP32 roofline of the rejecting pass: 8 FP32 operations per pair (dx, dy, d^2, the radius
+    # sum and the comparison) against the FP32 pipe's peak, 128 lanes x 152 SMs x the SM clock
+    # (no FMA: the library is compiled without contraction); the pass also holds the radii
+    # update, the map rebuild and the recorder, so this understates the overlap kernel alone
+    clk = _sm_max_mhz() * 1e6
+    fp32_peak = 128 * 152 * clk
     out.update({"radius_0.4_s": t_reject, "radius_0.4_pairs_per_s": N * N / t_reject,
+                "radius_0.4_fp32_ops_per_s": 8 * N * N / t_reject,
+                "fp32_pipe_peak_ops_per_s": fp32_peak,
+                "radius_0.4_fp32_frac": 8 * N * N / t_reject / fp32_peak,
                 "grown_create_s": t_create, "grown_update_s": t_update,
                 "grown_pairs_per_s": N * N / t_update, "synapses": S,
+                "grown_bound": "fp64 (acos and sin of the overlap area evaluated in double; "
+                               "86 % FP64-pipe busy, profiles/k_growth_plain.md)",
                 "error_word": net.error_word})
     net.close()
     return out
