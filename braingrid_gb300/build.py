@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, "libbg3.so")
 ROOT = os.path.dirname(HERE)
 
 SOURCES = ["bg3_step.cu", "bg3_growth.cu", "bg3_api.cu", "bg3_noalloc.cu", "bg3_serve.cu",
-           "bg3_selftest.cu", "bg3_serialize.cu"]
+           "bg3_selftest.cu", "bg3_serialize.cu", "bg3_hostrng.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]

@@ -178,6 +178,10 @@ def load(build_if_missing=True):
         "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
         "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
         "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
+        "bg3_norm_create": ([ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.POINTER(vp)],
+                            ctypes.c_int),
+        "bg3_norm_fill": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
+        "bg3_norm_destroy": ([vp], None),
         "bg3_upload_weights": ([vp, c_f32p], ctypes.c_int),
         "bg3_scale_weights": ([vp, ctypes.c_float], ctypes.c_int),
         "bg3_input_regular": ([vp, c_f32p, c_i32p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
@@ -266,6 +270,34 @@ def footprint(desc):
     if v < 0:
         check(v, "bg3_net_footprint")
     return v
+
+
+class NormStream:
+    """The reference's noise stream, Norm(mu, sigma, seed) (bg3_norm_*): take(n) returns the next
+    n values; consecutive takes continue one stream.  Host only."""
+
+    def __init__(self, seed, mu=0.0, sigma=1.0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        check(self.L.bg3_norm_create(int(seed) & 0xFFFFFFFF, mu, sigma, ctypes.byref(h)),
+              "bg3_norm_create")
+        self.h = h
+
+    def take(self, n):
+        out = np.empty(int(n), np.float32)
+        check(self.L.bg3_norm_fill(self.h, _p(out) if n else None, int(n)), "bg3_norm_fill")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.bg3_norm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Network:

@@ -1,0 +1,91 @@
+"""A BrainGrid run from its parameter files on the GPU: the reference's growth driver
+(Core/BGDriver.cpp, Core/Simulator.cpp:140-190) with this library as the model.
+
+    python -m braingrid_gb300.sim -t config.xml [-s stim.xml] [-o result.xml] [--noise device]
+
+reads the parameter file (braingrid_gb300.config), sets the network up as the reference does,
+runs numSims epochs of Tsim seconds with the epoch pass at each end (ConnGrowth's growth and
+recorder, or the plain recorder), and writes the reference's result file (braingrid_gb300.
+results) to -o, or to the file's stateOutputFileName.  With the reference's noise stream (the
+default) the result file is the reference's, byte for byte, wherever the run is bit-exact (see
+the parity tests); --noise device draws the noise on the GPU instead.  A Poisson stimulus draws
+its intervals on the GPU in either mode.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import config as cf
+from . import lib as bg
+from . import results
+
+
+def simulate(p, noise="reference", arrays=None, max_chunk_values=1 << 24):
+    """Runs p (config.Params); returns dict(text=result file, seconds=wall time of the epochs,
+    steps=simulation steps, error_word=the device error word)."""
+    a = arrays if arrays is not None else cf.setup(p)
+    inject = noise == "reference"
+    net = cf.network(p, a, noise_mode=bg.BG3_NOISE_INJECT if inject else bg.BG3_NOISE_DEVICE)
+    try:
+        N, spe = a["N"], p.steps_per_epoch
+        gen = bg.NormStream(p.seed) if inject else None
+        chunk = max(1, min(spe, max_chunk_values // max(N, 1)))
+        growth = p.conn_class == "ConnGrowth"
+        t0 = time.perf_counter()
+        for e in range(p.epochs):
+            done = 0
+            while done < spe:
+                k = min(chunk, spe - done)
+                if inject:
+                    # at most one value per neuron per step is consumed; what is left over
+                    # stays at the head of the device queue for the next chunk
+                    net.push_noise(gen.take(N * k))
+                net.step(k)
+                done += k
+            if growth:
+                net.growth(e + 1)
+            else:
+                net.record()
+        net.sync()
+        seconds = time.perf_counter() - t0
+        err = net.error_word
+        vthresh = net.download_lif(fields=("Vthresh",))["Vthresh"]
+        text = results.state_xml(growth, N, p.epochs, p.tsim, cf.DELTA_T, net.sim_step,
+                                 net.download_histories(), a["xloc"], a["yloc"], a["ntype"],
+                                 a["starter"], vthresh)
+        if gen is not None:
+            gen.close()
+        return dict(text=text, seconds=seconds, steps=net.sim_step, error_word=err)
+    finally:
+        net.close()
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("-t", "--config", required=True, help="parameter file")
+    ap.add_argument("-s", "--stim", default=None, help="stimulus file")
+    ap.add_argument("-o", "--output", default=None, help="result file (default: the "
+                    "parameter file's stateOutputFileName)")
+    ap.add_argument("--noise", choices=("reference", "device"), default="reference")
+    a = ap.parse_args(argv)
+    p = cf.read(a.config, a.stim)
+    r = simulate(p, a.noise)
+    out = a.output or p.output
+    if out:
+        d = os.path.dirname(out)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        with open(out, "w") as f:
+            f.write(r["text"])
+    sim_s = float(np.float32(p.tsim) * np.float32(p.epochs))
+    print(json.dumps({"output": out, "simulated_s": sim_s, "wall_s": round(r["seconds"], 3),
+                      "steps": r["steps"], "error_word": r["error_word"]}))
+    return 0 if r["error_word"] == 0 else 1
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -203,6 +203,16 @@ int bg3_scale_weights(bg3_net *net, float factor);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
 
+/* The reference's own noise stream on the host, for bg3_push_noise: Norm(mu, sigma, seed)
+ * (RNG/Norm.cpp:59-86, the Marsaglia polar method in float over MTRand,
+ * RNG/MersenneTwister.cpp), the generator the reference's single-threaded model creates from
+ * the parameter file's seed (Core/SingleThreadedSpikingModel.cpp:30).  bg3_norm_fill writes the
+ * next n values; consecutive fills continue one stream.  Host only (no device, no stream). */
+typedef struct bg3_norm bg3_norm;
+int bg3_norm_create(uint32_t seed, float mu, float sigma, bg3_norm **out);
+int bg3_norm_fill(bg3_norm *gen, float *values, int64_t n);
+void bg3_norm_destroy(bg3_norm *gen);
+
 /* ---- external input (one per network, as ISInput) --------------------------------------- */
 /* Regular pulses (Inputs/SInputRegular.cpp:20-112, HostSInputRegular.cpp:59-80): per-neuron
  * values and phase shifts as the reference's constructor computed them, the pulse and cycle

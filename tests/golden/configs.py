@@ -227,34 +227,95 @@ def neuron_ranges(c):
     return IZH_IF_RANGES if c.get("neuron") == "izh" else LIF_RANGES
 
 
-def write_config_tree(cfgdir):
-    """Write configfiles/bg3/<case>.xml and its NLists for every generated case."""
+STDP_NAMES = ("Apos", "Aneg", "STDPgap", "tauspost", "tauspre", "taupos", "tauneg", "WexExc",
+              "WexInh", "mupos", "muneg")
+
+
+def config_text(c, stdp_params=False):
+    """The case's BrainGrid parameter file.  stdp_params=True adds the case's STDP constants as
+    an <STDPParams> element (read by braingrid_gb300.config; the reference harness takes them
+    with --stdp instead)."""
+    p = dict(c)
+    p.update(c["growth"])
+    p["synapse_class"] = SYN_CLASS[c.get("synapse", 1)]
+    if c.get("static"):
+        p["connections"] = STATIC_XML.format(**c["static"])
+    else:
+        p["connections"] = GROWTH_XML.format(**c["growth"])
+    if c.get("neuron") == "izh":
+        p["neuron_class"] = "AllIZHNeurons"
+        p["neuron_params"] = _range_xml(IZH_IF_RANGES) + "\n" + _izh_xml(IZH_RANGES)
+    else:
+        p["neuron_class"] = "AllLIFNeurons"
+        p["neuron_params"] = _range_xml(LIF_RANGES)
+    text = _XML.format(**p)
+    if stdp_params and c.get("stdp") is not None:
+        st = "".join("<%s>%r</%s>" % (k, float(v), k) for k, v in zip(STDP_NAMES, c["stdp"]))
+        text = text.replace('name="SynapsesParams"></SynapsesParams>',
+                            'name="SynapsesParams"><STDPParams>%s</STDPParams></SynapsesParams>'
+                            % st)
+    return text
+
+
+def list_texts(c):
+    """The case's active (starter) and inhibitory neuron-list files."""
+    return ('<?xml version="1.0" encoding="UTF-8"?>\n<A>%s</A>\n'
+            % " ".join(str(i) for i in c["starters"]),
+            '<?xml version="1.0" encoding="UTF-8"?>\n<I>%s</I>\n'
+            % " ".join(str(i) for i in c["inh"]))
+
+
+def write_case(c, cfgdir, stdp_params=False):
+    """Write configfiles/bg3/<case>.xml, its neuron lists and its stimulus file under cfgdir
+    (the configfiles directory)."""
     d = os.path.join(cfgdir, "bg3")
     os.makedirs(d, exist_ok=True)
+    name = c["name"]
+    with open(os.path.join(d, name + ".xml"), "w") as f:
+        f.write(config_text(c, stdp_params))
+    active, inh = list_texts(c)
+    with open(os.path.join(d, name + "-active.xml"), "w") as f:
+        f.write(active)
+    with open(os.path.join(d, name + "-inh.xml"), "w") as f:
+        f.write(inh)
+    if c.get("stim") is not None:
+        with open(os.path.join(d, name + "-stim.xml"), "w") as f:
+            f.write(stim_xml(c["stim"]))
+
+
+# The reference's own test-small (configfiles/test-small.xml with its 10x10 NLists)
+TEST_SMALL = dict(name="ref_small", width=10, height=10, N=100, tsim=100.0, epochs=2, max_syn=200,
+                  seed=1, max_firing_rate=200, inh=[33, 66],
+                  starters=[7, 11, 14, 37, 41, 44, 67, 71, 74, 97],
+                  growth=dict(epsilon=0.60, beta=0.10, rho=1e-4, target_rate=1.9, min_radius=0.1,
+                              start_radius=0.4), radii=None)
+
+# Whole runs whose result file (Recorders/XmlGrowthRecorder.cpp:104-153) the compiled reference's
+# own driver wrote from the same parameter files: tests/golden/outputs.npz.  Every one keeps its
+# start radii below the grid spacing, so no synapse forms and a GPU run stays bit-exact.
+# (No DynamicLayout run: the reference refuses every DynamicLayout file, its
+# DynamicLayout::readParameters returning false after reading frac_EXC,
+# Layouts/DynamicLayout.cpp:60-78.)
+OUTPUT_CASES = ("ref_tiny", "ref_small", "c0", "c0_regular")
+
+
+def dynamic_layout_text(text, frac_exc, frac_starter):
+    """A parameter file with its FixedLayout replaced by DynamicLayout."""
+    return text.replace(
+        '<LayoutParams class="FixedLayout" name="LayoutParams">',
+        '<LayoutParams class="DynamicLayout" name="LayoutParams">'
+        '<frac_EXC name="frac_EXC">%r</frac_EXC><starter_neurons name="starter_neurons">%r'
+        '</starter_neurons>' % (frac_exc, frac_starter))
+
+
+def output_case(name):
+    """(case, parameter-file text, stimulus text or None) of an OUTPUT_CASES entry."""
+    c = TEST_SMALL if name == "ref_small" else case(name)
+    return c, config_text(c), (stim_xml(c["stim"]) if c.get("stim") else None)
+
+
+def write_config_tree(cfgdir):
+    """Write configfiles/bg3/<case>.xml and its NLists for every generated case."""
     for c in CASES:
-        if not c["config"].startswith("configfiles/bg3/"):
-            continue
-        p = dict(c)
-        p.update(c["growth"])
-        p["synapse_class"] = SYN_CLASS[c.get("synapse", 1)]
-        if c.get("static"):
-            p["connections"] = STATIC_XML.format(**c["static"])
-        else:
-            p["connections"] = GROWTH_XML.format(**c["growth"])
-        if c.get("neuron") == "izh":
-            p["neuron_class"] = "AllIZHNeurons"
-            p["neuron_params"] = _range_xml(IZH_IF_RANGES) + "\n" + _izh_xml(IZH_RANGES)
-        else:
-            p["neuron_class"] = "AllLIFNeurons"
-            p["neuron_params"] = _range_xml(LIF_RANGES)
-        with open(os.path.join(d, c["name"] + ".xml"), "w") as f:
-            f.write(_XML.format(**p))
-        with open(os.path.join(d, c["name"] + "-active.xml"), "w") as f:
-            f.write('<?xml version="1.0" encoding="UTF-8"?>\n<A>%s</A>\n'
-                    % " ".join(str(i) for i in c["starters"]))
-        with open(os.path.join(d, c["name"] + "-inh.xml"), "w") as f:
-            f.write('<?xml version="1.0" encoding="UTF-8"?>\n<I>%s</I>\n'
-                    % " ".join(str(i) for i in c["inh"]))
-        if c.get("stim") is not None:
-            with open(os.path.join(d, c["name"] + "-stim.xml"), "w") as f:
-                f.write(stim_xml(c["stim"]))
+        if c["config"].startswith("configfiles/bg3/"):
+            write_case(c, cfgdir)

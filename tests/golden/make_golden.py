@@ -10,7 +10,8 @@ harness on each case, and (4) keeps a compact subset of each dump as tests/golde
 The reference's own CPU golden outputs for test-tiny and test-small
 (old/validation/4-2016/growth/test-{tiny,small}-out.xml) are parsed into ref_goldens.npz, and the
 reference's checkpoint stream at the end of a few cases (Simulator::serialize) goes to
-serialize.npz (--only-serialize rewrites that file alone).
+serialize.npz (--only-serialize rewrites that file alone), and the reference driver's result
+files of whole runs (OUTPUT_CASES in configs.py) go to outputs.npz (--only-outputs).
 
 Nothing at test time reads the reference tree: the tests only read the .npz files written here.
 """
@@ -28,7 +29,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from oracle.refdump import read_dump  # noqa: E402
-from tests.golden.configs import write_config_tree, CASES  # noqa: E402
+from tests.golden.configs import (CASES, OUTPUT_CASES, list_texts, output_case,  # noqa: E402
+                                  write_config_tree)
 
 
 def build_reference(ref, fp64=False):
@@ -48,6 +50,40 @@ def run_harness(harness, workdir, cfg, args, out, serialize=None):
 
 # cases whose end-of-run checkpoint stream (Simulator::serialize) is kept in serialize.npz
 SERIALIZE_CASES = ("c0_grown", "c0_spiking", "c0_stdp", "izh_dstdp", "izh_static", "ragged", "ragged_izh")
+
+
+def run_outputs(growth, work, ref):
+    """The reference driver's result file for each OUTPUT_CASES entry, run from the same
+    parameter files the product reads (the reference's own test-tiny and test-small results must
+    come out equal to its committed goldens)."""
+    out = {}
+    d = os.path.join(work, "configfiles", "bg3")
+    os.makedirs(d, exist_ok=True)
+    os.makedirs(os.path.join(work, "results"), exist_ok=True)
+    for name in OUTPUT_CASES:
+        c, text, stim = output_case(name)
+        cfg = os.path.join(d, "out_%s.xml" % name)
+        with open(cfg, "w") as f:
+            f.write(text.replace("results/%s-out.xml" % c["name"], "results/out_%s.xml" % name))
+        active, inh = list_texts(c)
+        for suffix, t in (("-active.xml", active), ("-inh.xml", inh)):
+            with open(os.path.join(d, c["name"] + suffix), "w") as f:
+                f.write(t)
+        cmd = [growth, "-t", cfg]
+        if stim:
+            sp = os.path.join(d, "out_%s-stim.xml" % name)
+            with open(sp, "w") as f:
+                f.write(stim)
+            cmd += ["-s", sp]
+        subprocess.check_call(cmd, cwd=work, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        res = open(os.path.join(work, "results", "out_%s.xml" % name), "rb").read()
+        out[name] = np.frombuffer(res, np.uint8)
+        gold = {"ref_tiny": "test-tiny", "ref_small": "test-small"}.get(name)
+        if gold:
+            want = open(os.path.join(ref, "old/validation/4-2016/growth/%s-out.xml" % gold),
+                        "rb").read()
+            assert res == want, "%s: the driver's result differs from its golden" % name
+    return out
 
 
 def compact(d, keep_steps_every=None, syn_keep=None):
@@ -128,8 +164,19 @@ def main():
     ap.add_argument("--cases", default="")
     ap.add_argument("--only-serialize", action="store_true",
                     help="write serialize.npz only (the other fixtures stay as they are)")
+    ap.add_argument("--only-outputs", action="store_true",
+                    help="write outputs.npz only (the reference driver's result files)")
     a = ap.parse_args()
     harness = build_reference(a.ref)
+    if a.only_outputs:
+        work = tempfile.mkdtemp(prefix="bg_golden_")
+        try:
+            out = run_outputs(os.path.join(os.path.dirname(harness), "growth"), work, a.ref)
+            np.savez_compressed(os.path.join(HERE, "outputs.npz"), **out)
+            print("wrote outputs", sorted(out))
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+        return
     harness64 = build_reference(a.ref, fp64=True)
     work = tempfile.mkdtemp(prefix="bg_golden_")
     try:

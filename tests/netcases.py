@@ -4,16 +4,9 @@ import os
 import numpy as np
 
 from oracle import pyoracle as po
-from tests.golden.configs import IZH_IF_RANGES, IZH_RANGES, LIF_RANGES, case
+from tests.golden.configs import IZH_IF_RANGES, IZH_RANGES, LIF_RANGES, TEST_SMALL, case  # noqa: F401
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-
-# the reference's own test-small (configfiles/test-small.xml with its 10x10 NLists)
-TEST_SMALL = dict(name="ref_small", width=10, height=10, N=100, tsim=100.0, epochs=2, max_syn=200,
-                  seed=1, max_firing_rate=200, inh=[33, 66],
-                  starters=[7, 11, 14, 37, 41, 44, 67, 71, 74, 97],
-                  growth=dict(epsilon=0.60, beta=0.10, rho=1e-4, target_rate=1.9, min_radius=0.1,
-                              start_radius=0.4), radii=None)
 
 
 def load_fixture(name):

@@ -1,0 +1,102 @@
+"""Networks built from BrainGrid parameter files alone (braingrid_gb300.config / .sim) on the GPU.
+
+(1) A whole run from the parameter file, with the reference's noise stream made by the library
+(bg3_norm_*), writes the reference driver's result file byte for byte (tests/golden/outputs.npz,
+written by the compiled reference from the same files).  (2) A ConnStatic + dynamic STDP +
+Poisson network built by config.network runs in lock step with the oracle holding the same
+wiring (config's neighbour order), bit for bit."""
+import numpy as np
+import pytest
+
+from braingrid_gb300 import config as cf
+from braingrid_gb300 import lib as bg
+from braingrid_gb300 import sim
+from tests.golden import configs
+from tests.gpu_helpers import compare_input, compare_neurons, compare_synapses
+from tests.netcases import assert_same, oracle_from_case, steps_per_epoch
+
+pytestmark = pytest.mark.gpu
+
+
+def read_output_case(name, tmp_path):
+    c, text, stim = configs.output_case(name)
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    return cf.read(text, stim, root=str(tmp_path))
+
+
+@pytest.mark.parametrize("name", configs.OUTPUT_CASES)
+def test_run_from_parameter_file_writes_reference_result(name, tmp_path):
+    p = read_output_case(name, tmp_path)
+    r = sim.simulate(p, noise="reference")
+    assert r["error_word"] == 0
+    assert r["steps"] == p.steps_per_epoch * p.epochs
+    want = np.load("tests/golden/outputs.npz")[name].tobytes().decode()
+    if r["text"] != want:
+        got_l, want_l = r["text"].splitlines(), want.splitlines()
+        bad = [i for i, (a, b) in enumerate(zip(got_l, want_l)) if a != b]
+        raise AssertionError("%s: %d lines differ, first %r" % (
+            name, len(bad), [(got_l[i][:120], want_l[i][:120]) for i in bad[:2]]))
+
+
+def test_cli_writes_result_file(tmp_path):
+    c, text, stim = configs.output_case("ref_tiny")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    cfg = tmp_path / "tiny.xml"
+    cfg.write_text(text)
+    out = tmp_path / "out.xml"
+    import os
+    cwd = os.getcwd()
+    os.chdir(str(tmp_path))
+    try:
+        assert sim.main(["-t", str(cfg), "-o", str(out)]) == 0
+    finally:
+        os.chdir(cwd)
+    assert out.read_text() == np.load("tests/golden/outputs.npz")["ref_tiny"].tobytes().decode()
+
+
+def test_static_stdp_poisson_network_from_parameter_file(tmp_path):
+    c = configs.case("izh_static")
+    configs.write_case(c, str(tmp_path / "configfiles"), stdp_params=True)
+    base = str(tmp_path / "configfiles" / "bg3" / c["name"])
+    p = cf.read(base + ".xml", base + "-stim.xml", root=str(tmp_path))
+    a = cf.setup(p)
+    net = cf.network(p, a, noise_mode=bg.BG3_NOISE_INJECT)
+    # the uploads round-trip
+    g = net.download_synapses()
+    s = a["synapses"]
+    used = s["in_use"].astype(bool)
+    assert_same("in_use", g["in_use"], s["in_use"])
+    for k in ("src", "type", "W", "decay", "total_delay", "U", "D", "F", "u", "r"):
+        assert_same(k, g[k][used], s[k][used])
+    st = net.download_stdp()
+    want = cf.stdp_arrays(s, cf.stdp_constants(p))
+    for k in ("Apos", "Aneg", "Wex", "tauspost", "taupos", "tauneg"):
+        assert_same(k, st[k][used], want[k][used])
+    izh = net.download_izh()
+    for k in ("Aconst", "Bconst", "Cconst", "Dconst", "C3"):
+        assert_same(k, izh[k], a[k])
+
+    # the oracle with the same wiring: the case minus the reference's dump, then the synapses in
+    # creation order, then the weight draws skipped on its global generator
+    o = oracle_from_case(dict(c, static=None))
+    slots = a["creation_slots"]
+    M = p.max_syn
+    for sl in slots:
+        o.create_synapse(int(sl // M), int(s["src"][sl]), int(s["type"][sl]), float(s["W"][sl]))
+    assert o.rebuild_maps() == 0
+    o.rng_skip(len(slots))
+    spe = steps_per_epoch(c)
+    steps = spe
+    begin, isis = o.poisson_isi_draws(steps + 2)
+    net.push_poisson_isis(begin, isis)
+    net.push_noise(bg.NormStream(p.seed).take(c["N"] * steps + 64))
+    for t in range(1, steps + 1):
+        o.step_n(1)
+        net.step(1)
+        if t % 50 == 0:
+            compare_neurons(net, o, "step %d" % t)
+            compare_input(net, o, "step %d" % t)
+    compare_synapses(net, o, "end")
+    assert net.error_word == 0
+    net.close()
+    o.close()
