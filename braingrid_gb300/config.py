@@ -128,6 +128,14 @@ class MTRand:
         x = self.randint(n).astype(f32).astype(np.float64) * (1.0 / 4294967295.0)
         return x.astype(f32)
 
+    def rand1(self):
+        """One rand() as a float32 scalar (for sequential draws)."""
+        if self._pos == 624:
+            self._reload()
+        x = int(self._out[self._pos])
+        self._pos += 1
+        return f32(float(f32(x)) * (1.0 / 4294967295.0))
+
     def in_range(self, lo, hi, n=None):
         """inRange with scalar or per-draw bounds; n defaults to the bounds' length."""
         lo, hi = np.asarray(lo, f32), np.asarray(hi, f32)
@@ -140,15 +148,25 @@ class MTRand:
 _libm = None
 
 
-def expf(x):
-    """The C library's expf, which the reference's exp(float) calls (values are tabled once, so
-    the host library, not numpy's own exp, decides the last bit)."""
+def _m():
     global _libm
     if _libm is None:
         _libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
-        _libm.expf.restype = ctypes.c_float
-        _libm.expf.argtypes = [ctypes.c_float]
-    return f32(_libm.expf(float(f32(x))))
+        for fn in ("expf", "logf"):
+            getattr(_libm, fn).restype = ctypes.c_float
+            getattr(_libm, fn).argtypes = [ctypes.c_float]
+    return _libm
+
+
+def expf(x):
+    """The C library's expf, which the reference's exp(float) calls (the host library, not
+    numpy's own exp, decides the last bit)."""
+    return f32(_m().expf(float(f32(x))))
+
+
+def logf(x):
+    """The C library's logf (the reference's log(float))."""
+    return f32(_m().logf(float(f32(x))))
 
 
 # ---- parameters --------------------------------------------------------------------------------
@@ -471,7 +489,38 @@ def setup(p):
         _connect_static(p, rng, out)
     if stim is not None and stim["kind"] == "poisson":
         out["poisson"] = _poisson_input(p, out)
+    out["rng"] = rng                 # the global generator as setup leaves it
     return out
+
+
+def poisson_intervals(a, nsteps):
+    """The Poisson stimulus's interval draws for steps [0, nsteps) as the reference makes them
+    on the global generator after setup (HostSInputPoisson::inputStimulus, Inputs/
+    HostSInputPoisson.cpp:60-94): every step, neurons ascending, each masked neuron whose
+    counter runs out draws isi = -lambda log U ms until a second draw U' > exp(-isi^2 / 32) keeps
+    it, and waits (int)(isi / 1000 / deltaT + 0.5) steps.  The draws depend on the masks and
+    the counters only, so they are made ahead, event by event.  Returns (begin[N + 1], steps)
+    for bg3_push_poisson_isis (neuron i's intervals in steps[begin[i]:begin[i + 1]]); advances
+    a["rng"]."""
+    import heapq
+    pa = a["poisson"]["arrays"]
+    lam, rng, N = f32(a["poisson"]["lam"]), a["rng"], a["N"]
+    mlam = f32(-lam)
+    heap = [(max(int(c), 1) - 1, i) for i, c in enumerate(pa["nISIs"]) if pa["masks"][i]]
+    heapq.heapify(heap)
+    seqs = [[] for _ in range(N)]
+    while heap and heap[0][0] < nsteps:
+        t, i = heapq.heappop(heap)
+        isi = f32(mlam * logf(rng.rand1()))
+        while rng.rand1() <= expf(-(isi * isi) / f32(32)):
+            isi = f32(mlam * logf(rng.rand1()))
+        v = int(float((isi / f32(1000)) / DELTA_T) + 0.5)
+        seqs[i].append(v)
+        heapq.heappush(heap, (t + max(v, 1), i))
+    begin = np.zeros(N + 1, np.int32)
+    begin[1:] = np.cumsum([len(q) for q in seqs])
+    steps = np.array([v for q in seqs for v in q], np.int32)
+    return begin, steps
 
 
 def _create_neurons(p, rng, out):

@@ -8,8 +8,8 @@ runs numSims epochs of Tsim seconds with the epoch pass at each end (ConnGrowth'
 recorder, or the plain recorder), and writes the reference's result file (braingrid_gb300.
 results) to -o, or to the file's stateOutputFileName.  With the reference's noise stream (the
 default) the result file is the reference's, byte for byte, wherever the run is bit-exact (see
-the parity tests); --noise device draws the noise on the GPU instead.  A Poisson stimulus draws
-its intervals on the GPU in either mode.
+the parity tests): the noise and a Poisson stimulus's intervals are the reference's own draws,
+made on the host.  --noise device draws both on the GPU instead.
 """
 import argparse
 import json
@@ -33,6 +33,9 @@ def simulate(p, noise="reference", arrays=None, max_chunk_values=1 << 24):
     try:
         N, spe = a["N"], p.steps_per_epoch
         gen = bg.NormStream(p.seed) if inject else None
+        if inject and "poisson" in a:
+            # the reference's own intervals, drawn ahead on its global generator
+            net.push_poisson_isis(*cf.poisson_intervals(a, spe * p.epochs + 1))
         chunk = max(1, min(spe, max_chunk_values // max(N, 1)))
         growth = p.conn_class == "ConnGrowth"
         t0 = time.perf_counter()

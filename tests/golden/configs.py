@@ -293,9 +293,10 @@ TEST_SMALL = dict(name="ref_small", width=10, height=10, N=100, tsim=100.0, epoc
 # Whole runs whose result file (Recorders/XmlGrowthRecorder.cpp:104-153) the compiled reference's
 # own driver wrote from the same parameter files: tests/golden/outputs.npz.  Every one keeps its
 # start radii below the grid spacing, so no synapse forms and a GPU run stays bit-exact.
-# (No DynamicLayout run: the reference refuses every DynamicLayout file, its
-# DynamicLayout::readParameters returning false after reading frac_EXC,
-# Layouts/DynamicLayout.cpp:60-78.)
+# No DynamicLayout run: the reference refuses every DynamicLayout file, its
+# DynamicLayout::readParameters returning false after reading frac_EXC
+# (Layouts/DynamicLayout.cpp:60-78).  No Poisson run: the driver indexes its one-slot input
+# synapse object by maxSynapsesPerNeuron * neuron (Inputs/HostSInputPoisson.cpp:77) and faults.
 OUTPUT_CASES = ("ref_tiny", "ref_small", "c0", "c0_regular")
 
 

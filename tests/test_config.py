@@ -288,3 +288,21 @@ def test_result_file_format():
     assert results.complete_xml("m", np.array([[1, 2], [0.25, 0.1]], np.float32)) == \
         '<Matrix name="m" type="complete" rows="2" columns="2" multiplier="1.0">\n' \
         '   1 2 \n0.25 0.1 \n\n</Matrix>'
+
+
+@pytest.mark.parametrize("name", ["c0_poisson", "c0_poisson25", "izh_dstdp", "izh_static"])
+def test_poisson_intervals_match_the_oracle(name, tmp_path):
+    """The Poisson stimulus's intervals drawn ahead on the global generator after setup
+    (config.poisson_intervals) equal the oracle's, which replays HostSInputPoisson step by step
+    and is pinned to the reference harness's input state."""
+    from tests.netcases import steps_per_epoch
+    c = case(name)
+    p = read_case(c, tmp_path)
+    a = cf.setup(p)
+    n = steps_per_epoch(c) * c["epochs"] + 2
+    begin, steps = cf.poisson_intervals(a, n)
+    o = oracle_from_case(c)
+    ob, ov = o.poisson_isi_draws(n)
+    assert_same("begin", begin, ob)
+    assert_same("intervals", steps, ov)
+    o.close()

@@ -4,7 +4,8 @@
 (bg3_norm_*), writes the reference driver's result file byte for byte (tests/golden/outputs.npz,
 written by the compiled reference from the same files).  (2) A ConnStatic + dynamic STDP +
 Poisson network built by config.network runs in lock step with the oracle holding the same
-wiring (config's neighbour order), bit for bit."""
+wiring (config's neighbour order), bit for bit.  (3) With a Poisson stimulus (which the
+reference's driver cannot run) the run from the parameter files gives the oracle's result file."""
 import numpy as np
 import pytest
 
@@ -36,6 +37,20 @@ def test_run_from_parameter_file_writes_reference_result(name, tmp_path):
         bad = [i for i, (a, b) in enumerate(zip(got_l, want_l)) if a != b]
         raise AssertionError("%s: %d lines differ, first %r" % (
             name, len(bad), [(got_l[i][:120], want_l[i][:120]) for i in bad[:2]]))
+
+
+@pytest.mark.parametrize("name", ["c0_poisson25"])
+def test_run_with_poisson_stimulus_matches_oracle_result(name, tmp_path):
+    """A Poisson stimulus (the reference's driver faults on one, so the oracle, pinned to the
+    reference harness, writes the expected result file): the run from the parameter files with
+    the reference's noise and interval draws gives the oracle's result file byte for byte."""
+    from tests.test_config import oracle_output
+    c, text, stim = configs.output_case(name)
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    p = cf.read(text, stim, root=str(tmp_path))
+    r = sim.simulate(p, noise="reference")
+    assert r["error_word"] == 0
+    assert r["text"] == oracle_output(name)
 
 
 def test_cli_writes_result_file(tmp_path):
@@ -87,7 +102,8 @@ def test_static_stdp_poisson_network_from_parameter_file(tmp_path):
     o.rng_skip(len(slots))
     spe = steps_per_epoch(c)
     steps = spe
-    begin, isis = o.poisson_isi_draws(steps + 2)
+    # the product's own interval draws (equal to the oracle's, test_config)
+    begin, isis = cf.poisson_intervals(a, steps + 2)
     net.push_poisson_isis(begin, isis)
     net.push_noise(bg.NormStream(p.seed).take(c["N"] * steps + 64))
     for t in range(1, steps + 1):
