@@ -725,45 +725,57 @@ def _poisson_input(p, out):
 
 
 # ---- the network on the device -----------------------------------------------------------------
+def desc(p, noise_mode=bg.BG3_NOISE_DEVICE):
+    """The network shape (bg3_net_desc) of p; the noise keyed by the file's seed."""
+    if p.max_syn <= 0:
+        raise ConfigError("maxSynapsesPerNeuron must be positive")
+    return bg.NetDesc(p.n_neurons, p.max_syn, p.width, p.height, float(p.tsim), float(DELTA_T),
+                      p.max_firing_rate, max(p.epochs, 1), p.neuron_kind, p.synapse_kind,
+                      noise_mode, p.seed)
+
+
 def network(p, arrays=None, noise_mode=bg.BG3_NOISE_DEVICE, poisson_seed=None):
     """A bg3 network holding what setup(p) built: layout, neurons, synapses (ConnStatic), the
     ConnGrowth parameters, STDP constants and the stimulus.  Noise is keyed by the file's seed;
     with BG3_NOISE_INJECT push the reference's stream (NormStream(p.seed)) before stepping.
-    Poisson intervals are drawn on the device keyed by poisson_seed (default the file's seed)."""
+    Poisson intervals are drawn on the device keyed by poisson_seed (default the file's seed),
+    or pushed (poisson_intervals)."""
     a = arrays if arrays is not None else setup(p)
-    N = a["N"]
-    if p.max_syn <= 0:
-        raise ConfigError("maxSynapsesPerNeuron must be positive")
-    net = bg.Network(N, p.max_syn, p.width, p.height, float(p.tsim), float(DELTA_T),
-                     p.max_firing_rate, max(p.epochs, 1), p.synapse_kind, noise_mode, p.seed,
-                     neuron_kind=p.neuron_kind)
+    net = bg.Network.from_desc(desc(p, noise_mode))
     try:
-        net.upload_layout(a["xloc"], a["yloc"], a["ntype"])
-        net.upload_lif(Vm=a["Vm"], Vthresh=a["Vthresh"], Vreset=a["Vreset"], I0=a["I0"],
-                       Inoise=a["Inoise"], C1=a["C1"], C2=a["C2"], Trefract=a["Trefract"])
-        if p.neuron_kind == bg.BG3_NEURON_IZH:
-            net.upload_izh(**{k: a[k] for k in ("Aconst", "Bconst", "Cconst", "Dconst", "u", "C3")})
-        if "synapses" in a:
-            net.upload_synapses(0, counts=a["counts"], **a["synapses"])
-        if p.synapse_kind >= bg.BG3_SYN_STDP:
-            consts = stdp_constants(p)
-            net.set_stdp_constants(**consts)
-            if "synapses" in a:
-                s = a["synapses"]
-                net.upload_stdp(s["in_use"], s["type"], s["delayIdx"], **stdp_arrays(s, consts))
-        g = p.growth if p.conn_class == "ConnGrowth" else dict(
-            epsilon=0.6, beta=0.1, rho=1e-4, target_rate=1.0, min_radius=0.1, start_radius=0.4)
-        net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
-                          g["start_radius"], np.full(N, g["start_radius"], f32))
-        if "regular" in a:
-            r = a["regular"]
-            net.input_regular(r["values"], r["shifts"], r["n_steps_duration"],
-                              r["n_steps_cycle"], 0)
-        if "poisson" in a:
-            net.input_poisson(a["poisson"]["lam"],
-                              seed=p.seed if poisson_seed is None else poisson_seed, step=0,
-                              **a["poisson"]["arrays"])
+        configure(net, p, a, poisson_seed)
     except Exception:
         net.close()
         raise
     return net
+
+
+def configure(net, p, a, poisson_seed=None):
+    """Uploads setup(p)'s arrays a into a created network of p's shape (the served form's setup
+    callback calls this on the network the server made)."""
+    N = a["N"]
+    net.upload_layout(a["xloc"], a["yloc"], a["ntype"])
+    net.upload_lif(Vm=a["Vm"], Vthresh=a["Vthresh"], Vreset=a["Vreset"], I0=a["I0"],
+                   Inoise=a["Inoise"], C1=a["C1"], C2=a["C2"], Trefract=a["Trefract"])
+    if p.neuron_kind == bg.BG3_NEURON_IZH:
+        net.upload_izh(**{k: a[k] for k in ("Aconst", "Bconst", "Cconst", "Dconst", "u", "C3")})
+    if "synapses" in a:
+        net.upload_synapses(0, counts=a["counts"], **a["synapses"])
+    if p.synapse_kind >= bg.BG3_SYN_STDP:
+        consts = stdp_constants(p)
+        net.set_stdp_constants(**consts)
+        if "synapses" in a:
+            s = a["synapses"]
+            net.upload_stdp(s["in_use"], s["type"], s["delayIdx"], **stdp_arrays(s, consts))
+    g = p.growth if p.conn_class == "ConnGrowth" else dict(
+        epsilon=0.6, beta=0.1, rho=1e-4, target_rate=1.0, min_radius=0.1, start_radius=0.4)
+    net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
+                      g["start_radius"], np.full(N, g["start_radius"], f32))
+    if "regular" in a:
+        r = a["regular"]
+        net.input_regular(r["values"], r["shifts"], r["n_steps_duration"],
+                          r["n_steps_cycle"], 0)
+    if "poisson" in a:
+        net.input_poisson(a["poisson"]["lam"],
+                          seed=p.seed if poisson_seed is None else poisson_seed, step=0,
+                          **a["poisson"]["arrays"])

@@ -259,6 +259,22 @@ def lif_growth_job(side, epochs, seed, radius=None, weight_scale=0.003, target_r
     return Job(desc, epochs, True, setup, name or "lif%dx%d" % (side, side), **job_kw)
 
 
+def config_job(config, stim=None, root=None, epochs=None, name="", **job_kw):
+    """A job from a BrainGrid parameter file (and stimulus file): the network the reference's
+    setup makes from it (braingrid_gb300.config), its numSims epochs (or epochs) of Tsim seconds,
+    growth at each epoch end for ConnGrowth, the plain recorder otherwise; device noise keyed by
+    the file's seed.  config may also be an already read config.Params."""
+    from . import config as cf
+    p = config if isinstance(config, cf.Params) else cf.read(config, stim, root)
+    a = cf.setup(p)
+    desc = cf.desc(p)
+
+    def setup(net):
+        cf.configure(net, p, a)
+    return Job(desc, epochs or p.epochs, p.conn_class == "ConnGrowth", setup,
+               name or "config%dx%d" % (p.width, p.height), **job_kw)
+
+
 def izh_static_job(width, height, epochs, seed, epoch_duration=1.0, max_epochs=None, name="",
                    **job_kw):
     """The Izhikevich + STDP family: Izhikevich neurons, static wiring (10 nearest within radius 5,

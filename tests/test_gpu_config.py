@@ -116,3 +116,40 @@ def test_static_stdp_poisson_network_from_parameter_file(tmp_path):
     assert net.error_word == 0
     net.close()
     o.close()
+
+
+def test_parameter_file_job_served_like_a_plain_network(tmp_path):
+    """serve.config_job: a parameter file submitted to the job server (device noise) gives the
+    histories of the same file run as a plain network."""
+    from braingrid_gb300 import serve
+    jobs = []
+    for name in ("c0_regular", "izh_static"):
+        c = configs.case(name)
+        configs.write_case(c, str(tmp_path / "configfiles"), stdp_params=True)
+        base = str(tmp_path / "configfiles" / "bg3" / name)
+        stim = base + "-stim.xml" if c.get("stim") else None
+        jobs.append((cf.read(base + ".xml", stim, root=str(tmp_path)), name))
+    srv = serve.Server(max_resident=2, chunk_steps=400)
+    served = [serve.config_job(p, name=name) for p, name in jobs]
+    for j in served:
+        srv.submit(j)
+    done = srv.run_all()
+    srv.close()
+    assert len(done) == 2
+    for (p, name), job in zip(jobs, served):
+        assert job.result.status == 0 and job.result.error_word == 0, (name, job.error)
+        net = cf.network(p)
+        for e in range(p.epochs):
+            net.step(p.steps_per_epoch)
+            if p.conn_class == "ConnGrowth":
+                net.growth(e + 1)
+            else:
+                net.record()
+        b, s_, rh, ra = net.download_histories()
+        plain = dict(burstiness=b, spikes_hist=s_, rates_hist=rh, radii_hist=ra,
+                     Vm=net.download_lif(fields=("Vm",))["Vm"])
+        out = job.outputs()
+        for k in plain:
+            assert_same("%s served vs plain %s" % (name, k), out[k][:len(plain[k])], plain[k])
+        assert net.error_word == 0
+        net.close()
