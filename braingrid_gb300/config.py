@@ -40,6 +40,7 @@ count per source, the distances kept, and the weights, drawn one per synapse in 
 import ctypes
 import ctypes.util
 import os
+import re
 import xml.etree.ElementTree as ET
 from dataclasses import dataclass, field
 
@@ -254,8 +255,22 @@ def _value_list(text):
     return [_atoi(t) for t in (text or "").split()]
 
 
+def _parse(source):
+    """The root element of an XML file or text.  The XML declaration is dropped first: the
+    reference's files are read by TinyXML, which accepts declarations such as
+    standalone=no that a strict parser refuses."""
+    if not source.lstrip().startswith("<"):
+        with open(source, encoding="utf-8", errors="replace") as f:
+            source = f.read()
+    source = re.sub(r"^\s*<\?xml[^>]*\?>", "", source, count=1)
+    try:
+        return ET.fromstring(source)
+    except ET.ParseError as e:
+        raise ConfigError("malformed XML: %s" % e)
+
+
 def _read_list_file(path, root_tag):
-    doc = ET.parse(path).getroot()
+    doc = _parse(path)
     if doc.tag != root_tag:
         raise ConfigError("could not find <%s> in %s" % (root_tag, path))
     return _value_list(doc.text)
@@ -271,7 +286,7 @@ def read(config, stim=None, root=None):
     def path(p):
         return p if os.path.isabs(p) else os.path.join(root, p)
 
-    doc = ET.fromstring(config) if config.lstrip().startswith("<") else ET.parse(config).getroot()
+    doc = _parse(config)
     p = Params()
     si = doc.find("SimInfoParams")
     if si is None:
@@ -386,7 +401,7 @@ def _read_layout(p, sec, path):
 
 
 def _read_stim(stim, path, p):
-    doc = ET.fromstring(stim) if stim.lstrip().startswith("<") else ET.parse(stim).getroot()
+    doc = _parse(stim)
     if doc.tag != "InputParams":
         raise ConfigError("missing InputParams")
     m = doc.find("IMethod")

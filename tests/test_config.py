@@ -306,3 +306,16 @@ def test_poisson_intervals_match_the_oracle(name, tmp_path):
     assert_same("begin", begin, ob)
     assert_same("intervals", steps, ov)
     o.close()
+
+
+def test_tinyxml_style_declarations_are_read(tmp_path):
+    """The reference's stimulus files declare standalone=no without quotes (TinyXML takes it);
+    they read here too."""
+    c = case("c0_regular")
+    text = configs.stim_xml(c["stim"]).replace('<?xml version="1.0" standalone="no"?>',
+                                               '<?xml version="1.0" standalone=no?>')
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    p = cf.read(configs.config_text(c), text, root=str(tmp_path))
+    assert p.stim["kind"] == "regular" and p.stim["sync"] == "no"
+    with pytest.raises(cf.ConfigError):
+        cf.read(configs.config_text(c).replace("</BGSimParams>", ""), root=str(tmp_path))
