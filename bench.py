@@ -498,6 +498,10 @@ def run_growth():
                 "radius_0.4_fp32_frac": 8 * N * N / t_reject / fp32_peak,
                 "grown_create_s": t_create, "grown_update_s": t_update,
                 "grown_pairs_per_s": N * N / t_update, "synapses": S,
+                # every overlapping pair (one per synapse here: no radius contains another)
+                # evaluates the lens area with 2 acos and 2 sin
+                "grown_transcendental_calls": 4 * S,
+                "grown_transcendentals_per_s": 4 * S / t_update,
                 "grown_bound": "fp64 (acos and sin of the overlap area evaluated in double; "
                                "86 % FP64-pipe busy, profiles/k_growth_plain.md)",
                 "error_word": net.error_word})

@@ -551,8 +551,8 @@ def _create_neurons(p, rng, out):
     u = rng.rand(int(per.sum()))
 
     def draw(off, lo, hi):
-        v = u[first + off]
-        return (v * (f32(hi) - f32(lo)) if np.ndim(lo) == 0 else v * (hi - lo)).astype(f32) + lo
+        """inRange(lo, hi) with each neuron's draw number off: v * (hi - lo) + lo in float."""
+        return (u[first + off] * (f32(hi) - f32(lo))).astype(f32) + f32(lo)
 
     r = p.if_ranges
     Iinject = draw(0, *r["Iinject"])
