@@ -751,6 +751,28 @@ int bg3_scale_weights(bg3_net *n, float factor)
     return BG3_OK;
 }
 
+int bg3_set_noise_mode(bg3_net *n, int32_t mode, uint32_t seed)
+{
+    if (!n || (mode != BG3_NOISE_DEVICE && mode != BG3_NOISE_INJECT)) return BG3_EINVAL;
+    CK(cudaStreamSynchronize(n->stream));
+    // an injected stream starts empty: values pushed for the old mode are dropped
+    if (n->noise_dev) CK(cudaFree(n->noise_dev));
+    n->noise_dev = nullptr;
+    n->noise_cap = 0;
+    n->h.noise_buf = nullptr;
+    n->h.noise_len = 0;
+    unsigned long long zero = 0;
+    CK(cudaMemcpyAsync(n->h.noise_cursor, &zero, sizeof(zero), cudaMemcpyHostToDevice, n->stream));
+    n->h.noise_mode = mode;
+    n->h.noise_seed = seed;
+    n->desc.noise_mode = mode;
+    n->desc.noise_seed = seed;
+    int rc = push_desc(n);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(n->stream));
+    return BG3_OK;
+}
+
 int bg3_push_noise(bg3_net *n, const float *v, int64_t cnt)
 {
     if (!n || (!v && cnt) || cnt < 0 || n->h.noise_mode != BG3_NOISE_INJECT) return BG3_EINVAL;

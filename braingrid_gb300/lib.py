@@ -178,6 +178,7 @@ def load(build_if_missing=True):
         "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
         "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
         "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
+        "bg3_set_noise_mode": ([vp, ctypes.c_int32, ctypes.c_uint32], ctypes.c_int),
         "bg3_norm_create": ([ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.POINTER(vp)],
                             ctypes.c_int),
         "bg3_norm_fill": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
@@ -475,6 +476,11 @@ class Network:
     def scale_weights(self, factor):
         """W *= factor for every in-use synapse, on the device (bg3_scale_weights)."""
         check(self.L.bg3_scale_weights(self.h, float(factor)), "bg3_scale_weights")
+
+    def set_noise_mode(self, mode, seed):
+        check(self.L.bg3_set_noise_mode(self.h, int(mode), int(seed) & 0xFFFFFFFF),
+              "bg3_set_noise_mode")
+        self.desc.noise_mode, self.desc.noise_seed = int(mode), int(seed) & 0xFFFFFFFF
 
     def push_noise(self, values):
         v = np.ascontiguousarray(values, np.float32)

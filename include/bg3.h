@@ -200,6 +200,11 @@ int bg3_upload_weights(bg3_net *net, const float *W);
  * float, the same bits as a host loop over the downloaded weights).  No counterpart in the
  * reference: it builds benchmark networks from grown ones without moving the synapse arrays. */
 int bg3_scale_weights(bg3_net *net, float factor);
+/* Switches the noise source between steps (BG3_NOISE_DEVICE keyed by seed, or BG3_NOISE_INJECT
+ * starting from an empty stream), as the reference's model chooses its generator at setup
+ * (initMTGPU / normalMTGPU, Core/GPUSpikingModel.h:220-223).  Not for a network inside a batch
+ * (batches run device noise). */
+int bg3_set_noise_mode(bg3_net *net, int32_t mode, uint32_t seed);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
 
