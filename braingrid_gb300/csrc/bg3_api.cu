@@ -1345,6 +1345,22 @@ int bg3_download_growth(bg3_net *n, float *radii, float *rates)
     return BG3_OK;
 }
 
+int bg3_download_state(bg3_net *n, const bg3_state_view *v)
+{
+    if (!n || !v || (!v->radii != !v->rates)) return BG3_EINVAL;
+    if ((v->izh && n->h.neuron_kind != BG3_NEURON_IZH) ||
+        (v->stdp && n->h.syn_kind < BG3_SYN_STDP))
+        return BG3_EINVAL;
+    int rc = BG3_OK;
+    if (v->neurons && (rc = bg3_download_lif(n, v->neurons))) return rc;
+    if (v->izh && (rc = bg3_download_izh(n, v->izh))) return rc;
+    if (v->synapses && (rc = bg3_download_synapses(n, v->synapses))) return rc;
+    if (v->stdp && (rc = bg3_download_stdp(n, v->stdp))) return rc;
+    if (v->maps && (rc = bg3_download_maps(n, v->maps))) return rc;
+    if (v->radii && (rc = bg3_download_growth(n, v->radii, v->rates))) return rc;
+    return BG3_OK;
+}
+
 int bg3_download_histories(bg3_net *n, float *burst, float *spikes, float *rh, float *radh)
 {
     if (!n) return BG3_EINVAL;

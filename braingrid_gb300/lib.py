@@ -114,6 +114,12 @@ class IndexMaps(ctypes.Structure):
                                       "incomingSynapseBegin", "incomingSynapseCount")]
 
 
+class StateView(ctypes.Structure):
+    _fields_ = [("neurons", ctypes.POINTER(LifArrays)), ("izh", ctypes.POINTER(IzhArrays)),
+                ("synapses", ctypes.POINTER(SynArrays)), ("stdp", ctypes.POINTER(StdpArrays)),
+                ("maps", ctypes.POINTER(IndexMaps)), ("radii", c_f32p), ("rates", c_f32p)]
+
+
 _LIB = None
 
 
@@ -201,6 +207,7 @@ def load(build_if_missing=True):
         "bg3_total_synapses": ([vp], ctypes.c_int64),
         "bg3_download_maps": ([vp, ctypes.POINTER(IndexMaps)], ctypes.c_int),
         "bg3_download_growth": ([vp, c_f32p, c_f32p], ctypes.c_int),
+        "bg3_download_state": ([vp, ctypes.POINTER(StateView)], ctypes.c_int),
         "bg3_download_histories": ([vp, c_f32p, c_f32p, c_f32p, c_f32p], ctypes.c_int),
         "bg3_status_string": ([ctypes.c_int], ctypes.c_char_p),
         "bg3_enable_timing": ([vp, ctypes.c_int], ctypes.c_int),
@@ -619,6 +626,41 @@ class Network:
         for k in out:
             if k.endswith("IndexMap"):
                 out[k] = out[k][:T]
+        return out
+
+    def download_state(self, izh=False, stdp=False):
+        """Everything bg3_download_state returns, in one call: dict with 'neurons', 'synapses',
+        'maps', 'radii', 'rates' (and 'izh', 'stdp' when asked)."""
+        S, T = self.N * self.max_syn, self.total_synapses()
+        out = {"neurons": {k: np.zeros(self.N, dt) for k, dt in LIF_FIELDS},
+               "synapses": {k: np.zeros(S, dt) for k, dt in SYN_FIELDS},
+               "maps": {k: np.zeros(max(T, 1) if k.endswith("IndexMap") else self.N, np.uint32)
+                        for k, _ in IndexMaps._fields_},
+               "radii": np.zeros(self.N, np.float32), "rates": np.zeros(self.N, np.float32)}
+        out["neurons"]["history"] = np.zeros(self.N * self.max_spikes, np.uint64)
+        out["synapses"]["counts"] = np.zeros(self.N, np.uint32)
+        la = LifArrays(*[_p(out["neurons"][k]) for k, _ in LIF_FIELDS] +
+                       [_p(out["neurons"]["history"])])
+        sa = SynArrays()
+        for k in out["synapses"]:
+            setattr(sa, k, _p(out["synapses"][k]))
+        ma = IndexMaps(*[_p(out["maps"][k]) for k, _ in IndexMaps._fields_])
+        v = StateView(ctypes.pointer(la), None, ctypes.pointer(sa), None, ctypes.pointer(ma),
+                      _p(out["radii"]), _p(out["rates"]))
+        if izh:
+            out["izh"] = {k: np.zeros(self.N, np.float32) for k in IZH_FIELDS}
+            ia = IzhArrays(*[_p(out["izh"][k]) for k in IZH_FIELDS])
+            v.izh = ctypes.pointer(ia)
+        if stdp:
+            out["stdp"] = {k: np.zeros(S, dt) for k, dt in STDP_FIELDS}
+            st = StdpArrays()
+            for k, _ in STDP_FIELDS:
+                setattr(st, k, _p(out["stdp"][k]))
+            v.stdp = ctypes.pointer(st)
+        check(self.L.bg3_download_state(self.h, ctypes.byref(v)), "bg3_download_state")
+        for k in out["maps"]:
+            if k.endswith("IndexMap"):
+                out["maps"][k] = out["maps"][k][:T]
         return out
 
     def download_growth(self):

@@ -289,6 +289,18 @@ int bg3_download_growth(bg3_net *net, float *radii, float *rates);
  * rates and radii ((max_epochs+1) x n_neurons). */
 int bg3_download_histories(bg3_net *net, float *burstiness, float *spikes, float *rates_hist,
                            float *radii_hist);
+/* The whole observable state in one call (what the reference's model copies back at the end of
+ * a run, Core/GPUSpikingModel.cu:82-99, and its recorders read): each non-NULL member is filled
+ * as the single-purpose download above fills it; NULL members are skipped. */
+typedef struct {
+    bg3_lif_arrays *neurons;          /* Vm, spike counts, refractory counters, spike history */
+    bg3_izh_arrays *izh;              /* BG3_NEURON_IZH only                                  */
+    bg3_synapse_arrays *synapses;     /* slot arrays incl. delay queues, counts               */
+    bg3_stdp_arrays *stdp;            /* BG3_SYN_STDP / BG3_SYN_DYNSTDP only                  */
+    bg3_index_maps *maps;             /* incoming / outgoing index maps                       */
+    float *radii, *rates;             /* ConnGrowth state, n_neurons each (both or neither)   */
+} bg3_state_view;
+int bg3_download_state(bg3_net *net, const bg3_state_view *view);
 
 /* ---- allocation-free variant -------------------------------------------------------------- */
 /* No counterpart in the reference: an extra entry point for callers that cannot allocate device
