@@ -957,17 +957,35 @@ int bg3_download_poisson(bg3_net *n, bg3_poisson_arrays *a)
 // Device-noise mode: neurons(t0), then per step deliver + sweep whose epilogue integrates the
 // next step's neurons, the last sweep without that epilogue.  Runs of interior steps replay a
 // CUDA graph of GRAPH_STEPS (deliver, fused sweep) pairs.  Injected-noise mode: neurons,
-// deliver, sweep for every step.
+// deliver, sweep for every step, GRAPH_STEPS of them per graph replay.
 static int run_steps(bg3_net *n, int64_t nsteps)
 {
     if (nsteps <= 0) return BG3_OK;
     const NetDev &h = n->h;
     if (h.noise_mode == BG3_NOISE_INJECT) {
-        for (int64_t s = 0; s < nsteps; s++) {
+        // (neurons, deliver, sweep) per step; runs of GRAPH_STEPS steps replay a captured graph
+        // (the injected stream's cursor lives on the device, and a push or any other change of
+        // the descriptor drops the graph)
+        auto one = [&]() {
             bg3::launch_neurons(h, n->stream);
             bg3::launch_deliver(h, n->cfg, n->stream);
             bg3::launch_sweep(h, n->tm_psr, n->tm_cls, n->tm_psr16, n->tm_cls16, false, n->cfg, n->stream);
+        };
+        int64_t left = nsteps;
+        if (left >= GRAPH_STEPS && !n->graph) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+            for (int i = 0; i < GRAPH_STEPS; i++) one();
+            CK(cudaStreamEndCapture(n->stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&n->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { n->graph = nullptr; return BG3_ECUDA; }
         }
+        while (n->graph && left >= GRAPH_STEPS) {
+            CK(cudaGraphLaunch(n->graph, n->stream));
+            left -= GRAPH_STEPS;
+        }
+        for (; left > 0; left--) one();
         n->launches += (1 + step_kernels(h.syn_kind)) * nsteps;
         CK(cudaGetLastError());
         return BG3_OK;
