@@ -39,15 +39,19 @@ def simulate(p, noise="reference", arrays=None, max_chunk_values=1 << 24):
         chunk = max(1, min(spe, max_chunk_values // max(N, 1)))
         growth = p.conn_class == "ConnGrowth"
         t0 = time.perf_counter()
+        # the next chunk's noise is drawn on the host while the GPU runs the current chunk (the
+        # steps are queued asynchronously; the push waits for them); at most one value per
+        # neuron per step is consumed and what is left over stays queued for the next chunk
+        pending = gen.take(N * chunk) if inject else None
         for e in range(p.epochs):
             done = 0
             while done < spe:
                 k = min(chunk, spe - done)
                 if inject:
-                    # at most one value per neuron per step is consumed; what is left over
-                    # stays at the head of the device queue for the next chunk
-                    net.push_noise(gen.take(N * k))
+                    net.push_noise(pending)
                 net.step(k)
+                if inject:
+                    pending = gen.take(N * chunk)
                 done += k
             if growth:
                 net.growth(e + 1)
