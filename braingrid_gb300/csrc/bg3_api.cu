@@ -18,6 +18,7 @@
 
 namespace bg3 {
 void launch_neurons(const NetDev &h, cudaStream_t s);
+int neuron_launches(const NetDev &h);
 void launch_deliver(const NetDev &h, const LaunchCfg &c, cudaStream_t s);
 void launch_sweep(const NetDev &h, const CUtensorMap &tp, const CUtensorMap &tc,
                   const CUtensorMap &tp16, const CUtensorMap &tc16, bool fuse, const LaunchCfg &c,
@@ -986,7 +987,7 @@ static int run_steps(bg3_net *n, int64_t nsteps)
             left -= GRAPH_STEPS;
         }
         for (; left > 0; left--) one();
-        n->launches += (1 + step_kernels(h.syn_kind)) * nsteps;
+        n->launches += (bg3::neuron_launches(h) + step_kernels(h.syn_kind)) * nsteps;
         CK(cudaGetLastError());
         return BG3_OK;
     }

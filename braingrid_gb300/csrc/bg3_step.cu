@@ -141,6 +141,90 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__
     if (threadIdx.x == 0) *n.noise_cursor = cursor + (unsigned long long)s_running;
 }
 
+// Injected-noise mode for larger networks: the same stream positions from two passes over
+// 1024-neuron chunks taken from the top (chunk b holds neurons N-1-1024b down to N-1024(b+1)).
+// The count pass stores each chunk's number of integrating neurons, and the cursor at the start
+// of the step, in the map builder's scratch (outFill, unused between map builds); the apply
+// pass gives each neuron the integrating neurons of the chunks above it plus those above it in
+// its own chunk, and advances the cursor by the step's total.
+static const int INJ_CHUNK = 1024;
+
+__global__ void __launch_bounds__(1024) k_neurons_inject_count(const __grid_constant__ NetDev n)
+{
+    const int b = blockIdx.x;
+    const int i = n.N - 1 - b * INJ_CHUNK - (int)threadIdx.x;
+    bool integ = false;
+    if (i >= 0) {
+        NeuronIn x;
+        neuron_load(n, i, x);
+        integ = neuron_branch(x) == BR_INTEGRATE;
+    }
+    const int c = __syncthreads_count(integ);
+    if (threadIdx.x == 0) {
+        n.outFill[b] = (uint32_t)c;
+        if (b == 0) {
+            const unsigned long long cur = *n.noise_cursor;
+            n.outFill[gridDim.x] = (uint32_t)cur;
+            n.outFill[gridDim.x + 1] = (uint32_t)(cur >> 32);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_neurons_inject_apply(const __grid_constant__ NetDev n)
+{
+    __shared__ int warp_tot[32];
+    __shared__ long long s_above;
+    const int b = blockIdx.x, nb = gridDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long t = *n.step;
+    const unsigned long long cursor =
+        (unsigned long long)n.outFill[nb] | ((unsigned long long)n.outFill[nb + 1] << 32);
+    if (warp == 0) {
+        long long a = 0;
+        for (int k = lane; k < b; k += 32) a += n.outFill[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) s_above = a;
+    }
+    const int i = n.N - 1 - b * INJ_CHUNK - (int)threadIdx.x;
+    NeuronIn x;
+    if (i >= 0) neuron_load(n, i, x);
+    const int br = (i >= 0) ? neuron_branch(x) : BR_REFRACTORY;
+    const bool integ = (i >= 0) && br == BR_INTEGRATE;
+    const unsigned m = __ballot_sync(0xffffffffu, integ);
+    const int in_warp = __popc(m & ((1u << lane) - 1));
+    if (lane == 31) warp_tot[warp] = __popc(m);
+    __syncthreads();
+    if (warp == 0) {
+        const int v = warp_tot[lane];
+        int y = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += z;
+        }
+        warp_tot[lane] = y - v;  // exclusive prefix of warp totals
+    }
+    __syncthreads();
+    bool fired = false;
+    if (i >= 0) {
+        float noise = 0.0f;
+        if (integ) {
+            const long long pos = (long long)cursor + s_above + warp_tot[warp] + in_warp;
+            if (pos < n.noise_len) noise = n.noise_buf[pos];
+            else set_err(n, ERR_NOISE_EXHAUSTED);
+        }
+        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+        n.sp[i] = 0.0f;
+    }
+    ring_push(n, t, fired, i);
+    if (b == 0 && threadIdx.x == 0) {
+        long long tot = 0;
+        for (int k = 0; k < nb; k++) tot += n.outFill[k];
+        *n.noise_cursor = cursor + (unsigned long long)tot;
+    }
+}
+
 // ---- STDP ------------------------------------------------------------------------------------
 // AllSTDPSynapses::advanceSynapse / stdpLearning (Synapses/AllSTDPSynapses.cpp:283-472) and the
 // device form advanceSTDPSynapsesDevice (AllSynapsesDeviceFuncs_d.cu:100-380).  The only
@@ -925,9 +1009,15 @@ bool sweep_is_thin(const NetDev &h, const LaunchCfg &c) { return h.Mq <= c.thin_
 
 // ---- launchers -------------------------------------------------------------------------------
 
+int neuron_launches(const NetDev &h) { return (h.noise_mode == 1 && h.N > 2 * INJ_CHUNK) ? 2 : 1; }
+
 void launch_neurons(const NetDev &h, cudaStream_t s)
 {
-    if (h.noise_mode == 1)
+    if (h.noise_mode == 1 && h.N > 2 * INJ_CHUNK) {
+        const int nb = (h.N + INJ_CHUNK - 1) / INJ_CHUNK;
+        k_neurons_inject_count<<<nb, INJ_CHUNK, 0, s>>>(h);
+        k_neurons_inject_apply<<<nb, INJ_CHUNK, 0, s>>>(h);
+    } else if (h.noise_mode == 1)
         k_neurons_inject<<<1, 1024, 0, s>>>(h);
     else
         k_neurons_device<<<(h.N + 255) / 256, 256, 0, s>>>(h);

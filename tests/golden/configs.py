@@ -297,7 +297,14 @@ TEST_SMALL = dict(name="ref_small", width=10, height=10, N=100, tsim=100.0, epoc
 # DynamicLayout::readParameters returning false after reading frac_EXC
 # (Layouts/DynamicLayout.cpp:60-78).  No Poisson run: the driver indexes its one-slot input
 # synapse object by maxSynapsesPerNeuron * neuron (Inputs/HostSInputPoisson.cpp:77) and faults.
-OUTPUT_CASES = ("ref_tiny", "ref_small", "c0", "c0_regular")
+OUTPUT_CASES = ("ref_tiny", "ref_small", "c0", "c0_regular", "c100")
+
+# 100x100 LIF + DS + ConnGrowth, one epoch of 1 s at the stated start radius (10 % inhibitory, 1 %
+# starters on fixed strides): the injected-noise neuron pass of networks above 2,048 neurons
+C100 = dict(name="c100", width=100, height=100, N=10000, tsim=1.0, epochs=1, max_syn=100, seed=1,
+            max_firing_rate=200, inh=list(range(3, 10000, 10)), starters=list(range(7, 10000, 100)),
+            growth=dict(epsilon=0.60, beta=0.10, rho=1e-4, target_rate=1.0, min_radius=0.1,
+                        start_radius=0.4), radii=None)
 
 
 def dynamic_layout_text(text, frac_exc, frac_starter):
@@ -311,7 +318,7 @@ def dynamic_layout_text(text, frac_exc, frac_starter):
 
 def output_case(name):
     """(case, parameter-file text, stimulus text or None) of an OUTPUT_CASES entry."""
-    c = TEST_SMALL if name == "ref_small" else case(name)
+    c = {"ref_small": TEST_SMALL, "c100": C100}.get(name) or case(name)
     return c, config_text(c), (stim_xml(c["stim"]) if c.get("stim") else None)
 
 
