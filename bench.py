@@ -233,7 +233,9 @@ def run_bg3(args):
     e2e_s = time.perf_counter() - t0
     _, e2e_s = shard.reduce_timing(0, e2e_s, device="cuda")
     e2e = {"value": S * E2E_STEPS * e2e_iters * world / e2e_s, "unit": METRIC,
-           "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS}
+           "h2d_bytes_per_step": h2d / E2E_STEPS, "d2h_bytes_per_step": d2h / E2E_STEPS,
+           "l2": "not evicted between steps: consecutive steps of one run, whose per-step state "
+                 "(%.0f MB) fits the 129 MB L2" % (alg_bytes / 1e6)}
     err = net.error_word
     batched = izh_stdp = served = growth = None
     if world == 1:
