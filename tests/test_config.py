@@ -319,3 +319,12 @@ def test_tinyxml_style_declarations_are_read(tmp_path):
     assert p.stim["kind"] == "regular" and p.stim["sync"] == "no"
     with pytest.raises(cf.ConfigError):
         cf.read(configs.config_text(c).replace("</BGSimParams>", ""), root=str(tmp_path))
+
+
+def test_run_driver_imports_and_parses_arguments_without_a_gpu():
+    from braingrid_gb300 import sim
+    with pytest.raises(SystemExit) as e:
+        sim.main(["-h"])
+    assert e.value.code == 0
+    with pytest.raises(SystemExit):
+        sim.main(["-t", "x.xml", "--noise", "bogus"])
