@@ -113,6 +113,8 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
             a = pair_area(n.xloc[s], n.yloc[s], n.radii[s], xd, yd, rd);
             add = a > 0.0f;
         }
+        // most chunks add nothing (every pair beyond the radii): one barrier, no ordering
+        if (!__syncthreads_or(add)) continue;
         unsigned m = __ballot_sync(0xffffffffu, add);
         if (lane == 0) warp_cnt[warp] = __popc(m);
         __syncthreads();
