@@ -260,8 +260,11 @@ def _parse(source):
     reference's files are read by TinyXML, which accepts declarations such as
     standalone=no that a strict parser refuses."""
     if not source.lstrip().startswith("<"):
-        with open(source, encoding="utf-8", errors="replace") as f:
-            source = f.read()
+        try:
+            with open(source, encoding="utf-8", errors="replace") as f:
+                source = f.read()
+        except OSError as e:
+            raise ConfigError("cannot read %s: %s" % (source, e.strerror))
     source = re.sub(r"^\s*<\?xml[^>]*\?>", "", source, count=1)
     try:
         return ET.fromstring(source)

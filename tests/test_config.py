@@ -328,3 +328,33 @@ def test_run_driver_imports_and_parses_arguments_without_a_gpu():
     assert e.value.code == 0
     with pytest.raises(SystemExit):
         sim.main(["-t", "x.xml", "--noise", "bogus"])
+
+
+def test_missing_or_bad_neuron_lists_are_refused(tmp_path):
+    c = case("c0")
+    text = configs.config_text(c)
+    with pytest.raises(cf.ConfigError):            # the list files were never written
+        cf.read(text, root=str(tmp_path))
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    inh = tmp_path / "configfiles" / "bg3" / "c0-inh.xml"
+    inh.write_text('<?xml version="1.0"?>\n<I>3 100</I>\n')     # 100 is past the 10x10 grid
+    with pytest.raises(cf.ConfigError):
+        cf.read(text, root=str(tmp_path))
+    inh.write_text('<?xml version="1.0"?>\n<A>3</A>\n')         # wrong root element
+    with pytest.raises(cf.ConfigError):
+        cf.read(text, root=str(tmp_path))
+    inh.write_text('<?xml version="1.0"?>\n<I>3 17</I>\n')
+    p = cf.read(text, root=str(tmp_path))
+    a = cf.setup(p)
+    assert list(np.nonzero(a["ntype"] == cf.INH)[0]) == [3, 17]
+
+
+def test_poisson_mask_list_file(tmp_path):
+    c = case("c0_poisson")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    (tmp_path / "masks.xml").write_text('<?xml version="1.0"?>\n<M>0 5 9</M>\n')
+    stim = ('<?xml version="1.0" standalone=no?>\n<InputParams><IMethod name="SInputPoisson"/>'
+            '<IntParams fr_mean="10" weight="0.5"/><Masks><LayoutFiles '
+            'maskNListFileName="masks.xml"/></Masks></InputParams>')
+    p = cf.read(configs.config_text(c), stim, root=str(tmp_path))
+    assert list(np.nonzero(p.stim["masks"])[0]) == [0, 5, 9]
