@@ -1,12 +1,14 @@
 """A BrainGrid run from its parameter files on the GPU: the reference's growth driver
 (Core/BGDriver.cpp, Core/Simulator.cpp:140-190) with this library as the model.
 
-    python -m braingrid_gb300.sim -t config.xml [-s stim.xml] [-o result.xml] [--noise device]
+    python -m braingrid_gb300.sim -t config.xml [-s stim.xml] [-o result.xml] [-r state] [-w state]
+                                  [--noise device]
 
 reads the parameter file (braingrid_gb300.config), sets the network up as the reference does,
 runs numSims epochs of Tsim seconds with the epoch pass at each end (ConnGrowth's growth and
 recorder, or the plain recorder), and writes the reference's result file (braingrid_gb300.
-results) to -o, or to the file's stateOutputFileName.  With the reference's noise stream (the
+results) to -o, or to the file's stateOutputFileName; -r and -w read and write the reference's
+checkpoint stream as the driver's flags of those names do.  With the reference's noise stream (the
 default) the result file is the reference's, byte for byte, wherever the run is bit-exact (see
 the parity tests): the noise and a Poisson stimulus's intervals are the reference's own draws,
 made on the host.  --noise device draws both on the GPU instead.
@@ -24,14 +26,26 @@ from . import lib as bg
 from . import results
 
 
-def simulate(p, noise="reference", arrays=None, max_chunk_values=1 << 24):
+IF_SETUP = ("Cm", "Rm", "Vrest", "Vinit", "Iinject", "Tau")
+
+
+def simulate(p, noise="reference", arrays=None, restore=None, save=False,
+             max_chunk_values=1 << 24):
     """Runs p (config.Params); returns dict(text=result file, seconds=wall time of the epochs,
-    steps=simulation steps, error_word=the device error word)."""
+    steps=simulation steps, error_word=the device error word, stream=the reference's checkpoint
+    stream at the end when save).  restore: a checkpoint stream loaded after setup, as the
+    reference driver's -r does (Core/BGDriver.cpp:88-94: the model's state, then the recorder's
+    start values; the run then starts at step 0)."""
     a = arrays if arrays is not None else cf.setup(p)
     inject = noise == "reference"
     net = cf.network(p, a, noise_mode=bg.BG3_NOISE_INJECT if inject else bg.BG3_NOISE_DEVICE)
     try:
         N, spe = a["N"], p.steps_per_epoch
+        growth_conn = p.conn_class == "ConnGrowth"
+        if_fields = {k: a[k] for k in IF_SETUP}
+        if restore is not None:
+            extra = net.deserialize(restore, growth=growth_conn, step=0)
+            if_fields = {k: extra[k] for k in IF_SETUP}
         gen = bg.NormStream(p.seed) if inject else None
         if inject and "poisson" in a:
             # the reference's own intervals, drawn ahead on its global generator
@@ -66,7 +80,8 @@ def simulate(p, noise="reference", arrays=None, max_chunk_values=1 << 24):
                                  a["starter"], vthresh)
         if gen is not None:
             gen.close()
-        return dict(text=text, seconds=seconds, steps=net.sim_step, error_word=err)
+        stream = net.serialize(growth=growth_conn, **if_fields) if save else None
+        return dict(text=text, seconds=seconds, steps=net.sim_step, error_word=err, stream=stream)
     finally:
         net.close()
 
@@ -77,10 +92,21 @@ def main(argv=None):
     ap.add_argument("-s", "--stim", default=None, help="stimulus file")
     ap.add_argument("-o", "--output", default=None, help="result file (default: the "
                     "parameter file's stateOutputFileName)")
+    ap.add_argument("-r", "--read-state", default=None,
+                    help="checkpoint stream to start from (the reference driver's -r)")
+    ap.add_argument("-w", "--write-state", default=None,
+                    help="write the checkpoint stream at the end (the reference driver's -w)")
     ap.add_argument("--noise", choices=("reference", "device"), default="reference")
     a = ap.parse_args(argv)
     p = cf.read(a.config, a.stim)
-    r = simulate(p, a.noise)
+    restore = None
+    if a.read_state:
+        with open(a.read_state, "rb") as f:
+            restore = f.read()
+    r = simulate(p, a.noise, restore=restore, save=bool(a.write_state))
+    if a.write_state:
+        with open(a.write_state, "wb") as f:
+            f.write(r["stream"])
     out = a.output or p.output
     if out:
         d = os.path.dirname(out)

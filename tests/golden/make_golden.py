@@ -83,6 +83,21 @@ def run_outputs(growth, work, ref):
             want = open(os.path.join(ref, "old/validation/4-2016/growth/%s-out.xml" % gold),
                         "rb").read()
             assert res == want, "%s: the driver's result differs from its golden" % name
+    # the driver's -w and -r on c0: the end-of-run checkpoint stream, and a second run that
+    # starts from it (its result file and its own end-of-run stream)
+    res_dir = os.path.join(work, "results")
+    cfg = os.path.join(d, "out_c0.xml")
+    subprocess.check_call([growth, "-t", cfg, "-w", os.path.join(res_dir, "c0.ser")], cwd=work,
+                          stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    cfg2 = os.path.join(d, "out_c0_resumed.xml")
+    with open(cfg) as f, open(cfg2, "w") as g:
+        g.write(f.read().replace("results/out_c0.xml", "results/out_c0_resumed.xml"))
+    subprocess.check_call([growth, "-t", cfg2, "-r", os.path.join(res_dir, "c0.ser"), "-w",
+                           os.path.join(res_dir, "c0_resumed.ser")], cwd=work,
+                          stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    for key, fn in (("c0.ser", "c0.ser"), ("c0_resumed", "out_c0_resumed.xml"),
+                    ("c0_resumed.ser", "c0_resumed.ser")):
+        out[key] = np.frombuffer(open(os.path.join(res_dir, fn), "rb").read(), np.uint8)
     return out
 
 

@@ -358,3 +358,19 @@ def test_poisson_mask_list_file(tmp_path):
             'maskNListFileName="masks.xml"/></Masks></InputParams>')
     p = cf.read(configs.config_text(c), stim, root=str(tmp_path))
     assert list(np.nonzero(p.stim["masks"])[0]) == [0, 5, 9]
+
+
+def test_oracle_end_of_run_stream_matches_reference_driver():
+    """The driver's -w stream of the c0 run (tests/golden/outputs.npz) from the oracle's run,
+    Isyn tokens aside."""
+    from tests.netcases import steps_per_epoch
+    from tests.test_oracle_serialize import comparable
+    c, _, _ = configs.output_case("c0")
+    o = oracle_from_case(c)
+    for e in range(c["epochs"]):
+        o.step_n(steps_per_epoch(c))
+        o.growth()
+        o.record_epoch(e + 1)
+    want = np.load("tests/golden/outputs.npz")["c0.ser"].tobytes()
+    assert comparable(o.serialize(conn_growth=True), c) == comparable(want, c)
+    o.close()

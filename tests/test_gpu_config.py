@@ -153,3 +153,20 @@ def test_parameter_file_job_served_like_a_plain_network(tmp_path):
             assert_same("%s served vs plain %s" % (name, k), out[k][:len(plain[k])], plain[k])
         assert net.error_word == 0
         net.close()
+
+
+def test_driver_state_flags_match_reference(tmp_path):
+    """sim's -w and -r against the reference driver's: the end-of-run checkpoint stream of the
+    c0 run, and a second run started from that stream (its result file byte for byte, its own
+    end-of-run stream), every neuron's uninitialised Isyn token aside."""
+    from tests.test_oracle_serialize import comparable
+    out = np.load("tests/golden/outputs.npz")
+    c, text, stim = configs.output_case("c0")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    p = cf.read(text, stim, root=str(tmp_path))
+    r = sim.simulate(p, "reference", save=True)
+    assert comparable(r["stream"], c) == comparable(out["c0.ser"].tobytes(), c)
+    r2 = sim.simulate(p, "reference", restore=out["c0.ser"].tobytes(), save=True)
+    assert r2["error_word"] == 0
+    assert r2["text"] == out["c0_resumed"].tobytes().decode()
+    assert comparable(r2["stream"], c) == comparable(out["c0_resumed.ser"].tobytes(), c)
