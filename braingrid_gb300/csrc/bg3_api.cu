@@ -476,6 +476,18 @@ int64_t bg3_net_footprint(const bg3_net_desc *desc)
 
 uint64_t bg3_net_bytes(bg3_net *n) { return n ? n->bytes + sizeof(NetDev) : 0; }
 
+int bg3_set_device(int32_t device)
+{
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return BG3_ECUDA;
+    }
+    if (device < 0 || device >= count) return BG3_EINVAL;
+    CK(cudaSetDevice(device));
+    return BG3_OK;
+}
+
 int bg3_get_desc(bg3_net *n, bg3_net_desc *desc)
 {
     if (!n || !desc) return BG3_EINVAL;

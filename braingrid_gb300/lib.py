@@ -185,6 +185,7 @@ def load(build_if_missing=True):
         "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
         "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
         "bg3_set_noise_mode": ([vp, ctypes.c_int32, ctypes.c_uint32], ctypes.c_int),
+        "bg3_set_device": ([ctypes.c_int32], ctypes.c_int),
         "bg3_norm_create": ([ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.POINTER(vp)],
                             ctypes.c_int),
         "bg3_norm_fill": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
@@ -278,6 +279,11 @@ def footprint(desc):
     if v < 0:
         check(v, "bg3_net_footprint")
     return v
+
+
+def set_device(device):
+    """bg3_set_device: the CUDA device of the networks created afterwards on this thread."""
+    check(load().bg3_set_device(int(device)), "bg3_set_device")
 
 
 class NormStream:

@@ -2,7 +2,7 @@
 (Core/BGDriver.cpp, Core/Simulator.cpp:140-190) with this library as the model.
 
     python -m braingrid_gb300.sim -t config.xml [-s stim.xml] [-o result.xml] [-r state] [-w state]
-                                  [--noise device]
+                                  [-d device] [--noise device]
 
 reads the parameter file (braingrid_gb300.config), sets the network up as the reference does,
 runs numSims epochs of Tsim seconds with the epoch pass at each end (ConnGrowth's growth and
@@ -96,8 +96,11 @@ def main(argv=None):
                     help="checkpoint stream to start from (the reference driver's -r)")
     ap.add_argument("-w", "--write-state", default=None,
                     help="write the checkpoint stream at the end (the reference driver's -w)")
+    ap.add_argument("-d", "--deviceid", type=int, default=None, help="CUDA device id")
     ap.add_argument("--noise", choices=("reference", "device"), default="reference")
     a = ap.parse_args(argv)
+    if a.deviceid is not None:
+        bg.set_device(a.deviceid)
     p = cf.read(a.config, a.stim)
     restore = None
     if a.read_state:

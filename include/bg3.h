@@ -205,6 +205,9 @@ int bg3_scale_weights(bg3_net *net, float factor);
  * (initMTGPU / normalMTGPU, Core/GPUSpikingModel.h:220-223).  Not for a network inside a batch
  * (batches run device noise). */
 int bg3_set_noise_mode(bg3_net *net, int32_t mode, uint32_t seed);
+/* The CUDA device that networks created afterwards on this host thread use (the reference
+ * driver's -d, g_deviceId, Core/BGDriver.cpp:323-326); device 0 if never called. */
+int bg3_set_device(int32_t device);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
 

@@ -63,7 +63,9 @@ def test_cli_writes_result_file(tmp_path):
     cwd = os.getcwd()
     os.chdir(str(tmp_path))
     try:
-        assert sim.main(["-t", str(cfg), "-o", str(out)]) == 0
+        assert sim.main(["-t", str(cfg), "-o", str(out), "-d", "0"]) == 0
+        with pytest.raises(bg.Bg3Error):
+            bg.set_device(4096)
     finally:
         os.chdir(cwd)
     assert out.read_text() == np.load("tests/golden/outputs.npz")["ref_tiny"].tobytes().decode()
