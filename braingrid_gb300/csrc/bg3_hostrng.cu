@@ -13,9 +13,10 @@
 namespace {
 
 // MT19937 (Matsumoto and Nishimura 1998) with Knuth's seeding: the state is refilled 624 words
-// at a time and each word is tempered on the way out.
+// at a time, and the block's words are tempered and turned into uniforms in one loop.
 struct Mt {
     uint32_t s[624];
+    float u[624];
     int next = 624;
 
     explicit Mt(uint32_t seed)
@@ -35,20 +36,23 @@ struct Mt {
         for (; i < 227; i++) s[i] = mix(s[i + 397], s[i], s[i + 1]);
         for (; i < 623; i++) s[i] = mix(s[i - 227], s[i], s[i + 1]);
         s[623] = mix(s[396], s[623], s[0]);
+        // MTRand::rand as BrainGrid declares it (BGFLOAT): the tempered word over 2^32 - 1 in
+        // double, rounded to float
+        for (int i = 0; i < 624; i++) {
+            uint32_t y = s[i];
+            y ^= y >> 11;
+            y ^= (y << 7) & 0x9d2c5680u;
+            y ^= (y << 15) & 0xefc60000u;
+            y ^= y >> 18;
+            u[i] = (float)((double)(float)y * (1.0 / 4294967295.0));
+        }
         next = 0;
     }
-    uint32_t word()
+    float uniform()
     {
         if (next == 624) refill();
-        uint32_t y = s[next++];
-        y ^= y >> 11;
-        y ^= (y << 7) & 0x9d2c5680u;
-        y ^= (y << 15) & 0xefc60000u;
-        return y ^ (y >> 18);
+        return u[next++];
     }
-    // MTRand::rand as BrainGrid declares it (BGFLOAT): the word over 2^32 - 1 in double,
-    // rounded to float
-    float uniform() { return (float)((double)(float)word() * (1.0 / 4294967295.0)); }
 };
 
 }  // namespace

@@ -235,9 +235,9 @@ def test_refused_files(tmp_path):
 def test_norm_stream_matches_the_oracle():
     from braingrid_gb300 import lib as bg
     from oracle import pyoracle as po
-    want = po.norm_stream(5, 50001)
+    want = po.norm_stream(5, 1000001)
     g = bg.NormStream(5)
-    got = np.concatenate([g.take(1), g.take(0), g.take(30000), g.take(20000)])
+    got = np.concatenate([g.take(1), g.take(0), g.take(30000), g.take(970000)])
     assert_same("norm", got, want)
     g.close()
 
