@@ -374,3 +374,34 @@ def test_oracle_end_of_run_stream_matches_reference_driver():
     want = np.load("tests/golden/outputs.npz")["c0.ser"].tobytes()
     assert comparable(o.serialize(conn_growth=True), c) == comparable(want, c)
     o.close()
+
+
+def test_dense_static_wiring(tmp_path):
+    """ConnStatic with more connections per neuron than neighbours in reach (static_izh_1000's
+    shape: nConnsPerNeuron 999, radius 50 on a 40 x 25 grid): every source reaches every other
+    neuron, so no tie choice is left and the wiring is complete; one weight draw per synapse, from
+    the range of the source's type, in creation order (source, then nearness)."""
+    c = dict(case("izh_static"), name="dense", width=40, height=25, N=1000, max_syn=1000,
+             synapse=0, stdp=None, stim=None, inh=list(range(0, 1000, 5)), starters=[],
+             static=dict(n=999, radius=50.0, rewire=0.0, exc=(0.0, 0.5e-7), inh=(-0.5e-7, 0.0)))
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    p = cf.read(configs.config_text(c), root=str(tmp_path))
+    assert p.synapse_class == "AllSpikingSynapses" and p.static["n"] == 999
+    a = cf.setup(p)
+    s = a["synapses"]
+    assert a["counts"].tolist() == [999] * 1000
+    used = s["in_use"].astype(bool)
+    assert used.sum() == 999000
+    src = s["src"][used]
+    assert np.bincount(src, minlength=1000).tolist() == [999] * 1000
+    inh = a["ntype"] == cf.INH
+    w = s["W"][used]
+    assert np.all(w[inh[src]] <= 0) and np.all(w[~inh[src]] >= 0)
+    # the draws: the generator after the neuron draws, one per synapse in creation order
+    b = cf.setup(p)
+    slots = b["creation_slots"]
+    rng = cf.MTRand(1)
+    rng.rand(int(6 * 1000 + 4 * 1000))             # IF draws, then a, b, c, d (no starters)
+    lo = np.where(inh[b["synapses"]["src"][slots]], np.float32(-0.5e-7), np.float32(0.0))
+    hi = np.where(inh[b["synapses"]["src"][slots]], np.float32(0.0), np.float32(0.5e-7))
+    assert_same("W in creation order", b["synapses"]["W"][slots], rng.in_range(lo, hi))
