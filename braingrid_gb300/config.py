@@ -445,6 +445,94 @@ def _read_stim(stim, path, p):
     raise ConfigError("unsupported input method %r" % name)
 
 
+def write(p, lists_dir="configfiles/bg3", name="network"):
+    """p as a parameter file in the reference's element layout (the reverse of read), plus the
+    neuron-list files it names: returns (text, {relative path: list-file text}).  Values are
+    written with Python's shortest round-trip repr, so reading the text back gives p's float32
+    values exactly.  A file with STDPParams or ParameterDraw r_squared is this library's; the
+    reference's reader rejects those elements."""
+    def v(x):
+        return repr(float(x)) if not isinstance(x, (int, np.integer)) else str(int(x))
+
+    def rng(tag, lo, hi):
+        return '<%s name="%s"><min name="min">%s</min><max name="max">%s</max></%s>' % (
+            tag, tag, v(lo), v(hi), tag)
+
+    files = {}
+    neu = [rng(k, *p.if_ranges[k]) for k in IF_RANGES]
+    if p.neuron_class == "AllIZHNeurons":
+        if p.izh_draw == "r_squared":
+            neu.append("<ParameterDraw>r_squared</ParameterDraw>")
+        else:
+            for k in IZH_RANGES:
+                z = p.izh_ranges[k]
+                neu.append('<%s name="%s">%s</%s>' % (k, k, "".join(
+                    '<%s name="%s">%s</%s>' % (t, t, v(x), t)
+                    for t, x in zip(("minExc", "maxExc", "minInh", "maxInh"), z)), k))
+    syn = ""
+    if p.stdp is not None:
+        syn = "<STDPParams>%s</STDPParams>" % "".join(
+            "<%s>%s</%s>" % (k, v(p.stdp[k]), k) for k in STDP_DEFAULTS)
+    if p.conn_class == "ConnGrowth":
+        g = p.growth
+        conn = '<GrowthParams name="GrowthParams">%s</GrowthParams>' % "".join(
+            '<%s name="%s">%s</%s>' % (x, x, v(g[k]), x) for x, k in (
+                ("epsilon", "epsilon"), ("beta", "beta"), ("rho", "rho"),
+                ("targetRate", "target_rate"), ("minRadius", "min_radius"),
+                ("startRadius", "start_radius")))
+    else:
+        st = p.static
+        conn = ('<StaticConnectionsParams name="StaticConnectionsParams">'
+                '<nConnsPerNeuron name="nConnsPerNeuron">%d</nConnsPerNeuron>'
+                '<threshConnsRadius name="threshConnsRadius">%s</threshConnsRadius>'
+                '<pRewiring name="pRewiring">%s</pRewiring></StaticConnectionsParams>'
+                '<StaticConnectionsWeight name="StaticConnectionsWeight">'
+                '<minExc name="minExc">%s</minExc><maxExc name="maxExc">%s</maxExc>'
+                '<minInh name="minInh">%s</minInh><maxInh name="maxInh">%s</maxInh>'
+                '</StaticConnectionsWeight>' % (st["n"], v(st["radius"]), v(st["rewire"]),
+                                                v(st["exc"][0]), v(st["exc"][1]),
+                                                v(st["inh"][0]), v(st["inh"][1])))
+    if p.layout_class == "FixedLayout":
+        lay = []
+        for tag, root_tag, lst in (("activeNListFileName", "A", p.active_list),
+                                   ("inhNListFileName", "I", p.inh_list),
+                                   ("probedNListFileName", "P", p.probed_list)):
+            if not lst:
+                # an empty element, as the reference's files have it (an empty list file makes
+                # its reader fail)
+                lay.append('<%s name="%s" type="InputFile"/>' % (tag, tag))
+                continue
+            rel = "%s/%s-%s.xml" % (lists_dir, name, root_tag)
+            files[rel] = '<?xml version="1.0" encoding="UTF-8"?>\n<%s>%s</%s>\n' % (
+                root_tag, " ".join(str(int(i)) for i in lst), root_tag)
+            lay.append('<%s name="%s" type="InputFile">%s</%s>' % (tag, tag, rel, tag))
+        layout = '<LayoutFiles name="LayoutFiles">%s</LayoutFiles>' % "".join(lay)
+    else:
+        layout = ('<frac_EXC name="frac_EXC">%s</frac_EXC><starter_neurons '
+                  'name="starter_neurons">%s</starter_neurons>' % (v(p.frac_exc),
+                                                                   v(p.frac_starter)))
+    text = (
+        '<?xml version="1.0" encoding="UTF-8" standalone="no"?>\n<BGSimParams>\n'
+        '  <SimInfoParams name="SimInfoParams">'
+        '<PoolSize name="PoolSize"><x name="x">%d</x><y name="y">%d</y><z name="z">1</z></PoolSize>'
+        '<SimParams name="SimParams"><Tsim name="Tsim">%s</Tsim><numSims name="numSims">%d'
+        '</numSims></SimParams><SimConfig name="SimConfig"><maxFiringRate name="maxFiringRate">%d'
+        '</maxFiringRate><maxSynapsesPerNeuron name="maxSynapsesPerNeuron">%d'
+        '</maxSynapsesPerNeuron></SimConfig><Seed name="Seed"><value name="value">%d</value>'
+        '</Seed><OutputParams name="OutputParams"><stateOutputFileName '
+        'name="stateOutputFileName">%s</stateOutputFileName></OutputParams></SimInfoParams>\n'
+        '  <ModelParams>\n'
+        '    <NeuronsParams class="%s" name="NeuronsParams">%s</NeuronsParams>\n'
+        '    <SynapsesParams class="%s" name="SynapsesParams">%s</SynapsesParams>\n'
+        '    <ConnectionsParams class="%s" name="ConnectionsParams">%s</ConnectionsParams>\n'
+        '    <LayoutParams class="%s" name="LayoutParams">%s</LayoutParams>\n'
+        '  </ModelParams>\n</BGSimParams>\n' % (
+            p.width, p.height, v(p.tsim), p.epochs, p.max_firing_rate, p.max_syn, p.seed,
+            p.output or "results/%s-out.xml" % name, p.neuron_class, "".join(neu),
+            p.synapse_class, syn, p.conn_class, conn, p.layout_class, layout))
+    return text, files
+
+
 # ---- setup ------------------------------------------------------------------------------------
 def _steps(seconds):
     """static_cast<int>(seconds / deltaT + 0.5): float quotient, double sum."""

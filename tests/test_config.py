@@ -405,3 +405,52 @@ def test_dense_static_wiring(tmp_path):
     lo = np.where(inh[b["synapses"]["src"][slots]], np.float32(-0.5e-7), np.float32(0.0))
     hi = np.where(inh[b["synapses"]["src"][slots]], np.float32(0.0), np.float32(0.5e-7))
     assert_same("W in creation order", b["synapses"]["W"][slots], rng.in_range(lo, hi))
+
+
+@pytest.mark.parametrize("name", ["c0", "izh_static", "izh_dstdp", "c0_spiking"])
+def test_write_reads_back_to_the_same_parameters(name, tmp_path):
+    c = case(name)
+    p = read_case(c, tmp_path)
+    text, files = cf.write(p, name=name)
+    for rel, t in files.items():
+        f = tmp_path / "out" / rel
+        f.parent.mkdir(parents=True, exist_ok=True)
+        f.write_text(t)
+    q = cf.read(text, root=str(tmp_path / "out"))
+    for k in ("width", "height", "tsim", "epochs", "max_firing_rate", "max_syn", "seed",
+              "neuron_class", "synapse_class", "conn_class", "layout_class", "izh_draw",
+              "inh_list", "active_list", "stdp"):
+        assert getattr(q, k) == getattr(p, k), k
+    for k in p.if_ranges:
+        assert q.if_ranges[k] == p.if_ranges[k], k
+    assert q.izh_ranges == p.izh_ranges and q.growth == p.growth
+    assert {k: (v if not isinstance(v, tuple) else tuple(v)) for k, v in q.static.items()} == \
+        {k: (v if not isinstance(v, tuple) else tuple(v)) for k, v in p.static.items()}
+    a, b = cf.setup(p), cf.setup(q)
+    for k in ("Vthresh", "Inoise", "C1", "I0", "ntype"):
+        assert_same(k, b[k], a[k])
+
+
+def test_written_file_runs_in_the_reference_driver(tmp_path):
+    """A parameter file written by config.write (no extension elements) is read by the compiled
+    reference's own driver, which then writes the same result file as from the original."""
+    import os
+    import subprocess
+    growth = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle",
+                          "_ref", "growth")
+    if not os.path.exists(growth):
+        pytest.skip("the compiled reference is built only where its sources are")
+    c, text, _ = configs.output_case("c0")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    p = cf.read(text, root=str(tmp_path))
+    out_text, files = cf.write(p, name="w")
+    for rel, t in files.items():
+        f = tmp_path / rel
+        f.parent.mkdir(parents=True, exist_ok=True)
+        f.write_text(t)
+    (tmp_path / "results").mkdir(exist_ok=True)
+    (tmp_path / "w.xml").write_text(out_text.replace(p.output, "results/w-out.xml"))
+    subprocess.check_call([growth, "-t", "w.xml"], cwd=str(tmp_path), stdout=subprocess.DEVNULL,
+                          stderr=subprocess.DEVNULL, timeout=300)
+    got = (tmp_path / "results" / "w-out.xml").read_bytes()
+    assert got == np.load("tests/golden/outputs.npz")["c0"].tobytes()
