@@ -220,8 +220,13 @@ static int exp_class(bg3_net *n, float tau)
 
 // Per-type STDP constants: the float tables of tauspre / tauspost and the double tables of
 // taupos / tauneg (exp(-delta / taupos), exp(delta / tauneg) over a 3 tau window).
+// The weight-dependence exponents mu+ and mu- must be 0 (the reference's only values,
+// Synapses/AllSTDPSynapses.cpp:252-273): the reference raises W to them with the host libm's
+// pow, which no device function reproduces bit for bit, so other values are refused
+// (BG3_EUNSUPPORTED) rather than run with a different rounding.
 static int set_stdp_type(bg3_net *n, int type, const StdpConst &in)
 {
+    if (!(in.mupos == 0.0f) || !(in.muneg == 0.0f)) return BG3_EUNSUPPORTED;
     StdpConst c = in;
     int rc;
     if ((rc = exp_class(n, c.tauspre)) || (rc = exp_class(n, c.tauspost))) return rc;
@@ -2026,9 +2031,21 @@ struct CkptHeader {
     uint32_t n_dtab, n_ltab;   // decay / delay class tables
     uint32_t n_arrays;         // CKPT_ARRAYS
     uint32_t pad;
+    uint64_t checksum;         // FNV-1a 64 of every byte after the header
 };
-static const uint32_t CKPT_VERSION = 4;
+static_assert(sizeof(CkptHeader) == 136, "checkpoint header layout");
+static const uint32_t CKPT_VERSION = 5;
 static const char CKPT_MAGIC[8] = {'B', 'G', '3', 'C', 'K', 'P', 'T', 0};
+
+static uint64_t fnv1a64(const char *p, uint64_t n)
+{
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (uint64_t i = 0; i < n; i++) {
+        h ^= (uint8_t)p[i];
+        h *= 0x100000001b3ull;
+    }
+    return h;
+}
 
 static size_t alloc_size(const bg3_net *n, const void *p)
 {
@@ -2058,6 +2075,119 @@ static int aresize(bg3_net *n, T *&field, size_t bytes)
     if (!bytes) return BG3_OK;
     if (bytes % sizeof(T)) return BG3_EINVAL;
     return dalloc(n, &field, bytes / sizeof(T));
+}
+
+// Index of each array in the checkpoint's list.
+enum CkptArray {
+#define BG3_ENUM_ONE(f) CKA_##f,
+    BG3_NET_ARRAYS(BG3_ENUM_ONE)
+#undef BG3_ENUM_ONE
+    CKA_COUNT
+};
+
+// Arrays that an external input or its injected intervals add after bg3_create: a checkpoint
+// may hold them where the live network does not (or the reverse).  Every other array must have
+// the live network's allocation size exactly, so that no buffer a tensor map, a captured graph
+// or a kernel bound was derived from changes size.
+static bool ckpt_optional(int i)
+{
+    switch (i) {
+    case CKA_reg_values: case CKA_reg_shift: case CKA_pois_mask: case CKA_pois_nisi:
+    case CKA_in_psr: case CKA_in_decay: case CKA_in_queue: case CKA_in_delay: case CKA_in_ev:
+    case CKA_isi_begin: case CKA_isi_vals: case CKA_isi_cursor:
+        return true;
+    default:
+        return false;
+    }
+}
+
+// The allocation size an optional array has when present (dalloc's max(count, 1) elements);
+// 0 for isi_vals, whose length is the number of intervals drawn ahead.
+static uint64_t ckpt_optional_size(int i, uint64_t N)
+{
+    switch (i) {
+    case CKA_reg_values: case CKA_reg_shift: case CKA_pois_nisi: case CKA_in_psr:
+    case CKA_in_decay: case CKA_in_queue: case CKA_isi_cursor:
+        return 4 * N;
+    case CKA_pois_mask: case CKA_in_delay: return N;
+    case CKA_in_ev: return N * sizeof(EvSlot);
+    case CKA_isi_begin: return 4 * (N + 1);
+    default: return 0;
+    }
+}
+
+// Element i of an array held in a checkpoint's bytes (which need not be aligned).
+template <typename T>
+static T ckpt_get(const char *base, uint64_t i)
+{
+    T v;
+    memcpy(&v, base + i * sizeof(T), sizeof(T));
+    return v;
+}
+
+// Checks the index-like contents of a checkpoint (every value a kernel uses to address memory)
+// against the live network's shape.  Returns BG3_OK or BG3_EINVAL; reads host bytes only.
+static int ckpt_check_contents(const bg3_net *n, const NetDev &sv, const char *const *ap,
+                               const uint64_t *as, int64_t noise_count)
+{
+    const uint64_t N = (uint64_t)n->h.N, Np = (uint64_t)n->h.Np, Mq = (uint64_t)n->h.Mq;
+    const uint64_t S = Np * Mq * 4;
+    // per-dest in-use prefix and the slots behind it
+    for (uint64_t d = 0; d < N; d++) {
+        const uint32_t c = ckpt_get<uint32_t>(ap[CKA_count], d);
+        if (c > (uint32_t)n->h.max_syn) return BG3_EINVAL;
+        for (uint32_t k = 0; k < c; k++) {
+            const uint64_t q = slot_pos((int)k, (int)d, (int)Mq);
+            const int32_t s = ckpt_get<int32_t>(ap[CKA_src], q);
+            const int8_t t = ckpt_get<int8_t>(ap[CKA_stype], q);
+            const uint8_t l = ckpt_get<uint8_t>(ap[CKA_lcls], q);
+            const uint32_t dw = ckpt_get<uint32_t>(ap[CKA_dcls], q >> 3);
+            const uint32_t dc = (dw >> (4u * (uint32_t)(q & 7))) & 15u;
+            EvSlot e;
+            memcpy(&e, ap[CKA_ev] + q * sizeof(EvSlot), sizeof(EvSlot));
+            if (s < 0 || (uint64_t)s >= N || t < 0 || t > 3 || l >= (uint8_t)sv.n_delays ||
+                dc >= (uint32_t)sv.n_dcls || e.dcls >= (uint8_t)sv.n_dcls ||
+                (sv.n_pcls > 0 && e.pcls >= (uint8_t)sv.n_pcls))
+                return BG3_EINVAL;
+        }
+    }
+    // spike ring: per slot a count and that many neuron ids
+    for (uint64_t r = 0; r < BG3_RING; r++) {
+        const int32_t m = ckpt_get<int32_t>(ap[CKA_ring_n], r);
+        if (m < 0 || (uint64_t)m > N) return BG3_EINVAL;
+        for (int32_t i = 0; i < m; i++) {
+            const int32_t id = ckpt_get<int32_t>(ap[CKA_ring], r * N + (uint64_t)i);
+            if (id < 0 || (uint64_t)id >= N) return BG3_EINVAL;
+        }
+    }
+    // outgoing map: runs inside the map, entries inside the planes
+    const uint64_t om = as[CKA_outMap] / 4;
+    for (uint64_t i = 0; i < N * BG3_MAX_DELAYS; i++) {
+        const uint64_t b = ckpt_get<uint32_t>(ap[CKA_outBegin], i);
+        const uint64_t c = ckpt_get<uint32_t>(ap[CKA_outCount], i);
+        if (b + c > om) return BG3_EINVAL;
+    }
+    for (uint64_t i = 0; i < om; i++)
+        if (ckpt_get<uint32_t>(ap[CKA_outMap], i) >= S) return BG3_EINVAL;
+    // injected noise and intervals: cursors inside what is held
+    if (ckpt_get<unsigned long long>(ap[CKA_noise_cursor], 0) > (unsigned long long)noise_count)
+        return BG3_EINVAL;
+    if (as[CKA_isi_begin]) {
+        const uint64_t nv = as[CKA_isi_vals] / 4;
+        int32_t prev = 0;
+        for (uint64_t i = 0; i <= N; i++) {
+            const int32_t b = ckpt_get<int32_t>(ap[CKA_isi_begin], i);
+            if (b < prev || (uint64_t)b > nv) return BG3_EINVAL;
+            prev = b;
+        }
+    }
+    if (as[CKA_isi_cursor])
+        for (uint64_t i = 0; i < N; i++)
+            if (ckpt_get<int32_t>(ap[CKA_isi_cursor], i) < 0) return BG3_EINVAL;
+    if (as[CKA_in_delay])
+        for (uint64_t i = 0; i < N; i++)
+            if (ckpt_get<uint8_t>(ap[CKA_in_delay], i) > 31) return BG3_EINVAL;
+    return BG3_OK;
 }
 
 extern "C" {
@@ -2091,7 +2221,6 @@ int bg3_checkpoint_save(bg3_net *n, void *buf, uint64_t cap, uint64_t *len)
     hd.n_dtab = (uint32_t)n->dtab.size();
     hd.n_ltab = (uint32_t)n->ltab.size();
     hd.n_arrays = CKPT_ARRAYS;
-    memcpy(p, &hd, sizeof(hd));
     p += sizeof(hd);
     memcpy(p, &h, sizeof(NetDev));  // scalars; its pointers mean nothing to a reader
     p += sizeof(NetDev);
@@ -2113,9 +2242,18 @@ int bg3_checkpoint_save(bg3_net *n, void *buf, uint64_t cap, uint64_t *len)
     }
     BG3_NET_ARRAYS(BG3_SAVE_ONE)
 #undef BG3_SAVE_ONE
+    hd.checksum = fnv1a64((const char *)buf + sizeof(hd), total - sizeof(hd));
+    memcpy(buf, &hd, sizeof(hd));
     return BG3_OK;
 }
 
+// Loads in two phases.  The first reads and checks everything against the live network without
+// changing it: the header and checksum, every shape scalar of the saved descriptor, every
+// array's size (only an external input's arrays may differ, see ckpt_optional) and every
+// index-like value (ckpt_check_contents).  Any mismatch returns BG3_EINVAL with the network
+// untouched.  The second drops the captured graph, copies the arrays, takes the exp tables of the
+// saved time constants and only then installs the saved scalars; a CUDA or allocation failure in
+// it leaves the network unusable (destroy it), never pointing at another process's memory.
 int bg3_checkpoint_load(bg3_net *n, const void *buf, uint64_t len)
 {
     if (!n || !buf || len < sizeof(CkptHeader) + sizeof(NetDev)) return BG3_EINVAL;
@@ -2127,47 +2265,96 @@ int bg3_checkpoint_load(bg3_net *n, const void *buf, uint64_t len)
         memcmp(&hd.desc, &n->desc, sizeof(bg3_net_desc)) || hd.n_dtab > BG3_MAX_DCLS ||
         hd.n_ltab > BG3_MAX_DELAYS || hd.noise_count < 0)
         return BG3_EINVAL;
+    if (hd.checksum != fnv1a64(p + sizeof(hd), len - sizeof(hd))) return BG3_EINVAL;
     const bg3_launch_cfg lc = cfg_to(hd.cfg);
     if (!cfg_valid(&lc)) return BG3_EINVAL;
     p += sizeof(hd);
-    NetDev saved;
-    memcpy(&saved, p, sizeof(NetDev));
+    NetDev sv;
+    memcpy(&sv, p, sizeof(NetDev));
     p += sizeof(NetDev);
+    // noise_count is bounded by the bytes left before it enters any product
+    if ((uint64_t)hd.noise_count > (uint64_t)(end - p) / sizeof(float)) return BG3_EINVAL;
     const uint64_t fixed = hd.n_dtab * sizeof(float) + hd.n_ltab * sizeof(int32_t) +
                            (uint64_t)hd.noise_count * sizeof(float);
     if ((uint64_t)(end - p) < fixed) return BG3_EINVAL;
     const char *dtab = p, *ltab = p + hd.n_dtab * sizeof(float);
     const char *noise = p + hd.n_dtab * sizeof(float) + hd.n_ltab * sizeof(int32_t);
     p += fixed;
-    // walk the array list once to check it before anything changes
-    const char *arr = p;
-    for (uint32_t i = 0; i < CKPT_ARRAYS; i++) {
+    NetDev &h = n->h;
+    // shape scalars: what the live allocations, tensor maps and launch geometry derive from
+    if (sv.N != h.N || sv.Np != h.Np || sv.max_syn != h.max_syn || sv.max_spikes != h.max_spikes ||
+        sv.Mq != h.Mq || sv.ntiles != h.ntiles || sv.neuron_kind != h.neuron_kind ||
+        sv.syn_kind != h.syn_kind || fbits(sv.dt) != fbits(h.dt) ||
+        sv.n_burst_bins != h.n_burst_bins || sv.n_spike_bins != h.n_spike_bins ||
+        sv.max_epochs != h.max_epochs || sv.n_dcls != (int32_t)hd.n_dtab ||
+        sv.n_delays != (int32_t)hd.n_ltab || sv.n_expc < 0 || sv.n_expc > BG3_MAX_EXPC ||
+        sv.n_pcls < 0 || sv.n_pcls > BG3_MAX_PCLS || sv.input_kind < 0 || sv.input_kind > 2)
+        return BG3_EINVAL;
+    for (int t = 0; t < 4; t++)
+        if (sv.t_dcls[t] < 0 || sv.t_dcls[t] >= BG3_MAX_DCLS || sv.t_lcls[t] < 0 ||
+            sv.t_lcls[t] >= BG3_MAX_DELAYS || sv.t_pcls[t] < 0 || sv.t_pcls[t] >= BG3_MAX_PCLS ||
+            sv.stdp[t].dlen_pos < 0 || sv.stdp[t].dlen_pos > BG3_DEXP_LEN ||
+            sv.stdp[t].dlen_neg < 0 || sv.stdp[t].dlen_neg > BG3_DEXP_LEN ||
+            !(sv.stdp[t].mupos == 0.0f) || !(sv.stdp[t].muneg == 0.0f))
+            return BG3_EINVAL;
+    for (uint32_t i = 0; i < hd.n_ltab; i++) {
+        const int32_t D = ckpt_get<int32_t>(ltab, i);
+        if (D < 1 || D > 31) return BG3_EINVAL;
+    }
+    // the array list: sizes first
+    const char *ap[CKA_COUNT];
+    uint64_t as[CKA_COUNT];
+    const uint64_t N = (uint64_t)h.N;
+    for (int i = 0; i < CKA_COUNT; i++) {
         uint64_t s;
         if ((uint64_t)(end - p) < 8) return BG3_EINVAL;
         memcpy(&s, p, 8);
         p += 8;
         if ((uint64_t)(end - p) < s) return BG3_EINVAL;
+        ap[i] = p;
+        as[i] = s;
         p += s;
     }
     if (p != end) return BG3_EINVAL;
+    {
+        uint64_t live[CKA_COUNT];
+#define BG3_LIVE_ONE(f) live[CKA_##f] = alloc_size(n, h.f);
+        BG3_NET_ARRAYS(BG3_LIVE_ONE)
+#undef BG3_LIVE_ONE
+        for (int i = 0; i < CKA_COUNT; i++) {
+            if (as[i] == live[i]) continue;
+            if (!ckpt_optional(i)) return BG3_EINVAL;
+            const uint64_t want = ckpt_optional_size(i, N);
+            if (as[i] != 0 && (want ? as[i] != want : (as[i] % 4) != 0)) return BG3_EINVAL;
+        }
+    }
+    // an input's arrays come as a set, and the descriptor's input kind agrees with them
+    const bool reg = as[CKA_reg_values] && as[CKA_reg_shift];
+    const bool pois = as[CKA_pois_mask] && as[CKA_pois_nisi] && as[CKA_in_psr] &&
+                      as[CKA_in_decay] && as[CKA_in_queue] && as[CKA_in_delay] && as[CKA_in_ev] &&
+                      as[CKA_isi_cursor];
+    if ((sv.input_kind == 1 && !reg) || (sv.input_kind == 2 && !pois) ||
+        (as[CKA_isi_begin] != 0) != (as[CKA_isi_vals] != 0) || (as[CKA_isi_begin] && !pois))
+        return BG3_EINVAL;
+    int rc = ckpt_check_contents(n, sv, ap, as, hd.noise_count);
+    if (rc) return rc;
+
+    // ---- second phase: nothing above changed the network ----
     CK(cudaStreamSynchronize(n->stream));
-    NetDev &h = n->h;
-    int rc;
-    p = arr;
+    drop_graph(n);
 #define BG3_LOAD_ONE(f)                                                                           \
     {                                                                                             \
-        uint64_t s;                                                                               \
-        memcpy(&s, p, 8);                                                                         \
-        p += 8;                                                                                   \
-        if ((rc = aresize(n, h.f, (size_t)s))) return rc;                                         \
-        if (s) CK(cudaMemcpy((void *)h.f, p, (size_t)s, cudaMemcpyHostToDevice));                 \
-        p += s;                                                                                   \
+        if ((rc = aresize(n, h.f, (size_t)as[CKA_##f]))) return rc;                               \
+        if (as[CKA_##f])                                                                          \
+            CK(cudaMemcpy((void *)h.f, ap[CKA_##f], (size_t)as[CKA_##f], cudaMemcpyHostToDevice)); \
     }
     BG3_NET_ARRAYS(BG3_LOAD_ONE)
 #undef BG3_LOAD_ONE
     if (n->noise_dev) cudaFree(n->noise_dev);
     n->noise_dev = nullptr;
     n->noise_cap = 0;
+    h.noise_buf = nullptr;
+    h.noise_len = 0;
     if (hd.noise_count) {
         if (cudaMalloc(&n->noise_dev, (size_t)hd.noise_count * sizeof(float)) != cudaSuccess) {
             cudaGetLastError();
@@ -2178,33 +2365,51 @@ int bg3_checkpoint_load(bg3_net *n, const void *buf, uint64_t len)
                       cudaMemcpyHostToDevice));
         n->noise_cap = hd.noise_count;
     }
-    // scalars from the checkpoint, pointers of this network; exp tables looked up again
-    exp_release(n);
-    const NetDev live = h;
-    h = saved;
-#define BG3_KEEP_ONE(f) h.f = live.f;
+    // the saved scalars with this network's pointers; exp tables of the saved time constants
+    // taken before the old ones are released, so that a failure leaves the old ones in place
+    NetDev nh = sv;
+#define BG3_KEEP_ONE(f) nh.f = h.f;
     BG3_NET_ARRAYS(BG3_KEEP_ONE)
 #undef BG3_KEEP_ONE
-    h.noise_buf = n->noise_dev;
-    if (h.n_expc < 0 || h.n_expc > BG3_MAX_EXPC || h.n_pcls < 0 || h.n_pcls > BG3_MAX_PCLS)
-        return BG3_EINVAL;
-    for (int c = 0; c < h.n_expc; c++)
-        if ((rc = exp_table<float>(n, 0, h.expc_tau[c], BG3_EXP_LEN, &h.expc_tab[c]))) return rc;
+    nh.noise_buf = n->noise_dev;
+    nh.noise_len = hd.noise_count;
+    std::vector<ExpKey> old_keys;
+    old_keys.swap(n->exp_keys);
+    auto fail = [&](int code) {
+        const int32_t keep = h.n_expc;
+        exp_release(n);                 // the tables taken for nh
+        h.n_expc = keep;
+        n->exp_keys.swap(old_keys);     // h keeps its own
+        return code;
+    };
+    for (int c = 0; c < nh.n_expc; c++)
+        if ((rc = exp_table<float>(n, 0, nh.expc_tau[c], BG3_EXP_LEN, &nh.expc_tab[c])))
+            return fail(rc);
     for (int t = 0; t < 4; t++) {
-        StdpConst &s = h.stdp[t];
-        s.dpos = s.dneg = nullptr;
-        if (s.dlen_pos && (rc = exp_table<double>(n, 1, s.taupos, BG3_DEXP_LEN, &s.dpos))) return rc;
-        if (s.dlen_neg && (rc = exp_table<double>(n, 1, s.tauneg, BG3_DEXP_LEN, &s.dneg))) return rc;
+        StdpConst &st = nh.stdp[t];
+        st.dpos = st.dneg = nullptr;
+        if (st.dlen_pos && (rc = exp_table<double>(n, 1, st.taupos, BG3_DEXP_LEN, &st.dpos)))
+            return fail(rc);
+        if (st.dlen_neg && (rc = exp_table<double>(n, 1, st.tauneg, BG3_DEXP_LEN, &st.dneg)))
+            return fail(rc);
     }
-    for (int c = 0; c < h.n_pcls; c++) {
-        h.p_xD[c] = h.p_xF[c] = nullptr;
-        if (h.p_D[c] > 0.0f && std::isfinite(h.p_D[c]) &&
-            (rc = exp_table<float>(n, 0, h.p_D[c], BG3_EXP_LEN, &h.p_xD[c])))
-            return rc;
-        if (h.p_F[c] > 0.0f && std::isfinite(h.p_F[c]) &&
-            (rc = exp_table<float>(n, 0, h.p_F[c], BG3_EXP_LEN, &h.p_xF[c])))
-            return rc;
+    for (int c = 0; c < nh.n_pcls; c++) {
+        nh.p_xD[c] = nh.p_xF[c] = nullptr;
+        if (nh.p_D[c] > 0.0f && std::isfinite(nh.p_D[c]) &&
+            (rc = exp_table<float>(n, 0, nh.p_D[c], BG3_EXP_LEN, &nh.p_xD[c])))
+            return fail(rc);
+        if (nh.p_F[c] > 0.0f && std::isfinite(nh.p_F[c]) &&
+            (rc = exp_table<float>(n, 0, nh.p_F[c], BG3_EXP_LEN, &nh.p_xF[c])))
+            return fail(rc);
     }
+    {
+        std::vector<ExpKey> taken;
+        taken.swap(n->exp_keys);
+        n->exp_keys.swap(old_keys);
+        exp_release(n);                 // the old tables
+        n->exp_keys.swap(taken);
+    }
+    h = nh;
     n->dtab.resize(hd.n_dtab);
     n->ltab.resize(hd.n_ltab);
     if (hd.n_dtab) memcpy(n->dtab.data(), dtab, hd.n_dtab * sizeof(float));

@@ -1,16 +1,16 @@
 // Allocation-free variant of the outgoing synapse map build (bg3_outgoing_map_noalloc).
 //
-// Some callers cannot allocate device memory at the point where they need the map: code that
-// runs while a CUDA stream is being captured into a graph (cudaMalloc is not allowed there), a
-// host runtime that hands all device memory out of its own pool and forbids the library from
-// calling cudaMalloc/cudaFree behind its back, or a real-time loop that must not take the
-// allocator's locks.  This entry point takes the caller's device buffers for its inputs and
+// Some callers cannot allocate device memory at the point where they need the map: a host
+// runtime that hands all device memory out of its own pool and forbids the library from calling
+// cudaMalloc/cudaFree behind its back, or a real-time loop that must not take the allocator's
+// locks.  This entry point takes the caller's device buffers for its inputs and
 // outputs and allocates nothing: its only scratch (one counter per source neuron) lives in a
 // file-scope __device__ array of fixed size, which every GPU that loads the library holds until
 // the process exits.
 //
 // Limits and sharing:
-//   * at most BG3_NOALLOC_MAX_NEURONS neurons: more is rejected with BG3_EINVAL before any work
+//   * at most BG3_NOALLOC_MAX_NEURONS neurons, and n_neurons * max_syn at most 2^32 (slot ids
+//     are 32-bit, as the reference's BGSIZE): more is rejected with BG3_EINVAL before any work
 //     is queued; a source with more than BG3_NOALLOC_MAX_FANOUT synapses (known only on the
 //     device) sets bit 1 of the caller's status word and its run of the map stays unsorted;
 //   * every call uses the same scratch array and leaves the last call's counters in it; each
@@ -18,7 +18,11 @@
 //     streams, or different host threads on one device) race on it and must be serialised by
 //     the caller;
 //   * the first call on each device looks up the array's device address (cudaGetSymbolAddress)
-//     with that device current; make that first call before any stream capture.
+//     with that device current and keeps it for the life of the process; make that first call
+//     before any stream capture.  A cudaDeviceReset invalidates the kept address: a process that
+//     resets a device must not call this entry point on it again;
+//   * an error left pending by earlier CUDA calls of the process is cleared on entry, so that a
+//     launch failure reported here is this call's own.
 #include <cstdio>
 #include <mutex>
 
@@ -175,6 +179,12 @@ extern "C" int bg3_outgoing_map_noalloc(const int32_t *src_dev, const uint32_t *
                 n_neurons, BG3_NOALLOC_MAX_NEURONS);
         return BG3_EINVAL;
     }
+    if ((uint64_t)n_neurons * (uint64_t)max_syn > (1ull << 32)) {
+        fprintf(stderr, "bg3_outgoing_map_noalloc: %d x %d slots do not fit 32-bit slot ids\n",
+                n_neurons, max_syn);
+        return BG3_EINVAL;
+    }
+    cudaGetLastError();  // an earlier call's pending error is not this call's
     uint32_t *fill = nullptr;
     int rc = scratch_address(&fill);
     if (rc) return rc;
@@ -183,9 +193,13 @@ extern "C" int bg3_outgoing_map_noalloc(const int32_t *src_dev, const uint32_t *
     const int sb = 152 * 8;
     if (cudaMemsetAsync(status_dev, 0, sizeof(uint32_t), s) != cudaSuccess) return BG3_ECUDA;
     k_na_zero<<<nb, NOALLOC_THREADS, 0, s>>>(fill, count_dev, n_neurons);
+    if (cudaGetLastError() != cudaSuccess) return BG3_ECUDA;
     k_na_count<<<sb, NOALLOC_THREADS, 0, s>>>(src_dev, counts_dev, n_neurons, max_syn, count_dev, status_dev);
+    if (cudaGetLastError() != cudaSuccess) return BG3_ECUDA;
     k_na_scan<<<1, 1024, 0, s>>>(count_dev, begin_dev, n_neurons, status_dev);
+    if (cudaGetLastError() != cudaSuccess) return BG3_ECUDA;
     k_na_fill<<<sb, NOALLOC_THREADS, 0, s>>>(src_dev, counts_dev, n_neurons, max_syn, begin_dev, fill, map_dev);
+    if (cudaGetLastError() != cudaSuccess) return BG3_ECUDA;
     k_na_sort<<<n_neurons, NOALLOC_THREADS, 0, s>>>(begin_dev, count_dev, map_dev);
     if (cudaGetLastError() != cudaSuccess) return BG3_ECUDA;
     return BG3_OK;

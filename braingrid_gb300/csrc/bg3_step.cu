@@ -241,7 +241,8 @@ __device__ __forceinline__ unsigned long long hist_at(const NetDev &n, int i, in
     return n.history[(size_t)i * n.max_spikes + x];
 }
 
-__device__ __forceinline__ float pow_mu(float x, float mu) { return mu == 0.0f ? 1.0f : powf(x, mu); }
+// W^mu with mu = 0, the only exponent a network accepts (set_stdp_type refuses others)
+__device__ __forceinline__ float pow_mu(float, float) { return 1.0f; }
 
 // stdpLearning with delta = dk steps (dk the signed interval; 0 when not a small count)
 __device__ __forceinline__ float stdp_learn(const StdpConst &c, float W, float delta, float epost,

@@ -206,7 +206,9 @@ int bg3_scale_weights(bg3_net *net, float factor);
  * (batches run device noise). */
 int bg3_set_noise_mode(bg3_net *net, int32_t mode, uint32_t seed);
 /* The CUDA device that networks created afterwards on this host thread use (the reference
- * driver's -d, g_deviceId, Core/BGDriver.cpp:323-326); device 0 if never called. */
+ * driver's -d, g_deviceId, Core/BGDriver.cpp:323-326); device 0 if never called.  A network does
+ * not switch devices by itself: every later call on it must be made with the device it was
+ * created on current (as the reference, which sets the device once in setupSim). */
 int bg3_set_device(int32_t device);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
@@ -263,9 +265,12 @@ int bg3_epoch_record(bg3_net *net);
 
 /* AllSTDPSynapses::copySynapseHostToDevice (Synapses/AllSTDPSynapses_d.cu:125-195): the STDP
  * fields of the slots given by syn (in_use, type, delayIdx).  Constants must be uniform per
- * synapse type; post queues must be empty with total_delayPost 0 (BG3_EUNSUPPORTED otherwise). */
+ * synapse type; post queues must be empty with total_delayPost 0; the weight-dependence
+ * exponents mupos and muneg must be 0, the reference's values (it raises W to them with the
+ * host's pow, which the device cannot reproduce bit for bit).  BG3_EUNSUPPORTED otherwise. */
 int bg3_upload_stdp(bg3_net *net, const bg3_synapse_arrays *syn, const bg3_stdp_arrays *a);
-/* Constants for synapses created by the device growth pass from now on. */
+/* Constants for synapses created by the device growth pass from now on (mupos and muneg 0,
+ * BG3_EUNSUPPORTED otherwise, as for bg3_upload_stdp). */
 int bg3_set_stdp_constants(bg3_net *net, const bg3_stdp_constants *c);
 /* BG3_STDP_HOST (default) or BG3_STDP_DEVICE. */
 int bg3_set_stdp_arithmetic(bg3_net *net, int mode);
@@ -307,9 +312,9 @@ int bg3_download_state(bg3_net *net, const bg3_state_view *view);
 
 /* ---- allocation-free variant -------------------------------------------------------------- */
 /* No counterpart in the reference: an extra entry point for callers that cannot allocate device
- * memory when they need the map (code running under CUDA stream capture, where cudaMalloc is
- * not allowed; host runtimes that own every device allocation through their own pool; real-time
- * loops that must not enter the allocator).  Builds the outgoing synapse map in the reference's
+ * memory when they need the map (host runtimes that own every device allocation through their
+ * own pool; real-time loops that must not enter the allocator).  Builds the outgoing synapse map
+ * in the reference's
  * order (Core/SynapseIndexMap.h: per source neuron, the slot ids d * max_syn + k in ascending
  * order) from caller-owned DEVICE buffers and allocates nothing:
  *   src_dev     [n_neurons * max_syn] int32, reference slot layout (sourceNeuronIndex)
@@ -320,8 +325,11 @@ int bg3_download_state(bg3_net *net, const bg3_state_view *view);
  *   stream      cudaStream_t (NULL: the legacy default stream); the call only enqueues work.
  * Its scratch (one counter per neuron) is a fixed array inside the library, shared by all calls
  * on a device and kept until the process exits: calls that overlap on the GPU race on it.  More
- * than BG3_NOALLOC_MAX_NEURONS neurons is rejected with BG3_EINVAL.  The first call on each
- * device resolves the array's address with that device current; make it before any capture. */
+ * than BG3_NOALLOC_MAX_NEURONS neurons, or n_neurons * max_syn above 2^32 (32-bit slot ids), is
+ * rejected with BG3_EINVAL.  The first call on each device resolves the array's address with
+ * that device current and keeps it; make it before any stream capture.  After a cudaDeviceReset
+ * the kept address is stale: do not call this entry point on a device the process has reset.
+ * A CUDA error left pending by earlier calls is cleared on entry. */
 #define BG3_NOALLOC_MAX_NEURONS 65536
 #define BG3_NOALLOC_MAX_FANOUT 4096
 int bg3_outgoing_map_noalloc(const int32_t *src_dev, const uint32_t *counts_dev,
@@ -430,11 +438,14 @@ int bg3_batch_autotune(bg3_batch *batch, int32_t steps_per_trial, bg3_launch_cfg
  * bg3_checkpoint_save: with buf == NULL only *len is set (the bytes needed); with cap < *len it
  * returns BG3_EINVAL and writes nothing.  The format is this library build's own (host byte order,
  * checked by a header); it is not meant for other programs.
- * bg3_checkpoint_load: into a network made by bg3_create with the same bg3_net_desc (BG3_EINVAL
- * otherwise, before anything changes).  Arrays the checkpoint holds that the network lacks (an
- * input set up before the save) are allocated.  A network that is a member of a batch needs
- * bg3_batch_refresh afterwards.  If the load fails part way (a CUDA or allocation error), destroy
- * the network. */
+ * bg3_checkpoint_load: into a network made by bg3_create with the same bg3_net_desc.  Everything
+ * is checked before anything changes, and any mismatch is BG3_EINVAL with the network untouched:
+ * the header and a checksum of the bytes, every shape scalar, the size of every array (only the
+ * arrays of an external input may differ from the network's: the input set up before the save is
+ * allocated, one set up since is freed) and every value a kernel addresses memory with (source
+ * and neuron ids, row counts, class codes, map runs, cursors).  A network that is a member of a
+ * batch needs bg3_batch_refresh afterwards.  If the load fails after those checks (a CUDA or
+ * allocation error), destroy the network. */
 int bg3_checkpoint_save(bg3_net *net, void *buf, uint64_t cap, uint64_t *len);
 int bg3_checkpoint_load(bg3_net *net, const void *buf, uint64_t len);
 

@@ -27,6 +27,16 @@ LIF_CONFIG0_RANGES = [13.5e-9, 13.5e-9, 1.0e-9, 1.5e-9, 15.0e-3, 15.0e-3, 0.0, 0
                       13.5e-3, 13.5e-3, 13.0e-3, 13.0e-3, 13.565e-3, 13.655e-3, 13.0e-3, 13.0e-3]
 
 
+def reference_tree():
+    """The reference source tree the recipe oracle/ref.mk resolves (its REF, from the
+    BRAINGRID_REF environment variable or the recipe's default), or None where it is absent (as on
+    a machine that only runs the tests)."""
+    r = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "ref.mk"), "where"],
+                       capture_output=True, text=True)
+    path = r.stdout.strip()
+    return path if r.returncode == 0 and path else None
+
+
 def build(force=False):
     """Compile the oracle into oracle/_build/libbgoracle.so (host CPU, any architecture)."""
     src = os.path.join(HERE, "bg_oracle.c")

@@ -1,8 +1,12 @@
 # Builds the reference BrainGrid single-threaded simulator from its own sources, in place where
 # they lie, into oracle/_ref/ only.  This is test infrastructure (the checker), never the product.
 #
-#   make -f oracle/ref.mk REF=/root/reference            # FP32 build (BGFLOAT=float)
-#   make -f oracle/ref.mk REF=/root/reference fp64       # FP64 build (BGFLOAT=double)
+#   make -f oracle/ref.mk                 # FP32 build (BGFLOAT=float)
+#   make -f oracle/ref.mk fp64            # FP64 build (BGFLOAT=double)
+#   make -s -f oracle/ref.mk where        # prints the reference tree used, or fails if absent
+#
+# The reference tree is REF, else the BRAINGRID_REF environment variable, else the checkout
+# this recipe was written against; this recipe is the one place that names it.
 #
 # Outputs:
 #   oracle/_ref/growth            unmodified driver (Core/BGDriver.cpp), XML recorder, no HDF5
@@ -14,7 +18,8 @@
 # Flags follow the reference Makefile (Makefile:86): -O2 -std=c++98 -DTIXML_USE_STL -DDEBUG_OUT,
 # minus the profiling/strip flags (-pg -s -g), which do not change arithmetic.
 
-REF ?= /root/reference
+BRAINGRID_REF ?= /root/reference
+REF ?= $(BRAINGRID_REF)
 HERE := $(dir $(lastword $(MAKEFILE_LIST)))
 OUT ?= $(HERE)_ref
 OUT64 ?= $(HERE)_ref64
@@ -66,4 +71,7 @@ $(OUT64)/growth: $(OBJS64) $(OUT64)/obj/Core/BGDriver.o
 $(OUT64)/bg_ref_harness: $(OBJS64) $(HERE)ref_harness.cpp
 	$(CXX) $(REFFLAGS) $(INC) -include $(HERE)fp64/bgfloat_double.h -o $@ $(HERE)ref_harness.cpp $(OBJS64)
 
-.PHONY: all fp64
+where:
+	@test -f $(REF)/Core/BGDriver.cpp && echo $(abspath $(REF))
+
+.PHONY: all fp64 where

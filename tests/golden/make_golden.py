@@ -1,8 +1,8 @@
 """Generate the committed parity fixtures in tests/golden/ from the compiled reference.
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run in a checkout that has the reference sources (the tree oracle/ref.mk resolves, or --ref):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref PATH]
 
 It (1) writes the network configs and NLists under tests/golden/configs/, (2) builds the
 reference single-threaded simulator and oracle/ref_harness.cpp with oracle/ref.mk, (3) runs the
@@ -175,13 +175,19 @@ def parse_xml_matrix(text, name):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="reference source tree (default: the one oracle/ref.mk resolves)")
     ap.add_argument("--cases", default="")
     ap.add_argument("--only-serialize", action="store_true",
                     help="write serialize.npz only (the other fixtures stay as they are)")
     ap.add_argument("--only-outputs", action="store_true",
                     help="write outputs.npz only (the reference driver's result files)")
     a = ap.parse_args()
+    if a.ref is None:
+        from oracle import pyoracle
+        a.ref = pyoracle.reference_tree()
+        if a.ref is None:
+            sys.exit("no reference source tree: set BRAINGRID_REF or pass --ref")
     harness = build_reference(a.ref)
     if a.only_outputs:
         work = tempfile.mkdtemp(prefix="bg_golden_")

@@ -90,6 +90,31 @@ def test_resume_continues_bit_exact(name, noise):
     net2.close()
 
 
+# Checkpoint layout (this library's own format): a 136-byte header whose last 8 bytes are an
+# FNV-1a 64 checksum of everything after it, the saved descriptor (netdev_bytes), the decay and
+# delay tables, the injected noise, then every device array as [uint64 bytes][bytes] in a fixed
+# order: 'count' is the 34th array, 'ring_n' the 27th.
+HDR = 136
+ARR_COUNT, ARR_RING_N = 33, 26
+
+
+def array_offset(ck, index):
+    netdev = int(ck[12:16].view(np.uint32)[0])
+    noise = int(ck[104:112].view(np.int64)[0])
+    n_dtab, n_ltab = (int(v) for v in ck[112:120].view(np.uint32))
+    p = HDR + netdev + 4 * n_dtab + 4 * n_ltab + 4 * noise
+    for _ in range(index):
+        p += 8 + int(ck[p:p + 8].view(np.uint64)[0])
+    return p + 8
+
+
+def reseal(ck):
+    h = 0xcbf29ce484222325
+    for b in ck[HDR:].tobytes():
+        h = ((h ^ b) * 0x100000001b3) & 0xFFFFFFFFFFFFFFFF
+    ck[HDR - 8:HDR] = np.frombuffer(np.uint64(h).tobytes(), np.uint8)
+
+
 def test_checkpoint_is_refused_when_malformed_or_of_another_shape():
     c = case("c0_grown")
     o = oracle_from_case(c)
@@ -110,6 +135,20 @@ def test_checkpoint_is_refused_when_malformed_or_of_another_shape():
     corrupt[0] ^= 0xFF
     with pytest.raises(RuntimeError):
         net.load_checkpoint(corrupt)
+    # a flipped byte deep inside the arrays: the checksum refuses it
+    corrupt = ck.copy()
+    corrupt[ck.size // 2] ^= 0x10
+    with pytest.raises(RuntimeError):
+        net.load_checkpoint(corrupt)
+    # well-formed bytes (checksum recomputed) whose row count or spike-ring count would address
+    # memory outside the network: refused by the content checks
+    for array, value in ((ARR_COUNT, c["max_syn"] + 1), (ARR_RING_N, c["N"] + 1)):
+        forged = ck.copy()
+        off = array_offset(forged, array)
+        forged[off:off + 4] = np.frombuffer(np.int32(value).tobytes(), np.uint8)
+        reseal(forged)
+        with pytest.raises(RuntimeError):
+            net.load_checkpoint(forged)
     # another shape (one more neuron row)
     d = net.desc
     other = bg.Network(d.n_neurons + d.width, d.max_syn_per_neuron, d.width, d.height + 1,

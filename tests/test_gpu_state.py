@@ -38,3 +38,24 @@ def test_download_state_equals_single_downloads(name):
             net.download_state(izh=True)
     net.close()
     o.close()
+
+
+def test_stdp_weight_exponent_other_than_zero_is_refused():
+    """The reference raises W to mupos / muneg with the host's pow (both 0 in its createSynapse);
+    the library accepts only 0 and refuses other exponents instead of rounding them differently."""
+    from braingrid_gb300 import lib as bg
+    from tests.gpu_helpers import stdp_constants
+    c = case("c0_stdp")
+    o = oracle_from_case(c)
+    net = gpu_from_oracle(o, c, noise_mode=bg.BG3_NOISE_DEVICE)
+    k = stdp_constants(c)
+    net.set_stdp_constants(**k)
+    for field in ("mupos", "muneg"):
+        bad = dict(k, **{field: 0.5})
+        with pytest.raises(bg.Bg3Error) as e:
+            net.set_stdp_constants(**bad)
+        assert "(-6)" in str(e.value)  # BG3_EUNSUPPORTED
+    net.step(100)
+    assert net.error_word == 0
+    net.close()
+    o.close()
