@@ -823,6 +823,19 @@ int bg3_push_noise(bg3_net *n, const float *v, int64_t cnt)
     return BG3_OK;
 }
 
+int bg3_noise_pending(bg3_net *n, int64_t *pending)
+{
+    if (!n || !pending) return BG3_EINVAL;
+    *pending = 0;
+    if (n->h.noise_mode != BG3_NOISE_INJECT || !n->noise_dev) return BG3_OK;
+    unsigned long long cur = 0;
+    CK(cudaMemcpyAsync(&cur, n->h.noise_cursor, sizeof(cur), cudaMemcpyDeviceToHost, n->stream));
+    CK(cudaStreamSynchronize(n->stream));
+    const long long left = n->h.noise_len - (long long)cur;
+    *pending = left > 0 ? left : 0;
+    return BG3_OK;
+}
+
 // ---- external input -------------------------------------------------------------------------
 int bg3_input_regular(bg3_net *n, const float *values, const int32_t *shifts, int32_t dur,
                       int32_t cycle, int32_t in_cycle)

@@ -1,0 +1,368 @@
+// GPUSpikingModel on libbg3: the drop-in for the reference's Core/GPUSpikingModel.cu.
+//
+// Compiled by g++ with -DUSE_GPU against the reference's own headers, unchanged.  Its class
+// declaration is the reference's Core/GPUSpikingModel.h (which includes the CUDA sample header
+// Book.h only under __CUDACC__, never defined here), so BGDriver (Core/BGDriver.cpp:204-208),
+// Simulator and the XML parameter files drive this model exactly as they drive the reference's.
+// Nothing of the reference's CUDA code is compiled or linked: the GPU work goes through the C-ABI
+// of include/bg3.h.
+//
+// What the model does on each interface call (Core/IModel.h:64-151):
+//   setupSim           host setup as the reference (Model::setupSim), then one bg3_net for the
+//                      whole network, filled from the host objects through the classes' own
+//                      copy*HostToDevice members (bg3_classes.cpp);
+//   advance            queues the step; queued steps run as one bg3_step call (CUDA-graph replays
+//                      inside the library) when BG3_STEPS_PER_CALL steps have queued, or when the
+//                      state is next observed (epoch end, checkpoint, cleanup);
+//   updateConnections  the spike counts and histories the recorder reads come back to the host,
+//                      then the epoch's growth pass runs on the device (ConnGrowth) and its radii
+//                      and rates come back; a static network only rolls its device counters;
+//   updateHistory      the reference recorder (Model::updateHistory) on those host copies, then
+//                      the device spike counts are cleared as the reference's model does;
+//   deserialize        Model::deserialize into the host objects, then a fresh upload;
+//   cleanupSim         the whole device state back into the host objects, then the network is
+//                      freed (Core/GPUSpikingModel.cu:82-99).
+//
+// Noise.  By default the model draws the reference's own noise stream on the host:
+// rgNormrnd[0] = Norm(0, 1, seed), the generator the reference's single-threaded model creates
+// (Core/SingleThreadedSpikingModel.cpp:30), and the library consumes it in the reference's CPU
+// order, so a run matches the single-threaded reference spike for spike.  The values are drawn
+// ahead on the host while the GPU runs the previous steps.  With BG3_NOISE=device the library's
+// own generator (keyed by seed, step and neuron, one draw per neuron per step like the reference
+// GPU model's) is used instead and the host draws nothing.
+//
+// Checkpoints.  The reference's Model::serialize writes the host objects; when the run writes a
+// checkpoint (a memOutputFileName is set), the last epoch's updateHistory copies the whole device
+// state back into them first, so the stream holds the final state.
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "AllDSSynapses.h"
+#include "AllDynamicSTDPSynapses.h"
+#include "AllIFNeurons.h"
+#include "AllIZHNeurons.h"
+#include "AllSTDPSynapses.h"
+#include "ConnGrowth.h"
+#include "GPUSpikingModel.h"
+#include "Global.h"
+#include "Norm.h"
+#include "bg3_dropin.h"
+
+namespace {
+
+// What this model keeps beside the reference's class layout (whose members are the reference's
+// device pointers): the network, the queued steps and the noise drawn ahead.
+struct ModelState {
+    bg3_net *net;
+    bool reference_noise;
+    int64_t chunk;                        // steps per bg3_step call
+    int64_t queued;                       // steps advance() queued and not yet launched
+    std::vector<float> drawn;             // noise values drawn ahead, not yet pushed
+    int64_t held_at_launch;               // values the device held when the last steps launched
+    ModelState() : net(NULL), reference_noise(true), chunk(1000), queued(0), held_at_launch(0) {}
+};
+
+std::map<const GPUSpikingModel *, ModelState> g_state;
+
+ModelState &state_of(const GPUSpikingModel *m) { return g_state[m]; }
+
+int32_t neuron_kind(IAllNeurons *n)
+{
+    if (dynamic_cast<AllIZHNeurons *>(n)) return BG3_NEURON_IZH;
+    if (dynamic_cast<AllIFNeurons *>(n)) return BG3_NEURON_LIF;
+    fprintf(stderr, "GPUSpikingModel: neuron class not supported by libbg3\n");
+    exit(EXIT_FAILURE);
+}
+
+int32_t synapse_kind(IAllSynapses *s)
+{
+    if (dynamic_cast<AllDynamicSTDPSynapses *>(s)) return BG3_SYN_DYNSTDP;
+    if (dynamic_cast<AllSTDPSynapses *>(s)) return BG3_SYN_STDP;
+    if (dynamic_cast<AllDSSynapses *>(s)) return BG3_SYN_DS;
+    if (dynamic_cast<AllSpikingSynapses *>(s)) return BG3_SYN_SPIKING;
+    fprintf(stderr, "GPUSpikingModel: synapse class not supported by libbg3\n");
+    exit(EXIT_FAILURE);
+}
+
+// A fresh object of the network's synapse class, for reading what its createSynapse gives each
+// synapse type.
+AllSpikingSynapses *scratch_synapses(int32_t kind)
+{
+    switch (kind) {
+    case BG3_SYN_DYNSTDP: return new AllDynamicSTDPSynapses(1, 4);
+    case BG3_SYN_STDP: return new AllSTDPSynapses(1, 4);
+    case BG3_SYN_DS: return new AllDSSynapses(1, 4);
+    default: return new AllSpikingSynapses(1, 4);
+    }
+}
+
+// The per-type constants of synapses the device growth pass creates, taken from the reference's
+// own createSynapse (one synapse of each type II, IE, EI, EE on a scratch object), so that they
+// are the reference's values for this deltaT by construction.
+void set_type_constants(bg3_net *net, int32_t kind, const SimulationInfo *si)
+{
+    AllSpikingSynapses *s = scratch_synapses(kind);
+    BGFLOAT sp = 0;
+    for (int t = 0; t < 4; t++) s->createSynapse(t, 0, 0, &sp, si->deltaT, (synapseType)t);
+    bg3_type_constants c;
+    memset(&c, 0, sizeof(c));
+    for (int t = 0; t < 4; t++) {
+        c.tau[t] = s->tau[t];
+        c.decay[t] = s->decay[t];
+        c.total_delay[t] = s->total_delay[t];
+    }
+    const BGFLOAT *U = NULL, *D = NULL, *F = NULL, *u = NULL, *r = NULL;
+    if (AllDSSynapses *d = dynamic_cast<AllDSSynapses *>(s)) {
+        U = d->U; D = d->D; F = d->F; u = d->u; r = d->r;
+    } else if (AllDynamicSTDPSynapses *d = dynamic_cast<AllDynamicSTDPSynapses *>(s)) {
+        U = d->U; D = d->D; F = d->F; u = d->u; r = d->r;
+    }
+    if (U) {
+        for (int t = 0; t < 4; t++) {
+            c.U[t] = U[t];
+            c.D[t] = D[t];
+            c.F[t] = F[t];
+        }
+        c.u0 = u[0];
+        c.r0 = r[0];
+    }
+    bg3_dropin_check(bg3_set_type_constants(net, &c), "bg3_set_type_constants");
+    if (AllSTDPSynapses *p = dynamic_cast<AllSTDPSynapses *>(s)) {
+        bg3_stdp_constants k;
+        memset(&k, 0, sizeof(k));
+        for (int t = 0; t < 4; t++) {
+            k.Apos[t] = p->Apos[t]; k.Aneg[t] = p->Aneg[t]; k.STDPgap[t] = p->STDPgap[t];
+            k.tauspost[t] = p->tauspost[t]; k.tauspre[t] = p->tauspre[t];
+            k.taupos[t] = p->taupos[t]; k.tauneg[t] = p->tauneg[t]; k.Wex[t] = p->Wex[t];
+            k.mupos[t] = p->mupos[t]; k.muneg[t] = p->muneg[t];
+            k.useFroemkeDanSTDP[t] = p->useFroemkeDanSTDP[t] ? 1 : 0;
+        }
+        bg3_dropin_check(bg3_set_stdp_constants(net, &k), "bg3_set_stdp_constants");
+    }
+    delete s;
+}
+
+int64_t env_int(const char *name, int64_t dflt)
+{
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    char *end = NULL;
+    const long long x = strtoll(v, &end, 10);
+    return (end && !*end && x > 0) ? (int64_t)x : dflt;
+}
+
+void draw(std::vector<float> &out, int64_t n)
+{
+    Norm &g = *rgNormrnd[0];
+    const size_t old = out.size();
+    out.resize(old + (size_t)n);
+    for (int64_t i = 0; i < n; i++) out[old + (size_t)i] = g();
+}
+
+}  // namespace
+
+bg3_net *bg3_dropin_model_network(IModel *model)
+{
+    GPUSpikingModel *m = dynamic_cast<GPUSpikingModel *>(model);
+    if (!m) return NULL;
+    std::map<const GPUSpikingModel *, ModelState>::iterator it = g_state.find(m);
+    return it == g_state.end() ? NULL : it->second.net;
+}
+
+GPUSpikingModel::GPUSpikingModel(Connections *conns, IAllNeurons *neurons, IAllSynapses *synapses,
+                                 Layout *layout)
+    : Model(conns, neurons, synapses, layout), randNoise_d(NULL), synapseIndexMapDevice(NULL),
+      m_allSynapsesDevice(NULL), m_allNeuronsDevice(NULL)
+{
+}
+
+GPUSpikingModel::~GPUSpikingModel()
+{
+    std::map<const GPUSpikingModel *, ModelState>::iterator it = g_state.find(this);
+    if (it != g_state.end()) {
+        if (it->second.net) bg3_destroy(it->second.net);
+        g_state.erase(it);
+    }
+}
+
+// The network's device state: one bg3_net for neurons, synapses, maps and growth state, which
+// both device-struct pointers stand for (Core/GPUSpikingModel.cu:28-47 allocates the two SoA
+// structs and the noise array instead).  The host arrays go over through the classes' own copy
+// members; the index maps are rebuilt on the device from the synapse slots.
+void GPUSpikingModel::allocDeviceStruct(void **allNeuronsDevice, void **allSynapsesDevice,
+                                        SimulationInfo *sim_info)
+{
+    ModelState &st = state_of(this);
+    bg3_net_desc d;
+    memset(&d, 0, sizeof(d));
+    d.n_neurons = sim_info->totalNeurons;
+    d.max_syn_per_neuron = sim_info->maxSynapsesPerNeuron;
+    d.width = sim_info->width;
+    d.height = sim_info->height;
+    d.epoch_duration = sim_info->epochDuration;
+    d.delta_t = sim_info->deltaT;
+    d.max_firing_rate = sim_info->maxFiringRate;
+    d.max_epochs = sim_info->maxSteps;
+    d.neuron_kind = neuron_kind(m_neurons);
+    d.synapse_kind = synapse_kind(m_synapses);
+    d.noise_mode = st.reference_noise ? BG3_NOISE_INJECT : BG3_NOISE_DEVICE;
+    d.noise_seed = (uint32_t)sim_info->seed;
+    bg3_dropin_check(bg3_create(&d, &st.net), "bg3_create");
+    *allNeuronsDevice = st.net;
+    *allSynapsesDevice = st.net;
+    m_neurons->allocNeuronDeviceStruct(allNeuronsDevice, sim_info);
+    m_synapses->allocSynapseDeviceStruct(allSynapsesDevice, sim_info);
+
+    std::vector<int32_t> types(sim_info->totalNeurons);
+    for (int i = 0; i < sim_info->totalNeurons; i++) types[i] = m_layout->neuron_type_map[i];
+    bg3_dropin_check(bg3_upload_layout(st.net, &(*m_layout->xloc)[0], &(*m_layout->yloc)[0],
+                                       types.data()),
+                     "bg3_upload_layout");
+    set_type_constants(st.net, d.synapse_kind, sim_info);
+    m_neurons->copyNeuronHostToDevice(*allNeuronsDevice, sim_info);
+    m_synapses->copySynapseHostToDevice(*allSynapsesDevice, sim_info);
+    if (ConnGrowth *g = dynamic_cast<ConnGrowth *>(m_conns)) {
+        bg3_growth_params gp;
+        gp.epsilon = g->m_growth.epsilon;
+        gp.beta = g->m_growth.beta;
+        gp.rho = g->m_growth.rho;
+        gp.target_rate = g->m_growth.targetRate;
+        gp.min_radius = g->m_growth.minRadius;
+        gp.start_radius = g->m_growth.startRadius;
+        gp.max_rate = g->m_growth.maxRate;
+        bg3_dropin_check(bg3_upload_growth(st.net, &gp, &(*g->radii)[0], &(*g->rates)[0]),
+                         "bg3_upload_growth");
+    }
+}
+
+// Copies the device state back into the host objects and frees the network
+// (Core/GPUSpikingModel.cu:56-74).
+void GPUSpikingModel::deleteDeviceStruct(void **allNeuronsDevice, void **allSynapsesDevice,
+                                         SimulationInfo *sim_info)
+{
+    ModelState &st = state_of(this);
+    m_neurons->copyNeuronDeviceToHost(*allNeuronsDevice, sim_info);
+    m_neurons->deleteNeuronDeviceStruct(*allNeuronsDevice, sim_info);
+    m_synapses->copySynapseDeviceToHost(*allSynapsesDevice, sim_info);
+    m_synapses->deleteSynapseDeviceStruct(*allSynapsesDevice);
+    bg3_dropin_check(bg3_destroy(st.net), "bg3_destroy");
+    st.net = NULL;
+    *allNeuronsDevice = NULL;
+    *allSynapsesDevice = NULL;
+}
+
+void GPUSpikingModel::setupSim(SimulationInfo *sim_info)
+{
+    bg3_dropin_check(bg3_set_device(g_deviceId), "bg3_set_device");
+    Model::setupSim(sim_info);
+    ModelState &st = state_of(this);
+    const char *noise = getenv("BG3_NOISE");
+    st.reference_noise = !(noise && std::string(noise) == "device");
+    st.chunk = env_int("BG3_STEPS_PER_CALL", 1000);
+    st.queued = 0;
+    st.drawn.clear();
+    st.held_at_launch = 0;
+    if (st.reference_noise) rgNormrnd.push_back(new Norm(0, 1, sim_info->seed));
+    allocDeviceStruct((void **)&m_allNeuronsDevice, (void **)&m_allSynapsesDevice, sim_info);
+    m_neurons->setAdvanceNeuronsDeviceParams(*m_synapses);
+    m_synapses->setAdvanceSynapsesDeviceParams();
+}
+
+// Runs the steps advance() queued.  With the reference's noise the device must hold one value
+// per neuron per queued step (each step consumes at most that); the values drawn ahead go over
+// first, any shortfall is drawn now, and after the launch the next call's values are drawn while
+// the GPU runs: enough to hold two calls' worth, so the device never runs short and never piles
+// up more than that.
+static void run_queued(ModelState &st, const SimulationInfo *si)
+{
+    if (!st.queued) return;
+    const int64_t N = si->totalNeurons;
+    if (st.reference_noise) {
+        if (!st.drawn.empty())
+            bg3_dropin_check(bg3_push_noise(st.net, st.drawn.data(), (int64_t)st.drawn.size()),
+                             "bg3_push_noise");
+        st.drawn.clear();
+        int64_t held = 0;
+        bg3_dropin_check(bg3_noise_pending(st.net, &held), "bg3_noise_pending");
+        if (held < N * st.queued) {
+            draw(st.drawn, N * st.queued - held);
+            bg3_dropin_check(bg3_push_noise(st.net, st.drawn.data(), (int64_t)st.drawn.size()),
+                             "bg3_push_noise");
+            st.drawn.clear();
+            held = N * st.queued;
+        }
+        st.held_at_launch = held;
+    }
+    bg3_dropin_check(bg3_step(st.net, st.queued), "bg3_step");
+    if (st.reference_noise) {
+        const int64_t want = 2 * N * st.chunk - st.held_at_launch;
+        if (want > 0) draw(st.drawn, want);   // overlaps the steps just launched
+    }
+    st.queued = 0;
+}
+
+void GPUSpikingModel::advance(const SimulationInfo *sim_info)
+{
+    ModelState &st = state_of(this);
+    if (++st.queued >= st.chunk) run_queued(st, sim_info);
+}
+
+// Fused into the sweep of every step (the reference's calcSummationMapDevice,
+// Core/GPUSpikingModel.cu:382-416): nothing is left to do here.
+void GPUSpikingModel::calcSummationMap(const SimulationInfo *) {}
+
+void GPUSpikingModel::updateConnections(const SimulationInfo *sim_info)
+{
+    ModelState &st = state_of(this);
+    run_queued(st, sim_info);
+    AllSpikingNeurons *sn = dynamic_cast<AllSpikingNeurons *>(m_neurons);
+    sn->copyNeuronDeviceSpikeCountsToHost(m_allNeuronsDevice, sim_info);
+    sn->copyNeuronDeviceSpikeHistoryToHost(m_allNeuronsDevice, sim_info);
+    if (dynamic_cast<ConnGrowth *>(m_conns)) {
+        m_conns->updateSynapsesWeights(sim_info->totalNeurons, *m_neurons, *m_synapses, sim_info,
+                                       m_allNeuronsDevice, m_allSynapsesDevice, m_layout);
+    } else {
+        // no growth: the device's own recorder histories and its spike-count roll
+        bg3_dropin_check(bg3_epoch_record(st.net), "bg3_epoch_record");
+    }
+    uint32_t err = 0;
+    bg3_dropin_check(bg3_error_word(st.net, &err), "bg3_error_word");
+    if (err) {
+        fprintf(stderr, "GPUSpikingModel: device error word 0x%x after epoch %d\n", err,
+                sim_info->currentStep);
+        exit(EXIT_FAILURE);
+    }
+}
+
+void GPUSpikingModel::updateHistory(const SimulationInfo *sim_info)
+{
+    Model::updateHistory(sim_info);
+    dynamic_cast<AllSpikingNeurons *>(m_neurons)->clearNeuronSpikeCounts(m_allNeuronsDevice, sim_info);
+    if (sim_info->currentStep == sim_info->maxSteps && !sim_info->memOutputFileName.empty()) {
+        // the driver writes the checkpoint from the host objects next (Core/BGDriver.cpp:110-116)
+        m_neurons->copyNeuronDeviceToHost(m_allNeuronsDevice, sim_info);
+        m_synapses->copySynapseDeviceToHost(m_allSynapsesDevice, sim_info);
+    }
+}
+
+void GPUSpikingModel::deserialize(istream &input, const SimulationInfo *sim_info)
+{
+    Model::deserialize(input, sim_info);
+    m_neurons->copyNeuronHostToDevice(m_allNeuronsDevice, sim_info);
+    m_synapses->copySynapseHostToDevice(m_allSynapsesDevice, sim_info);
+    if (ConnGrowth *g = dynamic_cast<ConnGrowth *>(m_conns))
+        bg3_dropin_check(bg3_upload_growth(state_of(this).net, NULL, &(*g->radii)[0],
+                                           &(*g->rates)[0]),
+                         "bg3_upload_growth");
+}
+
+void GPUSpikingModel::cleanupSim(SimulationInfo *sim_info)
+{
+    ModelState &st = state_of(this);
+    run_queued(st, sim_info);
+    deleteDeviceStruct((void **)&m_allNeuronsDevice, (void **)&m_allSynapsesDevice, sim_info);
+    st.drawn.clear();
+    Model::cleanupSim(sim_info);
+}

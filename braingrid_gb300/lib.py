@@ -184,6 +184,7 @@ def load(build_if_missing=True):
         "bg3_set_type_constants": ([vp, ctypes.POINTER(TypeConstants)], ctypes.c_int),
         "bg3_upload_growth": ([vp, ctypes.POINTER(GrowthParams), c_f32p, c_f32p], ctypes.c_int),
         "bg3_push_noise": ([vp, c_f32p, ctypes.c_int64], ctypes.c_int),
+        "bg3_noise_pending": ([vp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
         "bg3_set_noise_mode": ([vp, ctypes.c_int32, ctypes.c_uint32], ctypes.c_int),
         "bg3_set_device": ([ctypes.c_int32], ctypes.c_int),
         "bg3_norm_create": ([ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.POINTER(vp)],
@@ -498,6 +499,12 @@ class Network:
     def push_noise(self, values):
         v = np.ascontiguousarray(values, np.float32)
         check(self.L.bg3_push_noise(self.h, _p(v), len(v)), "bg3_push_noise")
+
+    def noise_pending(self):
+        """Injected noise values pushed and not yet consumed."""
+        v = ctypes.c_int64()
+        check(self.L.bg3_noise_pending(self.h, ctypes.byref(v)), "bg3_noise_pending")
+        return v.value
 
     # hot path
     def step(self, n=1):

@@ -212,6 +212,11 @@ int bg3_set_noise_mode(bg3_net *net, int32_t mode, uint32_t seed);
 int bg3_set_device(int32_t device);
 /* Appends n values to the injected noise stream (BG3_NOISE_INJECT), in Norm draw order. */
 int bg3_push_noise(bg3_net *net, const float *values, int64_t n);
+/* Injected noise values pushed and not yet consumed (0 in device-noise mode); waits for the
+ * network's queued steps.  A host that draws the stream ahead uses it to keep at least one value
+ * per neuron per queued step on the device without piling up the rest.  No counterpart in the
+ * reference (its host model draws each value where it consumes it). */
+int bg3_noise_pending(bg3_net *net, int64_t *pending);
 
 /* The reference's own noise stream on the host, for bg3_push_noise: Norm(mu, sigma, seed)
  * (RNG/Norm.cpp:59-86, the Marsaglia polar method in float over MTRand,

@@ -1,0 +1,77 @@
+"""The reference-side drop-in (braingrid_gb300/dropin/): the reference's own driver, compiled
+unmodified with -DUSE_GPU, links against the drop-in and libbg3.so with no unresolved symbol and
+none of the reference's CUDA code, and a run reaches the model's first C-ABI call.
+
+Needs the reference's sources (the tree oracle/ref.mk resolves); skipped where they are absent.
+Without a GPU the run stops at that first call (bg3_set_device), which is what this test checks:
+the unchanged BGDriver parses the parameter file, creates the model through its USE_GPU branch
+(Core/BGDriver.cpp:204-208) and hands control to the drop-in."""
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from braingrid_gb300 import build as bgbuild
+from oracle import pyoracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+MK = os.path.join(ROOT, "braingrid_gb300", "dropin", "dropin.mk")
+OUT = os.path.join(ROOT, "braingrid_gb300", "_build", "dropin")
+EXE = os.path.join(OUT, "growth_bg3")
+
+
+@pytest.fixture(scope="module")
+def driver():
+    ref = pyoracle.reference_tree()
+    if ref is None:
+        pytest.skip("the reference's sources are not on this machine")
+    bgbuild.build()
+    subprocess.check_call(["make", "-s", "-f", MK, "-j8"], cwd=ROOT)
+    return ref
+
+
+def test_unchanged_driver_links_with_no_unresolved_symbol(driver):
+    assert os.path.exists(EXE)
+    r = subprocess.run(["ldd", "-r", EXE], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "undefined symbol" not in r.stdout + r.stderr
+    assert re.search(r"libbg3\.so => \S*_build/dropin/\.\./libbg3\.so", r.stdout), r.stdout
+
+
+def test_no_reference_cuda_or_sample_code_is_linked(driver):
+    objs = []
+    for d, _, files in os.walk(os.path.join(OUT, "ref")):
+        objs += [os.path.relpath(os.path.join(d, f), os.path.join(OUT, "ref")) for f in files]
+    assert "Core/BGDriver.o" in objs and "Core/Model.o" in objs
+    assert not [o for o in objs if o.endswith("_d.o") or "GPUSpikingModel" in o or
+                "GpuSInput" in o or "MersenneTwister_d" in o or "HostSInput" in o], objs
+    syms = subprocess.run(["nm", "-C", EXE], capture_output=True, text=True).stdout
+    for name in ("normalMTGPU", "initMTGPU", "calcSummationMapDevice", "cudaMalloc"):
+        assert name not in syms, name
+    # the model and the device members of the classes come from the drop-in
+    for name in ("GPUSpikingModel::advance", "AllLIFNeurons::advanceNeurons",
+                 "AllDSSynapses::copySynapseHostToDevice", "ConnGrowth::updateSynapsesWeights",
+                 "GpuSInputPoisson::init"):
+        assert re.search(r" T %s\(" % re.escape(name), syms), name
+
+
+def test_driver_reaches_the_drop_in(driver, tmp_path):
+    shutil.copytree(os.path.join(driver, "configfiles"), str(tmp_path / "configfiles"))
+    (tmp_path / "results").mkdir()
+    r = subprocess.run([EXE, "-t", "configfiles/test-tiny.xml"], cwd=str(tmp_path),
+                       capture_output=True, text=True, timeout=120)
+    out = r.stdout + r.stderr
+    assert "Setup simulation." in out
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        assert r.returncode == 0, out
+    else:
+        # no device: the model's first C-ABI call reports it and the driver exits as the
+        # reference's HANDLE_ERROR does
+        assert r.returncode != 0 and "bg3_set_device" in out, out
