@@ -88,6 +88,13 @@ CASES = [
           keep_steps_every=1000, syn_keep=(9,)),
     # FP64 reference on the 10x10 network (long-run comparison base)
     _case("c0_fp64", 10, 10, 1.0, 10, 100, fp64=True),
+    # FP64 reference on the 100x100 benchmark network's model (10,000 neurons, 100 starters,
+    # max 1000 synapses per neuron, seed 7), 2 x 1 s
+    _case("c1_fp64", 100, 100, 1.0, 2, 1000, seed=7, n_starters=100, site_seed=7, fp64=True),
+    # FP64 reference on the Izhikevich + dynamic STDP + Poisson network (izh_dstdp)
+    _case("izh_dstdp_fp64", 12, 12, 0.5, 2, 100, radii=1.3, max_firing_rate=1000, site_seed=4,
+          neuron="izh", synapse=3, stdp=STDP_SOFT, fp64=True,
+          stim=dict(kind="poisson", fr_mean=10.0, weight=0.5, masks=None)),
     # Regular pulse input, random per-neuron phase (sync="no": shifts drawn before the neurons)
     _case("c0_regular", 10, 10, 0.5, 2, 100, keep_steps_every=250,
           stim=dict(kind="regular", duration=0.005, interval=0.045, sync="no", values=REG_VALUES)),

@@ -206,14 +206,15 @@ def main():
         write_config_tree(cfgdir)
         os.makedirs(os.path.join(work, "results"), exist_ok=True)
         ser = {}
-        for case in CASES:
+        for case in ([] if a.cases else CASES):  # --cases: those fixtures alone
             if case["name"] in SERIALIZE_CASES:
                 path = os.path.join(work, case["name"] + ".ser")
                 run_harness(harness, work, case["config"], case["args"],
                             os.path.join(work, case["name"] + ".sbin"), serialize=path)
                 ser[case["name"]] = np.frombuffer(open(path, "rb").read(), np.uint8)
-        np.savez_compressed(os.path.join(HERE, "serialize.npz"), **ser)
-        print("wrote serialize", sorted(ser))
+        if ser:
+            np.savez_compressed(os.path.join(HERE, "serialize.npz"), **ser)
+            print("wrote serialize", sorted(ser))
         if a.only_serialize:
             return
         selected = [c for c in CASES if not a.cases or c["name"] in a.cases.split(",")]
@@ -222,8 +223,14 @@ def main():
             d = run_harness(h, work, case["config"], case["args"],
                             os.path.join(work, case["name"] + ".bin"))
             out = compact(d, case.get("keep_steps_every"), case.get("syn_keep"))
+            if case.get("fp64") and case["name"] != "c0_fp64":
+                # long-run comparison bases: the growth state after every epoch and the rasters
+                out = {k: v for k, v in out.items()
+                       if k.startswith(("post.rates", "post.radii", "raster#"))}
             np.savez_compressed(os.path.join(HERE, case["name"] + ".npz"), **out)
             print("wrote", case["name"], len(out), "arrays")
+        if a.cases:
+            return
         # the reference's own CPU goldens
         g = {}
         for nm in ("test-tiny", "test-small"):

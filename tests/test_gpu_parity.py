@@ -8,8 +8,10 @@ library rounds every float operation as the reference's x86-64 build does).
 Growth weights go through acos/sin; the device evaluates them in double and rounds once, while
 the reference uses glibc's float acosf/sinf, which are not correctly rounded for some arguments.
 Weights are therefore compared within 1e-5 relative, and the strict tests then load the oracle's
-weights (bg3_upload_weights) so that the following epochs stay bit-comparable.  The free-running
-test checks the long-run statistics instead.
+weights (bg3_upload_weights) so that the following epochs stay bit-comparable.
+test_free_running_on_own_growth_weights runs on the GPU's own growth weights instead: rasters
+bit-exact up to the first growth, then Vm and psr within 1e-5 relative for as long as the two
+rasters agree, and it reports the first step at which they part (if any).
 """
 import numpy as np
 import pytest
@@ -237,3 +239,107 @@ def test_device_weight_scaling_matches_host_scaling():
     assert_same("W", sa["W"], sb["W"])
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("name,epochs", [("c0_grown", 5), ("m30_grown", 5)])
+def test_free_running_on_own_growth_weights(name, epochs):
+    """No weight resync: the GPU keeps the weights its own growth passes computed (within 1e-5 of
+    the reference's) and the oracle keeps its own.  Every 50 steps: spike rasters (counts and
+    history) compared exactly; while they agree, Vm within 1e-5 relative and the psr of every
+    in-use synapse within 1e-5 relative; the index maps and per-pair synapse counts after every
+    growth exactly.  Before the first growth there are no synapses and everything is bit-exact.
+    The first step at which the rasters part, if any, is printed (pytest -s)."""
+    c = case(name)
+    spe = steps_per_epoch(c)
+    o = oracle_from_case(c)
+    net = gpu_from_oracle(o, c, n_noise=c["N"] * spe * epochs + 64)
+    every, first, worst_vm, worst_psr = 50, None, 0.0, 0.0
+    for e in range(epochs):
+        for k in range(spe // every):
+            o.step_n(every)
+            net.step(every)
+            t = e * spe + (k + 1) * every
+            g = net.download_lif()
+            same = (np.array_equal(g["spikeCount"], o.arr("spikeCount")) and
+                    np.array_equal(g["spikeCountOffset"], o.arr("spikeCountOffset")) and
+                    np.array_equal(g["history"], o.arr("history")))
+            if e == 0:
+                assert same, "rasters differ before the first growth (step %d)" % t
+                compare_neurons(net, o, "step %d" % t)
+            if not same:
+                if first is None:
+                    first = t
+                continue
+            if first is not None:
+                continue
+            vm, ovm = g["Vm"].astype(np.float64), o.arr("Vm").astype(np.float64)
+            rel = np.abs(vm - ovm) / np.maximum(np.abs(ovm), 1e-30)
+            worst_vm = max(worst_vm, float(rel.max()))
+            assert rel.max() <= 1e-5, "step %d: Vm relative difference %g" % (t, rel.max())
+            if o.total and t % 500 == 0:
+                used = o.arr("in_use").astype(bool)
+                ps = net.download_synapses()["psr"][used].astype(np.float64)
+                ops = o.arr("psr")[used].astype(np.float64)
+                rel = np.abs(ps - ops) / np.maximum(np.abs(ops), 1e-30)
+                rel[(ps == 0) & (ops == 0)] = 0.0
+                worst_psr = max(worst_psr, float(rel.max()))
+                assert rel.max() <= 1e-5, "step %d: psr relative difference %g" % (t, rel.max())
+        o.growth()
+        o.record_epoch(e + 1)
+        net.growth(e + 1)
+        if first is None:
+            r, q = net.download_growth()
+            assert_same("radii after growth %d" % (e + 1), r, o.arr("radii"))
+            compare_maps(net, o, "growth %d" % (e + 1))
+            sy = net.download_synapses()
+            assert_same("counts after growth %d" % (e + 1), sy["counts"], o.arr("counts"))
+            used = o.arr("in_use").astype(bool)
+            np.testing.assert_allclose(sy["W"][used], o.arr("W")[used], rtol=1e-5, atol=0)
+    assert o.total > 0 and net.error_word == 0
+    print("%s free running on the GPU's own growth weights, %d steps: rasters %s; worst Vm "
+          "relative difference %.3g, worst psr %.3g while they agreed"
+          % (name, epochs * spe, "identical throughout" if first is None else
+             "part at step %d" % first, worst_vm, worst_psr))
+
+
+def test_benchmark_shape_step_locked():
+    """The benchmark network's shape: 100x100 LIF + DS, 1,000 slots per neuron, one growth pass
+    at radius U[8.35, 8.45] wiring ~7.6 M synapses on the 32-dest TMA sweep path; maps and
+    per-pair counts bit-exact after the GPU's own growth pass, weights within 1e-5, then both
+    sides take the oracle's weights times the benchmark's 0.003 (float products, the same bits on
+    both) and every membrane starts just below threshold, so the first steps deliver heavy
+    bursts; 2,000 steps step-locked with injected noise, neuron state checked every 250 steps and
+    every synapse's state at 1,000 and 2,000."""
+    from tests.golden.configs import site_lists
+    N = 10000
+    c = dict(case("c0"), name="plain100", width=100, height=100, N=N, max_syn=1000, tsim=1.0,
+             epochs=1, max_firing_rate=200, radii=None, seed=7)
+    c["inh"], c["starters"] = site_lists(100, 100, 0.10, 100, seed=7)
+    o = oracle_from_case(c)
+    rs = np.random.RandomState(11)
+    o.arr("radii")[:] = rs.uniform(8.35, 8.45, N).astype(np.float32)
+    net = gpu_from_oracle(o, c, n_noise=N * 2100)
+    o.growth()
+    o.record_epoch(1)
+    net.growth(1)
+    assert o.total > 7000000, o.total
+    compare_maps(net, o, "growth")
+    sy = net.download_synapses()
+    assert_same("counts", sy["counts"], o.arr("counts"))
+    used = o.arr("in_use").astype(bool)
+    np.testing.assert_allclose(sy["W"][used], o.arr("W")[used], rtol=1e-5, atol=0)
+    o.arr("W")[:] = o.arr("W") * np.float32(0.003)
+    net.upload_weights(o.arr("W"))
+    o.arr("Vm")[:] = rs.uniform(13.0e-3, 15.2e-3, N).astype(np.float32)
+    net.upload_lif(Vm=o.arr("Vm"))
+    for t in range(250, 2001, 250):
+        o.step_n(250)
+        net.step(250)
+        compare_neurons(net, o, "step %d" % t)
+        compare_history(net, o, "step %d" % t)
+        if t % 1000 == 0:
+            compare_synapses(net, o, "step %d" % t)
+    fired = int(o.arr("spikeCount").sum())
+    assert fired > 1000, fired
+    assert net.error_word == 0
+    print("benchmark shape: %d synapses, %d spikes in 2,000 steps" % (o.total, fired))

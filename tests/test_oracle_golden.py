@@ -157,3 +157,34 @@ def test_fp32_vs_fp64_reference_long_run_gap():
     net_rel = abs(float(np.sum(q32)) - float(np.sum(q64))) / float(np.sum(q64))
     assert radii_rel < 2e-3, radii_rel
     assert net_rel < 0.08, net_rel
+
+
+@pytest.mark.parametrize("name,radii_tol,net_tol", [("c1_fp64", 1e-3, 0.08),
+                                                    ("izh_dstdp_fp64", 1e-6, 0.01)])
+def test_fp32_vs_fp64_reference_gap_per_config(name, radii_tol, net_tol):
+    """The FP32 path (the oracle, bit-exact with the FP32 reference and with the GPU in
+    injected-noise mode) against the reference built with BGFLOAT = double, per config.
+    Measured: the 100x100 benchmark model (10,000 neurons, 2 x 1 s): final radii 7.5e-4 relative,
+    network spike count 6.1 %, per-neuron rates median 33 % / max 500 % over the 160 neurons that
+    fire at all (1-6 spikes per epoch); the Izhikevich + dynamic STDP + Poisson network (144
+    neurons, 2 x 0.5 s): radii 2.3e-7, network spike count 0.17 %, per-neuron rates median 0 %, max
+    100 % (one spike more or less).  Per-neuron rates within 2 % are out of reach for any FP32
+    build of neurons that fire a handful of times per epoch."""
+    c = case(name)
+    fx = load_fixture(name)
+    o = oracle_from_case(c)
+    spe = steps_per_epoch(c)
+    q32, r32 = [], []
+    for e in range(c["epochs"]):
+        o.step_n(spe)
+        o.growth()
+        o.record_epoch(e + 1)
+        q32.append(o.arr("rates").astype(np.float64))
+        r32.append(o.arr("radii").astype(np.float64))
+    q64 = np.array([fx["post.rates#%d" % e] for e in range(c["epochs"])], np.float64)
+    r64 = np.array([fx["post.radii#%d" % e] for e in range(c["epochs"])], np.float64)
+    radii_rel = float(np.max(np.abs(np.array(r32) - r64) / r64))
+    net_rel = abs(float(np.sum(q32)) - float(np.sum(q64))) / float(np.sum(q64))
+    assert radii_rel < radii_tol, radii_rel
+    assert net_rel < net_tol, net_rel
+    o.close()
