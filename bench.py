@@ -237,9 +237,10 @@ def run_bg3(args):
            "l2": "not evicted between steps: consecutive steps of one run, whose per-step state "
                  "(%.0f MB) fits the 129 MB L2" % (alg_bytes / 1e6)}
     err = net.error_word
-    batched = izh_stdp = served = growth = None
+    batched = izh_stdp = served = growth = small = None
     if world == 1:
         growth = run_growth()
+        small = run_small()
         batched = run_batched(min(args.steps, 500), max(args.warmup, 20))
         izh_stdp = run_izh512(min(args.steps, 1000), max(args.warmup, 20))
         if args.serve_jobs > 0:
@@ -284,6 +285,7 @@ def run_bg3(args):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "growth": growth,
+            "small_network": small,
             "batched": batched,
             "batched_izh_stdp": izh_stdp,
             "served": served,
@@ -511,6 +513,63 @@ def run_growth():
     return out
 
 
+def run_small(steps=20000, warmup=2000):
+    """The 100-neuron network of the first configuration (10x10 LIF + DS + ConnGrowth, 10 %
+    inhibitory, 10 starters, max 100 synapses per neuron; at its stated 0.4 start radius it has no
+    synapses) stepped on the one-CTA path (many whole steps per launch) and on the multi-kernel
+    path, with the library's device noise and with the reference's Norm stream pushed ahead
+    (injected noise); host wall clock around synchronised bg3_step calls, beside the oracle C
+    port of the reference on one core of this host (the CPU baseline leg)."""
+    import time as _t
+    from braingrid_gb300 import lib as bg
+    from braingrid_gb300 import netgen
+    spec = netgen.lif_network(10, 10, frac_inh=0.10, seed=1)
+    N = spec["N"]
+    out = {"workload": "10x10 LIF + DS + ConnGrowth (first configuration), %d steps" % steps}
+    for mode, name in ((bg.BG3_NOISE_DEVICE, "device_noise"), (bg.BG3_NOISE_INJECT, "injected_noise")):
+        for small, tag in ((65536, "one_cta"), (0, "multi_kernel")):
+            net = netgen.make_gpu_network(spec, 100, noise_mode=mode, noise_seed=1)
+            net.set_launch(small_max_slots=small)
+            if mode == bg.BG3_NOISE_INJECT:
+                gen = bg.NormStream(1)
+                net.push_noise(gen.take(N * (steps + warmup)))
+                gen.close()
+            net.step(warmup)
+            net.sync()
+            l0 = net.launches
+            t0 = _t.perf_counter()
+            net.step(steps)
+            net.sync()
+            dt = _t.perf_counter() - t0
+            out["%s_%s_us_per_step" % (name, tag)] = dt * 1e6 / steps
+            out["%s_%s_launches" % (name, tag)] = net.launches - l0
+            out["%s_%s_error_word" % (name, tag)] = net.error_word
+            net.close()
+    out["cpu_baseline"] = small_cpu_baseline(spec, steps)
+    out["cpu_over_gpu_one_cta"] = (out["cpu_baseline"]["us_per_step"] /
+                                   out["device_noise_one_cta_us_per_step"])
+    return out
+
+
+def small_cpu_baseline(spec, steps):
+    """The oracle (the reference algorithm in C, one thread) on the same 100-neuron network."""
+    from oracle import pyoracle as po
+    N = spec["N"]
+    o = po.OracleNet(N, 100, 10, 10, 1.0, 1e-4, 200, 10)
+    for k in ("xloc", "yloc", "ntype", "Vm", "Vthresh", "Vreset", "I0", "Inoise", "C1", "C2",
+              "Trefract"):
+        o.arr(k)[:] = spec[k]
+    o.growth_init(0.60, 0.10, 1e-4, 1.0, 0.1, 0.4)
+    o.seed_noise(1)
+    o.step_n(1000)
+    t0 = time.perf_counter()
+    o.step_n(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"us_per_step": dt * 1e6 / steps, "cores": 1, "kind": "port",
+            "sample": "%d steps of the same network (oracle C port, one thread)" % steps}
+
+
 def run_izh512(steps, warmup):
     """The 512-network batch: Izhikevich + dynamic STDP networks (static wiring, Poisson drive) advanced
     as one batch against the same networks run one at a time with bg3_step."""
@@ -692,7 +751,7 @@ def main():
                     help="jobs of the served-stream trace")
     ap.add_argument("--serve-slots", type=float, default=SERVE_SLOTS,
                     help="served form: cap on the resident jobs' synapse slots (0 = none)")
-    ap.add_argument("--only", choices=["izh512", "serve", "growth"], default=None,
+    ap.add_argument("--only", choices=["izh512", "serve", "growth", "small"], default=None,
                     help="run one secondary workload alone and print its JSON")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -702,6 +761,9 @@ def main():
         return
     if args.only == "growth":
         print(json.dumps(run_growth()), flush=True)
+        return
+    if args.only == "small":
+        print(json.dumps(run_small()), flush=True)
         return
     if args.only == "serve":
         print(json.dumps(run_served(args.serve_jobs, int(args.serve_slots))), flush=True)

@@ -29,6 +29,8 @@ void launch_deliver_batch(int syn_kind, const NetDev *nets, int count, const Lau
 void launch_sweep_batch(const NetDev *nets, const CUtensorMap *maps, const int2 *tiles, int n_thick,
                         int n_thin, bool fuse, const LaunchCfg &c, cudaStream_t s);
 bool sweep_is_thin(const NetDev &h, const LaunchCfg &c);
+bool small_eligible(const NetDev &h, const LaunchCfg &c);
+void launch_small(const NetDev &h, int nsteps, cudaStream_t s);
 void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, int add_threads, cudaStream_t s);
 void launch_rebuild_maps(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 void launch_scale_weights(const NetDev &h, float f, cudaStream_t s);
@@ -36,6 +38,7 @@ void launch_record(const NetDev &h, const NetDev *d_net, cudaStream_t s);
 }  // namespace bg3
 
 static const int GRAPH_STEPS = 32;  // fused steps captured per CUDA graph replay
+static const int SMALL_STEPS = 4096;  // steps per launch of a small network (bg3::launch_small)
 
 // kernels one step launches after its neuron pass: delivery (+ post-spike STDP) and the sweep
 static inline int step_kernels(int syn_kind) { return syn_kind >= BG3_SYN_STDP ? 3 : 2; }
@@ -993,6 +996,17 @@ static int run_steps(bg3_net *n, int64_t nsteps)
 {
     if (nsteps <= 0) return BG3_OK;
     const NetDev &h = n->h;
+    if (bg3::small_eligible(h, n->cfg)) {
+        // a small network: up to SMALL_STEPS whole steps per launch, one CTA
+        for (int64_t left = nsteps; left > 0;) {
+            const int k = (int)std::min<int64_t>(left, SMALL_STEPS);
+            bg3::launch_small(h, k, n->stream);
+            n->launches += 1;
+            left -= k;
+        }
+        CK(cudaGetLastError());
+        return BG3_OK;
+    }
     if (h.noise_mode == BG3_NOISE_INJECT) {
         // (neurons, deliver, sweep) per step; runs of GRAPH_STEPS steps replay a captured graph
         // (the injected stream's cursor lives on the device, and a push or any other change of
@@ -1759,12 +1773,13 @@ static bool cfg_valid(const bg3_launch_cfg *c)
            (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512) &&
            (c->sweep_dests == 16 || c->sweep_dests == 32) &&
            (c->deliver_early == 0 || c->deliver_early == 1) && c->izh_hw_every >= 0 &&
-           c->izh_hw_every <= 8;
+           c->izh_hw_every <= 8 && c->small_max_slots >= 0;
 }
 static LaunchCfg cfg_from(const bg3_launch_cfg &c)
 {
     return LaunchCfg{c.sweep_stages, c.thin_max_quads, c.thin_warps, c.deliver_blocks,
-                     c.growth_threads, c.sweep_dests, c.deliver_early, c.izh_hw_every};
+                     c.growth_threads, c.sweep_dests, c.deliver_early, c.izh_hw_every,
+                     c.small_max_slots};
 }
 static bg3_launch_cfg cfg_to(const LaunchCfg &c)
 {
@@ -1777,6 +1792,7 @@ static bg3_launch_cfg cfg_to(const LaunchCfg &c)
     o.sweep_dests = c.sweep_dests;
     o.deliver_early = c.deliver_early;
     o.izh_hw_every = c.izh_hw_every;
+    o.small_max_slots = c.small_max_slots;
     return o;
 }
 
@@ -2046,7 +2062,7 @@ struct CkptHeader {
     uint32_t pad;
     uint64_t checksum;         // FNV-1a 64 of every byte after the header
 };
-static_assert(sizeof(CkptHeader) == 136, "checkpoint header layout");
+static_assert(sizeof(CkptHeader) == 144, "checkpoint header layout");
 static const uint32_t CKPT_VERSION = 5;
 static const char CKPT_MAGIC[8] = {'B', 'G', '3', 'C', 'K', 'P', 'T', 0};
 

@@ -892,27 +892,11 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
     sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise, n.ntiles * (SW_DESTS / D));
 }
 
-// Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
-// of a tile is 512 contiguous bytes of the plane (and 128 of the class plane), so the warp reads
-// it with one coalesced 16-byte load per lane, scales it, writes it back and adds it in row
-// order; the same epilogue as sweep_tile.  Lanes past N sit in the last tile's padding, whose
-// slots stay +0.0f.  For these networks a TMA pipeline per 32 dests would spend most of its time
-// in set-up.
-// Before it: the kernel's pdl_wait (spike delivery for this step has finished writing psr), the
-// dstep advance by the network's tile 0 and the block barrier, then pdl_trigger.
-template <bool FUSE>
-__device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile, const int nq,
-                                                const unsigned long long t)
+// psr *= decay for the first nq row quads of a 32-dest tile and the sum of each dest's rows in
+// row order (one lane per dest; a row quad is one coalesced 16-byte load per lane).
+__device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, const int nq,
+                                           const int lane)
 {
-    const int lane = threadIdx.x & 31;
-    const int d = tile * SW_DESTS + lane;
-    const bool valid = d < n.N;
-    NeuronIn x;
-    float noise = 0.0f;
-    if (FUSE && valid) {
-        neuron_load(n, d, x);  // in flight with the row loads below
-        noise = normal_device(n.noise_seed, t + 1, d);
-    }
     // this tile's row quads: [Mq][32 lanes] float4 of psr, 16 bits of class codes
     float4 *P = reinterpret_cast<float4 *>(n.psr) + (size_t)tile * n.Mq * 32 + lane;
     const uint16_t *C = reinterpret_cast<const uint16_t *>(n.dcls) + (size_t)tile * n.Mq * 32 + lane;
@@ -942,8 +926,34 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile,
             }
         }
     }
+    return acc;
+}
+
+// Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
+// of a tile is 512 contiguous bytes of the plane (and 128 of the class plane), so the warp reads
+// it with one coalesced 16-byte load per lane, scales it, writes it back and adds it in row
+// order; the same epilogue as sweep_tile.  Lanes past N sit in the last tile's padding, whose
+// slots stay +0.0f.  For these networks a TMA pipeline per 32 dests would spend most of its time
+// in set-up.
+// Before it: the kernel's pdl_wait (spike delivery for this step has finished writing psr), the
+// dstep advance by the network's tile 0 and the block barrier, then pdl_trigger.
+template <bool FUSE>
+__device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile, const int nq,
+                                                const unsigned long long t)
+{
+    const int lane = threadIdx.x & 31;
+    const int d = tile * SW_DESTS + lane;
+    const bool valid = d < n.N;
+    NeuronIn x;
+    float noise = 0.0f;
+    if (FUSE && valid) {
+        neuron_load(n, d, x);  // in flight with the row loads below
+        noise = normal_device(n.noise_seed, t + 1, d);
+    }
+    const float acc = thin_rows(n, tile, nq, lane);
     sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise, n.ntiles);
 }
+
 
 template <int SYN, bool FUSE, int ST, int D>
 __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ NetDev n,
@@ -1007,6 +1017,177 @@ __global__ void __launch_bounds__(1024) k_sweep_thin_batch(const NetDev *nets, c
 }
 
 bool sweep_is_thin(const NetDev &h, const LaunchCfg &c) { return h.Mq <= c.thin_max_quads; }
+
+// ---- small networks: many steps per launch ----------------------------------------------------
+// A network of at most SMALL_MAX_N neurons whose synapse planes hold at most the launch
+// configuration's small_max_slots slots is advanced by one CTA through many steps in one launch.
+// Each step runs the passes of a bg3_step call in their order — the neuron pass (device noise as
+// k_neurons_device, injected noise as k_neurons_inject), the spike arrivals and, for the STDP
+// kinds, the post-spike learning (as deliver_net and stdp_post_net), and the synapse sweep with
+// the summation (thin_rows) — with block barriers between them, which also make each pass's
+// global writes visible to the next.  A step of a 100-neuron network is then a few microseconds
+// of on-chip latency instead of two or three kernel launches.  The step counter, its delivery
+// copy and the injected stream's cursor are kept in registers and stored at the end.  No thread
+// waits on another block, so nothing here can wait forever.
+constexpr int SMALL_THREADS = 512;
+constexpr int SMALL_WARPS = SMALL_THREADS / 32;
+
+// Injected noise: the reference CPU order, neurons walked from the top in chunks of the block
+// (k_neurons_inject with a block of SMALL_THREADS); returns the step's number of draws.
+__device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsigned long long t,
+                                                          unsigned long long cursor,
+                                                          int *warp_tot, long long *s_running)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) *s_running = 0;
+    __syncthreads();
+    for (int top = n.N - 1; top >= 0; top -= SMALL_THREADS) {
+        const int i = top - (int)threadIdx.x;
+        NeuronIn x;
+        if (i >= 0) neuron_load(n, i, x);
+        const int br = (i >= 0) ? neuron_branch(x) : BR_REFRACTORY;
+        const bool integ = (i >= 0) && br == BR_INTEGRATE;
+        const unsigned m = __ballot_sync(0xffffffffu, integ);
+        const int in_warp = __popc(m & ((1u << lane) - 1));
+        if (lane == 31) warp_tot[warp] = __popc(m);
+        __syncthreads();
+        if (warp == 0) {
+            const int v = lane < SMALL_WARPS ? warp_tot[lane] : 0;
+            int y = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int z = __shfl_up_sync(0xffffffffu, y, o);
+                if (lane >= o) y += z;
+            }
+            if (lane < SMALL_WARPS) warp_tot[lane] = y - v;  // exclusive prefix of warp totals
+        }
+        __syncthreads();
+        const long long running = *s_running;
+        bool fired = false;
+        if (i >= 0) {
+            float noise = 0.0f;
+            if (integ) {
+                const long long pos = (long long)cursor + running + warp_tot[warp] + in_warp;
+                if (pos < n.noise_len) noise = n.noise_buf[pos];
+                else set_err(n, ERR_NOISE_EXHAUSTED);
+            }
+            fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+            n.sp[i] = 0.0f;
+        }
+        ring_push(n, t, fired, i);
+        __syncthreads();
+        if (threadIdx.x == SMALL_THREADS - 1) *s_running = running + warp_tot[warp] + __popc(m);
+        __syncthreads();
+    }
+    return *s_running;
+}
+
+template <int SYN, bool INJECT>
+__global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_constant__ NetDev n,
+                                                             int nsteps)
+{
+    __shared__ int warp_tot[SMALL_WARPS];
+    __shared__ long long s_running;
+    __shared__ int s_moff[BG3_MAX_DELAYS + 1];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned long long t = *n.step;
+    unsigned long long cursor = INJECT ? *n.noise_cursor : 0ull;
+    for (int s = 0; s < nsteps; s++, t++) {
+        // ---- neuron pass of step t
+        if (INJECT) {
+            cursor += (unsigned long long)small_neurons_inject(n, t, cursor, warp_tot, &s_running);
+        } else {
+            for (int i0 = 0; i0 < n.N; i0 += SMALL_THREADS) {
+                const int i = i0 + tid;
+                bool fired = false;
+                if (i < n.N) {
+                    NeuronIn x;
+                    neuron_load(n, i, x);
+                    const int br = neuron_branch(x);
+                    const float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
+                    fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+                    n.sp[i] = 0.0f;
+                }
+                ring_push(n, t, fired, i);
+            }
+        }
+        if (tid == 0) {
+            int off = 0;
+            for (int c = 0; c < n.n_delays; c++) {
+                s_moff[c] = off;
+                const int D = n.ltab[c];
+                if (D > 0 && (unsigned long long)D <= t)
+                    off += min(n.ring_n[(t - (unsigned long long)D) & (BG3_RING - 1)], n.N);
+            }
+            s_moff[n.n_delays] = off;
+        }
+        __syncthreads();
+        // ---- spike arrivals of step t: one warp per (delay class, neuron that fired) item;
+        // every synapse has one source, which fired once, so no two lanes touch one slot
+        const int M = s_moff[n.n_delays];
+        for (int item = warp; item < M; item += SMALL_WARPS) {
+            int c = 0;
+            while (item >= s_moff[c + 1]) c++;
+            const unsigned long long tf = t - (unsigned long long)n.ltab[c];
+            const int src = n.ring[(size_t)(tf & (BG3_RING - 1)) * n.N + (item - s_moff[c])];
+            const size_t ci = (size_t)c * n.N + src;
+            const uint32_t b = n.outBegin[ci], k = n.outCount[ci];
+            for (uint32_t j = (uint32_t)lane; j < k; j += 32)
+                deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, t, src);
+        }
+        if (tid == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;  // for the next neuron pass
+        __syncthreads();
+        if (SYN >= 2) {
+            // post-spike learning of the neurons that fired at step t, after the arrivals
+            const int slot = (int)(t & (BG3_RING - 1));
+            const int m = min(n.ring_n[slot], n.N);
+            for (int e = warp; e < m; e += SMALL_WARPS) {
+                const int d = n.ring[(size_t)slot * n.N + e];
+                const int cnt = (int)n.count[d];
+                for (int k = lane; k < cnt; k += 32) {
+                    const size_t p = slot_pos(k, d, n.Mq);
+                    n.ev[p].W = stdp_post(n, n.stdp[n.stype[p]], n.ev[p].W, n.src[p], d,
+                                          n.ltab[n.lcls[p]], t);
+                }
+            }
+            __syncthreads();
+        }
+        // ---- synapse sweep and summation of step t: one warp per 32-dest tile
+        for (int tile = warp; tile < n.ntiles; tile += SMALL_WARPS) {
+            const float acc = thin_rows(n, tile, thin_quads(n, tile), lane);
+            const int d = tile * SW_DESTS + lane;
+            if (d < n.N) n.sp[d] = acc;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        *n.step = t;
+        *n.dstep = t;
+        if (INJECT) *n.noise_cursor = cursor;
+        if (t >= 0xffffff00ull) set_err(n, ERR_STEP_RANGE);
+    }
+}
+
+bool small_eligible(const NetDev &h, const LaunchCfg &c)
+{
+    return h.N <= SMALL_MAX_N && (long long)h.Np * h.Mq * 4 <= (long long)c.small_max_slots;
+}
+
+// nsteps steps of a small network in one launch (small_eligible).
+void launch_small(const NetDev &h, int nsteps, cudaStream_t s)
+{
+    const bool inj = h.noise_mode == 1;
+    switch (h.syn_kind * 2 + (inj ? 1 : 0)) {
+    case 2: k_small_run<1, false><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    case 3: k_small_run<1, true><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    case 4: k_small_run<2, false><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    case 5: k_small_run<2, true><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    case 6: k_small_run<3, false><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    case 7: k_small_run<3, true><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    case 1: k_small_run<0, true><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    default: k_small_run<0, false><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
+    }
+}
 
 // ---- launchers -------------------------------------------------------------------------------
 

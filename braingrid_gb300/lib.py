@@ -66,7 +66,8 @@ class StdpConstants(ctypes.Structure):
 class LaunchCfg(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int32) for k in ("sweep_stages", "thin_max_quads", "thin_warps",
                                               "deliver_blocks", "growth_threads", "sweep_dests",
-                                              "deliver_early", "izh_hw_every")]
+                                              "deliver_early", "izh_hw_every",
+                                              "small_max_slots")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -704,6 +705,11 @@ class Network:
 
     def enable_timing(self, on=True):
         check(self.L.bg3_enable_timing(self.h, 1 if on else 0), "bg3_enable_timing")
+
+    @property
+    def launches(self):
+        """Kernels this network has launched so far (bg3_kernel_times)."""
+        return self.kernel_times()[3]
 
     def kernel_times(self):
         a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()

@@ -413,6 +413,11 @@ typedef struct {
                                  update's double-precision expression on the FP64 pipe, the others
                                  on the integer pipe (an exact restatement): 0 .. 8, 0 = none,
                                  1 = all (default).  Same results either way.                        */
+    int32_t small_max_slots;  /* a network of at most 2,048 neurons whose synapse planes hold at most
+                                 this many slots (neurons rounded up to 32 x max synapses rounded up
+                                 to 4) runs up to 4,096 whole steps per launch on one CTA, with no
+                                 launch between its passes (default 65,536; 0: never).  Same
+                                 results either way.                                                */
 } bg3_launch_cfg;
 int bg3_get_launch(bg3_net *net, bg3_launch_cfg *cfg);
 int bg3_set_launch(bg3_net *net, const bg3_launch_cfg *cfg);

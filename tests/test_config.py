@@ -45,7 +45,8 @@ def test_mtrand_matches_the_oracle_generator():
     assert_same("inRange", v, (u.astype(np.float32) * np.float32(5)) + np.float32(2))
 
 
-NAMES = [c["name"] for c in CASES if c["name"] != "c0_fp64"]
+# the FP64 reference runs are long-run comparison bases with no setup arrays kept
+NAMES = [c["name"] for c in CASES if not c.get("fp64")]
 
 
 @pytest.mark.parametrize("name", NAMES)

@@ -90,18 +90,18 @@ def test_resume_continues_bit_exact(name, noise):
     net2.close()
 
 
-# Checkpoint layout (this library's own format): a 136-byte header whose last 8 bytes are an
+# Checkpoint layout (this library's own format): a 144-byte header whose last 8 bytes are an
 # FNV-1a 64 checksum of everything after it, the saved descriptor (netdev_bytes), the decay and
 # delay tables, the injected noise, then every device array as [uint64 bytes][bytes] in a fixed
 # order: 'count' is the 34th array, 'ring_n' the 27th.
-HDR = 136
+HDR = 144
 ARR_COUNT, ARR_RING_N = 33, 26
 
 
 def array_offset(ck, index):
     netdev = int(ck[12:16].view(np.uint32)[0])
-    noise = int(ck[104:112].view(np.int64)[0])
-    n_dtab, n_ltab = (int(v) for v in ck[112:120].view(np.uint32))
+    noise = int(ck[112:120].view(np.int64)[0])
+    n_dtab, n_ltab = (int(v) for v in ck[120:128].view(np.uint32))
     p = HDR + netdev + 4 * n_dtab + 4 * n_ltab + 4 * noise
     for _ in range(index):
         p += 8 + int(ck[p:p + 8].view(np.uint64)[0])
