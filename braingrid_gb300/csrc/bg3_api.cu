@@ -398,6 +398,7 @@ int bg3_create(const bg3_net_desc *desc, bg3_net **out)
     A(outBegin, N * BG3_MAX_DELAYS) A(outCount, N * BG3_MAX_DELAYS) A(outFill, N * BG3_MAX_DELAYS)
     A(outMap, S)
     A(radii, N) A(rates, N) A(xloc, N) A(yloc, N) A(grow_exp, (size_t)max_spikes + 1)
+    A(grow_rmax, 1)
     A(burstiness, (size_t)std::max(h.n_burst_bins, 1)) A(spikes_hist, (size_t)std::max(h.n_spike_bins, 1))
     A(rates_hist, (size_t)(D.max_epochs + 1) * N) A(radii_hist, (size_t)(D.max_epochs + 1) * N)
     if (D.neuron_kind == BG3_NEURON_IZH) {
@@ -566,9 +567,16 @@ int bg3_upload_layout(bg3_net *n, const float *x, const float *y, const int32_t 
         if (ntype[i] != 1 && ntype[i] != 2) return BG3_EINVAL;
         t[i] = (int8_t)ntype[i];
     }
+    // the reference's grid (Layouts/Layout.cpp:41-52: xloc = i % width, yloc = i / width)?
+    const int W = n->desc.width, H = n->desc.height;
+    bool grid = W > 0 && H > 0 && (size_t)W * (size_t)H == N;
+    for (size_t i = 0; grid && i < N; i++)
+        grid = x[i] == (float)(i % (size_t)W) && y[i] == (float)(i / (size_t)W);
+    n->h.grid_w = grid ? W : 0;
+    n->h.grid_h = grid ? H : 0;
     int rc;
     if ((rc = h2d(n, n->h.xloc, x, N)) || (rc = h2d(n, n->h.yloc, y, N)) ||
-        (rc = h2d(n, n->h.ntype, t.data(), N)))
+        (rc = h2d(n, n->h.ntype, t.data(), N)) || (rc = push_desc(n)))
         return rc;
     CK(cudaStreamSynchronize(n->stream));
     return BG3_OK;
@@ -2041,7 +2049,8 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
     X(C1) X(C2) X(Trefract) X(sp) X(refr) X(spikeCount) X(spikeCountOffset) X(history) X(ntype)   \
     X(Aconst) X(Bconst) X(Cconst) X(Dconst) X(u_izh) X(C3) X(ring) X(ring_n) X(psr) X(dcls)       \
     X(lcls) X(ev) X(src) X(stype) X(count) X(dtab) X(ltab) X(outBegin) X(outCount) X(outMap)      \
-    X(outFill) X(radii) X(rates) X(xloc) X(yloc) X(grow_exp) X(burstiness) X(spikes_hist)         \
+    X(outFill) X(radii) X(rates) X(xloc) X(yloc) X(grow_exp) X(grow_rmax) X(burstiness)           \
+    X(spikes_hist)                                                                                \
     X(rates_hist) X(radii_hist) X(reg_values) X(reg_shift) X(pois_mask) X(pois_nisi) X(in_psr)    \
     X(in_decay) X(in_queue) X(in_delay) X(in_ev) X(isi_begin) X(isi_vals) X(isi_cursor)
 
@@ -2317,7 +2326,8 @@ int bg3_checkpoint_load(bg3_net *n, const void *buf, uint64_t len)
         sv.n_burst_bins != h.n_burst_bins || sv.n_spike_bins != h.n_spike_bins ||
         sv.max_epochs != h.max_epochs || sv.n_dcls != (int32_t)hd.n_dtab ||
         sv.n_delays != (int32_t)hd.n_ltab || sv.n_expc < 0 || sv.n_expc > BG3_MAX_EXPC ||
-        sv.n_pcls < 0 || sv.n_pcls > BG3_MAX_PCLS || sv.input_kind < 0 || sv.input_kind > 2)
+        sv.n_pcls < 0 || sv.n_pcls > BG3_MAX_PCLS || sv.input_kind < 0 || sv.input_kind > 2 ||
+        sv.grid_w < 0 || sv.grid_h < 0 || (long long)sv.grid_w * sv.grid_h != (sv.grid_w ? sv.N : 0))
         return BG3_EINVAL;
     for (int t = 0; t < 4; t++)
         if (sv.t_dcls[t] < 0 || sv.t_dcls[t] >= BG3_MAX_DCLS || sv.t_lcls[t] < 0 ||

@@ -2,10 +2,11 @@
 //
 //   k_growth_radii     rates = spikeCount / T; radii += T * rho * outgrowth      (O(N))
 //   k_growth_existing  W of every in-use synapse from the overlap area of its pair (O(S))
-//   k_growth_add       one CTA per destination scans all sources in ascending order, computes the
-//                      frontier distance / overlap area, and appends the new synapses in source
-//                      order after the row's in-use prefix                      (O(N^2), no N^2
-//                                                                                storage)
+//   k_growth_rmax      the largest radius (one CTA)
+//   k_growth_add       one CTA per destination scans the sources in ascending order (on the grid
+//                      layout only the window within the largest radius), computes the frontier
+//                      distance / overlap area, and appends the new synapses in source order after
+//                      the row's in-use prefix            (O(N^2) pairs, no N^2 storage)
 //   k_out_count/scan/fill  outgoing CSR rebuild per delay class (createSynapseImap)
 //   k_record_epoch     recorder histograms, rates/radii history, radius clamp, spike-count roll
 #include "bg3_internal.cuh"
@@ -81,8 +82,64 @@ __global__ void k_growth_existing(const NetDev *nets)
     }
 }
 
+// The largest radius after the epoch's radius update (negative radii count as 0), for the
+// overlap scan's window: one CTA.
+__global__ void __launch_bounds__(1024) k_growth_rmax(const NetDev *nets)
+{
+    const NetDev &n = nets[0];
+    __shared__ float wmax[32];
+    float m = 0.0f;
+    for (int i = threadIdx.x; i < n.N; i += blockDim.x) m = fmaxf(m, n.radii[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *n.grow_rmax = m;
+    }
+}
+
+// The sources a destination's overlap scan visits, in ascending index order: all N, or on the
+// reference's grid layout only the square window of rows and columns within K of the
+// destination, where K + 1 > fl(rmax + r_d).  Outside it |dx| or |dy| >= fl(rmax + r_d), so
+// len = sqrtf(dx^2 + dy^2) >= fl(r_s + r_d) (grid coordinates are whole numbers, their squares and
+// sums exact; sqrtf and rounding are monotone) and the pair's delta = len - (r_s + r_d) is not
+// negative: no overlap, exactly as the full scan finds.  Candidate c is source
+// (y0 + c / cw) * W + x0 + c % cw.
+struct ScanWindow {
+    int x0, y0, cw, count;  // cw = 0: the full scan (candidate c is source c)
+};
+__device__ __forceinline__ ScanWindow scan_window(const NetDev &n, int d, float rd)
+{
+    ScanWindow w = {0, 0, 0, n.N};
+    const int W = n.grid_w, H = n.grid_h;
+    if (W <= 0 || H <= 0 || (long long)W * H != (long long)n.N) return w;
+    const float bound = *n.grow_rmax + rd;
+    if (!(bound >= 0.0f) || bound > (float)(W + H)) return w;  // NaN, or a window wider than the grid
+    const int K = (int)ceilf(bound) - 1;
+    if (K < 0) {
+        w.count = 0;
+        return w;
+    }
+    const int xd = d % W, yd = d / W;
+    w.x0 = max(0, xd - K);
+    w.y0 = max(0, yd - K);
+    w.cw = min(W - 1, xd + K) - w.x0 + 1;
+    w.count = w.cw * (min(H - 1, yd + K) - w.y0 + 1);
+    return w;
+}
+__device__ __forceinline__ int window_source(const NetDev &n, const ScanWindow &w, int c)
+{
+    if (w.cw == 0) return c;
+    return (w.y0 + c / w.cw) * n.grid_w + w.x0 + c % w.cw;
+}
+
 // New synapses (ConnGrowth.cpp:441-454, AllSynapses::addSynapse :357-377, create* of
-// AllSpikingSynapses.cpp:192-240 / AllDSSynapses.cpp:180-218).  One CTA per destination.
+// AllSpikingSynapses.cpp:192-240 / AllDSSynapses.cpp:180-218).  One CTA per destination, over
+// the sources of its scan window in ascending order.
 template <int ADD_THREADS>
 __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
 {
@@ -105,8 +162,10 @@ __global__ void __launch_bounds__(ADD_THREADS) k_growth_add(const NetDev *nets)
     const float xd = n.xloc[d], yd = n.yloc[d], rd = n.radii[d];
     const int8_t td = n.ntype[d];
     const unsigned long long t = *n.step;
-    for (int base = 0; base < n.N; base += ADD_THREADS) {
-        int s = base + threadIdx.x;
+    const ScanWindow win = scan_window(n, d, rd);
+    for (int base = 0; base < win.count; base += ADD_THREADS) {
+        const int c = base + threadIdx.x;
+        const int s = c < win.count ? window_source(n, win, c) : n.N;
         float a = 0.0f;
         bool add = false;
         if (s < n.N && s != d && !((existing[s >> 5] >> (s & 31)) & 1u)) {
@@ -272,6 +331,7 @@ void launch_growth(const NetDev &h, const NetDev *d_net, int epoch, int add_thre
     k_growth_radii<<<nb, 256, 0, s>>>(d_net);
     int sb = 152 * 8;
     k_growth_existing<<<sb, 256, 0, s>>>(d_net);
+    k_growth_rmax<<<1, 1024, 0, s>>>(d_net);
     size_t smem = (size_t)((h.N + 31) / 32) * sizeof(uint32_t);
     if (add_threads == 128) k_growth_add<128><<<h.N, 128, smem, s>>>(d_net);
     else if (add_threads == 512) k_growth_add<512><<<h.N, 512, smem, s>>>(d_net);

@@ -139,6 +139,10 @@ struct NetDev {
     uint32_t *outBegin, *outCount, *outMap, *outFill;
     // growth
     float *radii, *rates, *xloc, *yloc;
+    // the layout is the reference's grid (xloc = i % grid_w, yloc = i / grid_w), so the overlap
+    // scan of a destination can stop at the sources beyond the largest radius; 0 otherwise
+    int32_t grid_w, grid_h;
+    float *grow_rmax;  // [1]: the largest radius of the epoch's growth pass
     float g_epsilon, g_beta, g_rho, g_target_rate, g_min_radius, g_start_radius, g_max_rate;
     float *grow_exp;   // [max_spikes + 1]: the outgrowth exp for each spike count (host libm)
     // recorder

@@ -6,8 +6,13 @@ from . import netgen
 # The plain single network: 100x100 LIF + DS + ConnGrowth, max 1000 synapses per neuron.
 # At the stated start radius (0.4) no pair overlaps, so throughput is measured on a pre-grown
 # state: radii ~ U[8.35, 8.45] wired by one device growth pass (~7.6 M synapses), weights scaled.
-PLAIN = dict(width=100, height=100, max_syn=1000, radius=8.4, weight_scale=0.003, seed=7,
-          frac_inh=0.10, epoch_duration=1.0, max_firing_rate=200, max_epochs=10)
+# Without input this network either stays near silent (0.03 Hz at weight scale 0.003) or, with
+# stronger weights, bursts to saturation; a Poisson drive of every neuron (the reference's
+# SInputPoisson: 10 Hz, weight 9.5, i.e. 95 nA per input synapse) with recurrent weights scaled
+# by 0.0003 holds it at about the growth rule's 1 Hz target rate (~1,000 spike arrivals per step).
+PLAIN = dict(width=100, height=100, max_syn=1000, radius=8.4, weight_scale=0.0003, seed=7,
+             frac_inh=0.10, epoch_duration=1.0, max_firing_rate=200, max_epochs=10,
+             poisson=dict(fr_mean=10.0, weight=9.5))
 
 
 def build(w=PLAIN):
@@ -16,13 +21,17 @@ def build(w=PLAIN):
                                   max_firing_rate=w["max_firing_rate"],
                                   max_epochs=w["max_epochs"], noise_seed=w["seed"])
     netgen.pregrow(net, spec, w["radius"], weight_scale=w["weight_scale"])
+    if w.get("poisson"):
+        arr, lam = netgen.poisson_arrays(spec, w["poisson"]["fr_mean"], w["poisson"]["weight"])
+        net.input_poisson(lam, seed=w["seed"], step=net.sim_step, **arr)
     return spec, net
 
 
 # The 36-network growth sweep: targetRate {0.1, 1.0, 1.9} Hz x excitatory fraction {0.80, 0.90,
-# 0.98} x 4 seeds, sizes cycling 30x30, 50x50, 70x70, 100x100; the plain network's model otherwise, with the
-# same pre-grown radius and weight scale.
+# 0.98} x 4 seeds, sizes cycling 30x30, 50x50, 70x70, 100x100; the plain network's model
+# otherwise, with the same pre-grown radius, weights scaled by 0.003 and no external input.
 SWEEP36_SIZES = [30, 50, 70, 100]
+SWEEP36_BASE = dict(PLAIN, weight_scale=0.003, poisson=None)
 
 
 def sweep36_members():
@@ -32,8 +41,8 @@ def sweep36_members():
         for fe in (0.80, 0.90, 0.98):
             for seed in range(4):
                 side = SWEEP36_SIZES[k % 4]
-                out.append(dict(PLAIN, width=side, height=side, frac_inh=round(1.0 - fe, 2),
-                                seed=seed, target_rate=tr))
+                out.append(dict(SWEEP36_BASE, width=side, height=side,
+                                frac_inh=round(1.0 - fe, 2), seed=seed, target_rate=tr))
                 k += 1
     return out
 
