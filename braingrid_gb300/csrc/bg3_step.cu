@@ -1032,11 +1032,31 @@ bool sweep_is_thin(const NetDev &h, const LaunchCfg &c) { return h.Mq <= c.thin_
 constexpr int SMALL_THREADS = 512;
 constexpr int SMALL_WARPS = SMALL_THREADS / 32;
 
+// ring_push with the spike counts of the ring's slots held in shared memory (the one-CTA path
+// keeps them there for the whole launch and stores them back at its end).
+__device__ __forceinline__ void ring_push_smem(const NetDev &n, int *s_ring_n,
+                                               unsigned long long t, bool fired, int i)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, fired);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    const int slot = (int)(t & (BG3_RING - 1));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&s_ring_n[slot], __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (fired) {
+        const int pos = base + __popc(mask & ((1u << lane) - 1));
+        if (pos < n.N) n.ring[(size_t)slot * n.N + pos] = i;
+        else set_err(n, ERR_SPIKE_LIST);
+    }
+}
+
 // Injected noise: the reference CPU order, neurons walked from the top in chunks of the block
 // (k_neurons_inject with a block of SMALL_THREADS); returns the step's number of draws.
 __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsigned long long t,
                                                           unsigned long long cursor,
-                                                          int *warp_tot, long long *s_running)
+                                                          int *warp_tot, long long *s_running,
+                                                          int *s_ring_n)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) *s_running = 0;
@@ -1074,7 +1094,7 @@ __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsig
             fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
             n.sp[i] = 0.0f;
         }
-        ring_push(n, t, fired, i);
+        ring_push_smem(n, s_ring_n, t, fired, i);
         __syncthreads();
         if (threadIdx.x == SMALL_THREADS - 1) *s_running = running + warp_tot[warp] + __popc(m);
         __syncthreads();
@@ -1089,13 +1109,19 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
     __shared__ int warp_tot[SMALL_WARPS];
     __shared__ long long s_running;
     __shared__ int s_moff[BG3_MAX_DELAYS + 1];
+    __shared__ int s_ring_n[BG3_RING];        // the ring's spike counts, stored back at the end
+    __shared__ int s_ltab[BG3_MAX_DELAYS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned long long t = *n.step;
     unsigned long long cursor = INJECT ? *n.noise_cursor : 0ull;
+    if (tid < BG3_RING) s_ring_n[tid] = n.ring_n[tid];
+    if (tid < BG3_MAX_DELAYS) s_ltab[tid] = tid < n.n_delays ? n.ltab[tid] : 0;
+    __syncthreads();
     for (int s = 0; s < nsteps; s++, t++) {
         // ---- neuron pass of step t
         if (INJECT) {
-            cursor += (unsigned long long)small_neurons_inject(n, t, cursor, warp_tot, &s_running);
+            cursor += (unsigned long long)small_neurons_inject(n, t, cursor, warp_tot, &s_running,
+                                                               s_ring_n);
         } else {
             for (int i0 = 0; i0 < n.N; i0 += SMALL_THREADS) {
                 const int i = i0 + tid;
@@ -1108,18 +1134,25 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
                     fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
                     n.sp[i] = 0.0f;
                 }
-                ring_push(n, t, fired, i);
+                ring_push_smem(n, s_ring_n, t, fired, i);
             }
         }
-        if (tid == 0) {
-            int off = 0;
-            for (int c = 0; c < n.n_delays; c++) {
-                s_moff[c] = off;
-                const int D = n.ltab[c];
+        __syncthreads();
+        if (warp == 0) {
+            // arrival items per delay class, then their offsets
+            int m = 0;
+            if (lane < n.n_delays) {
+                const int D = s_ltab[lane];
                 if (D > 0 && (unsigned long long)D <= t)
-                    off += min(n.ring_n[(t - (unsigned long long)D) & (BG3_RING - 1)], n.N);
+                    m = min(s_ring_n[(t - (unsigned long long)D) & (BG3_RING - 1)], n.N);
             }
-            s_moff[n.n_delays] = off;
+            int x = m;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane <= n.n_delays) s_moff[lane] = x - m;  // exclusive prefix; the last is M
         }
         __syncthreads();
         // ---- spike arrivals of step t: one warp per (delay class, neuron that fired) item;
@@ -1128,19 +1161,19 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
         for (int item = warp; item < M; item += SMALL_WARPS) {
             int c = 0;
             while (item >= s_moff[c + 1]) c++;
-            const unsigned long long tf = t - (unsigned long long)n.ltab[c];
+            const unsigned long long tf = t - (unsigned long long)s_ltab[c];
             const int src = n.ring[(size_t)(tf & (BG3_RING - 1)) * n.N + (item - s_moff[c])];
             const size_t ci = (size_t)c * n.N + src;
             const uint32_t b = n.outBegin[ci], k = n.outCount[ci];
             for (uint32_t j = (uint32_t)lane; j < k; j += 32)
                 deliver_hit<SYN>(n, n.outMap[b + j], (uint32_t)tf, t, src);
         }
-        if (tid == 0) n.ring_n[(t + 1) & (BG3_RING - 1)] = 0;  // for the next neuron pass
+        if (tid == 0) s_ring_n[(t + 1) & (BG3_RING - 1)] = 0;  // for the next neuron pass
         __syncthreads();
         if (SYN >= 2) {
             // post-spike learning of the neurons that fired at step t, after the arrivals
             const int slot = (int)(t & (BG3_RING - 1));
-            const int m = min(n.ring_n[slot], n.N);
+            const int m = min(s_ring_n[slot], n.N);
             for (int e = warp; e < m; e += SMALL_WARPS) {
                 const int d = n.ring[(size_t)slot * n.N + e];
                 const int cnt = (int)n.count[d];
@@ -1160,6 +1193,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
         }
         __syncthreads();
     }
+    if (tid < BG3_RING) n.ring_n[tid] = s_ring_n[tid];
     if (tid == 0) {
         *n.step = t;
         *n.dstep = t;

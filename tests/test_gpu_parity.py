@@ -305,7 +305,8 @@ def test_free_running_on_own_growth_weights(name, epochs):
 def test_benchmark_shape_step_locked():
     """The benchmark network's shape: 100x100 LIF + DS, 1,000 slots per neuron, one growth pass
     at radius U[8.35, 8.45] wiring ~7.6 M synapses on the 32-dest TMA sweep path; maps and
-    per-pair counts bit-exact after the GPU's own growth pass, weights within 1e-5, then both
+    per-pair counts bit-exact after the GPU's own growth pass, weights within 1e-5 relative or
+    1e-7 of the largest weight (see below), then both
     sides take the oracle's weights times the benchmark's 0.003 (float products, the same bits on
     both) and every membrane starts just below threshold, so the first steps deliver heavy
     bursts; 2,000 steps step-locked with injected noise, neuron state checked every 250 steps and
@@ -327,7 +328,14 @@ def test_benchmark_shape_step_locked():
     sy = net.download_synapses()
     assert_same("counts", sy["counts"], o.arr("counts"))
     used = o.arr("in_use").astype(bool)
-    np.testing.assert_allclose(sy["W"][used], o.arr("W")[used], rtol=1e-5, atol=0)
+    # A pair whose lenses barely overlap has angles near 0, where the reference's
+    # 2 theta - sin 2 theta cancels: a one-ulp difference between glibc's acosf and the
+    # correctly rounded acos grows there by ~6 / (2 theta)^2 (measured: 972 of 7.6 M weights
+    # differ by up to 2.2e-4 relative, all below 2e-9 against a largest weight of 2e-6, absolute
+    # differences at most 2.1e-14).  Such weights are compared against the network's scale.
+    wg, wo = sy["W"][used].astype(np.float64), o.arr("W")[used].astype(np.float64)
+    tol = 1e-5 * np.abs(wo) + 1e-7 * float(np.abs(wo).max())
+    assert np.all(np.abs(wg - wo) <= tol), float(np.max(np.abs(wg - wo) - tol))
     o.arr("W")[:] = o.arr("W") * np.float32(0.003)
     net.upload_weights(o.arr("W"))
     o.arr("Vm")[:] = rs.uniform(13.0e-3, 15.2e-3, N).astype(np.float32)
