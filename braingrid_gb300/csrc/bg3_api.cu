@@ -1780,7 +1780,7 @@ static bool cfg_valid(const bg3_launch_cfg *c)
            c->thin_warps <= 32 && c->deliver_blocks >= 1 && c->deliver_blocks <= 65535 &&
            (c->growth_threads == 128 || c->growth_threads == 256 || c->growth_threads == 512) &&
            (c->sweep_dests == 16 || c->sweep_dests == 32) &&
-           (c->deliver_early == 0 || c->deliver_early == 1) && c->izh_hw_every >= 0 &&
+           (c->deliver_early == 0 || c->deliver_early == 1) && c->izh_hw_every >= -1 &&
            c->izh_hw_every <= 8 && c->small_max_slots >= 0;
 }
 static LaunchCfg cfg_from(const bg3_launch_cfg &c)
@@ -1911,7 +1911,7 @@ static int tune(LaunchCfg &cur, bool thick, bool thin, int mq, bool batch, bool 
     if ((thin || mq <= 64) && (rc = try_param(&LaunchCfg::thin_warps, {4, 8, 16}))) return rc;
     if ((rc = try_param(&LaunchCfg::deliver_blocks, {152, 304, 608}))) return rc;
     if ((rc = try_param(&LaunchCfg::deliver_early, {0, 1}))) return rc;
-    if (izh && (rc = try_param(&LaunchCfg::izh_hw_every, {0, 1, 2, 3, 4}))) return rc;
+    if (izh && (rc = try_param(&LaunchCfg::izh_hw_every, {-1, 0, 1, 2, 3, 4}))) return rc;
     return BG3_OK;
 }
 

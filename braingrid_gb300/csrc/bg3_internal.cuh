@@ -537,11 +537,118 @@ __device__ __forceinline__ float izh_v_fp64(float Vint, float u, float C3, float
     return (float)((double)Vh * 0.001 + (double)c2sp);
 }
 
-// hw: evaluate the Izhikevich double expression with the hardware FP64 pipe instead of its
-// integer-pipe restatement (the same bits either way).
+// ---- the Izhikevich double expression in float-float arithmetic ------------------------------
+// A float-float value is hi + lo with |lo| <= ulp(hi) / 2 (Dekker, "A floating-point technique
+// for extending the available precision", 1971; Knuth's two-sum): about 48 significant bits, kept
+// with FP32 additions and fused multiply-adds (each fmaf rounds once, so two_prod's error term is
+// exact; -fmad=false stops only the contraction of separate operations).  The chain of the
+// reference's double operations is evaluated this way to within a bound E of the reference's own
+// double result; where that result's float rounding is certain (the value lies more than E away
+// from every rounding boundary, the midpoints between floats) the float is returned, and
+// otherwise ok = false and the caller evaluates the expression in hardware FP64.  The same bits
+// as the double evaluation, with the FP64 pipe used only for the rare uncertain values.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b)
+{
+    const float s = a + b, bb = s - a;
+    return FF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b)  // |a| >= |b| or a == 0
+{
+    const float s = a + b;
+    return FF{s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_add_f(FF a, float b)
+{
+    FF s = ff_two_sum(a.hi, b);
+    s.lo = s.lo + a.lo;
+    return ff_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ FF ff_mul_f(FF a, float b)
+{
+    const float p = a.hi * b;
+    float e = __fmaf_rn(a.hi, b, -p);
+    e = __fmaf_rn(a.lo, b, e);
+    return ff_fast_two_sum(p, e);
+}
+// Rounds a float-float value to float when no rounding boundary lies within err of it.
+__device__ __forceinline__ bool ff_round(FF a, float err, float &out)
+{
+    const uint32_t m = __float_as_uint(a.hi) & 0x7fffffffu;
+    if (m < 0x00800001u || m >= 0x7f000000u || !(err < 1e30f)) return false;  // tiny, huge, NaN
+    const float up = __uint_as_float(m + 1u) - __uint_as_float(m);    // gap above |hi|
+    const float dn = __uint_as_float(m) - __uint_as_float(m - 1u);    // gap below |hi|
+    const bool neg = (__float_as_uint(a.hi) >> 31) != 0u;
+    // distances from hi + lo to the midpoints above and below hi (on the real line)
+    const float half_hi = 0.5f * (neg ? dn : up), half_lo = 0.5f * (neg ? up : dn);
+    if (half_hi - a.lo <= err || half_lo + a.lo <= err) return false;
+    out = a.hi;
+    return true;
+}
+
+// (float)(v + C3 (0.04 v v + (double)(5 v) + 140 - u)) and (float)((double)Vb * 0.001 + c2sp)
+// as izh_v_fp64 computes them, from float-float arithmetic: the constants 0.04 and 0.001 as
+// three floats (exact to ~2^-72); every operation of the chain adds at most ~2^-46 of the
+// magnitudes it combines and the reference's seven double roundings ~2^-53 each, so
+// E = 2^-40 x (|C3| x M + |Vb|), M = 0.04 v^2 + 5 |v| + 140 + |u|, bounds the distance to the
+// reference's double with a wide margin (and likewise for the second expression).
+__device__ __forceinline__ float izh_v_ff(float Vint, float u, float C3, float c2sp, bool &ok)
+{
+    // the double constants split into three floats each (their sum is the double exactly)
+    constexpr float K04H = (float)0.04, K04M = (float)(0.04 - (double)K04H),
+                    K04L = (float)(0.04 - (double)K04H - (double)K04M);
+    constexpr float K001H = (float)0.001, K001M = (float)(0.001 - (double)K001H),
+                    K001L = (float)(0.001 - (double)K001H - (double)K001M);
+    if (!(fabsf(Vint) < 1e4f) || !(fabsf(u) < 1e4f) || !(fabsf(C3) < 1e4f) || !(fabsf(c2sp) < 1e4f)) {
+        ok = false;
+        return 0.0f;
+    }
+    FF t = ff_mul_f(FF{K04H, K04M}, Vint);
+    t.lo = __fmaf_rn(K04L, Vint, t.lo);
+    t = ff_mul_f(t, Vint);
+    const float v5 = 5.0f * Vint;
+    t = ff_add_f(t, v5);
+    t = ff_add_f(t, 140.0f);
+    t = ff_add_f(t, -u);
+    t = ff_mul_f(t, C3);
+    t = ff_add_f(t, Vint);
+    const float M = 0.04f * Vint * Vint + fabsf(v5) + 140.0f + fabsf(u);
+    float Vb;
+    if (!ff_round(t, (fabsf(C3) * M + fabsf(t.hi)) * 0x1p-40f, Vb)) {
+        ok = false;
+        return 0.0f;
+    }
+    FF w = ff_mul_f(FF{K001H, K001M}, Vb);
+    w.lo = __fmaf_rn(K001L, Vb, w.lo);
+    w = ff_add_f(w, c2sp);
+    float Vnew;
+    if (!ff_round(w, (fabsf(Vb) * 0.001f + fabsf(c2sp)) * 0x1p-40f, Vnew)) {
+        ok = false;
+        return 0.0f;
+    }
+    return Vnew;
+}
+
+// How a neuron's Izhikevich double expression is evaluated: the integer-pipe restatement, the
+// hardware FP64 pipe, or float-float arithmetic with the FP64 pipe for uncertain roundings (the
+// same bits every way).
+enum { IZH_SOFT = 0, IZH_HW = 1, IZH_FF = 2 };
+__device__ __forceinline__ int izh_mode(const NetDev &n, int i)
+{
+    if (n.izh_hw_every < 0) return IZH_FF;
+    if (n.izh_hw_every > 0 && ((i >> 5) % n.izh_hw_every) == 0) return IZH_HW;
+    return IZH_SOFT;
+}
+
+// mode: IZH_SOFT, IZH_HW or IZH_FF (izh_mode); the same bits every way.  FFOK = false compiles
+// the float-float branch out (IZH_FF then takes the FP64 pipe), for kernels without registers
+// to spare.
+template <bool FFOK = true>
 __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const NeuronIn &x, int br,
                                              float sp, float noise, unsigned long long t,
-                                             bool hw = false)
+                                             int mode = IZH_SOFT)
 {
     const bool izh = n.neuron_kind == 1;
     if (br == BR_REFRACTORY) {
@@ -574,7 +681,11 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
         // Vm = (float)((double)Vb * 0.001 + (double)(C2 sp)), each double operation rounded once
         // the double constants 0.04, 140.0 and 0.001 as (mantissa, exponent, sign)
         float Vnew;
-        if (hw) {
+        bool ffok = false;
+        if (FFOK && mode == IZH_FF) {
+            Vnew = izh_v_ff(Vint, u, C3, x.C2 * sp, ffok);
+            if (!ffok) Vnew = izh_v_fp64(Vint, u, C3, x.C2 * sp);  // uncertain rounding
+        } else if (mode == IZH_HW || mode == IZH_FF) {
             Vnew = izh_v_fp64(Vint, u, C3, x.C2 * sp);
         } else {
             constexpr SoftD K004 = {0x147ae147ae147bull, -5, 0u};

@@ -1,7 +1,8 @@
 // Self-tests.  bg3_selftest_binary64: the integer-pipe binary64 arithmetic (SoftD,
 // bg3_internal.cuh) against the hardware on random operands (random signs, mantissas, exponents
 // in [-300, 300]) and operand pairs that nearly cancel, for add, multiply and the conversion to
-// float.  bg3_selftest_timeout: the bounded mbarrier wait of the step kernels, run out on purpose.
+// float.  bg3_selftest_izhikevich: the Izhikevich update's double expression evaluated on the
+// integer pipe and in float-float arithmetic, against the FP64 pipe.  bg3_selftest_timeout: the bounded mbarrier wait of the step kernels, run out on purpose.
 #include "../../include/bg3.h"
 #include "bg3_internal.cuh"
 #include "bg3_ptx.cuh"
@@ -63,6 +64,56 @@ __global__ void k_softd_test(uint64_t n, uint64_t seed, unsigned long long *bad)
         if (local[k]) atomicAdd(&bad[k], local[k]);
 }
 
+// The Izhikevich update's double expression (izh_v_fp64) against its integer-pipe restatement
+// (neuron_apply's IZH_SOFT branch) and its float-float evaluation (izh_v_ff), on random membrane
+// potentials in [-100, 60] mV, recovery variables in [-40, 40], C3 in [0.02, 0.5] and summation
+// inputs C2 sp in [-0.05, 0.05] V, a quarter of them drawn near the values where the float
+// rounding is close (v with few mantissa bits).
+__device__ __forceinline__ float izh_v_soft(float Vint, float u, float C3, float c2sp, bool &ok)
+{
+    constexpr SoftD K004 = {0x147ae147ae147bull, -5, 0u};
+    constexpr SoftD K140 = {0x11800000000000ull, 7, 0u};
+    constexpr SoftD K0001 = {0x10624dd2f1a9fcull, -10, 0u};
+    const SoftD vd = sd_from_float(Vint, ok);
+    SoftD t = sd_mul(K004, vd, ok);
+    t = sd_mul(t, vd, ok);
+    t = sd_add(t, sd_from_float(5.0f * Vint, ok), ok);
+    t = sd_add(t, K140, ok);
+    SoftD nu = sd_from_float(u, ok);
+    nu.s ^= 1u;
+    t = sd_add(t, nu, ok);
+    t = sd_mul(sd_from_float(C3, ok), t, ok);
+    const float Vb = sd_to_float(sd_add(vd, t, ok), ok);
+    SoftD w = sd_mul(sd_from_float(Vb, ok), K0001, ok);
+    w = sd_add(w, sd_from_float(c2sp, ok), ok);
+    return sd_to_float(w, ok);
+}
+
+__global__ void k_izh_test(uint64_t n, uint64_t seed, unsigned long long *bad)
+{
+    unsigned long long local[4] = {0, 0, 0, 0};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r1 = mix64(seed ^ (2 * i)), r2 = mix64(seed ^ (2 * i + 1));
+        const float f1 = (float)(r1 >> 40) * 0x1p-24f, f2 = (float)((r1 >> 16) & 0xffffffull) * 0x1p-24f;
+        const float f3 = (float)(r2 >> 40) * 0x1p-24f, f4 = (float)((r2 >> 16) & 0xffffffull) * 0x1p-24f;
+        float Vint = -100.0f + 160.0f * f1;
+        if ((r2 & 3ull) == 0) Vint = __uint_as_float(__float_as_uint(Vint) & 0xffffff00u);
+        const float u = -40.0f + 80.0f * f2, C3 = 0.02f + 0.48f * f3, c2sp = -0.05f + 0.1f * f4;
+        const float hw = izh_v_fp64(Vint, u, C3, c2sp);
+        bool ok = true;
+        const float sw = izh_v_soft(Vint, u, C3, c2sp, ok);
+        if (ok && __float_as_uint(sw) != __float_as_uint(hw)) local[0]++;
+        bool ffok = false;
+        const float fv = izh_v_ff(Vint, u, C3, c2sp, ffok);
+        if (!ffok) local[2]++;
+        else if (__float_as_uint(fv) != __float_as_uint(hw)) local[1]++;
+        if (!ok) local[3]++;
+    }
+    for (int k = 0; k < 4; k++)
+        if (local[k]) atomicAdd(&bad[k], local[k]);
+}
+
 // A wait that nothing ends: an mbarrier expecting one arrival that never comes, waited on by a
 // warp with the step kernels' bounded wait at limit_ns.  No copy targets the barrier, so the
 // block may leave it pending; the kernel records whether the wait gave up and how long it took,
@@ -112,6 +163,25 @@ extern "C" int bg3_selftest_binary64(uint64_t samples, uint64_t seed, uint64_t *
         return BG3_ECUDA;
     }
     k_softd_test<<<152 * 8, 256>>>(samples, seed, d);
+    unsigned long long h[4];
+    const cudaError_t e1 = cudaDeviceSynchronize();
+    const cudaError_t e2 = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) return BG3_ECUDA;
+    for (int k = 0; k < 4; k++) counts[k] = h[k];
+    return BG3_OK;
+}
+
+extern "C" int bg3_selftest_izhikevich(uint64_t samples, uint64_t seed, uint64_t *counts)
+{
+    if (!counts) return BG3_EINVAL;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return BG3_ENOMEM;
+    if (cudaMemset(d, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(d);
+        return BG3_ECUDA;
+    }
+    k_izh_test<<<152 * 8, 256>>>(samples, seed, d);
     unsigned long long h[4];
     const cudaError_t e1 = cudaDeviceSynchronize();
     const cudaError_t e2 = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);

@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(256) k_neurons_device(const __grid_constant__ 
         neuron_load(n, i, x);
         const int br = neuron_branch(x);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t,
+                                 izh_mode(n, i));
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -130,7 +131,8 @@ __global__ void __launch_bounds__(1024) k_neurons_inject(const __grid_constant__
                 if (pos < n.noise_len) noise = n.noise_buf[pos];
                 else set_err(n, ERR_NOISE_EXHAUSTED);
             }
-            fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+            fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t,
+                                 izh_mode(n, i));
             n.sp[i] = 0.0f;
         }
         ring_push(n, t, fired, i);
@@ -214,7 +216,8 @@ __global__ void __launch_bounds__(1024) k_neurons_inject_apply(const __grid_cons
             if (pos < n.noise_len) noise = n.noise_buf[pos];
             else set_err(n, ERR_NOISE_EXHAUSTED);
         }
-        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t,
+                                 izh_mode(n, i));
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -648,7 +651,8 @@ __global__ void __launch_bounds__(256) k_neurons_device_batch(const NetDev *nets
         neuron_load(n, i, x);
         const int br = neuron_branch(x);
         float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+        fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t,
+                                 izh_mode(n, i));
         n.sp[i] = 0.0f;
     }
     ring_push(n, t, fired, i);
@@ -692,7 +696,9 @@ constexpr size_t sw_smem(int st, int D)
 // update of step t + 1 (device noise); the step counter advances here only when unfused (a fused
 // sweep's next delivery advances it).
 // x: the dest's neuron values (neuron_load after pdl_wait), noise: its N(0,1) draw for step t+1.
-template <bool FUSE>
+// FF: the epilogue may evaluate Izhikevich neurons in float-float arithmetic; the TMA sweep's
+// sum warp has no registers to spare for it and uses the FP64 pipe instead (the same bits).
+template <bool FUSE, bool FF = true>
 __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid, float acc,
                                              unsigned long long t, int lane, const NeuronIn &x,
                                              float noise, int tiles)
@@ -702,9 +708,8 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
         bool fired = false;
         if (valid) {
             const int br = neuron_branch(x);
-            const bool hw = n.izh_hw_every > 0 && ((d >> 5) % n.izh_hw_every) == 0;
-            fired = neuron_apply(n, d, x, br, input_apply(n, d, x, t1, acc),
-                                 br == BR_INTEGRATE ? noise : 0.0f, t1, hw);
+            fired = neuron_apply<FF>(n, d, x, br, input_apply(n, d, x, t1, acc),
+                                     br == BR_INTEGRATE ? noise : 0.0f, t1, izh_mode(n, d));
             n.sp[d] = 0.0f;
         }
         ring_push(n, t1, fired, d);
@@ -889,7 +894,7 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
         __syncwarp();
     }
 
-    sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise, n.ntiles * (SW_DESTS / D));
+    sweep_finish<FUSE, false>(n, d, valid, acc, t, lane, x, noise, n.ntiles * (SW_DESTS / D));
 }
 
 // psr *= decay for the first nq row quads of a 32-dest tile and the sum of each dest's rows in
@@ -1091,7 +1096,8 @@ __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsig
                 if (pos < n.noise_len) noise = n.noise_buf[pos];
                 else set_err(n, ERR_NOISE_EXHAUSTED);
             }
-            fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+            fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t,
+                                 izh_mode(n, i));
             n.sp[i] = 0.0f;
         }
         ring_push_smem(n, s_ring_n, t, fired, i);
@@ -1131,7 +1137,8 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
                     neuron_load(n, i, x);
                     const int br = neuron_branch(x);
                     const float noise = (br == BR_INTEGRATE) ? normal_device(n.noise_seed, t, i) : 0.0f;
-                    fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t);
+                    fired = neuron_apply(n, i, x, br, input_apply(n, i, x, t, n.sp[i]), noise, t,
+                                 izh_mode(n, i));
                     n.sp[i] = 0.0f;
                 }
                 ring_push_smem(n, s_ring_n, t, fired, i);

@@ -161,6 +161,8 @@ def load(build_if_missing=True):
         "bg3_set_stdp_constants": ([vp, ctypes.POINTER(StdpConstants)], ctypes.c_int),
         "bg3_set_stdp_arithmetic": ([vp, ctypes.c_int], ctypes.c_int),
         "bg3_epoch_record": ([vp], ctypes.c_int),
+        "bg3_selftest_izhikevich": ([ctypes.c_uint64, ctypes.c_uint64,
+                                     ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
         "bg3_selftest_binary64": ([ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
                                   ctypes.c_int),
         "bg3_get_launch": ([vp, ctypes.POINTER(LaunchCfg)], ctypes.c_int),
@@ -783,4 +785,13 @@ def selftest_binary64(samples=1 << 26, seed=1):
     arithmetic against the hardware."""
     c = (ctypes.c_uint64 * 4)()
     check(load().bg3_selftest_binary64(int(samples), int(seed), c), "bg3_selftest_binary64")
+    return tuple(int(x) for x in c)
+
+
+def selftest_izhikevich(samples=1 << 26, seed=1):
+    """(integer-pipe mismatches, float-float mismatches, float-float values handed to the FP64
+    pipe, operand sets outside the integer pipe's range) of the Izhikevich update's double
+    expression against the FP64 pipe."""
+    c = (ctypes.c_uint64 * 4)()
+    check(load().bg3_selftest_izhikevich(int(samples), int(seed), c), "bg3_selftest_izhikevich")
     return tuple(int(x) for x in c)

@@ -386,6 +386,12 @@ int bg3_bench_steps(bg3_net *net, int64_t nsteps, int64_t flush_bytes, float *st
  * add mismatches, multiply mismatches, conversion mismatches, cases outside the restated range
  * (which the update recomputes in hardware).  No counterpart in the reference. */
 int bg3_selftest_binary64(uint64_t samples, uint64_t seed, uint64_t *counts);
+/* Self-test of the three evaluations of the Izhikevich update's double expression (the FP64
+ * pipe, its integer-pipe restatement, and float-float arithmetic that hands uncertain roundings to
+ * the FP64 pipe) on `samples` random operand sets: counts[0..3] = integer-pipe mismatches against
+ * the FP64 pipe, float-float mismatches, float-float values handed to the FP64 pipe, operand sets
+ * outside the integer pipe's restated range.  No counterpart in the reference. */
+int bg3_selftest_izhikevich(uint64_t samples, uint64_t seed, uint64_t *counts);
 /* Failure-detection self-test: one warp waits, with the bounded mbarrier wait the step kernels
  * use, on a barrier that nothing completes, for at most limit_ns (1 .. 2e9).  The wait gives up,
  * the kernel returns normally and the context stays usable: *status = BG3_ERR_TIMEOUT, and
@@ -412,7 +418,9 @@ typedef struct {
     int32_t izh_hw_every;     /* Izhikevich networks: every k-th group of 32 neurons evaluates the
                                  update's double-precision expression on the FP64 pipe, the others
                                  on the integer pipe (an exact restatement): 0 .. 8, 0 = none,
-                                 1 = all (default).  Same results either way.                        */
+                                 1 = all (default); -1: every neuron in float-float arithmetic,
+                                 with the FP64 pipe only for values whose float rounding the
+                                 float-float result leaves uncertain.  Same results every way.      */
     int32_t small_max_slots;  /* a network of at most 2,048 neurons whose synapse planes hold at most
                                  this many slots (neurons rounded up to 32 x max synapses rounded up
                                  to 4) runs up to 4,096 whole steps per launch on one CTA, with no
