@@ -601,6 +601,7 @@ __device__ __forceinline__ float izh_v_ff(float Vint, float u, float C3, float c
                     K04L = (float)(0.04 - (double)K04H - (double)K04M);
     constexpr float K001H = (float)0.001, K001M = (float)(0.001 - (double)K001H),
                     K001L = (float)(0.001 - (double)K001H - (double)K001M);
+    ok = true;
     if (!(fabsf(Vint) < 1e4f) || !(fabsf(u) < 1e4f) || !(fabsf(C3) < 1e4f) || !(fabsf(c2sp) < 1e4f)) {
         ok = false;
         return 0.0f;
