@@ -70,12 +70,13 @@ struct LaunchCfg {
     int32_t deliver_early;    // 1: spiking/DS delivery prepares its arrivals during the previous
                               // sweep, 0: it starts after it
     int32_t izh_hw_every;     // Izhikevich update: every k-th 32-neuron tile in hardware FP64,
-                              // the others on the integer pipe (0: all on the integer pipe)
+                              // the others on the integer pipe (0: all on the integer pipe);
+                              // -1: float-float arithmetic, FP64 only for uncertain roundings
     int32_t small_max_slots;  // networks of at most SMALL_MAX_N neurons and this many synapse
                               // slots run many steps per launch in one CTA (0: never)
 };
 constexpr int SMALL_MAX_N = 2048;
-constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1, 1, 65536};
+constexpr LaunchCfg LAUNCH_DEFAULT = {6, 16, 8, 304, 256, 32, 1, -1, 65536};
 
 // plane position of slot (dest d, row k) and its inverse (Mq row quads per dest)
 __host__ __device__ __forceinline__ size_t slot_pos(int k, int d, int Mq)

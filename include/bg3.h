@@ -418,9 +418,10 @@ typedef struct {
     int32_t izh_hw_every;     /* Izhikevich networks: every k-th group of 32 neurons evaluates the
                                  update's double-precision expression on the FP64 pipe, the others
                                  on the integer pipe (an exact restatement): 0 .. 8, 0 = none,
-                                 1 = all (default); -1: every neuron in float-float arithmetic,
+                                 1 = all; -1 (default): every neuron in float-float arithmetic,
                                  with the FP64 pipe only for values whose float rounding the
-                                 float-float result leaves uncertain.  Same results every way.      */
+                                 float-float result leaves uncertain (~0.2 %).  Same results every
+                                 way.                                                                 */
     int32_t small_max_slots;  /* a network of at most 2,048 neurons whose synapse planes hold at most
                                  this many slots (neurons rounded up to 32 x max synapses rounded up
                                  to 4) runs up to 4,096 whole steps per launch on one CTA, with no

@@ -14,10 +14,10 @@ from tests.netcases import assert_same, oracle_from_case
 pytestmark = pytest.mark.gpu
 
 CONFIGS = [dict(sweep_stages=4, thin_warps=4, deliver_blocks=152, growth_threads=128,
-                izh_hw_every=0),
+                izh_hw_every=0, small_max_slots=0),
            dict(sweep_stages=8, thin_warps=16, deliver_blocks=608, growth_threads=512,
                 deliver_early=0),
-           dict(sweep_dests=16, sweep_stages=6, izh_hw_every=1),
+           dict(sweep_dests=16, sweep_stages=6, izh_hw_every=1, small_max_slots=0),
            dict(sweep_dests=16, sweep_stages=4, izh_hw_every=3),
            dict(thin_max_quads=64, thin_warps=2, deliver_blocks=17),
            dict(thin_max_quads=1, sweep_stages=6, deliver_blocks=1, deliver_early=0)]
@@ -107,6 +107,6 @@ def test_invalid_launch_configurations_are_rejected():
     net = make("c0_grown")
     for bad in (dict(sweep_stages=5), dict(thin_warps=0), dict(growth_threads=64),
                 dict(deliver_blocks=0), dict(sweep_dests=8), dict(deliver_early=2),
-                dict(izh_hw_every=9)):
+                dict(izh_hw_every=9), dict(izh_hw_every=-2), dict(small_max_slots=-1)):
         with pytest.raises(RuntimeError):
             net.set_launch(**bad)
