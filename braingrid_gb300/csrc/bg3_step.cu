@@ -1034,6 +1034,8 @@ bool sweep_is_thin(const NetDev &h, const LaunchCfg &c) { return h.Mq <= c.thin_
 // of on-chip latency instead of two or three kernel launches.  The step counter, its delivery
 // copy and the injected stream's cursor are kept in registers and stored at the end.  No thread
 // waits on another block, so nothing here can wait forever.
+// Up to SMALL_THREADS threads: a network of N neurons gets N rounded up to whole warps (at least
+// two), so that a small one pays for few warps at each barrier.
 constexpr int SMALL_THREADS = 512;
 constexpr int SMALL_WARPS = SMALL_THREADS / 32;
 
@@ -1057,7 +1059,7 @@ __device__ __forceinline__ void ring_push_smem(const NetDev &n, int *s_ring_n,
 }
 
 // Injected noise: the reference CPU order, neurons walked from the top in chunks of the block
-// (k_neurons_inject with a block of SMALL_THREADS); returns the step's number of draws.
+// (k_neurons_inject with the launch's block); returns the step's number of draws.
 __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsigned long long t,
                                                           unsigned long long cursor,
                                                           int *warp_tot, long long *s_running,
@@ -1066,7 +1068,8 @@ __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsig
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) *s_running = 0;
     __syncthreads();
-    for (int top = n.N - 1; top >= 0; top -= SMALL_THREADS) {
+    const int nt = (int)blockDim.x, nw = nt >> 5;
+    for (int top = n.N - 1; top >= 0; top -= nt) {
         const int i = top - (int)threadIdx.x;
         NeuronIn x;
         if (i >= 0) neuron_load(n, i, x);
@@ -1077,14 +1080,14 @@ __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsig
         if (lane == 31) warp_tot[warp] = __popc(m);
         __syncthreads();
         if (warp == 0) {
-            const int v = lane < SMALL_WARPS ? warp_tot[lane] : 0;
+            const int v = lane < nw ? warp_tot[lane] : 0;
             int y = v;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int z = __shfl_up_sync(0xffffffffu, y, o);
                 if (lane >= o) y += z;
             }
-            if (lane < SMALL_WARPS) warp_tot[lane] = y - v;  // exclusive prefix of warp totals
+            if (lane < nw) warp_tot[lane] = y - v;  // exclusive prefix of warp totals
         }
         __syncthreads();
         const long long running = *s_running;
@@ -1102,7 +1105,7 @@ __device__ __forceinline__ long long small_neurons_inject(const NetDev &n, unsig
         }
         ring_push_smem(n, s_ring_n, t, fired, i);
         __syncthreads();
-        if (threadIdx.x == SMALL_THREADS - 1) *s_running = running + warp_tot[warp] + __popc(m);
+        if ((int)threadIdx.x == nt - 1) *s_running = running + warp_tot[warp] + __popc(m);
         __syncthreads();
     }
     return *s_running;
@@ -1118,9 +1121,10 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
     __shared__ int s_ring_n[BG3_RING];        // the ring's spike counts, stored back at the end
     __shared__ int s_ltab[BG3_MAX_DELAYS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthreads = (int)blockDim.x, nwarps = nthreads >> 5;
     unsigned long long t = *n.step;
     unsigned long long cursor = INJECT ? *n.noise_cursor : 0ull;
-    if (tid < BG3_RING) s_ring_n[tid] = n.ring_n[tid];
+    for (int k = tid; k < BG3_RING; k += nthreads) s_ring_n[k] = n.ring_n[k];
     if (tid < BG3_MAX_DELAYS) s_ltab[tid] = tid < n.n_delays ? n.ltab[tid] : 0;
     __syncthreads();
     for (int s = 0; s < nsteps; s++, t++) {
@@ -1129,7 +1133,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
             cursor += (unsigned long long)small_neurons_inject(n, t, cursor, warp_tot, &s_running,
                                                                s_ring_n);
         } else {
-            for (int i0 = 0; i0 < n.N; i0 += SMALL_THREADS) {
+            for (int i0 = 0; i0 < n.N; i0 += nthreads) {
                 const int i = i0 + tid;
                 bool fired = false;
                 if (i < n.N) {
@@ -1165,7 +1169,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
         // ---- spike arrivals of step t: one warp per (delay class, neuron that fired) item;
         // every synapse has one source, which fired once, so no two lanes touch one slot
         const int M = s_moff[n.n_delays];
-        for (int item = warp; item < M; item += SMALL_WARPS) {
+        for (int item = warp; item < M; item += nwarps) {
             int c = 0;
             while (item >= s_moff[c + 1]) c++;
             const unsigned long long tf = t - (unsigned long long)s_ltab[c];
@@ -1181,7 +1185,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
             // post-spike learning of the neurons that fired at step t, after the arrivals
             const int slot = (int)(t & (BG3_RING - 1));
             const int m = min(s_ring_n[slot], n.N);
-            for (int e = warp; e < m; e += SMALL_WARPS) {
+            for (int e = warp; e < m; e += nwarps) {
                 const int d = n.ring[(size_t)slot * n.N + e];
                 const int cnt = (int)n.count[d];
                 for (int k = lane; k < cnt; k += 32) {
@@ -1193,14 +1197,14 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_run(const __grid_consta
             __syncthreads();
         }
         // ---- synapse sweep and summation of step t: one warp per 32-dest tile
-        for (int tile = warp; tile < n.ntiles; tile += SMALL_WARPS) {
+        for (int tile = warp; tile < n.ntiles; tile += nwarps) {
             const float acc = thin_rows(n, tile, thin_quads(n, tile), lane);
             const int d = tile * SW_DESTS + lane;
             if (d < n.N) n.sp[d] = acc;
         }
         __syncthreads();
     }
-    if (tid < BG3_RING) n.ring_n[tid] = s_ring_n[tid];
+    for (int k = tid; k < BG3_RING; k += nthreads) n.ring_n[k] = s_ring_n[k];
     if (tid == 0) {
         *n.step = t;
         *n.dstep = t;
@@ -1218,6 +1222,7 @@ bool small_eligible(const NetDev &h, const LaunchCfg &c)
 void launch_small(const NetDev &h, int nsteps, cudaStream_t s)
 {
     const bool inj = h.noise_mode == 1;
+    const int SMALL_THREADS = std::max(64, std::min(bg3::SMALL_THREADS, (h.N + 31) / 32 * 32));
     switch (h.syn_kind * 2 + (inj ? 1 : 0)) {
     case 2: k_small_run<1, false><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
     case 3: k_small_run<1, true><<<1, SMALL_THREADS, 0, s>>>(h, nsteps); break;
