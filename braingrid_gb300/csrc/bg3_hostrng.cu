@@ -3,82 +3,173 @@
 // MTRand (RNG/MersenneTwister.cpp), seeded with the parameter file's seed
 // (Core/SingleThreadedSpikingModel.cpp:30).  Host code only; built with -ffp-contract=off like
 // the rest of the library so that every product and sum rounds as the reference's do.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "bg3.h"
 
 namespace {
 
 // MT19937 (Matsumoto and Nishimura 1998) with Knuth's seeding: the state is refilled 624 words
-// at a time, and the block's words are tempered and turned into uniforms in one loop.
+// at a time (twist), and each word is tempered and turned into a uniform as MTRand::rand does.
 struct Mt {
     uint32_t s[624];
-    float u[624];
     int next = 624;
 
     explicit Mt(uint32_t seed)
     {
         s[0] = seed;
         for (uint32_t i = 1; i < 624; i++) s[i] = 1812433253u * (s[i - 1] ^ (s[i - 1] >> 30)) + i;
-        refill();
     }
     static uint32_t mix(uint32_t far, uint32_t hi, uint32_t lo)
     {
         uint32_t y = (hi & 0x80000000u) | (lo & 0x7fffffffu);
         return far ^ (y >> 1) ^ ((0u - (lo & 1u)) & 0x9908b0dfu);
     }
-    void refill()
+    void twist()
     {
         int i = 0;
         for (; i < 227; i++) s[i] = mix(s[i + 397], s[i], s[i + 1]);
         for (; i < 623; i++) s[i] = mix(s[i - 227], s[i], s[i + 1]);
         s[623] = mix(s[396], s[623], s[0]);
-        // MTRand::rand as BrainGrid declares it (BGFLOAT): the tempered word over 2^32 - 1 in
-        // double, rounded to float
-        for (int i = 0; i < 624; i++) {
-            uint32_t y = s[i];
-            y ^= y >> 11;
-            y ^= (y << 7) & 0x9d2c5680u;
-            y ^= (y << 15) & 0xefc60000u;
-            y ^= y >> 18;
-            u[i] = (float)((double)(float)y * (1.0 / 4294967295.0));
-        }
         next = 0;
     }
-    float uniform()
+    // MTRand::rand as BrainGrid declares it (BGFLOAT): the tempered word over 2^32 - 1 in
+    // double, rounded to float
+    static float uniform_of(uint32_t y)
     {
-        if (next == 624) refill();
-        return u[next++];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        return (float)((double)(float)y * (1.0 / 4294967295.0));
+    }
+    uint32_t word()
+    {
+        if (next == 624) twist();
+        return s[next++];
     }
 };
 
 }  // namespace
+
+// One attempt of the polar method on the uniform pair (u1, u2): whether it is accepted and,
+// if so, the pair of normal values it yields (RNG/Norm.cpp:59-86, in float as the reference).
+static inline bool polar_pair(float u1, float u2, float &x1, float &x2)
+{
+    const float v1 = 2 * u1 - 1;
+    const float v2 = 2 * u2 - 1;
+    const float w = v1 * v1 + v2 * v2;
+    if (w > 1) return false;
+    const float y = std::sqrt(-2 * std::log(w) / w);
+    x1 = v1 * y;
+    x2 = v2 * y;
+    return true;
+}
 
 struct bg3_norm {
     Mt mt;
     float mu, sigma;
     bool odd = true;  // Norm's constructor (RNG/Norm.h:70): the first call computes a pair
     float x2 = 0.0f;
+    std::vector<uint32_t> wbuf;  // generator words taken out and not yet consumed
+    size_t wpos = 0;
+    // per-thread pairs of a parallel fill, kept between calls so that their memory is reused
+    std::vector<std::vector<float>> part;
+    std::vector<std::vector<int64_t>> last;
     bg3_norm(uint32_t seed, float m, float s) : mt(seed), mu(m), sigma(s) {}
+
+    float uniform()
+    {
+        if (wpos < wbuf.size()) return Mt::uniform_of(wbuf[wpos++]);
+        return Mt::uniform_of(mt.word());
+    }
 
     float draw()
     {
         if ((odd = !odd)) return mu + sigma * x2;
-        float v1, v2, w;
-        do {
-            float u1 = mt.uniform();
-            float u2 = mt.uniform();
-            v1 = 2 * u1 - 1;
-            v2 = 2 * u2 - 1;
-            w = v1 * v1 + v2 * v2;
-        } while (w > 1);
-        float y = std::sqrt(-2 * std::log(w) / w);
-        float x1 = v1 * y;
-        x2 = v2 * y;
+        float x1;
+        for (;;) {
+            const float u1 = uniform();
+            const float u2 = uniform();
+            if (polar_pair(u1, u2, x1, x2)) break;
+        }
         return mu + sigma * x1;
+    }
+
+    // Appends at least k more words of the generator to wbuf.
+    void buffer_words(size_t k)
+    {
+        wbuf.erase(wbuf.begin(), wbuf.begin() + (ptrdiff_t)wpos);
+        wpos = 0;
+        const size_t want = wbuf.size() + k;
+        wbuf.reserve(want + 624);
+        while (wbuf.size() < want) {
+            if (mt.next == 624) mt.twist();
+            wbuf.insert(wbuf.end(), mt.s + mt.next, mt.s + 624);
+            mt.next = 624;
+        }
+    }
+
+    // The next 2P values of the stream as P whole pairs (odd must be true: no value pending).
+    // Only the generator's recurrence runs in order on this thread; tempering, the polar
+    // attempts and the logarithms are independent per pair of words, so threads take ranges of
+    // word pairs, keep their accepted pairs, and the pairs are then placed at the offsets the
+    // per-thread counts give: the same values in the same order as 2P sequential draws.
+    void fill_pairs(float *out, int64_t P)
+    {
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        int64_t done = 0;
+        while (done < P) {
+            const int64_t need = P - done;
+            // 4/pi attempts per accepted pair on average (the acceptance of the polar method is
+            // pi/4), plus six standard deviations: few attempts are made and not used
+            const size_t attempts =
+                (size_t)(1.2733 * (double)need + 6.0 * std::sqrt((double)need) + 64.0);
+            if (wbuf.size() - wpos < 2 * attempts) buffer_words(2 * attempts - (wbuf.size() - wpos));
+            const uint32_t *w = wbuf.data() + wpos;
+            const int64_t A = (int64_t)((wbuf.size() - wpos) / 2);
+            const int T = (int)std::max<int64_t>(1, std::min<int64_t>(hw, A / 16384));
+            if ((int)part.size() < T) {
+                part.resize(T);
+                last.resize(T);  // attempt index of each kept pair
+            }
+            auto run = [&](int k) {
+                const int64_t lo = A * k / T, hi = A * (k + 1) / T;
+                std::vector<float> &p = part[k];
+                std::vector<int64_t> &l = last[k];
+                p.clear();
+                l.clear();
+                p.reserve((size_t)(hi - lo) * 2);
+                l.reserve((size_t)(hi - lo));
+                float a, b;
+                for (int64_t j = lo; j < hi; j++) {
+                    if (!polar_pair(Mt::uniform_of(w[2 * j]), Mt::uniform_of(w[2 * j + 1]), a, b)) continue;
+                    p.push_back(mu + sigma * a);
+                    p.push_back(mu + sigma * b);
+                    l.push_back(j);
+                }
+            };
+            std::vector<std::thread> th;
+            for (int k = 1; k < T; k++) th.emplace_back(run, k);
+            run(0);
+            for (auto &x : th) x.join();
+            // place the pairs in order, up to the need
+            int64_t got = 0, used = A;
+            for (int k = 0; k < T && got < need; k++) {
+                const int64_t m = std::min<int64_t>((int64_t)last[k].size(), need - got);
+                std::copy(part[k].begin(), part[k].begin() + 2 * m, out + 2 * (done + got));
+                got += m;
+                if (got == need) used = last[k][m - 1] + 1;  // attempts after it stay unread
+            }
+            wpos += 2 * (size_t)used;
+            done += got;
+        }
     }
 };
 
@@ -89,10 +180,23 @@ extern "C" int bg3_norm_create(uint32_t seed, float mu, float sigma, bg3_norm **
     return *out ? BG3_OK : BG3_ENOMEM;
 }
 
+// Large fills run the polar attempts on several host threads (bg3_norm::fill_pairs); the values
+// are the sequential stream's, whatever the split of a stream into calls.
 extern "C" int bg3_norm_fill(bg3_norm *g, float *values, int64_t n)
 {
     if (!g || n < 0 || (n && !values)) return BG3_EINVAL;
-    for (int64_t i = 0; i < n; i++) values[i] = g->draw();
+    int64_t i = 0;
+    if (i < n && !g->odd) values[i++] = g->draw();  // the pending second value of a pair
+    const int64_t pairs = (n - i) / 2;
+    if (pairs >= 65536) {
+        try {
+            g->fill_pairs(values + i, pairs);
+        } catch (...) {  // no thread or no memory: the caller gets an error, the stream is lost
+            return BG3_ENOMEM;
+        }
+        i += 2 * pairs;
+    }
+    for (; i < n; i++) values[i] = g->draw();
     return BG3_OK;
 }
 

@@ -234,11 +234,15 @@ def test_refused_files(tmp_path):
 
 
 def test_norm_stream_matches_the_oracle():
+    """bg3_norm_fill gives the oracle's stream however it is split into calls: single values,
+    odd and even counts, and fills large enough to run the polar method on several threads
+    (starting with and without a pending second value of a pair)."""
     from braingrid_gb300 import lib as bg
     from oracle import pyoracle as po
-    want = po.norm_stream(5, 1000001)
+    want = po.norm_stream(5, 2600003)
     g = bg.NormStream(5)
-    got = np.concatenate([g.take(1), g.take(0), g.take(30000), g.take(970000)])
+    got = np.concatenate([g.take(1), g.take(0), g.take(30000), g.take(970000), g.take(300001),
+                          g.take(1000000), g.take(300001)])
     assert_same("norm", got, want)
     g.close()
 
