@@ -23,13 +23,14 @@
 //   cleanupSim         the whole device state back into the host objects, then the network is
 //                      freed (Core/GPUSpikingModel.cu:82-99).
 //
-// Noise.  By default the model draws the reference's own noise stream on the host:
-// rgNormrnd[0] = Norm(0, 1, seed), the generator the reference's single-threaded model creates
-// (Core/SingleThreadedSpikingModel.cpp:30), and the library consumes it in the reference's CPU
-// order, so a run matches the single-threaded reference spike for spike.  The values are drawn
-// ahead on the host while the GPU runs the previous steps.  With BG3_NOISE=device the library's
-// own generator (keyed by seed, step and neuron, one draw per neuron per step like the reference
-// GPU model's) is used instead and the host draws nothing.
+// Noise.  By default the model feeds the reference's own noise stream: Norm(0, 1, seed), the
+// generator the reference's single-threaded model creates (Core/SingleThreadedSpikingModel.cpp:
+// 30), drawn by the library's restatement of it (bg3_norm_*, the same values: MT19937 and the
+// polar method in float, with large fills spread over host threads), and the library consumes it
+// in the reference's CPU order, so a run matches the single-threaded reference spike for spike.
+// The values are drawn ahead on the host while the GPU runs the previous steps.  With
+// BG3_NOISE=device the library's own generator (keyed by seed, step and neuron, one draw per
+// neuron per step like the reference GPU model's) is used instead and the host draws nothing.
 //
 // Checkpoints.  The reference's Model::serialize writes the host objects; when the run writes a
 // checkpoint (a memOutputFileName is set), the last epoch's updateHistory copies the whole device
@@ -47,7 +48,6 @@
 #include "ConnGrowth.h"
 #include "GPUSpikingModel.h"
 #include "Global.h"
-#include "Norm.h"
 #include "bg3_dropin.h"
 
 namespace {
@@ -56,12 +56,14 @@ namespace {
 // device pointers): the network, the queued steps and the noise drawn ahead.
 struct ModelState {
     bg3_net *net;
+    bg3_norm *gen;                        // the reference's noise stream (reference noise only)
     bool reference_noise;
     int64_t chunk;                        // steps per bg3_step call
     int64_t queued;                       // steps advance() queued and not yet launched
     std::vector<float> drawn;             // noise values drawn ahead, not yet pushed
     int64_t held_at_launch;               // values the device held when the last steps launched
-    ModelState() : net(NULL), reference_noise(true), chunk(1000), queued(0), held_at_launch(0) {}
+    ModelState() : net(NULL), gen(NULL), reference_noise(true), chunk(1000), queued(0),
+                   held_at_launch(0) {}
 };
 
 std::map<const GPUSpikingModel *, ModelState> g_state;
@@ -153,12 +155,11 @@ int64_t env_int(const char *name, int64_t dflt)
     return (end && !*end && x > 0) ? (int64_t)x : dflt;
 }
 
-void draw(std::vector<float> &out, int64_t n)
+void draw(bg3_norm *gen, std::vector<float> &out, int64_t n)
 {
-    Norm &g = *rgNormrnd[0];
     const size_t old = out.size();
     out.resize(old + (size_t)n);
-    for (int64_t i = 0; i < n; i++) out[old + (size_t)i] = g();
+    bg3_dropin_check(bg3_norm_fill(gen, &out[old], n), "bg3_norm_fill");
 }
 
 }  // namespace
@@ -183,6 +184,7 @@ GPUSpikingModel::~GPUSpikingModel()
     std::map<const GPUSpikingModel *, ModelState>::iterator it = g_state.find(this);
     if (it != g_state.end()) {
         if (it->second.net) bg3_destroy(it->second.net);
+        if (it->second.gen) bg3_norm_destroy(it->second.gen);
         g_state.erase(it);
     }
 }
@@ -264,7 +266,11 @@ void GPUSpikingModel::setupSim(SimulationInfo *sim_info)
     st.queued = 0;
     st.drawn.clear();
     st.held_at_launch = 0;
-    if (st.reference_noise) rgNormrnd.push_back(new Norm(0, 1, sim_info->seed));
+    if (st.gen) bg3_norm_destroy(st.gen);
+    st.gen = NULL;
+    if (st.reference_noise)
+        bg3_dropin_check(bg3_norm_create((uint32_t)sim_info->seed, 0.0f, 1.0f, &st.gen),
+                         "bg3_norm_create");
     allocDeviceStruct((void **)&m_allNeuronsDevice, (void **)&m_allSynapsesDevice, sim_info);
     m_neurons->setAdvanceNeuronsDeviceParams(*m_synapses);
     m_synapses->setAdvanceSynapsesDeviceParams();
@@ -287,7 +293,7 @@ static void run_queued(ModelState &st, const SimulationInfo *si)
         int64_t held = 0;
         bg3_dropin_check(bg3_noise_pending(st.net, &held), "bg3_noise_pending");
         if (held < N * st.queued) {
-            draw(st.drawn, N * st.queued - held);
+            draw(st.gen, st.drawn, N * st.queued - held);
             bg3_dropin_check(bg3_push_noise(st.net, st.drawn.data(), (int64_t)st.drawn.size()),
                              "bg3_push_noise");
             st.drawn.clear();
@@ -298,7 +304,7 @@ static void run_queued(ModelState &st, const SimulationInfo *si)
     bg3_dropin_check(bg3_step(st.net, st.queued), "bg3_step");
     if (st.reference_noise) {
         const int64_t want = 2 * N * st.chunk - st.held_at_launch;
-        if (want > 0) draw(st.drawn, want);   // overlaps the steps just launched
+        if (want > 0) draw(st.gen, st.drawn, want);   // overlaps the steps just launched
     }
     st.queued = 0;
 }
