@@ -1485,15 +1485,24 @@ static int batch_refresh(bg3_batch *b)
             tiles.push_back(std::make_pair((int)m, make_int2((int)k, t)));
         }
     }
-    // TMA-swept tiles first, heaviest first; then the tiles of thin networks (one warp each)
+    // TMA-swept tiles first, heaviest first; then the tiles of thin networks (one warp each) in
+    // (network, tile) order, each network's run padded with (network, -1) entries to whole blocks
+    // of the thin sweep, so that a block serves one network
+    std::vector<int2> thin;
+    const int w = b->cfg.thin_warps;
+    for (auto &t : tiles) {
+        if (!bg3::sweep_is_thin(b->nets[t.second.x]->h, b->cfg)) continue;
+        thin.push_back(t.second);
+        if (t.second.y == b->nets[t.second.x]->h.ntiles - 1)
+            while (thin.size() % w) thin.push_back(make_int2(t.second.x, -1));
+    }
     std::stable_sort(tiles.begin(), tiles.end(),
                      [](const std::pair<int, int2> &a, const std::pair<int, int2> &c) { return a.first > c.first; });
     std::vector<int2> tl;
     for (auto &t : tiles)
         if (!bg3::sweep_is_thin(b->nets[t.second.x]->h, b->cfg)) tl.push_back(t.second);
     b->n_thick = (int)tl.size();
-    for (auto &t : tiles)
-        if (bg3::sweep_is_thin(b->nets[t.second.x]->h, b->cfg)) tl.push_back(t.second);
+    tl.insert(tl.end(), thin.begin(), thin.end());
     if ((int)tl.size() != b->ntiles) {
         if (b->d_tiles) cudaFree(b->d_tiles);
         b->d_tiles = nullptr;
@@ -1833,7 +1842,7 @@ int bg3_batch_set_launch(bg3_batch *b, const bg3_launch_cfg *c)
     if (!b || !cfg_valid(c)) return BG3_EINVAL;
     CK(cudaStreamSynchronize(b->stream));
     b->cfg = cfg_from(*c);
-    return batch_refresh(b);  // the thin / TMA split of the tiles depends on the configuration
+    return batch_refresh(b);  // the thin / TMA split and the thin tile table depend on it
 }
 
 // A device-side copy of a network's whole state (every allocation plus the injected-noise
@@ -2015,7 +2024,10 @@ int bg3_batch_autotune(bg3_batch *b, int32_t steps, bg3_launch_cfg *best, float 
     auto trial = [&](const LaunchCfg &c) -> float {
         for (size_t k = 0; k < b->nets.size(); k++)
             if (state_load(b->nets[k], sc[k]) != BG3_OK) return -1.0f;
+        // the thin / TMA split, the thin tile table's padding to blocks and the descriptors'
+        // Izhikevich option depend on these
         const bool split = b->cfg.thin_max_quads != c.thin_max_quads ||
+                           b->cfg.thin_warps != c.thin_warps ||
                            b->cfg.izh_hw_every != c.izh_hw_every;
         b->cfg = c;
         if (split && batch_refresh(b) != BG3_OK) return -1.0f;

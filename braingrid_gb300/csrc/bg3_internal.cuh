@@ -280,6 +280,16 @@ __device__ __forceinline__ float normal_device(uint32_t seed, unsigned long long
 
 __device__ __forceinline__ void set_err(const NetDev &n, uint32_t bit) { atomicOr(n.err, bit); }
 
+// A store to global memory as such (st.global, the default write-back policy).  The batched
+// kernels read their network's descriptor from shared memory; a plain store through a pointer
+// taken from it is a generic store, which as far as the compiler knows may write shared memory,
+// so every descriptor field would be read again after it.
+template <typename T>
+__device__ __forceinline__ void gst(T *p, T v)
+{
+    __stwb(p, v);
+}
+
 // ---- exact float <-> double conversions on the integer pipe ---------------------------------
 // GB300's FP64 pipe is narrow and the Izhikevich update (which the reference evaluates partly in
 // double) is bound by it; its conversions are done with integer operations instead.  Both are
@@ -654,22 +664,22 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
 {
     const bool izh = n.neuron_kind == 1;
     if (br == BR_REFRACTORY) {
-        n.refr[i] = x.refr - 1;
+        gst(&n.refr[i], x.refr - 1);
         return false;
     }
     if (br == BR_FIRE) {
         int cnt = n.spikeCount[i];
         int idx = (cnt + n.spikeCountOffset[i]) % n.max_spikes;
-        n.history[(size_t)i * n.max_spikes + idx] = t;
+        gst(&n.history[(size_t)i * n.max_spikes + idx], t);
         cnt += 1;
-        n.spikeCount[i] = cnt;
+        gst(&n.spikeCount[i], cnt);
         if (cnt >= n.max_spikes) set_err(n, ERR_HISTORY_OVERFLOW);
-        n.refr[i] = (int)((double)(x.Trefract / n.dt) + 0.5);
+        gst(&n.refr[i], (int)((double)(x.Trefract / n.dt) + 0.5));
         if (izh) {
-            n.Vm[i] = (float)((double)x.Cc * 0.001);
-            n.u_izh[i] = x.u + x.Dd;
+            gst(&n.Vm[i], (float)((double)x.Cc * 0.001));
+            gst(&n.u_izh[i], x.u + x.Dd);
         } else {
-            n.Vm[i] = n.Vreset[i];
+            gst(&n.Vm[i], n.Vreset[i]);
         }
         return true;
     }
@@ -709,10 +719,10 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
             Vnew = sd_to_float(w, ok);
             if (!ok) Vnew = izh_v_fp64(Vint, u, C3, x.C2 * sp);  // outside the restated range
         }
-        n.u_izh[i] = u + C3 * x.A * (x.B * Vint - u);
-        n.Vm[i] = Vnew;
+        gst(&n.u_izh[i], u + C3 * x.A * (x.B * Vint - u));
+        gst(&n.Vm[i], Vnew);
     } else {
-        n.Vm[i] = x.C1 * x.Vm + x.C2 * sp;
+        gst(&n.Vm[i], x.C1 * x.Vm + x.C2 * sp);
     }
     return false;
 }
@@ -724,7 +734,7 @@ __device__ __forceinline__ bool neuron_apply(const NetDev &n, int i, const Neuro
 __device__ __forceinline__ int32_t next_isi(const NetDev &n, int i)
 {
     const int32_t k = n.isi_cursor[i];
-    n.isi_cursor[i] = k + 1;
+    gst(&n.isi_cursor[i], k + 1);
     if (n.isi_begin) {
         const int32_t p = n.isi_begin[i] + k;
         if (p < n.isi_begin[i + 1]) return n.isi_vals[p];
@@ -759,7 +769,7 @@ __device__ __forceinline__ float input_apply(const NetDev &n, int i, const Neuro
             q |= 1u << ((uint32_t)(t + x.idelay) & 31u);
             c = next_isi(n, i);
         }
-        n.pois_nisi[i] = c;
+        gst(&n.pois_nisi[i], c);
         const uint32_t bit = 1u << ((uint32_t)t & 31u);
         float psr = x.ipsr;
         const float dec = x.idec;
@@ -769,13 +779,13 @@ __device__ __forceinline__ float input_apply(const NetDev &n, int i, const Neuro
             float u = e.u, r = e.r;
             if (e.last != BG3_NO_SPIKE32) ds_update(n, e, (uint32_t)t - e.last, u, r);
             psr = psr + ((e.W / dec) * u * r);
-            n.in_ev[i].u = u;
-            n.in_ev[i].r = r;
-            n.in_ev[i].last = (uint32_t)t;
+            gst(&n.in_ev[i].u, u);
+            gst(&n.in_ev[i].r, r);
+            gst(&n.in_ev[i].last, (uint32_t)t);
         }
-        n.in_queue[i] = q;
+        gst(&n.in_queue[i], q);
         psr = psr * dec;
-        n.in_psr[i] = psr;
+        gst(&n.in_psr[i], psr);
         sp = sp + psr;
     }
     return sp;
@@ -794,7 +804,7 @@ __device__ __forceinline__ void ring_push(const NetDev &n, unsigned long long t,
     base = __shfl_sync(0xffffffffu, base, leader);
     if (fired) {
         int pos = base + __popc(mask & ((1u << lane) - 1));
-        if (pos < n.N) n.ring[(size_t)slot * n.N + pos] = i;
+        if (pos < n.N) gst(&n.ring[(size_t)slot * n.N + pos], i);
         else set_err(n, ERR_SPIKE_LIST);
     }
 }

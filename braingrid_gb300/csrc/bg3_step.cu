@@ -36,6 +36,19 @@ __device__ __forceinline__ void dstep_advance(const NetDev &n, bool me, unsigned
     }
 }
 
+// The batched kernels find their network's descriptor in global memory (nets[k]); read there
+// field by field, every field is a dependent load (the plain kernels take theirs as a kernel
+// parameter).  Each block serves one network and first copies its descriptor into shared
+// memory with all its threads, 16 bytes each.
+static_assert(sizeof(NetDev) % 16 == 0, "descriptor copied in 16-byte words");
+__device__ __forceinline__ void block_copy_desc(NetDev *dst, const NetDev *src)
+{
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(NetDev) / 16); k += blockDim.x) d4[k] = s4[k];
+    __syncthreads();
+}
+
 // Spiking neurons whose spikes arrive at step t (one work item of the delivery pass per neuron
 // and delay class), from the spike ring.  A pass with at most DLV_LIGHT_ITEMS of them is light:
 // it starts during the TMA sweep before it and lets the sweep after it start early.  A heavy pass
@@ -596,7 +609,9 @@ __global__ void __launch_bounds__(256) k_deliver(const __grid_constant__ NetDev 
 template <int SYN>
 __global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets, int early)
 {
-    deliver_net<SYN>(nets[blockIdx.y], blockIdx.x, gridDim.x, early != 0);
+    __shared__ __align__(16) NetDev s_net;
+    block_copy_desc(&s_net, nets + blockIdx.y);
+    deliver_net<SYN>(s_net, blockIdx.x, gridDim.x, early != 0);
 }
 
 // The fPost branch (AllSTDPSynapses.cpp:368-418) for every in-use synapse onto a neuron that
@@ -632,16 +647,20 @@ __global__ void __launch_bounds__(256) k_stdp_post(const __grid_constant__ NetDe
 
 __global__ void __launch_bounds__(256) k_stdp_post_batch(const NetDev *nets)
 {
+    __shared__ __align__(16) NetDev s_net;
+    block_copy_desc(&s_net, nets + blockIdx.y);
     pdl_wait();
     pdl_trigger();
-    stdp_post_net(nets[blockIdx.y], (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+    stdp_post_net(s_net, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
                   (gridDim.x * blockDim.x) >> 5);
 }
 
 // Batched standalone neuron pass (device noise): grid.y indexes the network.
 __global__ void __launch_bounds__(256) k_neurons_device_batch(const NetDev *nets)
 {
-    const NetDev &n = nets[blockIdx.y];
+    __shared__ __align__(16) NetDev s_net;
+    block_copy_desc(&s_net, nets + blockIdx.y);
+    const NetDev &n = s_net;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x * blockDim.x >= (unsigned)n.N) return;  // whole warp-aligned block beyond N
     unsigned long long t = *n.step;
@@ -710,11 +729,11 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
             const int br = neuron_branch(x);
             fired = neuron_apply<FF>(n, d, x, br, input_apply(n, d, x, t1, acc),
                                      br == BR_INTEGRATE ? noise : 0.0f, t1, izh_mode(n, d));
-            n.sp[d] = 0.0f;
+            gst(&n.sp[d], 0.0f);
         }
         ring_push(n, t1, fired, d);
     } else if (valid) {
-        n.sp[d] = acc;
+        gst(&n.sp[d], acc);
     }
     // A fused sweep is always followed by the next step's delivery, which advances the step
     // counter after its wait; an unfused one (the last step of a call, injected noise) advances it
@@ -923,7 +942,7 @@ __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, cons
                 v[j].y = v[j].y * __ldg(&n.dtab[(c[j] >> 4) & 15u]);
                 v[j].z = v[j].z * __ldg(&n.dtab[(c[j] >> 8) & 15u]);
                 v[j].w = v[j].w * __ldg(&n.dtab[(c[j] >> 12) & 15u]);
-                P[(size_t)(q + j) * 32] = v[j];
+                gst(&P[(size_t)(q + j) * 32], v[j]);
                 acc = acc + v[j].x;
                 acc = acc + v[j].y;
                 acc = acc + v[j].z;
@@ -1003,21 +1022,26 @@ __global__ void __launch_bounds__(1024) k_sweep_thin(const __grid_constant__ Net
     if (active) sweep_thin_tile<FUSE>(n, tile, nq, t);
 }
 
-// Batched thin tiles: tiles[i] = (network, tile), one warp each.
+// Batched thin tiles: tiles[i] = (network, tile), one warp each.  Every block's entries belong to
+// one network (the tile table pads each network's run to whole blocks with tile -1 entries,
+// which do nothing), so the block shares one copy of the descriptor in shared memory.
 template <bool FUSE>
 __global__ void __launch_bounds__(1024) k_sweep_thin_batch(const NetDev *nets, const int2 *tiles,
                                                            int count)
 {
-    const int i = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
-    const bool active = i < count;
-    const int2 tr = active ? tiles[i] : make_int2(0, 0);
-    const NetDev &n = nets[tr.x];
+    __shared__ __align__(16) NetDev s_net;
+    const int first = blockIdx.x * (int)(blockDim.x >> 5);
+    const int i = first + (int)(threadIdx.x >> 5);
+    const int2 tr = i < count ? tiles[i] : make_int2(0, -1);
+    const bool active = tr.y >= 0;
+    block_copy_desc(&s_net, nets + tiles[min(first, count - 1)].x);
+    const NetDev &n = s_net;
     const int nq = active ? thin_quads(n, tr.y) : 0;
     pdl_wait();
-    const unsigned long long t = active ? *n.step : 0ull;
+    const unsigned long long t = *n.step;
     dstep_advance(n, active && tr.y == 0 && (threadIdx.x & 31) == 0, t);
     __syncthreads();
-    pdl_trigger();  // no shared memory held: an early next delivery keeps its L1
+    pdl_trigger();  // 1.7 KB of shared memory held: an early next delivery keeps its L1
     if (active) sweep_thin_tile<FUSE>(n, tr.y, nq, t);
 }
 

@@ -118,3 +118,71 @@ def test_batch_izhikevich_stdp_matches_plain_bit_exact():
     assert all(int(n.download_lif()["spikeCount"].sum()) > 0 for n in plain)
     errs = [n.error_word for n in plain + batched]
     assert all(e == 0 for e in errs), errs
+
+
+def make_thin_lif():
+    """Four LIF networks of 45 k-75 k neurons with at most 40 synapses per neuron (thin tiles,
+    last tile partial in three of them) and regular input: ~7,500 thin tiles, so that every warp
+    of the pipelined thin sweep runs several tiles in a row."""
+    nets = []
+    for w, h, seed in ((260, 260, 21), (301, 151, 22), (199, 257, 23), (283, 263, 24)):
+        spec = netgen.lif_network(w, h, seed=seed)
+        net = netgen.make_gpu_network(spec, 40, epoch_duration=0.5, max_firing_rate=400,
+                                      noise_seed=seed)
+        netgen.pregrow(net, spec, 1.6, weight_scale=0.5, seed=seed)
+        rs = np.random.RandomState(seed)
+        net.input_regular(rs.uniform(0.5e-9, 2e-9, spec["N"]), rs.randint(0, 100, spec["N"]),
+                          20, 100)
+        nets.append(net)
+    return nets
+
+
+def _compare(plain, batched, fields):
+    for k, (p, q) in enumerate(zip(plain, batched)):
+        gp, sp = state(p)
+        gq, sq = state(q)
+        for f in ("Vm", "nStepsInRefr", "spikeCount", "history"):
+            assert_same("net %d %s" % (k, f), gq[f], gp[f])
+        used = sp["in_use"].astype(bool)
+        for f in fields:
+            assert_same("net %d %s" % (k, f), sq[f][used], sp[f][used])
+
+
+def test_thin_lif_batch_with_regular_input_matches_plain_bit_exact():
+    plain = make_thin_lif()
+    batched = make_thin_lif()
+    assert all(n.total_synapses() > 0 for n in plain)
+    b = bg.Batch(batched)
+    for chunk in (1, 300, 45):
+        for n in plain:
+            n.step(chunk)
+        b.step(chunk)
+        b.sync()
+        _compare(plain, batched, ("psr", "u", "r", "lastSpike"))
+    assert sum(int(n.download_lif()["spikeCount"].sum()) for n in plain) > 0
+    errs = [n.error_word for n in plain + batched]
+    assert all(e == 0 for e in errs), errs
+
+
+def test_thin_izhikevich_batch_matches_plain_bit_exact():
+    """40 networks of the 512-network Izhikevich + dynamic STDP workload (N ~ U[500, 8000],
+    Poisson drive): ~5,300 thin tiles over 40 networks, so that warps' runs of tiles cross from
+    one network into the next."""
+    from braingrid_gb300 import workloads
+    plain = workloads.build_izh512(count=40, seed=5)
+    batched = workloads.build_izh512(count=40, seed=5)
+    b = bg.Batch(batched)
+    for chunk in (1, 400, 33):
+        for n in plain:
+            n.step(chunk)
+        b.step(chunk)
+        b.sync()
+        _compare(plain, batched, ("W", "psr", "u", "r", "lastSpike"))
+        for k, (p, q) in enumerate(zip(plain, batched)):
+            assert_same("net %d izh u" % k, q.download_izh()["u"], p.download_izh()["u"])
+    assert sum(int(n.download_lif()["spikeCount"].sum()) for n in plain) > 0
+    errs = [n.error_word for n in plain + batched]
+    assert all(e == 0 for e in errs), errs
+    b.close()
+    for n in plain + batched:
+        n.close()
