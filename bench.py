@@ -489,17 +489,15 @@ def _sm_max_mhz():
         return 2070.0
 
 
-def run_growth():
-    """ConnGrowth epoch pass (radii update, O(N^2) overlap scan, weight update / synapse
-    creation, map rebuild, recorder) on the headline network: at the stated start radius 0.4 (every pair
-    rejected), at the pre-grown radii U[8.35, 8.45] creating ~7.6 M synapses, and once more at
-    those radii updating them.  Host wall clock around a synchronised pass."""
+def _growth_passes(width, height, radius):
+    """Pass times (s) of one network: at the stated start radius 0.4 (every pair rejected), at
+    pre-grown radii U[radius - 0.05, radius + 0.05] creating the synapses, and once more at those
+    radii updating them.  Host wall clock around a synchronised pass."""
     import time as _t
     from braingrid_gb300 import netgen
-    spec = netgen.lif_network(WIDTH, HEIGHT, frac_inh=0.10, seed=SEED)
+    spec = netgen.lif_network(width, height, frac_inh=0.10, seed=SEED)
     net = netgen.make_gpu_network(spec, MAX_SYN, noise_seed=SEED)
     N = spec["N"]
-    out = {"pairs": N * N}
 
     def timed(epoch):
         net.sync()
@@ -510,33 +508,49 @@ def run_growth():
     timed(1)  # first pass loads the module's kernels
     t_reject = timed(2)
     rs = np.random.RandomState(11)
-    r = rs.uniform(RADIUS - 0.05, RADIUS + 0.05, N).astype(np.float32)
+    r = rs.uniform(radius - 0.05, radius + 0.05, N).astype(np.float32)
     g = netgen.GROWTH
     net.upload_growth(g["epsilon"], g["beta"], g["rho"], g["target_rate"], g["min_radius"],
                       g["start_radius"], r)
     t_create = timed(3)
     S = net.total_synapses()
     t_update = timed(4)
+    err = net.error_word
+    net.close()
+    return N, t_reject, t_create, t_update, S, err
+
+
+def run_growth():
+    """ConnGrowth epoch pass (radii update, O(N^2) overlap scan, weight update / synapse
+    creation, map rebuild, recorder) on the headline network (10^8 pairs) and on the served
+    stream's largest job, 200x200 (1.6e9 pairs): at the stated start radius 0.4 (every pair
+    rejected), at the pre-grown radii U[8.35, 8.45] creating the synapses, and once more at those
+    radii updating them."""
+    N, t_reject, t_create, t_update, S, err = _growth_passes(WIDTH, HEIGHT, RADIUS)
     # FP32 roofline of the rejecting pass: 8 FP32 operations per pair (dx, dy, d^2, the radius
     # sum and the comparison) against the FP32 pipe's peak, 128 lanes x 152 SMs x the SM clock
     # (no FMA: the library is compiled without contraction); the pass also holds the radii
     # update, the map rebuild and the recorder, so this understates the overlap kernel alone
     clk = _sm_max_mhz() * 1e6
     fp32_peak = 128 * 152 * clk
-    out.update({"radius_0.4_s": t_reject, "radius_0.4_pairs_per_s": N * N / t_reject,
-                "radius_0.4_fp32_ops_per_s": 8 * N * N / t_reject,
-                "fp32_pipe_peak_ops_per_s": fp32_peak,
-                "radius_0.4_fp32_frac": 8 * N * N / t_reject / fp32_peak,
-                "grown_create_s": t_create, "grown_update_s": t_update,
-                "grown_pairs_per_s": N * N / t_update, "synapses": S,
-                # every overlapping pair (one per synapse here: no radius contains another)
-                # evaluates the lens area with 2 acos and 2 sin
-                "grown_transcendental_calls": 4 * S,
-                "grown_transcendentals_per_s": 4 * S / t_update,
-                "grown_bound": "fp64 (acos and sin of the overlap area evaluated in double; "
-                               "86 % FP64-pipe busy, profiles/k_growth_plain.md)",
-                "error_word": net.error_word})
-    net.close()
+    out = {"pairs": N * N, "radius_0.4_s": t_reject, "radius_0.4_pairs_per_s": N * N / t_reject,
+           "radius_0.4_fp32_ops_per_s": 8 * N * N / t_reject,
+           "fp32_pipe_peak_ops_per_s": fp32_peak,
+           "radius_0.4_fp32_frac": 8 * N * N / t_reject / fp32_peak,
+           "grown_create_s": t_create, "grown_update_s": t_update,
+           "grown_pairs_per_s": N * N / t_update, "synapses": S,
+           # every overlapping pair (one per synapse here: no radius contains another)
+           # evaluates the lens area with 2 acos and 2 sin
+           "grown_transcendental_calls": 4 * S,
+           "grown_transcendentals_per_s": 4 * S / t_update,
+           "grown_bound": "fp64 (acos and sin of the overlap area evaluated in double; "
+                          "86 % FP64-pipe busy, profiles/k_growth_plain.md)",
+           "error_word": err}
+    N2, r2, c2, u2, S2, e2 = _growth_passes(200, 200, RADIUS)
+    out["served_largest_200x200"] = {
+        "pairs": N2 * N2, "radius_0.4_s": r2, "radius_0.4_pairs_per_s": N2 * N2 / r2,
+        "grown_create_s": c2, "grown_update_s": u2, "grown_pairs_per_s": N2 * N2 / u2,
+        "synapses": S2, "grown_transcendentals_per_s": 4 * S2 / u2, "error_word": e2}
     return out
 
 

@@ -1,6 +1,6 @@
 """Run a benchmark workload for a few steps, for profilers (ncu) to capture its kernels.
 
-    python -m braingrid_gb300.profile_case [--workload plain|sweep36|izh512|big|growth|heavy] [--steps 20] [--flush]
+    python -m braingrid_gb300.profile_case [--workload plain|sweep36|izh512|big|growth|growth200|heavy] [--steps 20] [--flush]
 
 plain is the 100x100 network of the headline, sweep36 the 36-network growth sweep, izh512 the
 Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
@@ -20,14 +20,22 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "sweep36", "izh512", "big", "growth", "heavy"])
+                    choices=["plain", "sweep36", "izh512", "big", "growth", "growth200",
+                             "heavy"])
     ap.add_argument("--count", type=int, default=512, help="networks of the izh512 workload")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
-    if a.workload == "growth":
-        # the 10,000-neuron network's growth pass at the pre-grown radii: creation, then an
-        # updating pass
-        spec, net = workloads.build()
+    if a.workload in ("growth", "growth200"):
+        # the growth pass at the pre-grown radii: creation, then an updating pass; growth is
+        # the 10,000-neuron network, growth200 the served stream's largest job (200x200)
+        from . import netgen
+        if a.workload == "growth":
+            spec, net = workloads.build()
+        else:
+            spec = netgen.lif_network(200, 200, frac_inh=0.10, seed=workloads.PLAIN["seed"])
+            net = netgen.make_gpu_network(spec, workloads.PLAIN["max_syn"],
+                                          noise_seed=workloads.PLAIN["seed"])
+            netgen.pregrow(net, spec, workloads.PLAIN["radius"])
         net.growth(2)
         net.sync()
         print("synapses", net.total_synapses(), "error_word", net.error_word)
