@@ -61,6 +61,8 @@ SWEEP_BYTES_PER_NEURON = 48 + 30
 REF_LAYOUT_BYTES_PER_SYN = 28
 # served form: resident work cap, about one and a half of the largest jobs' synapse slots
 SERVE_SLOTS = 60e6
+SERVED_LONG_JOBS = 64  # the second served trace: 64 jobs at epochs of 0.1 s
+SERVE_ORDER = 1  # admission least work first (bg3_serve_desc.order), passed over at most 8 times
 
 
 def peaks():
@@ -257,14 +259,18 @@ def run_bg3(args):
            "l2": "not evicted between steps: consecutive steps of one run, whose per-step state "
                  "(%.0f MB) fits the 129 MB L2" % (alg_bytes / 1e6)}
     err = net.error_word
-    batched = izh_stdp = served = growth = small = None
+    batched = izh_stdp = served = served64 = growth = small = None
     if world == 1:
         growth = run_growth()
         small = run_small()
         batched = run_batched(min(args.steps, 500), max(args.warmup, 20))
         izh_stdp = run_izh512(min(args.steps, 1000), max(args.warmup, 20))
         if args.serve_jobs > 0:
-            served = run_served(args.serve_jobs, int(args.serve_slots))
+            served = run_served(args.serve_jobs, int(args.serve_slots), order=SERVE_ORDER)
+            # a longer trace within the run's time: 64 jobs of the same families and epoch
+            # counts, at epochs of 0.1 s
+            served64 = run_served(SERVED_LONG_JOBS, int(args.serve_slots), epoch_duration=0.1,
+                                  order=SERVE_ORDER)
     else:
         # the batched and served forms spread over the ranks by instance (bin packed, no
         # collective); whole-job figures over the slowest rank
@@ -316,6 +322,7 @@ def run_bg3(args):
             "batched": batched,
             "batched_izh_stdp": izh_stdp,
             "served": served,
+            "served_64_jobs": served64,
             "gpu_launches": 2 * args.steps + 1,
             "clocks": clocks,
             "error_word": err,
@@ -460,7 +467,7 @@ def run_served_sharded(n_jobs, slots_cap, rank, world, chunk_steps=2000):
     from braingrid_gb300 import serve, shard, workloads
     trace = serve.sharded_trace(workloads.served_trace(n_jobs), rank, world)
     srv = serve.Server(hbm_budget_bytes=workloads.SERVED_BUDGET, max_resident=64,
-                       chunk_steps=chunk_steps, max_resident_slots=slots_cap)
+                       chunk_steps=chunk_steps, max_resident_slots=slots_cap, order=SERVE_ORDER)
     shard.barrier()  # one trace clock for all ranks
     times = serve.run_trace(srv, trace) if trace else {}
     srv.close()
@@ -661,16 +668,16 @@ def run_izh512(steps, warmup):
     return out
 
 
-def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
+def run_served(n_jobs, slots_cap=0, chunk_steps=2000, epoch_duration=1.0, order=0):
     """The served stream: a seeded open-loop Poisson trace (20 jobs/s) through the job server
     (continuous batching, footprint admission, 150 GB budget), then the same jobs one at a
     time through the plain API.  Latency = completion - arrival, host wall clock."""
     import time as _t
     from braingrid_gb300 import lib as bg
     from braingrid_gb300 import serve, workloads
-    trace = workloads.served_trace(n_jobs)
+    trace = workloads.served_trace(n_jobs, epoch_duration=epoch_duration)
     srv = serve.Server(hbm_budget_bytes=workloads.SERVED_BUDGET, max_resident=64,
-                       chunk_steps=chunk_steps, max_resident_slots=slots_cap)
+                       chunk_steps=chunk_steps, max_resident_slots=slots_cap, order=order)
     times = serve.run_trace(srv, trace)
     lat = {k: f - a for k, (a, f) in times.items()}
     finish = {k: f for k, (_, f) in times.items()}
@@ -683,7 +690,7 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     L = np.array([lat[j.id] for j in jobs])
     # plain: the same jobs, one at a time, each on its own network with bg3_step + epoch passes
     durations, setups = [], []
-    for _, job in workloads.served_trace(n_jobs):
+    for _, job in workloads.served_trace(n_jobs, epoch_duration=epoch_duration):
         d = job.desc
         t1 = _t.perf_counter()
         net = bg.Network(d.n_neurons, d.max_syn_per_neuron, d.width, d.height, d.epoch_duration,
@@ -711,8 +718,9 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000):
     pct = lambda x, q: float(np.percentile(x, q))
     return {"workload": "served stream: %d-job seeded Poisson trace at 20 jobs/s from the three "
                         "families (LIF sides U[10,200] pre-grown, Izhikevich N U[500,8000]), 1-20 "
-                        "epochs of 1 s, 150 GB admission budget" % n_jobs,
+                        "epochs of %g s, 150 GB admission budget" % (n_jobs, epoch_duration),
             "jobs": n_jobs, "all_ok": ok, "synapse_steps": syn_steps,
+            "admission_order": ["arrival", "least work first"][order],
             "max_resident_slots": int(slots_cap), "chunk_steps": chunk_steps,
             "served_p50_s": pct(L, 50), "served_p95_s": pct(L, 95), "served_p99_s": pct(L, 99),
             "served_makespan_s": span, "served_synapse_updates_per_s": syn_steps / span,
@@ -805,7 +813,8 @@ def main():
         print(json.dumps(run_small()), flush=True)
         return
     if args.only == "serve":
-        print(json.dumps(run_served(args.serve_jobs, int(args.serve_slots))), flush=True)
+        print(json.dumps(run_served(args.serve_jobs, int(args.serve_slots), order=SERVE_ORDER)),
+              flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -1,4 +1,5 @@
-// Served form of libbg3 (include/bg3_serve.h): FIFO admission by device footprint, continuous
+// Served form of libbg3 (include/bg3_serve.h): admission by device footprint (in arrival order
+// or least work first, with a bound on how often a job is passed over), continuous
 // batching of the resident jobs through the batched step (bg3_batch_*), per-job epoch ends.
 // Host code only; it drives the GPU through the public C-ABI.
 #include <algorithm>
@@ -120,18 +121,40 @@ static bool fits(const bg3_server *s, const Job *j)
     return true;
 }
 
-// Admits queued jobs in arrival order while the budgets and the job count allow; later jobs
-// may pass one that does not fit until it has been passed max_bypass times.
+// A queued job's work: synapse slots x the steps of its epochs still to run.
+static uint64_t work_left(const Job *j)
+{
+    const int64_t spe = std::max<int64_t>(1, steps_per_epoch(j->d.desc));
+    return j->slots * (uint64_t)std::max(0, j->d.epochs) * (uint64_t)spe;
+}
+
+// The queue index of the next job to admit, or -1: the oldest job once it has been passed
+// max_bypass times (or nothing while it does not fit), else the first fitting job in arrival
+// order, or the fitting job with the least work (ties to the earlier arrival).
+static long pick(const bg3_server *s)
+{
+    if (s->queue.empty()) return -1;
+    if (s->queue[0]->bypassed >= s->cfg.max_bypass) return fits(s, s->queue[0]) ? 0 : -1;
+    long best = -1;
+    for (size_t qi = 0; qi < s->queue.size(); qi++) {
+        const Job *j = s->queue[qi];
+        if (!fits(s, j)) continue;
+        if (s->cfg.order != BG3_ORDER_LEAST_WORK) return (long)qi;
+        if (best < 0 || work_left(j) < work_left(s->queue[(size_t)best])) best = (long)qi;
+    }
+    return best;
+}
+
+// Admits queued jobs (pick) while the budgets and the job count allow; every older job passed
+// over counts a bypass.
 static void admit(bg3_server *s)
 {
-    for (size_t qi = 0; qi < s->queue.size();) {
+    for (;;) {
         if ((int64_t)(s->resident.size() + s->joining.size()) >= s->cfg.max_resident) break;
+        const long p = pick(s);
+        if (p < 0) break;
+        const size_t qi = (size_t)p;
         Job *j = s->queue[qi];
-        if (qi > 0 && s->queue[0]->bypassed >= s->cfg.max_bypass) break;  // the head's turn
-        if (!fits(s, j)) {
-            qi++;
-            continue;
-        }
         for (size_t k = 0; k < qi; k++) s->queue[k]->bypassed++;
         s->queue.erase(s->queue.begin() + qi);
         s->bytes += (uint64_t)j->footprint;
@@ -171,7 +194,8 @@ extern "C" {
 
 int bg3_serve_create(const bg3_serve_desc *desc, bg3_server **out)
 {
-    if (!desc || !out || desc->max_resident <= 0 || desc->chunk_steps <= 0 || desc->max_bypass < 0)
+    if (!desc || !out || desc->max_resident <= 0 || desc->chunk_steps <= 0 || desc->max_bypass < 0 ||
+        (desc->order != BG3_ORDER_ARRIVAL && desc->order != BG3_ORDER_LEAST_WORK))
         return BG3_EINVAL;
     bg3_server *s = new (std::nothrow) bg3_server();
     if (!s) return BG3_ENOMEM;

@@ -18,7 +18,10 @@ SETUP_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
 class ServeDesc(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_resident", ctypes.c_int32),
                 ("chunk_steps", ctypes.c_int32), ("max_resident_slots", ctypes.c_uint64),
-                ("max_bypass", ctypes.c_int32)]
+                ("max_bypass", ctypes.c_int32), ("order", ctypes.c_int32)]
+
+
+ORDER_ARRIVAL, ORDER_LEAST_WORK = 0, 1  # bg3_serve_desc.order
 
 
 class JobResult(ctypes.Structure):
@@ -119,10 +122,10 @@ class Job:
 
 class Server:
     def __init__(self, hbm_budget_bytes=150 << 30, max_resident=64, chunk_steps=2000,
-                 max_resident_slots=0, max_bypass=8):
+                 max_resident_slots=0, max_bypass=8, order=ORDER_ARRIVAL):
         self.L = _bind()
         d = ServeDesc(int(hbm_budget_bytes), int(max_resident), int(chunk_steps),
-                      int(max_resident_slots), int(max_bypass))
+                      int(max_resident_slots), int(max_bypass), int(order))
         h = ctypes.c_void_p()
         bg.check(self.L.bg3_serve_create(ctypes.byref(d), ctypes.byref(h)), "bg3_serve_create")
         self.h = h

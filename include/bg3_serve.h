@@ -50,7 +50,13 @@ typedef struct {
     /* a job that does not fit may be passed by later jobs that do (backfill) at most this many
      * times; then admission waits for it */
     int32_t max_bypass;
+    /* which fitting queued job is admitted first: BG3_ORDER_ARRIVAL (0) the earliest,
+     * BG3_ORDER_LEAST_WORK (1) the one with the least work (synapse slots x steps); either way a
+     * job passed max_bypass times is admitted next (it ages into the head of the queue) */
+    int32_t order;
 } bg3_serve_desc;
+
+enum { BG3_ORDER_ARRIVAL = 0, BG3_ORDER_LEAST_WORK = 1 };
 
 /* Where a finished job's results go (host memory owned by the caller, valid until the job has
  * been returned by bg3_serve_take).  NULL pointers are skipped.  The histories are those of

@@ -136,6 +136,29 @@ def test_work_budget_backfills_small_jobs_past_a_large_one():
         check_same(a, j.outputs(), j.name)
 
 
+def test_least_work_first_admission_with_aging():
+    """ORDER_LEAST_WORK: with one job resident at a time the queued jobs are admitted least work
+    (synapse slots x steps) first, except that a job passed over max_bypass times goes next; the
+    results are the jobs' own either way."""
+    def jobs():
+        return [serve.lif_growth_job(20, 2, seed=21, radius=2.5, epoch_duration=T, name="big"),
+                serve.izh_static_job(10, 10, 2, seed=22, epoch_duration=T, name="two"),
+                serve.izh_static_job(10, 10, 1, seed=23, epoch_duration=T, name="one")]
+    alone = [run_alone(j) for j in jobs()]
+    for bypass, expect in ((8, ["one", "two", "big"]), (1, ["one", "big", "two"])):
+        js = jobs()
+        srv = serve.Server(max_resident=1, chunk_steps=400, max_bypass=bypass,
+                           order=serve.ORDER_LEAST_WORK)
+        for j in js:
+            srv.submit(j)
+        done = srv.run_all()
+        srv.close()
+        assert [j.name for j in done] == expect
+        for j, a in zip(js, alone):
+            assert j.result.status == 0
+            check_same(a, j.outputs(), j.name)
+
+
 @pytest.mark.parametrize("family", ["lif", "izh"])
 def test_exported_job_resumes_bit_exact(family):
     """A job exported after 2 of 4 epochs and resumed as a new job, in another server and among
