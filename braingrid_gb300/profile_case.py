@@ -1,6 +1,6 @@
 """Run a benchmark workload for a few steps, for profilers (ncu) to capture its kernels.
 
-    python -m braingrid_gb300.profile_case [--workload plain|sweep36|izh512|big|growth|growth200|heavy] [--steps 20] [--flush]
+    python -m braingrid_gb300.profile_case [--workload plain|sweep36|izh512|big|growth|growth200|heavy|small] [--steps 20] [--flush]
 
 plain is the 100x100 network of the headline, sweep36 the 36-network growth sweep, izh512 the
 Izhikevich + STDP batch (--count networks, 512 by default); big is three pre-grown LIF
@@ -8,7 +8,9 @@ networks of the served stream's largest sizes (166x166, 176x176, 180x180) after 
 growth pass (which restores the unscaled growth weights: the networks then fire at ~300 Hz),
 batched together.  heavy is one of those jobs (180x180) alone: 10,000 steps, a growth pass, 1,000
 steps (it then fires at ~300 Hz), then --steps steps timed kernel by kernel; its delivery passes
-after launch 11,000 are heavy ones.
+after launch 11,000 are heavy ones.  growth200 is the growth pass of the served stream's largest
+job (200x200, pre-grown); small the first configuration's 10x10 network on the one-CTA path
+(k_small_run, 4,096 steps per launch).
 """
 import argparse
 
@@ -21,7 +23,7 @@ def main():
     ap.add_argument("--flush", action="store_true", help="evict L2 before every step")
     ap.add_argument("--workload", default="plain",
                     choices=["plain", "sweep36", "izh512", "big", "growth", "growth200",
-                             "heavy"])
+                             "heavy", "small"])
     ap.add_argument("--count", type=int, default=512, help="networks of the izh512 workload")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
@@ -39,6 +41,16 @@ def main():
         net.growth(2)
         net.sync()
         print("synapses", net.total_synapses(), "error_word", net.error_word)
+        return
+    if a.workload == "small":
+        # the first configuration's 10x10 network (no synapse at its 0.4 start radius) on the
+        # one-CTA path: --steps whole steps, 4,096 per launch
+        from . import netgen
+        spec = netgen.lif_network(10, 10, frac_inh=0.10, seed=1)
+        net = netgen.make_gpu_network(spec, 100, noise_seed=1)
+        net.step(a.steps)
+        net.sync()
+        print("steps", a.steps, "launches", net.launches, "error_word", net.error_word)
         return
     if a.workload == "heavy":
         import numpy as np
