@@ -19,17 +19,23 @@ arrays are the reference's, bit for bit.  The noise generator is keyed by the fi
 stream pushed into BG3_NOISE_INJECT (lib.NormStream).
 
 Two element groups that the reference's files cannot express are read as well, so that the
-Izhikevich + STDP benchmark networks need no other override:
+Izhikevich + STDP benchmark networks need no other override.  They sit in <BG3Params>, a child of
+the root element that the reference's readers never visit (so its driver reads such a file, and
+the drop-in driver of braingrid_gb300/dropin applies the STDP constants), or, as this reader
+also accepts, inside <SynapsesParams> / <NeuronsParams> (where the reference's reader rejects
+them):
 
-  <SynapsesParams class="AllSTDPSynapses|AllDynamicSTDPSynapses"><STDPParams> holding any of
+  <STDPParams> (synapse classes AllSTDPSynapses, AllDynamicSTDPSynapses) holding any of
       Apos, Aneg, STDPgap, tauspost, tauspre, taupos, tauneg, WexExc, WexInh, mupos, muneg,
       useFroemkeDanSTDP: the constants of every synapse made (by ConnStatic or by growth), in
       place of AllSTDPSynapses::createSynapse's built-in ones (Synapses/AllSTDPSynapses.cpp:
       252-273); Wex is WexInh for synapses from inhibitory neurons, WexExc otherwise;
-  <NeuronsParams class="AllIZHNeurons"><ParameterDraw>r_squared</ParameterDraw>: Izhikevich's
-      (2003) spread instead of four flat ranges.  One draw r = inRange(0, 1) per neuron after its
-      IF draws; excitatory a = 0.02, b = 0.2, c = -65 + 15 r r, d = 8 - 6 r r; inhibitory
-      a = 0.02 + 0.08 r, b = 0.25 - 0.05 r, c = -65, d = 2 (float arithmetic, left to right).
+  <ParameterDraw>r_squared</ParameterDraw> (AllIZHNeurons): Izhikevich's (2003) spread instead
+      of four flat ranges.  One draw r = inRange(0, 1) per neuron after its IF draws; excitatory
+      a = 0.02, b = 0.2, c = -65 + 15 r r, d = 8 - 6 r r; inhibitory a = 0.02 + 0.08 r,
+      b = 0.25 - 0.05 r, c = -65, d = 2 (float arithmetic, left to right).  The drop-in driver
+      refuses it: the draw happens inside the reference's own setup, which that driver runs
+      unchanged.
 
 One difference from the reference: ConnStatic keeps each source's nConnsPerNeuron nearest
 neurons with equal distances in neuron-index order.  The reference sorts with std::sort, which
@@ -313,12 +319,17 @@ def read(config, stim=None, root=None):
     model = doc.find("ModelParams")
     if model is None:
         raise ConfigError("missing ModelParams")
-    _read_neurons(p, model.find("NeuronsParams"))
+    ext = doc.find("BG3Params")
+    if ext is not None:
+        unknown = [e.tag for e in ext if e.tag not in ("STDPParams", "ParameterDraw")]
+        if unknown:
+            raise ConfigError("unknown BG3Params element %r" % unknown[0])
+    _read_neurons(p, model.find("NeuronsParams"), ext)
     syn = model.find("SynapsesParams")
     p.synapse_class = syn.get("class", "") if syn is not None else ""
     if p.synapse_class not in SYNAPSE_CLASSES:
         raise ConfigError("unsupported synapse class %r" % p.synapse_class)
-    st = _child(syn, "STDPParams")
+    st = _extension(syn, ext, "STDPParams")
     if st is not None:
         if p.synapse_kind < bg.BG3_SYN_STDP:
             raise ConfigError("STDPParams given for %s" % p.synapse_class)
@@ -335,7 +346,15 @@ def read(config, stim=None, root=None):
     return p
 
 
-def _read_neurons(p, sec):
+def _extension(sec, ext, tag):
+    """The element tag of this reader's extensions: in <BG3Params> (ext) or inside sec, not both."""
+    a, b = _child(sec, tag), _child(ext, tag)
+    if a is not None and b is not None:
+        raise ConfigError("%s given twice" % tag)
+    return a if a is not None else b
+
+
+def _read_neurons(p, sec, ext=None):
     if sec is None or sec.get("class") not in NEURON_CLASSES:
         raise ConfigError("unsupported neuron class %r" % (sec.get("class") if sec is not None
                                                             else None))
@@ -347,8 +366,10 @@ def _read_neurons(p, sec):
         if lo > hi:
             raise ConfigError("%s: min above max" % name)
         p.if_ranges[name] = (lo, hi)
+    d = _extension(sec, ext, "ParameterDraw")
+    if d is not None and p.neuron_class != "AllIZHNeurons":
+        raise ConfigError("ParameterDraw given for %s" % p.neuron_class)
     if p.neuron_class == "AllIZHNeurons":
-        d = _child(sec, "ParameterDraw")
         p.izh_draw = _text(d, "ParameterDraw") if d is not None else "ranges"
         if p.izh_draw not in ("ranges", "r_squared"):
             raise ConfigError("ParameterDraw must be ranges or r_squared")
@@ -449,8 +470,8 @@ def write(p, lists_dir="configfiles/bg3", name="network"):
     """p as a parameter file in the reference's element layout (the reverse of read), plus the
     neuron-list files it names: returns (text, {relative path: list-file text}).  Values are
     written with Python's shortest round-trip repr, so reading the text back gives p's float32
-    values exactly.  A file with STDPParams or ParameterDraw r_squared is this library's; the
-    reference's reader rejects those elements."""
+    values exactly.  STDP constants and the r_squared draw go into <BG3Params> (see the module
+    docstring), which the reference's driver reads past."""
     def v(x):
         return repr(float(x)) if not isinstance(x, (int, np.integer)) else str(int(x))
 
@@ -459,10 +480,11 @@ def write(p, lists_dir="configfiles/bg3", name="network"):
             tag, tag, v(lo), v(hi), tag)
 
     files = {}
+    ext = []
     neu = [rng(k, *p.if_ranges[k]) for k in IF_RANGES]
     if p.neuron_class == "AllIZHNeurons":
         if p.izh_draw == "r_squared":
-            neu.append("<ParameterDraw>r_squared</ParameterDraw>")
+            ext.append("<ParameterDraw>r_squared</ParameterDraw>")
         else:
             for k in IZH_RANGES:
                 z = p.izh_ranges[k]
@@ -471,8 +493,8 @@ def write(p, lists_dir="configfiles/bg3", name="network"):
                     for t, x in zip(("minExc", "maxExc", "minInh", "maxInh"), z)), k))
     syn = ""
     if p.stdp is not None:
-        syn = "<STDPParams>%s</STDPParams>" % "".join(
-            "<%s>%s</%s>" % (k, v(p.stdp[k]), k) for k in STDP_DEFAULTS)
+        ext.append("<STDPParams>%s</STDPParams>" % "".join(
+            "<%s>%s</%s>" % (k, v(p.stdp[k]), k) for k in STDP_DEFAULTS))
     if p.conn_class == "ConnGrowth":
         g = p.growth
         conn = '<GrowthParams name="GrowthParams">%s</GrowthParams>' % "".join(
@@ -526,10 +548,11 @@ def write(p, lists_dir="configfiles/bg3", name="network"):
         '    <SynapsesParams class="%s" name="SynapsesParams">%s</SynapsesParams>\n'
         '    <ConnectionsParams class="%s" name="ConnectionsParams">%s</ConnectionsParams>\n'
         '    <LayoutParams class="%s" name="LayoutParams">%s</LayoutParams>\n'
-        '  </ModelParams>\n</BGSimParams>\n' % (
+        '  </ModelParams>\n%s</BGSimParams>\n' % (
             p.width, p.height, v(p.tsim), p.epochs, p.max_firing_rate, p.max_syn, p.seed,
             p.output or "results/%s-out.xml" % name, p.neuron_class, "".join(neu),
-            p.synapse_class, syn, p.conn_class, conn, p.layout_class, layout))
+            p.synapse_class, syn, p.conn_class, conn, p.layout_class, layout,
+            "  <BG3Params>%s</BG3Params>\n" % "".join(ext) if ext else ""))
     return text, files
 
 

@@ -10,7 +10,9 @@
 // What the model does on each interface call (Core/IModel.h:64-151):
 //   setupSim           host setup as the reference (Model::setupSim), then one bg3_net for the
 //                      whole network, filled from the host objects through the classes' own
-//                      copy*HostToDevice members (bg3_classes.cpp);
+//                      copy*HostToDevice members (bg3_classes.cpp); an STDP class's constants
+//                      come from the parameter file's <BG3Params><STDPParams> where it has one
+//                      (read_bg3_params);
 //   advance            queues the step; queued steps run as one bg3_step call (CUDA-graph replays
 //                      inside the library) when BG3_STEPS_PER_CALL steps have queued, or when the
 //                      state is next observed (epoch end, checkpoint, cleanup);
@@ -49,14 +51,19 @@
 #include "GPUSpikingModel.h"
 #include "Global.h"
 #include "bg3_dropin.h"
+#include "tinyxml.h"
 
 namespace {
 
 // What this model keeps beside the reference's class layout (whose members are the reference's
 // device pointers): the network, the queued steps and the noise drawn ahead.
+// Values of <BG3Params><STDPParams> by name (absent names keep createSynapse's values).
+typedef std::map<std::string, double> StdpParams;
+
 struct ModelState {
     bg3_net *net;
     bg3_norm *gen;                        // the reference's noise stream (reference noise only)
+    StdpParams stdp;                      // the parameter file's STDP constants
     bool reference_noise;
     int64_t chunk;                        // steps per bg3_step call
     int64_t queued;                       // steps advance() queued and not yet launched
@@ -100,10 +107,85 @@ AllSpikingSynapses *scratch_synapses(int32_t kind)
     }
 }
 
+// <BG3Params>, a child of the parameter file's root element: the reference's readers take their
+// elements by name (<SimInfoParams>, Core/SimulationInfo.cpp:24; <ModelParams>,
+// Core/FClassOfCategory.cpp:249) and never visit it.  <BG3Params><STDPParams> holds any of the
+// names below: the constants of every synapse of an STDP class, in place of the ones
+// AllSTDPSynapses::createSynapse writes (Synapses/AllSTDPSynapses.cpp:252-273); Wex is WexInh for
+// synapses from inhibitory neurons (II, IE) and WexExc otherwise, as braingrid_gb300.config
+// reads the same element.  <ParameterDraw> (the Izhikevich r^2 draw) is drawn inside the
+// reference's own AllIZHNeurons::createNeuron, which this driver runs unchanged, so a file
+// that asks for it is refused here.
+const char *const STDP_NAMES[] = {"Apos", "Aneg", "STDPgap", "tauspost", "tauspre", "taupos",
+                                  "tauneg", "WexExc", "WexInh", "mupos", "muneg",
+                                  "useFroemkeDanSTDP"};
+
+void refuse(const std::string &file, const std::string &what)
+{
+    fprintf(stderr, "%s: <BG3Params>: %s\n", file.c_str(), what.c_str());
+    exit(EXIT_FAILURE);
+}
+
+StdpParams read_bg3_params(const std::string &file)
+{
+    StdpParams out;
+    TiXmlDocument doc(file.c_str());
+    if (!doc.LoadFile()) return out;  // the reference's reader has already reported it
+    TiXmlElement *root = doc.FirstChildElement();
+    TiXmlElement *bp = root ? root->FirstChildElement("BG3Params") : NULL;
+    if (!bp) return out;
+    for (TiXmlElement *e = bp->FirstChildElement(); e; e = e->NextSiblingElement()) {
+        if (e->ValueStr() != "STDPParams")
+            refuse(file, "<" + e->ValueStr() + "> is not applied by this driver");
+        for (TiXmlElement *f = e->FirstChildElement(); f; f = f->NextSiblingElement()) {
+            const std::string name = f->ValueStr();
+            bool known = false;
+            for (size_t k = 0; k < sizeof(STDP_NAMES) / sizeof(STDP_NAMES[0]); k++)
+                known = known || name == STDP_NAMES[k];
+            const char *text = f->GetText();
+            if (!known || !text) refuse(file, "unknown or empty <STDPParams> element <" + name + ">");
+            out[name] = atof(text);
+        }
+    }
+    return out;
+}
+
+// The file's value for name, else dflt; as a float, the way the reference reads parameters.
+float stdp_value(const StdpParams &p, const char *name, float dflt)
+{
+    StdpParams::const_iterator it = p.find(name);
+    return it == p.end() ? dflt : (float)it->second;
+}
+
+// Writes the file's STDP constants into the host synapses the reference's setup made (before
+// they are uploaded).
+void apply_stdp_to_host(IAllSynapses *syn, const StdpParams &p)
+{
+    AllSTDPSynapses *s = dynamic_cast<AllSTDPSynapses *>(syn);
+    if (!s || p.empty()) return;
+    const BGSIZE total = (BGSIZE)s->count_neurons * s->maxSynapsesPerNeuron;
+    for (BGSIZE i = 0; i < total; i++) {
+        if (!s->in_use[i]) continue;
+        const bool inh_src = s->type[i] == II || s->type[i] == IE;
+        s->Apos[i] = stdp_value(p, "Apos", s->Apos[i]);
+        s->Aneg[i] = stdp_value(p, "Aneg", s->Aneg[i]);
+        s->STDPgap[i] = stdp_value(p, "STDPgap", s->STDPgap[i]);
+        s->tauspost[i] = stdp_value(p, "tauspost", s->tauspost[i]);
+        s->tauspre[i] = stdp_value(p, "tauspre", s->tauspre[i]);
+        s->taupos[i] = stdp_value(p, "taupos", s->taupos[i]);
+        s->tauneg[i] = stdp_value(p, "tauneg", s->tauneg[i]);
+        s->Wex[i] = stdp_value(p, inh_src ? "WexInh" : "WexExc", s->Wex[i]);
+        s->mupos[i] = stdp_value(p, "mupos", s->mupos[i]);
+        s->muneg[i] = stdp_value(p, "muneg", s->muneg[i]);
+        s->useFroemkeDanSTDP[i] = stdp_value(p, "useFroemkeDanSTDP", s->useFroemkeDanSTDP[i] ? 1.0f : 0.0f) != 0.0f;
+    }
+}
+
 // The per-type constants of synapses the device growth pass creates, taken from the reference's
 // own createSynapse (one synapse of each type II, IE, EI, EE on a scratch object), so that they
-// are the reference's values for this deltaT by construction.
-void set_type_constants(bg3_net *net, int32_t kind, const SimulationInfo *si)
+// are the reference's values for this deltaT by construction; the STDP ones then take the
+// parameter file's <BG3Params> values (fp), like the synapses the host setup made.
+void set_type_constants(bg3_net *net, int32_t kind, const SimulationInfo *si, const StdpParams &fp)
 {
     AllSpikingSynapses *s = scratch_synapses(kind);
     BGFLOAT sp = 0;
@@ -140,6 +222,21 @@ void set_type_constants(bg3_net *net, int32_t kind, const SimulationInfo *si)
             k.taupos[t] = p->taupos[t]; k.tauneg[t] = p->tauneg[t]; k.Wex[t] = p->Wex[t];
             k.mupos[t] = p->mupos[t]; k.muneg[t] = p->muneg[t];
             k.useFroemkeDanSTDP[t] = p->useFroemkeDanSTDP[t] ? 1 : 0;
+        }
+        if (!fp.empty()) {  // the parameter file's constants (apply_stdp_to_host, per type)
+            for (int t = 0; t < 4; t++) {
+                k.Apos[t] = stdp_value(fp, "Apos", k.Apos[t]);
+                k.Aneg[t] = stdp_value(fp, "Aneg", k.Aneg[t]);
+                k.STDPgap[t] = stdp_value(fp, "STDPgap", k.STDPgap[t]);
+                k.tauspost[t] = stdp_value(fp, "tauspost", k.tauspost[t]);
+                k.tauspre[t] = stdp_value(fp, "tauspre", k.tauspre[t]);
+                k.taupos[t] = stdp_value(fp, "taupos", k.taupos[t]);
+                k.tauneg[t] = stdp_value(fp, "tauneg", k.tauneg[t]);
+                k.Wex[t] = stdp_value(fp, (t == II || t == IE) ? "WexInh" : "WexExc", k.Wex[t]);
+                k.mupos[t] = stdp_value(fp, "mupos", k.mupos[t]);
+                k.muneg[t] = stdp_value(fp, "muneg", k.muneg[t]);
+                k.useFroemkeDanSTDP[t] = stdp_value(fp, "useFroemkeDanSTDP", (float)k.useFroemkeDanSTDP[t]) != 0.0f;
+            }
         }
         bg3_dropin_check(bg3_set_stdp_constants(net, &k), "bg3_set_stdp_constants");
     }
@@ -222,7 +319,7 @@ void GPUSpikingModel::allocDeviceStruct(void **allNeuronsDevice, void **allSynap
     bg3_dropin_check(bg3_upload_layout(st.net, &(*m_layout->xloc)[0], &(*m_layout->yloc)[0],
                                        types.data()),
                      "bg3_upload_layout");
-    set_type_constants(st.net, d.synapse_kind, sim_info);
+    set_type_constants(st.net, d.synapse_kind, sim_info, st.stdp);
     m_neurons->copyNeuronHostToDevice(*allNeuronsDevice, sim_info);
     m_synapses->copySynapseHostToDevice(*allSynapsesDevice, sim_info);
     if (ConnGrowth *g = dynamic_cast<ConnGrowth *>(m_conns)) {
@@ -257,9 +354,17 @@ void GPUSpikingModel::deleteDeviceStruct(void **allNeuronsDevice, void **allSyna
 
 void GPUSpikingModel::setupSim(SimulationInfo *sim_info)
 {
+    ModelState &st = state_of(this);
+    st.stdp = read_bg3_params(sim_info->stateInputFileName);
+    if (!st.stdp.empty()) {
+        if (!dynamic_cast<AllSTDPSynapses *>(m_synapses))
+            refuse(sim_info->stateInputFileName, "STDPParams given for a synapse class without STDP");
+        fprintf(stderr, "BG3Params: %d STDP constants from %s\n", (int)st.stdp.size(),
+                sim_info->stateInputFileName.c_str());
+    }
     bg3_dropin_check(bg3_set_device(g_deviceId), "bg3_set_device");
     Model::setupSim(sim_info);
-    ModelState &st = state_of(this);
+    apply_stdp_to_host(m_synapses, st.stdp);
     const char *noise = getenv("BG3_NOISE");
     st.reference_noise = !(noise && std::string(noise) == "device");
     st.chunk = env_int("BG3_STEPS_PER_CALL", 1000);

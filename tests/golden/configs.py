@@ -240,8 +240,9 @@ STDP_NAMES = ("Apos", "Aneg", "STDPgap", "tauspost", "tauspre", "taupos", "taune
 
 def config_text(c, stdp_params=False):
     """The case's BrainGrid parameter file.  stdp_params=True adds the case's STDP constants as
-    an <STDPParams> element (read by braingrid_gb300.config; the reference harness takes them
-    with --stdp instead)."""
+    an <STDPParams> element inside <SynapsesParams>, stdp_params="root" inside a root-level
+    <BG3Params> (both read by braingrid_gb300.config, the second also by the drop-in driver; the
+    reference harness takes them with --stdp instead)."""
     p = dict(c)
     p.update(c["growth"])
     p["synapse_class"] = SYN_CLASS[c.get("synapse", 1)]
@@ -258,9 +259,14 @@ def config_text(c, stdp_params=False):
     text = _XML.format(**p)
     if stdp_params and c.get("stdp") is not None:
         st = "".join("<%s>%r</%s>" % (k, float(v), k) for k, v in zip(STDP_NAMES, c["stdp"]))
-        text = text.replace('name="SynapsesParams"></SynapsesParams>',
-                            'name="SynapsesParams"><STDPParams>%s</STDPParams></SynapsesParams>'
-                            % st)
+        if stdp_params == "root":
+            text = text.replace("</BGSimParams>",
+                                "<BG3Params><STDPParams>%s</STDPParams></BG3Params>\n"
+                                "</BGSimParams>" % st)
+        else:
+            text = text.replace('name="SynapsesParams"></SynapsesParams>',
+                                'name="SynapsesParams"><STDPParams>%s</STDPParams>'
+                                '</SynapsesParams>' % st)
     return text
 
 

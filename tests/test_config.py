@@ -6,6 +6,8 @@ from the same file (the fixtures' setup arrays), bit for bit, and with the oracl
 fixtures hold no setup copy (input arrays).  ConnStatic's wiring is compared up to the order of
 equal distances (see config's docstring).  No GPU: the network itself is built in
 test_gpu_config.py."""
+import os
+
 import numpy as np
 import pytest
 
@@ -231,6 +233,51 @@ def test_refused_files(tmp_path):
         cf.read(good.replace('name="SynapsesParams"></SynapsesParams>',
                              'name="SynapsesParams"><STDPParams><Apos>1</Apos></STDPParams>'
                              '</SynapsesParams>'), root=str(tmp_path))
+
+
+def test_extensions_in_bg3params(tmp_path):
+    """<STDPParams> / <ParameterDraw> in a root-level <BG3Params> (which the reference's readers
+    do not visit) read as they do inside the model's sections; config.write puts them there."""
+    c = case("izh_static")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    inside = cf.read(configs.config_text(c, stdp_params=True), root=str(tmp_path))
+    root_text = configs.config_text(c, stdp_params="root")
+    outside = cf.read(root_text, root=str(tmp_path))
+    assert outside.stdp is not None and outside.stdp == inside.stdp
+    assert "<BG3Params>" in root_text and "<STDPParams>" not in root_text.split("</ModelParams>")[0]
+    text, files = cf.write(outside)
+    assert "<BG3Params><STDPParams>" in text and "<STDPParams>" not in text.split("</ModelParams>")[0]
+    for rel, body in files.items():
+        os.makedirs(os.path.dirname(str(tmp_path / rel)), exist_ok=True)
+        with open(str(tmp_path / rel), "w") as f:
+            f.write(body)
+    assert cf.read(text, root=str(tmp_path)).stdp == outside.stdp
+    bad = [
+        # the same element twice
+        configs.config_text(c, stdp_params=True).replace(
+            "</BGSimParams>", "<BG3Params><STDPParams><Apos>1</Apos></STDPParams></BG3Params>"
+            "</BGSimParams>"),
+        # an element this reader does not know
+        root_text.replace("<BG3Params>", "<BG3Params><Bogus>1</Bogus>"),
+        # STDP constants for a synapse class without STDP
+        root_text.replace("AllDynamicSTDPSynapses", "AllDSSynapses"),
+    ]
+    for b in bad:
+        assert b != root_text
+        with pytest.raises(cf.ConfigError):
+            cf.read(b, root=str(tmp_path))
+    # the r^2 draw in BG3Params, for Izhikevich neurons and (refused) for LIF ones
+    izh = cf.read(root_text.replace("<BG3Params>",
+                                    "<BG3Params><ParameterDraw>r_squared</ParameterDraw>"),
+                  root=str(tmp_path))
+    assert izh.izh_draw == "r_squared"
+    lif = case("c0")
+    configs.write_case(lif, str(tmp_path / "configfiles"))
+    for b in (configs.config_text(lif).replace(
+            "</BGSimParams>", "<BG3Params><ParameterDraw>r_squared</ParameterDraw></BG3Params>"
+            "</BGSimParams>"),):
+        with pytest.raises(cf.ConfigError):
+            cf.read(b, root=str(tmp_path))
 
 
 def test_norm_stream_matches_the_oracle():

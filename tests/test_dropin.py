@@ -75,3 +75,33 @@ def test_driver_reaches_the_drop_in(driver, tmp_path):
         # no device: the model's first C-ABI call reports it and the driver exits as the
         # reference's HANDLE_ERROR does
         assert r.returncode != 0 and "bg3_set_device" in out, out
+
+
+def _run_driver(tmp_path, text, name):
+    cfg = tmp_path / "configfiles" / "bg3" / (name + ".xml")
+    cfg.write_text(text)
+    (tmp_path / "results").mkdir(exist_ok=True)
+    r = subprocess.run([EXE, "-t", str(cfg.relative_to(tmp_path))], cwd=str(tmp_path),
+                       capture_output=True, text=True, timeout=120)
+    return r.returncode, r.stdout + r.stderr
+
+
+def test_bg3params_stdp_constants_reach_the_drop_in(driver, tmp_path):
+    """A parameter file carrying STDP constants in a root-level <BG3Params> (the Izhikevich +
+    dynamic STDP + ConnStatic case): the reference's readers take the file, the drop-in reads the
+    eleven constants before its first C-ABI call; <ParameterDraw> there, and STDP constants for a
+    class without STDP, are refused with a message."""
+    from tests.golden import configs
+    from tests.golden.configs import case
+    c = case("izh_static")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    text = configs.config_text(c, stdp_params="root")
+    rc, out = _run_driver(tmp_path, text, "izh_static_bg3")
+    assert "BG3Params: 11 STDP constants from configfiles/bg3/izh_static_bg3.xml" in out, out
+    assert "Unrecognized" not in out
+    rc, out = _run_driver(tmp_path, text.replace("<BG3Params>", "<BG3Params><ParameterDraw>"
+                                                 "r_squared</ParameterDraw>"), "izh_draw")
+    assert rc != 0 and "<ParameterDraw> is not applied by this driver" in out, out
+    rc, out = _run_driver(tmp_path, text.replace("AllDynamicSTDPSynapses", "AllDSSynapses"),
+                          "izh_ds")
+    assert rc != 0 and "STDPParams given for a synapse class without STDP" in out, out
