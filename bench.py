@@ -62,7 +62,7 @@ REF_LAYOUT_BYTES_PER_SYN = 28
 # served form: resident work cap, about one and a half of the largest jobs' synapse slots
 SERVE_SLOTS = 60e6
 SERVED_LONG_JOBS = 64  # the second served trace: 64 jobs at epochs of 0.1 s
-SERVE_ORDER = 1  # admission least work first (bg3_serve_desc.order), passed over at most 8 times
+SERVE_ORDER = 0  # admission in arrival order with backfill (bg3_serve_desc.order)
 
 
 def peaks():
@@ -668,7 +668,7 @@ def run_izh512(steps, warmup):
     return out
 
 
-def run_served(n_jobs, slots_cap=0, chunk_steps=2000, epoch_duration=1.0, order=0):
+def run_served(n_jobs, slots_cap=0, chunk_steps=2000, epoch_duration=1.0, order=0, max_bypass=8):
     """The served stream: a seeded open-loop Poisson trace (20 jobs/s) through the job server
     (continuous batching, footprint admission, 150 GB budget), then the same jobs one at a
     time through the plain API.  Latency = completion - arrival, host wall clock."""
@@ -677,7 +677,8 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000, epoch_duration=1.0, order=
     from braingrid_gb300 import serve, workloads
     trace = workloads.served_trace(n_jobs, epoch_duration=epoch_duration)
     srv = serve.Server(hbm_budget_bytes=workloads.SERVED_BUDGET, max_resident=64,
-                       chunk_steps=chunk_steps, max_resident_slots=slots_cap, order=order)
+                       chunk_steps=chunk_steps, max_resident_slots=slots_cap, order=order,
+                       max_bypass=max_bypass)
     times = serve.run_trace(srv, trace)
     lat = {k: f - a for k, (a, f) in times.items()}
     finish = {k: f for k, (_, f) in times.items()}
@@ -721,6 +722,7 @@ def run_served(n_jobs, slots_cap=0, chunk_steps=2000, epoch_duration=1.0, order=
                         "epochs of %g s, 150 GB admission budget" % (n_jobs, epoch_duration),
             "jobs": n_jobs, "all_ok": ok, "synapse_steps": syn_steps,
             "admission_order": ["arrival", "least work first"][order],
+            "max_bypass": max_bypass,
             "max_resident_slots": int(slots_cap), "chunk_steps": chunk_steps,
             "served_p50_s": pct(L, 50), "served_p95_s": pct(L, 95), "served_p99_s": pct(L, 99),
             "served_makespan_s": span, "served_synapse_updates_per_s": syn_steps / span,

@@ -726,10 +726,11 @@ __device__ __forceinline__ void sweep_finish(const NetDev &n, int d, bool valid,
         const unsigned long long t1 = t + 1;
         bool fired = false;
         if (valid) {
+            // the summation point stays 0: the call's first neuron pass cleared it, and a fused
+            // sweep hands its sum to the update directly
             const int br = neuron_branch(x);
             fired = neuron_apply<FF>(n, d, x, br, input_apply(n, d, x, t1, acc),
                                      br == BR_INTEGRATE ? noise : 0.0f, t1, izh_mode(n, d));
-            gst(&n.sp[d], 0.0f);
         }
         ring_push(n, t1, fired, d);
     } else if (valid) {
