@@ -332,6 +332,17 @@ def run_bg3(args):
         dist.destroy_process_group()
 
 
+def _batch_graph_seconds(batch, steps):
+    """Host wall clock around batch.step(steps): the path a caller runs (CUDA graphs of 32 fused
+    steps, each step's sweep overlapping the kernels before it), synchronised on both sides."""
+    import time as _t
+    batch.sync()
+    t0 = _t.perf_counter()
+    batch.step(steps)
+    batch.sync()
+    return _t.perf_counter() - t0
+
+
 def run_batched(steps, warmup):
     """The 36-network growth sweep as one batch (one launch per kernel per step) against the
     same networks run one network at a time with bg3_step (each on its own CUDA graph)."""
@@ -349,6 +360,7 @@ def run_batched(steps, warmup):
     # batched: device time per step with CUDA events (the working set, ~1 GB, exceeds L2)
     ms = batch.bench_steps(steps)
     t_batch = float(np.sum(ms)) / 1e3
+    t_graph = _batch_graph_seconds(batch, steps)
     # plain: every network advanced on its own for the same number of steps, back to back
     for n in nets:
         n.step(warmup)
@@ -388,7 +400,14 @@ def run_batched(steps, warmup):
            "plain_lockstep_ms_per_step": t_lock * 1e3,
            "plain_lockstep_timing": "host wall clock, %d steps of 36 bg3_step(1) calls" % lock,
            "batched_over_plain": t_plain / t_batch,
-           "batched_over_plain_lockstep": t_lock * steps / t_batch, "error_word": int(err),
+           "batched_over_plain_lockstep": t_lock * steps / t_batch,
+           "batched_timing": "CUDA events around each step (the step's kernels launched one by "
+                             "one, the next step's sweep not overlapping them)",
+           "batched_graph_ms_per_step": t_graph * 1e3 / steps,
+           "batched_graph_synapse_updates_per_s": S * steps / t_graph,
+           "batched_graph_timing": "host wall clock around one bg3_batch_step call (CUDA graphs "
+                                   "of 32 steps), as the plain form",
+           "batched_graph_over_plain": t_plain / t_graph, "error_word": int(err),
            "launch": launch}
     batch.close()
     for n in nets:
@@ -635,6 +654,7 @@ def run_izh512(steps, warmup):
     batch.sync()
     ms = batch.bench_steps(steps)
     t_batch = float(np.sum(ms)) / 1e3
+    t_graph = _batch_graph_seconds(batch, steps)
     for n in nets:
         n.step(warmup)
     for n in nets:
@@ -660,7 +680,17 @@ def run_izh512(steps, warmup):
            "plain_ms_per_step": t_plain * 1e3 / steps,
            "plain_timing": "host wall clock around %d sequential bg3_step runs" % len(nets),
            "batched_over_plain": t_plain / t_batch,
-           "mean_rate_hz": spikes / float(N) / ((steps + 2 * warmup) * 1e-4),
+           "batched_timing": "CUDA events around each step (the step's kernels launched one by "
+                             "one, the next step's sweep not overlapping them)",
+           "batched_graph_ms_per_step": t_graph * 1e3 / steps,
+           "batched_graph_synapse_updates_per_s": S * steps / t_graph,
+           "batched_graph_neuron_steps_per_s": N * steps / t_graph,
+           "batched_graph_timing": "host wall clock around one bg3_batch_step call (CUDA graphs "
+                                   "of 32 steps), as the plain form",
+           "batched_graph_over_plain": t_plain / t_graph,
+           # every network ran warmup + steps (events) + steps (graph) in the batch, then
+           # warmup + steps on its own
+           "mean_rate_hz": spikes / float(N) / ((3 * steps + 2 * warmup) * 1e-4),
            "error_word": int(err), "launch": launch}
     batch.close()
     for n in nets:
