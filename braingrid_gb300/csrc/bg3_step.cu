@@ -918,17 +918,20 @@ __device__ __forceinline__ void sweep_tile(const NetDev &n, const CUtensorMap *t
 }
 
 // psr *= decay for the first nq row quads of a 32-dest tile and the sum of each dest's rows in
-// row order (one lane per dest; a row quad is one coalesced 16-byte load per lane).
+// row order (one lane per dest; a row quad is one coalesced 16-byte load per lane).  between()
+// runs once the first four row quads' loads are issued and before their data is used: work that
+// needs no row data (the neuron pass's noise draw) then hides their latency.
+template <typename F>
 __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, const int nq,
-                                           const int lane)
+                                           const int lane, F &&between)
 {
     // this tile's row quads: [Mq][32 lanes] float4 of psr, 16 bits of class codes
     float4 *P = reinterpret_cast<float4 *>(n.psr) + (size_t)tile * n.Mq * 32 + lane;
     const uint16_t *C = reinterpret_cast<const uint16_t *>(n.dcls) + (size_t)tile * n.Mq * 32 + lane;
     float acc = 0.0f;
-    for (int q = 0; q < nq; q += 4) {
-        float4 v[4];
-        uint32_t c[4];
+    float4 v[4];
+    uint32_t c[4];
+    auto load = [&](int q) {
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (q + j < nq) {
@@ -936,6 +939,8 @@ __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, cons
                 c[j] = C[(size_t)(q + j) * 32];
             }
         }
+    };
+    auto apply = [&](int q) {
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (q + j < nq) {
@@ -950,8 +955,21 @@ __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, cons
                 acc = acc + v[j].w;
             }
         }
+    };
+    load(0);
+    between();
+    apply(0);
+    for (int q = 4; q < nq; q += 4) {
+        load(q);
+        apply(q);
     }
     return acc;
+}
+
+__device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, const int nq,
+                                           const int lane)
+{
+    return thin_rows(n, tile, nq, lane, [] {});
 }
 
 // Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
@@ -971,11 +989,10 @@ __device__ __forceinline__ void sweep_thin_tile(const NetDev &n, const int tile,
     const bool valid = d < n.N;
     NeuronIn x;
     float noise = 0.0f;
-    if (FUSE && valid) {
-        neuron_load(n, d, x);  // in flight with the row loads below
-        noise = normal_device(n.noise_seed, t + 1, d);
-    }
-    const float acc = thin_rows(n, tile, nq, lane);
+    if (FUSE && valid) neuron_load(n, d, x);  // in flight with the row loads
+    const float acc = thin_rows(n, tile, nq, lane, [&] {
+        if (FUSE && valid) noise = normal_device(n.noise_seed, t + 1, d);
+    });
     sweep_finish<FUSE>(n, d, valid, acc, t, lane, x, noise, n.ntiles);
 }
 
