@@ -1007,15 +1007,18 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(const __grid_constant__ Ne
 }
 
 // Batched form: one launch sweeps every tile of every network of a batch.  tiles[b] = (network,
-// tile); maps holds each network's two tensor maps (psr, class) in global memory.
+// tile); maps holds each network's two tensor maps (psr, class) in global memory; the block's
+// network descriptor is copied into shared memory first (block_copy_desc).
 template <bool FUSE, int ST>
 __global__ void __launch_bounds__(SW_THREADS) k_sweep_batch(const NetDev *nets,
                                                             const CUtensorMap *maps,
                                                             const int2 *tiles)
 {
     extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(16) NetDev s_net;
     const int2 tr = tiles[blockIdx.x];
-    sweep_tile<FUSE, ST, SW_DESTS>(nets[tr.x], &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
+    block_copy_desc(&s_net, nets + tr.x);
+    sweep_tile<FUSE, ST, SW_DESTS>(s_net, &maps[2 * tr.x], &maps[2 * tr.x + 1], tr.y, smem_raw);
 }
 
 // Row-quad count of a thin tile (read before pdl_wait: the counts change only between calls).
