@@ -956,9 +956,9 @@ __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, cons
             }
         }
     };
-    load(0);
+    if (nq > 0) load(0);  // nq is the warp's: a uniform branch
     between();
-    apply(0);
+    if (nq > 0) apply(0);
     for (int q = 4; q < nq; q += 4) {
         load(q);
         apply(q);
@@ -966,10 +966,39 @@ __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, cons
     return acc;
 }
 
+// The same without work in between (the one-CTA path): row quads in groups of four.
 __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, const int nq,
                                            const int lane)
 {
-    return thin_rows(n, tile, nq, lane, [] {});
+    float4 *P = reinterpret_cast<float4 *>(n.psr) + (size_t)tile * n.Mq * 32 + lane;
+    const uint16_t *C = reinterpret_cast<const uint16_t *>(n.dcls) + (size_t)tile * n.Mq * 32 + lane;
+    float acc = 0.0f;
+    for (int q = 0; q < nq; q += 4) {
+        float4 v[4];
+        uint32_t c[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (q + j < nq) {
+                v[j] = P[(size_t)(q + j) * 32];
+                c[j] = C[(size_t)(q + j) * 32];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (q + j < nq) {
+                v[j].x = v[j].x * __ldg(&n.dtab[c[j] & 15u]);
+                v[j].y = v[j].y * __ldg(&n.dtab[(c[j] >> 4) & 15u]);
+                v[j].z = v[j].z * __ldg(&n.dtab[(c[j] >> 8) & 15u]);
+                v[j].w = v[j].w * __ldg(&n.dtab[(c[j] >> 12) & 15u]);
+                gst(&P[(size_t)(q + j) * 32], v[j]);
+                acc = acc + v[j].x;
+                acc = acc + v[j].y;
+                acc = acc + v[j].z;
+                acc = acc + v[j].w;
+            }
+        }
+    }
+    return acc;
 }
 
 // Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
