@@ -54,3 +54,21 @@ def test_hot_kernels_do_not_spill():
     assert len(hot) == 9, sorted(rep)
     spilling = {k: v for k, v in hot.items() if v[1] or v[2]}
     assert not spilling, spilling
+
+
+def test_serve_desc_validation_without_a_gpu():
+    """bg3_serve_create checks its descriptor on the host (no device call): an admission order
+    other than arrival (0) or least work (1), a negative bypass bound and a zero chunk are refused;
+    a valid descriptor makes a server that an empty destroy frees."""
+    from braingrid_gb300 import serve
+    lib = serve._bind()
+    ok = dict(hbm_budget_bytes=1 << 30, max_resident=4, chunk_steps=100, max_resident_slots=0,
+              max_bypass=8, order=serve.ORDER_LEAST_WORK)
+    h = ctypes.c_void_p()
+    assert lib.bg3_serve_create(ctypes.byref(serve.ServeDesc(**ok)), ctypes.byref(h)) == 0
+    assert lib.bg3_serve_destroy(h) == 0
+    for bad in (dict(order=2), dict(order=-1), dict(max_bypass=-1), dict(chunk_steps=0),
+                dict(max_resident=0)):
+        d = serve.ServeDesc(**dict(ok, **bad))
+        h = ctypes.c_void_p()
+        assert lib.bg3_serve_create(ctypes.byref(d), ctypes.byref(h)) != 0, bad
