@@ -58,6 +58,11 @@ METRIC = "synapse-updates/s"
 # written: 28 B) is reported beside it.
 SWEEP_BYTES_PER_SYN = 8.5
 SWEEP_BYTES_PER_NEURON = 48 + 30
+# the batched workloads' neuron passes: LIF without input (the growth sweep) 48 B; Izhikevich
+# (reads Vm, Vthresh, refr, Trefract, I0, Inoise, C2, a, b, c, d, u, C3 and writes Vm, u: 60 B)
+# with its Poisson input synapse (30 B) and the tile's row counts (4 B): 94 B
+SWEEP36_BYTES_PER_NEURON = 48
+IZH_BYTES_PER_NEURON = 60 + 30 + 4
 REF_LAYOUT_BYTES_PER_SYN = 28
 # served form: resident work cap, about one and a half of the largest jobs' synapse slots
 SERVE_SLOTS = 60e6
@@ -335,6 +340,11 @@ def run_bg3(args):
         dist.destroy_process_group()
 
 
+def _alg_gbs(S, N, bytes_per_neuron, seconds_per_step):
+    """Algorithmic GB/s of a batched step: 8.5 B per synapse and the neuron pass's bytes."""
+    return (SWEEP_BYTES_PER_SYN * S + bytes_per_neuron * N) / seconds_per_step / 1e9
+
+
 def _batch_graph_seconds(batch, steps):
     """Host wall clock around batch.step(steps): the path a caller runs (CUDA graphs of 32 fused
     steps, each step's sweep overlapping the kernels before it), synchronised on both sides,
@@ -396,7 +406,11 @@ def run_batched(steps, warmup):
            "batched_synapse_updates_per_s": S * steps / t_batch,
            "batched_neuron_steps_per_s": N * steps / t_batch,
            "batched_ms_per_step": t_batch * 1e3 / steps,
-           "batched_sweep_gbs": 9.0 * S / (t_batch / steps) / 1e9,
+           "batched_sweep_gbs": _alg_gbs(S, N, SWEEP36_BYTES_PER_NEURON, t_batch / steps),
+           "batched_frac_of_peak": _alg_gbs(S, N, SWEEP36_BYTES_PER_NEURON, t_batch / steps) /
+                                   peaks()[0],
+           "algorithmic_bytes_per_step": SWEEP_BYTES_PER_SYN * S + SWEEP36_BYTES_PER_NEURON * N,
+           "bytes_per_synapse": SWEEP_BYTES_PER_SYN, "bytes_per_neuron": SWEEP36_BYTES_PER_NEURON,
            "plain_synapse_updates_per_s": S * steps / t_plain,
            "plain_neuron_steps_per_s": N * steps / t_plain,
            "plain_ms_per_step": t_plain * 1e3 / steps,
@@ -685,6 +699,11 @@ def run_izh512(steps, warmup):
            "plain_ms_per_step": t_plain * 1e3 / steps,
            "plain_timing": "host wall clock around %d sequential bg3_step runs" % len(nets),
            "batched_over_plain": t_plain / t_batch,
+           "batched_gbs": _alg_gbs(S, N, IZH_BYTES_PER_NEURON, t_batch / steps),
+           "batched_frac_of_peak": _alg_gbs(S, N, IZH_BYTES_PER_NEURON, t_batch / steps) /
+                                   peaks()[0],
+           "algorithmic_bytes_per_step": SWEEP_BYTES_PER_SYN * S + IZH_BYTES_PER_NEURON * N,
+           "bytes_per_synapse": SWEEP_BYTES_PER_SYN, "bytes_per_neuron": IZH_BYTES_PER_NEURON,
            "batched_timing": "CUDA events around each step (the step's kernels launched one by "
                              "one, the next step's sweep not overlapping them)",
            "batched_graph_ms_per_step": t_graph * 1e3 / steps,
