@@ -416,7 +416,8 @@ __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_
 // positions, the DS update of u, r and the last-spike step, and the psr increment are done first;
 // pdl_wait() then waits for the sweep, and only the psr read-modify-write comes after it.  The
 // step comes from the pass's own counter (dstep), since the sweep advances `step` at its end.
-// STDP kinds wait first: their pre-spike walks read the post neurons' latest spikes.
+// STDP kinds prepare the same way and wait before their pre-spike walks, which read the post
+// neurons' latest spikes.
 constexpr int DLV_CHUNK = 128;
 constexpr int DLV_GROUP = 32;
 
@@ -497,11 +498,6 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb, bo
     __shared__ int32_t s_src[DLV_GROUP];
     __shared__ int s_moff[BG3_MAX_DELAYS + 1];
     bool waited = false;
-    if (SYN >= 2) {
-        pdl_wait();
-        pdl_trigger();
-        waited = true;
-    }
     const unsigned long long t = *n.dstep;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     if (threadIdx.x == 0) {
@@ -564,6 +560,11 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb, bo
             const uint32_t first = lo ? s_pref[lo - 1] : 0u;
             const uint32_t base = (ch - first) * DLV_CHUNK;
             if (SYN >= 2) {  // STDP: the pre-spike walks go one synapse at a time
+                if (!waited) {
+                    pdl_wait();  // the walks read the post neurons' spikes of the sweep before
+                    pdl_trigger();
+                    waited = true;
+                }
                 const uint32_t end = min(s_cnt[lo], base + (uint32_t)DLV_CHUNK);
                 for (uint32_t j = base + lane; j < end; j += 32)
                     deliver_hit<SYN>(n, n.outMap[s_beg[lo] + j], s_tf[lo], t, s_src[lo]);
