@@ -1003,9 +1003,10 @@ __device__ __forceinline__ float thin_rows(const NetDev &n, const int tile, cons
 }
 
 // Thin networks (at most THIN_QUADS row quads per dest): one warp per 32-dest tile.  A row quad
-// of a tile is 512 contiguous bytes of the plane (and 128 of the class plane), so the warp reads
+// of a tile is 512 contiguous bytes of the plane (and 64 of the class plane), so the warp reads
 // it with one coalesced 16-byte load per lane, scales it, writes it back and adds it in row
-// order; the same epilogue as sweep_tile.  Lanes past N sit in the last tile's padding, whose
+// order; the same epilogue as sweep_tile.  The noise draw runs while the neuron state and the
+// first row quads are in flight.  Lanes past N sit in the last tile's padding, whose
 // slots stay +0.0f.  For these networks a TMA pipeline per 32 dests would spend most of its time
 // in set-up.
 // Before it: the kernel's pdl_wait (spike delivery for this step has finished writing psr), the
