@@ -381,8 +381,6 @@ def run_batched(steps, warmup):
         n.step(max(warmup, GRAPH_WARMUP))  # builds each network's step graph before timing
     for n in nets:
         n.sync()
-    import torch
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = _t.perf_counter()
     for n in nets:
         n.step(steps)
