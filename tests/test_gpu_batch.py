@@ -186,3 +186,23 @@ def test_thin_izhikevich_batch_matches_plain_bit_exact():
     b.close()
     for n in plain + batched:
         n.close()
+
+
+@pytest.mark.parametrize("warps", [1, 32])
+def test_thin_tile_table_padding_at_any_block_size(warps):
+    """The thin tile table pads each network's tiles to whole blocks of the configured warps: one
+    warp a block (no padding) and 32 (a network of up to 32 tiles in one block, the rest idle
+    entries) give the plain networks' results bit for bit."""
+    plain = make_mixed_stdp()
+    batched = make_mixed_stdp()
+    b = bg.Batch(batched)
+    b.set_launch(thin_warps=warps)
+    for chunk in (1, 300):
+        for n in plain:
+            n.step(chunk)
+        b.step(chunk)
+        b.sync()
+        _compare(plain, batched, ("W", "psr", "u", "r", "lastSpike"))
+    errs = [n.error_word for n in plain + batched]
+    assert all(e == 0 for e in errs), errs
+    b.close()
