@@ -51,8 +51,10 @@ def build(verbose=False, extra=()):
         if _stale(obj, [src] + headers):
             # -Xptxas -v: ptxas's per-kernel registers and spills, kept beside the object
             # (ptxas_report) for the no-spill check of the hot kernels
-            jobs.append(([nvcc()] + ARCH + FLAGS + list(extra) + ["-Xptxas", "-v", "-c", src, "-o", obj],
-                         obj + ".ptxas.txt"))
+            # the host noise generator's loops are vectorised at -O3 (host code only)
+            host = ["-Xcompiler", "-O3"] if s == "bg3_hostrng.cu" else []
+            jobs.append(([nvcc()] + ARCH + FLAGS + host + list(extra) +
+                         ["-Xptxas", "-v", "-c", src, "-o", obj], obj + ".ptxas.txt"))
 
     def run(cmd):
         if verbose:

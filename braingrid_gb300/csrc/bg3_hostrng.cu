@@ -39,6 +39,15 @@ struct Mt {
         s[623] = mix(s[396], s[623], s[0]);
         next = 0;
     }
+    // The same recurrence from a block of 624 words (prev) into the next block (out, another
+    // array): each loop reads only words that are already final, so the compiler vectorises it.
+    static void next_block(const uint32_t *__restrict prev, uint32_t *__restrict out)
+    {
+        for (int i = 0; i < 227; i++) out[i] = mix(prev[i + 397], prev[i], prev[i + 1]);
+        for (int i = 227; i < 454; i++) out[i] = mix(out[i - 227], prev[i], prev[i + 1]);
+        for (int i = 454; i < 623; i++) out[i] = mix(out[i - 227], prev[i], prev[i + 1]);
+        out[623] = mix(out[396], prev[623], out[0]);
+    }
     // MTRand::rand as BrainGrid declares it (BGFLOAT): the tempered word over 2^32 - 1 in
     // double, rounded to float
     static float uniform_of(uint32_t y)
@@ -71,6 +80,13 @@ static inline bool polar_pair(float u1, float u2, float &x1, float &x2)
     x2 = v2 * y;
     return true;
 }
+// Whether that attempt is accepted (the same arithmetic, without the logarithm).
+static inline bool polar_accepts(float u1, float u2)
+{
+    const float v1 = 2 * u1 - 1;
+    const float v2 = 2 * u2 - 1;
+    return !(v1 * v1 + v2 * v2 > 1);
+}
 
 struct bg3_norm {
     Mt mt;
@@ -79,9 +95,6 @@ struct bg3_norm {
     float x2 = 0.0f;
     std::vector<uint32_t> wbuf;  // generator words taken out and not yet consumed
     size_t wpos = 0;
-    // per-thread pairs of a parallel fill, kept between calls so that their memory is reused
-    std::vector<std::vector<float>> part;
-    std::vector<std::vector<int64_t>> last;
     bg3_norm(uint32_t seed, float m, float s) : mt(seed), mu(m), sigma(s) {}
 
     float uniform()
@@ -102,25 +115,35 @@ struct bg3_norm {
         return mu + sigma * x1;
     }
 
-    // Appends at least k more words of the generator to wbuf.
+    // Appends at least k more words of the generator to wbuf: the current block's words not yet
+    // taken, then whole blocks generated in place (no copy of the state), the last one kept as
+    // the generator's state.
     void buffer_words(size_t k)
     {
         wbuf.erase(wbuf.begin(), wbuf.begin() + (ptrdiff_t)wpos);
         wpos = 0;
-        const size_t want = wbuf.size() + k;
-        wbuf.reserve(want + 624);
-        while (wbuf.size() < want) {
-            if (mt.next == 624) mt.twist();
+        if (mt.next < 624) {
+            const size_t r = (size_t)(624 - mt.next);
             wbuf.insert(wbuf.end(), mt.s + mt.next, mt.s + 624);
             mt.next = 624;
+            k = k > r ? k - r : 0;
         }
+        const size_t nb = (k + 623) / 624;
+        if (!nb) return;
+        const size_t old = wbuf.size();
+        wbuf.resize(old + nb * 624);
+        uint32_t *dst = wbuf.data() + old;
+        Mt::next_block(mt.s, dst);
+        for (size_t b = 1; b < nb; b++) Mt::next_block(dst + (b - 1) * 624, dst + b * 624);
+        std::copy(dst + (nb - 1) * 624, dst + nb * 624, mt.s);
     }
 
     // The next 2P values of the stream as P whole pairs (odd must be true: no value pending).
-    // Only the generator's recurrence runs in order on this thread; tempering, the polar
+    // Only the generator's recurrence runs in order on this thread.  Tempering, the polar
     // attempts and the logarithms are independent per pair of words, so threads take ranges of
-    // word pairs, keep their accepted pairs, and the pairs are then placed at the offsets the
-    // per-thread counts give: the same values in the same order as 2P sequential draws.
+    // word pairs: a first pass counts each range's accepted attempts, which gives every range the
+    // place of its pairs in the output, and a second writes them there: the same values in the
+    // same order as 2P sequential draws.
     void fill_pairs(float *out, int64_t P)
     {
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -135,38 +158,47 @@ struct bg3_norm {
             const uint32_t *w = wbuf.data() + wpos;
             const int64_t A = (int64_t)((wbuf.size() - wpos) / 2);
             const int T = (int)std::max<int64_t>(1, std::min<int64_t>(hw, A / 16384));
-            if ((int)part.size() < T) {
-                part.resize(T);
-                last.resize(T);  // attempt index of each kept pair
-            }
-            auto run = [&](int k) {
-                const int64_t lo = A * k / T, hi = A * (k + 1) / T;
-                std::vector<float> &p = part[k];
-                std::vector<int64_t> &l = last[k];
-                p.clear();
-                l.clear();
-                p.reserve((size_t)(hi - lo) * 2);
-                l.reserve((size_t)(hi - lo));
-                float a, b;
-                for (int64_t j = lo; j < hi; j++) {
-                    if (!polar_pair(Mt::uniform_of(w[2 * j]), Mt::uniform_of(w[2 * j + 1]), a, b)) continue;
-                    p.push_back(mu + sigma * a);
-                    p.push_back(mu + sigma * b);
-                    l.push_back(j);
-                }
+            std::vector<int64_t> cnt(T, 0), off(T, 0), take(T, 0), last(T, -1);
+            auto parallel = [&](auto &&fn) {
+                std::vector<std::thread> th;
+                for (int k = 1; k < T; k++) th.emplace_back(fn, k);
+                fn(0);
+                for (auto &x : th) x.join();
             };
-            std::vector<std::thread> th;
-            for (int k = 1; k < T; k++) th.emplace_back(run, k);
-            run(0);
-            for (auto &x : th) x.join();
-            // place the pairs in order, up to the need
-            int64_t got = 0, used = A;
-            for (int k = 0; k < T && got < need; k++) {
-                const int64_t m = std::min<int64_t>((int64_t)last[k].size(), need - got);
-                std::copy(part[k].begin(), part[k].begin() + 2 * m, out + 2 * (done + got));
-                got += m;
-                if (got == need) used = last[k][m - 1] + 1;  // attempts after it stay unread
+            parallel([&](int k) {
+                const int64_t lo = A * k / T, hi = A * (k + 1) / T;
+                int64_t c = 0;
+                for (int64_t j = lo; j < hi; j++)
+                    c += polar_accepts(Mt::uniform_of(w[2 * j]), Mt::uniform_of(w[2 * j + 1])) ? 1 : 0;
+                cnt[k] = c;
+            });
+            int64_t got = 0;
+            for (int k = 0; k < T; k++) {
+                off[k] = got;
+                take[k] = std::min<int64_t>(cnt[k], need - got);
+                got += take[k];
             }
+            parallel([&](int k) {
+                if (take[k] <= 0) return;
+                const int64_t lo = A * k / T, hi = A * (k + 1) / T;
+                float *o = out + 2 * (done + off[k]);
+                int64_t c = 0;
+                float a, b;
+                for (int64_t j = lo; j < hi && c < take[k]; j++) {
+                    if (!polar_pair(Mt::uniform_of(w[2 * j]), Mt::uniform_of(w[2 * j + 1]), a, b)) continue;
+                    o[2 * c] = mu + sigma * a;
+                    o[2 * c + 1] = mu + sigma * b;
+                    c++;
+                    last[k] = j;
+                }
+            });
+            int64_t used = A;
+            if (got == need)  // the attempts after the last pair taken stay unread
+                for (int k = T - 1; k >= 0; k--)
+                    if (take[k] > 0) {
+                        used = last[k] + 1;
+                        break;
+                    }
             wpos += 2 * (size_t)used;
             done += got;
         }
