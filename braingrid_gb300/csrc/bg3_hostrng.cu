@@ -2,7 +2,9 @@
 // exactly without its code: Norm (RNG/Norm.cpp:59-86), the Marsaglia polar method in float over
 // MTRand (RNG/MersenneTwister.cpp), seeded with the parameter file's seed
 // (Core/SingleThreadedSpikingModel.cpp:30).  Host code only; built with -ffp-contract=off like
-// the rest of the library so that every product and sum rounds as the reference's do.
+// the rest of the library so that every product and sum rounds as the reference's do (and with
+// the host compiler's -O3, which vectorises the generator's recurrence; the values are the
+// integer recurrence's and the same float operations either way).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>

@@ -222,7 +222,10 @@ int bg3_noise_pending(bg3_net *net, int64_t *pending);
  * (RNG/Norm.cpp:59-86, the Marsaglia polar method in float over MTRand,
  * RNG/MersenneTwister.cpp), the generator the reference's single-threaded model creates from
  * the parameter file's seed (Core/SingleThreadedSpikingModel.cpp:30).  bg3_norm_fill writes the
- * next n values; consecutive fills continue one stream.  Host only (no device, no stream). */
+ * next n values; consecutive fills continue one stream.  Fills of 131,072 values or more run the
+ * polar method's arithmetic on up to 16 host threads (the same values).  Host only (no device,
+ * no stream); one generator is not to be filled from two threads at once.  BG3_ENOMEM when a
+ * thread or memory cannot be had, after which the stream is lost. */
 typedef struct bg3_norm bg3_norm;
 int bg3_norm_create(uint32_t seed, float mu, float sigma, bg3_norm **out);
 int bg3_norm_fill(bg3_norm *gen, float *values, int64_t n);
