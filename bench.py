@@ -598,7 +598,7 @@ def run_growth():
 
 
 def run_small(steps=20000, warmup=2000):
-    """The 100-neuron network of the first configuration (10x10 LIF + DS + ConnGrowth, 10 %
+    """The 100-neuron network (10x10 LIF + DS + ConnGrowth, 10 %
     inhibitory, 10 starters, max 100 synapses per neuron; at its stated 0.4 start radius it has no
     synapses) stepped on the one-CTA path (many whole steps per launch) and on the multi-kernel
     path, with the library's device noise and with the reference's Norm stream pushed ahead
@@ -609,7 +609,7 @@ def run_small(steps=20000, warmup=2000):
     from braingrid_gb300 import netgen
     spec = netgen.lif_network(10, 10, frac_inh=0.10, seed=1)
     N = spec["N"]
-    out = {"workload": "10x10 LIF + DS + ConnGrowth (first configuration), %d steps" % steps}
+    out = {"workload": "10x10 LIF + DS + ConnGrowth, start radius 0.4, %d steps" % steps}
     for mode, name in ((bg.BG3_NOISE_DEVICE, "device_noise"), (bg.BG3_NOISE_INJECT, "injected_noise")):
         for small, tag in ((65536, "one_cta"), (0, "multi_kernel")):
             net = netgen.make_gpu_network(spec, 100, noise_mode=mode, noise_seed=1)

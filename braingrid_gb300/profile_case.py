@@ -9,7 +9,7 @@ growth pass (which restores the unscaled growth weights: the networks then fire 
 batched together.  heavy is one of those jobs (180x180) alone: 10,000 steps, a growth pass, 1,000
 steps (it then fires at ~300 Hz), then --steps steps timed kernel by kernel; its delivery passes
 after launch 11,000 are heavy ones.  growth200 is the growth pass of the served stream's largest
-job (200x200, pre-grown); small the first configuration's 10x10 network on the one-CTA path
+job (200x200, pre-grown); small the 10x10 LIF + DS + ConnGrowth network (100 neurons) on the one-CTA path
 (k_small_run, 4,096 steps per launch).
 """
 import argparse
@@ -43,7 +43,7 @@ def main():
         print("synapses", net.total_synapses(), "error_word", net.error_word)
         return
     if a.workload == "small":
-        # the first configuration's 10x10 network (no synapse at its 0.4 start radius) on the
+        # the 10x10 LIF + DS + ConnGrowth network (no synapse at its 0.4 start radius) on the
         # one-CTA path: --steps whole steps, 4,096 per launch
         from . import netgen
         spec = netgen.lif_network(10, 10, frac_inh=0.10, seed=1)
