@@ -31,11 +31,12 @@ them):
       place of AllSTDPSynapses::createSynapse's built-in ones (Synapses/AllSTDPSynapses.cpp:
       252-273); Wex is WexInh for synapses from inhibitory neurons, WexExc otherwise;
   <ParameterDraw>r_squared</ParameterDraw> (AllIZHNeurons): Izhikevich's (2003) spread instead
-      of four flat ranges.  One draw r = inRange(0, 1) per neuron after its IF draws; excitatory
-      a = 0.02, b = 0.2, c = -65 + 15 r r, d = 8 - 6 r r; inhibitory a = 0.02 + 0.08 r,
-      b = 0.25 - 0.05 r, c = -65, d = 2 (float arithmetic, left to right).  The drop-in driver
-      refuses it: the draw happens inside the reference's own setup, which that driver runs
-      unchanged.
+      of four flat ranges.  The neuron's four range draws are made as before (so the generator's
+      stream, and everything drawn after the neurons, is that of the flat-range file) and the
+      first of them, as r = inRange(0, 1), gives all four: excitatory a = 0.02, b = 0.2,
+      c = -65 + 15 r r, d = 8 - 6 r r; inhibitory a = 0.02 + 0.08 r, b = 0.25 - 0.05 r, c = -65,
+      d = 2 (float arithmetic, left to right).  The drop-in driver replays the same draws from
+      the generator's state before the neurons drew.
 
 One difference from the reference: ConnStatic keeps each source's nConnsPerNeuron nearest
 neurons with equal distances in neuron-index order.  The reference sorts with std::sort, which
@@ -655,11 +656,12 @@ def poisson_intervals(a, nsteps):
 def _create_neurons(p, rng, out):
     """AllIFNeurons::createAllNeurons / createNeuron / initNeuronConstsFromParamValues and the
     Izhikevich additions.  Per neuron: Iinject, Inoise, Vthresh, Vrest, Vreset, Vinit; two more
-    (Vthresh, Vreset) for a starter; then a, b, c, d (or r) for an Izhikevich neuron."""
+    (Vthresh, Vreset) for a starter; then a, b, c, d for an Izhikevich neuron (with the r^2
+    draw the first of these is r and the other three are unused)."""
     N = out["N"]
     ntype, starter = out["ntype"], out["starter"]
     izh = p.neuron_class == "AllIZHNeurons"
-    extra = (1 if p.izh_draw == "r_squared" else 4) if izh else 0
+    extra = 4 if izh else 0
     per = 6 + 2 * starter.astype(np.int64) + extra
     first = np.concatenate([[0], np.cumsum(per)[:-1]])
     u = rng.rand(int(per.sum()))

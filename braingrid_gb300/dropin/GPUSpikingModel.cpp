@@ -12,7 +12,8 @@
 //                      whole network, filled from the host objects through the classes' own
 //                      copy*HostToDevice members (bg3_classes.cpp); an STDP class's constants
 //                      come from the parameter file's <BG3Params><STDPParams> where it has one
-//                      (read_bg3_params);
+//                      (read_bg3_params), and <BG3Params><ParameterDraw>r_squared</ParameterDraw>
+//                      gives Izhikevich neurons Izhikevich's r^2 spread (redraw_izh_r_squared);
 //   advance            queues the step; queued steps run as one bg3_step call (CUDA-graph replays
 //                      inside the library) when BG3_STEPS_PER_CALL steps have queued, or when the
 //                      state is next observed (epoch end, checkpoint, cleanup);
@@ -113,9 +114,8 @@ AllSpikingSynapses *scratch_synapses(int32_t kind)
 // names below: the constants of every synapse of an STDP class, in place of the ones
 // AllSTDPSynapses::createSynapse writes (Synapses/AllSTDPSynapses.cpp:252-273); Wex is WexInh for
 // synapses from inhibitory neurons (II, IE) and WexExc otherwise, as braingrid_gb300.config
-// reads the same element.  <ParameterDraw> (the Izhikevich r^2 draw) is drawn inside the
-// reference's own AllIZHNeurons::createNeuron, which this driver runs unchanged, so a file
-// that asks for it is refused here.
+// reads the same element.  <BG3Params><ParameterDraw> is "ranges" (the reference's flat ranges)
+// or "r_squared" (redraw_izh_r_squared below).
 const char *const STDP_NAMES[] = {"Apos", "Aneg", "STDPgap", "tauspost", "tauspre", "taupos",
                                   "tauneg", "WexExc", "WexInh", "mupos", "muneg",
                                   "useFroemkeDanSTDP"};
@@ -126,15 +126,23 @@ void refuse(const std::string &file, const std::string &what)
     exit(EXIT_FAILURE);
 }
 
-StdpParams read_bg3_params(const std::string &file)
+StdpParams read_bg3_params(const std::string &file, bool &r_squared)
 {
     StdpParams out;
+    r_squared = false;
     TiXmlDocument doc(file.c_str());
     if (!doc.LoadFile()) return out;  // the reference's reader has already reported it
     TiXmlElement *root = doc.FirstChildElement();
     TiXmlElement *bp = root ? root->FirstChildElement("BG3Params") : NULL;
     if (!bp) return out;
     for (TiXmlElement *e = bp->FirstChildElement(); e; e = e->NextSiblingElement()) {
+        if (e->ValueStr() == "ParameterDraw") {
+            const std::string how = e->GetText() ? e->GetText() : "";
+            if (how != "ranges" && how != "r_squared")
+                refuse(file, "<ParameterDraw> must be ranges or r_squared");
+            r_squared = how == "r_squared";
+            continue;
+        }
         if (e->ValueStr() != "STDPParams")
             refuse(file, "<" + e->ValueStr() + "> is not applied by this driver");
         for (TiXmlElement *f = e->FirstChildElement(); f; f = f->NextSiblingElement()) {
@@ -179,6 +187,53 @@ void apply_stdp_to_host(IAllSynapses *syn, const StdpParams &p)
         s->muneg[i] = stdp_value(p, "muneg", s->muneg[i]);
         s->useFroemkeDanSTDP[i] = stdp_value(p, "useFroemkeDanSTDP", s->useFroemkeDanSTDP[i] ? 1.0f : 0.0f) != 0.0f;
     }
+}
+
+// <ParameterDraw>r_squared</ParameterDraw>: Izhikevich's (2003) heterogeneous parameters.  The
+// reference's AllIZHNeurons::createNeuron (Neurons/AllIZHNeurons.cpp:412-432) draws a, b, c, d
+// from flat ranges, four inRange draws after the six of AllIFNeurons::createNeuron and, for a
+// starter neuron, its two more (Neurons/AllIFNeurons.cpp:401-439).  This draw keeps those draws
+// (so the generator's stream, and everything drawn after the neurons, is unchanged) and takes
+// the first of the four as r = inRange(0, 1): excitatory a = 0.02, b = 0.2, c = -65 + 15 r r,
+// d = 8 - 6 r r; inhibitory a = 0.02 + 0.08 r, b = 0.25 - 0.05 r, c = -65, d = 2, in float, left
+// to right.  r is replayed here from a copy of the generator taken before the neurons drew, in
+// their order, and the host neurons take the four values before they are uploaded.  Returns the
+// FNV-1a hash of the four arrays' bytes (a, then b, c, d), which the log line reports.
+//
+// A copy of the generator that draws on its own: MTRand's implicit copy keeps the original's
+// read pointer into the original's state, so the copy points it into its own state, where
+// MTRand keeps it (pNext = state + N - left, RNG/MersenneTwister.cpp:93-99,278-290).  (MTRand's
+// save and load are declared inline and defined only inside the RNG's own file.)
+struct GeneratorCopy : MTRand {
+    explicit GeneratorCopy(const MTRand &from) : MTRand(from) { pNext = state + (N - left); }
+};
+
+uint64_t redraw_izh_r_squared(AllIZHNeurons *n, const Layout *layout, const MTRand &saved, int count)
+{
+    GeneratorCopy g(saved);
+    for (int i = 0; i < count; i++) {
+        for (int k = 0; k < (layout->starter_map[i] ? 8 : 6); k++) g();
+        const BGFLOAT r = g.inRange(0, 1);
+        for (int k = 0; k < 3; k++) g();
+        if (layout->neuron_type_map[i] == EXC) {
+            n->Aconst[i] = 0.02f;
+            n->Bconst[i] = 0.2f;
+            n->Cconst[i] = -65.0f + 15.0f * r * r;
+            n->Dconst[i] = 8.0f - 6.0f * r * r;
+        } else {
+            n->Aconst[i] = 0.02f + 0.08f * r;
+            n->Bconst[i] = 0.25f - 0.05f * r;
+            n->Cconst[i] = -65.0f;
+            n->Dconst[i] = 2.0f;
+        }
+    }
+    uint64_t h = 1469598103934665603ull;
+    const BGFLOAT *arrays[4] = {n->Aconst, n->Bconst, n->Cconst, n->Dconst};
+    for (int a = 0; a < 4; a++) {
+        const unsigned char *b = reinterpret_cast<const unsigned char *>(arrays[a]);
+        for (size_t k = 0; k < (size_t)count * sizeof(BGFLOAT); k++) h = (h ^ b[k]) * 1099511628211ull;
+    }
+    return h;
 }
 
 // The per-type constants of synapses the device growth pass creates, taken from the reference's
@@ -355,16 +410,39 @@ void GPUSpikingModel::deleteDeviceStruct(void **allNeuronsDevice, void **allSyna
 void GPUSpikingModel::setupSim(SimulationInfo *sim_info)
 {
     ModelState &st = state_of(this);
-    st.stdp = read_bg3_params(sim_info->stateInputFileName);
+    const std::string &file = sim_info->stateInputFileName;
+    bool r_squared = false;
+    st.stdp = read_bg3_params(file, r_squared);
     if (!st.stdp.empty()) {
         if (!dynamic_cast<AllSTDPSynapses *>(m_synapses))
-            refuse(sim_info->stateInputFileName, "STDPParams given for a synapse class without STDP");
-        fprintf(stderr, "BG3Params: %d STDP constants from %s\n", (int)st.stdp.size(),
-                sim_info->stateInputFileName.c_str());
+            refuse(file, "STDPParams given for a synapse class without STDP");
+        fprintf(stderr, "BG3Params: %d STDP constants from %s\n", (int)st.stdp.size(), file.c_str());
     }
-    bg3_dropin_check(bg3_set_device(g_deviceId), "bg3_set_device");
-    Model::setupSim(sim_info);
+    AllIZHNeurons *izh = dynamic_cast<AllIZHNeurons *>(m_neurons);
+    if (r_squared && !izh) refuse(file, "ParameterDraw given for a neuron class other than AllIZHNeurons");
+    // The host setup comes first and the device is selected after it (the reference selects it
+    // first; nothing in the host setup touches the device).
+    if (r_squared) {
+        // Model::setupSim's steps (Core/Model.cpp:136-158, with Model::createAllNeurons,
+        // Core/Model.cpp:117-129), with the generator's state saved before the neurons draw
+        m_neurons->setupNeurons(sim_info);
+        m_synapses->setupSynapses(sim_info);
+        m_layout->setupLayout(sim_info);
+        if (sim_info->simRecorder != NULL) sim_info->simRecorder->initDefaultValues();
+        m_layout->generateNeuronTypeMap(sim_info->totalNeurons);
+        m_layout->initStarterMap(sim_info->totalNeurons);
+        const GeneratorCopy saved(rng);
+        m_neurons->createAllNeurons(sim_info, m_layout);
+        m_conns->setupConnections(sim_info, m_layout, m_neurons, m_synapses);
+        m_synapses->createSynapseImap(m_synapseIndexMap, sim_info);
+        const uint64_t h = redraw_izh_r_squared(izh, m_layout, saved, sim_info->totalNeurons);
+        fprintf(stderr, "BG3Params: Izhikevich r^2 draw for %d neurons (a, b, c, d FNV-1a %016llx)\n",
+                sim_info->totalNeurons, (unsigned long long)h);
+    } else {
+        Model::setupSim(sim_info);
+    }
     apply_stdp_to_host(m_synapses, st.stdp);
+    bg3_dropin_check(bg3_set_device(g_deviceId), "bg3_set_device");
     const char *noise = getenv("BG3_NOISE");
     st.reference_noise = !(noise && std::string(noise) == "device");
     st.chunk = env_int("BG3_STEPS_PER_CALL", 1000);

@@ -27,7 +27,7 @@ CXX ?= g++
 
 # the reference's headers are C++98 (in-class float constants), so this directory's files are too
 REFFLAGS = -O2 -std=c++98 -w -DTIXML_USE_STL -DDEBUG_OUT -DUSE_GPU
-OURFLAGS = -O2 -std=c++98 -Wall -Wno-unused-parameter -DTIXML_USE_STL -DDEBUG_OUT -DUSE_GPU
+OURFLAGS = -O2 -std=c++98 -ffp-contract=off -Wall -Wno-unused-parameter -DTIXML_USE_STL -DDEBUG_OUT -DUSE_GPU
 
 DIRS = Connections Core Inputs Layouts Matrix Neurons paramcontainer Recorders RNG Synapses Utils tinyxml
 INC = $(addprefix -I$(REF)/,$(DIRS))

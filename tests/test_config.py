@@ -194,10 +194,11 @@ def test_izh_r_squared_draws(tmp_path):
     p = cf.read(text, root=str(tmp_path))
     assert p.izh_draw == "r_squared"
     a = cf.setup(p)
-    # the IF draws are those of the flat-range file (one r per neuron follows them)
+    # the draw keeps the flat ranges' four draws per neuron, so every other value the setup draws
+    # is that of the flat-range file, for every neuron
     fx = load_fixture("izh_grown")
-    for k in ("Iinject", "Inoise", "Vrest", "Vinit"):
-        assert_same(k, a[k][:1], fx[k][:1])
+    for k in ("Iinject", "Inoise", "Vthresh", "Vrest", "Vreset", "Vinit"):
+        assert_same(k, a[k], fx[k])
     inh = a["ntype"] == 1
     f32 = np.float32
     r_inh = (a["Aconst"][inh] - f32(0.02)) / f32(0.08)

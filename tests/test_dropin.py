@@ -89,8 +89,8 @@ def _run_driver(tmp_path, text, name):
 def test_bg3params_stdp_constants_reach_the_drop_in(driver, tmp_path):
     """A parameter file carrying STDP constants in a root-level <BG3Params> (the Izhikevich +
     dynamic STDP + ConnStatic case): the reference's readers take the file, the drop-in reads the
-    eleven constants before its first C-ABI call; <ParameterDraw> there, and STDP constants for a
-    class without STDP, are refused with a message."""
+    eleven constants before its first C-ABI call; STDP constants for a class without STDP, and a
+    <ParameterDraw> other than ranges or r_squared, are refused with a message."""
     from tests.golden import configs
     from tests.golden.configs import case
     c = case("izh_static")
@@ -100,8 +100,46 @@ def test_bg3params_stdp_constants_reach_the_drop_in(driver, tmp_path):
     assert "BG3Params: 11 STDP constants from configfiles/bg3/izh_static_bg3.xml" in out, out
     assert "Unrecognized" not in out
     rc, out = _run_driver(tmp_path, text.replace("<BG3Params>", "<BG3Params><ParameterDraw>"
-                                                 "r_squared</ParameterDraw>"), "izh_draw")
-    assert rc != 0 and "<ParameterDraw> is not applied by this driver" in out, out
+                                                 "squared</ParameterDraw>"), "izh_draw")
+    assert rc != 0 and "<ParameterDraw> must be ranges or r_squared" in out, out
     rc, out = _run_driver(tmp_path, text.replace("AllDynamicSTDPSynapses", "AllDSSynapses"),
                           "izh_ds")
     assert rc != 0 and "STDPParams given for a synapse class without STDP" in out, out
+
+
+def _fnv1a64(data):
+    h = 1469598103934665603
+    for b in data:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def test_r_squared_draw_in_the_drop_in_equals_the_config_reader(driver, tmp_path):
+    """<BG3Params><ParameterDraw>r_squared</ParameterDraw> on the Izhikevich + dynamic STDP +
+    ConnStatic case: the drop-in replays the draw from the reference's generator after the
+    reference's own host setup; its a, b, c, d are those braingrid_gb300.config draws from the
+    same file, byte for byte (the FNV-1a hash the driver logs, before its first C-ABI call).  A
+    Lif network asking for the draw is refused."""
+    from braingrid_gb300 import config as cf
+    from tests.golden import configs
+    from tests.golden.configs import case
+    c = case("izh_static")
+    configs.write_case(c, str(tmp_path / "configfiles"))
+    text = configs.config_text(c, stdp_params="root").replace(
+        "<BG3Params>", "<BG3Params><ParameterDraw>r_squared</ParameterDraw>")
+    rc, out = _run_driver(tmp_path, text, "izh_r2")
+    line = [l for l in out.splitlines() if "Izhikevich r^2 draw" in l]
+    assert line, out
+    p = cf.read(text, root=str(tmp_path))
+    assert p.izh_draw == "r_squared"
+    a = cf.setup(p)
+    want = _fnv1a64(b"".join(a[k].astype("<f4").tobytes()
+                             for k in ("Aconst", "Bconst", "Cconst", "Dconst")))
+    assert "for %d neurons" % len(a["Aconst"]) in line[0], line[0]
+    assert "FNV-1a %016x" % want in line[0], (line[0], "%016x" % want)
+    configs.write_case(case("c0_stdp"), str(tmp_path / "configfiles"))
+    lif = configs.config_text(case("c0_stdp")).replace(
+        "</BGSimParams>", "<BG3Params><ParameterDraw>r_squared</ParameterDraw></BG3Params>"
+        "</BGSimParams>")
+    rc, out = _run_driver(tmp_path, lif, "lif_r2")
+    assert rc != 0 and "ParameterDraw given for a neuron class other than AllIZHNeurons" in out, out
