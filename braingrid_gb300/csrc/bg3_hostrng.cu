@@ -161,9 +161,17 @@ struct bg3_norm {
             const int64_t A = (int64_t)((wbuf.size() - wpos) / 2);
             const int T = (int)std::max<int64_t>(1, std::min<int64_t>(hw, A / 16384));
             std::vector<int64_t> cnt(T, 0), off(T, 0), take(T, 0), last(T, -1);
+            // ranges 1.. on threads of their own, range 0 here; ranges whose thread could not be
+            // started run here too, so every started thread is joined
             auto parallel = [&](auto &&fn) {
                 std::vector<std::thread> th;
-                for (int k = 1; k < T; k++) th.emplace_back(fn, k);
+                th.reserve((size_t)T);
+                int k = 1;
+                try {
+                    for (; k < T; k++) th.emplace_back(fn, k);
+                } catch (...) {
+                }
+                for (int j = k; j < T; j++) fn(j);
                 fn(0);
                 for (auto &x : th) x.join();
             };

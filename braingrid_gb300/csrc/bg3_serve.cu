@@ -122,10 +122,11 @@ static bool fits(const bg3_server *s, const Job *j)
 }
 
 // A queued job's work: synapse slots x the steps of its epochs still to run.
-static uint64_t work_left(const Job *j)
+static double work_left(const Job *j)
 {
     const int64_t spe = std::max<int64_t>(1, steps_per_epoch(j->d.desc));
-    return j->slots * (uint64_t)std::max(0, j->d.epochs) * (uint64_t)spe;
+    // in double: only compared, and no product of the three overflows there
+    return (double)j->slots * (double)std::max(0, j->d.epochs) * (double)spe;
 }
 
 // The queue index of the next job to admit, or -1: the oldest job once it has been passed
