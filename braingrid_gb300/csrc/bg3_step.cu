@@ -260,25 +260,61 @@ __device__ __forceinline__ unsigned long long hist_at(const NetDev &n, int i, in
 // W^mu with mu = 0, the only exponent a network accepts (set_stdp_type refuses others)
 __device__ __forceinline__ float pow_mu(float, float) { return 1.0f; }
 
-// stdpLearning with delta = dk steps (dk the signed interval; 0 when not a small count)
-__device__ __forceinline__ float stdp_learn(const StdpConst &c, float W, float delta, float epost,
-                                            float epre, long long dk)
+// One stdpLearning call with delta = dk steps (dk the signed interval; 0 when not a small count),
+// in two parts.  stdp_inc: the weight change, which W does not enter (W^mu = 1): false when delta
+// lies within the gap (W unchanged, no clamp), else epost * epre * dw in double.  stdp_apply: W
+// plus that change, rounded to float, then the clamps.  So the walks below can find a walk's
+// changes before W is known and apply them in order after.
+__device__ __forceinline__ bool stdp_inc(const StdpConst &c, float delta, float epost, float epre,
+                                         long long dk, double &inc)
 {
     const double d = (double)delta;
     float dw;
     if (d < (double)(-c.gap)) {
         const double e = (dk < 0 && -dk < (long long)c.dlen_neg) ? c.dneg[-dk] : exp(d / (double)c.tauneg);
-        dw = (float)((double)(pow_mu(W, c.muneg) * c.Aneg) * e);
+        dw = (float)((double)(pow_mu(0.0f, c.muneg) * c.Aneg) * e);
     } else if (d > (double)c.gap) {
         const double e = (dk > 0 && dk < (long long)c.dlen_pos) ? c.dpos[dk] : exp(-d / (double)c.taupos);
-        dw = (float)((double)(pow_mu(c.Wex - W, c.mupos) * c.Apos) * e);
+        dw = (float)((double)(pow_mu(0.0f, c.mupos) * c.Apos) * e);
     } else {
-        return W;
+        return false;
     }
-    W = (float)((double)W + (double)epost * (double)epre * (double)dw);
+    inc = (double)epost * (double)epre * (double)dw;
+    return true;
+}
+__device__ __forceinline__ float stdp_apply(const StdpConst &c, float W, double inc)
+{
+    W = (float)((double)W + inc);
     if ((c.Wex < 0.0f && W > 0.0f) || (c.Wex > 0.0f && W < 0.0f)) W = 0.0f;
     if (fabsf(W) > fabsf(c.Wex)) W = c.Wex;
     return W;
+}
+__device__ __forceinline__ float stdp_learn(const StdpConst &c, float W, float delta, float epost,
+                                            float epre, long long dk)
+{
+    double inc;
+    return stdp_inc(c, delta, epost, epre, dk, inc) ? stdp_apply(c, W, inc) : W;
+}
+
+// A neuron's history entries -1 .. -4 read together (those of them that exist: off >= -ms), so
+// that a walk's first steps do not wait on one load each; hist_get takes the rest from memory.
+struct Hist4 {
+    unsigned long long h0, h1, h2, h3;
+};
+__device__ __forceinline__ void hist_load4(const NetDev &n, int i, int co, Hist4 &c)
+{
+    const int ms = n.max_spikes;
+    c.h0 = hist_at(n, i, co, -1);  // max_spikes >= 1
+    c.h1 = ms >= 2 ? hist_at(n, i, co, -2) : BG3_ULONG_MAX;
+    c.h2 = ms >= 3 ? hist_at(n, i, co, -3) : BG3_ULONG_MAX;
+    c.h3 = ms >= 4 ? hist_at(n, i, co, -4) : BG3_ULONG_MAX;
+}
+// entry off (-ms <= off <= -1)
+__device__ __forceinline__ unsigned long long hist_get(const NetDev &n, int i, int co, int off,
+                                                       const Hist4 &c)
+{
+    return off == -1 ? c.h0 : off == -2 ? c.h1 : off == -3 ? c.h2 : off == -4 ? c.h3
+                                                                    : hist_at(n, i, co, off);
 }
 
 // The fPre branch: a spike from pre arrives at the synapse onto post at step t.  Returns W.
@@ -311,13 +347,15 @@ __device__ float stdp_pre(const NetDev &n, const StdpConst &c, float W, int pre,
         return W;
     }
     const int cpre = n.spikeCount[pre] + n.spikeCountOffset[pre];
-    float epre = 1.0f;
+    Hist4 hp;
+    hist_load4(n, post, cpost, hp);
     const unsigned long long sp2 = hist_at(n, pre, cpre, -2);
+    float epre = 1.0f;
     if ((long long)sp2 > 0 && c.useFD)
         epre = (float)(1.0 - (double)exp_interval(n, t - sp2, true, c.tauspre));
     for (int off = -1;; --off) {
         if (off < -ms) { set_err(n, ERR_STDP_RING); break; }
-        const unsigned long long sh = hist_at(n, post, cpost, off);
+        const unsigned long long sh = hist_get(n, post, cpost, off, hp);
         if (sh == BG3_ULONG_MAX) break;
         const long long dk = (long long)(sh - t);
         const float delta = (float)dk * n.dt;
@@ -325,7 +363,7 @@ __device__ float stdp_pre(const NetDev &n, const StdpConst &c, float W, int pre,
         float epost = 1.0f;
         if (c.useFD) {
             if (off - 1 < -ms) { set_err(n, ERR_STDP_RING); break; }
-            const unsigned long long sh2 = hist_at(n, post, cpost, off - 1);
+            const unsigned long long sh2 = hist_get(n, post, cpost, off - 1, hp);
             if (sh2 == BG3_ULONG_MAX) break;
             epost = (float)(1.0 - (double)exp_interval(n, sh - sh2, true, c.tauspost));
         }
@@ -334,21 +372,79 @@ __device__ float stdp_pre(const NetDev &n, const StdpConst &c, float W, int pre,
     return W;
 }
 
-// The fPost branch: post fired at step t; walk the pre history (both builds agree here).
-__device__ float stdp_post(const NetDev &n, const StdpConst &c, float W, int pre, int post,
-                           int total_delay, unsigned long long t)
+// The fPost branch: post fired at step t; walk the pre history (both builds agree here).  The
+// walk does not depend on W, so it runs in two parts: stdp_post_prep reads everything it needs
+// (spike counts, histories, tables) and makes its first four steps, keeping their weight changes;
+// stdp_post_finish applies them to W and makes any further steps.  The post-spike pass calls
+// the first before its wait on the delivery of the same step (the one writer of W there).
+constexpr int POST_STEPS = 4;
+struct PostPrep {
+    double inc0, inc1, inc2, inc3;  // the changes of steps 1 .. 4 (those with a bit in mask)
+    float epost;
+    int cpre;
+    int mask;                       // bit k: step k + 1 changed W
+    int next;                       // 0: the walk has ended; else the entry it continues from
+};
+__device__ __forceinline__ void stdp_post_prep(const NetDev &n, const StdpConst &c, int pre,
+                                               int post, int total_delay, unsigned long long t,
+                                               PostPrep &q)
 {
     const int ms = n.max_spikes;
     const bool sgn = n.stdp_signed != 0;
     const int cpost = n.spikeCount[post] + n.spikeCountOffset[post];
     const int cpre = n.spikeCount[pre] + n.spikeCountOffset[pre];
-    float epost = 1.0f;
     const unsigned long long q2 = hist_at(n, post, cpost, -2);
+    Hist4 hp;
+    hist_load4(n, pre, cpre, hp);
+    float epost = 1.0f;
     const bool ok = sgn ? ((long long)q2 > 0) : (q2 != BG3_ULONG_MAX);
     if (ok && c.useFD) epost = (float)(1.0 - (double)exp_interval(n, t - q2, sgn, c.tauspost));
-    for (int off = -1;; --off) {
+    q.epost = epost;
+    q.cpre = cpre;
+    q.mask = 0;
+    q.next = 0;
+    q.inc0 = q.inc1 = q.inc2 = q.inc3 = 0.0;
+#pragma unroll
+    for (int k = 0; k < POST_STEPS; k++) {
+        const int off = -1 - k;
+        if (off < -ms) { set_err(n, ERR_STDP_RING); return; }
+        const unsigned long long sh = hist_get(n, pre, cpre, off, hp);
+        if (sh == BG3_ULONG_MAX) return;
+        const unsigned long long dd = t - (unsigned long long)(long long)total_delay - sh;
+        const float delta = (sgn ? (float)(long long)dd : (float)dd) * n.dt;
+        if (delta <= 0.0f || (double)delta >= 3.0 * (double)c.taupos) return;
+        float epre = 1.0f;
+        if (c.useFD) {
+            if (off - 1 < -ms) { set_err(n, ERR_STDP_RING); return; }
+            const unsigned long long sh2 = hist_get(n, pre, cpre, off - 1, hp);
+            if (sh2 == BG3_ULONG_MAX) return;
+            epre = (float)(1.0 - (double)exp_interval(n, sh - sh2, sgn, c.tauspre));
+        }
+        double inc;
+        if (stdp_inc(c, delta, epost, epre, (long long)dd, inc)) {
+            q.mask |= 1 << k;
+            if (k == 0) q.inc0 = inc;
+            else if (k == 1) q.inc1 = inc;
+            else if (k == 2) q.inc2 = inc;
+            else q.inc3 = inc;
+        }
+    }
+    q.next = -1 - POST_STEPS;
+}
+__device__ __forceinline__ float stdp_post_finish(const NetDev &n, const StdpConst &c, float W,
+                                                  int pre, int total_delay, unsigned long long t,
+                                                  const PostPrep &q)
+{
+    if (q.mask & 1) W = stdp_apply(c, W, q.inc0);
+    if (q.mask & 2) W = stdp_apply(c, W, q.inc1);
+    if (q.mask & 4) W = stdp_apply(c, W, q.inc2);
+    if (q.mask & 8) W = stdp_apply(c, W, q.inc3);
+    if (!q.next) return W;
+    const int ms = n.max_spikes;
+    const bool sgn = n.stdp_signed != 0;
+    for (int off = q.next;; --off) {
         if (off < -ms) { set_err(n, ERR_STDP_RING); break; }
-        const unsigned long long sh = hist_at(n, pre, cpre, off);
+        const unsigned long long sh = hist_at(n, pre, q.cpre, off);
         if (sh == BG3_ULONG_MAX) break;
         const unsigned long long dd = t - (unsigned long long)(long long)total_delay - sh;
         const float delta = (sgn ? (float)(long long)dd : (float)dd) * n.dt;
@@ -356,13 +452,20 @@ __device__ float stdp_post(const NetDev &n, const StdpConst &c, float W, int pre
         float epre = 1.0f;
         if (c.useFD) {
             if (off - 1 < -ms) { set_err(n, ERR_STDP_RING); break; }
-            const unsigned long long sh2 = hist_at(n, pre, cpre, off - 1);
+            const unsigned long long sh2 = hist_at(n, pre, q.cpre, off - 1);
             if (sh2 == BG3_ULONG_MAX) break;
             epre = (float)(1.0 - (double)exp_interval(n, sh - sh2, sgn, c.tauspre));
         }
-        W = stdp_learn(c, W, delta, epost, epre, (long long)dd);
+        W = stdp_learn(c, W, delta, q.epost, epre, (long long)dd);
     }
     return W;
+}
+__device__ float stdp_post(const NetDev &n, const StdpConst &c, float W, int pre, int post,
+                           int total_delay, unsigned long long t)
+{
+    PostPrep q;
+    stdp_post_prep(n, c, pre, post, total_delay, t, q);
+    return stdp_post_finish(n, c, W, pre, total_delay, t, q);
 }
 
 // ---- spike arrival ---------------------------------------------------------------------------
@@ -370,10 +473,62 @@ __device__ float stdp_post(const NetDev &n, const StdpConst &c, float W, int pre
 // AllSpikingSynapses::advanceSynapse (Synapses/AllSpikingSynapses.cpp:297-319) followed by
 // changePSR — AllDSSynapses.cpp:227-247 for DS and dynamic STDP, AllSpikingSynapses.cpp:327-334
 // for spiking and STDP synapses; the STDP kinds (2, 3) first run the fPre learning walk.
+// The STDP kinds' arrival in two parts: stdp_hit_prep reads what passes before the previous sweep
+// wrote (the event slot; the DS update of u and r for dynamic STDP), stdp_hit_finish what that
+// sweep writes (psr; the post neuron's spikes, which the fPre walk reads) and stores.  The
+// delivery pass calls the first before its wait on that sweep.
+struct StdpHit {
+    EvSlot e;
+    const StdpConst *c;
+    float dec, u, r;
+    int d;
+    bool ok;
+};
+template <int SYN>
+__device__ __forceinline__ void stdp_hit_prep(const NetDev &n, uint32_t p, uint32_t tf, uint32_t t,
+                                              StdpHit &h)
+{
+    h.e = n.ev[p];
+    h.ok = (int32_t)(tf - h.e.born) >= 0;  // else the synapse did not exist when the spike left
+    if (!h.ok) return;
+    h.dec = n.dtab[h.e.dcls];
+    h.c = &n.stdp[n.stype[p]];
+    int k;
+    pos_slot(p, n.Mq, k, h.d);
+    h.u = h.e.u;
+    h.r = h.e.r;
+    if (SYN == 3 && h.e.last != BG3_NO_SPIKE32) ds_update(n, h.e, t - h.e.last, h.u, h.r);
+}
+template <int SYN>
+__device__ __forceinline__ void stdp_hit_finish(const NetDev &n, uint32_t p, unsigned long long t64,
+                                                int src, const StdpHit &h)
+{
+    if (!h.ok) return;
+    float ps = n.psr[p];
+    const float W = stdp_pre(n, *h.c, h.e.W, src, h.d, t64);
+    n.ev[p].W = W;
+    if (SYN == 3) {
+        ps = ps + ((W / h.dec) * h.u * h.r);
+        EvSlot *q = &n.ev[p];
+        q->u = h.u;
+        q->r = h.r;
+        q->last = (uint32_t)t64;
+    } else {
+        ps = ps + W / h.dec;
+    }
+    n.psr[p] = ps;
+}
+
 template <int SYN>
 __device__ __forceinline__ void deliver_hit(const NetDev &n, uint32_t p, uint32_t tf,
                                             unsigned long long t64, int src)
 {
+    if (SYN >= 2) {
+        StdpHit h;
+        stdp_hit_prep<SYN>(n, p, tf, (uint32_t)t64, h);
+        stdp_hit_finish<SYN>(n, p, t64, src, h);
+        return;
+    }
     const uint32_t t = (uint32_t)t64;
     EvSlot e = n.ev[p];
     if ((int32_t)(tf - e.born) < 0) return;  // the synapse did not exist when the spike left
@@ -560,14 +715,18 @@ __device__ __forceinline__ void deliver_net(const NetDev &n, int bid, int nb, bo
             const uint32_t first = lo ? s_pref[lo - 1] : 0u;
             const uint32_t base = (ch - first) * DLV_CHUNK;
             if (SYN >= 2) {  // STDP: the pre-spike walks go one synapse at a time
-                if (!waited) {
-                    pdl_wait();  // the walks read the post neurons' spikes of the sweep before
-                    pdl_trigger();
-                    waited = true;
-                }
                 const uint32_t end = min(s_cnt[lo], base + (uint32_t)DLV_CHUNK);
-                for (uint32_t j = base + lane; j < end; j += 32)
-                    deliver_hit<SYN>(n, n.outMap[s_beg[lo] + j], s_tf[lo], t, s_src[lo]);
+                for (uint32_t j = base + lane; j < end; j += 32) {
+                    const uint32_t p = n.outMap[s_beg[lo] + j];
+                    StdpHit h;
+                    stdp_hit_prep<SYN>(n, p, s_tf[lo], (uint32_t)t, h);
+                    if (!waited) {
+                        pdl_wait();  // the walks read the post neurons' spikes of the sweep before
+                        pdl_trigger();
+                        waited = true;
+                    }
+                    stdp_hit_finish<SYN>(n, p, t, s_src[lo], h);
+                }
             } else {
                 Arrivals a;
                 deliver_prep<SYN>(n, s_beg[lo], s_cnt[lo], base, s_tf[lo], (uint32_t)t, lane, a);
@@ -620,29 +779,46 @@ __global__ void __launch_bounds__(256) k_deliver_batch(const NetDev *nets, int e
 // total_delayPost 0, so the post queue is read in the same step).  One warp per fired neuron,
 // one lane per incoming synapse; runs after the arrivals of step t (the fPre branch comes first
 // in the reference) and before the sweep.
+//
+// The pass is a programmatic dependent of the delivery, which launches it only once the sweep
+// before has finished: the step (the delivery's own counter, dstep, which only that sweep
+// advances), the fired neurons, every spike count and history are final when it starts; only W
+// is written by the delivery.  So each synapse's walk is prepared (stdp_post_prep) before the
+// wait on the delivery, and W is read, learned and stored after it.
 __device__ __forceinline__ void stdp_post_net(const NetDev &n, int gw, int nw)
 {
-    const unsigned long long t = *n.step;
+    const unsigned long long t = *n.dstep;
     const int slot = (int)(t & (BG3_RING - 1));
     const int m = min(n.ring_n[slot], n.N);
     const int32_t *ids = n.ring + (size_t)slot * n.N;
     const int lane = threadIdx.x & 31;
+    bool waited = false;
     for (int s = gw; s < m; s += nw) {
         const int d = ids[s];
         const int cnt = (int)n.count[d];
         for (int k = lane; k < cnt; k += 32) {
             const size_t p = slot_pos(k, d, n.Mq);
-            const float W = n.ev[p].W;
-            const float W2 = stdp_post(n, n.stdp[n.stype[p]], W, n.src[p], d, n.ltab[n.lcls[p]], t);
-            n.ev[p].W = W2;
+            const StdpConst &c = n.stdp[n.stype[p]];
+            const int pre = n.src[p];
+            const int delay = n.ltab[n.lcls[p]];
+            PostPrep q;
+            stdp_post_prep(n, c, pre, d, delay, t, q);
+            if (!waited) {
+                pdl_wait();
+                pdl_trigger();
+                waited = true;
+            }
+            n.ev[p].W = stdp_post_finish(n, c, n.ev[p].W, pre, delay, t, q);
         }
+    }
+    if (!waited) {
+        pdl_wait();
+        pdl_trigger();
     }
 }
 
 __global__ void __launch_bounds__(256) k_stdp_post(const __grid_constant__ NetDev n)
 {
-    pdl_wait();
-    pdl_trigger();
     stdp_post_net(n, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
 }
 
@@ -650,8 +826,6 @@ __global__ void __launch_bounds__(256) k_stdp_post_batch(const NetDev *nets)
 {
     __shared__ __align__(16) NetDev s_net;
     block_copy_desc(&s_net, nets + blockIdx.y);
-    pdl_wait();
-    pdl_trigger();
     stdp_post_net(s_net, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
                   (gridDim.x * blockDim.x) >> 5);
 }

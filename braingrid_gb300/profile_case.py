@@ -10,7 +10,9 @@ batched together.  heavy is one of those jobs (180x180) alone: 10,000 steps, a g
 steps (it then fires at ~300 Hz), then --steps steps timed kernel by kernel; its delivery passes
 after launch 11,000 are heavy ones.  growth200 is the growth pass of the served stream's largest
 job (200x200, pre-grown); small the 10x10 LIF + DS + ConnGrowth network (100 neurons) on the one-CTA path
-(k_small_run, 4,096 steps per launch).
+(k_small_run, 4,096 steps per launch).  --settle runs a batched workload for that many steps
+first (the izh512 networks' firing rate rises from ~1 Hz to a steady ~15 Hz over the first
+~1,200 steps as STDP strengthens their synapses).
 """
 import argparse
 
@@ -25,6 +27,8 @@ def main():
                     choices=["plain", "sweep36", "izh512", "big", "growth", "growth200",
                              "heavy", "small"])
     ap.add_argument("--count", type=int, default=512, help="networks of the izh512 workload")
+    ap.add_argument("--settle", type=int, default=0,
+                    help="batched workloads: steps run (as one call) before the profiled steps")
     a = ap.parse_args()
     flush = (256 << 20) if a.flush else 0
     if a.workload in ("growth", "growth200"):
@@ -99,6 +103,8 @@ def main():
                       float(c.sum()) / c.size / 0.1)
                 nets.append(net)
         batch = bg.Batch(nets)
+        if a.settle:
+            batch.step(a.settle)
         batch.bench_steps(a.steps, flush)
         S = sum(n.total_synapses() for n in nets)
         print("steps", a.steps, "networks", len(nets), "synapses", S)
